@@ -1,0 +1,195 @@
+/*
+ * mrg.h -- C ABI of the GB300-native gridFFT / SENSE hot path.
+ *
+ * One plan replaces one uwmri/mri_recon `gridFFT` operator (src/gridFFT.h:28-194)
+ * together with the coil-batched `gridFFT_CoilThreaded` (src/gridFFT_CoilThreaded.h:26-191)
+ * and the CG / FISTA loops of `RECON::full_recon` (src/recon_lib.cpp:1523-2212) that drive
+ * them.  Every entry point returns an mrg_status and never exits the process (the
+ * reference calls exit(1), e.g. src/ArrayTemplates.cpp:290-293).
+ *
+ * Naming: the reference calls E^H (k-space -> image) `gridFFT::forward` and E
+ * (image -> k-space) `gridFFT::backward`.  Here mrg_adjoint* is E^H and mrg_forward*
+ * is E; each declaration names the reference function it replaces.
+ *
+ * Layouts follow the reference's Blitz arrays: images are complex64 [Nz][Ny][Nx]
+ * (x fastest, column-major in Blitz terms), k-space samples are flat complex64 arrays
+ * of M samples (the readout x projection x slice arrays of src/mri_data.h, flattened
+ * readout-fastest), trajectories are float32 arrays in the reference's units
+ * (k in [-N/2, N/2], src/commandline_recon.cxx:68-72).
+ *
+ * Pointers may be device pointers or host pointers; host buffers are staged through
+ * device memory inside the call.  `stream` is a cudaStream_t (NULL = legacy default).
+ * A plan is not re-entrant: calls on one plan must be serialised on one stream, as the
+ * reference's shared k3d_grid makes one gridFFT instance non-re-entrant.
+ */
+#ifndef MRG_H
+#define MRG_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct mrg_plan mrg_plan;
+
+typedef enum mrg_status {
+  MRG_OK = 0,
+  MRG_ERR_INVALID = 1,     /* bad argument or shape */
+  MRG_ERR_CUDA = 2,        /* CUDA runtime error (message in mrg_last_error) */
+  MRG_ERR_NOMEM = 3,       /* device allocation failed */
+  MRG_ERR_STATE = 4,       /* call out of order (e.g. no trajectory set) */
+  MRG_ERR_TIMEOUT = 5,     /* reserved: a bounded device-side wait ran out */
+  MRG_ERR_UNSUPPORTED = 6  /* grid size or option this build does not implement */
+} mrg_status;
+
+/* gridFFT kernel types (src/gridFFT.h:19-22) */
+enum { MRG_KERNEL_TRIANGLE = 0, MRG_KERNEL_KAISER = 1, MRG_KERNEL_SINC = 2, MRG_KERNEL_POLY = 3 };
+
+/* Operator options; the gridFFT public fields set before precalc_gridding
+ * (src/gridFFT.cpp:28-60 defaults, :187-245 command-line flags). */
+typedef struct mrg_config {
+  float overgrid;    /* gridFFT::overgrid, -overgrid (default 1.5) */
+  float dwin;        /* gridFFT::dwinX/Y/Z, -dwinX (-1: kernel default, 2.5 for Kaiser) */
+  int kernel_type;   /* gridFFT::kernel_type, -kaiser/-triangle/-sinc/-poly_kernel */
+  float k_rad;       /* gridFFT::k_rad, Gaussian taper radius of E^H (default 9999) */
+  int time_grid;     /* gridFFT::time_grid, -time_grid: print per-stage device times */
+  int tile;          /* gridding tile edge in grid points (0: autotune) */
+  int max_pairs;     /* (sample, tile) pairs per gridding work item (0: default) */
+} mrg_config;
+
+/* Fills the reference defaults (src/gridFFT.cpp:28-60). */
+void mrg_config_default(mrg_config *cfg);
+
+/* Text of the last error on this thread ("" when none). */
+const char *mrg_last_error(void);
+
+/* Replaces gridFFT::precalc_gridding(Nz, Ny, Nx, data) (src/gridFFT.cpp:475-643) for a
+ * 3D non-Cartesian trajectory, and gridFFT_CoilThreaded::precalc_gridding for ncoil
+ * coils (src/gridFFT_CoilThreaded.cpp:403-568).  nframes trajectories (gated frames /
+ * encodes, src/recon_lib.cpp:675-776) can be set on one plan. */
+mrg_status mrg_plan_create(const mrg_config *cfg, int Nx, int Ny, int Nz, int ncoil, int nframes, mrg_plan **out);
+mrg_status mrg_plan_destroy(mrg_plan *plan);
+
+/* Geometry as computed by precalc_gridding: grid size S (Sx,Sy,Sz), crop start og_s
+ * (src/gridFFT.cpp:536-541), grid ratio grid_x/y/z, Kaiser beta, kernel half width and
+ * LUT length (src/gridFFT.cpp:330-340). */
+mrg_status mrg_plan_info(const mrg_plan *plan, int S[3], int og[3], float grid[3], float beta[3], float dwin[3],
+                         int *lut_len);
+/* Host copies of the kernel lookup tables grid_filterX/Y/Z (3*lut_len floats) and the
+ * deapodisation windows winx, winy, winz (Sx+Sy+Sz floats), src/gridFFT.cpp:276-631. */
+mrg_status mrg_get_tables(const mrg_plan *plan, float *lut, float *win);
+
+/* Coil sensitivity maps: ncoil complex64 images, coil c at smaps + c*coil_stride
+ * (elements).  Replaces the `smaps` container passed to every forward/backward call
+ * (src/recon_lib.cpp:1560-1621). */
+mrg_status mrg_set_smaps(mrg_plan *plan, const void *smaps, int64_t coil_stride, void *stream);
+
+/* Trajectory and per-sample weight of one frame: kx, ky, kz, kw of M samples.  kw is
+ * the density compensation times the frame's gating weight (the reference's
+ * TimeWeight, src/recon_lib.cpp:1543-1557).  Samples with kw == 0 or outside the grid
+ * contribute nothing (src/gridFFT.cpp:1035-1098). */
+mrg_status mrg_set_traj(mrg_plan *plan, int frame, const float *kx, const float *ky, const float *kz,
+                        const float *kw, int64_t M, void *stream);
+
+/* Measured k-space of one frame: ncoil arrays of M complex64, coil c at
+ * data + c*coil_stride.  Used by mrg_cg / mrg_fista (data.kdata, src/mri_data.h). */
+mrg_status mrg_set_data(mrg_plan *plan, int frame, const void *data, int64_t coil_stride, void *stream);
+
+/* E^H, all coils of a frame: X += sum_c gridFFT::forward(X, smap_c, data_c, k, kw)
+ * (src/gridFFT.cpp:791-812; coil-batched src/gridFFT_CoilThreaded.cpp:999-1031). */
+mrg_status mrg_adjoint(mrg_plan *plan, int frame, const void *data, int64_t coil_stride, void *X, void *stream);
+
+/* E, all coils of a frame: data_c = gridFFT::backward(X, smap_c) (src/gridFFT.cpp:824-844),
+ * or data_c = E_c X - diff_c when diff is not NULL (backward_residual,
+ * src/gridFFT.cpp:856-876). */
+mrg_status mrg_forward(mrg_plan *plan, int frame, const void *X, void *data, int64_t coil_stride, const void *diff,
+                       void *stream);
+
+/* out = sum_c E_c^H W E_c X for one frame (the operator of the CG loop,
+ * src/recon_lib.cpp:1614-1622).  out is overwritten. */
+mrg_status mrg_normal(mrg_plan *plan, int frame, const void *X, void *out, void *stream);
+
+/* Per-coil calls with an explicit sensitivity map, the exact per-coil surface of
+ * gridFFT::forward / backward / backward_residual (src/gridFFT.h:109-164).  Valid on a
+ * plan created with ncoil == 1; smap may be NULL (the no-smap overloads,
+ * src/gridFFT.cpp:759-789 and :887-906). */
+mrg_status mrg_adjoint_coil(mrg_plan *plan, int frame, const void *smap, const void *data, void *X, void *stream);
+mrg_status mrg_forward_coil(mrg_plan *plan, int frame, const void *X, const void *smap, void *data, const void *diff,
+                            void *stream);
+
+/* SENSE conjugate gradient (src/recon_lib.cpp:1523-1759): X (nframes images) is
+ * overwritten with the result of max_iter iterations from x0 = 0, FP32 vectors and
+ * FP64 scalars.  resid (host, may be NULL) receives sum|r|^2 after each iteration.
+ * use_graph != 0 captures one iteration as a CUDA graph and replays it. */
+mrg_status mrg_cg(mrg_plan *plan, int max_iter, void *X, double *resid, int use_graph, void *stream);
+
+/* FISTA / IST with L1-wavelet fraction thresholding and optional locally-low-rank
+ * thresholding in time (src/recon_lib.cpp:1761-2212, :2416-2527; src/threshold.cpp;
+ * src/wavelet3D.cpp; src/clear.cpp:233-556). */
+typedef struct mrg_fista_params {
+  int max_iter;          /* -max_iter */
+  int max_eig_iter;      /* max_eigen_iterations (default 30) */
+  int fista;             /* 1 FISTA, 0 IST */
+  int cycle_spins;       /* -cycle_spins (default 4) */
+  int wave_levels[3];    /* -wavelet_levelsX/Y/Z (default 4) */
+  int wave_type;         /* 0 DB2, 1 DB4 (-wavelet_type, default DB4) */
+  float thresh;          /* -thresh: fraction of coefficients set to zero */
+  int use_threshold;     /* -threshold_type fraction (1) or none (0) */
+  int llr_block[3];      /* -clear_nx/ny/nz (default 4) */
+  int llr_block_iter;    /* -clear_block_iter (default 4) */
+  float llr_alpha;       /* -clear_alpha_time (0: off) */
+  float clear_amp;       /* -clear_amp (default 4) */
+  float clear_t2;        /* -clear_t2 (default 6) */
+  int64_t rand_skip;     /* rand() draws consumed before the first shift; -1: the
+                            2*N^3*nframes draws of the max-eigen seeding */
+} mrg_fista_params;
+
+void mrg_fista_params_default(mrg_fista_params *p);
+
+/* X (nframes images, overwritten), resid (host, may be NULL): sum|E^H W(Ex-d)|^2 per
+ * iteration, step (host, may be NULL): the 1/max-eigenvalue step size. */
+mrg_status mrg_fista(mrg_plan *plan, const mrg_fista_params *params, void *X, double *resid, float *step,
+                     int use_graph, void *stream);
+
+/* Building blocks exposed for drop-in use and parity tests. */
+/* WAVELET3D::forward/backward (src/wavelet3D.cpp:563-624) on nvol volumes of
+ * Nx*Ny*Nz complex64, in place, circular shifts shift[3] (wavelet3D.cpp:443-448). */
+mrg_status mrg_wavelet(void *X, int nvol, int Nx, int Ny, int Nz, const int levels[3], const int shift[3],
+                       int wave_type, int inverse, void *stream);
+/* THRESHOLD::get_threshold for fraction thresholding (src/threshold.cpp:251-391) over
+ * nvol volumes of nvox complex64; result written to *value (host). */
+mrg_status mrg_fraction_threshold(const void *X, int nvol, int64_t nvox, float fraction, float *value, void *stream);
+/* THRESHOLD::thresholding, soft, grouped complex (src/threshold.cpp:766-814). */
+mrg_status mrg_soft_threshold(void *X, int64_t n, float value, void *stream);
+/* LOWRANKCOIL::update_threshold (src/clear.cpp:233-351) in time, Ne = 1: returns smax. */
+mrg_status mrg_llr_update_threshold(const void *X, int nframes, int Nx, int Ny, int Nz, const int block[3],
+                                    float clear_amp, float clear_t2, int iteration, float *smax, void *stream);
+/* LOWRANKCOIL::thresh (src/clear.cpp:356-556) in time, Ne = 1, with the block shifts
+ * drawn from the rand() stream after rand_skip draws. */
+mrg_status mrg_llr_thresh(void *X, int nframes, int Nx, int Ny, int Nz, const int block[3], int block_iter,
+                          float alpha, float smax, int64_t rand_skip, void *stream);
+
+/* Host-only (no GPU needed): the geometry and tables mrg_plan_create would build,
+ * i.e. gridFFT::precalc_gridding's S, og_s, grid ratio, Kaiser beta and the LUT / window
+ * tables (src/gridFFT.cpp:276-643).  lut (3*lut_len) and win (Sx+Sy+Sz) may be NULL
+ * to query sizes first. */
+mrg_status mrg_plan_geometry(const mrg_config *cfg, int Nx, int Ny, int Nz, int S[3], int og[3], float grid[3],
+                             float beta[3], int *lut_len, float *lut, float *win);
+/* Host-only: n values of the glibc rand() stream for the default seed after `skip`
+ * draws, the source of the reference's wavelet and block shifts
+ * (src/wavelet3D.cpp:443-448, src/clear.cpp:408-410). */
+mrg_status mrg_rand_stream(int64_t skip, int n, int *out);
+
+/* Per-stage device timings of the last operator call (ms): zero, grid, fft, accumulate
+ * for E^H and copy, fft, igrid for E, as printed by -time_grid (src/gridFFT.cpp:727-778). */
+mrg_status mrg_last_timings(const mrg_plan *plan, float out[8]);
+
+/* Number of kernels this library launched since load (process-wide counter). */
+int64_t mrg_kernel_launches(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MRG_H */

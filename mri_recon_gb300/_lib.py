@@ -1,0 +1,94 @@
+"""ctypes binding of libmrg.so (include/mrg.h).
+
+There is no fallback: if the CUDA library is missing or fails to load, every
+entry point raises.  Build it with ``python -m mri_recon_gb300.build`` or
+``__graft_entry__.build()``.
+"""
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libmrg.so")
+
+MRG_OK = 0
+STATUS = {0: "MRG_OK", 1: "MRG_ERR_INVALID", 2: "MRG_ERR_CUDA", 3: "MRG_ERR_NOMEM", 4: "MRG_ERR_STATE",
+          5: "MRG_ERR_TIMEOUT", 6: "MRG_ERR_UNSUPPORTED"}
+
+# Every function declared in include/mrg.h: name -> (restype, argtypes)
+_vp = ctypes.c_void_p
+_i = ctypes.c_int
+_i64 = ctypes.c_int64
+_f = ctypes.c_float
+_ip = ctypes.POINTER(ctypes.c_int)
+_fp = ctypes.POINTER(ctypes.c_float)
+_dp = ctypes.POINTER(ctypes.c_double)
+
+
+class MrgConfig(ctypes.Structure):
+    _fields_ = [("overgrid", ctypes.c_float), ("dwin", ctypes.c_float), ("kernel_type", ctypes.c_int),
+                ("k_rad", ctypes.c_float), ("time_grid", ctypes.c_int), ("tile", ctypes.c_int),
+                ("max_pairs", ctypes.c_int)]
+
+
+class MrgFistaParams(ctypes.Structure):
+    _fields_ = [("max_iter", ctypes.c_int), ("max_eig_iter", ctypes.c_int), ("fista", ctypes.c_int),
+                ("cycle_spins", ctypes.c_int), ("wave_levels", ctypes.c_int * 3), ("wave_type", ctypes.c_int),
+                ("thresh", ctypes.c_float), ("use_threshold", ctypes.c_int), ("llr_block", ctypes.c_int * 3),
+                ("llr_block_iter", ctypes.c_int), ("llr_alpha", ctypes.c_float), ("clear_amp", ctypes.c_float),
+                ("clear_t2", ctypes.c_float), ("rand_skip", ctypes.c_int64)]
+
+
+SIGNATURES = {
+    "mrg_config_default": (None, [ctypes.POINTER(MrgConfig)]),
+    "mrg_last_error": (ctypes.c_char_p, []),
+    "mrg_plan_create": (_i, [ctypes.POINTER(MrgConfig), _i, _i, _i, _i, _i, ctypes.POINTER(_vp)]),
+    "mrg_plan_destroy": (_i, [_vp]),
+    "mrg_plan_info": (_i, [_vp, _ip, _ip, _fp, _fp, _fp, _ip]),
+    "mrg_get_tables": (_i, [_vp, _fp, _fp]),
+    "mrg_set_smaps": (_i, [_vp, _vp, _i64, _vp]),
+    "mrg_set_traj": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _i64, _vp]),
+    "mrg_set_data": (_i, [_vp, _i, _vp, _i64, _vp]),
+    "mrg_adjoint": (_i, [_vp, _i, _vp, _i64, _vp, _vp]),
+    "mrg_forward": (_i, [_vp, _i, _vp, _vp, _i64, _vp, _vp]),
+    "mrg_normal": (_i, [_vp, _i, _vp, _vp, _vp]),
+    "mrg_adjoint_coil": (_i, [_vp, _i, _vp, _vp, _vp, _vp]),
+    "mrg_forward_coil": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _vp]),
+    "mrg_cg": (_i, [_vp, _i, _vp, _dp, _i, _vp]),
+    "mrg_fista_params_default": (None, [ctypes.POINTER(MrgFistaParams)]),
+    "mrg_fista": (_i, [_vp, ctypes.POINTER(MrgFistaParams), _vp, _dp, _fp, _i, _vp]),
+    "mrg_wavelet": (_i, [_vp, _i, _i, _i, _i, _ip, _ip, _i, _i, _vp]),
+    "mrg_fraction_threshold": (_i, [_vp, _i, _i64, _f, _fp, _vp]),
+    "mrg_soft_threshold": (_i, [_vp, _i64, _f, _vp]),
+    "mrg_llr_update_threshold": (_i, [_vp, _i, _i, _i, _i, _ip, _f, _f, _i, _fp, _vp]),
+    "mrg_llr_thresh": (_i, [_vp, _i, _i, _i, _i, _ip, _i, _f, _f, _i64, _vp]),
+    "mrg_plan_geometry": (_i, [ctypes.POINTER(MrgConfig), _i, _i, _i, _ip, _ip, _fp, _fp, _ip, _fp, _fp]),
+    "mrg_rand_stream": (_i, [_i64, _i, _ip]),
+    "mrg_last_timings": (_i, [_vp, _fp]),
+    "mrg_kernel_launches": (_i64, []),
+}
+
+_lib = None
+
+
+class MrgError(RuntimeError):
+    pass
+
+
+def load():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise MrgError("libmrg.so is not built (%s); run __graft_entry__.build()" % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(status):
+    if status != MRG_OK:
+        msg = load().mrg_last_error().decode(errors="replace")
+        raise MrgError("%s: %s" % (STATUS.get(status, str(status)), msg))

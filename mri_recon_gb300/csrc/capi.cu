@@ -1,0 +1,768 @@
+// Plan object and C ABI (include/mrg.h).
+//
+// A plan owns the device state that one reference gridFFT / gridFFT_CoilThreaded
+// instance owns on the host (k3d_grid, LUT, windows; src/gridFFT.h:28-194),
+// plus the per-frame sorted trajectories and the CG / FISTA work vectors of
+// RECON::full_recon (src/recon_lib.cpp:1523-2212).
+//
+// Device memory layout (complex64 unless noted):
+//   grid  [Sz][Sy][Sx][C]        oversampled k-space, all coils adjacent
+//   t2    [Sz][Sy][Nx][C]        after the y pass (E) / before the y pass (E^H)
+//   t1    [Sz][Ny][Nx][C]        after the z pass (E) / before the z pass (E^H)
+//   smap  [Nz][Ny][Nx][C]        coil maps, coils adjacent
+//   y     [nvalid][C]            k-space samples in tile-sorted order
+//   images [frame][Nz][Ny][Nx]   as the reference's X, R, P, LHS
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+
+#include "mrg_internal.h"
+
+namespace mrg {
+static thread_local std::string g_err;
+void set_error(const std::string &msg) { g_err = msg; }
+std::atomic<int64_t> g_launches{0};
+}  // namespace mrg
+
+using namespace mrg;
+
+struct mrg_plan {
+  Geometry geo;
+  mrg_config cfg;
+  int C = 1, T = 1;
+  int64_t nimg = 0;
+  int B = 8;
+  int max_pairs = 4096;
+  float *d_lut = nullptr, *d_win = nullptr;
+  float2 *d_grid = nullptr, *d_t2 = nullptr, *d_t1 = nullptr, *d_smap = nullptr;
+  bool has_smaps = false;
+  float2 *d_y = nullptr;
+  int64_t y_cap = 0;
+  std::vector<FrameTraj> frames;
+  // solver state
+  float2 *d_R = nullptr, *d_P = nullptr, *d_L = nullptr, *d_Xo = nullptr;
+  double *d_part = nullptr;
+  int nblk = 0;
+  Scalars *d_sc = nullptr;
+  double *d_resid = nullptr;
+  int resid_cap = 0;
+  // staging for host pointers
+  void *d_stage[4] = {nullptr, nullptr, nullptr, nullptr};
+  size_t stage_cap[4] = {0, 0, 0, 0};
+  float timings[8] = {0};
+  // cached CG graph
+  cudaGraphExec_t cg_exec = nullptr;
+  void *cg_key[2] = {nullptr, nullptr};
+};
+
+// ---------------------------------------------------------------------------
+// helpers
+// ---------------------------------------------------------------------------
+static GridConst grid_const(const mrg_plan *p) {
+  GridConst g;
+  for (int d = 0; d < 3; d++) {
+    g.S[d] = p->geo.S[d];
+    g.grid[d] = p->geo.grid[d];
+    g.cen[d] = (float)(p->geo.S[d] / 2);
+    g.dwin[d] = p->geo.dwin[d];
+    g.gmod[d] = p->geo.grid_mod[d];
+    g.lut[d] = p->d_lut + (size_t)d * p->geo.lut_len;
+    g.nt[d] = p->geo.S[d] / p->B;
+  }
+  g.k_rad = p->geo.k_rad;
+  g.B = p->B;
+  g.C = p->C;
+  return g;
+}
+
+static bool is_device_ptr(const void *ptr) {
+  if (!ptr) return false;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+static mrg_status stage_buf(mrg_plan *p, int slot, size_t bytes, void **out) {
+  if (p->stage_cap[slot] < bytes) {
+    cudaFree(p->d_stage[slot]);
+    p->d_stage[slot] = nullptr;
+    p->stage_cap[slot] = 0;
+    MRG_CUDA(cudaMalloc(&p->d_stage[slot], bytes));
+    p->stage_cap[slot] = bytes;
+  }
+  *out = p->d_stage[slot];
+  return MRG_OK;
+}
+
+// Device view of a caller buffer: device pointers pass through, host buffers are
+// copied into staging slot `slot` (when `copy_in`).
+static mrg_status dev_view(mrg_plan *p, int slot, const void *ptr, size_t bytes, bool copy_in, cudaStream_t st,
+                           void **dev, bool *staged) {
+  *staged = false;
+  if (!ptr) {
+    *dev = nullptr;
+    return MRG_OK;
+  }
+  if (is_device_ptr(ptr)) {
+    *dev = const_cast<void *>(ptr);
+    return MRG_OK;
+  }
+  MRG_TRY(stage_buf(p, slot, bytes, dev));
+  if (copy_in) MRG_CUDA(cudaMemcpyAsync(*dev, ptr, bytes, cudaMemcpyHostToDevice, st));
+  *staged = true;
+  return MRG_OK;
+}
+
+// A captured CG graph holds raw pointers: drop it whenever a buffer it uses moves.
+static void invalidate_graphs(mrg_plan *p) {
+  if (p->cg_exec) {
+    cudaGraphExecDestroy(p->cg_exec);
+    p->cg_exec = nullptr;
+  }
+}
+
+static mrg_status ensure_y(mrg_plan *p, int64_t n) {
+  if (p->y_cap >= n) return MRG_OK;
+  invalidate_graphs(p);
+  cudaFree(p->d_y);
+  p->d_y = nullptr;
+  p->y_cap = 0;
+  MRG_CUDA(cudaMalloc(&p->d_y, sizeof(float2) * (size_t)std::max<int64_t>(n, 1)));
+  p->y_cap = n;
+  return MRG_OK;
+}
+
+static int pass_ib(int64_t inner, int C) {
+  if (C > 32) return 32;
+  return C * (32 / C);
+}
+
+// E for one frame: image X -> sorted samples y (minus diff if given).
+// smap: interleaved plan maps when C > 1 or an explicit single-coil map (may be NULL).
+static mrg_status run_E(mrg_plan *p, const FrameTraj &ft, const float2 *X, const float2 *smap, const float2 *diff,
+                        float2 *y, cudaStream_t st) {
+  const Geometry &g = p->geo;
+  const int C = p->C;
+  const int64_t Nx = g.N[0], Ny = g.N[1], Nz = g.N[2], Sx = g.S[0], Sy = g.S[1], Sz = g.S[2];
+  const float *wx = p->d_win, *wy = p->d_win + Sx, *wz = p->d_win + Sx + Sy;
+  FftPass a;
+  memset(&a, 0, sizeof(a));
+  // z pass with set_image (src/gridFFT.cpp:972-986 + fft3 along z)
+  a.S = (int)Sz; a.sign = -1; a.mode = FFT_SETIMG;
+  a.Lin = (int)Nz; a.in_off = g.og[2]; a.Lout = (int)Sz; a.out_off = 0;
+  a.inner = (int)(Nx * C); a.IB = pass_ib(a.inner, C); a.lfast = 0;
+  a.nlines = Ny * Nx * C;
+  a.in_ls = Nx * Ny * C; a.in_os = Nx * C; a.out_ls = Ny * Nx * C; a.out_os = Nx * C;
+  a.scale = (float)(1. / std::sqrt((float)Sz));
+  a.in = smap; a.smap = smap; a.has_smap = smap != nullptr; a.X = X; a.out = p->d_t1;
+  a.wl = wz + g.og[2]; a.wo = wy + g.og[1]; a.wi = wx + g.og[0]; a.C = C;
+  MRG_TRY(launch_fft(a, st));
+  // y pass
+  FftPass b;
+  memset(&b, 0, sizeof(b));
+  b.S = (int)Sy; b.sign = -1; b.mode = FFT_PLAIN;
+  b.Lin = (int)Ny; b.in_off = g.og[1]; b.Lout = (int)Sy; b.out_off = 0;
+  b.inner = (int)(Nx * C); b.IB = pass_ib(b.inner, C);
+  b.nlines = Sz * Nx * C;
+  b.in_ls = Nx * C; b.in_os = Ny * Nx * C; b.out_ls = Nx * C; b.out_os = Sy * Nx * C;
+  b.scale = (float)(1. / std::sqrt((float)Sy));
+  b.in = p->d_t1; b.out = p->d_t2; b.C = C;
+  MRG_TRY(launch_fft(b, st));
+  // x pass
+  FftPass c;
+  memset(&c, 0, sizeof(c));
+  c.S = (int)Sx; c.sign = -1; c.mode = FFT_PLAIN;
+  c.Lin = (int)Nx; c.in_off = g.og[0]; c.Lout = (int)Sx; c.out_off = 0;
+  c.inner = C; c.IB = pass_ib(C, C); c.lfast = (C == 1);
+  c.nlines = Sz * Sy * C;
+  c.in_ls = C; c.in_os = Nx * C; c.out_ls = C; c.out_os = Sx * C;
+  c.scale = (float)(1. / std::sqrt((float)Sx));
+  c.in = p->d_t2; c.out = p->d_grid; c.C = C;
+  MRG_TRY(launch_fft(c, st));
+  // ungrid (src/gridFFT.cpp:1166-1322)
+  const GridConst gc = grid_const(p);
+  MRG_TRY(launch_ungrid(gc, ft, p->d_grid, diff, y, st));
+  return MRG_OK;
+}
+
+// E^H for one frame: sorted samples y -> X += ...
+static mrg_status run_EH(mrg_plan *p, const FrameTraj &ft, const float2 *y, const float2 *smap, float2 *X,
+                         cudaStream_t st) {
+  const Geometry &g = p->geo;
+  const int C = p->C;
+  const int64_t Nx = g.N[0], Ny = g.N[1], Nz = g.N[2], Sx = g.S[0], Sy = g.S[1], Sz = g.S[2];
+  const float *wx = p->d_win, *wy = p->d_win + Sx, *wz = p->d_win + Sx + Sy;
+  const GridConst gc = grid_const(p);
+  MRG_TRY(launch_grid(gc, ft, y, p->d_grid, st));  // src/gridFFT.cpp:1009-1164
+  FftPass a;
+  memset(&a, 0, sizeof(a));
+  a.S = (int)Sx; a.sign = +1; a.mode = FFT_PLAIN;
+  a.Lin = (int)Sx; a.in_off = 0; a.Lout = (int)Nx; a.out_off = g.og[0];
+  a.inner = C; a.IB = pass_ib(C, C); a.lfast = (C == 1);
+  a.nlines = Sz * Sy * C;
+  a.in_ls = C; a.in_os = Sx * C; a.out_ls = C; a.out_os = Nx * C;
+  a.scale = (float)(1. / std::sqrt((float)Sx));
+  a.in = p->d_grid; a.out = p->d_t2; a.C = C;
+  MRG_TRY(launch_fft(a, st));
+  FftPass b;
+  memset(&b, 0, sizeof(b));
+  b.S = (int)Sy; b.sign = +1; b.mode = FFT_PLAIN;
+  b.Lin = (int)Sy; b.in_off = 0; b.Lout = (int)Ny; b.out_off = g.og[1];
+  b.inner = (int)(Nx * C); b.IB = pass_ib(b.inner, C);
+  b.nlines = Sz * Nx * C;
+  b.in_ls = Nx * C; b.in_os = Sy * Nx * C; b.out_ls = Nx * C; b.out_os = Ny * Nx * C;
+  b.scale = (float)(1. / std::sqrt((float)Sy));
+  b.in = p->d_t2; b.out = p->d_t1; b.C = C;
+  MRG_TRY(launch_fft(b, st));
+  // z pass with accumulate (src/gridFFT.cpp:926-941)
+  FftPass c;
+  memset(&c, 0, sizeof(c));
+  c.S = (int)Sz; c.sign = +1; c.mode = FFT_ACCUM;
+  c.Lin = (int)Sz; c.in_off = 0; c.Lout = (int)Nz; c.out_off = g.og[2];
+  c.inner = (int)(Nx * C); c.IB = pass_ib(c.inner, C);
+  c.nlines = Ny * Nx * C;
+  c.in_ls = Ny * Nx * C; c.in_os = Nx * C; c.out_ls = Nx * Ny * C; c.out_os = Nx * C;
+  c.scale = (float)(1. / std::sqrt((float)Sz));
+  c.in = p->d_t1; c.smap = smap; c.has_smap = smap != nullptr; c.acc = X;
+  c.acc_atomic = (c.IB % C) != 0; c.acc_l = Nx * Ny; c.acc_o = Nx;
+  c.wl = wz + g.og[2]; c.wo = wy + g.og[1]; c.wi = wx + g.og[0]; c.C = C;
+  MRG_TRY(launch_fft(c, st));
+  return MRG_OK;
+}
+
+static mrg_status check_frame(const mrg_plan *p, int frame) {
+  if (!p) {
+    set_error("null plan");
+    return MRG_ERR_INVALID;
+  }
+  if (frame < 0 || frame >= p->T) {
+    set_error("frame index out of range");
+    return MRG_ERR_INVALID;
+  }
+  if (p->frames[frame].M == 0) {
+    set_error("no trajectory set for this frame");
+    return MRG_ERR_STATE;
+  }
+  return MRG_OK;
+}
+
+static const float2 *plan_smap(const mrg_plan *p) { return p->has_smaps ? p->d_smap : nullptr; }
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+void mrg_config_default(mrg_config *cfg) {
+  if (!cfg) return;
+  cfg->overgrid = 1.5f;
+  cfg->dwin = -1.0f;
+  cfg->kernel_type = MRG_KERNEL_KAISER;
+  cfg->k_rad = 9999.0f;
+  cfg->time_grid = 0;
+  cfg->tile = 0;
+  cfg->max_pairs = 0;
+}
+
+const char *mrg_last_error(void) { return g_err.c_str(); }
+
+int64_t mrg_kernel_launches(void) { return g_launches.load(); }
+
+mrg_status mrg_plan_create(const mrg_config *cfg_in, int Nx, int Ny, int Nz, int ncoil, int nframes, mrg_plan **out) {
+  if (!out) {
+    set_error("out is NULL");
+    return MRG_ERR_INVALID;
+  }
+  *out = nullptr;
+  if (Nx <= 0 || Ny <= 0 || Nz <= 0 || ncoil <= 0 || nframes <= 0) {
+    set_error("sizes must be positive");
+    return MRG_ERR_INVALID;
+  }
+  mrg_config cfg;
+  if (cfg_in) cfg = *cfg_in; else mrg_config_default(&cfg);
+  if (!(cfg.overgrid >= 1.0f) || cfg.kernel_type < 0 || cfg.kernel_type > 3) {
+    set_error("bad config");
+    return MRG_ERR_INVALID;
+  }
+  mrg_plan *p = new mrg_plan();
+  p->cfg = cfg;
+  p->C = ncoil;
+  p->T = nframes;
+  build_geometry(p->geo, cfg, Nx, Ny, Nz);
+  for (int d = 0; d < 3; d++) {
+    if (!fft_size_supported(p->geo.S[d])) {
+      set_error("oversampled size " + std::to_string(p->geo.S[d]) + " not supported by this build");
+      delete p;
+      return MRG_ERR_UNSUPPORTED;
+    }
+    if (p->geo.dwin[d] > 2.5f) {
+      set_error("kernel half width above 2.5 not supported by this build");
+      delete p;
+      return MRG_ERR_UNSUPPORTED;
+    }
+  }
+  p->B = cfg.tile > 0 ? cfg.tile : 8;
+  if (p->geo.S[0] % p->B || p->geo.S[1] % p->B || p->geo.S[2] % p->B || p->B < 4 || p->B > 16) {
+    set_error("tile must be 4..16 and divide the grid");
+    delete p;
+    return MRG_ERR_INVALID;
+  }
+  p->max_pairs = cfg.max_pairs > 0 ? cfg.max_pairs : 4096;
+  p->nimg = (int64_t)Nx * Ny * Nz;
+  p->frames.resize(nframes);
+  mrg_status rs = fft_init_device();
+  const int64_t S3 = (int64_t)p->geo.S[0] * p->geo.S[1] * p->geo.S[2];
+  const int64_t t2n = (int64_t)Nx * p->geo.S[1] * p->geo.S[2];
+  const int64_t t1n = (int64_t)Nx * Ny * p->geo.S[2];
+  auto fail = [&](mrg_status s) {
+    mrg_plan_destroy(p);
+    return s;
+  };
+  if (rs != MRG_OK) return fail(rs);
+#define ALLOC(ptr, bytes)                                                             \
+  do {                                                                                \
+    if (cudaMalloc((void **)&(ptr), (bytes)) != cudaSuccess) {                        \
+      cudaGetLastError();                                                             \
+      set_error(std::string("device allocation failed: ") + #ptr);                   \
+      return fail(MRG_ERR_NOMEM);                                                     \
+    }                                                                                 \
+  } while (0)
+  ALLOC(p->d_lut, sizeof(float) * 3 * p->geo.lut_len);
+  ALLOC(p->d_win, sizeof(float) * (p->geo.S[0] + p->geo.S[1] + p->geo.S[2]));
+  ALLOC(p->d_grid, sizeof(float2) * S3 * ncoil);
+  ALLOC(p->d_t2, sizeof(float2) * t2n * ncoil);
+  ALLOC(p->d_t1, sizeof(float2) * t1n * ncoil);
+  ALLOC(p->d_sc, sizeof(Scalars));
+  p->nblk = reduce_blocks(p->nimg * nframes);
+  ALLOC(p->d_part, sizeof(double) * 3 * p->nblk);
+#undef ALLOC
+  std::vector<float> lut(3 * (size_t)p->geo.lut_len), win;
+  for (int d = 0; d < 3; d++) std::copy(p->geo.lut[d].begin(), p->geo.lut[d].end(), lut.begin() + (size_t)d * p->geo.lut_len);
+  for (int d = 0; d < 3; d++) win.insert(win.end(), p->geo.win[d].begin(), p->geo.win[d].end());
+  if (cudaMemcpy(p->d_lut, lut.data(), sizeof(float) * lut.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(p->d_win, win.data(), sizeof(float) * win.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+    set_error("table upload failed");
+    return fail(MRG_ERR_CUDA);
+  }
+  *out = p;
+  return MRG_OK;
+}
+
+mrg_status mrg_plan_destroy(mrg_plan *p) {
+  if (!p) return MRG_OK;
+  for (auto &f : p->frames) traj_free(f);
+  cudaFree(p->d_lut); cudaFree(p->d_win); cudaFree(p->d_grid); cudaFree(p->d_t2); cudaFree(p->d_t1);
+  cudaFree(p->d_smap); cudaFree(p->d_y); cudaFree(p->d_R); cudaFree(p->d_P); cudaFree(p->d_L); cudaFree(p->d_Xo);
+  cudaFree(p->d_part); cudaFree(p->d_sc); cudaFree(p->d_resid);
+  for (int k = 0; k < 4; k++) cudaFree(p->d_stage[k]);
+  if (p->cg_exec) cudaGraphExecDestroy(p->cg_exec);
+  delete p;
+  return MRG_OK;
+}
+
+mrg_status mrg_plan_info(const mrg_plan *p, int S[3], int og[3], float grid[3], float beta[3], float dwin[3],
+                         int *lut_len) {
+  if (!p) {
+    set_error("null plan");
+    return MRG_ERR_INVALID;
+  }
+  for (int d = 0; d < 3; d++) {
+    if (S) S[d] = p->geo.S[d];
+    if (og) og[d] = p->geo.og[d];
+    if (grid) grid[d] = p->geo.grid[d];
+    if (beta) beta[d] = p->geo.beta[d];
+    if (dwin) dwin[d] = p->geo.dwin[d];
+  }
+  if (lut_len) *lut_len = p->geo.lut_len;
+  return MRG_OK;
+}
+
+mrg_status mrg_get_tables(const mrg_plan *p, float *lut, float *win) {
+  if (!p) {
+    set_error("null plan");
+    return MRG_ERR_INVALID;
+  }
+  size_t o = 0;
+  for (int d = 0; d < 3; d++) {
+    if (lut) memcpy(lut + (size_t)d * p->geo.lut_len, p->geo.lut[d].data(), sizeof(float) * p->geo.lut_len);
+    if (win) memcpy(win + o, p->geo.win[d].data(), sizeof(float) * p->geo.S[d]);
+    o += p->geo.S[d];
+  }
+  return MRG_OK;
+}
+
+mrg_status mrg_set_smaps(mrg_plan *p, const void *smaps, int64_t coil_stride, void *stream) {
+  if (!p || !smaps) {
+    set_error("null argument");
+    return MRG_ERR_INVALID;
+  }
+  if (coil_stride < p->nimg && p->C > 1) {
+    set_error("coil_stride smaller than one image");
+    return MRG_ERR_INVALID;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  if (!p->d_smap) MRG_CUDA(cudaMalloc(&p->d_smap, sizeof(float2) * p->nimg * p->C));
+  void *src;
+  bool staged;
+  const size_t bytes = sizeof(float2) * (size_t)(coil_stride * (p->C - 1) + p->nimg);
+  MRG_TRY(dev_view(p, 0, smaps, bytes, true, st, &src, &staged));
+  MRG_TRY(launch_interleave((const float2 *)src, coil_stride, p->C, p->nimg, p->d_smap, st));
+  if (staged) MRG_CUDA(cudaStreamSynchronize(st));
+  p->has_smaps = true;
+  return MRG_OK;
+}
+
+mrg_status mrg_set_traj(mrg_plan *p, int frame, const float *kx, const float *ky, const float *kz, const float *kw,
+                        int64_t M, void *stream) {
+  if (!p || !kx || !ky || !kz || !kw) {
+    set_error("null argument");
+    return MRG_ERR_INVALID;
+  }
+  if (frame < 0 || frame >= p->T) {
+    set_error("frame index out of range");
+    return MRG_ERR_INVALID;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t bytes = sizeof(float) * (size_t)M;
+  void *dx, *dy, *dz, *dw;
+  bool s0, s1, s2, s3;
+  MRG_TRY(dev_view(p, 0, kx, bytes, true, st, &dx, &s0));
+  MRG_TRY(dev_view(p, 1, ky, bytes, true, st, &dy, &s1));
+  MRG_TRY(dev_view(p, 2, kz, bytes, true, st, &dz, &s2));
+  MRG_TRY(dev_view(p, 3, kw, bytes, true, st, &dw, &s3));
+  const GridConst gc = grid_const(p);
+  MRG_TRY(traj_setup(gc, p->frames[frame], (const float *)dx, (const float *)dy, (const float *)dz,
+                     (const float *)dw, M, p->max_pairs, st));
+  invalidate_graphs(p);
+  MRG_TRY(ensure_y(p, (int64_t)p->frames[frame].nvalid * p->C));
+  return MRG_OK;
+}
+
+mrg_status mrg_set_data(mrg_plan *p, int frame, const void *data, int64_t coil_stride, void *stream) {
+  MRG_TRY(check_frame(p, frame));
+  if (!data) {
+    set_error("null data");
+    return MRG_ERR_INVALID;
+  }
+  FrameTraj &ft = p->frames[frame];
+  if (p->C > 1 && coil_stride < ft.M) {
+    set_error("coil_stride smaller than the sample count");
+    return MRG_ERR_INVALID;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  if (!ft.dsorted) MRG_CUDA(cudaMalloc(&ft.dsorted, sizeof(float2) * std::max<int64_t>(1, (int64_t)ft.nvalid * p->C)));
+  void *src;
+  bool staged;
+  const size_t bytes = sizeof(float2) * (size_t)(coil_stride * (p->C - 1) + ft.M);
+  MRG_TRY(dev_view(p, 0, data, bytes, true, st, &src, &staged));
+  MRG_TRY(launch_gather_samples(ft, p->C, (const float2 *)src, coil_stride, ft.dsorted, st));
+  if (staged) MRG_CUDA(cudaStreamSynchronize(st));
+  ft.has_data = true;
+  return MRG_OK;
+}
+
+mrg_status mrg_adjoint(mrg_plan *p, int frame, const void *data, int64_t coil_stride, void *X, void *stream) {
+  MRG_TRY(check_frame(p, frame));
+  if (!data || !X) {
+    set_error("null argument");
+    return MRG_ERR_INVALID;
+  }
+  if (p->C > 1 && !p->has_smaps) {
+    set_error("coil maps not set");
+    return MRG_ERR_STATE;
+  }
+  const FrameTraj &ft = p->frames[frame];
+  if (p->C > 1 && coil_stride < ft.M) {
+    set_error("coil_stride smaller than the sample count");
+    return MRG_ERR_INVALID;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  void *dd, *dX;
+  bool sd, sX;
+  MRG_TRY(dev_view(p, 0, data, sizeof(float2) * (size_t)(coil_stride * (p->C - 1) + ft.M), true, st, &dd, &sd));
+  MRG_TRY(dev_view(p, 1, X, sizeof(float2) * p->nimg, true, st, &dX, &sX));
+  MRG_TRY(launch_gather_samples(ft, p->C, (const float2 *)dd, coil_stride, p->d_y, st));
+  MRG_TRY(run_EH(p, ft, p->d_y, plan_smap(p), (float2 *)dX, st));
+  if (sX) {
+    MRG_CUDA(cudaMemcpyAsync(X, dX, sizeof(float2) * p->nimg, cudaMemcpyDeviceToHost, st));
+    MRG_CUDA(cudaStreamSynchronize(st));
+  }
+  return MRG_OK;
+}
+
+mrg_status mrg_forward(mrg_plan *p, int frame, const void *X, void *data, int64_t coil_stride, const void *diff,
+                       void *stream) {
+  MRG_TRY(check_frame(p, frame));
+  if (!data || !X) {
+    set_error("null argument");
+    return MRG_ERR_INVALID;
+  }
+  if (p->C > 1 && !p->has_smaps) {
+    set_error("coil maps not set");
+    return MRG_ERR_STATE;
+  }
+  const FrameTraj &ft = p->frames[frame];
+  if (p->C > 1 && coil_stride < ft.M) {
+    set_error("coil_stride smaller than the sample count");
+    return MRG_ERR_INVALID;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t dbytes = sizeof(float2) * (size_t)(coil_stride * (p->C - 1) + ft.M);
+  void *dX, *dd, *ddf = nullptr;
+  bool sX, sd, sdf = false;
+  MRG_TRY(dev_view(p, 0, X, sizeof(float2) * p->nimg, true, st, &dX, &sX));
+  MRG_TRY(dev_view(p, 1, data, dbytes, false, st, &dd, &sd));
+  float2 *dsort = nullptr;
+  if (diff) {
+    // the sorted copy of diff lives behind the samples in the y buffer
+    MRG_TRY(dev_view(p, 2, diff, dbytes, true, st, &ddf, &sdf));
+    const int64_t ny = std::max<int64_t>(1, (int64_t)ft.nvalid * p->C);
+    MRG_TRY(ensure_y(p, 2 * ny));
+    dsort = p->d_y + ny;
+    MRG_TRY(launch_gather_samples(ft, p->C, (const float2 *)ddf, coil_stride, dsort, st));
+  }
+  MRG_TRY(run_E(p, ft, (const float2 *)dX, plan_smap(p), dsort, p->d_y, st));
+  MRG_TRY(launch_scatter_samples(ft, p->C, p->d_y, (float2 *)dd, coil_stride, st));
+  if (sd) {
+    MRG_CUDA(cudaMemcpyAsync(data, dd, dbytes, cudaMemcpyDeviceToHost, st));
+    MRG_CUDA(cudaStreamSynchronize(st));
+  }
+  return MRG_OK;
+}
+
+mrg_status mrg_normal(mrg_plan *p, int frame, const void *X, void *out, void *stream) {
+  MRG_TRY(check_frame(p, frame));
+  if (!X || !out) {
+    set_error("null argument");
+    return MRG_ERR_INVALID;
+  }
+  if (p->C > 1 && !p->has_smaps) {
+    set_error("coil maps not set");
+    return MRG_ERR_STATE;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  void *dX, *dO;
+  bool sX, sO;
+  MRG_TRY(dev_view(p, 0, X, sizeof(float2) * p->nimg, true, st, &dX, &sX));
+  MRG_TRY(dev_view(p, 1, out, sizeof(float2) * p->nimg, false, st, &dO, &sO));
+  const FrameTraj &ft = p->frames[frame];
+  MRG_TRY(launch_zero(dO, sizeof(float2) * p->nimg, st));
+  MRG_TRY(run_E(p, ft, (const float2 *)dX, plan_smap(p), nullptr, p->d_y, st));
+  MRG_TRY(run_EH(p, ft, p->d_y, plan_smap(p), (float2 *)dO, st));
+  if (sO) {
+    MRG_CUDA(cudaMemcpyAsync(out, dO, sizeof(float2) * p->nimg, cudaMemcpyDeviceToHost, st));
+    MRG_CUDA(cudaStreamSynchronize(st));
+  }
+  return MRG_OK;
+}
+
+mrg_status mrg_adjoint_coil(mrg_plan *p, int frame, const void *smap, const void *data, void *X, void *stream) {
+  MRG_TRY(check_frame(p, frame));
+  if (p->C != 1) {
+    set_error("per-coil calls need a single-coil plan");
+    return MRG_ERR_INVALID;
+  }
+  if (!data || !X) {
+    set_error("null argument");
+    return MRG_ERR_INVALID;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  const FrameTraj &ft = p->frames[frame];
+  void *dd, *dX, *ds;
+  bool sd, sX, ss;
+  MRG_TRY(dev_view(p, 0, data, sizeof(float2) * (size_t)ft.M, true, st, &dd, &sd));
+  MRG_TRY(dev_view(p, 1, X, sizeof(float2) * p->nimg, true, st, &dX, &sX));
+  MRG_TRY(dev_view(p, 2, smap, sizeof(float2) * p->nimg, true, st, &ds, &ss));
+  MRG_TRY(launch_gather_samples(ft, 1, (const float2 *)dd, 0, p->d_y, st));
+  MRG_TRY(run_EH(p, ft, p->d_y, (const float2 *)ds, (float2 *)dX, st));
+  if (sX) {
+    MRG_CUDA(cudaMemcpyAsync(X, dX, sizeof(float2) * p->nimg, cudaMemcpyDeviceToHost, st));
+    MRG_CUDA(cudaStreamSynchronize(st));
+  }
+  return MRG_OK;
+}
+
+mrg_status mrg_forward_coil(mrg_plan *p, int frame, const void *X, const void *smap, void *data, const void *diff,
+                            void *stream) {
+  MRG_TRY(check_frame(p, frame));
+  if (p->C != 1) {
+    set_error("per-coil calls need a single-coil plan");
+    return MRG_ERR_INVALID;
+  }
+  if (!data || !X) {
+    set_error("null argument");
+    return MRG_ERR_INVALID;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  const FrameTraj &ft = p->frames[frame];
+  const size_t dbytes = sizeof(float2) * (size_t)ft.M;
+  void *dX, *ds, *dd;
+  bool sX, ss, sd;
+  MRG_TRY(dev_view(p, 0, X, sizeof(float2) * p->nimg, true, st, &dX, &sX));
+  MRG_TRY(dev_view(p, 1, smap, sizeof(float2) * p->nimg, true, st, &ds, &ss));
+  MRG_TRY(dev_view(p, 2, data, dbytes, false, st, &dd, &sd));
+  float2 *dsort = nullptr;
+  if (diff) {
+    void *ddf;
+    bool sdf;
+    MRG_TRY(dev_view(p, 3, diff, dbytes, true, st, &ddf, &sdf));
+    const int64_t ny = std::max<int64_t>(1, (int64_t)ft.nvalid);
+    MRG_TRY(ensure_y(p, 2 * ny));
+    dsort = p->d_y + ny;
+    MRG_TRY(launch_gather_samples(ft, 1, (const float2 *)ddf, 0, dsort, st));
+  }
+  MRG_TRY(run_E(p, ft, (const float2 *)dX, (const float2 *)ds, dsort, p->d_y, st));
+  MRG_TRY(launch_scatter_samples(ft, 1, p->d_y, (float2 *)dd, 0, st));
+  if (sd) {
+    MRG_CUDA(cudaMemcpyAsync(data, dd, dbytes, cudaMemcpyDeviceToHost, st));
+    MRG_CUDA(cudaStreamSynchronize(st));
+  }
+  return MRG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// SENSE-CG (src/recon_lib.cpp:1523-1759)
+// ---------------------------------------------------------------------------
+static mrg_status ensure_solver(mrg_plan *p, bool fista) {
+  const size_t vb = sizeof(float2) * (size_t)p->nimg * p->T;
+  if (!p->d_R) MRG_CUDA(cudaMalloc(&p->d_R, vb));
+  if (!p->d_P) MRG_CUDA(cudaMalloc(&p->d_P, vb));
+  if (!p->d_L) MRG_CUDA(cudaMalloc(&p->d_L, vb));
+  if (fista && !p->d_Xo) MRG_CUDA(cudaMalloc(&p->d_Xo, vb));
+  return MRG_OK;
+}
+
+static mrg_status ensure_resid(mrg_plan *p, int n) {
+  if (p->resid_cap >= n) return MRG_OK;
+  invalidate_graphs(p);
+  cudaFree(p->d_resid);
+  p->d_resid = nullptr;
+  MRG_CUDA(cudaMalloc(&p->d_resid, sizeof(double) * std::max(n, 1)));
+  p->resid_cap = n;
+  return MRG_OK;
+}
+
+// LHS = sum_c E^H W E P per frame, then the vector updates of one CG iteration.
+static mrg_status cg_iteration(mrg_plan *p, float2 *X, cudaStream_t st) {
+  const int64_t n = p->nimg;
+  const int64_t nt = n * p->T;
+  for (int t = 0; t < p->T; t++) {
+    const FrameTraj &ft = p->frames[t];
+    float2 *Lt = p->d_L + t * n;
+    MRG_TRY(launch_zero(Lt, sizeof(float2) * n, st));
+    MRG_TRY(run_E(p, ft, p->d_P + t * n, plan_smap(p), nullptr, p->d_y, st));
+    MRG_TRY(run_EH(p, ft, p->d_y, plan_smap(p), Lt, st));
+  }
+  MRG_TRY(cg_dots(p->d_R, p->d_P, p->d_L, nt, p->d_part, p->nblk, p->d_sc, st));
+  MRG_TRY(cg_update(X, p->d_R, p->d_P, p->d_L, nt, p->d_part, p->nblk, p->d_sc, p->d_resid, st));
+  MRG_TRY(cg_pupdate(p->d_P, p->d_R, nt, p->d_sc, st));
+  return MRG_OK;
+}
+
+mrg_status mrg_cg(mrg_plan *p, int max_iter, void *X, double *resid, int use_graph, void *stream) {
+  if (!p || !X || max_iter < 0) {
+    set_error("bad argument");
+    return MRG_ERR_INVALID;
+  }
+  for (int t = 0; t < p->T; t++) {
+    MRG_TRY(check_frame(p, t));
+    if (!p->frames[t].has_data) {
+      set_error("k-space data not set for a frame");
+      return MRG_ERR_STATE;
+    }
+  }
+  if (p->C > 1 && !p->has_smaps) {
+    set_error("coil maps not set");
+    return MRG_ERR_STATE;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  MRG_TRY(ensure_solver(p, false));
+  MRG_TRY(ensure_resid(p, max_iter));
+  const int64_t n = p->nimg, nt = n * p->T;
+  void *dX;
+  bool sX;
+  MRG_TRY(dev_view(p, 0, X, sizeof(float2) * nt, false, st, &dX, &sX));
+  float2 *Xd = (float2 *)dX;
+  // R = sum_c E^H W d, P = R, X = 0  (src/recon_lib.cpp:1537-1573)
+  MRG_TRY(launch_zero(Xd, sizeof(float2) * nt, st));
+  MRG_TRY(launch_zero(p->d_R, sizeof(float2) * nt, st));
+  for (int t = 0; t < p->T; t++)
+    MRG_TRY(run_EH(p, p->frames[t], p->frames[t].dsorted, plan_smap(p), p->d_R + t * n, st));
+  MRG_TRY(launch_copy(p->d_P, p->d_R, nt, st));
+  Scalars z;
+  memset(&z, 0, sizeof(z));
+  MRG_CUDA(cudaMemcpyAsync(p->d_sc, &z, sizeof(Scalars), cudaMemcpyHostToDevice, st));
+  MRG_CUDA(cudaStreamSynchronize(st));
+  if (use_graph && max_iter > 0) {
+    if (!p->cg_exec || p->cg_key[0] != dX) {
+      invalidate_graphs(p);
+      cudaStream_t cs;
+      MRG_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+      cudaGraph_t graph;
+      if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+        cudaStreamDestroy(cs);
+        set_error("stream capture failed to start");
+        return MRG_ERR_CUDA;
+      }
+      const mrg_status cap = cg_iteration(p, Xd, cs);
+      const cudaError_t ee = cudaStreamEndCapture(cs, &graph);
+      cudaStreamDestroy(cs);
+      if (cap != MRG_OK) return cap;
+      if (ee != cudaSuccess) {
+        set_error(std::string("stream capture failed: ") + cudaGetErrorString(ee));
+        return MRG_ERR_CUDA;
+      }
+      const cudaError_t ie = cudaGraphInstantiate(&p->cg_exec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (ie != cudaSuccess) {
+        p->cg_exec = nullptr;
+        set_error(std::string("graph instantiate failed: ") + cudaGetErrorString(ie));
+        return MRG_ERR_CUDA;
+      }
+      p->cg_key[0] = dX;
+    }
+    for (int it = 0; it < max_iter; it++) {
+      MRG_CUDA(cudaGraphLaunch(p->cg_exec, st));
+      count_launch();
+    }
+  } else {
+    for (int it = 0; it < max_iter; it++) MRG_TRY(cg_iteration(p, Xd, st));
+  }
+  if (resid && max_iter > 0)
+    MRG_CUDA(cudaMemcpyAsync(resid, p->d_resid, sizeof(double) * max_iter, cudaMemcpyDeviceToHost, st));
+  if (sX) MRG_CUDA(cudaMemcpyAsync(X, dX, sizeof(float2) * nt, cudaMemcpyDeviceToHost, st));
+  if (resid || sX) MRG_CUDA(cudaStreamSynchronize(st));
+  return MRG_OK;
+}
+
+mrg_status mrg_last_timings(const mrg_plan *p, float out[8]) {
+  if (!p || !out) {
+    set_error("null argument");
+    return MRG_ERR_INVALID;
+  }
+  memcpy(out, p->timings, sizeof(p->timings));
+  return MRG_OK;
+}
+
+void mrg_fista_params_default(mrg_fista_params *q) {
+  if (!q) return;
+  q->max_iter = 50;
+  q->max_eig_iter = 30;
+  q->fista = 1;
+  q->cycle_spins = 4;
+  q->wave_levels[0] = q->wave_levels[1] = q->wave_levels[2] = 4;
+  q->wave_type = 1;
+  q->thresh = 0.0f;
+  q->use_threshold = 0;
+  q->llr_block[0] = q->llr_block[1] = q->llr_block[2] = 4;
+  q->llr_block_iter = 4;
+  q->llr_alpha = 0.0f;
+  q->clear_amp = 4.0f;
+  q->clear_t2 = 6.0f;
+  q->rand_skip = -1;
+}
+
+}  // extern "C"

@@ -1,0 +1,313 @@
+// Batched strided complex FFT passes for the oversampled 3D grid.
+//
+// Replaces the per-axis line FFTs of NDarray::fft3 (src/ArrayTemplates.cpp:276-427)
+// as used by gridFFT::do_fft / do_ifft (src/gridFFT.cpp:645-711): every axis is
+// transformed with FFTW's sign convention (forward = exp(-i...)) and scaled by
+// 1/sqrt(S).  The E side is pruned (only the crop of the image is non-zero) and
+// the E^H side only produces the crop it keeps, which is exact because the
+// dropped inputs are zero and the dropped outputs are never read.
+//
+// One CTA transforms IB lines (consecutive "inner" elements, coalesced rows of
+// IB complex values) of length S = 8*Q held in shared memory as [S][IB+1].
+// Each line is split S = 8 x Q (four-step): 8-point DFTs across the 8 threads
+// of a line, a twiddle, then a Q-point DFT in registers per thread.  Twiddles
+// come from a constant-memory table exp(-2 pi i m / 2304), 2304 being a common
+// multiple of every supported S.
+#include "mrg_internal.h"
+
+namespace mrg {
+
+constexpr int TW_LCM = 2304;
+__constant__ float2 c_tw[TW_LCM];
+
+static const int kSupportedQ[] = {3, 6, 9, 12, 18, 24, 36, 48};
+
+bool fft_size_supported(int S) {
+  if (S % 8) return false;
+  for (int q : kSupportedQ)
+    if (q * 8 == S) return true;
+  return false;
+}
+
+mrg_status fft_init_device() {
+  static thread_local int done_dev = -1;
+  int dev = 0;
+  MRG_CUDA(cudaGetDevice(&dev));
+  if (done_dev == dev) return MRG_OK;
+  std::vector<float2> tw(TW_LCM);
+  for (int m = 0; m < TW_LCM; m++) {
+    double a = -2.0 * 3.141592653589793238462643 * (double)m / (double)TW_LCM;
+    tw[m] = make_float2((float)cos(a), (float)sin(a));
+  }
+  MRG_CUDA(cudaMemcpyToSymbol(c_tw, tw.data(), sizeof(float2) * TW_LCM));
+  done_dev = dev;
+  return MRG_OK;
+}
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+// SIGN * i * a
+template <int SIGN>
+__device__ __forceinline__ float2 imul(float2 a) {
+  return SIGN > 0 ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
+}
+template <int SIGN>
+__device__ __forceinline__ float2 twid(int m) {
+  float2 w = c_tw[m];
+  if (SIGN > 0) w.y = -w.y;
+  return w;
+}
+
+// t[q] <- sum_p t[p] * exp(SIGN*2*pi*i*p*q/P)
+template <int P, int SIGN>
+__device__ __forceinline__ void bfly(float2 (&t)[P]) {
+  if constexpr (P == 2) {
+    float2 a = t[0], b = t[1];
+    t[0] = cadd(a, b);
+    t[1] = csub(a, b);
+  } else if constexpr (P == 3) {
+    const float h = 0.86602540378443864676f;
+    float2 s = cadd(t[1], t[2]), d = csub(t[1], t[2]);
+    float2 m = make_float2(t[0].x - 0.5f * s.x, t[0].y - 0.5f * s.y);
+    float2 r = imul<SIGN>(make_float2(h * d.x, h * d.y));
+    t[0] = cadd(t[0], s);
+    t[1] = cadd(m, r);
+    t[2] = csub(m, r);
+  } else if constexpr (P == 4) {
+    float2 a = cadd(t[0], t[2]), b = csub(t[0], t[2]);
+    float2 c = cadd(t[1], t[3]), d = imul<SIGN>(csub(t[1], t[3]));
+    t[0] = cadd(a, c);
+    t[2] = csub(a, c);
+    t[1] = cadd(b, d);
+    t[3] = csub(b, d);
+  } else {
+    static_assert(P == 2 || P == 3 || P == 4, "radix");
+  }
+}
+
+constexpr int first_factor(int q) { return (q % 4 == 0) ? 4 : ((q % 2 == 0) ? 2 : 3); }
+
+// In-register DFT of length Q (decimation in time), natural order in and out.
+template <int Q, int SIGN>
+__device__ __forceinline__ void reg_fft(float2 (&v)[Q]) {
+  if constexpr (Q == 1) {
+    return;
+  } else {
+    constexpr int P = first_factor(Q);
+    constexpr int Q2 = Q / P;
+    float2 sub[P][Q2];
+#pragma unroll
+    for (int p = 0; p < P; p++)
+#pragma unroll
+      for (int m = 0; m < Q2; m++) sub[p][m] = v[p + P * m];
+#pragma unroll
+    for (int p = 0; p < P; p++) reg_fft<Q2, SIGN>(sub[p]);
+#pragma unroll
+    for (int k = 0; k < Q2; k++) {
+      float2 t[P];
+#pragma unroll
+      for (int p = 0; p < P; p++) t[p] = (p * k == 0) ? sub[p][k] : cmul(sub[p][k], twid<SIGN>(p * k * (TW_LCM / Q)));
+      bfly<P, SIGN>(t);
+#pragma unroll
+      for (int q = 0; q < P; q++) v[k + Q2 * q] = t[q];
+    }
+  }
+}
+
+template <int Q, int SIGN, int MODE>
+__global__ void __launch_bounds__(256, 2) k_fft(const FftPass p) {
+  constexpr int S = 8 * Q;
+  extern __shared__ float2 sm[];
+  const int IB = p.IB, IBp = p.IB + 1;
+  const int tid = threadIdx.x;
+  const int j = tid % IB, t = tid / IB;  // 8 threads per line
+  const int64_t line = (int64_t)blockIdx.x * IB + j;
+  const bool lv = line < p.nlines;
+  int64_t o = 0, i = 0;
+  if (lv) {
+    o = line / p.inner;
+    i = line - o * p.inner;
+  }
+
+  // ---- load (zero rows outside [in_off, in_off + Lin)) ----
+  if (!p.lfast) {
+    const int64_t ib = o * p.in_os + i;
+    for (int r = t; r < S; r += 8) {
+      float2 v = make_float2(0.f, 0.f);
+      const int li = r - p.in_off;
+      if (lv && li >= 0 && li < p.Lin) {
+        const int64_t off = ib + (int64_t)li * p.in_ls;
+        if constexpr (MODE == FFT_SETIMG) {
+          const int64_t vox = off / p.C;
+          const float w = (p.wl[li] * p.wo[o]) * p.wi[i / p.C];
+          const float2 x = p.X[vox];
+          v = make_float2(w * x.x, w * x.y);
+          if (p.has_smap) v = cmul(v, p.smap[off]);
+        } else {
+          v = p.in[off];
+        }
+      }
+      sm[r * IBp + j] = v;
+    }
+  } else {
+    // inner == 1 and in_ls == 1: each line is contiguous; sweep along lines.
+    const int64_t l0 = (int64_t)blockIdx.x * IB;
+    for (int e = tid; e < S * IB; e += blockDim.x) {
+      const int jj = e / S, r = e - jj * S;
+      float2 v = make_float2(0.f, 0.f);
+      const int li = r - p.in_off;
+      const int64_t ln = l0 + jj;
+      if (ln < p.nlines && li >= 0 && li < p.Lin) v = p.in[ln * p.in_os + li];
+      sm[r * IBp + jj] = v;
+    }
+  }
+  __syncthreads();
+
+  // ---- step A: 8-point DFTs over n1 (rows Q*n1 + n2), twiddle W_S^(n2*k1) ----
+  for (int n2 = t; n2 < Q; n2 += 8) {
+    float2 a[8];
+#pragma unroll
+    for (int n1 = 0; n1 < 8; n1++) a[n1] = sm[(Q * n1 + n2) * IBp + j];
+    reg_fft<8, SIGN>(a);
+#pragma unroll
+    for (int k1 = 1; k1 < 8; k1++) a[k1] = cmul(a[k1], twid<SIGN>(n2 * k1 * (TW_LCM / S)));
+#pragma unroll
+    for (int k1 = 0; k1 < 8; k1++) sm[(Q * k1 + n2) * IBp + j] = a[k1];
+  }
+  __syncthreads();
+
+  // ---- step C: Q-point DFT of rows Q*t .. Q*t+Q-1 -> rows t + 8*k2 ----
+  {
+    float2 v[Q];
+#pragma unroll
+    for (int n2 = 0; n2 < Q; n2++) v[n2] = sm[(Q * t + n2) * IBp + j];
+    reg_fft<Q, SIGN>(v);
+    __syncthreads();
+#pragma unroll
+    for (int k2 = 0; k2 < Q; k2++) sm[(t + 8 * k2) * IBp + j] = v[k2];
+  }
+  __syncthreads();
+
+  // ---- store ----
+  if constexpr (MODE != FFT_ACCUM) {
+    if (!p.lfast) {
+      if (lv) {
+        const int64_t ob = o * p.out_os + i;
+        for (int r = t; r < p.Lout; r += 8) {
+          float2 v = sm[(r + p.out_off) * IBp + j];
+          p.out[ob + (int64_t)r * p.out_ls] = make_float2(v.x * p.scale, v.y * p.scale);
+        }
+      }
+    } else {
+      const int64_t l0 = (int64_t)blockIdx.x * IB;
+      for (int e = tid; e < p.Lout * IB; e += blockDim.x) {
+        const int jj = e / p.Lout, r = e - jj * p.Lout;
+        const int64_t ln = l0 + jj;
+        if (ln < p.nlines) {
+          float2 v = sm[(r + p.out_off) * IBp + jj];
+          p.out[ln * p.out_os + r] = make_float2(v.x * p.scale, v.y * p.scale);
+        }
+      }
+    }
+  } else {
+    // X += sum_c (wl*wo*wi) * v * conj(smap)   (gridFFT::accumulate, src/gridFFT.cpp:926-941)
+    const int C = p.C;
+    if (lv) {
+      const int64_t sb = o * p.out_os + i;
+      for (int r = t; r < p.Lout; r += 8) {
+        float2 v = sm[(r + p.out_off) * IBp + j];
+        v = make_float2(v.x * p.scale, v.y * p.scale);
+        const float w = (p.wl[r] * p.wo[o]) * p.wi[i / C];
+        v = make_float2(w * v.x, w * v.y);
+        if (p.has_smap) {
+          float2 s = p.smap[sb + (int64_t)r * p.out_ls];
+          s.y = -s.y;
+          v = cmul(v, s);
+        }
+        if (p.acc_atomic) {
+          float2 *dst = p.acc + (int64_t)r * p.acc_l + o * p.acc_o + i / C;
+          atomicAdd(&dst->x, v.x);
+          atomicAdd(&dst->y, v.y);
+        } else {
+          sm[(r + p.out_off) * IBp + j] = v;
+        }
+      }
+    }
+    if (!p.acc_atomic) {
+      __syncthreads();
+      // IB is a multiple of C: the C lines of one voxel are consecutive in this CTA.
+      const int G = IB / C;
+      const int64_t line0 = (int64_t)blockIdx.x * IB;
+      for (int e = tid; e < p.Lout * G; e += blockDim.x) {
+        const int g = e % G, r = e / G;
+        const int64_t ln = line0 + (int64_t)g * C;
+        if (ln >= p.nlines) continue;
+        const int64_t oo = ln / p.inner, ii = ln - oo * p.inner;
+        float2 s = make_float2(0.f, 0.f);
+        for (int c = 0; c < C; c++) s = cadd(s, sm[(r + p.out_off) * IBp + g * C + c]);
+        float2 *dst = p.acc + (int64_t)r * p.acc_l + oo * p.acc_o + ii / C;
+        float2 cur = *dst;
+        *dst = cadd(cur, s);
+      }
+    }
+  }
+}
+
+template <int Q>
+static mrg_status launch_q(const FftPass &p, cudaStream_t st) {
+  const size_t smem = (size_t)8 * Q * (p.IB + 1) * sizeof(float2);
+  const int64_t nblk64 = (p.nlines + p.IB - 1) / p.IB;
+  if (nblk64 > 0x7fffffff) {
+    set_error("fft pass too large");
+    return MRG_ERR_UNSUPPORTED;
+  }
+  const dim3 grid((unsigned)nblk64), block(8 * p.IB);
+  void (*fn)(const FftPass);
+  if (p.mode == FFT_SETIMG) fn = k_fft<Q, -1, FFT_SETIMG>;
+  else if (p.mode == FFT_ACCUM) fn = k_fft<Q, +1, FFT_ACCUM>;
+  else if (p.sign < 0) fn = k_fft<Q, -1, FFT_PLAIN>;
+  else fn = k_fft<Q, +1, FFT_PLAIN>;
+  static int attr_set[4] = {0, 0, 0, 0};  // per instantiation: set the smem cap once
+  const int slot = p.mode == FFT_PLAIN ? (p.sign < 0 ? 0 : 1) : (p.mode == FFT_SETIMG ? 2 : 3);
+  if (!attr_set[slot]) {
+    MRG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 8 * Q * 33 * (int)sizeof(float2)));
+    attr_set[slot] = 1;
+  }
+  fn<<<grid, block, smem, st>>>(p);
+  MRG_LAUNCHED();
+  return MRG_OK;
+}
+
+mrg_status launch_fft(const FftPass &p, cudaStream_t st) {
+  if (p.nlines <= 0) return MRG_OK;
+  if ((p.mode == FFT_SETIMG && p.sign >= 0) || (p.mode == FFT_ACCUM && p.sign <= 0)) {
+    set_error("fft pass: mode/sign mismatch");
+    return MRG_ERR_INVALID;
+  }
+  if (p.IB < 1 || p.IB > 32) {
+    set_error("fft pass: bad IB");
+    return MRG_ERR_INVALID;
+  }
+  if (p.lfast && (p.mode != FFT_PLAIN || p.inner != 1)) {
+    set_error("fft pass: contiguous-line mode needs a plain pass over single lines");
+    return MRG_ERR_INVALID;
+  }
+  switch (p.S) {
+    case 24: return launch_q<3>(p, st);
+    case 48: return launch_q<6>(p, st);
+    case 72: return launch_q<9>(p, st);
+    case 96: return launch_q<12>(p, st);
+    case 144: return launch_q<18>(p, st);
+    case 192: return launch_q<24>(p, st);
+    case 288: return launch_q<36>(p, st);
+    case 384: return launch_q<48>(p, st);
+    default:
+      set_error("unsupported FFT length " + std::to_string(p.S));
+      return MRG_ERR_UNSUPPORTED;
+  }
+}
+
+}  // namespace mrg

@@ -1,0 +1,184 @@
+// Host-side plan geometry: grid size, crop, Kaiser-Bessel (or triangle / sinc /
+// polynomial) lookup table and deapodisation windows.  These are set-up tables
+// computed once per plan with the formulas and float/double promotions of
+// gridFFT::precalc_kernel and gridFFT::precalc_gridding
+// (src/gridFFT.cpp:276-643), so the tables match the reference's bit for bit
+// when compiled without floating-point contraction.
+#include <algorithm>
+#include <cmath>
+
+#include "mrg_internal.h"
+
+namespace mrg {
+
+static const double kRefPI = 3.14159265359;  // src/gridFFT.h:24
+
+// I0 by the Abramowitz & Stegun 9.8.1/9.8.2 polynomials, in the reference's
+// float/double mix (src/gridFFT.cpp:1325-1352).
+static float bessel_i0(float x) {
+  float ax, ans;
+  double y;
+  if ((ax = std::fabs(x)) < 3.75f) {
+    y = x / 3.75;
+    y *= y;
+    ans = (float)(1.0 + y * (3.5156229 + y * (3.0899424 + y * (1.2067492 + y * (0.2659732 + y * (0.360768e-1 + y * 0.45813e-2))))));
+  } else {
+    y = 3.75 / ax;
+    ans = (float)((std::exp((double)ax) / std::sqrt((double)ax)) *
+                  (0.39894228 + y * (0.1328592e-1 + y * (0.225319e-2 + y * (-0.157565e-2 + y * (0.916281e-2 + y * (-0.2057706e-1 + y * (0.2635537e-1 + y * (-0.1647633e-1 + y * 0.392377e-2)))))))));
+  }
+  return ans;
+}
+
+void build_geometry(Geometry &g, const mrg_config &cfg, int Nx, int Ny, int Nz) {
+  g.N[0] = Nx;
+  g.N[1] = Ny;
+  g.N[2] = Nz;
+  g.k_rad = cfg.k_rad;
+  g.kernel_type = cfg.kernel_type;
+  for (int d = 0; d < 3; d++) {
+    // rounded gridding ratio: S is a multiple of 16 (src/gridFFT.cpp:500-527)
+    g.grid[d] = (float)(16.0 * std::ceil((cfg.overgrid * (float)g.N[d]) / 16.0) / (float)g.N[d]);
+    g.S[d] = (int)(g.grid[d] * g.N[d]);
+    g.og[d] = (int)((float)g.N[d] * (g.grid[d] - 1) / 2.0);  // src/gridFFT.cpp:536-541
+  }
+  for (int d = 0; d < 3; d++) {
+    g.grid_mod[d] = 600;  // table points per grid unit (src/gridFFT.cpp:278-280)
+    float dw = cfg.dwin;
+    if (dw == -1) dw = (cfg.kernel_type == MRG_KERNEL_TRIANGLE) ? 1.0f : (cfg.kernel_type == MRG_KERNEL_POLY ? 2.0f : 2.5f);
+    g.dwin[d] = dw;
+    const int glen = (int)((float)dw * (float)g.grid_mod[d]);
+    g.lut_len = glen + 10;
+    std::vector<float> &f = g.lut[d];
+    f.assign(glen + 10, 0.0f);
+    g.beta[d] = 0.0f;
+    switch (cfg.kernel_type) {
+      case MRG_KERNEL_TRIANGLE:
+        for (int i = 0; i < glen + 1; i++) f[i] = 1.0f - (float)i / (float)glen;
+        break;
+      case MRG_KERNEL_SINC:
+        for (int i = 0; i < glen + 1; i++) {
+          const float pos = ((float)i * (float)dw) / ((float)glen);
+          f[i] = (pos < 0.01f) ? 1.0f : (float)(std::sin(pos * kRefPI) / (pos * kRefPI));
+          f[i] *= (float)(0.54 + 0.46 * std::cos(kRefPI * (float)i / ((float)glen)));
+        }
+        break;
+      case MRG_KERNEL_POLY: {
+        const int len = glen + 10;
+        for (int i = 0; i < len; i++) {
+          const double x = double(i) / double(len), x2 = x * x, x3 = x * x2, x4 = x2 * x2, x5 = x * x4;
+          f[i] = (float)(1. + 0.04522831 * x - 3.36020304 * x2 + 1.12417012 * x3 + 2.82448025 * x4 - 1.63447764 * x5);
+        }
+      } break;
+      default: {  // Kaiser-Bessel, beta after Beatty et al. (src/gridFFT.cpp:342-381)
+        const float a = g.grid[d];
+        float beta = (float)(kRefPI * sqrtf((float)((dw * dw) / (a * a) * (a - 0.5) * (a - 0.5) - 0.8)));
+        const float bmin = (float)std::sqrt(std::pow(kRefPI * 2 * dw / a, 2.0) - 9.6752);
+        beta = (bmin > beta) ? bmin : beta;
+        g.beta[d] = beta;
+        for (int i = 0; i < glen + 1; i++) {
+          const float pos = ((float)i) / ((float)glen);
+          const float arg = sqrtf((float)(1.0 - pos * pos));
+          f[i] = bessel_i0(beta * arg) / bessel_i0(beta);
+        }
+      } break;
+    }
+    // normalise to sum 0.5*grid_mod (src/gridFFT.cpp:470-472); summed in double
+    double s = 0.0;
+    for (float v : f) s += v;
+    const double scale = 0.5 * g.grid_mod[d] / s;
+    for (float &v : f) v = (float)(v * scale);
+  }
+  // deapodisation windows with the chop sign, 1/S and the crop folded in,
+  // normalised by the (signed) maximum (src/gridFFT.cpp:550-631)
+  for (int d = 0; d < 3; d++) {
+    const int S = g.S[d];
+    std::vector<float> &w = g.win[d];
+    w.assign(S, 0.0f);
+    const int og_e = g.og[d] + g.N[d];
+    for (int i = 0; i < S; i++) {
+      const float ipos = i - (float)S / 2.0f;
+      for (int gp = 0; gp < g.dwin[d] * g.grid_mod[d]; gp++)
+        w[i] = (float)(w[i] + 2 * std::cos(2 * kRefPI * ipos * gp / (float)g.grid_mod[d] / (float)S) * g.lut[d][gp]);
+      w[i] = (float)g.grid_mod[d] / w[i];
+      const float fact = (float)(2 * (i % 2) - 1);
+      w[i] *= fact / S;
+      w[i] = (float)(w[i] * ((i < g.og[d]) ? 0.0 : 1.0));
+      w[i] = (float)(w[i] * ((i > og_e - 1) ? 0.0 : 1.0));
+    }
+    float mx = w[0];
+    for (float v : w) mx = std::max(mx, v);
+    for (float &v : w) v /= mx;
+  }
+}
+
+// glibc random(): r[i] = r[i-3] + r[i-31] (mod 2^32), seeded by the
+// Park-Miller LCG from seed 1, first 310 values discarded, output r >> 1.
+GlibcRand::GlibcRand() {
+  int32_t s[34];
+  s[0] = 1;
+  for (int i = 1; i < 31; i++) {
+    int64_t v = (16807LL * s[i - 1]) % 2147483647LL;
+    if (v < 0) v += 2147483647LL;
+    s[i] = (int32_t)v;
+  }
+  for (int i = 31; i < 34; i++) s[i] = s[i - 31];
+  for (int i = 0; i < 34; i++) r[i] = (uint32_t)s[i];
+  pos = 34;
+  skip(310);
+}
+
+void GlibcRand::skip(int64_t n) {
+  for (int64_t k = 0; k < n; k++) {
+    r[pos % 34] = r[(pos - 31) % 34] + r[(pos - 3) % 34];
+    pos++;
+  }
+}
+
+int GlibcRand::next() {
+  const uint32_t v = r[(pos - 31) % 34] + r[(pos - 3) % 34];
+  r[pos % 34] = v;
+  pos++;
+  return (int)(v >> 1);
+}
+
+}  // namespace mrg
+
+extern "C" {
+
+mrg_status mrg_plan_geometry(const mrg_config *cfg_in, int Nx, int Ny, int Nz, int S[3], int og[3], float grid[3],
+                             float beta[3], int *lut_len, float *lut, float *win) {
+  if (Nx <= 0 || Ny <= 0 || Nz <= 0) {
+    mrg::set_error("sizes must be positive");
+    return MRG_ERR_INVALID;
+  }
+  mrg_config cfg;
+  if (cfg_in) cfg = *cfg_in; else mrg_config_default(&cfg);
+  mrg::Geometry g;
+  mrg::build_geometry(g, cfg, Nx, Ny, Nz);
+  size_t o = 0;
+  for (int d = 0; d < 3; d++) {
+    if (S) S[d] = g.S[d];
+    if (og) og[d] = g.og[d];
+    if (grid) grid[d] = g.grid[d];
+    if (beta) beta[d] = g.beta[d];
+    if (lut) std::copy(g.lut[d].begin(), g.lut[d].end(), lut + (size_t)d * g.lut_len);
+    if (win) std::copy(g.win[d].begin(), g.win[d].end(), win + o);
+    o += g.S[d];
+  }
+  if (lut_len) *lut_len = g.lut_len;
+  return MRG_OK;
+}
+
+mrg_status mrg_rand_stream(int64_t skip, int n, int *out) {
+  if (n < 0 || skip < 0 || (n > 0 && !out)) {
+    mrg::set_error("bad argument");
+    return MRG_ERR_INVALID;
+  }
+  mrg::GlibcRand r;
+  r.skip(skip);
+  for (int i = 0; i < n; i++) out[i] = r.next();
+  return MRG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,208 @@
+// Internal declarations shared by the CUDA translation units of libmrg.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "mrg.h"
+
+namespace mrg {
+
+// ---------------------------------------------------------------------------
+// errors and launch accounting
+// ---------------------------------------------------------------------------
+void set_error(const std::string &msg);
+extern std::atomic<int64_t> g_launches;
+inline void count_launch(int n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+#define MRG_CUDA(call)                                                                          \
+  do {                                                                                          \
+    cudaError_t e_ = (call);                                                                    \
+    if (e_ != cudaSuccess) {                                                                    \
+      ::mrg::set_error(std::string(#call) + " failed: " + cudaGetErrorString(e_));              \
+      return e_ == cudaErrorMemoryAllocation ? MRG_ERR_NOMEM : MRG_ERR_CUDA;                    \
+    }                                                                                           \
+  } while (0)
+#define MRG_LAUNCHED()                                                                          \
+  do {                                                                                          \
+    ::mrg::count_launch();                                                                      \
+    cudaError_t e_ = cudaGetLastError();                                                        \
+    if (e_ != cudaSuccess) {                                                                    \
+      ::mrg::set_error(std::string("kernel launch failed: ") + cudaGetErrorString(e_));         \
+      return MRG_ERR_CUDA;                                                                      \
+    }                                                                                           \
+  } while (0)
+#define MRG_TRY(call)              \
+  do {                             \
+    mrg_status s_ = (call);        \
+    if (s_ != MRG_OK) return s_;   \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// Geometry: grid sizes, crop, kernel LUT and deapodisation windows, computed on
+// the host exactly as gridFFT::precalc_gridding / precalc_kernel do
+// (src/gridFFT.cpp:276-643).
+// ---------------------------------------------------------------------------
+struct Geometry {
+  int N[3], S[3], og[3];
+  float grid[3], dwin[3], beta[3], grid_mod[3];
+  float k_rad;
+  int kernel_type;
+  int lut_len;
+  std::vector<float> lut[3];
+  std::vector<float> win[3];
+};
+void build_geometry(Geometry &g, const mrg_config &cfg, int Nx, int Ny, int Nz);
+
+// glibc random() stream for the default seed (srand never called by the reference).
+struct GlibcRand {
+  uint32_t r[34];
+  int64_t pos;
+  GlibcRand();
+  void skip(int64_t n);
+  int next();
+};
+
+// ---------------------------------------------------------------------------
+// Batched strided FFT pass (fft.cu).  A pass transforms `nlines` lines of
+// length S; line j = (o, i) with o = j / inner, i = j % inner.  Input row l of
+// line (o,i) sits at in[o*in_os + (l - in_off)*in_ls + i] for l in
+// [in_off, in_off + Lin) and is zero elsewhere; output rows [out_off,
+// out_off + Lout) go to out[o*out_os + (l - out_off)*out_ls + i].
+// ---------------------------------------------------------------------------
+enum { FFT_PLAIN = 0, FFT_SETIMG = 1, FFT_ACCUM = 2 };
+struct FftPass {
+  int S, sign, mode;
+  int Lin, in_off, Lout, out_off;
+  int inner, IB, lfast;
+  int64_t nlines;
+  int64_t in_ls, in_os, out_ls, out_os;
+  float scale;
+  const float2 *in;
+  float2 *out;
+  // FFT_SETIMG: v = (wl[l]*wo[o])*wi[i/C] * X[off/C] * in[off]  (in = smap or NULL)
+  // FFT_ACCUM : acc[(l*No + o)*Ni + i/C] += sum_c (wl*wo*wi)*v*conj(smap[...])
+  const float2 *X;
+  const float2 *smap;
+  float2 *acc;
+  const float *wl, *wo, *wi;
+  int C, has_smap;
+  int acc_atomic;
+  int64_t acc_l, acc_o;  // accumulator strides for l and o (i/C has stride 1)
+};
+bool fft_size_supported(int S);
+mrg_status fft_init_device();
+mrg_status launch_fft(const FftPass &p, cudaStream_t st);
+
+// ---------------------------------------------------------------------------
+// Gridding (gridding.cu)
+// ---------------------------------------------------------------------------
+struct GridConst {
+  int S[3];
+  float grid[3], cen[3], dwin[3], gmod[3];
+  const float *lut[3];
+  float k_rad;
+  int B;       // tile edge
+  int nt[3];   // tiles per axis
+  int C;       // coils
+};
+
+struct FrameTraj {
+  int64_t M = 0;
+  int nvalid = 0;
+  float4 *spos = nullptr;   // [M] sorted, valid first: (dkx, dky, dkz, kw)
+  float *stap = nullptr;    // [M] taper exp(-|k|^2/(2 k_rad^2))
+  int *perm = nullptr;      // [M] sorted -> original sample index
+  int *pairs = nullptr;     // sample index per (sample, tile) pair, grouped by tile
+  int64_t npairs = 0;
+  int4 *items = nullptr;    // (tile, p0, p1, split)
+  int nitems = 0;
+  int *split_tiles = nullptr;
+  int nsplit = 0;
+  float2 *dsorted = nullptr;  // measured data [nvalid][C]
+  bool has_data = false;
+};
+
+mrg_status traj_setup(const GridConst &gc, FrameTraj &ft, const float *kx, const float *ky, const float *kz,
+                      const float *kw, int64_t M, int max_pairs, cudaStream_t st);
+void traj_free(FrameTraj &ft);
+// y[s][c] = sum over taps of grid (gridFFT::chop_grid_backward), minus diff[s][c] if given.
+mrg_status launch_ungrid(const GridConst &gc, const FrameTraj &ft, const float2 *grid, const float2 *diff,
+                         float2 *y, cudaStream_t st);
+// grid = scatter of y*kw*taper (gridFFT::chop_grid_forward); every tile written.
+mrg_status launch_grid(const GridConst &gc, const FrameTraj &ft, const float2 *y, float2 *grid, cudaStream_t st);
+// dst[s][c] = src[c*stride + perm[s]], s < nvalid
+mrg_status launch_gather_samples(const FrameTraj &ft, int C, const float2 *src, int64_t stride, float2 *dst,
+                                 cudaStream_t st);
+// dst[c*stride + perm[s]] = s < nvalid ? src[s][c] : 0
+mrg_status launch_scatter_samples(const FrameTraj &ft, int C, const float2 *src, float2 *dst, int64_t stride,
+                                  cudaStream_t st);
+
+// ---------------------------------------------------------------------------
+// Vector kernels (solver.cu)
+// ---------------------------------------------------------------------------
+struct Scalars {
+  double rr, rn, e;
+  double pl[2];
+  float alpha[2], beta[2];
+  float step;
+  int it;
+  int pad;
+};
+mrg_status launch_interleave(const float2 *src, int64_t stride, int C, int64_t n, float2 *dst, cudaStream_t st);
+mrg_status launch_zero(void *p, size_t bytes, cudaStream_t st);
+mrg_status launch_copy(float2 *dst, const float2 *src, int64_t n, cudaStream_t st);
+mrg_status cg_dots(const float2 *R, const float2 *P, const float2 *L, int64_t n, double *part, int nblk,
+                   Scalars *sc, cudaStream_t st);
+mrg_status cg_update(float2 *X, float2 *R, const float2 *P, const float2 *L, int64_t n, double *part, int nblk,
+                     Scalars *sc, double *resid, cudaStream_t st);
+mrg_status cg_pupdate(float2 *P, const float2 *R, int64_t n, const Scalars *sc, cudaStream_t st);
+int reduce_blocks(int64_t n);
+
+// FISTA pieces
+mrg_status launch_fill(float2 *X, int64_t n, float2 v, cudaStream_t st);
+mrg_status energy(const float2 *R, int64_t n, double *part, int nblk, double *out, cudaStream_t st);
+mrg_status power_scale(float2 *X, const float2 *R, int64_t n, Scalars *sc, cudaStream_t st);
+mrg_status fista_momentum(float2 *X, float2 *Xo, int64_t n, const Scalars *sc, int fista, cudaStream_t st);
+mrg_status grad_step(float2 *X, const float2 *R, int64_t n, const Scalars *sc, double *part, int nblk,
+                     double *resid, cudaStream_t st);
+mrg_status bump_iteration(Scalars *sc, cudaStream_t st);
+
+// wavelet.cu
+mrg_status wavelet3d(float2 *X, int nvol, const int N[3], const int L[3], int max_level, const int *shifts_dev,
+                     int wave_type, int inverse, cudaStream_t st);
+void wavelet_levels(const int N[3], const int levels_in[3], int L[3], int *max_level);
+
+// threshold.cu
+struct ThrWork {
+  float *mag = nullptr;
+  unsigned long long *cnt = nullptr;
+  float *state = nullptr;  // value, min_t, max_t, done
+  double *dstate = nullptr;
+  int64_t cap = 0;
+};
+mrg_status thr_alloc(ThrWork &w, int64_t n);
+void thr_free(ThrWork &w);
+// value written to *out_dev (device float), scaled by `scale`
+mrg_status fraction_threshold(const float2 *X, int64_t n, float fraction, float scale, ThrWork &w, float *out_dev,
+                              cudaStream_t st);
+mrg_status soft_threshold(float2 *X, int64_t n, const float *value_dev, cudaStream_t st);
+
+// llr.cu
+struct LlrWork {
+  double *sig = nullptr;
+  float *smax = nullptr;
+  int nb = 0;
+};
+mrg_status llr_alloc(LlrWork &w, int nblocks);
+void llr_free(LlrWork &w);
+mrg_status llr_update(const float2 *X, int Nt, const int N[3], const int bs[3], float amp, float t2,
+                      const int *iter_dev, LlrWork &w, cudaStream_t st);
+mrg_status llr_apply(float2 *X, int Nt, const int N[3], const int bs[3], int block_iter, float alpha,
+                     const int *shifts_dev, const float *smax_dev, cudaStream_t st);
+
+}  // namespace mrg

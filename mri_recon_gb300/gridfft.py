@@ -1,0 +1,274 @@
+"""Python mirror of the reference's gridFFT / RECON call surface over libmrg.
+
+``Plan`` is the coil-batched operator (the reference's gridFFT_CoilThreaded plus
+the CG / FISTA loops of RECON::full_recon).  ``gridFFT`` keeps the per-coil
+member functions and public fields of the reference class
+(src/gridFFT.h:28-194) so code written against it ports line for line:
+
+    g = gridFFT(); g.overgrid = 1.5; g.kernel_type = KAISER_KERNEL
+    g.precalc_gridding(Nz, Ny, Nx)
+    g.forward(X, smap, data, kx, ky, kz, kw)    # X += E^H (data * kw)
+    g.backward(X, smap, data, kx, ky, kz, kw)   # data = E X
+
+Arrays may be torch tensors (CUDA or CPU) or numpy arrays: complex64 images of
+shape (Nz, Ny, Nx), complex64 k-space of M samples, float32 trajectories.
+Device tensors are used in place; host arrays are staged by the library.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+
+TRIANGLE_KERNEL, KAISER_KERNEL, SINC_KERNEL, POLY_KERNEL = 0, 1, 2, 3
+
+try:  # torch is plumbing for device memory and streams
+    import torch
+except Exception:  # pragma: no cover
+    torch = None
+
+
+def _is_tensor(a):
+    return torch is not None and isinstance(a, torch.Tensor)
+
+
+class _Args:
+    """Keeps host arrays alive for the duration of a call and yields raw pointers."""
+
+    def __init__(self):
+        self.keep = []
+
+    def ptr(self, a, dtype=None):
+        if a is None:
+            return None
+        if _is_tensor(a):
+            if not a.is_contiguous():
+                a = a.contiguous()
+                self.keep.append(a)
+            return a.data_ptr()
+        arr = np.ascontiguousarray(a, dtype=dtype) if dtype is not None else np.ascontiguousarray(a)
+        self.keep.append(arr)
+        return arr.ctypes.data
+
+
+def _stream(stream=None):
+    if stream is not None:
+        return stream
+    if torch is not None and torch.cuda.is_available():
+        return torch.cuda.current_stream().cuda_stream
+    return None
+
+
+def _numel(a):
+    return a.numel() if _is_tensor(a) else int(np.asarray(a).size)
+
+
+class Plan:
+    """Coil-batched gridFFT plan with ``ncoils`` coils and ``nframes`` trajectories."""
+
+    def __init__(self, N, ncoils=1, nframes=1, overgrid=1.5, dwin=-1.0, kernel_type=KAISER_KERNEL, k_rad=9999.0,
+                 tile=0, max_pairs=0, time_grid=0):
+        L = _lib.load()
+        if np.isscalar(N):
+            N = (N, N, N)
+        self.N = tuple(int(n) for n in N)  # (Nx, Ny, Nz)
+        self.ncoils, self.nframes = int(ncoils), int(nframes)
+        cfg = _lib.MrgConfig()
+        L.mrg_config_default(ctypes.byref(cfg))
+        cfg.overgrid, cfg.dwin, cfg.kernel_type, cfg.k_rad = overgrid, dwin, kernel_type, k_rad
+        cfg.tile, cfg.max_pairs, cfg.time_grid = tile, max_pairs, time_grid
+        h = ctypes.c_void_p()
+        _lib.check(L.mrg_plan_create(ctypes.byref(cfg), self.N[0], self.N[1], self.N[2], self.ncoils, self.nframes,
+                                     ctypes.byref(h)))
+        self._h = h
+        S = (ctypes.c_int * 3)()
+        og = (ctypes.c_int * 3)()
+        gr = (ctypes.c_float * 3)()
+        be = (ctypes.c_float * 3)()
+        dw = (ctypes.c_float * 3)()
+        ll = ctypes.c_int()
+        _lib.check(L.mrg_plan_info(h, S, og, gr, be, dw, ctypes.byref(ll)))
+        self.S, self.og, self.grid_ratio, self.beta, self.dwin = tuple(S), tuple(og), tuple(gr), tuple(be), tuple(dw)
+        self.lut_len = ll.value
+        self.M = [0] * self.nframes
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.load().mrg_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def ishape(self):
+        return (self.N[2], self.N[1], self.N[0])
+
+    def tables(self):
+        lut = np.zeros(3 * self.lut_len, np.float32)
+        win = np.zeros(sum(self.S), np.float32)
+        _lib.check(_lib.load().mrg_get_tables(self._h, lut.ctypes.data_as(_lib._fp), win.ctypes.data_as(_lib._fp)))
+        s0, s1 = self.S[0], self.S[0] + self.S[1]
+        return lut.reshape(3, self.lut_len), (win[:s0], win[s0:s1], win[s1:])
+
+    # -- inputs ---------------------------------------------------------------
+    def set_smaps(self, smaps, stream=None):
+        """smaps: (C, Nz, Ny, Nx) complex64."""
+        a = _Args()
+        stride = _numel(smaps) // self.ncoils
+        _lib.check(_lib.load().mrg_set_smaps(self._h, a.ptr(smaps, np.complex64), stride, _stream(stream)))
+
+    def set_traj(self, frame, kx, ky, kz, kw, stream=None):
+        a = _Args()
+        M = _numel(kx)
+        _lib.check(_lib.load().mrg_set_traj(self._h, frame, a.ptr(kx, np.float32), a.ptr(ky, np.float32),
+                                            a.ptr(kz, np.float32), a.ptr(kw, np.float32), M, _stream(stream)))
+        self.M[frame] = M
+
+    def set_data(self, frame, data, stream=None):
+        """data: (C, M) complex64."""
+        a = _Args()
+        stride = _numel(data) // self.ncoils
+        _lib.check(_lib.load().mrg_set_data(self._h, frame, a.ptr(data, np.complex64), stride, _stream(stream)))
+
+    # -- operators ------------------------------------------------------------
+    def adjoint(self, frame, data, X, stream=None):
+        """X += sum_c E_c^H (data_c * kw)   (gridFFT::forward).  Returns X."""
+        a = _Args()
+        stride = _numel(data) // self.ncoils
+        if not _is_tensor(X):
+            X = np.ascontiguousarray(X, dtype=np.complex64)
+        _lib.check(_lib.load().mrg_adjoint(self._h, frame, a.ptr(data, np.complex64), stride, a.ptr(X),
+                                           _stream(stream)))
+        return X
+
+    def forward(self, frame, X, out=None, diff=None, stream=None):
+        """data_c = E_c X (- diff_c)   (gridFFT::backward / backward_residual).  Returns (C, M)."""
+        a = _Args()
+        M = self.M[frame]
+        if out is None:
+            if _is_tensor(X) and X.is_cuda:
+                out = torch.empty((self.ncoils, M), dtype=torch.complex64, device=X.device)
+            else:
+                out = np.zeros((self.ncoils, M), np.complex64)
+        _lib.check(_lib.load().mrg_forward(self._h, frame, a.ptr(X, np.complex64), a.ptr(out), M,
+                                           a.ptr(diff, np.complex64), _stream(stream)))
+        return out
+
+    def normal(self, frame, X, out=None, stream=None):
+        a = _Args()
+        if out is None:
+            if _is_tensor(X) and X.is_cuda:
+                out = torch.empty(self.ishape, dtype=torch.complex64, device=X.device)
+            else:
+                out = np.zeros(self.ishape, np.complex64)
+        _lib.check(_lib.load().mrg_normal(self._h, frame, a.ptr(X, np.complex64), a.ptr(out), _stream(stream)))
+        return out
+
+    def adjoint_coil(self, frame, smap, data, X, stream=None):
+        a = _Args()
+        _lib.check(_lib.load().mrg_adjoint_coil(self._h, frame, a.ptr(smap, np.complex64), a.ptr(data, np.complex64),
+                                                a.ptr(X), _stream(stream)))
+        return X
+
+    def forward_coil(self, frame, X, smap, out, diff=None, stream=None):
+        a = _Args()
+        _lib.check(_lib.load().mrg_forward_coil(self._h, frame, a.ptr(X, np.complex64), a.ptr(smap, np.complex64),
+                                                a.ptr(out), a.ptr(diff, np.complex64), _stream(stream)))
+        return out
+
+    # -- solvers --------------------------------------------------------------
+    def cg(self, iters, X=None, use_graph=True, stream=None):
+        """SENSE-CG from x0 = 0.  Returns (X (nframes, Nz, Ny, Nx), residual history)."""
+        a = _Args()
+        if X is None:
+            if torch is not None and torch.cuda.is_available():
+                X = torch.empty((self.nframes,) + self.ishape, dtype=torch.complex64, device="cuda")
+            else:
+                X = np.zeros((self.nframes,) + self.ishape, np.complex64)
+        resid = np.zeros(max(iters, 1), np.float64)
+        _lib.check(_lib.load().mrg_cg(self._h, iters, a.ptr(X), resid.ctypes.data_as(_lib._dp), int(bool(use_graph)),
+                                      _stream(stream)))
+        return X, resid[:iters]
+
+    def fista(self, params, X=None, use_graph=True, stream=None):
+        a = _Args()
+        if X is None:
+            if torch is not None and torch.cuda.is_available():
+                X = torch.empty((self.nframes,) + self.ishape, dtype=torch.complex64, device="cuda")
+            else:
+                X = np.zeros((self.nframes,) + self.ishape, np.complex64)
+        n = max(params.max_iter, 1)
+        resid = np.zeros(n, np.float64)
+        step = ctypes.c_float()
+        _lib.check(_lib.load().mrg_fista(self._h, ctypes.byref(params), a.ptr(X), resid.ctypes.data_as(_lib._dp),
+                                         ctypes.byref(step), int(bool(use_graph)), _stream(stream)))
+        return X, resid[:params.max_iter], step.value
+
+
+def fista_params(**kw):
+    p = _lib.MrgFistaParams()
+    _lib.load().mrg_fista_params_default(ctypes.byref(p))
+    for k, v in kw.items():
+        if k in ("wave_levels", "llr_block"):
+            getattr(p, k)[:] = list(v)
+        else:
+            setattr(p, k, v)
+    return p
+
+
+class gridFFT:
+    """Per-coil drop-in for the reference class gridFFT (src/gridFFT.h:28-194).
+
+    Public fields set before precalc_gridding keep the reference names and
+    defaults (src/gridFFT.cpp:28-60).  The trajectory passed to each call is
+    uploaded and sorted once and re-used while the same arrays are passed.
+    """
+
+    def __init__(self):
+        self.overgrid = 1.5
+        self.kernel_type = KAISER_KERNEL
+        self.dwinX = self.dwinY = self.dwinZ = -1.0
+        self.k_rad = 9999.0
+        self.time_grid = 0
+        self._plan = None
+        self._traj_key = None
+
+    def precalc_gridding(self, Nz, Ny, Nx, data=None):
+        if not (self.dwinX == self.dwinY == self.dwinZ):
+            raise ValueError("anisotropic kernel widths are not supported")
+        self._plan = Plan((Nx, Ny, Nz), 1, 1, overgrid=self.overgrid, dwin=self.dwinX, kernel_type=self.kernel_type,
+                          k_rad=self.k_rad, time_grid=self.time_grid)
+        p = self._plan
+        self.Sx, self.Sy, self.Sz = p.S
+        self.og_sx, self.og_sy, self.og_sz = p.og
+        self.og_ex, self.og_ey, self.og_ez = (p.og[0] + Nx, p.og[1] + Ny, p.og[2] + Nz)
+        self.grid_x, self.grid_y, self.grid_z = p.grid_ratio
+        self.betaX, self.betaY, self.betaZ = p.beta
+        self.dwinX, self.dwinY, self.dwinZ = p.dwin
+        self.Nx, self.Ny, self.Nz = Nx, Ny, Nz
+
+    def _traj(self, kx, ky, kz, kw):
+        key = tuple((id(a), _numel(a)) for a in (kx, ky, kz, kw))
+        if key != self._traj_key:
+            self._plan.set_traj(0, kx, ky, kz, kw)
+            self._traj_key = key
+            self._traj_refs = (kx, ky, kz, kw)
+
+    def forward(self, X, smap, data, kx, ky, kz, kw):
+        """X += E^H data (gridFFT::forward, src/gridFFT.cpp:791-812).  smap may be None."""
+        self._traj(kx, ky, kz, kw)
+        return self._plan.adjoint_coil(0, smap, data, X)
+
+    def backward(self, X, smap, data, kx, ky, kz, kw):
+        """data = E X (gridFFT::backward, src/gridFFT.cpp:824-844)."""
+        self._traj(kx, ky, kz, kw)
+        return self._plan.forward_coil(0, X, smap, data)
+
+    def backward_residual(self, X, smap, data, kx, ky, kz, kw, diff_data):
+        """data = E X - diff_data (gridFFT::backward_residual, src/gridFFT.cpp:856-876)."""
+        self._traj(kx, ky, kz, kw)
+        return self._plan.forward_coil(0, X, smap, data, diff=diff_data)

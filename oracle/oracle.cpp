@@ -1,0 +1,1052 @@
+// ===========================================================================
+// ORACLE -- TEST INFRASTRUCTURE ONLY.
+//
+// CPU restatement of the uwmri/mri_recon gridFFT / recon_lib hot path, used
+// only by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg as
+// the checker.  Nothing in the product (mri_recon_gb300/) links or calls it.
+//
+// Parity unpinned: the reference ships no golden vectors or known-answer tests
+// for this path and cannot be built here (it needs Blitz++ 0.10, FFTW 3.3.6-pl2,
+// Armadillo 9.800.2 and HDF5, none of which are present).  Sub-pieces are pinned
+// against independent implementations instead (numpy.fft for the FFT, the glibc
+// rand() stream, the closed-form Daubechies-4 filters, scipy's I0).
+//
+// Two precisions share one template:
+//   R = float  : mirrors the reference's FP32 arithmetic, including its
+//                float/double promotions (e.g. `(1.0 - dz)` in the tap weights).
+//   R = double : FP64 twin of the same algorithm (same float LUT and windows).
+//
+// Layouts: images are column-major x-fastest (index x + Nx*(y + Ny*z)), i.e. a
+// C-ordered (Nz, Ny, Nx) numpy array.  k-space samples are flat arrays of M.
+// ===========================================================================
+#include <omp.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+template <typename R>
+using cx = std::complex<R>;
+
+static const double kPI = 3.14159265359;  // gridFFT.h:24 (the reference's PI)
+
+enum { K_TRIANGLE = 0, K_KAISER = 1, K_SINC = 2, K_POLY = 3 };  // gridFFT.h:19-22
+
+// ---------------------------------------------------------------------------
+// bessi0: polynomial I0 approximation (Abramowitz & Stegun 9.8.1 / 9.8.2), in
+// the mixed float/double form of gridFFT.cpp:1325-1352.
+// ---------------------------------------------------------------------------
+static float orc_bessi0(float x) {
+  float ax, ans;
+  double y;
+  if ((ax = std::fabs(x)) < 3.75f) {
+    y = x / 3.75;
+    y *= y;
+    ans = (float)(1.0 + y * (3.5156229 + y * (3.0899424 + y * (1.2067492 + y * (0.2659732 + y * (0.360768e-1 + y * 0.45813e-2))))));
+  } else {
+    y = 3.75 / ax;
+    ans = (float)((std::exp((double)ax) / std::sqrt((double)ax)) *
+                  (0.39894228 + y * (0.1328592e-1 + y * (0.225319e-2 + y * (-0.157565e-2 + y * (0.916281e-2 + y * (-0.2057706e-1 + y * (0.2635537e-1 + y * (-0.1647633e-1 + y * 0.392377e-2)))))))));
+  }
+  return ans;
+}
+
+// ---------------------------------------------------------------------------
+// Geometry, kernel LUT and deapodisation windows
+// (gridFFT.cpp:276-473 precalc_kernel, :475-643 precalc_gridding).
+// ---------------------------------------------------------------------------
+struct Geom {
+  int N[3], S[3], og_s[3], og_e[3];
+  float grid[3], dwin[3], grid_mod[3], beta[3];
+  int grid_in[3], fft_in[3];
+  float k_rad;
+  int lut_len;
+  std::vector<float> lut[3];
+  std::vector<float> win[3];
+};
+
+static void build_geom(Geom &g, int Nx, int Ny, int Nz, float overgrid, float dwin_in, int ktype, float k_rad) {
+  g.N[0] = Nx; g.N[1] = Ny; g.N[2] = Nz;
+  g.k_rad = k_rad;
+  for (int d = 0; d < 3; d++) {
+    g.grid_in[d] = 1;  // 3D non-Cartesian (mri_data.cpp:324-325)
+    g.fft_in[d] = 1;
+    // gridFFT.cpp:500-527
+    g.grid[d] = (float)(16.0 * std::ceil((overgrid * (float)g.N[d]) / 16.0) / (float)g.N[d]);
+    g.S[d] = (int)(g.grid[d] * g.N[d]);
+  }
+  // precalc_kernel (gridFFT.cpp:276-473)
+  for (int d = 0; d < 3; d++) {
+    g.grid_mod[d] = 600;
+    float dw = dwin_in;
+    if (dw == -1) dw = (ktype == K_TRIANGLE) ? 1.0f : (ktype == K_POLY ? 2.0f : 2.5f);
+    g.dwin[d] = dw;
+    int glen = (int)((float)dw * (float)g.grid_mod[d]);
+    g.lut_len = glen + 10;
+    std::vector<float> &f = g.lut[d];
+    f.assign(glen + 10, 0.0f);
+    g.beta[d] = 0;
+    if (ktype == K_TRIANGLE) {
+      for (int i = 0; i < glen + 1; i++) f[i] = 1.0f - (float)i / (float)glen;
+    } else if (ktype == K_KAISER) {
+      float a = g.grid[d];  // grid_scale = 1
+      float beta = (float)(kPI * sqrtf((float)((dw * dw) / (a * a) * (a - 0.5) * (a - 0.5) - 0.8)));
+      float bmin = (float)std::sqrt(std::pow(kPI * 2 * dw / a, 2.0) - 9.6752);
+      beta = (bmin > beta) ? bmin : beta;
+      g.beta[d] = beta;
+      for (int i = 0; i < glen + 1; i++) {
+        float pos = ((float)i) / ((float)glen);
+        float arg = sqrtf((float)(1.0 - pos * pos));
+        f[i] = orc_bessi0(beta * arg) / orc_bessi0(beta);
+      }
+    } else if (ktype == K_SINC) {
+      for (int i = 0; i < glen + 1; i++) {
+        float pos = ((float)i * (float)dw) / ((float)glen);
+        f[i] = (pos < 0.01f) ? 1.0f : (float)(std::sin(pos * kPI) / (pos * kPI));
+        f[i] *= (float)(0.54 + 0.46 * std::cos(kPI * (float)i / ((float)glen)));
+      }
+    } else {  // polynomial table (gridFFT.cpp:248-269), filled over the whole length
+      int len = glen + 10;
+      for (int i = 0; i < len; i++) {
+        double x = double(i) / double(len), x2 = x * x, x3 = x * x2, x4 = x2 * x2, x5 = x * x4;
+        f[i] = (float)(1. + 0.04522831 * x - 3.36020304 * x2 + 1.12417012 * x3 + 2.82448025 * x4 - 1.63447764 * x5);
+      }
+    }
+    double s = 0;
+    for (float v : f) s += v;
+    double scale = 0.5 * g.grid_mod[d] / s;
+    for (float &v : f) v = (float)(v * scale);
+  }
+  // crop (gridFFT.cpp:536-541)
+  for (int d = 0; d < 3; d++) {
+    g.og_s[d] = (int)((float)g.N[d] * (g.grid[d] - 1) / 2.0);
+    g.og_e[d] = g.og_s[d] + g.N[d];
+  }
+  // deapodisation windows with chop and crop (gridFFT.cpp:550-631)
+  for (int d = 0; d < 3; d++) {
+    int S = g.S[d];
+    std::vector<float> &w = g.win[d];
+    w.assign(S, 0.0f);
+    for (int i = 0; i < S; i++) {
+      float ipos = i - (float)S / 2.0f;
+      for (int gp = 0; gp < g.dwin[d] * g.grid_mod[d]; gp++) {
+        w[i] = (float)(w[i] + 2 * std::cos(2 * kPI * ipos * gp / (float)g.grid_mod[d] / (float)S) * g.lut[d][gp]);
+      }
+      w[i] = (float)g.grid_mod[d] / w[i];
+      float fact = (float)(2 * (i % 2) - 1);
+      w[i] *= fact / S;
+      w[i] = (float)(w[i] * ((i < g.og_s[d]) ? 0.0 : 1.0));
+      w[i] = (float)(w[i] * ((i > g.og_e[d] - 1) ? 0.0 : 1.0));
+    }
+    float mx = w[0];
+    for (float v : w) mx = std::max(mx, v);
+    for (float &v : w) v /= mx;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Mixed-radix FFT (recursive decimation in time), any length.  Replaces the
+// reference's FFTW 1D plans (ArrayTemplates.cpp:298-309).  sign = -1 is
+// FFTW_FORWARD, +1 is FFTW_BACKWARD; unscaled.
+// ---------------------------------------------------------------------------
+template <typename R>
+struct FFT1 {
+  int n;
+  std::vector<int> fac;
+  std::vector<cx<R>> tw;  // exp(sign*2*pi*i*k/n)
+  explicit FFT1(int n_, int sign) : n(n_) {
+    int m = n;
+    for (int p : {4, 2, 3, 5, 7}) while (m % p == 0) { fac.push_back(p); m /= p; }
+    for (int p = 11; m > 1; p += 2) while (m % p == 0) { fac.push_back(p); m /= p; }
+    tw.resize(n);
+    for (int k = 0; k < n; k++) {
+      double a = sign * 2.0 * M_PI * (double)k / (double)n;
+      tw[k] = cx<R>((R)std::cos(a), (R)std::sin(a));
+    }
+  }
+  void rec(const cx<R> *in, long is, cx<R> *out, int len, int fi, long ts) const {
+    if (len == 1) { out[0] = in[0]; return; }
+    int p = fac[fi], m = len / p;
+    for (int r = 0; r < p; r++) rec(in + r * is, is * p, out + r * m, m, fi + 1, ts * p);
+    cx<R> t[64];
+    std::vector<cx<R>> tv;
+    cx<R> *tp = t;
+    if (p > 64) { tv.resize(p); tp = tv.data(); }
+    for (int k = 0; k < m; k++) {
+      for (int r = 0; r < p; r++) tp[r] = out[r * m + k] * tw[(long)r * k * ts % n];
+      for (int q = 0; q < p; q++) {
+        cx<R> acc(0, 0);
+        for (int r = 0; r < p; r++) acc += tp[r] * tw[(long)r * q * m * ts % n];
+        out[k + m * q] = acc;
+      }
+    }
+  }
+  void run(cx<R> *data, cx<R> *work) const {
+    std::memcpy(work, data, sizeof(cx<R>) * n);
+    rec(work, 1, data, n, 0, 1);
+  }
+};
+
+// fft3 along one axis of a sub-box of an array with dims (D0,D1,D2), column-major,
+// per-axis scale 1/sqrt(N) in float (ArrayTemplates.cpp:276-427, chop = 0).
+// The sub-box is [lo0,hi0) x [lo1,hi1) x [lo2,hi2).
+template <typename R>
+static void fft3_axis(cx<R> *a, const int D[3], int axis, int sign, const int lo[3], const int hi[3]) {
+  int N = D[axis];
+  FFT1<R> plan(N, sign);
+  R scale = (sizeof(R) == 4) ? (R)(1. / std::sqrt((float)N)) : (R)(1.0 / std::sqrt((double)N));
+  long st[3] = {1, (long)D[0], (long)D[0] * D[1]};
+  int o1 = (axis == 0) ? 1 : 0, o2 = (axis == 2) ? 1 : 2;
+  if (axis == 1) { o1 = 0; o2 = 2; }
+#pragma omp parallel
+  {
+    std::vector<cx<R>> buf(N), work(N);
+#pragma omp for collapse(2) schedule(static)
+    for (int b = lo[o2]; b < hi[o2]; b++) {
+      for (int c = lo[o1]; c < hi[o1]; c++) {
+        cx<R> *base = a + (long)b * st[o2] + (long)c * st[o1];
+        for (int i = 0; i < N; i++) buf[i] = base[(long)i * st[axis]];
+        plan.run(buf.data(), work.data());
+        for (int i = 0; i < N; i++) base[(long)i * st[axis]] = buf[i] * scale;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Operator (one coil), gridFFT.cpp:645-1322.
+// ---------------------------------------------------------------------------
+template <typename R>
+struct OPlan {
+  Geom g;
+  std::vector<cx<R>> grid;  // k3d_grid, S0*S1*S2
+  long gsize() const { return (long)g.S[0] * g.S[1] * g.S[2]; }
+  long isize() const { return (long)g.N[0] * g.N[1] * g.N[2]; }
+
+  // do_fft (gridFFT.cpp:645-671): pruned FFTW_FORWARD, z then y then x.
+  void do_fft() {
+    int lo[3] = {0, 0, 0}, hi[3] = {g.S[0], g.S[1], g.S[2]};
+    int l1[3] = {g.og_s[0], g.og_s[1], 0}, h1[3] = {g.og_e[0] + 1, g.og_e[1] + 1, g.S[2]};
+    fft3_axis<R>(grid.data(), g.S, 2, -1, l1, h1);
+    int l2[3] = {g.og_s[0], 0, 0}, h2[3] = {g.og_e[0] + 1, g.S[1], g.S[2]};
+    fft3_axis<R>(grid.data(), g.S, 1, -1, l2, h2);
+    fft3_axis<R>(grid.data(), g.S, 0, -1, lo, hi);
+  }
+  // do_ifft (gridFFT.cpp:673-711): full FFTW_BACKWARD, x then y then z.
+  void do_ifft() {
+    int lo[3] = {0, 0, 0}, hi[3] = {g.S[0], g.S[1], g.S[2]};
+    fft3_axis<R>(grid.data(), g.S, 0, +1, lo, hi);
+    fft3_axis<R>(grid.data(), g.S, 1, +1, lo, hi);
+    fft3_axis<R>(grid.data(), g.S, 2, +1, lo, hi);
+  }
+
+  // Tap weight along one axis before rounding: LUT linear interpolation in the
+  // reference's float/double mix (gridFFT.cpp:1113-1116); the caller applies
+  // the running product and the chop sign and rounds once, as the reference.
+  inline double tap_raw(int d, R del) const {
+    const std::vector<float> &f = g.lut[d];
+    if (sizeof(R) == 4) {
+      float delf = (float)del;
+      float dd = delf - (float)((int)delf);
+      return f[(int)delf] * (1.0 - dd) + f[(int)delf + 1] * dd;
+    } else {
+      int i0 = (int)del;
+      double dd = (double)del - (double)i0;
+      return (double)f[i0] * (1.0 - dd) + (double)f[i0 + 1] * dd;
+    }
+  }
+
+  // Per-sample tap range along one axis (gridFFT.cpp:1059-1098): returns
+  // false when the sample is outside the grid.
+  inline bool tap_range(int d, float k, R &dk, int &s, int &e) const {
+    float c = (float)(g.S[d] / 2);
+    if (sizeof(R) == 4) {
+      float dkf = k * g.grid[d] + c;
+      dk = dkf;
+      s = std::max((int)std::ceil(dkf - g.dwin[d]), 0);
+      e = std::min((int)std::floor(dkf + g.dwin[d]), g.S[d] - 1);
+    } else {
+      dk = (R)k * (R)g.grid[d] + (R)c;
+      s = std::max((int)std::ceil(dk - (R)g.dwin[d]), 0);
+      e = std::min((int)std::floor(dk + (R)g.dwin[d]), g.S[d] - 1);
+    }
+    return !(s >= g.S[d] || e < 0);
+  }
+
+  // chop_grid_forward (gridFFT.cpp:1009-1164): scatter data*kw*taper.
+  void grid_forward(const cx<R> *data, const float *kx, const float *ky, const float *kz, const float *kw, long M) {
+    const int Sx = g.S[0], Sy = g.S[1];
+    R *gp = reinterpret_cast<R *>(grid.data());
+#pragma omp parallel for schedule(dynamic, 4096)
+    for (long i = 0; i < M; i++) {
+      float kwv = kw[i];
+      if (kwv == 0) continue;
+      cx<R> temp = data[i];
+      temp *= (R)kwv;
+      if (temp == cx<R>(0, 0)) continue;
+      R dk[3];
+      int s[3], e[3];
+      float kk[3] = {kx[i], ky[i], kz[i]};
+      bool ok = true;
+      for (int d = 0; d < 3; d++) ok = ok && tap_range(d, kk[d], dk[d], s[d], e[d]);
+      if (!ok) continue;
+      if (sizeof(R) == 4) {
+        float kr = kk[0] * kk[0] + kk[1] * kk[1] + kk[2] * kk[2];
+        temp *= (R)(float)std::exp(-kr / (2.0 * g.k_rad * g.k_rad));
+      } else {
+        R kr = (R)kk[0] * kk[0] + (R)kk[1] * kk[1] + (R)kk[2] * kk[2];
+        temp *= (R)std::exp(-kr / (2.0 * (double)g.k_rad * (double)g.k_rad));
+      }
+      for (int lz = s[2]; lz <= e[2]; lz++) {
+        R wtz = (R)tap_raw(2, std::fabs((R)g.grid_mod[2] * (dk[2] - (R)lz)));
+        wtz *= (R)(2 * (lz % 2) - 1);
+        for (int ly = s[1]; ly <= e[1]; ly++) {
+          R wty = (R)(wtz * tap_raw(1, std::fabs((R)g.grid_mod[1] * (dk[1] - (R)ly))));
+          wty *= (R)(2 * (ly % 2) - 1);
+          for (int lx = s[0]; lx <= e[0]; lx++) {
+            R wtx = (R)(wty * tap_raw(0, std::fabs((R)g.grid_mod[0] * (dk[0] - (R)lx))));
+            wtx *= (R)(2 * (lx % 2) - 1);
+            cx<R> t2 = wtx * temp;
+            long idx = 2 * ((long)lx + (long)Sx * (ly + (long)Sy * lz));
+#pragma omp atomic
+            gp[idx] += t2.real();
+#pragma omp atomic
+            gp[idx + 1] += t2.imag();
+          }
+        }
+      }
+    }
+  }
+
+  // chop_grid_backward (gridFFT.cpp:1166-1322): gather, optional residual.
+  void grid_backward(cx<R> *data, const float *kx, const float *ky, const float *kz, const float *kw, long M,
+                     const cx<R> *diff) const {
+    const int Sx = g.S[0], Sy = g.S[1];
+#pragma omp parallel for schedule(dynamic, 4096)
+    for (long i = 0; i < M; i++) {
+      if (kw[i] == 0) { data[i] = 0; continue; }
+      R dk[3];
+      int s[3], e[3];
+      float kk[3] = {kx[i], ky[i], kz[i]};
+      bool ok = true;
+      for (int d = 0; d < 3 && ok; d++) ok = tap_range(d, kk[d], dk[d], s[d], e[d]);
+      if (!ok) { data[i] = 0; continue; }
+      cx<R> temp(0, 0);
+      for (int lz = s[2]; lz <= e[2]; lz++) {
+        R wtz = (R)tap_raw(2, std::fabs((R)g.grid_mod[2] * (dk[2] - (R)lz)));
+        wtz *= (R)(2 * (lz % 2) - 1);
+        for (int ly = s[1]; ly <= e[1]; ly++) {
+          R wty = (R)(wtz * tap_raw(1, std::fabs((R)g.grid_mod[1] * (dk[1] - (R)ly))));
+          wty *= (R)(2 * (ly % 2) - 1);
+          for (int lx = s[0]; lx <= e[0]; lx++) {
+            R wtx = (R)(wty * tap_raw(0, std::fabs((R)g.grid_mod[0] * (dk[0] - (R)lx))));
+            wtx *= (R)(2 * (lx % 2) - 1);
+            temp += wtx * grid[(long)lx + (long)Sx * (ly + (long)Sy * lz)];
+          }
+        }
+      }
+      data[i] = diff ? temp - diff[i] : temp;
+    }
+  }
+
+  // set_image (gridFFT.cpp:972-1002) into a zeroed grid.
+  void set_image(const cx<R> *X, const cx<R> *smap) {
+    std::fill(grid.begin(), grid.end(), cx<R>(0, 0));
+    const int Nx = g.N[0], Ny = g.N[1], Nz = g.N[2];
+#pragma omp parallel for
+    for (int k = 0; k < Nz; k++) {
+      R wtz = g.win[2][k + g.og_s[2]];
+      for (int j = 0; j < Ny; j++) {
+        R wty = wtz * (R)g.win[1][j + g.og_s[1]];
+        for (int i = 0; i < Nx; i++) {
+          R wt = wty * (R)g.win[0][i + g.og_s[0]];
+          long ii = i + (long)Nx * (j + (long)Ny * k);
+          cx<R> v = wt * X[ii];
+          if (smap) v = v * smap[ii];
+          grid[(i + g.og_s[0]) + (long)g.S[0] * ((j + g.og_s[1]) + (long)g.S[1] * (k + g.og_s[2]))] = v;
+        }
+      }
+    }
+  }
+
+  // accumulate (gridFFT.cpp:926-956): X += win * image * conj(smap).
+  void accumulate(cx<R> *X, const cx<R> *smap) const {
+    const int Nx = g.N[0], Ny = g.N[1], Nz = g.N[2];
+#pragma omp parallel for
+    for (int k = 0; k < Nz; k++) {
+      R wtz = g.win[2][k + g.og_s[2]];
+      for (int j = 0; j < Ny; j++) {
+        R wty = wtz * (R)g.win[1][j + g.og_s[1]];
+        for (int i = 0; i < Nx; i++) {
+          R wt = wty * (R)g.win[0][i + g.og_s[0]];
+          long ii = i + (long)Nx * (j + (long)Ny * k);
+          cx<R> im = grid[(i + g.og_s[0]) + (long)g.S[0] * ((j + g.og_s[1]) + (long)g.S[1] * (k + g.og_s[2]))];
+          X[ii] += smap ? wt * im * std::conj(smap[ii]) : wt * im;
+        }
+      }
+    }
+  }
+
+  // gridFFT::forward (E^H, gridFFT.cpp:791-812)
+  void adjoint(cx<R> *X, const cx<R> *smap, const cx<R> *data, const float *kx, const float *ky, const float *kz,
+               const float *kw, long M) {
+    std::fill(grid.begin(), grid.end(), cx<R>(0, 0));
+    grid_forward(data, kx, ky, kz, kw, M);
+    do_ifft();
+    accumulate(X, smap);
+  }
+  // gridFFT::backward / backward_residual (E, gridFFT.cpp:824-876)
+  void forward(const cx<R> *X, const cx<R> *smap, cx<R> *data, const float *kx, const float *ky, const float *kz,
+               const float *kw, long M, const cx<R> *diff) {
+    set_image(X, smap);
+    do_fft();
+    grid_backward(data, kx, ky, kz, kw, M, diff);
+  }
+};
+
+// ---------------------------------------------------------------------------
+// glibc random() TYPE_3 stream for the default seed (the additive lagged
+// Fibonacci generator r[i] = r[i-3] + r[i-31], output r >> 1, seeded by the
+// Park-Miller LCG).  The reference draws its wavelet and block shifts from
+// rand() without calling srand (wavelet3D.cpp:443-448, clear.cpp:408-410).
+// ---------------------------------------------------------------------------
+struct GRand {
+  uint32_t r[34];
+  int pos;
+  explicit GRand(uint32_t seed = 1) {
+    int32_t s[34];
+    s[0] = (int32_t)seed;
+    for (int i = 1; i < 31; i++) {
+      int64_t v = (16807LL * s[i - 1]) % 2147483647LL;
+      if (v < 0) v += 2147483647LL;
+      s[i] = (int32_t)v;
+    }
+    for (int i = 31; i < 34; i++) s[i] = s[i - 31];
+    for (int i = 0; i < 34; i++) r[i] = (uint32_t)s[i];
+    pos = 34;
+    for (int i = 34; i < 344; i++) step();
+  }
+  uint32_t step() {
+    uint32_t v = r[(pos - 31) % 34] + r[(pos - 3) % 34];
+    r[pos % 34] = v;
+    pos++;
+    if (pos >= 34 * 1000000) pos = 34 + (pos % 34);
+    return v;
+  }
+  int next() { return (int)(step() >> 1); }
+};
+
+// ---------------------------------------------------------------------------
+// 3D wavelet (wavelet3D.cpp:563-791): separable periodic DWT with shifts.
+// ---------------------------------------------------------------------------
+struct Wave {
+  int N[3], L[3], S[3], max_level, wN;
+  float lpf[4], hpf[4], Slpf[4], Shpf[4];
+  Wave(int nx, int ny, int nz, const int lev[3], int type) {
+    N[0] = nx; N[1] = ny; N[2] = nz;
+    for (int d = 0; d < 3; d++) { L[d] = lev[d]; S[d] = 0; }
+    if (type == 0) {  // DB2 (Haar), wavelet3D.cpp:122-140
+      wN = 2;
+      float h = (float)(1.0 / std::sqrt(2.0));
+      lpf[0] = h; lpf[1] = h; hpf[0] = -h; hpf[1] = h;
+      Slpf[0] = h; Slpf[1] = h; Shpf[0] = h; Shpf[1] = -h;
+    } else {  // DB4 closed form; arrangement as wavelet3D.cpp:168-186
+      wN = 4;
+      double s3 = std::sqrt(3.0), d = 4.0 * std::sqrt(2.0);
+      double h0 = (1 + s3) / d, h1 = (3 + s3) / d, h2 = (3 - s3) / d, h3 = (1 - s3) / d;
+      lpf[0] = (float)h3; lpf[1] = (float)h2; lpf[2] = (float)h1; lpf[3] = (float)h0;
+      hpf[0] = (float)-h0; hpf[1] = (float)h1; hpf[2] = (float)-h2; hpf[3] = (float)h3;
+      Slpf[0] = (float)h0; Slpf[1] = (float)h1; Slpf[2] = (float)h2; Slpf[3] = (float)h3;
+      Shpf[0] = (float)h3; Shpf[1] = (float)-h2; Shpf[2] = (float)h1; Shpf[3] = (float)-h0;
+    }
+    // setup_wavelet_directions (wavelet3D.cpp:99-110)
+    max_level = 0;
+    for (int dd = 0; dd < 3; dd++) {
+      while (std::floor(N[dd] / std::pow(2.0, L[dd])) != (N[dd] / std::pow(2.0, L[dd]))) L[dd]--;
+      max_level = std::max(max_level, L[dd]);
+    }
+  }
+  template <typename R>
+  void w1d(const cx<R> *in, cx<R> *out, int pts, int dir) const {
+    for (int p = 0; p < pts / 2; p++) {
+      cx<R> a(0, 0), b(0, 0);
+      for (int f = 0; f < wN; f++) {
+        int c = ((2 * p - f + S[dir]) + pts) % pts;
+        a += (R)lpf[f] * in[c];
+        b += (R)hpf[f] * in[c];
+      }
+      out[p] = a;
+      out[p + pts / 2] = b;
+    }
+  }
+  template <typename R>
+  void iw1d(const cx<R> *in, cx<R> *out, int pts, int dir) const {
+    for (int p = 0; p < pts; p++) out[p] = 0;
+    for (int p = 0; p < pts / 2; p++)
+      for (int f = 0; f < wN; f++) {
+        int c = ((2 * p + f - wN + 1 + S[dir]) + pts) % pts;
+        out[c] += in[p] * (R)Slpf[f];
+        out[c] += in[p + pts / 2] * (R)Shpf[f];
+      }
+  }
+  template <typename R>
+  void axis(cx<R> *X, int Lz, int Ly, int Lx, int ax, int inv) const {
+    long sx = 1, sy = N[0], sz = (long)N[0] * N[1];
+    int Ls[3] = {Lx, Ly, Lz};
+    long st[3] = {sx, sy, sz};
+    int n = Ls[ax];
+    int a1 = (ax == 0) ? 1 : 0, a2 = (ax == 2) ? 1 : 2;
+#pragma omp parallel
+    {
+      std::vector<cx<R>> b1(n), b2(n);
+#pragma omp for collapse(2)
+      for (int q = 0; q < Ls[a2]; q++)
+        for (int p = 0; p < Ls[a1]; p++) {
+          cx<R> *base = X + q * st[a2] + p * st[a1];
+          for (int i = 0; i < n; i++) b1[i] = base[i * st[ax]];
+          if (inv) iw1d(b1.data(), b2.data(), n, ax); else w1d(b1.data(), b2.data(), n, ax);
+          for (int i = 0; i < n; i++) base[i * st[ax]] = b2[i];
+        }
+    }
+  }
+  template <typename R>
+  void forward(cx<R> *X) const {
+    int sz = N[2], sy = N[1], sx = N[0];
+    for (int l = 0; l < max_level; l++) {
+      if (l < L[0]) axis(X, sz, sy, sx, 0, 0);
+      if (l < L[1]) axis(X, sz, sy, sx, 1, 0);
+      if (l < L[2]) axis(X, sz, sy, sx, 2, 0);
+      if (l < L[2]) sz = N[2] / (int)std::pow(2.0, l + 1);
+      if (l < L[1]) sy = N[1] / (int)std::pow(2.0, l + 1);
+      if (l < L[0]) sx = N[0] / (int)std::pow(2.0, l + 1);
+    }
+  }
+  template <typename R>
+  void backward(cx<R> *X) const {
+    int sz = N[2] / (int)std::pow(2.0, L[2]), sy = N[1] / (int)std::pow(2.0, L[1]), sx = N[0] / (int)std::pow(2.0, L[0]);
+    for (int l = max_level - 1; l >= 0; l--) {
+      if (l < L[2]) sz = N[2] / (int)std::pow(2.0, l);
+      if (l < L[1]) sy = N[1] / (int)std::pow(2.0, l);
+      if (l < L[0]) sx = N[0] / (int)std::pow(2.0, l);
+      if (l < L[2]) axis(X, sz, sy, sx, 2, 1);
+      if (l < L[1]) axis(X, sz, sy, sx, 1, 1);
+      if (l < L[0]) axis(X, sz, sy, sx, 0, 1);
+    }
+  }
+  void random_shift(GRand &rng) {
+    for (int d = 0; d < 3; d++) S[d] = rng.next() % wN;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Fraction threshold (threshold.cpp:251-391, group_complex = true) and soft
+// thresholding (threshold.cpp:766-814).
+// ---------------------------------------------------------------------------
+template <typename R>
+static float get_threshold(cx<R> **vols, int nvol, long nvox, float fraction, double thresh_member) {
+  float mx = 0, mn = (float)std::abs(vols[0][0]);
+  for (int v = 0; v < nvol; v++)
+    for (long i = 0; i < nvox; i++) {
+      float a = (float)std::abs(vols[v][i]);
+      mx = std::max(mx, a);
+      mn = std::min(mn, a);
+    }
+  long total = (long)nvol * nvox;
+  long found = total;
+  long target = (long)(fraction * (double)total);
+  long acc = (long)(0.001 * (double)total);
+  if (target < 2) return 0.0f;
+  float value = (float)(0.5 * (mx - mn));
+  float max_t = (float)(thresh_member * mx);
+  float min_t = mn;
+  int iter = 0;
+  while ((std::labs(found - target) > acc) && (iter < 64)) {
+    if (iter > 0) {
+      if (found > target) max_t = value; else min_t = value;
+      value = (float)(0.5 * (max_t + min_t));
+    }
+    iter++;
+    found = 0;
+    for (int v = 0; v < nvol; v++) {
+      long c = 0;
+#pragma omp parallel for reduction(+ : c)
+      for (long i = 0; i < nvox; i++) c += ((float)std::abs(vols[v][i]) < value) ? 1 : 0;
+      found += c;
+    }
+  }
+  return value;
+}
+
+template <typename R>
+static void soft_threshold(cx<R> *X, long n, float value) {
+#pragma omp parallel for
+  for (long i = 0; i < n; i++) {
+    float cc = (float)std::abs(X[i]);
+    if (cc <= value) X[i] = 0;
+    else X[i] *= (R)(1.0f - value / cc);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Locally low rank in time (clear.cpp:233-556, dim = 0, Ne = 1).  SVD by
+// one-sided Jacobi in double (the reference uses Armadillo's LAPACK SVD in
+// complex<double>; singular values and the thresholded reconstruction are
+// unique).
+// ---------------------------------------------------------------------------
+static void jacobi_svd(std::vector<cx<double>> &A, int m, int n, std::vector<double> &s, std::vector<cx<double>> &V) {
+  // A is m x n column-major; on exit A = U*diag(s), V is n x n column-major.
+  V.assign((size_t)n * n, 0);
+  for (int i = 0; i < n; i++) V[i + (size_t)n * i] = 1;
+  for (int sweep = 0; sweep < 60; sweep++) {
+    double off = 0;
+    for (int p = 0; p < n - 1; p++)
+      for (int q = p + 1; q < n; q++) {
+        double a = 0, b = 0;
+        cx<double> c(0, 0);
+        for (int i = 0; i < m; i++) {
+          cx<double> x = A[i + (size_t)m * p], y = A[i + (size_t)m * q];
+          a += std::norm(x);
+          b += std::norm(y);
+          c += std::conj(x) * y;
+        }
+        double ac = std::abs(c);
+        if (a == 0 || b == 0 || ac == 0) continue;
+        double rel = ac / std::sqrt(a * b);
+        off = std::max(off, rel);
+        if (rel < 1e-14) continue;
+        cx<double> ph = c / ac;  // rotate in the complex plane, then a real Jacobi rotation
+        double zeta = (b - a) / (2 * ac);
+        double t = (zeta >= 0 ? 1.0 : -1.0) / (std::fabs(zeta) + std::sqrt(1 + zeta * zeta));
+        double cs = 1 / std::sqrt(1 + t * t), sn = cs * t;
+        for (int i = 0; i < m; i++) {
+          cx<double> x = A[i + (size_t)m * p], y = A[i + (size_t)m * q] * std::conj(ph);
+          A[i + (size_t)m * p] = cs * x - sn * y;
+          A[i + (size_t)m * q] = (sn * x + cs * y) * ph;
+        }
+        for (int i = 0; i < n; i++) {
+          cx<double> x = V[i + (size_t)n * p], y = V[i + (size_t)n * q] * std::conj(ph);
+          V[i + (size_t)n * p] = cs * x - sn * y;
+          V[i + (size_t)n * q] = (sn * x + cs * y) * ph;
+        }
+      }
+    if (off < 1e-14) break;
+  }
+  s.assign(n, 0);
+  for (int j = 0; j < n; j++) {
+    double a = 0;
+    for (int i = 0; i < m; i++) a += std::norm(A[i + (size_t)m * j]);
+    s[j] = std::sqrt(a);
+  }
+}
+
+struct LLRParams {
+  int bs[3];
+  int block_iter;
+  float alpha;
+  float clear_amp, clear_t2;
+};
+
+template <typename R>
+static float llr_update_threshold(cx<R> **X, int Nt, const int N[3], LLRParams &p, int iter) {
+  for (int d = 0; d < 3; d++) p.bs[d] = std::min(p.bs[d], N[d]);
+  int B[3] = {N[0] / p.bs[0], N[1] / p.bs[1], N[2] / p.bs[2]};
+  int nb = B[0] * B[1] * B[2];
+  int Np = p.bs[0] * p.bs[1] * p.bs[2];
+  std::vector<double> sb(nb);
+#pragma omp parallel for schedule(dynamic)
+  for (int b = 0; b < nb; b++) {
+    int bi = b / (B[1] * B[2]), bj = (b / B[2]) % B[1], bk = b % B[2];
+    int i0 = bi * p.bs[0], j0 = bj * p.bs[1], k0 = bk * p.bs[2];
+    std::vector<cx<double>> A((size_t)Np * Nt), V;
+    std::vector<double> s;
+    for (int t = 0; t < Nt; t++) {
+      int c = 0;
+      for (int kk = k0; kk < k0 + p.bs[2]; kk++)
+        for (int jj = j0; jj < j0 + p.bs[1]; jj++)
+          for (int ii = i0; ii < i0 + p.bs[0]; ii++)
+            A[c++ + (size_t)Np * t] = cx<double>(X[t][ii + (long)N[0] * (jj + (long)N[1] * kk)]);
+    }
+    jacobi_svd(A, Np, Nt, s, V);
+    sb[b] = *std::max_element(s.begin(), s.end());
+  }
+  float amp = 1 + p.clear_amp * std::exp(-((float)iter) / p.clear_t2);
+  std::vector<double> nz;
+  for (double v : sb) if (v != 0) nz.push_back(v);
+  std::sort(nz.begin(), nz.end());
+  double med = 0;
+  if (!nz.empty()) {
+    size_t h = nz.size() / 2;
+    med = (nz.size() % 2) ? nz[h] : 0.5 * (nz[h - 1] + nz[h]);
+  }
+  return (float)(med * amp);
+}
+
+template <typename R>
+static void llr_thresh(cx<R> **X, int Nt, const int N[3], const LLRParams &p, float smax, GRand &rng) {
+  int B[3] = {N[0] / p.bs[0], N[1] / p.bs[1], N[2] / p.bs[2]};
+  int nb = B[0] * B[1] * B[2];
+  int Np = p.bs[0] * p.bs[1] * p.bs[2];
+  double clear_alpha = p.alpha;
+  if (clear_alpha == 0.0) return;
+  clear_alpha *= smax;
+  for (int it = 0; it < p.block_iter; it++) {
+    int sh[3];
+    for (int d = 0; d < 3; d++) sh[d] = rng.next() % p.bs[d] - p.bs[d] / 2;
+    if (p.block_iter == 1) sh[0] = sh[1] = sh[2] = 0;
+#pragma omp parallel for schedule(dynamic)
+    for (int b = 0; b < nb; b++) {
+      int bi = b / (B[1] * B[2]), bj = (b / B[2]) % B[1], bk = b % B[2];
+      int i0 = bi * p.bs[0] + sh[0], j0 = bj * p.bs[1] + sh[1], k0 = bk * p.bs[2] + sh[2];
+      std::vector<cx<double>> A((size_t)Np * Nt), A0, V;
+      std::vector<double> s;
+      std::vector<long> idx(Np);
+      int c = 0;
+      for (int kk = k0; kk < k0 + p.bs[2]; kk++)
+        for (int jj = j0; jj < j0 + p.bs[1]; jj++)
+          for (int ii = i0; ii < i0 + p.bs[0]; ii++) {
+            int px = (ii + N[0]) % N[0], py = (jj + N[1]) % N[1], pz = (kk + N[2]) % N[2];
+            idx[c++] = px + (long)N[0] * (py + (long)N[1] * pz);
+          }
+      for (int t = 0; t < Nt; t++)
+        for (int i = 0; i < Np; i++) A[i + (size_t)Np * t] = cx<double>(X[t][idx[i]]);
+      jacobi_svd(A, Np, Nt, s, V);
+      // X = U diag(s') V^H with U*diag(s) = A (rotated)
+      std::vector<double> f(Nt);
+      for (int j = 0; j < Nt; j++) {
+        double sp = std::max(s[j] - clear_alpha / p.block_iter, 0.0);
+        f[j] = (s[j] > 0) ? sp / s[j] : 0.0;
+      }
+      for (int i = 0; i < Np; i++)
+        for (int t = 0; t < Nt; t++) {
+          cx<double> acc(0, 0);
+          for (int j = 0; j < Nt; j++) acc += A[i + (size_t)Np * j] * f[j] * std::conj(V[t + (size_t)Nt * j]);
+          X[t][idx[i]] = cx<R>((R)acc.real(), (R)acc.imag());
+        }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// C ABI for ctypes (tests / bench baseline leg).
+// ---------------------------------------------------------------------------
+struct OHandle {
+  int prec;  // 0 float, 1 double
+  OPlan<float> pf;
+  OPlan<double> pd;
+  Geom &g() { return prec ? pd.g : pf.g; }
+};
+
+template <typename R>
+static OPlan<R> &P(OHandle *h);
+template <>
+OPlan<float> &P<float>(OHandle *h) { return h->pf; }
+template <>
+OPlan<double> &P<double>(OHandle *h) { return h->pd; }
+
+struct OFrames {
+  int Nt, C;
+  const float **kx, **ky, **kz, **kw;
+  const long *M;
+  const void **data;   // [t*C + c]
+  const void **smaps;  // [c]
+};
+
+struct OFistaParams {
+  int max_iter;
+  int max_eig_iter;
+  int cycle_spins;
+  int wave_levels[3];
+  int wave_type;       // 0 DB2, 1 DB4
+  float thresh;        // fraction (-thresh)
+  int use_threshold;   // fraction thresholding on/off
+  int llr_bs[3];
+  int llr_block_iter;
+  float llr_alpha;     // clear_alpha_time (0 = off)
+  float clear_amp, clear_t2;
+  long rand_skip;      // rand() draws consumed before the first shift
+};
+
+template <typename R>
+static void normal_op(OHandle *h, const OFrames &F, int t, const cx<R> *X, cx<R> *out, std::vector<cx<R>> &tmp,
+                      bool residual) {
+  OPlan<R> &p = P<R>(h);
+  long M = F.M[t];
+  tmp.resize(M);
+  for (int c = 0; c < F.C; c++) {
+    const cx<R> *sm = (const cx<R> *)F.smaps[c];
+    const cx<R> *d = (const cx<R> *)F.data[t * F.C + c];
+    p.forward(X, sm, tmp.data(), F.kx[t], F.ky[t], F.kz[t], F.kw[t], M, residual ? d : nullptr);
+    p.adjoint(out, sm, tmp.data(), F.kx[t], F.ky[t], F.kz[t], F.kw[t], M);
+  }
+}
+
+// SENSE-CG (recon_lib.cpp:1523-1759).  X[t] must be zero on entry.
+template <typename R>
+static void run_cg(OHandle *h, const OFrames &F, int iters, void **Xv, double *resid) {
+  OPlan<R> &p = P<R>(h);
+  long n = p.isize();
+  int Nt = F.Nt, Nz = p.g.N[2];
+  long plane = (long)p.g.N[0] * p.g.N[1];
+  std::vector<std::vector<cx<R>>> Rr(Nt, std::vector<cx<R>>(n)), Pp(Nt), L(Nt, std::vector<cx<R>>(n));
+  std::vector<cx<R>> tmp;
+  cx<R> **X = (cx<R> **)Xv;
+  for (int t = 0; t < Nt; t++) {
+    for (int c = 0; c < F.C; c++)
+      p.adjoint(Rr[t].data(), (const cx<R> *)F.smaps[c], (const cx<R> *)F.data[t * F.C + c], F.kx[t], F.ky[t], F.kz[t],
+                F.kw[t], F.M[t]);
+    Pp[t] = Rr[t];
+  }
+  for (int it = 0; it < iters; it++) {
+    for (int t = 0; t < Nt; t++) {
+      std::fill(L[t].begin(), L[t].end(), cx<R>(0, 0));
+      normal_op<R>(h, F, t, Pp[t].data(), L[t].data(), tmp, false);
+    }
+    std::vector<cx<double>> a_rr(Nz), a_pl(Nz), a_rn(Nz);
+    for (int t = 0; t < Nt; t++) {
+#pragma omp parallel for
+      for (int k = 0; k < Nz; k++)
+        for (long q = 0; q < plane; q++) {
+          long i = k * plane + q;
+          a_rr[k] += (double)(R)std::norm(Rr[t][i]);
+          cx<R> pl = std::conj(Pp[t][i]) * L[t][i];
+          a_pl[k] += cx<double>(pl.real(), pl.imag());
+        }
+    }
+    cx<double> rr(0, 0), pl(0, 0), rn(0, 0);
+    for (int k = 0; k < Nz; k++) { rr += a_rr[k]; pl += a_pl[k]; }
+    cx<double> ds = rr / pl;
+    cx<R> scale((R)ds.real(), (R)ds.imag());
+    for (int t = 0; t < Nt; t++) {
+#pragma omp parallel for
+      for (int k = 0; k < Nz; k++)
+        for (long q = 0; q < plane; q++) {
+          long i = k * plane + q;
+          X[t][i] += scale * Pp[t][i];
+          Rr[t][i] -= scale * L[t][i];
+          a_rn[k] += (double)(R)std::norm(Rr[t][i]);
+        }
+    }
+    for (int k = 0; k < Nz; k++) rn += a_rn[k];
+    cx<double> d2 = rn / rr;
+    cx<R> scale2((R)d2.real(), (R)d2.imag());
+    for (int t = 0; t < Nt; t++)
+#pragma omp parallel for
+      for (long i = 0; i < n; i++) Pp[t][i] = Rr[t][i] + scale2 * Pp[t][i];
+    if (resid) resid[it] = rn.real();
+  }
+}
+
+// FISTA / IST (recon_lib.cpp:1761-2212) with L1 wavelet threshold
+// (recon_lib.cpp:2416-2527) and optional LLR in time (recon_lib.cpp:2117-2121).
+template <typename R>
+static void run_fista(OHandle *h, const OFrames &F, const OFistaParams &q, void **Xv, double *resid, float *step_out,
+                      float *thr_out) {
+  OPlan<R> &p = P<R>(h);
+  long n = p.isize();
+  int Nt = F.Nt;
+  cx<R> **X = (cx<R> **)Xv;
+  std::vector<std::vector<cx<R>>> Rr(Nt, std::vector<cx<R>>(n)), Xo(Nt, std::vector<cx<R>>(n, cx<R>(0, 0)));
+  std::vector<cx<R>> tmp;
+  GRand rng(1);
+  for (long i = 0; i < q.rand_skip; i++) rng.step();
+  // Max eigenvalue by power iteration; seed is the constant -0.5-0.5i because
+  // std::rand()/RAND_MAX is an integer division (recon_lib.cpp:1809-1811).
+  for (int t = 0; t < Nt; t++) std::fill(X[t], X[t] + n, cx<R>((R)-0.5, (R)-0.5));
+  cx<R> step(1, 0);
+  for (int it = 0; it < q.max_eig_iter; it++) {
+    for (int t = 0; t < Nt; t++) {
+      std::fill(Rr[t].begin(), Rr[t].end(), cx<R>(0, 0));
+      normal_op<R>(h, F, t, X[t], Rr[t].data(), tmp, false);
+    }
+    double e = 0;
+    for (int t = 0; t < Nt; t++) for (long i = 0; i < n; i++) e += (double)(R)std::norm(Rr[t][i]);
+    double max_eig = std::sqrt(e);
+    cx<R> sc((R)(1. / max_eig), 0);
+    for (int t = 0; t < Nt; t++) for (long i = 0; i < n; i++) X[t][i] = sc * Rr[t][i];
+    step = cx<R>((R)(1. / max_eig), 0);
+  }
+  if (step_out) *step_out = (float)step.real();
+  for (int t = 0; t < Nt; t++) std::fill(X[t], X[t] + n, cx<R>(0, 0));
+  Wave wave(p.g.N[0], p.g.N[1], p.g.N[2], q.wave_levels, q.wave_type);
+  LLRParams lp;
+  for (int d = 0; d < 3; d++) lp.bs[d] = q.llr_bs[d];
+  lp.block_iter = q.llr_block_iter; lp.alpha = q.llr_alpha; lp.clear_amp = q.clear_amp; lp.clear_t2 = q.clear_t2;
+  for (int it = 0; it < q.max_iter; it++) {
+    // fista_update (recon_lib.cpp:2177-2212)
+    R A = (R)(float)(1.0 + (it - 1.0) / (it + 1.0));
+    R B = (R)(float)(-(it - 1.0) / (it + 1.0));
+    for (int t = 0; t < Nt; t++)
+      for (long i = 0; i < n; i++) {
+        cx<R> x0 = Xo[t][i], x1 = X[t][i];
+        X[t][i] = A * x1 + B * x0;
+        Xo[t][i] = x1;
+      }
+    for (int t = 0; t < Nt; t++) {
+      std::fill(Rr[t].begin(), Rr[t].end(), cx<R>(0, 0));
+      normal_op<R>(h, F, t, X[t], Rr[t].data(), tmp, true);
+    }
+    double e = 0;
+    for (int t = 0; t < Nt; t++) for (long i = 0; i < n; i++) e += (double)(R)std::norm(Rr[t][i]);
+    if (resid) resid[it] = e;
+    for (int t = 0; t < Nt; t++)
+      for (long i = 0; i < n; i++) X[t][i] -= Rr[t][i] * step;
+    if (q.llr_alpha > 0) {
+      float smax = llr_update_threshold<R>(X, Nt, p.g.N, lp, it);
+      llr_thresh<R>(X, Nt, p.g.N, lp, smax, rng);
+    }
+    if (q.use_threshold) {
+      float thr = 0;
+      for (int spin = 0; spin < q.cycle_spins; spin++) {
+        wave.random_shift(rng);
+        for (int t = 0; t < Nt; t++) wave.forward<R>(X[t]);
+        if (spin == 0) thr = (float)(1. / (float)q.cycle_spins) * get_threshold<R>(X, Nt, n, q.thresh, q.thresh);
+        for (int t = 0; t < Nt; t++) soft_threshold<R>(X[t], n, thr);
+        for (int t = 0; t < Nt; t++) wave.backward<R>(X[t]);
+      }
+      if (thr_out) thr_out[it] = thr;
+    }
+  }
+}
+
+extern "C" {
+
+void *orc_plan_create(int Nx, int Ny, int Nz, float overgrid, float dwin, int ktype, float k_rad, int prec) {
+  OHandle *h = new OHandle();
+  h->prec = prec;
+  Geom &g = h->g();
+  build_geom(g, Nx, Ny, Nz, overgrid, dwin, ktype, k_rad);
+  if (prec) h->pd.grid.assign(h->pd.gsize(), 0); else h->pf.grid.assign(h->pf.gsize(), 0);
+  return h;
+}
+void orc_plan_destroy(void *h) { delete (OHandle *)h; }
+
+void orc_plan_info(void *hv, int *S, int *og, float *grid, float *beta, float *dwin, int *lut_len) {
+  Geom &g = ((OHandle *)hv)->g();
+  for (int d = 0; d < 3; d++) {
+    S[d] = g.S[d]; og[d] = g.og_s[d]; grid[d] = g.grid[d]; beta[d] = g.beta[d]; dwin[d] = g.dwin[d];
+  }
+  *lut_len = g.lut_len;
+}
+void orc_get_tables(void *hv, float *lut, float *win) {
+  Geom &g = ((OHandle *)hv)->g();
+  int o = 0;
+  for (int d = 0; d < 3; d++) { std::memcpy(lut + (size_t)d * g.lut_len, g.lut[d].data(), 4 * g.lut_len); }
+  for (int d = 0; d < 3; d++) { std::memcpy(win + o, g.win[d].data(), 4 * g.S[d]); o += g.S[d]; }
+}
+
+void orc_adjoint(void *hv, void *X, const void *smap, const void *data, const float *kx, const float *ky,
+                 const float *kz, const float *kw, long M) {
+  OHandle *h = (OHandle *)hv;
+  if (h->prec) h->pd.adjoint((cx<double> *)X, (const cx<double> *)smap, (const cx<double> *)data, kx, ky, kz, kw, M);
+  else h->pf.adjoint((cx<float> *)X, (const cx<float> *)smap, (const cx<float> *)data, kx, ky, kz, kw, M);
+}
+void orc_forward(void *hv, const void *X, const void *smap, void *data, const float *kx, const float *ky,
+                 const float *kz, const float *kw, long M, const void *diff) {
+  OHandle *h = (OHandle *)hv;
+  if (h->prec) h->pd.forward((const cx<double> *)X, (const cx<double> *)smap, (cx<double> *)data, kx, ky, kz, kw, M, (const cx<double> *)diff);
+  else h->pf.forward((const cx<float> *)X, (const cx<float> *)smap, (cx<float> *)data, kx, ky, kz, kw, M, (const cx<float> *)diff);
+}
+// Stage access for kernel-level tests: the plan's grid buffer.
+void orc_get_grid(void *hv, void *out) {
+  OHandle *h = (OHandle *)hv;
+  if (h->prec) std::memcpy(out, h->pd.grid.data(), sizeof(cx<double>) * h->pd.gsize());
+  else std::memcpy(out, h->pf.grid.data(), sizeof(cx<float>) * h->pf.gsize());
+}
+void orc_set_grid(void *hv, const void *in) {
+  OHandle *h = (OHandle *)hv;
+  if (h->prec) std::memcpy(h->pd.grid.data(), in, sizeof(cx<double>) * h->pd.gsize());
+  else std::memcpy(h->pf.grid.data(), in, sizeof(cx<float>) * h->pf.gsize());
+}
+void orc_grid(void *hv, const void *data, const float *kx, const float *ky, const float *kz, const float *kw, long M) {
+  OHandle *h = (OHandle *)hv;
+  if (h->prec) { std::fill(h->pd.grid.begin(), h->pd.grid.end(), 0); h->pd.grid_forward((const cx<double> *)data, kx, ky, kz, kw, M); }
+  else { std::fill(h->pf.grid.begin(), h->pf.grid.end(), 0); h->pf.grid_forward((const cx<float> *)data, kx, ky, kz, kw, M); }
+}
+void orc_ungrid(void *hv, void *data, const float *kx, const float *ky, const float *kz, const float *kw, long M, const void *diff) {
+  OHandle *h = (OHandle *)hv;
+  if (h->prec) h->pd.grid_backward((cx<double> *)data, kx, ky, kz, kw, M, (const cx<double> *)diff);
+  else h->pf.grid_backward((cx<float> *)data, kx, ky, kz, kw, M, (const cx<float> *)diff);
+}
+void orc_set_image(void *hv, const void *X, const void *smap) {
+  OHandle *h = (OHandle *)hv;
+  if (h->prec) h->pd.set_image((const cx<double> *)X, (const cx<double> *)smap);
+  else h->pf.set_image((const cx<float> *)X, (const cx<float> *)smap);
+}
+void orc_accumulate(void *hv, void *X, const void *smap) {
+  OHandle *h = (OHandle *)hv;
+  if (h->prec) h->pd.accumulate((cx<double> *)X, (const cx<double> *)smap);
+  else h->pf.accumulate((cx<float> *)X, (const cx<float> *)smap);
+}
+void orc_fft3(void *hv, int dir) {  // dir -1: do_fft, +1: do_ifft
+  OHandle *h = (OHandle *)hv;
+  if (h->prec) { if (dir < 0) h->pd.do_fft(); else h->pd.do_ifft(); }
+  else { if (dir < 0) h->pf.do_fft(); else h->pf.do_ifft(); }
+}
+void orc_fft1d(int n, void *data, int sign, int prec) {
+  if (prec) { FFT1<double> f(n, sign); std::vector<cx<double>> w(n); f.run((cx<double> *)data, w.data()); }
+  else { FFT1<float> f(n, sign); std::vector<cx<float>> w(n); f.run((cx<float> *)data, w.data()); }
+}
+
+void orc_cg(void *hv, const OFrames *F, int iters, void **X, double *resid) {
+  OHandle *h = (OHandle *)hv;
+  if (h->prec) run_cg<double>(h, *F, iters, X, resid); else run_cg<float>(h, *F, iters, X, resid);
+}
+void orc_fista(void *hv, const OFrames *F, const OFistaParams *q, void **X, double *resid, float *step, float *thr) {
+  OHandle *h = (OHandle *)hv;
+  if (h->prec) run_fista<double>(h, *F, *q, X, resid, step, thr); else run_fista<float>(h, *F, *q, X, resid, step, thr);
+}
+// E^H W E per frame, summed over coils, accumulated into out.
+void orc_normal(void *hv, const OFrames *F, int t, const void *X, void *out) {
+  OHandle *h = (OHandle *)hv;
+  if (h->prec) { std::vector<cx<double>> tmp; normal_op<double>(h, *F, t, (const cx<double> *)X, (cx<double> *)out, tmp, false); }
+  else { std::vector<cx<float>> tmp; normal_op<float>(h, *F, t, (const cx<float> *)X, (cx<float> *)out, tmp, false); }
+}
+
+void orc_wavelet(int Nx, int Ny, int Nz, const int *levels, const int *shift, int wtype, void *X, int inverse, int prec) {
+  Wave w(Nx, Ny, Nz, levels, wtype);
+  for (int d = 0; d < 3; d++) w.S[d] = shift[d];
+  if (prec) { if (inverse) w.backward<double>((cx<double> *)X); else w.forward<double>((cx<double> *)X); }
+  else { if (inverse) w.backward<float>((cx<float> *)X); else w.forward<float>((cx<float> *)X); }
+}
+void orc_wavelet_info(int Nx, int Ny, int Nz, const int *levels, int wtype, int *L_out, float *filters) {
+  Wave w(Nx, Ny, Nz, levels, wtype);
+  for (int d = 0; d < 3; d++) L_out[d] = w.L[d];
+  for (int i = 0; i < w.wN; i++) {
+    filters[i] = w.lpf[i]; filters[4 + i] = w.hpf[i]; filters[8 + i] = w.Slpf[i]; filters[12 + i] = w.Shpf[i];
+  }
+}
+float orc_fraction_threshold(void **vols, int nvol, long nvox, float fraction, int prec) {
+  if (prec) return get_threshold<double>((cx<double> **)vols, nvol, nvox, fraction, fraction);
+  return get_threshold<float>((cx<float> **)vols, nvol, nvox, fraction, fraction);
+}
+void orc_soft_threshold(void *X, long n, float value, int prec) {
+  if (prec) soft_threshold<double>((cx<double> *)X, n, value); else soft_threshold<float>((cx<float> *)X, n, value);
+}
+float orc_llr_update_threshold(void **X, int Nt, const int *N, const int *bs, float amp, float t2, int iter, int prec) {
+  LLRParams p;
+  for (int d = 0; d < 3; d++) p.bs[d] = bs[d];
+  p.block_iter = 1; p.alpha = 0; p.clear_amp = amp; p.clear_t2 = t2;
+  if (prec) return llr_update_threshold<double>((cx<double> **)X, Nt, N, p, iter);
+  return llr_update_threshold<float>((cx<float> **)X, Nt, N, p, iter);
+}
+void orc_llr_thresh(void **X, int Nt, const int *N, const int *bs, int block_iter, float alpha, float smax,
+                    long rand_skip, int prec) {
+  LLRParams p;
+  for (int d = 0; d < 3; d++) p.bs[d] = std::min(bs[d], N[d]);
+  p.block_iter = block_iter; p.alpha = alpha; p.clear_amp = 0; p.clear_t2 = 1;
+  GRand rng(1);
+  for (long i = 0; i < rand_skip; i++) rng.step();
+  if (prec) llr_thresh<double>((cx<double> **)X, Nt, N, p, smax, rng);
+  else llr_thresh<float>((cx<float> **)X, Nt, N, p, smax, rng);
+}
+void orc_glibc_rand(long skip, int n, int *out) {
+  GRand rng(1);
+  for (long i = 0; i < skip; i++) rng.step();
+  for (int i = 0; i < n; i++) out[i] = rng.next();
+}
+int orc_num_threads(void) { return omp_get_max_threads(); }
+}

@@ -1,0 +1,320 @@
+"""ORACLE -- TEST INFRASTRUCTURE ONLY.
+
+ctypes front end for ``oracle/_build/liboracle.so``, the CPU restatement of the
+uwmri/mri_recon gridFFT / recon_lib hot path (see ``oracle.cpp``).  Only the
+tests, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg import this
+module, and only as the checker.  Parity unpinned: the reference has no golden
+vectors for this path and cannot be built here.
+
+Array conventions follow the reference: images are C-ordered (Nz, Ny, Nx)
+complex arrays (column-major x-fastest in the reference's terms), k-space data
+are flat complex arrays of M samples, trajectories are float32.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
+_lib = None
+
+KAISER, TRIANGLE, SINC, POLY = 1, 0, 2, 3
+
+
+def build():
+    """Compile the oracle shared library (make, in oracle/)."""
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH):
+            build()
+        L = ctypes.CDLL(_LIB_PATH)
+        vp, fp, ip, dp = ctypes.c_void_p, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)
+        L.orc_plan_create.restype = vp
+        L.orc_plan_create.argtypes = [ctypes.c_int] * 3 + [ctypes.c_float, ctypes.c_float, ctypes.c_int, ctypes.c_float, ctypes.c_int]
+        L.orc_plan_destroy.argtypes = [vp]
+        L.orc_plan_info.argtypes = [vp, ip, ip, fp, fp, fp, ip]
+        L.orc_get_tables.argtypes = [vp, fp, fp]
+        L.orc_adjoint.argtypes = [vp, vp, vp, vp, fp, fp, fp, fp, ctypes.c_long]
+        L.orc_forward.argtypes = [vp, vp, vp, vp, fp, fp, fp, fp, ctypes.c_long, vp]
+        L.orc_get_grid.argtypes = [vp, vp]
+        L.orc_set_grid.argtypes = [vp, vp]
+        L.orc_grid.argtypes = [vp, vp, fp, fp, fp, fp, ctypes.c_long]
+        L.orc_ungrid.argtypes = [vp, vp, fp, fp, fp, fp, ctypes.c_long, vp]
+        L.orc_set_image.argtypes = [vp, vp, vp]
+        L.orc_accumulate.argtypes = [vp, vp, vp]
+        L.orc_fft3.argtypes = [vp, ctypes.c_int]
+        L.orc_fft1d.argtypes = [ctypes.c_int, vp, ctypes.c_int, ctypes.c_int]
+        L.orc_cg.argtypes = [vp, vp, ctypes.c_int, ctypes.POINTER(vp), dp]
+        L.orc_fista.argtypes = [vp, vp, vp, ctypes.POINTER(vp), dp, fp, fp]
+        L.orc_normal.argtypes = [vp, vp, ctypes.c_int, vp, vp]
+        L.orc_wavelet.argtypes = [ctypes.c_int] * 3 + [ip, ip, ctypes.c_int, vp, ctypes.c_int, ctypes.c_int]
+        L.orc_wavelet_info.argtypes = [ctypes.c_int] * 3 + [ip, ctypes.c_int, ip, fp]
+        L.orc_fraction_threshold.restype = ctypes.c_float
+        L.orc_fraction_threshold.argtypes = [ctypes.POINTER(vp), ctypes.c_int, ctypes.c_long, ctypes.c_float, ctypes.c_int]
+        L.orc_soft_threshold.argtypes = [vp, ctypes.c_long, ctypes.c_float, ctypes.c_int]
+        L.orc_llr_update_threshold.restype = ctypes.c_float
+        L.orc_llr_update_threshold.argtypes = [ctypes.POINTER(vp), ctypes.c_int, ip, ip, ctypes.c_float, ctypes.c_float, ctypes.c_int, ctypes.c_int]
+        L.orc_llr_thresh.argtypes = [ctypes.POINTER(vp), ctypes.c_int, ip, ip, ctypes.c_int, ctypes.c_float, ctypes.c_float, ctypes.c_long, ctypes.c_int]
+        L.orc_glibc_rand.argtypes = [ctypes.c_long, ctypes.c_int, ip]
+        L.orc_num_threads.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def _f32(a):
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    return a, a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None else None
+
+
+def _ip(vals):
+    arr = (ctypes.c_int * len(vals))(*[int(v) for v in vals])
+    return arr
+
+
+class _Frames(ctypes.Structure):
+    _fields_ = [("Nt", ctypes.c_int), ("C", ctypes.c_int),
+                ("kx", ctypes.c_void_p), ("ky", ctypes.c_void_p), ("kz", ctypes.c_void_p), ("kw", ctypes.c_void_p),
+                ("M", ctypes.c_void_p), ("data", ctypes.c_void_p), ("smaps", ctypes.c_void_p)]
+
+
+class FistaParams(ctypes.Structure):
+    _fields_ = [("max_iter", ctypes.c_int), ("max_eig_iter", ctypes.c_int), ("cycle_spins", ctypes.c_int),
+                ("wave_levels", ctypes.c_int * 3), ("wave_type", ctypes.c_int), ("thresh", ctypes.c_float),
+                ("use_threshold", ctypes.c_int), ("llr_bs", ctypes.c_int * 3), ("llr_block_iter", ctypes.c_int),
+                ("llr_alpha", ctypes.c_float), ("clear_amp", ctypes.c_float), ("clear_t2", ctypes.c_float),
+                ("rand_skip", ctypes.c_long)]
+
+
+class Plan:
+    """One gridFFT operator (one coil at a time), FP32 (prec=0) or FP64 (prec=1)."""
+
+    def __init__(self, N, overgrid=1.5, dwin=-1.0, kernel=KAISER, k_rad=9999.0, prec=0):
+        if np.isscalar(N):
+            N = (N, N, N)
+        self.N = tuple(int(n) for n in N)  # (Nx, Ny, Nz)
+        self.prec = prec
+        self.cdt = np.complex128 if prec else np.complex64
+        self.h = lib().orc_plan_create(self.N[0], self.N[1], self.N[2], overgrid, dwin, kernel, k_rad, prec)
+        S = (ctypes.c_int * 3)()
+        og = (ctypes.c_int * 3)()
+        gr = (ctypes.c_float * 3)()
+        be = (ctypes.c_float * 3)()
+        dw = (ctypes.c_float * 3)()
+        ll = ctypes.c_int()
+        lib().orc_plan_info(self.h, S, og, gr, be, dw, ctypes.byref(ll))
+        self.S = tuple(S)
+        self.og = tuple(og)
+        self.grid_ratio = tuple(gr)
+        self.beta = tuple(be)
+        self.dwin = tuple(dw)
+        self.lut_len = ll.value
+
+    def __del__(self):
+        try:
+            lib().orc_plan_destroy(self.h)
+        except Exception:
+            pass
+
+    @property
+    def ishape(self):
+        return (self.N[2], self.N[1], self.N[0])
+
+    @property
+    def gshape(self):
+        return (self.S[2], self.S[1], self.S[0])
+
+    def tables(self):
+        lut = np.zeros(3 * self.lut_len, np.float32)
+        win = np.zeros(sum(self.S), np.float32)
+        lib().orc_get_tables(self.h, lut.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), win.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+        s0, s1 = self.S[0], self.S[0] + self.S[1]
+        return lut.reshape(3, self.lut_len), (win[:s0], win[s0:s1], win[s1:])
+
+    def _c(self, a):
+        return None if a is None else np.ascontiguousarray(a, dtype=self.cdt)
+
+    def adjoint(self, X, smap, data, kx, ky, kz, kw):
+        """gridFFT::forward (E^H): X += accumulate(ifft(grid(data*kw)))."""
+        X = self._c(X)
+        assert X.flags.writeable
+        smap, data = self._c(smap), self._c(data)
+        kx, px = _f32(kx); ky, py = _f32(ky); kz, pz = _f32(kz); kw, pw = _f32(kw)
+        lib().orc_adjoint(self.h, _ptr(X), _ptr(smap), _ptr(data), px, py, pz, pw, kx.size)
+        return X
+
+    def forward(self, X, smap, kx, ky, kz, kw, diff=None):
+        """gridFFT::backward (E), or backward_residual when diff is given."""
+        X, smap, diff = self._c(X), self._c(smap), self._c(diff)
+        kx, px = _f32(kx); ky, py = _f32(ky); kz, pz = _f32(kz); kw, pw = _f32(kw)
+        out = np.zeros(kx.size, self.cdt)
+        lib().orc_forward(self.h, _ptr(X), _ptr(smap), _ptr(out), px, py, pz, pw, kx.size, _ptr(diff))
+        return out
+
+    # stage access
+    def grid(self, data, kx, ky, kz, kw):
+        data = self._c(data)
+        kx, px = _f32(kx); ky, py = _f32(ky); kz, pz = _f32(kz); kw, pw = _f32(kw)
+        lib().orc_grid(self.h, _ptr(data), px, py, pz, pw, kx.size)
+        return self.get_grid()
+
+    def ungrid(self, grid, kx, ky, kz, kw, diff=None):
+        self.set_grid(grid)
+        diff = self._c(diff)
+        kx, px = _f32(kx); ky, py = _f32(ky); kz, pz = _f32(kz); kw, pw = _f32(kw)
+        out = np.zeros(kx.size, self.cdt)
+        lib().orc_ungrid(self.h, _ptr(out), px, py, pz, pw, kx.size, _ptr(diff))
+        return out
+
+    def get_grid(self):
+        g = np.zeros(self.gshape, self.cdt)
+        lib().orc_get_grid(self.h, _ptr(g))
+        return g
+
+    def set_grid(self, g):
+        g = self._c(g).reshape(self.gshape)
+        lib().orc_set_grid(self.h, _ptr(g))
+
+    def set_image(self, X, smap):
+        X, smap = self._c(X), self._c(smap)
+        lib().orc_set_image(self.h, _ptr(X), _ptr(smap))
+        return self.get_grid()
+
+    def accumulate(self, grid, X, smap):
+        self.set_grid(grid)
+        X, smap = self._c(X), self._c(smap)
+        lib().orc_accumulate(self.h, _ptr(X), _ptr(smap))
+        return X
+
+    def fft3(self, grid, direction):
+        self.set_grid(grid)
+        lib().orc_fft3(self.h, int(direction))
+        return self.get_grid()
+
+    # solvers ---------------------------------------------------------------
+    def _frames(self, frames, smaps):
+        """frames: list of dicts with kx, ky, kz, kw (float32, M) and data (C, M)."""
+        C = len(smaps)
+        keep = []
+        Nt = len(frames)
+        arrs = {k: (ctypes.c_void_p * Nt)() for k in ("kx", "ky", "kz", "kw")}
+        Ms = (ctypes.c_long * Nt)()
+        datas = (ctypes.c_void_p * (Nt * C))()
+        for t, fr in enumerate(frames):
+            for k in ("kx", "ky", "kz", "kw"):
+                a = np.ascontiguousarray(fr[k], dtype=np.float32)
+                keep.append(a)
+                arrs[k][t] = a.ctypes.data
+            Ms[t] = keep[-1].size
+            for c in range(C):
+                d = self._c(fr["data"][c])
+                keep.append(d)
+                datas[t * C + c] = d.ctypes.data
+        sm = (ctypes.c_void_p * C)()
+        for c in range(C):
+            s = self._c(smaps[c])
+            keep.append(s)
+            sm[c] = s.ctypes.data
+        F = _Frames(Nt, C, ctypes.cast(arrs["kx"], ctypes.c_void_p), ctypes.cast(arrs["ky"], ctypes.c_void_p),
+                    ctypes.cast(arrs["kz"], ctypes.c_void_p), ctypes.cast(arrs["kw"], ctypes.c_void_p),
+                    ctypes.cast(Ms, ctypes.c_void_p), ctypes.cast(datas, ctypes.c_void_p), ctypes.cast(sm, ctypes.c_void_p))
+        keep += [arrs, Ms, datas, sm]
+        return F, keep
+
+    def normal(self, frames, smaps, t, X):
+        F, keep = self._frames(frames, smaps)
+        X = self._c(X)
+        out = np.zeros(self.ishape, self.cdt)
+        lib().orc_normal(self.h, ctypes.byref(F), t, _ptr(X), _ptr(out))
+        return out
+
+    def cg(self, frames, smaps, iters):
+        F, keep = self._frames(frames, smaps)
+        Nt = len(frames)
+        X = [np.zeros(self.ishape, self.cdt) for _ in range(Nt)]
+        Xp = (ctypes.c_void_p * Nt)(*[x.ctypes.data for x in X])
+        resid = np.zeros(max(iters, 1), np.float64)
+        lib().orc_cg(self.h, ctypes.byref(F), iters, Xp, resid.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+        return X, resid[:iters]
+
+    def fista(self, frames, smaps, params):
+        F, keep = self._frames(frames, smaps)
+        Nt = len(frames)
+        X = [np.zeros(self.ishape, self.cdt) for _ in range(Nt)]
+        Xp = (ctypes.c_void_p * Nt)(*[x.ctypes.data for x in X])
+        n = max(params.max_iter, 1)
+        resid = np.zeros(n, np.float64)
+        thr = np.zeros(n, np.float32)
+        step = ctypes.c_float()
+        lib().orc_fista(self.h, ctypes.byref(F), ctypes.byref(params), Xp, resid.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                        ctypes.byref(step), thr.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+        return X, resid[:params.max_iter], step.value, thr[:params.max_iter]
+
+
+def fft1d(x, sign, prec=1):
+    x = np.ascontiguousarray(x, dtype=np.complex128 if prec else np.complex64).copy()
+    lib().orc_fft1d(x.size, _ptr(x), int(sign), prec)
+    return x
+
+
+def wavelet(X, levels, shift, wtype=1, inverse=False):
+    X = np.ascontiguousarray(X).copy()
+    prec = 1 if X.dtype == np.complex128 else 0
+    Nz, Ny, Nx = X.shape
+    lib().orc_wavelet(Nx, Ny, Nz, _ip(levels), _ip(shift), wtype, _ptr(X), int(inverse), prec)
+    return X
+
+
+def wavelet_info(shape_xyz, levels, wtype=1):
+    L = (ctypes.c_int * 3)()
+    f = np.zeros(16, np.float32)
+    lib().orc_wavelet_info(shape_xyz[0], shape_xyz[1], shape_xyz[2], _ip(levels), wtype, L, f.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+    return tuple(L), f.reshape(4, 4)
+
+
+def fraction_threshold(vols, fraction):
+    prec = 1 if vols[0].dtype == np.complex128 else 0
+    arr = (ctypes.c_void_p * len(vols))(*[v.ctypes.data for v in vols])
+    return lib().orc_fraction_threshold(arr, len(vols), vols[0].size, fraction, prec)
+
+
+def soft_threshold(X, value):
+    X = np.ascontiguousarray(X).copy()
+    prec = 1 if X.dtype == np.complex128 else 0
+    lib().orc_soft_threshold(_ptr(X), X.size, value, prec)
+    return X
+
+
+def llr_update_threshold(vols, bs, amp=4.0, t2=6.0, iteration=0):
+    prec = 1 if vols[0].dtype == np.complex128 else 0
+    Nz, Ny, Nx = vols[0].shape
+    arr = (ctypes.c_void_p * len(vols))(*[v.ctypes.data for v in vols])
+    return lib().orc_llr_update_threshold(arr, len(vols), _ip((Nx, Ny, Nz)), _ip(bs), amp, t2, iteration, prec)
+
+
+def llr_thresh(vols, bs, block_iter, alpha, smax, rand_skip):
+    vols = [np.ascontiguousarray(v).copy() for v in vols]
+    prec = 1 if vols[0].dtype == np.complex128 else 0
+    Nz, Ny, Nx = vols[0].shape
+    arr = (ctypes.c_void_p * len(vols))(*[v.ctypes.data for v in vols])
+    lib().orc_llr_thresh(arr, len(vols), _ip((Nx, Ny, Nz)), _ip(bs), block_iter, alpha, smax, rand_skip, prec)
+    return vols
+
+
+def glibc_rand(skip, n):
+    out = (ctypes.c_int * n)()
+    lib().orc_glibc_rand(skip, n, out)
+    return np.array(out[:], dtype=np.int64)
+
+
+def num_threads():
+    return lib().orc_num_threads()

@@ -1,0 +1,49 @@
+"""Seeded test cases shared by the CPU and GPU tests."""
+import numpy as np
+
+from mri_recon_gb300 import synth
+
+
+def rel(a, b):
+    a = np.asarray(a).astype(np.complex128)
+    b = np.asarray(b).astype(np.complex128)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def case(N=32, C=4, nproj=600, nread=None, seed=7, jitter=0.0, noise=0.01, ellipsoids=6, nudft=False):
+    """Phantom, coil maps, radial trajectory and k-space for one frame."""
+    nread = nread or N
+    kx, ky, kz, kw = synth.radial_trajectory(N, nproj, nread, jitter_grid=jitter, seed=seed)
+    img = synth.phantom(N, ellipsoids, seed=seed)
+    smaps = synth.coil_maps(N, C, seed=seed + 1)
+    rng = np.random.default_rng(seed)
+    if nudft:
+        data = np.stack([synth.nudft(img * smaps[c], kx, ky, kz) for c in range(C)]).astype(np.complex64)
+        data = synth.add_noise(data, noise, seed + 2)
+    else:
+        data = (rng.standard_normal((C, kx.size)) + 1j * rng.standard_normal((C, kx.size))).astype(np.complex64)
+    X = (rng.standard_normal(img.shape) + 1j * rng.standard_normal(img.shape)).astype(np.complex64)
+    return dict(N=N, C=C, kx=kx, ky=ky, kz=kz, kw=kw, img=img, smaps=smaps, data=data, X=X)
+
+
+def edge_trajectory(N, seed=3):
+    """Samples that exercise the reference's edge rules: kw == 0, outside the grid,
+    on the grid boundary (clipped taps), exactly half-integer grid positions (a
+    sixth tap), and the k-space centre."""
+    rng = np.random.default_rng(seed)
+    S = 16 * int(np.ceil(1.5 * N / 16))
+    g = S / N
+    pts = []
+    pts += [(0.0, 0.0, 0.0)]
+    half = N / 2
+    pts += [(half, 0, 0), (-half, 0, 0), (0, half * 0.999, 0), (0, 0, -half)]          # near/at the edge
+    pts += [(half * 1.2, 0, 0), (0, -half * 1.6, 0), (0, 0, 3 * half)]                  # outside the grid
+    # with g = 1.5, odd integer k puts dk = k*g + S/2 exactly on x.5, where
+    # ceil(dk - 2.5) .. floor(dk + 2.5) spans six taps
+    pts += [(1.0, 5.0, -3.0), (7.0, -1.0, 3.0), (-5.0, 1.0, 9.0)]
+    pts += [tuple(rng.uniform(-half, half, 3)) for _ in range(200)]
+    k = np.array(pts, np.float32)
+    kw = np.sum(k.astype(np.float64) ** 2, 1).astype(np.float32)
+    kw[5] = 0.0
+    kw[20] = 0.0
+    return k[:, 0].copy(), k[:, 1].copy(), k[:, 2].copy(), kw

@@ -1,0 +1,159 @@
+"""GPU parity of the gridFFT operators against the oracle (relative L2 <= 1e-5
+per operator application, the FP32 tolerance of the hot path)."""
+import numpy as np
+import pytest
+
+from tests.helpers import case, edge_trajectory, rel
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-5
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _plan(m, c, nframes=1, **kw):
+    p = m.Plan(c["N"], c["C"], nframes, **kw)
+    p.set_traj(0, c["kx"], c["ky"], c["kz"], c["kw"])
+    p.set_smaps(c["smaps"])
+    return p
+
+
+def _oracle_E(O, c, prec, diff=None):
+    p = O.Plan(c["N"], prec=prec)
+    a = (c["kx"], c["ky"], c["kz"], c["kw"])
+    return np.stack([p.forward(c["X"], c["smaps"][k], *a, diff=None if diff is None else diff[k]) for k in range(c["C"])])
+
+
+def _oracle_EH(O, c, prec):
+    p = O.Plan(c["N"], prec=prec)
+    a = (c["kx"], c["ky"], c["kz"], c["kw"])
+    X = np.zeros(p.ishape, p.cdt)
+    for k in range(c["C"]):
+        X = p.adjoint(X, c["smaps"][k], c["data"][k], *a)
+    return X
+
+
+@pytest.mark.parametrize("N,C,nproj", [(32, 4, 700), (64, 8, 1500), (48, 3, 500)])
+def test_forward_E_matches_oracle(mrg_lib, oracle_lib, N, C, nproj):
+    torch = _torch()
+    c = case(N=N, C=C, nproj=nproj)
+    p = _plan(mrg_lib, c)
+    X = torch.from_numpy(c["X"]).cuda()
+    y = p.forward(0, X).cpu().numpy()
+    assert rel(y, _oracle_E(oracle_lib, c, 0)) < TOL
+    assert rel(y, _oracle_E(oracle_lib, c, 1)) < TOL
+
+
+def test_forward_residual_matches_oracle(mrg_lib, oracle_lib):
+    torch = _torch()
+    c = case(N=32, C=4, nproj=700)
+    p = _plan(mrg_lib, c)
+    y = p.forward(0, torch.from_numpy(c["X"]).cuda(), diff=torch.from_numpy(c["data"]).cuda()).cpu().numpy()
+    assert rel(y, _oracle_E(oracle_lib, c, 0, diff=c["data"])) < TOL
+
+
+@pytest.mark.parametrize("N,C,nproj", [(32, 4, 700), (64, 8, 1500), (48, 3, 500), (32, 20, 400)])
+def test_adjoint_EH_matches_oracle(mrg_lib, oracle_lib, N, C, nproj):
+    torch = _torch()
+    c = case(N=N, C=C, nproj=nproj)
+    p = _plan(mrg_lib, c)
+    X = torch.zeros(c["X"].shape, dtype=torch.complex64, device="cuda")
+    p.adjoint(0, torch.from_numpy(c["data"]).cuda(), X)
+    got = X.cpu().numpy()
+    assert rel(got, _oracle_EH(oracle_lib, c, 0)) < TOL
+    assert rel(got, _oracle_EH(oracle_lib, c, 1)) < TOL
+
+
+def test_adjoint_accumulates_into_X(mrg_lib, oracle_lib):
+    torch = _torch()
+    c = case(N=32, C=2, nproj=300)
+    p = _plan(mrg_lib, c)
+    X0 = torch.from_numpy(c["X"]).cuda()
+    X = X0.clone()
+    p.adjoint(0, torch.from_numpy(c["data"]).cuda(), X)
+    ref = c["X"].astype(np.complex128) + _oracle_EH(oracle_lib, c, 1)
+    assert rel(X.cpu().numpy(), ref) < TOL
+
+
+def test_normal_operator_matches_oracle(mrg_lib, oracle_lib):
+    torch = _torch()
+    c = case(N=32, C=4, nproj=700)
+    p = _plan(mrg_lib, c)
+    got = p.normal(0, torch.from_numpy(c["X"]).cuda()).cpu().numpy()
+    O = oracle_lib.Plan(32, prec=1)
+    fr = [dict(kx=c["kx"], ky=c["ky"], kz=c["kz"], kw=c["kw"], data=c["data"])]
+    ref = O.normal(fr, c["smaps"], 0, c["X"])
+    assert rel(got, ref) < TOL
+
+
+def test_host_pointers_are_staged(mrg_lib, oracle_lib):
+    """numpy (host) buffers go through the same path as device tensors."""
+    c = case(N=32, C=2, nproj=300)
+    p = _plan(mrg_lib, c)
+    y = p.forward(0, c["X"])
+    assert isinstance(y, np.ndarray)
+    assert rel(y, _oracle_E(oracle_lib, c, 1)) < TOL
+    X = np.zeros(c["X"].shape, np.complex64)
+    p.adjoint(0, c["data"], X)
+    assert rel(X, _oracle_EH(oracle_lib, c, 1)) < TOL
+
+
+def test_edge_samples(mrg_lib, oracle_lib):
+    """kw == 0, samples outside the grid, clipped taps at the grid edge, six-tap
+    half-integer positions: E writes 0 where the reference does."""
+    torch = _torch()
+    N, C = 32, 2
+    c = case(N=N, C=C, nproj=10)
+    c["kx"], c["ky"], c["kz"], c["kw"] = edge_trajectory(N)
+    M = c["kx"].size
+    rng = np.random.default_rng(1)
+    c["data"] = (rng.standard_normal((C, M)) + 1j * rng.standard_normal((C, M))).astype(np.complex64)
+    p = _plan(mrg_lib, c)
+    y = p.forward(0, torch.from_numpy(c["X"]).cuda()).cpu().numpy()
+    ref = _oracle_E(oracle_lib, c, 1)
+    assert rel(y, ref) < TOL
+    assert np.all(y[:, 5] == 0) and np.all(y[:, 20] == 0)     # kw == 0
+    assert np.all(y[:, 5:8] == 0)                               # outside the grid
+    X = torch.zeros(c["X"].shape, dtype=torch.complex64, device="cuda")
+    p.adjoint(0, torch.from_numpy(c["data"]).cuda(), X)
+    assert rel(X.cpu().numpy(), _oracle_EH(oracle_lib, c, 1)) < TOL
+
+
+def test_per_coil_drop_in_matches_oracle(mrg_lib, oracle_lib):
+    """The reference's per-coil gridFFT surface (plain path, one coil per call)."""
+    torch = _torch()
+    c = case(N=32, C=3, nproj=500)
+    g = mrg_lib.gridFFT()
+    g.precalc_gridding(32, 32, 32)
+    assert (g.Sx, g.og_sx, g.og_ex) == (48, 8, 40)
+    a = [torch.from_numpy(v).cuda() for v in (c["kx"], c["ky"], c["kz"], c["kw"])]
+    X = torch.zeros(c["X"].shape, dtype=torch.complex64, device="cuda")
+    Xin = torch.from_numpy(c["X"]).cuda()
+    ys = []
+    for k in range(c["C"]):
+        sm = torch.from_numpy(c["smaps"][k]).cuda()
+        d = torch.empty(c["kx"].size, dtype=torch.complex64, device="cuda")
+        g.backward(Xin, sm, d, *a)
+        ys.append(d.cpu().numpy())
+        g.forward(X, sm, torch.from_numpy(c["data"][k]).cuda(), *a)
+    assert rel(np.stack(ys), _oracle_E(oracle_lib, c, 1)) < TOL
+    assert rel(X.cpu().numpy(), _oracle_EH(oracle_lib, c, 1)) < TOL
+    # residual form and the no-smap overloads
+    d = torch.empty(c["kx"].size, dtype=torch.complex64, device="cuda")
+    g.backward_residual(Xin, None, d, *a, torch.from_numpy(c["data"][0]).cuda())
+    O = oracle_lib.Plan(32, prec=1)
+    ref = O.forward(c["X"], None, c["kx"], c["ky"], c["kz"], c["kw"], diff=c["data"][0])
+    assert rel(d.cpu().numpy(), ref) < TOL
+
+
+def test_errors_do_not_exit(mrg_lib):
+    import mri_recon_gb300 as m
+    c = case(N=32, C=2, nproj=50)
+    p = m.Plan(32, 2, 1)
+    with pytest.raises(m.MrgError, match="STATE"):
+        p.forward(0, c["X"])                       # no trajectory yet
+    with pytest.raises(m.MrgError, match="UNSUPPORTED"):
+        m.Plan(100, 1, 1)                           # S = 160: radix 5 not built

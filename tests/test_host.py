@@ -1,0 +1,86 @@
+"""Host-side logic of the product, checked without a GPU: the C ABI library
+loads and exports every declared symbol, the plan geometry and tables equal
+the oracle's, and the rand() stream matches."""
+import ctypes
+import os
+import re
+
+import numpy as np
+
+from tests.conftest import ROOT
+
+
+def declared_symbols():
+    src = open(os.path.join(ROOT, "include", "mrg.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(mrg_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol(mrg_lib):
+    lib = ctypes.CDLL(mrg_lib.LIB_PATH)
+    names = declared_symbols()
+    assert len(names) >= 20
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    # and the Python binding covers the same set
+    from mri_recon_gb300 import _lib
+    assert sorted(_lib.SIGNATURES) == names
+
+
+def _geometry(L, N, kernel=1, overgrid=1.5, dwin=-1.0):
+    from mri_recon_gb300._lib import MrgConfig, _fp, _ip
+    cfg = MrgConfig()
+    L.mrg_config_default(ctypes.byref(cfg))
+    cfg.kernel_type, cfg.overgrid, cfg.dwin = kernel, overgrid, dwin
+    S = (ctypes.c_int * 3)()
+    og = (ctypes.c_int * 3)()
+    gr = (ctypes.c_float * 3)()
+    be = (ctypes.c_float * 3)()
+    ll = ctypes.c_int()
+    assert L.mrg_plan_geometry(ctypes.byref(cfg), N, N, N, S, og, gr, be, ctypes.byref(ll), None, None) == 0
+    lut = np.zeros(3 * ll.value, np.float32)
+    win = np.zeros(sum(S), np.float32)
+    assert L.mrg_plan_geometry(ctypes.byref(cfg), N, N, N, S, og, gr, be, ctypes.byref(ll),
+                               lut.ctypes.data_as(_fp), win.ctypes.data_as(_fp)) == 0
+    return tuple(S), tuple(og), tuple(be), lut.reshape(3, -1), win
+
+
+def test_geometry_tables_equal_oracle(mrg_lib, oracle_lib):
+    L = mrg_lib.load()
+    for N in (32, 64, 96, 128, 256):
+        S, og, beta, lut, win = _geometry(L, N)
+        p = oracle_lib.Plan(N)
+        olut, owin = p.tables()
+        assert S == p.S and og == p.og
+        assert np.array_equal(lut, olut)
+        assert np.array_equal(win, np.concatenate(owin))
+        assert beta == p.beta
+
+
+def test_geometry_other_kernels(mrg_lib, oracle_lib):
+    L = mrg_lib.load()
+    for k in (0, 2, 3):
+        S, og, beta, lut, win = _geometry(L, 64, kernel=k)
+        p = oracle_lib.Plan(64, kernel=k)
+        olut, owin = p.tables()
+        assert np.array_equal(lut, olut)
+        assert np.array_equal(win, np.concatenate(owin))
+
+
+def test_rand_stream_matches_oracle(mrg_lib, oracle_lib):
+    L = mrg_lib.load()
+    out = (ctypes.c_int * 25)()
+    assert L.mrg_rand_stream(1000, 25, out) == 0
+    assert np.array_equal(np.array(out[:]), oracle_lib.glibc_rand(1000, 25))
+
+
+def test_errors_are_reported_not_fatal(mrg_lib):
+    from mri_recon_gb300._lib import MrgConfig
+    L = mrg_lib.load()
+    h = ctypes.c_void_p()
+    assert L.mrg_plan_create(None, 0, 64, 64, 1, 1, ctypes.byref(h)) == 1
+    assert b"positive" in L.mrg_last_error()
+    assert L.mrg_rand_stream(-1, 3, None) == 1
+    cfg = MrgConfig()
+    L.mrg_config_default(ctypes.byref(cfg))
+    assert abs(cfg.overgrid - 1.5) < 1e-7 and cfg.kernel_type == 1 and abs(cfg.k_rad - 9999.0) < 1e-3
