@@ -1,0 +1,163 @@
+// Standalone C ABI for the FISTA building blocks: wavelet, fraction / soft
+// threshold and the low-rank block operations, on caller buffers.
+#include <cstring>
+
+#include "mrg_internal.h"
+
+using namespace mrg;
+
+namespace {
+struct DevBuf {
+  void *p = nullptr;
+  ~DevBuf() { cudaFree(p); }
+};
+
+bool is_dev(const void *ptr) {
+  cudaPointerAttributes a;
+  if (!ptr || cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// Device view of a caller buffer (host buffers copied in; written back by the caller).
+mrg_status view(const void *ptr, size_t bytes, DevBuf &tmp, cudaStream_t st, float2 **out) {
+  if (is_dev(ptr)) {
+    *out = (float2 *)const_cast<void *>(ptr);
+    return MRG_OK;
+  }
+  MRG_CUDA(cudaMalloc(&tmp.p, bytes));
+  MRG_CUDA(cudaMemcpyAsync(tmp.p, ptr, bytes, cudaMemcpyHostToDevice, st));
+  *out = (float2 *)tmp.p;
+  return MRG_OK;
+}
+
+mrg_status back(void *ptr, const DevBuf &tmp, size_t bytes, cudaStream_t st) {
+  if (tmp.p) {
+    MRG_CUDA(cudaMemcpyAsync(ptr, tmp.p, bytes, cudaMemcpyDeviceToHost, st));
+    MRG_CUDA(cudaStreamSynchronize(st));
+  }
+  return MRG_OK;
+}
+}  // namespace
+
+extern "C" {
+
+mrg_status mrg_wavelet(void *X, int nvol, int Nx, int Ny, int Nz, const int levels[3], const int shift[3], int wave_type,
+                       int inverse, void *stream) {
+  if (!X || !levels || !shift || nvol <= 0 || Nx <= 0 || Ny <= 0 || Nz <= 0 || wave_type < 0 || wave_type > 1) {
+    set_error("bad argument");
+    return MRG_ERR_INVALID;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  const int N[3] = {Nx, Ny, Nz};
+  int L[3], ml;
+  wavelet_levels(N, levels, L, &ml);
+  const int wN = wave_type == 0 ? 2 : 4;
+  int sh[3];
+  for (int d = 0; d < 3; d++) sh[d] = ((shift[d] % wN) + wN) % wN;
+  const size_t bytes = sizeof(float2) * (size_t)nvol * Nx * Ny * Nz;
+  DevBuf tmp, dsh;
+  float2 *d;
+  MRG_TRY(view(X, bytes, tmp, st, &d));
+  MRG_CUDA(cudaMalloc(&dsh.p, sizeof(sh)));
+  MRG_CUDA(cudaMemcpyAsync(dsh.p, sh, sizeof(sh), cudaMemcpyHostToDevice, st));
+  MRG_TRY(wavelet3d(d, nvol, N, L, ml, (const int *)dsh.p, wave_type, inverse, st));
+  MRG_TRY(back(X, tmp, bytes, st));
+  MRG_CUDA(cudaStreamSynchronize(st));
+  return MRG_OK;
+}
+
+mrg_status mrg_fraction_threshold(const void *X, int nvol, int64_t nvox, float fraction, float *value, void *stream) {
+  if (!X || !value || nvol <= 0 || nvox <= 0) {
+    set_error("bad argument");
+    return MRG_ERR_INVALID;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  const int64_t n = (int64_t)nvol * nvox;
+  DevBuf tmp, out;
+  float2 *d;
+  MRG_TRY(view(X, sizeof(float2) * n, tmp, st, &d));
+  ThrWork w;
+  mrg_status s = thr_alloc(w, n);
+  if (s == MRG_OK) {
+    MRG_CUDA(cudaMalloc(&out.p, sizeof(float)));
+    s = fraction_threshold(d, n, fraction, 1.0f, w, (float *)out.p, st);
+    if (s == MRG_OK && cudaMemcpyAsync(value, out.p, sizeof(float), cudaMemcpyDeviceToHost, st) != cudaSuccess) s = MRG_ERR_CUDA;
+    if (s == MRG_OK && cudaStreamSynchronize(st) != cudaSuccess) s = MRG_ERR_CUDA;
+  }
+  thr_free(w);
+  return s;
+}
+
+mrg_status mrg_soft_threshold(void *X, int64_t n, float value, void *stream) {
+  if (!X || n <= 0) {
+    set_error("bad argument");
+    return MRG_ERR_INVALID;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  DevBuf tmp, dv;
+  float2 *d;
+  MRG_TRY(view(X, sizeof(float2) * n, tmp, st, &d));
+  MRG_CUDA(cudaMalloc(&dv.p, sizeof(float)));
+  MRG_CUDA(cudaMemcpyAsync(dv.p, &value, sizeof(float), cudaMemcpyHostToDevice, st));
+  MRG_TRY(soft_threshold(d, n, (const float *)dv.p, st));
+  MRG_TRY(back(X, tmp, sizeof(float2) * n, st));
+  MRG_CUDA(cudaStreamSynchronize(st));
+  return MRG_OK;
+}
+
+mrg_status mrg_llr_update_threshold(const void *X, int nframes, int Nx, int Ny, int Nz, const int block[3],
+                                    float clear_amp, float clear_t2, int iteration, float *smax, void *stream) {
+  if (!X || !block || !smax || nframes <= 0 || Nx <= 0 || Ny <= 0 || Nz <= 0) {
+    set_error("bad argument");
+    return MRG_ERR_INVALID;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  const int N[3] = {Nx, Ny, Nz};
+  const size_t bytes = sizeof(float2) * (size_t)nframes * Nx * Ny * Nz;
+  DevBuf tmp;
+  float2 *d;
+  MRG_TRY(view(X, bytes, tmp, st, &d));
+  LlrWork w;
+  mrg_status s = llr_update_ex(d, nframes, N, block, clear_amp, clear_t2, nullptr, iteration, w, st);
+  if (s == MRG_OK && cudaMemcpyAsync(smax, w.smax, sizeof(float), cudaMemcpyDeviceToHost, st) != cudaSuccess) s = MRG_ERR_CUDA;
+  if (s == MRG_OK && cudaStreamSynchronize(st) != cudaSuccess) s = MRG_ERR_CUDA;
+  llr_free(w);
+  return s;
+}
+
+mrg_status mrg_llr_thresh(void *X, int nframes, int Nx, int Ny, int Nz, const int block[3], int block_iter, float alpha,
+                          float smax, int64_t rand_skip, void *stream) {
+  if (!X || !block || nframes <= 0 || Nx <= 0 || Ny <= 0 || Nz <= 0 || block_iter <= 0 || rand_skip < 0) {
+    set_error("bad argument");
+    return MRG_ERR_INVALID;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  const int N[3] = {Nx, Ny, Nz};
+  int bs[3];
+  for (int d = 0; d < 3; d++) bs[d] = std::min(block[d], N[d]);
+  // block shifts in the reference's draw order (clear.cpp:408-415)
+  GlibcRand r;
+  r.skip(rand_skip);
+  std::vector<int> sh(3 * block_iter);
+  for (int it = 0; it < block_iter; it++) {
+    for (int d = 0; d < 3; d++) sh[3 * it + d] = r.next() % bs[d] - bs[d] / 2;
+    if (block_iter == 1) sh[0] = sh[1] = sh[2] = 0;
+  }
+  const size_t bytes = sizeof(float2) * (size_t)nframes * Nx * Ny * Nz;
+  DevBuf tmp, dsh, dsm;
+  float2 *d;
+  MRG_TRY(view(X, bytes, tmp, st, &d));
+  MRG_CUDA(cudaMalloc(&dsh.p, sizeof(int) * sh.size()));
+  MRG_CUDA(cudaMemcpyAsync(dsh.p, sh.data(), sizeof(int) * sh.size(), cudaMemcpyHostToDevice, st));
+  MRG_CUDA(cudaMalloc(&dsm.p, sizeof(float)));
+  MRG_CUDA(cudaMemcpyAsync(dsm.p, &smax, sizeof(float), cudaMemcpyHostToDevice, st));
+  MRG_TRY(llr_apply(d, nframes, N, bs, block_iter, alpha, (const int *)dsh.p, (const float *)dsm.p, st));
+  MRG_TRY(back(X, tmp, bytes, st));
+  MRG_CUDA(cudaStreamSynchronize(st));
+  return MRG_OK;
+}
+
+}  // extern "C"

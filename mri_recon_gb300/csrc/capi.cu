@@ -14,6 +14,7 @@
 //   images [frame][Nz][Ny][Nx]   as the reference's X, R, P, LHS
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <mutex>
 
 #include "mrg_internal.h"
@@ -53,6 +54,11 @@ struct mrg_plan {
   // cached CG graph
   cudaGraphExec_t cg_exec = nullptr;
   void *cg_key[2] = {nullptr, nullptr};
+  // FISTA state
+  ThrWork thr;
+  LlrWork llr;
+  int *d_wshift = nullptr, *d_lshift = nullptr;
+  float *d_thr = nullptr;
 };
 
 // ---------------------------------------------------------------------------
@@ -359,6 +365,11 @@ mrg_status mrg_plan_destroy(mrg_plan *p) {
   cudaFree(p->d_part); cudaFree(p->d_sc); cudaFree(p->d_resid);
   for (int k = 0; k < 4; k++) cudaFree(p->d_stage[k]);
   if (p->cg_exec) cudaGraphExecDestroy(p->cg_exec);
+  thr_free(p->thr);
+  llr_free(p->llr);
+  cudaFree(p->d_wshift);
+  cudaFree(p->d_lshift);
+  cudaFree(p->d_thr);
   delete p;
   return MRG_OK;
 }
@@ -737,6 +748,223 @@ mrg_status mrg_cg(mrg_plan *p, int max_iter, void *X, double *resid, int use_gra
   if (resid || sX) MRG_CUDA(cudaStreamSynchronize(st));
   return MRG_OK;
 }
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// FISTA / IST (src/recon_lib.cpp:1761-2212)
+// ---------------------------------------------------------------------------
+struct FistaCtx {
+  const mrg_fista_params *q;
+  int N[3], L[3], max_level, bs[3];
+  float2 *X;
+};
+
+static mrg_status capture(mrg_plan *p, const std::function<mrg_status(cudaStream_t)> &body, cudaGraphExec_t *exec) {
+  cudaStream_t cs;
+  MRG_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  cudaGraph_t graph;
+  if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+    cudaStreamDestroy(cs);
+    set_error("stream capture failed to start");
+    return MRG_ERR_CUDA;
+  }
+  const mrg_status cap = body(cs);
+  const cudaError_t ee = cudaStreamEndCapture(cs, &graph);
+  cudaStreamDestroy(cs);
+  if (cap != MRG_OK) {
+    if (ee == cudaSuccess) cudaGraphDestroy(graph);
+    return cap;
+  }
+  if (ee != cudaSuccess) {
+    set_error(std::string("stream capture failed: ") + cudaGetErrorString(ee));
+    return MRG_ERR_CUDA;
+  }
+  const cudaError_t ie = cudaGraphInstantiate(exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (ie != cudaSuccess) {
+    *exec = nullptr;
+    set_error(std::string("graph instantiate failed: ") + cudaGetErrorString(ie));
+    return MRG_ERR_CUDA;
+  }
+  (void)p;
+  return MRG_OK;
+}
+
+// One power-iteration step: X = E^H W E X / ||E^H W E X||, step = 1/||.||
+// (src/recon_lib.cpp:1818-1906).
+static mrg_status power_step(mrg_plan *p, float2 *X, cudaStream_t st) {
+  const int64_t n = p->nimg, nt = n * p->T;
+  MRG_TRY(launch_zero(p->d_R, sizeof(float2) * nt, st));
+  for (int t = 0; t < p->T; t++) {
+    MRG_TRY(run_E(p, p->frames[t], X + t * n, plan_smap(p), nullptr, p->d_y, st));
+    MRG_TRY(run_EH(p, p->frames[t], p->d_y, plan_smap(p), p->d_R + t * n, st));
+  }
+  MRG_TRY(energy(p->d_R, nt, p->d_part, p->nblk, &p->d_sc->e, st));
+  MRG_TRY(power_scale(X, p->d_R, nt, p->d_sc, st));
+  return MRG_OK;
+}
+
+static mrg_status fista_iteration(mrg_plan *p, const FistaCtx &f, cudaStream_t st) {
+  const mrg_fista_params &q = *f.q;
+  const int64_t n = p->nimg, nt = n * p->T;
+  float2 *X = f.X;
+  MRG_TRY(fista_momentum(X, p->d_Xo, nt, p->d_sc, q.fista, st));  // fista_update
+  MRG_TRY(launch_zero(p->d_R, sizeof(float2) * nt, st));
+  for (int t = 0; t < p->T; t++) {  // R = E^H W (E x - d)
+    MRG_TRY(run_E(p, p->frames[t], X + t * n, plan_smap(p), p->frames[t].dsorted, p->d_y, st));
+    MRG_TRY(run_EH(p, p->frames[t], p->d_y, plan_smap(p), p->d_R + t * n, st));
+  }
+  MRG_TRY(grad_step(X, p->d_R, nt, p->d_sc, p->d_part, p->nblk, p->d_resid, st));  // X -= step R
+  if (q.llr_alpha > 0.0f) {  // lranktime.update_threshold / thresh (src/recon_lib.cpp:2117-2121)
+    MRG_TRY(llr_update_ex(X, p->T, f.N, f.bs, q.clear_amp, q.clear_t2, p->d_sc, 0, p->llr, st));
+    MRG_TRY(llr_apply_ex(X, p->T, f.N, f.bs, q.llr_block_iter, q.llr_alpha, p->d_lshift, p->d_sc,
+                         3 * q.llr_block_iter, 0, p->llr.smax, st));
+  }
+  if (q.use_threshold) {  // L1_threshold with cycle spinning (src/recon_lib.cpp:2491-2509)
+    const float scale = (float)(1. / (float)q.cycle_spins);
+    for (int spin = 0; spin < q.cycle_spins; spin++) {
+      MRG_TRY(wavelet3d_ex(X, p->T, f.N, f.L, f.max_level, p->d_wshift, p->d_sc, 3 * q.cycle_spins, 3 * spin,
+                           q.wave_type, 0, st));
+      if (spin == 0) MRG_TRY(fraction_threshold(X, nt, q.thresh, scale, p->thr, p->d_thr, st));
+      MRG_TRY(soft_threshold(X, nt, p->d_thr, st));
+      MRG_TRY(wavelet3d_ex(X, p->T, f.N, f.L, f.max_level, p->d_wshift, p->d_sc, 3 * q.cycle_spins, 3 * spin,
+                           q.wave_type, 1, st));
+    }
+  }
+  MRG_TRY(bump_iteration(p->d_sc, st));
+  return MRG_OK;
+}
+
+extern "C" mrg_status mrg_fista(mrg_plan *p, const mrg_fista_params *q, void *X, double *resid, float *step,
+                                int use_graph, void *stream) {
+  if (!p || !q || !X || q->max_iter < 0 || q->max_eig_iter < 0) {
+    set_error("bad argument");
+    return MRG_ERR_INVALID;
+  }
+  if (q->use_threshold && (q->cycle_spins < 1 || q->wave_type < 0 || q->wave_type > 1)) {
+    set_error("bad wavelet / cycle-spin parameters");
+    return MRG_ERR_INVALID;
+  }
+  if (q->llr_alpha > 0.0f && (q->llr_block_iter < 1 || q->llr_block[0] < 1 || q->llr_block[1] < 1 || q->llr_block[2] < 1)) {
+    set_error("bad low-rank block parameters");
+    return MRG_ERR_INVALID;
+  }
+  for (int t = 0; t < p->T; t++) {
+    MRG_TRY(check_frame(p, t));
+    if (!p->frames[t].has_data) {
+      set_error("k-space data not set for a frame");
+      return MRG_ERR_STATE;
+    }
+  }
+  if (p->C > 1 && !p->has_smaps) {
+    set_error("coil maps not set");
+    return MRG_ERR_STATE;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  MRG_TRY(ensure_solver(p, true));
+  MRG_TRY(ensure_resid(p, std::max(q->max_iter, 1)));
+  invalidate_graphs(p);
+  const int64_t n = p->nimg, nt = n * p->T;
+  FistaCtx f;
+  f.q = q;
+  for (int d = 0; d < 3; d++) {
+    f.N[d] = p->geo.N[d];
+    f.bs[d] = std::min(q->llr_block[d], f.N[d]);  // clear.cpp:246-248
+  }
+  wavelet_levels(f.N, q->wave_levels, f.L, &f.max_level);
+  // rand() draws in the reference's order: per iteration the low-rank block
+  // shifts (clear.cpp:408-415), then 3 wavelet shifts per cycle spin
+  // (wavelet3D.cpp:443-448), after the max-eigen seeding draws.
+  GlibcRand rng;
+  rng.skip(q->rand_skip >= 0 ? q->rand_skip : 2 * nt);
+  const int wN = q->wave_type == 0 ? 2 : 4;
+  const int iters = std::max(q->max_iter, 1);
+  std::vector<int> wsh((size_t)iters * 3 * std::max(q->cycle_spins, 1), 0);
+  std::vector<int> lsh((size_t)iters * 3 * std::max(q->llr_block_iter, 1), 0);
+  for (int it = 0; it < q->max_iter; it++) {
+    if (q->llr_alpha > 0.0f)
+      for (int b = 0; b < q->llr_block_iter; b++) {
+        int *s3 = &lsh[((size_t)it * q->llr_block_iter + b) * 3];
+        for (int d = 0; d < 3; d++) s3[d] = rng.next() % f.bs[d] - f.bs[d] / 2;
+        if (q->llr_block_iter == 1) s3[0] = s3[1] = s3[2] = 0;
+      }
+    if (q->use_threshold)
+      for (int sp = 0; sp < q->cycle_spins; sp++)
+        for (int d = 0; d < 3; d++) wsh[((size_t)it * q->cycle_spins + sp) * 3 + d] = rng.next() % wN;
+  }
+  cudaFree(p->d_wshift);
+  cudaFree(p->d_lshift);
+  p->d_wshift = p->d_lshift = nullptr;
+  MRG_CUDA(cudaMalloc(&p->d_wshift, sizeof(int) * wsh.size()));
+  MRG_CUDA(cudaMalloc(&p->d_lshift, sizeof(int) * lsh.size()));
+  MRG_CUDA(cudaMemcpyAsync(p->d_wshift, wsh.data(), sizeof(int) * wsh.size(), cudaMemcpyHostToDevice, st));
+  MRG_CUDA(cudaMemcpyAsync(p->d_lshift, lsh.data(), sizeof(int) * lsh.size(), cudaMemcpyHostToDevice, st));
+  if (!p->d_thr) MRG_CUDA(cudaMalloc(&p->d_thr, sizeof(float)));
+  if (q->use_threshold) MRG_TRY(thr_alloc(p->thr, nt));
+  void *dX;
+  bool sX;
+  MRG_TRY(dev_view(p, 0, X, sizeof(float2) * nt, false, st, &dX, &sX));
+  f.X = (float2 *)dX;
+  Scalars z;
+  memset(&z, 0, sizeof(z));
+  z.step = 1.0f;
+  MRG_CUDA(cudaMemcpyAsync(p->d_sc, &z, sizeof(Scalars), cudaMemcpyHostToDevice, st));
+  // power iteration from the constant seed -0.5-0.5i (std::rand()/RAND_MAX is an
+  // integer division, src/recon_lib.cpp:1809-1811)
+  MRG_TRY(launch_fill(f.X, nt, make_float2(-0.5f, -0.5f), st));
+  if (q->max_eig_iter > 0) {
+    if (use_graph) {
+      cudaGraphExec_t ge = nullptr;
+      MRG_TRY(power_step(p, f.X, st));  // first step eagerly: sets kernel attributes outside capture
+      MRG_CUDA(cudaStreamSynchronize(st));
+      MRG_TRY(capture(p, [&](cudaStream_t cs) { return power_step(p, f.X, cs); }, &ge));
+      mrg_status rs = MRG_OK;
+      for (int it = 1; it < q->max_eig_iter && rs == MRG_OK; it++) {
+        if (cudaGraphLaunch(ge, st) != cudaSuccess) rs = MRG_ERR_CUDA;
+        count_launch();
+      }
+      cudaGraphExecDestroy(ge);
+      if (rs != MRG_OK) {
+        set_error("graph launch failed");
+        return rs;
+      }
+    } else {
+      for (int it = 0; it < q->max_eig_iter; it++) MRG_TRY(power_step(p, f.X, st));
+    }
+  }
+  // X = 0, X_old = 0, iteration counter 0 (step kept)
+  MRG_TRY(launch_zero(f.X, sizeof(float2) * nt, st));
+  MRG_TRY(launch_zero(p->d_Xo, sizeof(float2) * nt, st));
+  MRG_CUDA(cudaMemcpyAsync(&p->d_sc->it, &z.it, sizeof(int), cudaMemcpyHostToDevice, st));
+  MRG_CUDA(cudaStreamSynchronize(st));
+  if (use_graph && q->max_iter > 1) {
+    MRG_TRY(fista_iteration(p, f, st));  // iteration 0 eagerly, then replay the captured iteration
+    MRG_CUDA(cudaStreamSynchronize(st));
+    cudaGraphExec_t ge = nullptr;
+    MRG_TRY(capture(p, [&](cudaStream_t cs) { return fista_iteration(p, f, cs); }, &ge));
+    mrg_status rs = MRG_OK;
+    for (int it = 1; it < q->max_iter && rs == MRG_OK; it++) {
+      if (cudaGraphLaunch(ge, st) != cudaSuccess) rs = MRG_ERR_CUDA;
+      count_launch();
+    }
+    cudaGraphExecDestroy(ge);
+    if (rs != MRG_OK) {
+      set_error("graph launch failed");
+      return rs;
+    }
+  } else {
+    for (int it = 0; it < q->max_iter; it++) MRG_TRY(fista_iteration(p, f, st));
+  }
+  if (resid && q->max_iter > 0)
+    MRG_CUDA(cudaMemcpyAsync(resid, p->d_resid, sizeof(double) * q->max_iter, cudaMemcpyDeviceToHost, st));
+  if (step) MRG_CUDA(cudaMemcpyAsync(step, &p->d_sc->step, sizeof(float), cudaMemcpyDeviceToHost, st));
+  if (sX) MRG_CUDA(cudaMemcpyAsync(X, dX, sizeof(float2) * nt, cudaMemcpyDeviceToHost, st));
+  MRG_CUDA(cudaStreamSynchronize(st));
+  return MRG_OK;
+}
+
+extern "C" {
 
 mrg_status mrg_last_timings(const mrg_plan *p, float out[8]) {
   if (!p || !out) {

@@ -10,17 +10,14 @@
 // One CTA transforms IB lines (consecutive "inner" elements, coalesced rows of
 // IB complex values) of length S = 8*Q held in shared memory as [S][IB+1].
 // Each line is split S = 8 x Q (four-step): 8-point DFTs across the 8 threads
-// of a line, a twiddle, then a Q-point DFT in registers per thread.  Twiddles
-// come from a constant-memory table exp(-2 pi i m / 2304), 2304 being a common
-// multiple of every supported S.
+// of a line, a twiddle, then a Q-point DFT in registers per thread (radices 2,
+// 3, 4, 5).  Twiddles exp(-2 pi i m / S) are computed on the host in double,
+// staged in shared memory per CTA and read as broadcasts.
 #include "mrg_internal.h"
 
 namespace mrg {
 
-constexpr int TW_LCM = 2304;
-__constant__ float2 c_tw[TW_LCM];
-
-static const int kSupportedQ[] = {3, 6, 9, 12, 18, 24, 36, 48};
+static const int kSupportedQ[] = {3, 5, 6, 9, 10, 12, 15, 18, 20, 24, 30, 36, 40, 45, 48};
 
 bool fft_size_supported(int S) {
   if (S % 8) return false;
@@ -29,18 +26,25 @@ bool fft_size_supported(int S) {
   return false;
 }
 
+// Per-size twiddle tables exp(-2 pi i m / S), m < S, built once per device.
+static float2 *g_tw[1024];
+static int g_tw_dev = -1;
+
 mrg_status fft_init_device() {
-  static thread_local int done_dev = -1;
   int dev = 0;
   MRG_CUDA(cudaGetDevice(&dev));
-  if (done_dev == dev) return MRG_OK;
-  std::vector<float2> tw(TW_LCM);
-  for (int m = 0; m < TW_LCM; m++) {
-    double a = -2.0 * 3.141592653589793238462643 * (double)m / (double)TW_LCM;
-    tw[m] = make_float2((float)cos(a), (float)sin(a));
+  if (g_tw_dev == dev) return MRG_OK;
+  for (int q : kSupportedQ) {
+    const int S = 8 * q;
+    std::vector<float2> tw(S);
+    for (int m = 0; m < S; m++) {
+      const double a = -2.0 * 3.141592653589793238462643 * (double)m / (double)S;
+      tw[m] = make_float2((float)cos(a), (float)sin(a));
+    }
+    MRG_CUDA(cudaMalloc(&g_tw[S], sizeof(float2) * S));
+    MRG_CUDA(cudaMemcpy(g_tw[S], tw.data(), sizeof(float2) * S, cudaMemcpyHostToDevice));
   }
-  MRG_CUDA(cudaMemcpyToSymbol(c_tw, tw.data(), sizeof(float2) * TW_LCM));
-  done_dev = dev;
+  g_tw_dev = dev;
   return MRG_OK;
 }
 
@@ -55,8 +59,8 @@ __device__ __forceinline__ float2 imul(float2 a) {
   return SIGN > 0 ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
 }
 template <int SIGN>
-__device__ __forceinline__ float2 twid(int m) {
-  float2 w = c_tw[m];
+__device__ __forceinline__ float2 twid(const float2 *tw, int m) {
+  float2 w = tw[m];
   if (SIGN > 0) w.y = -w.y;
   return w;
 }
@@ -83,16 +87,31 @@ __device__ __forceinline__ void bfly(float2 (&t)[P]) {
     t[2] = csub(a, c);
     t[1] = cadd(b, d);
     t[3] = csub(b, d);
+  } else if constexpr (P == 5) {
+    const float c1 = 0.30901699437494742410f, c2 = -0.80901699437494742410f;
+    const float s1 = 0.95105651629515357212f, s2 = 0.58778525229247312917f;
+    const float2 a1 = cadd(t[1], t[4]), a2 = cadd(t[2], t[3]);
+    const float2 b1 = csub(t[1], t[4]), b2 = csub(t[2], t[3]);
+    const float2 m1 = make_float2(t[0].x + c1 * a1.x + c2 * a2.x, t[0].y + c1 * a1.y + c2 * a2.y);
+    const float2 m2 = make_float2(t[0].x + c2 * a1.x + c1 * a2.x, t[0].y + c2 * a1.y + c1 * a2.y);
+    const float2 r1 = imul<SIGN>(make_float2(s1 * b1.x + s2 * b2.x, s1 * b1.y + s2 * b2.y));
+    const float2 r2 = imul<SIGN>(make_float2(s2 * b1.x - s1 * b2.x, s2 * b1.y - s1 * b2.y));
+    t[0] = cadd(t[0], cadd(a1, a2));
+    t[1] = cadd(m1, r1);
+    t[4] = csub(m1, r1);
+    t[2] = cadd(m2, r2);
+    t[3] = csub(m2, r2);
   } else {
-    static_assert(P == 2 || P == 3 || P == 4, "radix");
+    static_assert(P == 2 || P == 3 || P == 4 || P == 5, "radix");
   }
 }
 
-constexpr int first_factor(int q) { return (q % 4 == 0) ? 4 : ((q % 2 == 0) ? 2 : 3); }
+constexpr int first_factor(int q) { return (q % 4 == 0) ? 4 : ((q % 2 == 0) ? 2 : ((q % 3 == 0) ? 3 : 5)); }
 
-// In-register DFT of length Q (decimation in time), natural order in and out.
-template <int Q, int SIGN>
-__device__ __forceinline__ void reg_fft(float2 (&v)[Q]) {
+// In-register DFT of length Q (decimation in time), natural order in and out;
+// tw is the length-S table, S a multiple of Q.
+template <int Q, int SIGN, int S>
+__device__ __forceinline__ void reg_fft(float2 (&v)[Q], const float2 *tw) {
   if constexpr (Q == 1) {
     return;
   } else {
@@ -104,12 +123,12 @@ __device__ __forceinline__ void reg_fft(float2 (&v)[Q]) {
 #pragma unroll
       for (int m = 0; m < Q2; m++) sub[p][m] = v[p + P * m];
 #pragma unroll
-    for (int p = 0; p < P; p++) reg_fft<Q2, SIGN>(sub[p]);
+    for (int p = 0; p < P; p++) reg_fft<Q2, SIGN, S>(sub[p], tw);
 #pragma unroll
     for (int k = 0; k < Q2; k++) {
       float2 t[P];
 #pragma unroll
-      for (int p = 0; p < P; p++) t[p] = (p * k == 0) ? sub[p][k] : cmul(sub[p][k], twid<SIGN>(p * k * (TW_LCM / Q)));
+      for (int p = 0; p < P; p++) t[p] = (p * k == 0) ? sub[p][k] : cmul(sub[p][k], twid<SIGN>(tw, p * k * (S / Q)));
       bfly<P, SIGN>(t);
 #pragma unroll
       for (int q = 0; q < P; q++) v[k + Q2 * q] = t[q];
@@ -120,9 +139,11 @@ __device__ __forceinline__ void reg_fft(float2 (&v)[Q]) {
 template <int Q, int SIGN, int MODE>
 __global__ void __launch_bounds__(256, 2) k_fft(const FftPass p) {
   constexpr int S = 8 * Q;
-  extern __shared__ float2 sm[];
+  extern __shared__ float2 sm[];  // [S][IB+1] data, then S twiddles
   const int IB = p.IB, IBp = p.IB + 1;
   const int tid = threadIdx.x;
+  float2 *tw = sm + S * IBp;
+  for (int m = tid; m < S; m += blockDim.x) tw[m] = p.tw[m];
   const int j = tid % IB, t = tid / IB;  // 8 threads per line
   const int64_t line = (int64_t)blockIdx.x * IB + j;
   const bool lv = line < p.nlines;
@@ -171,9 +192,9 @@ __global__ void __launch_bounds__(256, 2) k_fft(const FftPass p) {
     float2 a[8];
 #pragma unroll
     for (int n1 = 0; n1 < 8; n1++) a[n1] = sm[(Q * n1 + n2) * IBp + j];
-    reg_fft<8, SIGN>(a);
+    reg_fft<8, SIGN, S>(a, tw);
 #pragma unroll
-    for (int k1 = 1; k1 < 8; k1++) a[k1] = cmul(a[k1], twid<SIGN>(n2 * k1 * (TW_LCM / S)));
+    for (int k1 = 1; k1 < 8; k1++) a[k1] = cmul(a[k1], twid<SIGN>(tw, n2 * k1));
 #pragma unroll
     for (int k1 = 0; k1 < 8; k1++) sm[(Q * k1 + n2) * IBp + j] = a[k1];
   }
@@ -184,7 +205,7 @@ __global__ void __launch_bounds__(256, 2) k_fft(const FftPass p) {
     float2 v[Q];
 #pragma unroll
     for (int n2 = 0; n2 < Q; n2++) v[n2] = sm[(Q * t + n2) * IBp + j];
-    reg_fft<Q, SIGN>(v);
+    reg_fft<Q, SIGN, S>(v, tw);
     __syncthreads();
 #pragma unroll
     for (int k2 = 0; k2 < Q; k2++) sm[(t + 8 * k2) * IBp + j] = v[k2];
@@ -258,7 +279,7 @@ __global__ void __launch_bounds__(256, 2) k_fft(const FftPass p) {
 
 template <int Q>
 static mrg_status launch_q(const FftPass &p, cudaStream_t st) {
-  const size_t smem = (size_t)8 * Q * (p.IB + 1) * sizeof(float2);
+  const size_t smem = (size_t)8 * Q * (p.IB + 2) * sizeof(float2);
   const int64_t nblk64 = (p.nlines + p.IB - 1) / p.IB;
   if (nblk64 > 0x7fffffff) {
     set_error("fft pass too large");
@@ -273,10 +294,12 @@ static mrg_status launch_q(const FftPass &p, cudaStream_t st) {
   static int attr_set[4] = {0, 0, 0, 0};  // per instantiation: set the smem cap once
   const int slot = p.mode == FFT_PLAIN ? (p.sign < 0 ? 0 : 1) : (p.mode == FFT_SETIMG ? 2 : 3);
   if (!attr_set[slot]) {
-    MRG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 8 * Q * 33 * (int)sizeof(float2)));
+    MRG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 8 * Q * 34 * (int)sizeof(float2)));
     attr_set[slot] = 1;
   }
-  fn<<<grid, block, smem, st>>>(p);
+  FftPass pp = p;
+  pp.tw = g_tw[8 * Q];
+  fn<<<grid, block, smem, st>>>(pp);
   MRG_LAUNCHED();
   return MRG_OK;
 }
@@ -297,12 +320,19 @@ mrg_status launch_fft(const FftPass &p, cudaStream_t st) {
   }
   switch (p.S) {
     case 24: return launch_q<3>(p, st);
+    case 40: return launch_q<5>(p, st);
     case 48: return launch_q<6>(p, st);
     case 72: return launch_q<9>(p, st);
+    case 80: return launch_q<10>(p, st);
     case 96: return launch_q<12>(p, st);
+    case 120: return launch_q<15>(p, st);
     case 144: return launch_q<18>(p, st);
+    case 160: return launch_q<20>(p, st);
     case 192: return launch_q<24>(p, st);
+    case 240: return launch_q<30>(p, st);
     case 288: return launch_q<36>(p, st);
+    case 320: return launch_q<40>(p, st);
+    case 360: return launch_q<45>(p, st);
     case 384: return launch_q<48>(p, st);
     default:
       set_error("unsupported FFT length " + std::to_string(p.S));

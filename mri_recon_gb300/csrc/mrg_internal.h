@@ -84,6 +84,7 @@ struct FftPass {
   float scale;
   const float2 *in;
   float2 *out;
+  const float2 *tw;  // set by launch_fft: exp(-2 pi i m / S)
   // FFT_SETIMG: v = (wl[l]*wo[o])*wi[i/C] * X[off/C] * in[off]  (in = smap or NULL)
   // FFT_ACCUM : acc[(l*No + o)*Ni + i/C] += sum_c (wl*wo*wi)*v*conj(smap[...])
   const float2 *X;
@@ -172,7 +173,9 @@ mrg_status grad_step(float2 *X, const float2 *R, int64_t n, const Scalars *sc, d
                      double *resid, cudaStream_t st);
 mrg_status bump_iteration(Scalars *sc, cudaStream_t st);
 
-// wavelet.cu
+// wavelet.cu (shifts[(sc ? sc->it : 0) * per_it + off + axis])
+mrg_status wavelet3d_ex(float2 *X, int nvol, const int N[3], const int L[3], int max_level, const int *shifts,
+                        const Scalars *sc, int per_it, int off, int wave_type, int inverse, cudaStream_t st);
 mrg_status wavelet3d(float2 *X, int nvol, const int N[3], const int L[3], int max_level, const int *shifts_dev,
                      int wave_type, int inverse, cudaStream_t st);
 void wavelet_levels(const int N[3], const int levels_in[3], int L[3], int *max_level);
@@ -202,6 +205,11 @@ mrg_status llr_alloc(LlrWork &w, int nblocks);
 void llr_free(LlrWork &w);
 mrg_status llr_update(const float2 *X, int Nt, const int N[3], const int bs[3], float amp, float t2,
                       const int *iter_dev, LlrWork &w, cudaStream_t st);
+mrg_status llr_update_ex(const float2 *X, int Nt, const int N[3], const int bs[3], float amp, float t2,
+                         const Scalars *sc, int iter_fixed, LlrWork &w, cudaStream_t st);
+mrg_status llr_apply_ex(float2 *X, int Nt, const int N[3], const int bs[3], int block_iter, float alpha,
+                        const int *shifts, const Scalars *sc, int per_it, int off_base, const float *smax_dev,
+                        cudaStream_t st);
 mrg_status llr_apply(float2 *X, int Nt, const int N[3], const int bs[3], int block_iter, float alpha,
                      const int *shifts_dev, const float *smax_dev, cudaStream_t st);
 

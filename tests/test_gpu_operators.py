@@ -156,4 +156,4 @@ def test_errors_do_not_exit(mrg_lib):
     with pytest.raises(m.MrgError, match="STATE"):
         p.forward(0, c["X"])                       # no trajectory yet
     with pytest.raises(m.MrgError, match="UNSUPPORTED"):
-        m.Plan(100, 1, 1)                           # S = 160: radix 5 not built
+        m.Plan(112, 1, 1)                           # S = 176 = 16*11: radix 11 not built
