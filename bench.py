@@ -1,0 +1,385 @@
+#!/usr/bin/env python3
+"""SENSE-CG iterations/s on one GB300 (gridFFT E^H W E + FP64-scalar CG).
+
+Workload: 256^3 image, 32 coils, 3D radial 65536 x 256 (16.8M samples per coil),
+1.5x oversampled grid (384^3), Kaiser-Bessel half width 2.5, density
+compensation |k|^2: the large SENSE-CG configuration.  Seeded synthetic data:
+200-ellipsoid phantom, Gaussian coil maps, k-space from this library's own
+forward operator plus 0.5% complex Gaussian noise.
+
+A step is one CG iteration (all 32 coils: E, E^H, FP64 dots and updates),
+replayed from a captured CUDA graph with every input resident in HBM; each
+iteration touches far more than L2 (the 384^3 x 32 grid alone is 14.5 GB), so
+no flush is needed between steps.  `e2e` is the same metric through the C ABI
+with host buffers: trajectory and k-space copied in, 30 CG iterations, image
+copied back, all inside the timed region.
+
+--impl reference times the CPU restatement of the reference algorithm (the
+oracle; the reference itself cannot be built here) on the host cores: one
+coil's E^H W E per step, scaled to a 32-coil iteration.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "SENSE-CG iter/s at 256³×32 coils, batched vs plain GPU, ≤1e-4 err vs FP64 oracle"
+UNIT = "iter/s"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="cg256")
+    ap.add_argument("--e2e-solves", type=int, default=2)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain per-coil GPU path")
+    return ap.parse_args()
+
+
+def workload(cfg_name):
+    from mri_recon_gb300 import synth
+    c = dict(synth.CONFIGS[cfg_name])
+    N = c["N"]
+    S = 16 * int(np.ceil(1.5 * N / 16))
+    M = c["nproj"] * c["nread"]
+    c.update(S=S, M=M)
+    c["desc"] = ("SENSE-CG %d^3 x %d coils, 3D radial %d x %d (%.1fM samples/coil), %d^3 grid (1.5x), "
+                 "Kaiser-Bessel half width 2.5, DCF |k|^2" % (N, c["coils"], c["nproj"], c["nread"], M / 1e6, S))
+    return c
+
+
+def bytes_model(c, nvalid, npairs):
+    """Algorithmic HBM bytes per launch of each stage (read inputs once, write outputs once)."""
+    N, S, C = c["N"], c["S"], c["coils"]
+    b = 8  # complex64
+    img, smap = N ** 3 * b, N ** 3 * C * b
+    t1, t2, g = N * N * S * C * b, N * S * S * C * b, S ** 3 * C * b
+    y = nvalid * C * b
+    return {
+        "E_zfft_setimg": img + smap + t1,
+        "E_yfft": t1 + t2,
+        "E_xfft": t2 + g,
+        "E_ungrid": g + nvalid * 16 + y,
+        "EH_grid": y + nvalid * 20 + npairs * 4 + g,
+        "EH_xfft": g + t2,
+        "EH_yfft": t2 + t1,
+        "EH_zfft_accum": t1 + smap + 2 * img,
+    }
+
+
+STAGES = ["E_zfft_setimg", "E_yfft", "E_xfft", "E_ungrid", "EH_grid", "EH_xfft", "EH_yfft", "EH_zfft_accum"]
+KERNEL_OF = {"E_zfft_setimg": "k_fft<Q,-1,SETIMG>", "E_yfft": "k_fft<Q,-1,PLAIN>", "E_xfft": "k_fft<Q,-1,PLAIN>",
+             "E_ungrid": "k_ungrid<32>", "EH_grid": "k_grid<16>", "EH_xfft": "k_fft<Q,+1,PLAIN>",
+             "EH_yfft": "k_fft<Q,+1,PLAIN>", "EH_zfft_accum": "k_fft<Q,+1,ACCUM>"}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        try:
+            d = json.load(open(p))
+            for k in ("hbm_gbs", "hbm_GBs", "hbm"):
+                if k in d:
+                    return float(d[k]), "measured"
+        except Exception:
+            pass
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+def ncu_traffic(stage):
+    """DRAM bytes per launch from the committed ncu summary, if one covers this stage."""
+    p = os.path.join(ROOT, "profiles", "ncu_traffic_cg256.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        parts = line.strip().strip("|").split("|")
+        parts = [x.strip() for x in parts]
+        if len(parts) >= 3 and parts[0] == stage:
+            try:
+                return float(parts[2])
+            except ValueError:
+                return None
+    return None
+
+
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.f = None
+
+    def start(self):
+        try:
+            self.f = tempfile.TemporaryFile(mode="w+")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, r[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_sample(c, img, smap0, kx, ky, kz, kw):
+    """One coil's E^H W E at full size with the FP32 CPU restatement (OpenMP, all host threads)."""
+    from oracle import oracle as O
+    O.build()
+    p = O.Plan(c["N"], prec=0)
+    frames = [dict(kx=kx, ky=ky, kz=kz, kw=kw, data=np.zeros((1, 1), np.complex64))]
+    t0 = time.perf_counter()
+    out = p.normal(frames, smap0[None], 0, img)
+    dt = time.perf_counter() - t0
+    return dt, out, O.num_threads()
+
+
+def run_reference(a):
+    """CPU arm: the oracle port of the reference algorithm on the host cores."""
+    import torch.distributed as dist  # noqa: F401
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from mri_recon_gb300 import synth
+    c = workload(a.config)
+    N, C = c["N"], c["coils"]
+    kx, ky, kz, kw = synth.radial_trajectory(N, c["nproj"], c["nread"])
+    img = synth.phantom(N, c["ellipsoids"], seed=c["seed"])
+    smap0 = synth.coil_map(N, C, 0, seed=c["seed"] + 1)
+    times = []
+    threads = 1
+    for s in range(a.warmup + a.steps):
+        dt, _, threads = cpu_sample(c, img, smap0, kx, ky, kz, kw)
+        if s >= a.warmup:
+            times.append(dt * C)
+    ms = 1000.0 * float(np.mean(times))
+    value = 1000.0 / ms
+    sample = "per step: one coil's E^H W E (1 of %d) at %d^3, FP32 CPU restatement, x%d coils = one CG iteration" % (
+        C, N, C)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": {"workload": c["desc"], "parallelism": "replicas"}, "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(a):
+    import torch
+    import torch.distributed as dist
+
+    import mri_recon_gb300 as m
+    from mri_recon_gb300 import synth
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    st = torch.cuda.current_stream()
+    L = m.load()
+
+    c = workload(a.config)
+    N, C, M = c["N"], c["coils"], c["M"]
+    kx, ky, kz, kw = synth.radial_trajectory(N, c["nproj"], c["nread"])
+    img = synth.phantom(N, c["ellipsoids"], seed=c["seed"])
+    smaps = synth.coil_maps_torch(N, C, dev, seed=c["seed"] + 1)
+    plan = m.Plan(N, C, 1)
+    plan.set_traj(0, kx, ky, kz, kw)
+    plan.set_smaps(smaps)
+    x_true = torch.from_numpy(img).to(dev)
+    y = plan.forward(0, x_true)                                    # (C, M) on the device
+    gen = torch.Generator(device=dev).manual_seed(c["seed"])
+    sig = c["noise"] * float(y.abs().max())
+    y += sig * torch.complex(torch.randn(y.shape, generator=gen, device=dev),
+                             torch.randn(y.shape, generator=gen, device=dev))
+    plan.set_data(0, y)
+    torch.cuda.synchronize()
+
+    # --- device-resident timed region: K CG iterations replayed from a graph ---
+    X = torch.empty((1, N, N, N), dtype=torch.complex64, device=dev)
+    plan.cg_init(a.warmup + a.steps + 8, X)
+    plan.cg_iterate(a.warmup, X)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clk = Clocks(local)
+    clk.start()
+    l0 = L.mrg_kernel_launches()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(st)
+    plan.cg_iterate(a.steps, X)
+    e1.record(st)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    ms_total = e0.elapsed_time(e1)
+    launches = L.mrg_kernel_launches() - l0
+    clocks = clk.stop()
+    t = torch.tensor([ms_total], dtype=torch.float64, device=dev)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_total = float(t.item())
+    ms = ms_total / a.steps
+    value = world * a.steps / (ms_total / 1000.0)
+    resid = plan.cg_residuals(a.warmup + a.steps)
+
+    # --- per-stage timing (eager, events between stages) for the roofline ---
+    plan.set_timing(True)
+    plan.cg_iterate(2, X, use_graph=False)
+    torch.cuda.synchronize()
+    tms, calls = plan.timings()
+    plan.set_timing(False)
+    fi = plan.frame_info(0)
+    bm = bytes_model(c, fi["nvalid"], fi["npairs"])
+    per_launch_ms = {s: float(tms[i]) / max(calls, 1) for i, s in enumerate(STAGES)}
+    dom = max(per_launch_ms, key=per_launch_ms.get)
+    peak, peak_kind = peaks()
+    achieved = bm[dom] / (per_launch_ms[dom] / 1000.0) / 1e9
+    iter_bytes = sum(bm.values()) + 9 * N ** 3 * 8
+    roofline = {"bound": "hbm", "kernel": KERNEL_OF[dom], "stage": dom, "achieved": achieved, "peak": peak,
+                "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                "traffic": ncu_traffic(dom), "algorithmic_bytes_per_launch": bm[dom],
+                "launch_ms": per_launch_ms[dom]}
+    iteration_roofline = {"bytes_per_iter": iter_bytes, "achieved_GBs": iter_bytes * value / world / 1e9,
+                          "frac": iter_bytes * value / world / 1e9 / peak, "peak_source": peak_kind,
+                          "stage_ms": per_launch_ms}
+
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+           "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic",
+           "config": {"workload": c["desc"], "N": N, "coils": C, "samples_per_coil": M, "grid": c["S"],
+                      "l2": "inputs larger than L2 (the 384^3 x 32 grid is 14.5 GB)", "parallelism":
+                      "replicas" if world > 1 else "single", "graph": "one CG iteration per CUDA graph replay"},
+           "gpu_launches": int(launches), "roofline": roofline, "iteration_roofline": iteration_roofline,
+           "cg_residual_first_last": [float(resid[0]), float(resid[-1])]}
+    if clocks:
+        out["clocks"] = clocks
+
+    # --- plain per-coil GPU path: one coil per call, as the reference's coil loop ---
+    if not a.no_plain and rank == 0:
+        pp = m.Plan(N, 1, 1)
+        pp.set_traj(0, *[torch.from_numpy(v).to(dev) for v in (kx, ky, kz, kw)])
+        ytmp = torch.empty(M, dtype=torch.complex64, device=dev)
+        Lh = torch.zeros((N, N, N), dtype=torch.complex64, device=dev)
+        P0 = X[0]
+        pp.forward_coil(0, P0, smaps[0], ytmp)
+        pp.adjoint_coil(0, smaps[0], ytmp, Lh)
+        torch.cuda.synchronize()
+        p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        p0.record(st)
+        for cc in range(C):
+            pp.forward_coil(0, P0, smaps[cc], ytmp)
+            pp.adjoint_coil(0, smaps[cc], ytmp, Lh)
+        p1.record(st)
+        torch.cuda.synchronize()
+        plain_ms = p0.elapsed_time(p1)
+        out["plain_gpu"] = {"value": 1000.0 / plain_ms, "unit": UNIT, "ms_per_iter": plain_ms,
+                            "note": "per-coil E then E^H through the C ABI (operators only; CG vector updates "
+                                    "excluded), same kernels with one coil per call",
+                            "batched_over_plain": value / world / (1000.0 / plain_ms)}
+        # parity of the per-coil operator at full size against the FP32 CPU restatement (coil 0)
+        if not a.no_cpu:
+            Lh.zero_()
+            xin = torch.from_numpy(img).to(dev)
+            pp.forward_coil(0, xin, smaps[0], ytmp)
+            pp.adjoint_coil(0, smaps[0], ytmp, Lh)
+            gpu0 = Lh.cpu().numpy()
+            smap0 = smaps[0].cpu().numpy()
+            dt, ref0, threads = cpu_sample(c, img, smap0, kx, ky, kz, kw)
+            cpu_val = 1.0 / (dt * C)
+            out["cpu_baseline"] = {"value": cpu_val, "unit": UNIT, "cores": threads, "kind": "port",
+                                   "sample": "one coil's E^H W E (1 of %d) at %d^3 with the FP32 CPU restatement "
+                                             "(OpenMP), x%d = one CG iteration" % (C, N, C)}
+            err = float(np.linalg.norm(gpu0 - ref0) / np.linalg.norm(ref0))
+            out["parity"] = {"rel_l2_vs_fp32_oracle": err, "scope": "E^H W E, coil 0, %d^3, full trajectory" % N}
+        del pp
+
+    # --- e2e through the C ABI with host buffers ---
+    iters = int(c.get("iters", 30))
+    y_host = y.cpu().pin_memory()
+    traj_host = [torch.from_numpy(v).pin_memory() for v in (kx, ky, kz, kw)]
+    X_host = torch.empty((1, N, N, N), dtype=torch.complex64).pin_memory()
+    del y
+    times = []
+    for s in range(1 + a.e2e_solves):
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        t0 = time.perf_counter()
+        plan.set_traj(0, *traj_host)
+        plan.set_data(0, y_host)
+        plan.cg(iters, X=X_host, use_graph=True)
+        torch.cuda.synchronize()
+        if s > 0:
+            times.append(time.perf_counter() - t0)
+    tt = torch.tensor([max(times)], dtype=torch.float64, device=dev)
+    if world > 1:
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    e2e_val = world * iters / float(tt.item())
+    out["e2e"] = {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(C * M * 8 + 4 * M * 4),
+                  "d2h_bytes_per_step": int(N ** 3 * 8 + iters * 8),
+                  "step": "one %d-iteration solve: trajectory + k-space host->device, set-up, CG, image "
+                          "device->host" % iters}
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)
+
+
+if __name__ == "__main__":
+    main()

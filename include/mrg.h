@@ -92,6 +92,12 @@ mrg_status mrg_set_smaps(mrg_plan *plan, const void *smaps, int64_t coil_stride,
 mrg_status mrg_set_traj(mrg_plan *plan, int frame, const float *kx, const float *ky, const float *kz,
                         const float *kw, int64_t M, void *stream);
 
+/* Sample bookkeeping of one frame after mrg_set_traj: M samples, nvalid of them
+ * contribute (kw != 0 and inside the grid), npairs (sample, tile) pairs and nitems
+ * gridding work items. */
+mrg_status mrg_frame_info(const mrg_plan *plan, int frame, int64_t *M, int64_t *nvalid, int64_t *npairs,
+                          int64_t *nitems);
+
 /* Measured k-space of one frame: ncoil arrays of M complex64, coil c at
  * data + c*coil_stride.  Used by mrg_cg / mrg_fista (data.kdata, src/mri_data.h). */
 mrg_status mrg_set_data(mrg_plan *plan, int frame, const void *data, int64_t coil_stride, void *stream);
@@ -123,6 +129,14 @@ mrg_status mrg_forward_coil(mrg_plan *plan, int frame, const void *X, const void
  * FP64 scalars.  resid (host, may be NULL) receives sum|r|^2 after each iteration.
  * use_graph != 0 captures one iteration as a CUDA graph and replays it. */
 mrg_status mrg_cg(mrg_plan *plan, int max_iter, void *X, double *resid, int use_graph, void *stream);
+
+/* The same loop in three calls, for callers that time or interleave iterations:
+ * mrg_cg_init sets X = 0, R = P = sum_c E^H W d (src/recon_lib.cpp:1537-1573) and reserves
+ * room for max_iter residuals; mrg_cg_iterate runs n more iterations; mrg_cg_residuals
+ * copies the first n residuals to the host.  X must be device memory here. */
+mrg_status mrg_cg_init(mrg_plan *plan, int max_iter, void *X, void *stream);
+mrg_status mrg_cg_iterate(mrg_plan *plan, int n, void *X, int use_graph, void *stream);
+mrg_status mrg_cg_residuals(mrg_plan *plan, double *resid, int n, void *stream);
 
 /* FISTA / IST with L1-wavelet fraction thresholding and optional locally-low-rank
  * thresholding in time (src/recon_lib.cpp:1761-2212, :2416-2527; src/threshold.cpp;
@@ -181,9 +195,15 @@ mrg_status mrg_plan_geometry(const mrg_config *cfg, int Nx, int Ny, int Nz, int 
  * (src/wavelet3D.cpp:443-448, src/clear.cpp:408-410). */
 mrg_status mrg_rand_stream(int64_t skip, int n, int *out);
 
-/* Per-stage device timings of the last operator call (ms): zero, grid, fft, accumulate
- * for E^H and copy, fft, igrid for E, as printed by -time_grid (src/gridFFT.cpp:727-778). */
-mrg_status mrg_last_timings(const mrg_plan *plan, float out[8]);
+/* Per-stage device timing, the -time_grid stages of src/gridFFT.cpp:727-778 split at
+ * this build's kernels.  While enabled, operator calls run eagerly (no graph), each
+ * stage is bracketed by CUDA events and its time accumulated:
+ *   out[0..3] E:   set_image+z FFT, y FFT, x FFT, ungrid (chop_grid_backward)
+ *   out[4..7] E^H: grid (chop_grid_forward), x FFT, y FFT, z FFT+accumulate
+ * mrg_last_timings returns the accumulated ms and the number of operator calls
+ * since the previous read, then resets them. */
+mrg_status mrg_set_timing(mrg_plan *plan, int enable);
+mrg_status mrg_last_timings(mrg_plan *plan, float out[8], int *calls);
 
 /* Number of kernels this library launched since load (process-wide counter). */
 int64_t mrg_kernel_launches(void);

@@ -48,6 +48,8 @@ SIGNATURES = {
     "mrg_set_smaps": (_i, [_vp, _vp, _i64, _vp]),
     "mrg_set_traj": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _i64, _vp]),
     "mrg_set_data": (_i, [_vp, _i, _vp, _i64, _vp]),
+    "mrg_frame_info": (_i, [_vp, _i, ctypes.POINTER(_i64), ctypes.POINTER(_i64), ctypes.POINTER(_i64),
+                            ctypes.POINTER(_i64)]),
     "mrg_adjoint": (_i, [_vp, _i, _vp, _i64, _vp, _vp]),
     "mrg_forward": (_i, [_vp, _i, _vp, _vp, _i64, _vp, _vp]),
     "mrg_normal": (_i, [_vp, _i, _vp, _vp, _vp]),
@@ -63,7 +65,11 @@ SIGNATURES = {
     "mrg_llr_thresh": (_i, [_vp, _i, _i, _i, _i, _ip, _i, _f, _f, _i64, _vp]),
     "mrg_plan_geometry": (_i, [ctypes.POINTER(MrgConfig), _i, _i, _i, _ip, _ip, _fp, _fp, _ip, _fp, _fp]),
     "mrg_rand_stream": (_i, [_i64, _i, _ip]),
-    "mrg_last_timings": (_i, [_vp, _fp]),
+    "mrg_cg_init": (_i, [_vp, _i, _vp, _vp]),
+    "mrg_cg_iterate": (_i, [_vp, _i, _vp, _i, _vp]),
+    "mrg_cg_residuals": (_i, [_vp, _dp, _i, _vp]),
+    "mrg_set_timing": (_i, [_vp, _i]),
+    "mrg_last_timings": (_i, [_vp, _fp, _ip]),
     "mrg_kernel_launches": (_i64, []),
 }
 

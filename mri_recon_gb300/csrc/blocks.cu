@@ -54,9 +54,14 @@ mrg_status mrg_wavelet(void *X, int nvol, int Nx, int Ny, int Nz, const int leve
   const int N[3] = {Nx, Ny, Nz};
   int L[3], ml;
   wavelet_levels(N, levels, L, &ml);
-  const int wN = wave_type == 0 ? 2 : 4;
   int sh[3];
-  for (int d = 0; d < 3; d++) sh[d] = ((shift[d] % wN) + wN) % wN;
+  for (int d = 0; d < 3; d++) {
+    if (shift[d] < 0) {
+      set_error("wavelet shifts must be non-negative (rand() % wN in the reference)");
+      return MRG_ERR_INVALID;
+    }
+    sh[d] = shift[d];
+  }
   const size_t bytes = sizeof(float2) * (size_t)nvol * Nx * Ny * Nz;
   DevBuf tmp, dsh;
   float2 *d;

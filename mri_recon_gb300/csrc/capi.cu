@@ -51,6 +51,9 @@ struct mrg_plan {
   void *d_stage[4] = {nullptr, nullptr, nullptr, nullptr};
   size_t stage_cap[4] = {0, 0, 0, 0};
   float timings[8] = {0};
+  int timing_on = 0, timing_calls = 0;
+  cudaEvent_t tev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  int64_t graph_kernels = 0;  // kernels per replay of cg_exec
   // cached CG graph
   cudaGraphExec_t cg_exec = nullptr;
   void *cg_key[2] = {nullptr, nullptr};
@@ -146,6 +149,26 @@ static int pass_ib(int64_t inner, int C) {
   return C * (32 / C);
 }
 
+// Stage timing (mrg_set_timing): events between the four stages of E or E^H.
+static void tmark(mrg_plan *p, int k, cudaStream_t st) {
+  if (p->timing_on) cudaEventRecord(p->tev[k], st);
+}
+static void tcollect(mrg_plan *p, int base) {
+  if (!p->timing_on) return;
+  cudaEventSynchronize(p->tev[4]);
+  for (int k = 0; k < 4; k++) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, p->tev[k], p->tev[k + 1]);
+    p->timings[base + k] += ms;
+  }
+  if (base == 0) p->timing_calls += 1;
+  if (p->cfg.time_grid) {
+    const float *t = p->timings + base;
+    if (base == 0) printf("Backward::copy+zfft:%.3f,yfft:%.3f,xfft:%.3f,igrid:%.3f ms\n", t[0], t[1], t[2], t[3]);
+    else printf("Forward::grid:%.3f,xfft:%.3f,yfft:%.3f,zfft+accumulate:%.3f ms\n", t[0], t[1], t[2], t[3]);
+  }
+}
+
 // E for one frame: image X -> sorted samples y (minus diff if given).
 // smap: interleaved plan maps when C > 1 or an explicit single-coil map (may be NULL).
 static mrg_status run_E(mrg_plan *p, const FrameTraj &ft, const float2 *X, const float2 *smap, const float2 *diff,
@@ -165,7 +188,9 @@ static mrg_status run_E(mrg_plan *p, const FrameTraj &ft, const float2 *X, const
   a.scale = (float)(1. / std::sqrt((float)Sz));
   a.in = smap; a.smap = smap; a.has_smap = smap != nullptr; a.X = X; a.out = p->d_t1;
   a.wl = wz + g.og[2]; a.wo = wy + g.og[1]; a.wi = wx + g.og[0]; a.C = C;
+  tmark(p, 0, st);
   MRG_TRY(launch_fft(a, st));
+  tmark(p, 1, st);
   // y pass
   FftPass b;
   memset(&b, 0, sizeof(b));
@@ -177,6 +202,7 @@ static mrg_status run_E(mrg_plan *p, const FrameTraj &ft, const float2 *X, const
   b.scale = (float)(1. / std::sqrt((float)Sy));
   b.in = p->d_t1; b.out = p->d_t2; b.C = C;
   MRG_TRY(launch_fft(b, st));
+  tmark(p, 2, st);
   // x pass
   FftPass c;
   memset(&c, 0, sizeof(c));
@@ -188,9 +214,12 @@ static mrg_status run_E(mrg_plan *p, const FrameTraj &ft, const float2 *X, const
   c.scale = (float)(1. / std::sqrt((float)Sx));
   c.in = p->d_t2; c.out = p->d_grid; c.C = C;
   MRG_TRY(launch_fft(c, st));
+  tmark(p, 3, st);
   // ungrid (src/gridFFT.cpp:1166-1322)
   const GridConst gc = grid_const(p);
   MRG_TRY(launch_ungrid(gc, ft, p->d_grid, diff, y, st));
+  tmark(p, 4, st);
+  tcollect(p, 0);
   return MRG_OK;
 }
 
@@ -202,7 +231,9 @@ static mrg_status run_EH(mrg_plan *p, const FrameTraj &ft, const float2 *y, cons
   const int64_t Nx = g.N[0], Ny = g.N[1], Nz = g.N[2], Sx = g.S[0], Sy = g.S[1], Sz = g.S[2];
   const float *wx = p->d_win, *wy = p->d_win + Sx, *wz = p->d_win + Sx + Sy;
   const GridConst gc = grid_const(p);
+  tmark(p, 0, st);
   MRG_TRY(launch_grid(gc, ft, y, p->d_grid, st));  // src/gridFFT.cpp:1009-1164
+  tmark(p, 1, st);
   FftPass a;
   memset(&a, 0, sizeof(a));
   a.S = (int)Sx; a.sign = +1; a.mode = FFT_PLAIN;
@@ -213,6 +244,7 @@ static mrg_status run_EH(mrg_plan *p, const FrameTraj &ft, const float2 *y, cons
   a.scale = (float)(1. / std::sqrt((float)Sx));
   a.in = p->d_grid; a.out = p->d_t2; a.C = C;
   MRG_TRY(launch_fft(a, st));
+  tmark(p, 2, st);
   FftPass b;
   memset(&b, 0, sizeof(b));
   b.S = (int)Sy; b.sign = +1; b.mode = FFT_PLAIN;
@@ -223,6 +255,7 @@ static mrg_status run_EH(mrg_plan *p, const FrameTraj &ft, const float2 *y, cons
   b.scale = (float)(1. / std::sqrt((float)Sy));
   b.in = p->d_t2; b.out = p->d_t1; b.C = C;
   MRG_TRY(launch_fft(b, st));
+  tmark(p, 3, st);
   // z pass with accumulate (src/gridFFT.cpp:926-941)
   FftPass c;
   memset(&c, 0, sizeof(c));
@@ -236,6 +269,8 @@ static mrg_status run_EH(mrg_plan *p, const FrameTraj &ft, const float2 *y, cons
   c.acc_atomic = (c.IB % C) != 0; c.acc_l = Nx * Ny; c.acc_o = Nx;
   c.wl = wz + g.og[2]; c.wo = wy + g.og[1]; c.wi = wx + g.og[0]; c.C = C;
   MRG_TRY(launch_fft(c, st));
+  tmark(p, 4, st);
+  tcollect(p, 4);
   return MRG_OK;
 }
 
@@ -353,6 +388,10 @@ mrg_status mrg_plan_create(const mrg_config *cfg_in, int Nx, int Ny, int Nz, int
     set_error("table upload failed");
     return fail(MRG_ERR_CUDA);
   }
+  if (cfg.time_grid) {
+    const mrg_status ts = mrg_set_timing(p, 1);
+    if (ts != MRG_OK) return fail(ts);
+  }
   *out = p;
   return MRG_OK;
 }
@@ -365,6 +404,8 @@ mrg_status mrg_plan_destroy(mrg_plan *p) {
   cudaFree(p->d_part); cudaFree(p->d_sc); cudaFree(p->d_resid);
   for (int k = 0; k < 4; k++) cudaFree(p->d_stage[k]);
   if (p->cg_exec) cudaGraphExecDestroy(p->cg_exec);
+  for (int k = 0; k < 5; k++)
+    if (p->tev[k]) cudaEventDestroy(p->tev[k]);
   thr_free(p->thr);
   llr_free(p->llr);
   cudaFree(p->d_wshift);
@@ -449,6 +490,17 @@ mrg_status mrg_set_traj(mrg_plan *p, int frame, const float *kx, const float *ky
                      (const float *)dw, M, p->max_pairs, st));
   invalidate_graphs(p);
   MRG_TRY(ensure_y(p, (int64_t)p->frames[frame].nvalid * p->C));
+  return MRG_OK;
+}
+
+mrg_status mrg_frame_info(const mrg_plan *p, int frame, int64_t *M, int64_t *nvalid, int64_t *npairs,
+                          int64_t *nitems) {
+  MRG_TRY(check_frame(p, frame));
+  const FrameTraj &ft = p->frames[frame];
+  if (M) *M = ft.M;
+  if (nvalid) *nvalid = ft.nvalid;
+  if (npairs) *npairs = ft.npairs;
+  if (nitems) *nitems = ft.nitems;
   return MRG_OK;
 }
 
@@ -634,6 +686,8 @@ mrg_status mrg_forward_coil(mrg_plan *p, int frame, const void *X, const void *s
   return MRG_OK;
 }
 
+static mrg_status capture(mrg_plan *p, const std::function<mrg_status(cudaStream_t)> &body, cudaGraphExec_t *exec);
+
 // ---------------------------------------------------------------------------
 // SENSE-CG (src/recon_lib.cpp:1523-1759)
 // ---------------------------------------------------------------------------
@@ -673,11 +727,7 @@ static mrg_status cg_iteration(mrg_plan *p, float2 *X, cudaStream_t st) {
   return MRG_OK;
 }
 
-mrg_status mrg_cg(mrg_plan *p, int max_iter, void *X, double *resid, int use_graph, void *stream) {
-  if (!p || !X || max_iter < 0) {
-    set_error("bad argument");
-    return MRG_ERR_INVALID;
-  }
+static mrg_status cg_ready(mrg_plan *p) {
   for (int t = 0; t < p->T; t++) {
     MRG_TRY(check_frame(p, t));
     if (!p->frames[t].has_data) {
@@ -689,14 +739,24 @@ mrg_status mrg_cg(mrg_plan *p, int max_iter, void *X, double *resid, int use_gra
     set_error("coil maps not set");
     return MRG_ERR_STATE;
   }
+  return MRG_OK;
+}
+
+mrg_status mrg_cg_init(mrg_plan *p, int max_iter, void *X, void *stream) {
+  if (!p || !X || max_iter < 0) {
+    set_error("bad argument");
+    return MRG_ERR_INVALID;
+  }
+  if (!is_device_ptr(X)) {
+    set_error("mrg_cg_init needs X in device memory (mrg_cg stages host buffers)");
+    return MRG_ERR_INVALID;
+  }
+  MRG_TRY(cg_ready(p));
   cudaStream_t st = (cudaStream_t)stream;
   MRG_TRY(ensure_solver(p, false));
-  MRG_TRY(ensure_resid(p, max_iter));
+  MRG_TRY(ensure_resid(p, std::max(max_iter, 1)));
   const int64_t n = p->nimg, nt = n * p->T;
-  void *dX;
-  bool sX;
-  MRG_TRY(dev_view(p, 0, X, sizeof(float2) * nt, false, st, &dX, &sX));
-  float2 *Xd = (float2 *)dX;
+  float2 *Xd = (float2 *)X;
   // R = sum_c E^H W d, P = R, X = 0  (src/recon_lib.cpp:1537-1573)
   MRG_TRY(launch_zero(Xd, sizeof(float2) * nt, st));
   MRG_TRY(launch_zero(p->d_R, sizeof(float2) * nt, st));
@@ -707,45 +767,91 @@ mrg_status mrg_cg(mrg_plan *p, int max_iter, void *X, double *resid, int use_gra
   memset(&z, 0, sizeof(z));
   MRG_CUDA(cudaMemcpyAsync(p->d_sc, &z, sizeof(Scalars), cudaMemcpyHostToDevice, st));
   MRG_CUDA(cudaStreamSynchronize(st));
-  if (use_graph && max_iter > 0) {
-    if (!p->cg_exec || p->cg_key[0] != dX) {
+  return MRG_OK;
+}
+
+mrg_status mrg_cg_iterate(mrg_plan *p, int nit, void *X, int use_graph, void *stream) {
+  if (!p || !X || nit < 0) {
+    set_error("bad argument");
+    return MRG_ERR_INVALID;
+  }
+  if (!p->d_R) {
+    set_error("mrg_cg_init not called");
+    return MRG_ERR_STATE;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  float2 *Xd = (float2 *)X;
+  if (use_graph && !p->timing_on && nit > 0) {
+    if (!p->cg_exec || p->cg_key[0] != X) {
       invalidate_graphs(p);
-      cudaStream_t cs;
-      MRG_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
-      cudaGraph_t graph;
-      if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
-        cudaStreamDestroy(cs);
-        set_error("stream capture failed to start");
-        return MRG_ERR_CUDA;
-      }
-      const mrg_status cap = cg_iteration(p, Xd, cs);
-      const cudaError_t ee = cudaStreamEndCapture(cs, &graph);
-      cudaStreamDestroy(cs);
-      if (cap != MRG_OK) return cap;
-      if (ee != cudaSuccess) {
-        set_error(std::string("stream capture failed: ") + cudaGetErrorString(ee));
-        return MRG_ERR_CUDA;
-      }
-      const cudaError_t ie = cudaGraphInstantiate(&p->cg_exec, graph, 0);
-      cudaGraphDestroy(graph);
-      if (ie != cudaSuccess) {
-        p->cg_exec = nullptr;
-        set_error(std::string("graph instantiate failed: ") + cudaGetErrorString(ie));
-        return MRG_ERR_CUDA;
-      }
-      p->cg_key[0] = dX;
+      const int64_t before = g_launches.load();
+      MRG_TRY(capture(p, [&](cudaStream_t cs) { return cg_iteration(p, Xd, cs); }, &p->cg_exec));
+      p->graph_kernels = g_launches.load() - before;  // captured, not launched
+      g_launches.fetch_sub(p->graph_kernels);
+      p->cg_key[0] = X;
     }
-    for (int it = 0; it < max_iter; it++) {
+    for (int it = 0; it < nit; it++) {
       MRG_CUDA(cudaGraphLaunch(p->cg_exec, st));
-      count_launch();
+      count_launch((int)p->graph_kernels);
     }
   } else {
-    for (int it = 0; it < max_iter; it++) MRG_TRY(cg_iteration(p, Xd, st));
+    for (int it = 0; it < nit; it++) MRG_TRY(cg_iteration(p, Xd, st));
   }
-  if (resid && max_iter > 0)
-    MRG_CUDA(cudaMemcpyAsync(resid, p->d_resid, sizeof(double) * max_iter, cudaMemcpyDeviceToHost, st));
+  return MRG_OK;
+}
+
+mrg_status mrg_cg_residuals(mrg_plan *p, double *resid, int n, void *stream) {
+  if (!p || (n > 0 && !resid) || n < 0 || n > p->resid_cap) {
+    set_error("bad argument");
+    return MRG_ERR_INVALID;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  if (n > 0) MRG_CUDA(cudaMemcpyAsync(resid, p->d_resid, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+  MRG_CUDA(cudaStreamSynchronize(st));
+  return MRG_OK;
+}
+
+mrg_status mrg_cg(mrg_plan *p, int max_iter, void *X, double *resid, int use_graph, void *stream) {
+  if (!p || !X || max_iter < 0) {
+    set_error("bad argument");
+    return MRG_ERR_INVALID;
+  }
+  MRG_TRY(cg_ready(p));
+  cudaStream_t st = (cudaStream_t)stream;
+  const int64_t nt = p->nimg * p->T;
+  void *dX;
+  bool sX;
+  MRG_TRY(dev_view(p, 0, X, sizeof(float2) * nt, false, st, &dX, &sX));
+  MRG_TRY(mrg_cg_init(p, max_iter, dX, stream));
+  MRG_TRY(mrg_cg_iterate(p, max_iter, dX, use_graph, stream));
+  if (resid && max_iter > 0) MRG_TRY(mrg_cg_residuals(p, resid, max_iter, stream));
   if (sX) MRG_CUDA(cudaMemcpyAsync(X, dX, sizeof(float2) * nt, cudaMemcpyDeviceToHost, st));
-  if (resid || sX) MRG_CUDA(cudaStreamSynchronize(st));
+  MRG_CUDA(cudaStreamSynchronize(st));
+  return MRG_OK;
+}
+
+mrg_status mrg_set_timing(mrg_plan *p, int enable) {
+  if (!p) {
+    set_error("null plan");
+    return MRG_ERR_INVALID;
+  }
+  if (enable && !p->tev[0])
+    for (int k = 0; k < 5; k++) MRG_CUDA(cudaEventCreate(&p->tev[k]));
+  p->timing_on = enable ? 1 : 0;
+  memset(p->timings, 0, sizeof(p->timings));
+  p->timing_calls = 0;
+  return MRG_OK;
+}
+
+mrg_status mrg_last_timings(mrg_plan *p, float out[8], int *calls) {
+  if (!p || !out) {
+    set_error("null argument");
+    return MRG_ERR_INVALID;
+  }
+  memcpy(out, p->timings, sizeof(p->timings));
+  if (calls) *calls = p->timing_calls;
+  memset(p->timings, 0, sizeof(p->timings));
+  p->timing_calls = 0;
   return MRG_OK;
 }
 
@@ -965,15 +1071,6 @@ extern "C" mrg_status mrg_fista(mrg_plan *p, const mrg_fista_params *q, void *X,
 }
 
 extern "C" {
-
-mrg_status mrg_last_timings(const mrg_plan *p, float out[8]) {
-  if (!p || !out) {
-    set_error("null argument");
-    return MRG_ERR_INVALID;
-  }
-  memcpy(out, p->timings, sizeof(p->timings));
-  return MRG_OK;
-}
 
 void mrg_fista_params_default(mrg_fista_params *q) {
   if (!q) return;

@@ -99,7 +99,8 @@ __global__ void __launch_bounds__(256) k_wave(const WaveArgs a) {
       const int p = (o < h) ? o : o - h;
       const float *flt = (o < h) ? a.f.lpf : a.f.hpf;
       for (int f = 0; f < wN; f++) {
-        const int c = ((2 * p - f + S) + L) % L;
+        int c = (2 * p - f + S) % L;
+        if (c < 0) c += L;
         const float2 v = sm[c * 33 + jj];
         acc.x += flt[f] * v.x;
         acc.y += flt[f] * v.y;

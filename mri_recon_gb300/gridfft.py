@@ -128,6 +128,12 @@ class Plan:
                                             a.ptr(kz, np.float32), a.ptr(kw, np.float32), M, _stream(stream)))
         self.M[frame] = M
 
+    def frame_info(self, frame):
+        """dict(M, nvalid, npairs, nitems) of a frame after set_traj."""
+        v = [ctypes.c_int64() for _ in range(4)]
+        _lib.check(_lib.load().mrg_frame_info(self._h, frame, *[ctypes.byref(x) for x in v]))
+        return dict(zip(("M", "nvalid", "npairs", "nitems"), (x.value for x in v)))
+
     def set_data(self, frame, data, stream=None):
         """data: (C, M) complex64."""
         a = _Args()
@@ -193,6 +199,28 @@ class Plan:
         _lib.check(_lib.load().mrg_cg(self._h, iters, a.ptr(X), resid.ctypes.data_as(_lib._dp), int(bool(use_graph)),
                                       _stream(stream)))
         return X, resid[:iters]
+
+    def cg_init(self, max_iter, X, stream=None):
+        """X (device tensor, nframes images) = 0; R = P = E^H W d."""
+        _lib.check(_lib.load().mrg_cg_init(self._h, max_iter, X.data_ptr(), _stream(stream)))
+
+    def cg_iterate(self, n, X, use_graph=True, stream=None):
+        _lib.check(_lib.load().mrg_cg_iterate(self._h, n, X.data_ptr(), int(bool(use_graph)), _stream(stream)))
+
+    def cg_residuals(self, n, stream=None):
+        r = np.zeros(max(n, 1), np.float64)
+        _lib.check(_lib.load().mrg_cg_residuals(self._h, r.ctypes.data_as(_lib._dp), n, _stream(stream)))
+        return r[:n]
+
+    def set_timing(self, on):
+        _lib.check(_lib.load().mrg_set_timing(self._h, int(bool(on))))
+
+    def timings(self):
+        """Accumulated per-stage ms since the last read: (E[4], E^H[4]), number of E calls."""
+        out = np.zeros(8, np.float32)
+        calls = ctypes.c_int()
+        _lib.check(_lib.load().mrg_last_timings(self._h, out.ctypes.data_as(_lib._fp), ctypes.byref(calls)))
+        return out, calls.value
 
     def fista(self, params, X=None, use_graph=True, stream=None):
         a = _Args()

@@ -121,6 +121,51 @@ def coil_maps(N, ncoils, seed=99, sigma=0.4, radius=0.6):
     return out
 
 
+def coil_map(N, ncoils, c, seed=99, sigma=0.4, radius=0.6, normalise=True):
+    """Coil c of coil_maps(N, ncoils, seed), computed alone (complex64 (N, N, N))."""
+    g = _rng(seed)
+    centres = fibonacci_sphere(ncoils) * radius
+    phases = g.uniform(0, 2 * np.pi, ncoils)
+    x = (np.arange(N, dtype=np.float64) - N / 2) / N
+    sos = np.zeros((N, N, N), np.float64) if normalise else None
+    m_c = None
+    for k in range(ncoils) if normalise else [c]:
+        gx = np.exp(-((x - centres[k, 0]) ** 2) / (2 * sigma ** 2))
+        gy = np.exp(-((x - centres[k, 1]) ** 2) / (2 * sigma ** 2))
+        gz = np.exp(-((x - centres[k, 2]) ** 2) / (2 * sigma ** 2))
+        m = gz[:, None, None] * gy[None, :, None] * gx[None, None, :]
+        if normalise:
+            sos += m * m
+        if k == c:
+            m_c = m
+    out = (m_c * np.exp(1j * phases[c])).astype(np.complex64)
+    if normalise:
+        out /= np.sqrt(sos).astype(np.float32)
+    return out
+
+
+def coil_maps_torch(N, ncoils, device, seed=99, sigma=0.4, radius=0.6):
+    """coil_maps() evaluated on a torch device (same formula and seed)."""
+    import torch
+    g = _rng(seed)
+    centres = torch.tensor(fibonacci_sphere(ncoils) * radius, dtype=torch.float64, device=device)
+    phases = torch.tensor(g.uniform(0, 2 * np.pi, ncoils), dtype=torch.float64, device=device)
+    x = (torch.arange(N, dtype=torch.float64, device=device) - N / 2) / N
+    gx = torch.exp(-((x[None, :] - centres[:, 0:1]) ** 2) / (2 * sigma ** 2))   # (C, N)
+    gy = torch.exp(-((x[None, :] - centres[:, 1:2]) ** 2) / (2 * sigma ** 2))
+    gz = torch.exp(-((x[None, :] - centres[:, 2:3]) ** 2) / (2 * sigma ** 2))
+    sos = torch.zeros((N, N, N), dtype=torch.float64, device=device)
+    for c in range(ncoils):
+        sos += (gz[c][:, None, None] * gy[c][None, :, None] * gx[c][None, None, :]) ** 2
+    rs = (1.0 / torch.sqrt(sos)).to(torch.float32)
+    out = torch.empty((ncoils, N, N, N), dtype=torch.complex64, device=device)
+    for c in range(ncoils):
+        m = (gz[c][:, None, None] * gy[c][None, :, None] * gx[c][None, None, :]).to(torch.float32) * rs
+        ph = torch.polar(torch.ones((), dtype=torch.float64, device=device), phases[c]).to(torch.complex64)
+        out[c] = m.to(torch.complex64) * ph
+    return out
+
+
 def nudft(img, kx, ky, kz, chunk=8192):
     """FP64 direct NUDFT y(k) = sum_r img(r) exp(-2 pi i k.(r - N/2)/N).
 

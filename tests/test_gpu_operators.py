@@ -9,6 +9,13 @@ pytestmark = pytest.mark.gpu
 TOL = 1e-5
 
 
+def fp64_bound(ref32, ref64):
+    """Against the FP64 twin the GPU may not be closer than the reference's own
+    FP32 arithmetic is: when the grid ratio S/N is not representable in float
+    (e.g. 80/48) the FP32 reference itself sits ~1.7e-5 from FP64."""
+    return max(TOL, 1.25 * rel(ref32, ref64))
+
+
 def _torch():
     import torch
     return torch
@@ -43,8 +50,9 @@ def test_forward_E_matches_oracle(mrg_lib, oracle_lib, N, C, nproj):
     p = _plan(mrg_lib, c)
     X = torch.from_numpy(c["X"]).cuda()
     y = p.forward(0, X).cpu().numpy()
-    assert rel(y, _oracle_E(oracle_lib, c, 0)) < TOL
-    assert rel(y, _oracle_E(oracle_lib, c, 1)) < TOL
+    r32, r64 = _oracle_E(oracle_lib, c, 0), _oracle_E(oracle_lib, c, 1)
+    assert rel(y, r32) < TOL
+    assert rel(y, r64) < fp64_bound(r32, r64)
 
 
 def test_forward_residual_matches_oracle(mrg_lib, oracle_lib):
@@ -63,8 +71,9 @@ def test_adjoint_EH_matches_oracle(mrg_lib, oracle_lib, N, C, nproj):
     X = torch.zeros(c["X"].shape, dtype=torch.complex64, device="cuda")
     p.adjoint(0, torch.from_numpy(c["data"]).cuda(), X)
     got = X.cpu().numpy()
-    assert rel(got, _oracle_EH(oracle_lib, c, 0)) < TOL
-    assert rel(got, _oracle_EH(oracle_lib, c, 1)) < TOL
+    r32, r64 = _oracle_EH(oracle_lib, c, 0), _oracle_EH(oracle_lib, c, 1)
+    assert rel(got, r32) < TOL
+    assert rel(got, r64) < fp64_bound(r32, r64)
 
 
 def test_adjoint_accumulates_into_X(mrg_lib, oracle_lib):
