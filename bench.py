@@ -164,11 +164,12 @@ class Clocks:
                 "samples": len(sm)}
 
 
-def cpu_sample(c, img, smap0, kx, ky, kz, kw):
-    """One coil's E^H W E at full size with the FP32 CPU restatement (OpenMP, all host threads)."""
+def cpu_sample(c, img, smap0, kx, ky, kz, kw, prec=0):
+    """One coil's E^H W E at full size with the CPU restatement (OpenMP, all host threads);
+    prec 0 is the FP32 restatement (the timed baseline), 1 its FP64 twin."""
     from oracle import oracle as O
     O.build()
-    p = O.Plan(c["N"], prec=0)
+    p = O.Plan(c["N"], prec=prec)
     frames = [dict(kx=kx, ky=ky, kz=kz, kw=kw, data=np.zeros((1, 1), np.complex64))]
     t0 = time.perf_counter()
     out = p.normal(frames, smap0[None], 0, img)
@@ -336,8 +337,13 @@ def run_ours(a):
             out["cpu_baseline"] = {"value": cpu_val, "unit": UNIT, "cores": threads, "kind": "port",
                                    "sample": "one coil's E^H W E (1 of %d) at %d^3 with the FP32 CPU restatement "
                                              "(OpenMP), x%d = one CG iteration" % (C, N, C)}
-            err = float(np.linalg.norm(gpu0 - ref0) / np.linalg.norm(ref0))
-            out["parity"] = {"rel_l2_vs_fp32_oracle": err, "scope": "E^H W E, coil 0, %d^3, full trajectory" % N}
+            _, ref64, _ = cpu_sample(c, img, smap0, kx, ky, kz, kw, prec=1)
+
+            def rl(a, b):
+                return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+            out["parity"] = {"rel_l2_vs_fp32_oracle": rl(gpu0, ref0), "rel_l2_vs_fp64_oracle": rl(gpu0, ref64),
+                             "fp32_oracle_vs_fp64_oracle": rl(ref0, ref64),
+                             "scope": "E^H W E, coil 0, %d^3, full trajectory" % N}
         del pp
 
     # --- e2e through the C ABI with host buffers ---

@@ -78,6 +78,9 @@ static GridConst grid_const(const mrg_plan *p) {
     g.lut[d] = p->d_lut + (size_t)d * p->geo.lut_len;
     g.nt[d] = p->geo.S[d] / p->B;
   }
+  g.nb[0] = p->geo.S[0] / BLK_X;
+  g.nb[1] = p->geo.S[1] / BLK_Y;
+  g.nb[2] = p->geo.S[2] / BLK_Z;
   g.k_rad = p->geo.k_rad;
   g.B = p->B;
   g.C = p->C;
@@ -169,10 +172,11 @@ static void tcollect(mrg_plan *p, int base) {
   }
 }
 
-// E for one frame: image X -> sorted samples y (minus diff if given).
+// E for one frame: image X -> sorted samples y (minus diff if given); with
+// `weigh` the samples come out multiplied by kw and the taper, ready for run_EH.
 // smap: interleaved plan maps when C > 1 or an explicit single-coil map (may be NULL).
 static mrg_status run_E(mrg_plan *p, const FrameTraj &ft, const float2 *X, const float2 *smap, const float2 *diff,
-                        float2 *y, cudaStream_t st) {
+                        float2 *y, bool weigh, cudaStream_t st) {
   const Geometry &g = p->geo;
   const int C = p->C;
   const int64_t Nx = g.N[0], Ny = g.N[1], Nz = g.N[2], Sx = g.S[0], Sy = g.S[1], Sz = g.S[2];
@@ -217,13 +221,13 @@ static mrg_status run_E(mrg_plan *p, const FrameTraj &ft, const float2 *X, const
   tmark(p, 3, st);
   // ungrid (src/gridFFT.cpp:1166-1322)
   const GridConst gc = grid_const(p);
-  MRG_TRY(launch_ungrid(gc, ft, p->d_grid, diff, y, st));
+  MRG_TRY(launch_ungrid(gc, ft, p->d_grid, diff, y, weigh, st));
   tmark(p, 4, st);
   tcollect(p, 0);
   return MRG_OK;
 }
 
-// E^H for one frame: sorted samples y -> X += ...
+// E^H for one frame: weighted sorted samples yw (data * kw * taper) -> X += ...
 static mrg_status run_EH(mrg_plan *p, const FrameTraj &ft, const float2 *y, const float2 *smap, float2 *X,
                          cudaStream_t st) {
   const Geometry &g = p->geo;
@@ -547,7 +551,7 @@ mrg_status mrg_adjoint(mrg_plan *p, int frame, const void *data, int64_t coil_st
   bool sd, sX;
   MRG_TRY(dev_view(p, 0, data, sizeof(float2) * (size_t)(coil_stride * (p->C - 1) + ft.M), true, st, &dd, &sd));
   MRG_TRY(dev_view(p, 1, X, sizeof(float2) * p->nimg, true, st, &dX, &sX));
-  MRG_TRY(launch_gather_samples(ft, p->C, (const float2 *)dd, coil_stride, p->d_y, st));
+  MRG_TRY(launch_gather_samples(ft, p->C, (const float2 *)dd, coil_stride, p->d_y, st, true));
   MRG_TRY(run_EH(p, ft, p->d_y, plan_smap(p), (float2 *)dX, st));
   if (sX) {
     MRG_CUDA(cudaMemcpyAsync(X, dX, sizeof(float2) * p->nimg, cudaMemcpyDeviceToHost, st));
@@ -587,7 +591,7 @@ mrg_status mrg_forward(mrg_plan *p, int frame, const void *X, void *data, int64_
     dsort = p->d_y + ny;
     MRG_TRY(launch_gather_samples(ft, p->C, (const float2 *)ddf, coil_stride, dsort, st));
   }
-  MRG_TRY(run_E(p, ft, (const float2 *)dX, plan_smap(p), dsort, p->d_y, st));
+  MRG_TRY(run_E(p, ft, (const float2 *)dX, plan_smap(p), dsort, p->d_y, false, st));
   MRG_TRY(launch_scatter_samples(ft, p->C, p->d_y, (float2 *)dd, coil_stride, st));
   if (sd) {
     MRG_CUDA(cudaMemcpyAsync(data, dd, dbytes, cudaMemcpyDeviceToHost, st));
@@ -613,7 +617,7 @@ mrg_status mrg_normal(mrg_plan *p, int frame, const void *X, void *out, void *st
   MRG_TRY(dev_view(p, 1, out, sizeof(float2) * p->nimg, false, st, &dO, &sO));
   const FrameTraj &ft = p->frames[frame];
   MRG_TRY(launch_zero(dO, sizeof(float2) * p->nimg, st));
-  MRG_TRY(run_E(p, ft, (const float2 *)dX, plan_smap(p), nullptr, p->d_y, st));
+  MRG_TRY(run_E(p, ft, (const float2 *)dX, plan_smap(p), nullptr, p->d_y, true, st));
   MRG_TRY(run_EH(p, ft, p->d_y, plan_smap(p), (float2 *)dO, st));
   if (sO) {
     MRG_CUDA(cudaMemcpyAsync(out, dO, sizeof(float2) * p->nimg, cudaMemcpyDeviceToHost, st));
@@ -639,7 +643,7 @@ mrg_status mrg_adjoint_coil(mrg_plan *p, int frame, const void *smap, const void
   MRG_TRY(dev_view(p, 0, data, sizeof(float2) * (size_t)ft.M, true, st, &dd, &sd));
   MRG_TRY(dev_view(p, 1, X, sizeof(float2) * p->nimg, true, st, &dX, &sX));
   MRG_TRY(dev_view(p, 2, smap, sizeof(float2) * p->nimg, true, st, &ds, &ss));
-  MRG_TRY(launch_gather_samples(ft, 1, (const float2 *)dd, 0, p->d_y, st));
+  MRG_TRY(launch_gather_samples(ft, 1, (const float2 *)dd, 0, p->d_y, st, true));
   MRG_TRY(run_EH(p, ft, p->d_y, (const float2 *)ds, (float2 *)dX, st));
   if (sX) {
     MRG_CUDA(cudaMemcpyAsync(X, dX, sizeof(float2) * p->nimg, cudaMemcpyDeviceToHost, st));
@@ -677,7 +681,7 @@ mrg_status mrg_forward_coil(mrg_plan *p, int frame, const void *X, const void *s
     dsort = p->d_y + ny;
     MRG_TRY(launch_gather_samples(ft, 1, (const float2 *)ddf, 0, dsort, st));
   }
-  MRG_TRY(run_E(p, ft, (const float2 *)dX, (const float2 *)ds, dsort, p->d_y, st));
+  MRG_TRY(run_E(p, ft, (const float2 *)dX, (const float2 *)ds, dsort, p->d_y, false, st));
   MRG_TRY(launch_scatter_samples(ft, 1, p->d_y, (float2 *)dd, 0, st));
   if (sd) {
     MRG_CUDA(cudaMemcpyAsync(data, dd, dbytes, cudaMemcpyDeviceToHost, st));
@@ -718,7 +722,7 @@ static mrg_status cg_iteration(mrg_plan *p, float2 *X, cudaStream_t st) {
     const FrameTraj &ft = p->frames[t];
     float2 *Lt = p->d_L + t * n;
     MRG_TRY(launch_zero(Lt, sizeof(float2) * n, st));
-    MRG_TRY(run_E(p, ft, p->d_P + t * n, plan_smap(p), nullptr, p->d_y, st));
+    MRG_TRY(run_E(p, ft, p->d_P + t * n, plan_smap(p), nullptr, p->d_y, true, st));
     MRG_TRY(run_EH(p, ft, p->d_y, plan_smap(p), Lt, st));
   }
   MRG_TRY(cg_dots(p->d_R, p->d_P, p->d_L, nt, p->d_part, p->nblk, p->d_sc, st));
@@ -760,8 +764,10 @@ mrg_status mrg_cg_init(mrg_plan *p, int max_iter, void *X, void *stream) {
   // R = sum_c E^H W d, P = R, X = 0  (src/recon_lib.cpp:1537-1573)
   MRG_TRY(launch_zero(Xd, sizeof(float2) * nt, st));
   MRG_TRY(launch_zero(p->d_R, sizeof(float2) * nt, st));
-  for (int t = 0; t < p->T; t++)
-    MRG_TRY(run_EH(p, p->frames[t], p->frames[t].dsorted, plan_smap(p), p->d_R + t * n, st));
+  for (int t = 0; t < p->T; t++) {
+    MRG_TRY(launch_weigh_samples(p->frames[t], p->C, p->frames[t].dsorted, p->d_y, st));
+    MRG_TRY(run_EH(p, p->frames[t], p->d_y, plan_smap(p), p->d_R + t * n, st));
+  }
   MRG_TRY(launch_copy(p->d_P, p->d_R, nt, st));
   Scalars z;
   memset(&z, 0, sizeof(z));
@@ -903,7 +909,7 @@ static mrg_status power_step(mrg_plan *p, float2 *X, cudaStream_t st) {
   const int64_t n = p->nimg, nt = n * p->T;
   MRG_TRY(launch_zero(p->d_R, sizeof(float2) * nt, st));
   for (int t = 0; t < p->T; t++) {
-    MRG_TRY(run_E(p, p->frames[t], X + t * n, plan_smap(p), nullptr, p->d_y, st));
+    MRG_TRY(run_E(p, p->frames[t], X + t * n, plan_smap(p), nullptr, p->d_y, true, st));
     MRG_TRY(run_EH(p, p->frames[t], p->d_y, plan_smap(p), p->d_R + t * n, st));
   }
   MRG_TRY(energy(p->d_R, nt, p->d_part, p->nblk, &p->d_sc->e, st));
@@ -918,7 +924,7 @@ static mrg_status fista_iteration(mrg_plan *p, const FistaCtx &f, cudaStream_t s
   MRG_TRY(fista_momentum(X, p->d_Xo, nt, p->d_sc, q.fista, st));  // fista_update
   MRG_TRY(launch_zero(p->d_R, sizeof(float2) * nt, st));
   for (int t = 0; t < p->T; t++) {  // R = E^H W (E x - d)
-    MRG_TRY(run_E(p, p->frames[t], X + t * n, plan_smap(p), p->frames[t].dsorted, p->d_y, st));
+    MRG_TRY(run_E(p, p->frames[t], X + t * n, plan_smap(p), p->frames[t].dsorted, p->d_y, true, st));
     MRG_TRY(run_EH(p, p->frames[t], p->d_y, plan_smap(p), p->d_R + t * n, st));
   }
   MRG_TRY(grad_step(X, p->d_R, nt, p->d_sc, p->d_part, p->nblk, p->d_resid, st));  // X -= step R

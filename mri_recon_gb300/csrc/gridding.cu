@@ -10,13 +10,17 @@
 // [z][y][x][coil] for the grid), so one weight computation serves every coil
 // and a group of G lanes (lane = coil) moves C contiguous complex values per tap.
 //
-// Samples are sorted by the grid tile (B^3 points) that holds their centre.
+// Samples are sorted by the grid tile (B^3 points) that holds their centre, and
+// their tap weights (LUT interpolation and chop sign) are computed once per
+// trajectory and reused by every E and E^H call.
 // Ungridding walks samples in that order (tile-local gathers hit L1/L2).
-// Gridding is owner-computes: each tile is produced by the work items that own
-// it, from the list of every sample whose kernel support touches the tile, so
-// the accumulation runs in shared memory with shared atomics and the tile is
-// written to HBM once with plain stores; only tiles whose pair list is split
-// across several items (the dense k-space centre) use global atomics.
+// Gridding is output-driven: a warp owns an 8x2x2 block of grid points (lane =
+// point) and keeps all coils of its point in registers while it walks the list
+// of samples whose kernel support touches the block (8x2x2 points: a 5-tap
+// support meets 13.5 blocks on average, the fewest for 32 points); each grid value is written
+// to HBM once with plain stores, without atomics.  Only blocks whose list is
+// split across several work items (the dense k-space centre) add with global
+// atomics into a block zeroed beforehand.
 #include <algorithm>
 
 #include "mrg_internal.h"
@@ -112,38 +116,57 @@ __global__ void k_traj_sort(int64_t M, const int *__restrict__ key, const int *_
   }
 }
 
-template <bool FILL>
-__global__ void k_pairs(GridConst g, int nvalid, const float4 *__restrict__ spos, int *pcnt, const int *__restrict__ poff,
-                        int *pcur, int *pairs) {
+// Tap weights of every valid sample, computed once (src/gridFFT.cpp:1110-1148).
+__global__ void k_sample_weights(GridConst g, int nvalid, const float4 *__restrict__ spos, float4 *swt, int4 *sst) {
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nvalid; s += gridDim.x * blockDim.x) {
     const float4 p = spos[s];
     const float dk[3] = {p.x, p.y, p.z};
-    int lo[3], hi[3];
+    float w[24];
+    int st[3], n[3];
+#pragma unroll
     for (int d = 0; d < 3; d++) {
       int a, b;
       tap_range(g, d, dk[d], a, b);
-      lo[d] = a / g.B;
-      hi[d] = b / g.B;
+      st[d] = a;
+      n[d] = b - a + 1;
+#pragma unroll
+      for (int k = 0; k < 8; k++) w[8 * d + k] = (k < n[d]) ? tap_w(g.lut[d], g.gmod[d], dk[d], a + k) : 0.0f;
     }
-    for (int tz = lo[2]; tz <= hi[2]; tz++)
-      for (int ty = lo[1]; ty <= hi[1]; ty++)
-        for (int tx = lo[0]; tx <= hi[0]; tx++) {
-          const int tile = (tz * g.nt[1] + ty) * g.nt[0] + tx;
-          if (FILL) pairs[poff[tile] + atomicAdd(&pcur[tile], 1)] = s;
-          else atomicAdd(&pcnt[tile], 1);
+#pragma unroll
+    for (int k = 0; k < 6; k++) swt[6 * (int64_t)s + k] = make_float4(w[4 * k], w[4 * k + 1], w[4 * k + 2], w[4 * k + 3]);
+    sst[s] = make_int4(st[0], st[1], st[2], n[0] | (n[1] << 4) | (n[2] << 8));
+  }
+}
+
+// (sample, block) pairs: count (FILL = false) or fill the per-block lists.
+template <bool FILL>
+__global__ void k_pairs(GridConst g, int nvalid, const int4 *__restrict__ sst, int *pcnt, const int *__restrict__ poff,
+                        int *pcur, int *pairs) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nvalid; s += gridDim.x * blockDim.x) {
+    const int4 t = sst[s];
+    const int nx = t.w & 15, ny = (t.w >> 4) & 15, nz = (t.w >> 8) & 15;
+    const int x0 = t.x / BLK_X, x1 = (t.x + nx - 1) / BLK_X;
+    const int y0 = t.y / BLK_Y, y1 = (t.y + ny - 1) / BLK_Y;
+    const int z0 = t.z / BLK_Z, z1 = (t.z + nz - 1) / BLK_Z;
+    for (int bz = z0; bz <= z1; bz++)
+      for (int by = y0; by <= y1; by++)
+        for (int bx = x0; bx <= x1; bx++) {
+          const int blk = (bz * g.nb[1] + by) * g.nb[0] + bx;
+          if (FILL) pairs[poff[blk] + atomicAdd(&pcur[blk], 1)] = s;
+          else atomicAdd(&pcnt[blk], 1);
         }
   }
 }
 
-__global__ void k_item_count(int ntiles, const int *__restrict__ pcnt, int maxp, int *icnt) {
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ntiles; t += gridDim.x * blockDim.x)
+__global__ void k_item_count(int nblocks, const int *__restrict__ pcnt, int maxp, int *icnt) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nblocks; t += gridDim.x * blockDim.x)
     icnt[t] = max(1, (pcnt[t] + maxp - 1) / maxp);
 }
 
-__global__ void k_item_fill(int ntiles, const int *__restrict__ pcnt, const int *__restrict__ poff,
+__global__ void k_item_fill(int nblocks, const int *__restrict__ pcnt, const int *__restrict__ poff,
                             const int *__restrict__ icnt, const int *__restrict__ ioff, int maxp, int4 *items,
                             int *split, int *nsplit) {
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ntiles; t += gridDim.x * blockDim.x) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nblocks; t += gridDim.x * blockDim.x) {
     const int n = icnt[t];
     for (int k = 0; k < n; k++) {
       const int p0 = poff[t] + k * maxp;
@@ -173,11 +196,22 @@ void traj_free(FrameTraj &ft) {
   cudaFree(ft.spos);
   cudaFree(ft.stap);
   cudaFree(ft.perm);
+  cudaFree(ft.swt);
+  cudaFree(ft.sst);
   cudaFree(ft.pairs);
   cudaFree(ft.items);
-  cudaFree(ft.split_tiles);
+  cudaFree(ft.split_blocks);
   cudaFree(ft.dsorted);
   ft = FrameTraj();
+}
+
+static mrg_status read_int(const int *dev, int *host, cudaStream_t st, const char *what) {
+  if (cudaMemcpyAsync(host, dev, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess) {
+    set_error(std::string(what) + ": " + cudaGetErrorString(cudaGetLastError()));
+    return MRG_ERR_CUDA;
+  }
+  return MRG_OK;
 }
 
 mrg_status traj_setup(const GridConst &gc, FrameTraj &ft, const float *kx, const float *ky, const float *kz,
@@ -188,6 +222,7 @@ mrg_status traj_setup(const GridConst &gc, FrameTraj &ft, const float *kx, const
     return MRG_ERR_INVALID;
   }
   const int ntiles = gc.nt[0] * gc.nt[1] * gc.nt[2];
+  const int nblocks = gc.nb[0] * gc.nb[1] * gc.nb[2];
   ft.M = M;
   float4 *pos = nullptr;
   float *tap = nullptr;
@@ -207,6 +242,12 @@ mrg_status traj_setup(const GridConst &gc, FrameTraj &ft, const float *kx, const
       return rs;             \
     }                        \
   } while (0)
+#define SETUP_LAUNCHED()                                                                  \
+  do {                                                                                    \
+    count_launch();                                                                       \
+    if (cudaGetLastError() != cudaSuccess) SETUP_TRY(MRG_ERR_CUDA);                       \
+  } while (0)
+  // 1. positions, validity, sort key (tile of the sample centre); counting sort by tile
   SETUP_TRY(dalloc(&pos, M));
   SETUP_TRY(dalloc(&tap, M));
   SETUP_TRY(dalloc(&key, M));
@@ -219,118 +260,103 @@ mrg_status traj_setup(const GridConst &gc, FrameTraj &ft, const float *kx, const
   SETUP_TRY(launch_zero(cnt, sizeof(int) * (ntiles + 1), st));
   SETUP_TRY(launch_zero(cur, sizeof(int) * (ntiles + 1), st));
   k_traj_prep<<<grid_blocks(M, 256), 256, 0, st>>>(gc, kx, ky, kz, kw, M, pos, tap, key, cnt, ntiles);
-  SETUP_TRY(cudaGetLastError() == cudaSuccess ? MRG_OK : MRG_ERR_CUDA);
-  count_launch();
+  SETUP_LAUNCHED();
   k_scan<<<1, 1024, 0, st>>>(cnt, off, ntiles + 1);
-  count_launch();
+  SETUP_LAUNCHED();
   k_traj_sort<<<grid_blocks(M, 256), 256, 0, st>>>(M, key, off, cur, pos, tap, ft.spos, ft.stap, ft.perm);
-  count_launch();
+  SETUP_LAUNCHED();
   int nvalid = 0;
-  if (cudaMemcpyAsync(&nvalid, off + ntiles, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-      cudaStreamSynchronize(st) != cudaSuccess) {
-    set_error(std::string("trajectory sort failed: ") + cudaGetErrorString(cudaGetLastError()));
-    cleanup();
-    traj_free(ft);
-    return MRG_ERR_CUDA;
-  }
+  SETUP_TRY(read_int(off + ntiles, &nvalid, st, "trajectory sort failed"));
   ft.nvalid = nvalid;
 
-  // (sample, tile) pairs
-  SETUP_TRY(dalloc(&pcnt, ntiles + 1));
-  SETUP_TRY(dalloc(&poff, ntiles + 2));
-  SETUP_TRY(dalloc(&pcur, ntiles + 1));
-  SETUP_TRY(launch_zero(pcnt, sizeof(int) * (ntiles + 1), st));
-  SETUP_TRY(launch_zero(pcur, sizeof(int) * (ntiles + 1), st));
-  k_pairs<false><<<grid_blocks(nvalid, 256), 256, 0, st>>>(gc, nvalid, ft.spos, pcnt, nullptr, nullptr, nullptr);
-  count_launch();
-  k_scan<<<1, 1024, 0, st>>>(pcnt, poff, ntiles);
-  count_launch();
+  // 2. tap weights once per trajectory
+  SETUP_TRY(dalloc(&ft.swt, 6 * (int64_t)nvalid));
+  SETUP_TRY(dalloc(&ft.sst, nvalid));
+  k_sample_weights<<<grid_blocks(nvalid, 256), 256, 0, st>>>(gc, nvalid, ft.spos, ft.swt, ft.sst);
+  SETUP_LAUNCHED();
+
+  // 3. (sample, block) pair lists
+  SETUP_TRY(dalloc(&pcnt, nblocks + 1));
+  SETUP_TRY(dalloc(&poff, nblocks + 2));
+  SETUP_TRY(dalloc(&pcur, nblocks + 1));
+  SETUP_TRY(launch_zero(pcnt, sizeof(int) * (nblocks + 1), st));
+  SETUP_TRY(launch_zero(pcur, sizeof(int) * (nblocks + 1), st));
+  k_pairs<false><<<grid_blocks(nvalid, 256), 256, 0, st>>>(gc, nvalid, ft.sst, pcnt, nullptr, nullptr, nullptr);
+  SETUP_LAUNCHED();
+  k_scan<<<1, 1024, 0, st>>>(pcnt, poff, nblocks);
+  SETUP_LAUNCHED();
   int npairs = 0;
-  if (cudaMemcpyAsync(&npairs, poff + ntiles, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-      cudaStreamSynchronize(st) != cudaSuccess) {
-    set_error("pair count failed");
-    cleanup();
-    traj_free(ft);
-    return MRG_ERR_CUDA;
-  }
+  SETUP_TRY(read_int(poff + nblocks, &npairs, st, "pair count failed"));
   ft.npairs = npairs;
   SETUP_TRY(dalloc(&ft.pairs, npairs));
-  k_pairs<true><<<grid_blocks(nvalid, 256), 256, 0, st>>>(gc, nvalid, ft.spos, nullptr, poff, pcur, ft.pairs);
-  count_launch();
+  k_pairs<true><<<grid_blocks(nvalid, 256), 256, 0, st>>>(gc, nvalid, ft.sst, nullptr, poff, pcur, ft.pairs);
+  SETUP_LAUNCHED();
 
-  // work items: at most max_pairs pairs each; every tile gets >= 1 item
-  SETUP_TRY(dalloc(&icnt, ntiles + 1));
-  SETUP_TRY(dalloc(&ioff, ntiles + 2));
+  // 4. work items: at most max_pairs pairs each; every block gets >= 1 item
+  SETUP_TRY(dalloc(&icnt, nblocks + 1));
+  SETUP_TRY(dalloc(&ioff, nblocks + 2));
   SETUP_TRY(dalloc(&nsplit, 1));
   SETUP_TRY(launch_zero(nsplit, sizeof(int), st));
-  k_item_count<<<grid_blocks(ntiles, 256), 256, 0, st>>>(ntiles, pcnt, max_pairs, icnt);
-  count_launch();
-  k_scan<<<1, 1024, 0, st>>>(icnt, ioff, ntiles);
-  count_launch();
+  k_item_count<<<grid_blocks(nblocks, 256), 256, 0, st>>>(nblocks, pcnt, max_pairs, icnt);
+  SETUP_LAUNCHED();
+  k_scan<<<1, 1024, 0, st>>>(icnt, ioff, nblocks);
+  SETUP_LAUNCHED();
   int nitems = 0;
-  if (cudaMemcpyAsync(&nitems, ioff + ntiles, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-      cudaStreamSynchronize(st) != cudaSuccess) {
-    set_error("item count failed");
-    cleanup();
-    traj_free(ft);
-    return MRG_ERR_CUDA;
-  }
+  SETUP_TRY(read_int(ioff + nblocks, &nitems, st, "item count failed"));
   ft.nitems = nitems;
   SETUP_TRY(dalloc(&ft.items, nitems));
-  SETUP_TRY(dalloc(&ft.split_tiles, ntiles));
-  k_item_fill<<<grid_blocks(ntiles, 256), 256, 0, st>>>(ntiles, pcnt, poff, icnt, ioff, max_pairs, ft.items,
-                                                        ft.split_tiles, nsplit);
-  count_launch();
+  SETUP_TRY(dalloc(&ft.split_blocks, nblocks));
+  k_item_fill<<<grid_blocks(nblocks, 256), 256, 0, st>>>(nblocks, pcnt, poff, icnt, ioff, max_pairs, ft.items,
+                                                         ft.split_blocks, nsplit);
+  SETUP_LAUNCHED();
   int ns = 0;
-  if (cudaMemcpyAsync(&ns, nsplit, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-      cudaStreamSynchronize(st) != cudaSuccess) {
-    set_error("item fill failed");
-    cleanup();
-    traj_free(ft);
-    return MRG_ERR_CUDA;
-  }
+  SETUP_TRY(read_int(nsplit, &ns, st, "item fill failed"));
   ft.nsplit = ns;
   cleanup();
 #undef SETUP_TRY
+#undef SETUP_LAUNCHED
   return MRG_OK;
 }
 
 // ---------------------------------------------------------------------------
-// ungridding: y[s][c] = sum_taps w * grid[tap][c]  (- diff[s][c])
+// ungridding: y[s][c] = sum_taps w * grid[tap][c]  (- diff[s][c]) [* kw * taper]
 // ---------------------------------------------------------------------------
 template <int G>
-__global__ void __launch_bounds__(256) k_ungrid(const GridConst g, int nvalid, const float4 *__restrict__ spos,
-                                               const float2 *__restrict__ grid, const float2 *__restrict__ diff,
-                                               float2 *__restrict__ y) {
+__global__ void __launch_bounds__(256) k_ungrid(const GridConst g, int nvalid, const float4 *__restrict__ swt,
+                                               const int4 *__restrict__ sst, const float4 *__restrict__ spos,
+                                               const float *__restrict__ stap, const float2 *__restrict__ grid,
+                                               const float2 *__restrict__ diff, float2 *__restrict__ y, int weigh) {
   const int64_t gid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
   const int lane = threadIdx.x % G;
   if (gid >= nvalid) return;
-  const float4 p = spos[gid];
-  int xs, xe, ys, ye, zs, ze;
-  tap_range(g, 0, p.x, xs, xe);
-  tap_range(g, 1, p.y, ys, ye);
-  tap_range(g, 2, p.z, zs, ze);
-  float wx[6];
-#pragma unroll
-  for (int a = 0; a < 6; a++) wx[a] = (xs + a <= xe) ? tap_w(g.lut[0], g.gmod[0], p.x, xs + a) : 0.0f;
+  const int4 t = __ldg(sst + gid);
+  const int nx = t.w & 15, ny = (t.w >> 4) & 15, nz = (t.w >> 8) & 15;
+  const float *w = reinterpret_cast<const float *>(swt + 6 * gid);
+  const float4 wa = __ldg(swt + 6 * gid), wb = __ldg(swt + 6 * gid + 1);
+  const float wx[6] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y};
   const int C = g.C;
   const int64_t S0 = g.S[0], S1 = g.S[1];
+  float kwt_kw = 0.f, kwt_tp = 0.f;
+  if (weigh) {
+    kwt_kw = __ldg(&spos[gid].w);
+    kwt_tp = __ldg(stap + gid);
+  }
   for (int cb = 0; cb < C; cb += G) {
     const int c = cb + lane;
     if (c >= C) break;
     float2 acc = make_float2(0.f, 0.f);
-    for (int lz = zs; lz <= ze; lz++) {
-      const float wz = tap_w(g.lut[2], g.gmod[2], p.z, lz);
-      for (int ly = ys; ly <= ye; ly++) {
-        const float wzy = wz * tap_w(g.lut[1], g.gmod[1], p.y, ly);
-        const float2 *row = grid + (((int64_t)lz * S1 + ly) * S0 + xs) * C + c;
+    for (int kz = 0; kz < nz; kz++) {
+      const float wz = __ldg(w + 16 + kz);
+      for (int ky = 0; ky < ny; ky++) {
+        const float wzy = wz * __ldg(w + 8 + ky);
+        const float2 *row = grid + (((int64_t)(t.z + kz) * S1 + (t.y + ky)) * S0 + t.x) * C + c;
 #pragma unroll
         for (int a = 0; a < 6; a++) {
-          if (xs + a <= xe) {
-            const float w = wzy * wx[a];
+          if (a < nx) {
+            const float ww = wzy * wx[a];
             const float2 v = __ldg(row + (int64_t)a * C);
-            acc.x += w * v.x;
-            acc.y += w * v.y;
+            acc.x += ww * v.x;
+            acc.y += ww * v.y;
           }
         }
       }
@@ -341,170 +367,192 @@ __global__ void __launch_bounds__(256) k_ungrid(const GridConst g, int nvalid, c
       acc.x -= d.x;
       acc.y -= d.y;
     }
+    if (weigh) {  // temp = data * kw; temp *= taper  (src/gridFFT.cpp:1039-1108)
+      acc = make_float2(__fmul_rn(__fmul_rn(acc.x, kwt_kw), kwt_tp), __fmul_rn(__fmul_rn(acc.y, kwt_kw), kwt_tp));
+    }
     y[o] = acc;
   }
 }
 
 mrg_status launch_ungrid(const GridConst &gc, const FrameTraj &ft, const float2 *grid, const float2 *diff, float2 *y,
-                         cudaStream_t st) {
+                         bool weigh, cudaStream_t st) {
   if (ft.nvalid == 0) return MRG_OK;
   int G = 1;
   while (G < gc.C && G < 32) G *= 2;
   const int64_t threads = (int64_t)ft.nvalid * G;
   const int blocks = (int)((threads + 255) / 256);
+  const int wf = weigh ? 1 : 0;
+#define UNGRID_ARGS gc, ft.nvalid, ft.swt, ft.sst, ft.spos, ft.stap, grid, diff, y, wf
   switch (G) {
-    case 1: k_ungrid<1><<<blocks, 256, 0, st>>>(gc, ft.nvalid, ft.spos, grid, diff, y); break;
-    case 2: k_ungrid<2><<<blocks, 256, 0, st>>>(gc, ft.nvalid, ft.spos, grid, diff, y); break;
-    case 4: k_ungrid<4><<<blocks, 256, 0, st>>>(gc, ft.nvalid, ft.spos, grid, diff, y); break;
-    case 8: k_ungrid<8><<<blocks, 256, 0, st>>>(gc, ft.nvalid, ft.spos, grid, diff, y); break;
-    case 16: k_ungrid<16><<<blocks, 256, 0, st>>>(gc, ft.nvalid, ft.spos, grid, diff, y); break;
-    default: k_ungrid<32><<<blocks, 256, 0, st>>>(gc, ft.nvalid, ft.spos, grid, diff, y); break;
+    case 1: k_ungrid<1><<<blocks, 256, 0, st>>>(UNGRID_ARGS); break;
+    case 2: k_ungrid<2><<<blocks, 256, 0, st>>>(UNGRID_ARGS); break;
+    case 4: k_ungrid<4><<<blocks, 256, 0, st>>>(UNGRID_ARGS); break;
+    case 8: k_ungrid<8><<<blocks, 256, 0, st>>>(UNGRID_ARGS); break;
+    case 16: k_ungrid<16><<<blocks, 256, 0, st>>>(UNGRID_ARGS); break;
+    default: k_ungrid<32><<<blocks, 256, 0, st>>>(UNGRID_ARGS); break;
   }
+#undef UNGRID_ARGS
   MRG_LAUNCHED();
   return MRG_OK;
 }
 
 // ---------------------------------------------------------------------------
-// gridding: owner-computes tiles, shared-memory accumulation
+// gridding: a warp owns an 8x2x2 block (lane = point), coils in registers
 // ---------------------------------------------------------------------------
-__global__ void k_zero_tiles(const GridConst g, const int *__restrict__ tiles, int n, float2 *grid) {
-  const int B = g.B, C = g.C;
-  const int per = B * B * B * C;
+__global__ void k_zero_blocks(const GridConst g, const int *__restrict__ blocks, int n, float2 *grid) {
+  const int C = g.C;
+  const int per = BLK_X * BLK_Y * BLK_Z * C;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < (int64_t)n * per;
        e += (int64_t)gridDim.x * blockDim.x) {
-    const int t = tiles[e / per];
+    const int b = blocks[e / per];
     int r = (int)(e % per);
     const int c = r % C;
     r /= C;
-    const int px = r % B, py = (r / B) % B, pz = r / (B * B);
-    const int tx = t % g.nt[0], ty = (t / g.nt[0]) % g.nt[1], tz = t / (g.nt[0] * g.nt[1]);
-    const int64_t gi = ((((int64_t)(tz * B + pz)) * g.S[1] + (ty * B + py)) * g.S[0] + (tx * B + px)) * C + c;
+    const int px = r % BLK_X, py = (r / BLK_X) % BLK_Y, pz = r / (BLK_X * BLK_Y);
+    const int bx = b % g.nb[0], by = (b / g.nb[0]) % g.nb[1], bz = b / (g.nb[0] * g.nb[1]);
+    const int64_t gi = (((int64_t)(bz * BLK_Z + pz) * g.S[1] + (by * BLK_Y + py)) * g.S[0] + (bx * BLK_X + px)) * C + c;
     grid[gi] = make_float2(0.f, 0.f);
   }
 }
 
-template <int G>
-__global__ void __launch_bounds__(256) k_grid(const GridConst g, const int4 *__restrict__ items,
-                                             const int *__restrict__ pairs, const float4 *__restrict__ spos,
-                                             const float *__restrict__ stap, const float2 *__restrict__ y,
+// CC coils per pass (coils [c0, c0 + CC) of this blockIdx.y), VEC: coil pairs loaded as float4.
+template <int CC, bool VEC>
+__global__ void __launch_bounds__(256) k_grid(const GridConst g, int nitems, const int4 *__restrict__ items,
+                                             const int *__restrict__ pairs, const float4 *__restrict__ swt,
+                                             const int4 *__restrict__ sst, const float2 *__restrict__ yw,
                                              float2 *__restrict__ grid) {
-  extern __shared__ float tile[];  // [B^3][2][G]
-  const int B = g.B, B3 = B * B * B;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int item = blockIdx.x * 8 + warp;
+  if (item >= nitems) return;
+  const int4 it = __ldg(items + item);
   const int C = g.C;
-  const int4 it = items[blockIdx.x];
-  const int cb = blockIdx.y * G;
-  for (int e = threadIdx.x; e < B3 * 2 * G; e += blockDim.x) tile[e] = 0.0f;
-  const int tx = it.x % g.nt[0], ty = (it.x / g.nt[0]) % g.nt[1], tz = it.x / (g.nt[0] * g.nt[1]);
-  const int x0 = tx * B, y0 = ty * B, z0 = tz * B;
-  __syncthreads();
-
-  const int lane = threadIdx.x % G;
-  const int grp = threadIdx.x / G, ngrp = blockDim.x / G;
-  const int c = cb + lane;
-  for (int q = it.y + grp; q < it.z; q += ngrp) {
-    const int s = pairs[q];
-    const float4 p = spos[s];
-    int xs, xe, ys, ye, zs, ze;
-    tap_range(g, 0, p.x, xs, xe);
-    tap_range(g, 1, p.y, ys, ye);
-    tap_range(g, 2, p.z, zs, ze);
-    xs = max(xs, x0); xe = min(xe, x0 + B - 1);
-    ys = max(ys, y0); ye = min(ye, y0 + B - 1);
-    zs = max(zs, z0); ze = min(ze, z0 + B - 1);
-    if (c >= C) continue;
-    float2 v = y[(int64_t)s * C + c];
-    // temp = data * kw; temp *= taper  (src/gridFFT.cpp:1039-1108)
-    const float tp = stap[s];
-    v = make_float2(__fmul_rn(__fmul_rn(v.x, p.w), tp), __fmul_rn(__fmul_rn(v.y, p.w), tp));
-    float wx[6];
+  const int c0 = blockIdx.y * CC;
+  const int nc = min(CC, C - c0);
+  const int bx = it.x % g.nb[0], by = (it.x / g.nb[0]) % g.nb[1], bz = it.x / (g.nb[0] * g.nb[1]);
+  const int gx = bx * BLK_X + (lane % BLK_X), gy = by * BLK_Y + ((lane / BLK_X) % BLK_Y),
+            gz = bz * BLK_Z + lane / (BLK_X * BLK_Y);
+  float2 acc[CC];
 #pragma unroll
-    for (int a = 0; a < 6; a++) wx[a] = (xs + a <= xe) ? tap_w(g.lut[0], g.gmod[0], p.x, xs + a) : 0.0f;
-    for (int lz = zs; lz <= ze; lz++) {
-      const float wz = tap_w(g.lut[2], g.gmod[2], p.z, lz);
-      for (int ly = ys; ly <= ye; ly++) {
-        const float wzy = wz * tap_w(g.lut[1], g.gmod[1], p.y, ly);
-        float *row = tile + ((((lz - z0) * B + (ly - y0)) * B + (xs - x0)) * 2 * G) + lane;
+  for (int c = 0; c < CC; c++) acc[c] = make_float2(0.f, 0.f);
+  int s_next = (it.y < it.z) ? __ldg(pairs + it.y) : 0;
+  for (int q = it.y; q < it.z; q++) {
+    const int s = s_next;
+    if (q + 1 < it.z) s_next = __ldg(pairs + q + 1);
+    const int4 t = __ldg(sst + s);
+    const int ax = gx - t.x, ay = gy - t.y, az = gz - t.z;
+    const float *w = reinterpret_cast<const float *>(swt + 6 * (int64_t)s);
+    const float wx = (ax >= 0 && ax < 8) ? __ldg(w + ax) : 0.0f;
+    const float wy = (ay >= 0 && ay < 8) ? __ldg(w + 8 + ay) : 0.0f;
+    const float wz = (az >= 0 && az < 8) ? __ldg(w + 16 + az) : 0.0f;
+    const float ww = (wz * wy) * wx;  // src/gridFFT.cpp:1113-1140 order
+    const float2 *v = yw + (int64_t)s * C + c0;
+    if (VEC) {
+      const float4 *v4 = reinterpret_cast<const float4 *>(v);
 #pragma unroll
-        for (int a = 0; a < 6; a++) {
-          if (xs + a <= xe) {
-            const float w = wzy * wx[a];
-            atomicAdd(row + a * 2 * G, w * v.x);
-            atomicAdd(row + a * 2 * G + G, w * v.y);
-          }
+      for (int c = 0; c < CC / 2; c++) {
+        if (2 * c < nc) {
+          const float4 u = __ldg(v4 + c);
+          acc[2 * c].x += ww * u.x;
+          acc[2 * c].y += ww * u.y;
+          acc[2 * c + 1].x += ww * u.z;
+          acc[2 * c + 1].y += ww * u.w;
+        }
+      }
+    } else {
+#pragma unroll
+      for (int c = 0; c < CC; c++) {
+        if (c < nc) {
+          const float2 u = __ldg(v + c);
+          acc[c].x += ww * u.x;
+          acc[c].y += ww * u.y;
         }
       }
     }
   }
-  __syncthreads();
-
-  const bool split = it.w != 0;
-  for (int e = threadIdx.x; e < B3 * G; e += blockDim.x) {
-    const int l = e % G, pt = e / G;
-    const int cc = cb + l;
-    if (cc >= C) continue;
-    const int px = pt % B, py = (pt / B) % B, pz = pt / (B * B);
-    const int64_t gi = ((((int64_t)(z0 + pz)) * g.S[1] + (y0 + py)) * g.S[0] + (x0 + px)) * C + cc;
-    const float re = tile[pt * 2 * G + l], im = tile[pt * 2 * G + G + l];
-    if (split) {
-      atomicAdd(&grid[gi].x, re);
-      atomicAdd(&grid[gi].y, im);
-    } else {
-      grid[gi] = make_float2(re, im);
-    }
+  const int64_t gi = (((int64_t)gz * g.S[1] + gy) * g.S[0] + gx) * C + c0;
+  if (it.w) {
+#pragma unroll
+    for (int c = 0; c < CC; c++)
+      if (c < nc) {
+        atomicAdd(&grid[gi + c].x, acc[c].x);
+        atomicAdd(&grid[gi + c].y, acc[c].y);
+      }
+  } else if (VEC) {
+    float4 *o4 = reinterpret_cast<float4 *>(grid + gi);
+#pragma unroll
+    for (int c = 0; c < CC / 2; c++)
+      if (2 * c < nc) o4[c] = make_float4(acc[2 * c].x, acc[2 * c].y, acc[2 * c + 1].x, acc[2 * c + 1].y);
+  } else {
+#pragma unroll
+    for (int c = 0; c < CC; c++)
+      if (c < nc) grid[gi + c] = acc[c];
   }
 }
 
-static int grid_group(int C) {
-  int G = 1;
-  while (G < C && G < 16) G *= 2;
-  return G;
-}
-
-mrg_status launch_grid(const GridConst &gc, const FrameTraj &ft, const float2 *y, float2 *grid, cudaStream_t st) {
-  const int G = grid_group(gc.C);
-  const int nchunks = (gc.C + G - 1) / G;
-  if (ft.nsplit > 0) {
-    const int64_t n = (int64_t)ft.nsplit * gc.B * gc.B * gc.B * gc.C;
-    k_zero_tiles<<<grid_blocks(n, 256), 256, 0, st>>>(gc, ft.split_tiles, ft.nsplit, grid);
-    MRG_LAUNCHED();
-  }
-  const size_t smem = (size_t)gc.B * gc.B * gc.B * 2 * G * sizeof(float);
-  const dim3 blocks(ft.nitems, nchunks);
-  void (*fn)(const GridConst, const int4 *, const int *, const float4 *, const float *, const float2 *, float2 *);
-  switch (G) {
-    case 1: fn = k_grid<1>; break;
-    case 2: fn = k_grid<2>; break;
-    case 4: fn = k_grid<4>; break;
-    case 8: fn = k_grid<8>; break;
-    default: fn = k_grid<16>; break;
-  }
-  static int attr_set[5] = {0, 0, 0, 0, 0};  // smem cap for the largest tile (16^3), once per kernel
-  const int slot = G == 1 ? 0 : G == 2 ? 1 : G == 4 ? 2 : G == 8 ? 3 : 4;
-  if (!attr_set[slot]) {
-    MRG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)std::min<size_t>(16 * 16 * 16 * 2 * G * sizeof(float), 227 * 1024)));
-    attr_set[slot] = 1;
-  }
-  if (smem > 227 * 1024) {
-    set_error("gridding tile too large for shared memory");
-    return MRG_ERR_INVALID;
-  }
-  fn<<<blocks, 256, smem, st>>>(gc, ft.items, ft.pairs, ft.spos, ft.stap, y, grid);
+template <int CC>
+static mrg_status launch_grid_cc(const GridConst &gc, const FrameTraj &ft, const float2 *yw, float2 *grid,
+                                 cudaStream_t st) {
+  const bool vec = (gc.C % 2 == 0) && (CC % 2 == 0);
+  const dim3 blocks((unsigned)((ft.nitems + 7) / 8), (unsigned)((gc.C + CC - 1) / CC));
+  if (vec)
+    k_grid<CC, true><<<blocks, 256, 0, st>>>(gc, ft.nitems, ft.items, ft.pairs, ft.swt, ft.sst, yw, grid);
+  else
+    k_grid<CC, false><<<blocks, 256, 0, st>>>(gc, ft.nitems, ft.items, ft.pairs, ft.swt, ft.sst, yw, grid);
   MRG_LAUNCHED();
   return MRG_OK;
+}
+
+mrg_status launch_grid(const GridConst &gc, const FrameTraj &ft, const float2 *yw, float2 *grid, cudaStream_t st) {
+  if (ft.nsplit > 0) {
+    const int64_t n = (int64_t)ft.nsplit * BLK_X * BLK_Y * BLK_Z * gc.C;
+    k_zero_blocks<<<grid_blocks(n, 256), 256, 0, st>>>(gc, ft.split_blocks, ft.nsplit, grid);
+    MRG_LAUNCHED();
+  }
+  const int C = gc.C;
+  if (C <= 1) return launch_grid_cc<1>(gc, ft, yw, grid, st);
+  if (C <= 2) return launch_grid_cc<2>(gc, ft, yw, grid, st);
+  if (C <= 4) return launch_grid_cc<4>(gc, ft, yw, grid, st);
+  if (C <= 8) return launch_grid_cc<8>(gc, ft, yw, grid, st);
+  if (C <= 16) return launch_grid_cc<16>(gc, ft, yw, grid, st);
+  if (C <= 24) return launch_grid_cc<24>(gc, ft, yw, grid, st);
+  return launch_grid_cc<32>(gc, ft, yw, grid, st);
 }
 
 // ---------------------------------------------------------------------------
 // sample reordering between the user's per-coil layout and [sorted][coil]
 // ---------------------------------------------------------------------------
 __global__ void k_gather_samples(int nvalid, int C, const int *__restrict__ perm, const float2 *__restrict__ src,
-                                 int64_t stride, float2 *__restrict__ dst) {
+                                 int64_t stride, float2 *__restrict__ dst, const float4 *__restrict__ spos,
+                                 const float *__restrict__ stap) {
   const int64_t n = (int64_t)nvalid * C;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t s = e / C;
     const int c = (int)(e - s * C);
-    dst[e] = src[(int64_t)c * stride + perm[s]];
+    float2 v = src[(int64_t)c * stride + perm[s]];
+    if (spos) {
+      const float kw = spos[s].w, tp = stap[s];
+      v = make_float2(__fmul_rn(__fmul_rn(v.x, kw), tp), __fmul_rn(__fmul_rn(v.y, kw), tp));
+    }
+    dst[e] = v;
   }
+}
+
+__global__ void k_weigh_samples(int nvalid, int C, const float2 *__restrict__ src, float2 *__restrict__ dst,
+                                const float4 *__restrict__ spos, const float *__restrict__ stap) {
+  const int64_t n = (int64_t)nvalid * C;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t s = e / C;
+    const float kw = spos[s].w, tp = stap[s];
+    const float2 v = src[e];
+    dst[e] = make_float2(__fmul_rn(__fmul_rn(v.x, kw), tp), __fmul_rn(__fmul_rn(v.y, kw), tp));
+  }
+}
+
+mrg_status launch_weigh_samples(const FrameTraj &ft, int C, const float2 *src, float2 *dst, cudaStream_t st) {
+  if (ft.nvalid == 0) return MRG_OK;
+  k_weigh_samples<<<grid_blocks((int64_t)ft.nvalid * C, 256), 256, 0, st>>>(ft.nvalid, C, src, dst, ft.spos, ft.stap);
+  MRG_LAUNCHED();
+  return MRG_OK;
 }
 
 __global__ void k_scatter_samples(int64_t M, int nvalid, int C, const int *__restrict__ perm,
@@ -519,9 +567,10 @@ __global__ void k_scatter_samples(int64_t M, int nvalid, int C, const int *__res
 }
 
 mrg_status launch_gather_samples(const FrameTraj &ft, int C, const float2 *src, int64_t stride, float2 *dst,
-                                 cudaStream_t st) {
+                                 cudaStream_t st, bool weigh) {
   if (ft.nvalid == 0) return MRG_OK;
-  k_gather_samples<<<grid_blocks((int64_t)ft.nvalid * C, 256), 256, 0, st>>>(ft.nvalid, C, ft.perm, src, stride, dst);
+  k_gather_samples<<<grid_blocks((int64_t)ft.nvalid * C, 256), 256, 0, st>>>(
+      ft.nvalid, C, ft.perm, src, stride, dst, weigh ? ft.spos : nullptr, weigh ? ft.stap : nullptr);
   MRG_LAUNCHED();
   return MRG_OK;
 }

@@ -102,13 +102,18 @@ mrg_status launch_fft(const FftPass &p, cudaStream_t st);
 // ---------------------------------------------------------------------------
 // Gridding (gridding.cu)
 // ---------------------------------------------------------------------------
+// Gridding blocks: one warp owns BLK_X x BLK_Y x BLK_Z grid points (lane = point).
+constexpr int BLK_X = 8, BLK_Y = 2, BLK_Z = 2;
+static_assert(BLK_X * BLK_Y * BLK_Z == 32, "one grid point per lane");
+
 struct GridConst {
   int S[3];
   float grid[3], cen[3], dwin[3], gmod[3];
   const float *lut[3];
   float k_rad;
-  int B;       // tile edge
-  int nt[3];   // tiles per axis
+  int B;       // sort tile edge (sample order)
+  int nt[3];   // sort tiles per axis
+  int nb[3];   // gridding blocks per axis
   int C;       // coils
 };
 
@@ -118,27 +123,32 @@ struct FrameTraj {
   float4 *spos = nullptr;   // [M] sorted, valid first: (dkx, dky, dkz, kw)
   float *stap = nullptr;    // [M] taper exp(-|k|^2/(2 k_rad^2))
   int *perm = nullptr;      // [M] sorted -> original sample index
-  int *pairs = nullptr;     // sample index per (sample, tile) pair, grouped by tile
+  float4 *swt = nullptr;    // [nvalid][6] tap weights wx[8], wy[8], wz[8] (chop sign included, zero padded)
+  int4 *sst = nullptr;      // [nvalid] first tap (sx, sy, sz) and tap counts nx | ny << 4 | nz << 8
+  int *pairs = nullptr;     // sample index per (sample, block) pair, grouped by block
   int64_t npairs = 0;
-  int4 *items = nullptr;    // (tile, p0, p1, split)
+  int4 *items = nullptr;    // (block, p0, p1, split)
   int nitems = 0;
-  int *split_tiles = nullptr;
+  int *split_blocks = nullptr;
   int nsplit = 0;
-  float2 *dsorted = nullptr;  // measured data [nvalid][C]
+  float2 *dsorted = nullptr;  // measured data [nvalid][C], unweighted
   bool has_data = false;
 };
 
 mrg_status traj_setup(const GridConst &gc, FrameTraj &ft, const float *kx, const float *ky, const float *kz,
                       const float *kw, int64_t M, int max_pairs, cudaStream_t st);
 void traj_free(FrameTraj &ft);
-// y[s][c] = sum over taps of grid (gridFFT::chop_grid_backward), minus diff[s][c] if given.
+// y[s][c] = sum over taps of grid (gridFFT::chop_grid_backward), minus diff[s][c] if given;
+// with `weigh` the result is multiplied by kw and the taper, ready for launch_grid.
 mrg_status launch_ungrid(const GridConst &gc, const FrameTraj &ft, const float2 *grid, const float2 *diff,
-                         float2 *y, cudaStream_t st);
-// grid = scatter of y*kw*taper (gridFFT::chop_grid_forward); every tile written.
-mrg_status launch_grid(const GridConst &gc, const FrameTraj &ft, const float2 *y, float2 *grid, cudaStream_t st);
-// dst[s][c] = src[c*stride + perm[s]], s < nvalid
+                         float2 *y, bool weigh, cudaStream_t st);
+// grid = scatter of the already weighted samples yw (gridFFT::chop_grid_forward); every point written.
+mrg_status launch_grid(const GridConst &gc, const FrameTraj &ft, const float2 *yw, float2 *grid, cudaStream_t st);
+// dst[s][c] = src[c*stride + perm[s]] (times kw*taper with `weigh`), s < nvalid
 mrg_status launch_gather_samples(const FrameTraj &ft, int C, const float2 *src, int64_t stride, float2 *dst,
-                                 cudaStream_t st);
+                                 cudaStream_t st, bool weigh = false);
+// dst[s][c] = src[s][c] * kw * taper
+mrg_status launch_weigh_samples(const FrameTraj &ft, int C, const float2 *src, float2 *dst, cudaStream_t st);
 // dst[c*stride + perm[s]] = s < nvalid ? src[s][c] : 0
 mrg_status launch_scatter_samples(const FrameTraj &ft, int C, const float2 *src, float2 *dst, int64_t stride,
                                   cudaStream_t st);
