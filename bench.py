@@ -82,7 +82,7 @@ def bytes_model(c, nvalid, npairs):
 
 STAGES = ["E_zfft_setimg", "E_yfft", "E_xfft", "E_ungrid", "EH_grid", "EH_xfft", "EH_yfft", "EH_zfft_accum"]
 KERNEL_OF = {"E_zfft_setimg": "k_fft<Q,-1,SETIMG>", "E_yfft": "k_fft<Q,-1,PLAIN>", "E_xfft": "k_fft<Q,-1,PLAIN>",
-             "E_ungrid": "k_ungrid<32>", "EH_grid": "k_grid<16>", "EH_xfft": "k_fft<Q,+1,PLAIN>",
+             "E_ungrid": "k_ungrid<32>", "EH_grid": "k_grid<32,true>", "EH_xfft": "k_fft<Q,+1,PLAIN>",
              "EH_yfft": "k_fft<Q,+1,PLAIN>", "EH_zfft_accum": "k_fft<Q,+1,ACCUM>"}
 
 

@@ -193,6 +193,7 @@ static mrg_status run_E(mrg_plan *p, const FrameTraj &ft, const float2 *X, const
   a.in = smap; a.smap = smap; a.has_smap = smap != nullptr; a.X = X; a.out = p->d_t1;
   a.wl = wz + g.og[2]; a.wo = wy + g.og[1]; a.wi = wx + g.og[0]; a.C = C;
   tmark(p, 0, st);
+  fft_vectorize(a);
   MRG_TRY(launch_fft(a, st));
   tmark(p, 1, st);
   // y pass
@@ -205,6 +206,7 @@ static mrg_status run_E(mrg_plan *p, const FrameTraj &ft, const float2 *X, const
   b.in_ls = Nx * C; b.in_os = Ny * Nx * C; b.out_ls = Nx * C; b.out_os = Sy * Nx * C;
   b.scale = (float)(1. / std::sqrt((float)Sy));
   b.in = p->d_t1; b.out = p->d_t2; b.C = C;
+  fft_vectorize(b);
   MRG_TRY(launch_fft(b, st));
   tmark(p, 2, st);
   // x pass
@@ -217,6 +219,7 @@ static mrg_status run_E(mrg_plan *p, const FrameTraj &ft, const float2 *X, const
   c.in_ls = C; c.in_os = Nx * C; c.out_ls = C; c.out_os = Sx * C;
   c.scale = (float)(1. / std::sqrt((float)Sx));
   c.in = p->d_t2; c.out = p->d_grid; c.C = C;
+  fft_vectorize(c);
   MRG_TRY(launch_fft(c, st));
   tmark(p, 3, st);
   // ungrid (src/gridFFT.cpp:1166-1322)
@@ -247,6 +250,7 @@ static mrg_status run_EH(mrg_plan *p, const FrameTraj &ft, const float2 *y, cons
   a.in_ls = C; a.in_os = Sx * C; a.out_ls = C; a.out_os = Nx * C;
   a.scale = (float)(1. / std::sqrt((float)Sx));
   a.in = p->d_grid; a.out = p->d_t2; a.C = C;
+  fft_vectorize(a);
   MRG_TRY(launch_fft(a, st));
   tmark(p, 2, st);
   FftPass b;
@@ -258,6 +262,7 @@ static mrg_status run_EH(mrg_plan *p, const FrameTraj &ft, const float2 *y, cons
   b.in_ls = Nx * C; b.in_os = Sy * Nx * C; b.out_ls = Nx * C; b.out_os = Ny * Nx * C;
   b.scale = (float)(1. / std::sqrt((float)Sy));
   b.in = p->d_t2; b.out = p->d_t1; b.C = C;
+  fft_vectorize(b);
   MRG_TRY(launch_fft(b, st));
   tmark(p, 3, st);
   // z pass with accumulate (src/gridFFT.cpp:926-941)
@@ -272,6 +277,7 @@ static mrg_status run_EH(mrg_plan *p, const FrameTraj &ft, const float2 *y, cons
   c.in = p->d_t1; c.smap = smap; c.has_smap = smap != nullptr; c.acc = X;
   c.acc_atomic = (c.IB % C) != 0; c.acc_l = Nx * Ny; c.acc_o = Nx;
   c.wl = wz + g.og[2]; c.wo = wy + g.og[1]; c.wi = wx + g.og[0]; c.C = C;
+  fft_vectorize(c);
   MRG_TRY(launch_fft(c, st));
   tmark(p, 4, st);
   tcollect(p, 4);

@@ -140,9 +140,9 @@ template <int Q, int SIGN, int MODE>
 __global__ void __launch_bounds__(256, 2) k_fft(const FftPass p) {
   constexpr int S = 8 * Q;
   extern __shared__ float2 sm[];  // [S][IB+1] data, then S twiddles
-  const int IB = p.IB, IBp = p.IB + 1;
+  const int IB = p.IB, IBp = p.lfast ? p.IB + 1 : p.IB;  // pad only for column-wise (contiguous-line) access
   const int tid = threadIdx.x;
-  float2 *tw = sm + S * IBp;
+  float2 *tw = sm + S * (p.IB + 1);
   for (int m = tid; m < S; m += blockDim.x) tw[m] = p.tw[m];
   const int j = tid % IB, t = tid / IB;  // 8 threads per line
   const int64_t line = (int64_t)blockIdx.x * IB + j;
@@ -154,7 +154,54 @@ __global__ void __launch_bounds__(256, 2) k_fft(const FftPass p) {
   }
 
   // ---- load (zero rows outside [in_off, in_off + Lin)) ----
-  if (!p.lfast) {
+  if (p.vec16 && !(MODE == FFT_SETIMG && !p.has_smap)) {
+    // 16-byte asynchronous copies (two adjacent lines per copy), many in flight
+    const int npair = IB >> 1;
+    const int jp = tid % npair, r0 = tid / npair, rstep = blockDim.x / npair;
+    const int64_t ln = (int64_t)blockIdx.x * IB + 2 * jp;
+    const bool pv = ln < p.nlines;
+    int64_t po = 0, pi = 0;
+    if (pv) {
+      po = ln / p.inner;
+      pi = ln - po * p.inner;
+    }
+    const float2 *src = (MODE == FFT_SETIMG) ? p.smap : p.in;
+    const float2 *gb = src + po * p.in_os + pi;
+    for (int li = r0; li < p.Lin; li += rstep) {
+      float2 *dst = sm + (li + p.in_off) * IBp + 2 * jp;
+      if (pv) {
+        const unsigned sa = (unsigned)__cvta_generic_to_shared(dst);
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gb + (int64_t)li * p.in_ls));
+      } else {
+        *reinterpret_cast<float4 *>(dst) = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+    }
+    for (int e = tid; e < (S - p.Lin) * IB; e += blockDim.x) {
+      const int jj = e % IB, k = e / IB;
+      const int r = (k < p.in_off) ? k : k + p.Lin;
+      sm[r * IBp + jj] = make_float2(0.f, 0.f);
+    }
+    asm volatile("cp.async.commit_group;\n" ::);
+    asm volatile("cp.async.wait_group 0;\n" ::);
+    __syncthreads();
+    if constexpr (MODE == FFT_SETIMG) {
+      // image = (winz*winy)*winx * X * smap  (src/gridFFT.cpp:972-986); smap already in smem
+      if (lv) {
+        const int64_t ib = o * p.in_os + i;
+        const float wyx_o = p.wo[o];
+        const float wxi = p.wi[i / p.C];
+#pragma unroll 4
+        for (int li = t; li < p.Lin; li += 8) {
+          const int64_t off = ib + (int64_t)li * p.in_ls;
+          const float w = (p.wl[li] * wyx_o) * wxi;
+          const float2 x = __ldg(p.X + off / p.C);
+          float2 *d = sm + (li + p.in_off) * IBp + j;
+          *d = cmul(make_float2(w * x.x, w * x.y), *d);
+        }
+      }
+      __syncthreads();
+    }
+  } else if (!p.lfast) {
     const int64_t ib = o * p.in_os + i;
     for (int r = t; r < S; r += 8) {
       float2 v = make_float2(0.f, 0.f);
@@ -173,6 +220,7 @@ __global__ void __launch_bounds__(256, 2) k_fft(const FftPass p) {
       }
       sm[r * IBp + j] = v;
     }
+    __syncthreads();
   } else {
     // inner == 1 and in_ls == 1: each line is contiguous; sweep along lines.
     const int64_t l0 = (int64_t)blockIdx.x * IB;
@@ -184,8 +232,8 @@ __global__ void __launch_bounds__(256, 2) k_fft(const FftPass p) {
       if (ln < p.nlines && li >= 0 && li < p.Lin) v = p.in[ln * p.in_os + li];
       sm[r * IBp + jj] = v;
     }
+    __syncthreads();
   }
-  __syncthreads();
 
   // ---- step A: 8-point DFTs over n1 (rows Q*n1 + n2), twiddle W_S^(n2*k1) ----
   for (int n2 = t; n2 < Q; n2 += 8) {
@@ -214,7 +262,21 @@ __global__ void __launch_bounds__(256, 2) k_fft(const FftPass p) {
 
   // ---- store ----
   if constexpr (MODE != FFT_ACCUM) {
-    if (!p.lfast) {
+    if (p.vec16o) {
+      const int npair = IB >> 1;
+      const int jp = tid % npair, r0 = tid / npair, rstep = blockDim.x / npair;
+      const int64_t ln = (int64_t)blockIdx.x * IB + 2 * jp;
+      if (ln < p.nlines) {
+        const int64_t po = ln / p.inner, pi = ln - po * p.inner;
+        float4 *ob = reinterpret_cast<float4 *>(p.out + po * p.out_os + pi);
+        const int64_t ls4 = p.out_ls / 2;
+#pragma unroll 4
+        for (int r = r0; r < p.Lout; r += rstep) {
+          const float4 v = *reinterpret_cast<const float4 *>(sm + (r + p.out_off) * IBp + 2 * jp);
+          ob[(int64_t)r * ls4] = make_float4(v.x * p.scale, v.y * p.scale, v.z * p.scale, v.w * p.scale);
+        }
+      }
+    } else if (!p.lfast) {
       if (lv) {
         const int64_t ob = o * p.out_os + i;
         for (int r = t; r < p.Lout; r += 8) {
@@ -238,6 +300,7 @@ __global__ void __launch_bounds__(256, 2) k_fft(const FftPass p) {
     const int C = p.C;
     if (lv) {
       const int64_t sb = o * p.out_os + i;
+#pragma unroll 4
       for (int r = t; r < p.Lout; r += 8) {
         float2 v = sm[(r + p.out_off) * IBp + j];
         v = make_float2(v.x * p.scale, v.y * p.scale);
@@ -304,6 +367,14 @@ static mrg_status launch_q(const FftPass &p, cudaStream_t st) {
   return MRG_OK;
 }
 
+void fft_vectorize(FftPass &p) {
+  auto al = [](const void *q) { return ((uintptr_t)q & 15) == 0; };
+  const bool pairs = !p.lfast && (p.IB % 2 == 0) && (p.inner % 2 == 0) && (p.nlines % 2 == 0);
+  const float2 *src = (p.mode == FFT_SETIMG) ? p.smap : p.in;
+  p.vec16 = pairs && src && al(src) && (p.in_os % 2 == 0) && (p.in_ls % 2 == 0);
+  p.vec16o = pairs && p.mode != FFT_ACCUM && p.out && al(p.out) && (p.out_os % 2 == 0) && (p.out_ls % 2 == 0);
+}
+
 mrg_status launch_fft(const FftPass &p, cudaStream_t st) {
   if (p.nlines <= 0) return MRG_OK;
   if ((p.mode == FFT_SETIMG && p.sign >= 0) || (p.mode == FFT_ACCUM && p.sign <= 0)) {
@@ -312,6 +383,10 @@ mrg_status launch_fft(const FftPass &p, cudaStream_t st) {
   }
   if (p.IB < 1 || p.IB > 32) {
     set_error("fft pass: bad IB");
+    return MRG_ERR_INVALID;
+  }
+  if ((p.vec16 || p.vec16o) && (p.lfast || (p.IB & 1))) {
+    set_error("fft pass: 16-byte copies need paired lines");
     return MRG_ERR_INVALID;
   }
   if (p.lfast && (p.mode != FFT_PLAIN || p.inner != 1)) {

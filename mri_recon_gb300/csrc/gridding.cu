@@ -333,7 +333,9 @@ __global__ void __launch_bounds__(256) k_ungrid(const GridConst g, int nvalid, c
   const int nx = t.w & 15, ny = (t.w >> 4) & 15, nz = (t.w >> 8) & 15;
   const float *w = reinterpret_cast<const float *>(swt + 6 * gid);
   const float4 wa = __ldg(swt + 6 * gid), wb = __ldg(swt + 6 * gid + 1);
+  const float4 wc = __ldg(swt + 6 * gid + 2), wd = __ldg(swt + 6 * gid + 3);
   const float wx[6] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y};
+  const float wy[6] = {wc.x, wc.y, wc.z, wc.w, wd.x, wd.y};
   const int C = g.C;
   const int64_t S0 = g.S[0], S1 = g.S[1];
   float kwt_kw = 0.f, kwt_tp = 0.f;
@@ -347,16 +349,21 @@ __global__ void __launch_bounds__(256) k_ungrid(const GridConst g, int nvalid, c
     float2 acc = make_float2(0.f, 0.f);
     for (int kz = 0; kz < nz; kz++) {
       const float wz = __ldg(w + 16 + kz);
-      for (int ky = 0; ky < ny; ky++) {
-        const float wzy = wz * __ldg(w + 8 + ky);
-        const float2 *row = grid + (((int64_t)(t.z + kz) * S1 + (t.y + ky)) * S0 + t.x) * C + c;
+      const float2 *slab = grid + (((int64_t)(t.z + kz) * S1 + t.y) * S0 + t.x) * C + c;
+      // all taps of one z slice unrolled: up to 36 independent gathers in flight
 #pragma unroll
-        for (int a = 0; a < 6; a++) {
-          if (a < nx) {
-            const float ww = wzy * wx[a];
-            const float2 v = __ldg(row + (int64_t)a * C);
-            acc.x += ww * v.x;
-            acc.y += ww * v.y;
+      for (int ky = 0; ky < 6; ky++) {
+        if (ky < ny) {
+          const float wzy = wz * wy[ky];
+          const float2 *row = slab + (int64_t)ky * S0 * C;
+#pragma unroll
+          for (int a = 0; a < 6; a++) {
+            if (a < nx) {
+              const float ww = wzy * wx[a];
+              const float2 v = __ldg(row + (int64_t)a * C);
+              acc.x += ww * v.x;
+              acc.y += ww * v.y;
+            }
           }
         }
       }
@@ -415,15 +422,38 @@ __global__ void k_zero_blocks(const GridConst g, const int *__restrict__ blocks,
   }
 }
 
-// CC coils per pass (coils [c0, c0 + CC) of this blockIdx.y), VEC: coil pairs loaded as float4.
+__device__ __forceinline__ void cp16(void *dst, const void *src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src));
+}
+__device__ __forceinline__ void cp8(void *dst, const void *src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src));
+}
+
+// Shared memory per warp: 32 staged pairs x (CC coil values, 24 weights, first taps).
+template <int CC>
+struct GridStage {
+  static constexpr int V = 32 * CC;    // float2
+  static constexpr int W = 32 * 24;    // float
+  static constexpr int T = 32;         // int4
+  static constexpr size_t bytes = V * 8 + W * 4 + T * 16;
+};
+
+// CC coils per pass (coils [c0, c0 + CC) of this blockIdx.y); VEC: coil pairs copied as 16 bytes.
+// A warp stages up to 32 pairs at a time (one lane per pair, independent async
+// copies), then accumulates them from shared memory into its registers.
 template <int CC, bool VEC>
 __global__ void __launch_bounds__(256) k_grid(const GridConst g, int nitems, const int4 *__restrict__ items,
                                              const int *__restrict__ pairs, const float4 *__restrict__ swt,
                                              const int4 *__restrict__ sst, const float2 *__restrict__ yw,
                                              float2 *__restrict__ grid) {
+  extern __shared__ __align__(16) unsigned char gsm_raw[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int item = blockIdx.x * 8 + warp;
   if (item >= nitems) return;
+  unsigned char *base = gsm_raw + warp * GridStage<CC>::bytes;
+  float2 *sv = reinterpret_cast<float2 *>(base);
+  float *sw = reinterpret_cast<float *>(base + GridStage<CC>::V * 8);
+  int4 *stt = reinterpret_cast<int4 *>(base + GridStage<CC>::V * 8 + GridStage<CC>::W * 4);
   const int4 it = __ldg(items + item);
   const int C = g.C;
   const int c0 = blockIdx.y * CC;
@@ -434,40 +464,55 @@ __global__ void __launch_bounds__(256) k_grid(const GridConst g, int nitems, con
   float2 acc[CC];
 #pragma unroll
   for (int c = 0; c < CC; c++) acc[c] = make_float2(0.f, 0.f);
-  int s_next = (it.y < it.z) ? __ldg(pairs + it.y) : 0;
-  for (int q = it.y; q < it.z; q++) {
-    const int s = s_next;
-    if (q + 1 < it.z) s_next = __ldg(pairs + q + 1);
-    const int4 t = __ldg(sst + s);
-    const int ax = gx - t.x, ay = gy - t.y, az = gz - t.z;
-    const float *w = reinterpret_cast<const float *>(swt + 6 * (int64_t)s);
-    const float wx = (ax >= 0 && ax < 8) ? __ldg(w + ax) : 0.0f;
-    const float wy = (ay >= 0 && ay < 8) ? __ldg(w + 8 + ay) : 0.0f;
-    const float wz = (az >= 0 && az < 8) ? __ldg(w + 16 + az) : 0.0f;
-    const float ww = (wz * wy) * wx;  // src/gridFFT.cpp:1113-1140 order
-    const float2 *v = yw + (int64_t)s * C + c0;
-    if (VEC) {
-      const float4 *v4 = reinterpret_cast<const float4 *>(v);
+  for (int q0 = it.y; q0 < it.z; q0 += 32) {
+    const int nq = min(32, it.z - q0);
+    if (lane < nq) {
+      const int s = __ldg(pairs + q0 + lane);
+      cp16(stt + lane, sst + s);
 #pragma unroll
-      for (int c = 0; c < CC / 2; c++) {
-        if (2 * c < nc) {
-          const float4 u = __ldg(v4 + c);
+      for (int k = 0; k < 6; k++) cp16(sw + lane * 24 + 4 * k, swt + 6 * (int64_t)s + k);
+      const float2 *v = yw + (int64_t)s * C + c0;
+      if (VEC) {
+#pragma unroll
+        for (int c = 0; c < CC / 2; c++)
+          if (2 * c < nc) cp16(sv + lane * CC + 2 * c, v + 2 * c);
+      } else {
+#pragma unroll
+        for (int c = 0; c < CC; c++)
+          if (c < nc) cp8(sv + lane * CC + c, v + c);
+      }
+    }
+    asm volatile("cp.async.commit_group;\n" ::);
+    asm volatile("cp.async.wait_group 0;\n" ::);
+    __syncwarp();
+    for (int k = 0; k < nq; k++) {
+      const int4 t = stt[k];
+      const int ax = gx - t.x, ay = gy - t.y, az = gz - t.z;
+      const float *w = sw + k * 24;
+      const float wx = (ax >= 0 && ax < 8) ? w[ax] : 0.0f;
+      const float wy = (ay >= 0 && ay < 8) ? w[8 + ay] : 0.0f;
+      const float wz = (az >= 0 && az < 8) ? w[16 + az] : 0.0f;
+      const float ww = (wz * wy) * wx;  // src/gridFFT.cpp:1113-1140 order
+      const float2 *v = sv + k * CC;
+      if (VEC) {
+#pragma unroll
+        for (int c = 0; c < CC / 2; c++) {
+          const float4 u = *reinterpret_cast<const float4 *>(v + 2 * c);
           acc[2 * c].x += ww * u.x;
           acc[2 * c].y += ww * u.y;
           acc[2 * c + 1].x += ww * u.z;
           acc[2 * c + 1].y += ww * u.w;
         }
-      }
-    } else {
+      } else {
 #pragma unroll
-      for (int c = 0; c < CC; c++) {
-        if (c < nc) {
-          const float2 u = __ldg(v + c);
+        for (int c = 0; c < CC; c++) {
+          const float2 u = v[c];
           acc[c].x += ww * u.x;
           acc[c].y += ww * u.y;
         }
       }
     }
+    __syncwarp();
   }
   const int64_t gi = (((int64_t)gz * g.S[1] + gy) * g.S[0] + gx) * C + c0;
   if (it.w) {
@@ -492,12 +537,19 @@ __global__ void __launch_bounds__(256) k_grid(const GridConst g, int nitems, con
 template <int CC>
 static mrg_status launch_grid_cc(const GridConst &gc, const FrameTraj &ft, const float2 *yw, float2 *grid,
                                  cudaStream_t st) {
-  const bool vec = (gc.C % 2 == 0) && (CC % 2 == 0);
+  const bool vec = (gc.C % 2 == 0) && (CC % 2 == 0) && (((uintptr_t)yw & 15) == 0);
   const dim3 blocks((unsigned)((ft.nitems + 7) / 8), (unsigned)((gc.C + CC - 1) / CC));
+  const size_t smem = 8 * GridStage<CC>::bytes;
+  static bool attr = false;
+  if (!attr) {
+    MRG_CUDA(cudaFuncSetAttribute(k_grid<CC, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    MRG_CUDA(cudaFuncSetAttribute(k_grid<CC, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = true;
+  }
   if (vec)
-    k_grid<CC, true><<<blocks, 256, 0, st>>>(gc, ft.nitems, ft.items, ft.pairs, ft.swt, ft.sst, yw, grid);
+    k_grid<CC, true><<<blocks, 256, smem, st>>>(gc, ft.nitems, ft.items, ft.pairs, ft.swt, ft.sst, yw, grid);
   else
-    k_grid<CC, false><<<blocks, 256, 0, st>>>(gc, ft.nitems, ft.items, ft.pairs, ft.swt, ft.sst, yw, grid);
+    k_grid<CC, false><<<blocks, 256, smem, st>>>(gc, ft.nitems, ft.items, ft.pairs, ft.swt, ft.sst, yw, grid);
   MRG_LAUNCHED();
   return MRG_OK;
 }

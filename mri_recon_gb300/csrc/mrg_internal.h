@@ -79,6 +79,7 @@ struct FftPass {
   int S, sign, mode;
   int Lin, in_off, Lout, out_off;
   int inner, IB, lfast;
+  int vec16, vec16o;  // 16-byte loads / stores of line pairs (set by fft_vectorize)
   int64_t nlines;
   int64_t in_ls, in_os, out_ls, out_os;
   float scale;
@@ -96,6 +97,8 @@ struct FftPass {
   int64_t acc_l, acc_o;  // accumulator strides for l and o (i/C has stride 1)
 };
 bool fft_size_supported(int S);
+// Enables 16-byte line-pair copies when every stride, the line count and the pointers allow it.
+void fft_vectorize(FftPass &p);
 mrg_status fft_init_device();
 mrg_status launch_fft(const FftPass &p, cudaStream_t st);
 
