@@ -500,6 +500,7 @@ mrg_status mrg_set_traj(mrg_plan *p, int frame, const float *kx, const float *ky
                      (const float *)dw, M, p->max_pairs, st));
   invalidate_graphs(p);
   MRG_TRY(ensure_y(p, (int64_t)p->frames[frame].nvalid * p->C));
+  if (p->cfg.tile == 0) MRG_TRY(autotune_frame(gc, p->frames[frame], p->d_grid, p->d_y, st));
   return MRG_OK;
 }
 

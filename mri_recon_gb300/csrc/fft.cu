@@ -190,13 +190,27 @@ __global__ void __launch_bounds__(256, 2) k_fft(const FftPass p) {
         const int64_t ib = o * p.in_os + i;
         const float wyx_o = p.wo[o];
         const float wxi = p.wi[i / p.C];
-#pragma unroll 4
-        for (int li = t; li < p.Lin; li += 8) {
-          const int64_t off = ib + (int64_t)li * p.in_ls;
-          const float w = (p.wl[li] * wyx_o) * wxi;
-          const float2 x = __ldg(p.X + off / p.C);
-          float2 *d = sm + (li + p.in_off) * IBp + j;
-          *d = cmul(make_float2(w * x.x, w * x.y), *d);
+        const int64_t xb = ib / p.C, xs = p.in_ls / p.C;  // X has no coil axis
+        for (int l0 = t; l0 < p.Lin; l0 += 64) {
+          float2 xv[8];
+          float wv[8];
+#pragma unroll
+          for (int k = 0; k < 8; k++) {  // 8 independent loads in flight
+            const int li = l0 + 8 * k;
+            if (li < p.Lin) {
+              xv[k] = __ldg(p.X + xb + (int64_t)li * xs);
+              wv[k] = __ldg(p.wl + li);
+            }
+          }
+#pragma unroll
+          for (int k = 0; k < 8; k++) {
+            const int li = l0 + 8 * k;
+            if (li < p.Lin) {
+              const float w = (wv[k] * wyx_o) * wxi;
+              float2 *d = sm + (li + p.in_off) * IBp + j;
+              *d = cmul(make_float2(w * xv[k].x, w * xv[k].y), *d);
+            }
+          }
         }
       }
       __syncthreads();
@@ -300,23 +314,37 @@ __global__ void __launch_bounds__(256, 2) k_fft(const FftPass p) {
     const int C = p.C;
     if (lv) {
       const int64_t sb = o * p.out_os + i;
-#pragma unroll 4
-      for (int r = t; r < p.Lout; r += 8) {
-        float2 v = sm[(r + p.out_off) * IBp + j];
-        v = make_float2(v.x * p.scale, v.y * p.scale);
-        const float w = (p.wl[r] * p.wo[o]) * p.wi[i / C];
-        v = make_float2(w * v.x, w * v.y);
-        if (p.has_smap) {
-          float2 s = p.smap[sb + (int64_t)r * p.out_ls];
-          s.y = -s.y;
-          v = cmul(v, s);
+      for (int r0 = t; r0 < p.Lout; r0 += 64) {
+        float2 sv[8];
+        float wv[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) {  // 8 independent smap loads in flight
+          const int r = r0 + 8 * k;
+          if (r < p.Lout) {
+            sv[k] = p.has_smap ? __ldg(p.smap + sb + (int64_t)r * p.out_ls) : make_float2(1.f, 0.f);
+            wv[k] = __ldg(p.wl + r);
+          }
         }
-        if (p.acc_atomic) {
-          float2 *dst = p.acc + (int64_t)r * p.acc_l + o * p.acc_o + i / C;
-          atomicAdd(&dst->x, v.x);
-          atomicAdd(&dst->y, v.y);
-        } else {
-          sm[(r + p.out_off) * IBp + j] = v;
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+          const int r = r0 + 8 * k;
+          if (r >= p.Lout) continue;
+          float2 v = sm[(r + p.out_off) * IBp + j];
+          v = make_float2(v.x * p.scale, v.y * p.scale);
+          const float w = (wv[k] * p.wo[o]) * p.wi[i / C];
+          v = make_float2(w * v.x, w * v.y);
+          if (p.has_smap) {
+            float2 s2 = sv[k];
+            s2.y = -s2.y;
+            v = cmul(v, s2);
+          }
+          if (p.acc_atomic) {
+            float2 *dst = p.acc + (int64_t)r * p.acc_l + o * p.acc_o + i / C;
+            atomicAdd(&dst->x, v.x);
+            atomicAdd(&dst->y, v.y);
+          } else {
+            sm[(r + p.out_off) * IBp + j] = v;
+          }
         }
       }
     }

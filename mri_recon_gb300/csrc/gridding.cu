@@ -22,6 +22,7 @@
 // split across several work items (the dense k-space centre) add with global
 // atomics into a block zeroed beforehand.
 #include <algorithm>
+#include <functional>
 
 #include "mrg_internal.h"
 
@@ -321,31 +322,31 @@ mrg_status traj_setup(const GridConst &gc, FrameTraj &ft, const float *kx, const
 // ---------------------------------------------------------------------------
 // ungridding: y[s][c] = sum_taps w * grid[tap][c]  (- diff[s][c]) [* kw * taper]
 // ---------------------------------------------------------------------------
+// G lanes per sample, one lane per coil of the chunk [blockIdx.y*G, +G).  A CTA
+// walks SPB consecutive (tile-sorted) samples for one coil chunk, so the grid
+// neighbourhood it reads is small enough for L1 to catch the reuse between
+// neighbouring samples.
 template <int G>
-__global__ void __launch_bounds__(256) k_ungrid(const GridConst g, int nvalid, const float4 *__restrict__ swt,
+__global__ void __launch_bounds__(256) k_ungrid(const GridConst g, int nvalid, int spb, const float4 *__restrict__ swt,
                                                const int4 *__restrict__ sst, const float4 *__restrict__ spos,
                                                const float *__restrict__ stap, const float2 *__restrict__ grid,
                                                const float2 *__restrict__ diff, float2 *__restrict__ y, int weigh) {
-  const int64_t gid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
-  const int lane = threadIdx.x % G;
-  if (gid >= nvalid) return;
-  const int4 t = __ldg(sst + gid);
-  const int nx = t.w & 15, ny = (t.w >> 4) & 15, nz = (t.w >> 8) & 15;
-  const float *w = reinterpret_cast<const float *>(swt + 6 * gid);
-  const float4 wa = __ldg(swt + 6 * gid), wb = __ldg(swt + 6 * gid + 1);
-  const float4 wc = __ldg(swt + 6 * gid + 2), wd = __ldg(swt + 6 * gid + 3);
-  const float wx[6] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y};
-  const float wy[6] = {wc.x, wc.y, wc.z, wc.w, wd.x, wd.y};
+  constexpr int GPB = 256 / G;  // sample groups per CTA
+  const int lane = threadIdx.x % G, grp = threadIdx.x / G;
   const int C = g.C;
+  const int c = blockIdx.y * G + lane;
   const int64_t S0 = g.S[0], S1 = g.S[1];
-  float kwt_kw = 0.f, kwt_tp = 0.f;
-  if (weigh) {
-    kwt_kw = __ldg(&spos[gid].w);
-    kwt_tp = __ldg(stap + gid);
-  }
-  for (int cb = 0; cb < C; cb += G) {
-    const int c = cb + lane;
-    if (c >= C) break;
+  const int64_t s_begin = (int64_t)blockIdx.x * spb;
+  const int64_t s_end = min((int64_t)nvalid, s_begin + spb);
+  for (int64_t gid = s_begin + grp; gid < s_end; gid += GPB) {
+    const int4 t = __ldg(sst + gid);
+    const int nx = t.w & 15, ny = (t.w >> 4) & 15, nz = (t.w >> 8) & 15;
+    const float *w = reinterpret_cast<const float *>(swt + 6 * gid);
+    const float4 wa = __ldg(swt + 6 * gid), wb = __ldg(swt + 6 * gid + 1);
+    const float4 wc = __ldg(swt + 6 * gid + 2), wd = __ldg(swt + 6 * gid + 3);
+    const float wx[6] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y};
+    const float wy[6] = {wc.x, wc.y, wc.z, wc.w, wd.x, wd.y};
+    if (c >= C) continue;
     float2 acc = make_float2(0.f, 0.f);
     for (int kz = 0; kz < nz; kz++) {
       const float wz = __ldg(w + 16 + kz);
@@ -375,21 +376,27 @@ __global__ void __launch_bounds__(256) k_ungrid(const GridConst g, int nvalid, c
       acc.y -= d.y;
     }
     if (weigh) {  // temp = data * kw; temp *= taper  (src/gridFFT.cpp:1039-1108)
-      acc = make_float2(__fmul_rn(__fmul_rn(acc.x, kwt_kw), kwt_tp), __fmul_rn(__fmul_rn(acc.y, kwt_kw), kwt_tp));
+      const float kw = __ldg(&spos[gid].w), tp = __ldg(stap + gid);
+      acc = make_float2(__fmul_rn(__fmul_rn(acc.x, kw), tp), __fmul_rn(__fmul_rn(acc.y, kw), tp));
     }
     y[o] = acc;
   }
 }
 
+static int ungrid_group_default(int C) {
+  int G = 1;
+  while (G < C && G < 8) G *= 2;
+  return G;
+}
+
 mrg_status launch_ungrid(const GridConst &gc, const FrameTraj &ft, const float2 *grid, const float2 *diff, float2 *y,
                          bool weigh, cudaStream_t st) {
   if (ft.nvalid == 0) return MRG_OK;
-  int G = 1;
-  while (G < gc.C && G < 32) G *= 2;
-  const int64_t threads = (int64_t)ft.nvalid * G;
-  const int blocks = (int)((threads + 255) / 256);
+  int G = ft.ungrid_G > 0 ? ft.ungrid_G : ungrid_group_default(gc.C);
+  const int spb = ft.ungrid_spb > 0 ? ft.ungrid_spb : 256;
+  const dim3 blocks((unsigned)((ft.nvalid + spb - 1) / spb), (unsigned)((gc.C + G - 1) / G));
   const int wf = weigh ? 1 : 0;
-#define UNGRID_ARGS gc, ft.nvalid, ft.swt, ft.sst, ft.spos, ft.stap, grid, diff, y, wf
+#define UNGRID_ARGS gc, ft.nvalid, spb, ft.swt, ft.sst, ft.spos, ft.stap, grid, diff, y, wf
   switch (G) {
     case 1: k_ungrid<1><<<blocks, 256, 0, st>>>(UNGRID_ARGS); break;
     case 2: k_ungrid<2><<<blocks, 256, 0, st>>>(UNGRID_ARGS); break;
@@ -561,6 +568,8 @@ mrg_status launch_grid(const GridConst &gc, const FrameTraj &ft, const float2 *y
     MRG_LAUNCHED();
   }
   const int C = gc.C;
+  if (ft.grid_cc == 16 && C > 16) return launch_grid_cc<16>(gc, ft, yw, grid, st);
+  if (ft.grid_cc == 8 && C > 8) return launch_grid_cc<8>(gc, ft, yw, grid, st);
   if (C <= 1) return launch_grid_cc<1>(gc, ft, yw, grid, st);
   if (C <= 2) return launch_grid_cc<2>(gc, ft, yw, grid, st);
   if (C <= 4) return launch_grid_cc<4>(gc, ft, yw, grid, st);
@@ -568,6 +577,70 @@ mrg_status launch_grid(const GridConst &gc, const FrameTraj &ft, const float2 *y
   if (C <= 16) return launch_grid_cc<16>(gc, ft, yw, grid, st);
   if (C <= 24) return launch_grid_cc<24>(gc, ft, yw, grid, st);
   return launch_grid_cc<32>(gc, ft, yw, grid, st);
+}
+
+// ---------------------------------------------------------------------------
+// Autotuner: times the candidate launch shapes of this frame on the plan's own
+// buffers (contents irrelevant for timing) and keeps the fastest.
+//   ungridding: lanes per sample (coil chunk) G and samples per CTA
+//   gridding:   coils per pass CC (registers and occupancy against pair re-reads)
+// ---------------------------------------------------------------------------
+static float time_ms(cudaStream_t st, const std::function<mrg_status()> &f, int reps) {
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  if (f() != MRG_OK) {  // warm
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return 1e30f;
+  }
+  cudaEventRecord(a, st);
+  for (int r = 0; r < reps; r++)
+    if (f() != MRG_OK) break;
+  cudaEventRecord(b, st);
+  cudaEventSynchronize(b);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return ms / reps;
+}
+
+mrg_status autotune_frame(const GridConst &gc, FrameTraj &ft, float2 *grid, float2 *y, cudaStream_t st) {
+  if (ft.nvalid == 0) return MRG_OK;
+  float best = 1e30f;
+  int bestG = ungrid_group_default(gc.C), bestS = 256;
+  for (int G : {4, 8, 16, 32}) {
+    if (G > 2 * gc.C && G > 4) continue;
+    for (int spb : {128, 512}) {
+      ft.ungrid_G = G;
+      ft.ungrid_spb = spb;
+      const float ms = time_ms(st, [&]() { return launch_ungrid(gc, ft, grid, nullptr, y, false, st); }, 2);
+      if (ms < best) {
+        best = ms;
+        bestG = G;
+        bestS = spb;
+      }
+    }
+  }
+  ft.ungrid_G = bestG;
+  ft.ungrid_spb = bestS;
+  ft.tune_ungrid_ms = best;
+  best = 1e30f;
+  int bestCC = 0;
+  for (int cc : {0, 16, 8}) {
+    if (cc && gc.C <= cc) continue;
+    ft.grid_cc = cc;
+    const float ms = time_ms(st, [&]() { return launch_grid(gc, ft, y, grid, st); }, 2);
+    if (ms < best) {
+      best = ms;
+      bestCC = cc;
+    }
+  }
+  ft.grid_cc = bestCC;
+  ft.tune_grid_ms = best;
+  MRG_CUDA(cudaGetLastError());
+  return MRG_OK;
 }
 
 // ---------------------------------------------------------------------------

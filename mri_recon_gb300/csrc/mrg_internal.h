@@ -136,6 +136,9 @@ struct FrameTraj {
   int nsplit = 0;
   float2 *dsorted = nullptr;  // measured data [nvalid][C], unweighted
   bool has_data = false;
+  // launch shapes picked by autotune_frame (0: defaults)
+  int ungrid_G = 0, ungrid_spb = 0, grid_cc = 0;
+  float tune_ungrid_ms = 0.f, tune_grid_ms = 0.f;
 };
 
 mrg_status traj_setup(const GridConst &gc, FrameTraj &ft, const float *kx, const float *ky, const float *kz,
@@ -147,6 +150,9 @@ mrg_status launch_ungrid(const GridConst &gc, const FrameTraj &ft, const float2 
                          float2 *y, bool weigh, cudaStream_t st);
 // grid = scatter of the already weighted samples yw (gridFFT::chop_grid_forward); every point written.
 mrg_status launch_grid(const GridConst &gc, const FrameTraj &ft, const float2 *yw, float2 *grid, cudaStream_t st);
+// Times the candidate launch shapes of the ungridding and gridding kernels for this
+// frame on the given buffers and stores the fastest in `ft`.
+mrg_status autotune_frame(const GridConst &gc, FrameTraj &ft, float2 *grid, float2 *y, cudaStream_t st);
 // dst[s][c] = src[c*stride + perm[s]] (times kw*taper with `weigh`), s < nvalid
 mrg_status launch_gather_samples(const FrameTraj &ft, int C, const float2 *src, int64_t stride, float2 *dst,
                                  cudaStream_t st, bool weigh = false);

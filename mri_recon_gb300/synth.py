@@ -209,6 +209,8 @@ CONFIGS = {
                    seed=1237),
     "grad96": dict(N=96, coils=8, nproj=6000, nread=96, batch=4, jitter=0.05, ellipsoids=10, noise=0.01, seed=1238),
     "cg256": dict(N=256, coils=32, nproj=65536, nread=256, ellipsoids=200, noise=0.005, iters=30, seed=1239),
+    # the 256^3 x 32 kernels at 1/8 of the volume (~2 GB on the device): the case ncu profiles run on
+    "prof128": dict(N=128, coils=32, nproj=16384, nread=128, ellipsoids=50, noise=0.005, iters=5, seed=1240),
 }
 
 

@@ -62,6 +62,8 @@ static float orc_bessi0(float x) {
 struct Geom {
   int N[3], S[3], og_s[3], og_e[3];
   float grid[3], dwin[3], grid_mod[3], beta[3];
+  double kb_norm[3];  // LUT normalisation factor (analytic evaluation)
+  int eval;           // 0: LUT as the reference, 1: analytic Kaiser-Bessel
   int grid_in[3], fft_in[3];
   float k_rad;
   int lut_len;
@@ -69,9 +71,23 @@ struct Geom {
   std::vector<float> win[3];
 };
 
-static void build_geom(Geom &g, int Nx, int Ny, int Nz, float overgrid, float dwin_in, int ktype, float k_rad) {
+// I0 by its power series sum_k ((z/2)^k / k!)^2 (double; z <= 20 here).
+static double i0_series(double z) {
+  const double q = 0.25 * z * z;
+  double t = 1.0, s = 1.0;
+  for (int k = 1; k < 200; k++) {
+    t *= q / ((double)k * (double)k);
+    s += t;
+    if (t < 1e-18 * s) break;
+  }
+  return s;
+}
+
+static void build_geom(Geom &g, int Nx, int Ny, int Nz, float overgrid, float dwin_in, int ktype, float k_rad,
+                       int eval) {
   g.N[0] = Nx; g.N[1] = Ny; g.N[2] = Nz;
   g.k_rad = k_rad;
+  g.eval = eval;
   for (int d = 0; d < 3; d++) {
     g.grid_in[d] = 1;  // 3D non-Cartesian (mri_data.cpp:324-325)
     g.fft_in[d] = 1;
@@ -119,6 +135,7 @@ static void build_geom(Geom &g, int Nx, int Ny, int Nz, float overgrid, float dw
     double s = 0;
     for (float v : f) s += v;
     double scale = 0.5 * g.grid_mod[d] / s;
+    g.kb_norm[d] = scale;
     for (float &v : f) v = (float)(v * scale);
   }
   // crop (gridFFT.cpp:536-541)
@@ -249,6 +266,12 @@ struct OPlan {
   // the running product and the chop sign and rounds once, as the reference.
   inline double tap_raw(int d, R del) const {
     const std::vector<float> &f = g.lut[d];
+    if (g.eval == 1) {  // analytic Kaiser-Bessel with the LUT's normalisation
+      const double u = (double)del / ((double)g.grid_mod[d] * (double)g.dwin[d]);
+      if (u > 1.0) return 0.0;
+      const double b = (double)g.beta[d];
+      return g.kb_norm[d] * i0_series(b * std::sqrt(1.0 - u * u)) / i0_series(b);
+    }
     if (sizeof(R) == 4) {
       float delf = (float)del;
       float dd = delf - (float)((int)delf);
@@ -914,11 +937,11 @@ static void run_fista(OHandle *h, const OFrames &F, const OFistaParams &q, void 
 
 extern "C" {
 
-void *orc_plan_create(int Nx, int Ny, int Nz, float overgrid, float dwin, int ktype, float k_rad, int prec) {
+void *orc_plan_create(int Nx, int Ny, int Nz, float overgrid, float dwin, int ktype, float k_rad, int prec, int eval) {
   OHandle *h = new OHandle();
   h->prec = prec;
   Geom &g = h->g();
-  build_geom(g, Nx, Ny, Nz, overgrid, dwin, ktype, k_rad);
+  build_geom(g, Nx, Ny, Nz, overgrid, dwin, ktype, k_rad, eval);
   if (prec) h->pd.grid.assign(h->pd.gsize(), 0); else h->pf.grid.assign(h->pf.gsize(), 0);
   return h;
 }

@@ -36,7 +36,8 @@ def lib():
         L = ctypes.CDLL(_LIB_PATH)
         vp, fp, ip, dp = ctypes.c_void_p, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)
         L.orc_plan_create.restype = vp
-        L.orc_plan_create.argtypes = [ctypes.c_int] * 3 + [ctypes.c_float, ctypes.c_float, ctypes.c_int, ctypes.c_float, ctypes.c_int]
+        L.orc_plan_create.argtypes = [ctypes.c_int] * 3 + [ctypes.c_float, ctypes.c_float, ctypes.c_int, ctypes.c_float,
+                                                             ctypes.c_int, ctypes.c_int]
         L.orc_plan_destroy.argtypes = [vp]
         L.orc_plan_info.argtypes = [vp, ip, ip, fp, fp, fp, ip]
         L.orc_get_tables.argtypes = [vp, fp, fp]
@@ -98,13 +99,14 @@ class FistaParams(ctypes.Structure):
 class Plan:
     """One gridFFT operator (one coil at a time), FP32 (prec=0) or FP64 (prec=1)."""
 
-    def __init__(self, N, overgrid=1.5, dwin=-1.0, kernel=KAISER, k_rad=9999.0, prec=0):
+    def __init__(self, N, overgrid=1.5, dwin=-1.0, kernel=KAISER, k_rad=9999.0, prec=0, analytic=False):
         if np.isscalar(N):
             N = (N, N, N)
         self.N = tuple(int(n) for n in N)  # (Nx, Ny, Nz)
         self.prec = prec
         self.cdt = np.complex128 if prec else np.complex64
-        self.h = lib().orc_plan_create(self.N[0], self.N[1], self.N[2], overgrid, dwin, kernel, k_rad, prec)
+        self.h = lib().orc_plan_create(self.N[0], self.N[1], self.N[2], overgrid, dwin, kernel, k_rad, prec,
+                                       1 if analytic else 0)
         S = (ctypes.c_int * 3)()
         og = (ctypes.c_int * 3)()
         gr = (ctypes.c_float * 3)()
