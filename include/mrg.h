@@ -54,8 +54,11 @@ typedef struct mrg_config {
   int kernel_type;   /* gridFFT::kernel_type, -kaiser/-triangle/-sinc/-poly_kernel */
   float k_rad;       /* gridFFT::k_rad, Gaussian taper radius of E^H (default 9999) */
   int time_grid;     /* gridFFT::time_grid, -time_grid: print per-stage device times */
-  int tile;          /* gridding tile edge in grid points (0: autotune) */
-  int max_pairs;     /* (sample, tile) pairs per gridding work item (0: default) */
+  int tile;          /* sample-sort tile edge in grid points (0: default 8 and autotuned launch shapes) */
+  int max_pairs;     /* (sample, block) pairs per gridding work item (0: default) */
+  int kernel_eval;   /* 0: interpolate the 600-per-unit table as the reference (src/gridFFT.cpp:1113-1116);
+                        1: evaluate the Kaiser-Bessel kernel analytically (same beta and scale), the
+                        form whose derivative mrg_grad uses, for finite-difference-consistent gradients */
 } mrg_config;
 
 /* Fills the reference defaults (src/gridFFT.cpp:28-60). */
@@ -98,6 +101,11 @@ mrg_status mrg_set_traj(mrg_plan *plan, int frame, const float *kx, const float 
 mrg_status mrg_frame_info(const mrg_plan *plan, int frame, int64_t *M, int64_t *nvalid, int64_t *npairs,
                           int64_t *nitems);
 
+/* Launch shapes the autotuner chose for a frame (mrg_config.tile == 0): out = {ungrid lanes
+ * per sample, ungrid samples per CTA, gridding coils per pass (0: all), 0}; ms = the timed
+ * ungrid and grid kernels. */
+mrg_status mrg_frame_tuning(const mrg_plan *plan, int frame, int out[4], float ms[2]);
+
 /* Measured k-space of one frame: ncoil arrays of M complex64, coil c at
  * data + c*coil_stride.  Used by mrg_cg / mrg_fista (data.kdata, src/mri_data.h). */
 mrg_status mrg_set_data(mrg_plan *plan, int frame, const void *data, int64_t coil_stride, void *stream);
@@ -129,6 +137,19 @@ mrg_status mrg_forward_coil(mrg_plan *plan, int frame, const void *X, const void
  * FP64 scalars.  resid (host, may be NULL) receives sum|r|^2 after each iteration.
  * use_graph != 0 captures one iteration as a CUDA graph and replays it. */
 mrg_status mrg_cg(mrg_plan *plan, int max_iter, void *X, double *resid, int use_graph, void *stream);
+
+/* Differentiable E (no counterpart in the reference; its operator is gridFFT::backward,
+ * src/gridFFT.cpp:824-844, with unit density weights): for one frame
+ *   loss   = sum_c || E_c(x, k) - y_c ||^2                     (host double, may be NULL)
+ *   grad_x = 2 sum_c E_c^* (E_c x - y_c)  complex64 image       (the exact adjoint, no kw or taper)
+ *   grad_k = dloss/dk as float32 [3][M] (kx, ky, kz rows) in the reference's k units,
+ * from the analytic derivative of the Kaiser-Bessel kernel.  kw of the frame only selects
+ * samples (kw == 0 or outside the grid: E is 0 there and grad_k is 0).  With
+ * kernel_eval = 0 the forward interpolates the table while the derivative is analytic (they
+ * differ at the table's resolution); kernel_eval = 1 makes both analytic.
+ * y: ncoil arrays of M complex64, coil c at y + c*coil_stride. */
+mrg_status mrg_grad(mrg_plan *plan, int frame, const void *X, const void *y, int64_t coil_stride, double *loss,
+                    void *grad_x, float *grad_k, void *stream);
 
 /* The same loop in three calls, for callers that time or interleave iterations:
  * mrg_cg_init sets X = 0, R = P = sum_c E^H W d (src/recon_lib.cpp:1537-1573) and reserves

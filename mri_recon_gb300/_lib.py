@@ -27,7 +27,7 @@ _dp = ctypes.POINTER(ctypes.c_double)
 class MrgConfig(ctypes.Structure):
     _fields_ = [("overgrid", ctypes.c_float), ("dwin", ctypes.c_float), ("kernel_type", ctypes.c_int),
                 ("k_rad", ctypes.c_float), ("time_grid", ctypes.c_int), ("tile", ctypes.c_int),
-                ("max_pairs", ctypes.c_int)]
+                ("max_pairs", ctypes.c_int), ("kernel_eval", ctypes.c_int)]
 
 
 class MrgFistaParams(ctypes.Structure):
@@ -48,6 +48,7 @@ SIGNATURES = {
     "mrg_set_smaps": (_i, [_vp, _vp, _i64, _vp]),
     "mrg_set_traj": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _i64, _vp]),
     "mrg_set_data": (_i, [_vp, _i, _vp, _i64, _vp]),
+    "mrg_frame_tuning": (_i, [_vp, _i, _ip, _fp]),
     "mrg_frame_info": (_i, [_vp, _i, ctypes.POINTER(_i64), ctypes.POINTER(_i64), ctypes.POINTER(_i64),
                             ctypes.POINTER(_i64)]),
     "mrg_adjoint": (_i, [_vp, _i, _vp, _i64, _vp, _vp]),
@@ -65,6 +66,7 @@ SIGNATURES = {
     "mrg_llr_thresh": (_i, [_vp, _i, _i, _i, _i, _ip, _i, _f, _f, _i64, _vp]),
     "mrg_plan_geometry": (_i, [ctypes.POINTER(MrgConfig), _i, _i, _i, _ip, _ip, _fp, _fp, _ip, _fp, _fp]),
     "mrg_rand_stream": (_i, [_i64, _i, _ip]),
+    "mrg_grad": (_i, [_vp, _i, _vp, _vp, _i64, _dp, _vp, _fp, _vp]),
     "mrg_cg_init": (_i, [_vp, _i, _vp, _vp]),
     "mrg_cg_iterate": (_i, [_vp, _i, _vp, _i, _vp]),
     "mrg_cg_residuals": (_i, [_vp, _dp, _i, _vp]),

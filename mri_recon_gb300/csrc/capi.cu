@@ -57,6 +57,10 @@ struct mrg_plan {
   // cached CG graph
   cudaGraphExec_t cg_exec = nullptr;
   void *cg_key[2] = {nullptr, nullptr};
+  // autotuned launch shapes, reused while the sample count stays within 2x
+  int tuned_G = 0, tuned_spb = 0, tuned_cc = -1;
+  int64_t tuned_nvalid = 0;
+  float tuned_ms[2] = {0.f, 0.f};
   // FISTA state
   ThrWork thr;
   LlrWork llr;
@@ -84,6 +88,11 @@ static GridConst grid_const(const mrg_plan *p) {
   g.k_rad = p->geo.k_rad;
   g.B = p->B;
   g.C = p->C;
+  g.eval = p->cfg.kernel_eval;
+  for (int d = 0; d < 3; d++) {
+    g.beta[d] = p->geo.beta[d];
+    g.kb_norm[d] = p->geo.kb_norm[d];
+  }
   return g;
 }
 
@@ -175,8 +184,22 @@ static void tcollect(mrg_plan *p, int base) {
 // E for one frame: image X -> sorted samples y (minus diff if given); with
 // `weigh` the samples come out multiplied by kw and the taper, ready for run_EH.
 // smap: interleaved plan maps when C > 1 or an explicit single-coil map (may be NULL).
+static mrg_status run_E_grid(mrg_plan *p, const float2 *X, const float2 *smap, cudaStream_t st);
+
 static mrg_status run_E(mrg_plan *p, const FrameTraj &ft, const float2 *X, const float2 *smap, const float2 *diff,
                         float2 *y, bool weigh, cudaStream_t st) {
+  MRG_TRY(run_E_grid(p, X, smap, st));
+  tmark(p, 3, st);
+  // ungrid (src/gridFFT.cpp:1166-1322)
+  const GridConst gc = grid_const(p);
+  MRG_TRY(launch_ungrid(gc, ft, p->d_grid, diff, y, weigh, st));
+  tmark(p, 4, st);
+  tcollect(p, 0);
+  return MRG_OK;
+}
+
+// E up to the oversampled grid: set_image + z FFT, y FFT, x FFT (src/gridFFT.cpp:645-671, :972-986).
+static mrg_status run_E_grid(mrg_plan *p, const float2 *X, const float2 *smap, cudaStream_t st) {
   const Geometry &g = p->geo;
   const int C = p->C;
   const int64_t Nx = g.N[0], Ny = g.N[1], Nz = g.N[2], Sx = g.S[0], Sy = g.S[1], Sz = g.S[2];
@@ -221,12 +244,6 @@ static mrg_status run_E(mrg_plan *p, const FrameTraj &ft, const float2 *X, const
   c.in = p->d_t2; c.out = p->d_grid; c.C = C;
   fft_vectorize(c);
   MRG_TRY(launch_fft(c, st));
-  tmark(p, 3, st);
-  // ungrid (src/gridFFT.cpp:1166-1322)
-  const GridConst gc = grid_const(p);
-  MRG_TRY(launch_ungrid(gc, ft, p->d_grid, diff, y, weigh, st));
-  tmark(p, 4, st);
-  tcollect(p, 0);
   return MRG_OK;
 }
 
@@ -316,6 +333,7 @@ void mrg_config_default(mrg_config *cfg) {
   cfg->time_grid = 0;
   cfg->tile = 0;
   cfg->max_pairs = 0;
+  cfg->kernel_eval = 0;
 }
 
 const char *mrg_last_error(void) { return g_err.c_str(); }
@@ -334,7 +352,8 @@ mrg_status mrg_plan_create(const mrg_config *cfg_in, int Nx, int Ny, int Nz, int
   }
   mrg_config cfg;
   if (cfg_in) cfg = *cfg_in; else mrg_config_default(&cfg);
-  if (!(cfg.overgrid >= 1.0f) || cfg.kernel_type < 0 || cfg.kernel_type > 3) {
+  if (!(cfg.overgrid >= 1.0f) || cfg.kernel_type < 0 || cfg.kernel_type > 3 || cfg.kernel_eval < 0 ||
+      cfg.kernel_eval > 1 || (cfg.kernel_eval == 1 && cfg.kernel_type != MRG_KERNEL_KAISER)) {
     set_error("bad config");
     return MRG_ERR_INVALID;
   }
@@ -500,7 +519,25 @@ mrg_status mrg_set_traj(mrg_plan *p, int frame, const float *kx, const float *ky
                      (const float *)dw, M, p->max_pairs, st));
   invalidate_graphs(p);
   MRG_TRY(ensure_y(p, (int64_t)p->frames[frame].nvalid * p->C));
-  if (p->cfg.tile == 0) MRG_TRY(autotune_frame(gc, p->frames[frame], p->d_grid, p->d_y, st));
+  if (p->cfg.tile == 0) {
+    FrameTraj &ft = p->frames[frame];
+    const int64_t nv = ft.nvalid;
+    if (p->tuned_cc >= 0 && nv <= 2 * p->tuned_nvalid && 2 * nv >= p->tuned_nvalid) {
+      ft.ungrid_G = p->tuned_G;
+      ft.ungrid_spb = p->tuned_spb;
+      ft.grid_cc = p->tuned_cc;
+      ft.tune_ungrid_ms = p->tuned_ms[0];
+      ft.tune_grid_ms = p->tuned_ms[1];
+    } else {
+      MRG_TRY(autotune_frame(gc, ft, p->d_grid, p->d_y, st));
+      p->tuned_G = ft.ungrid_G;
+      p->tuned_spb = ft.ungrid_spb;
+      p->tuned_cc = ft.grid_cc;
+      p->tuned_nvalid = nv;
+      p->tuned_ms[0] = ft.tune_ungrid_ms;
+      p->tuned_ms[1] = ft.tune_grid_ms;
+    }
+  }
   return MRG_OK;
 }
 
@@ -512,6 +549,22 @@ mrg_status mrg_frame_info(const mrg_plan *p, int frame, int64_t *M, int64_t *nva
   if (nvalid) *nvalid = ft.nvalid;
   if (npairs) *npairs = ft.npairs;
   if (nitems) *nitems = ft.nitems;
+  return MRG_OK;
+}
+
+mrg_status mrg_frame_tuning(const mrg_plan *p, int frame, int out[4], float ms[2]) {
+  MRG_TRY(check_frame(p, frame));
+  const FrameTraj &ft = p->frames[frame];
+  if (out) {
+    out[0] = ft.ungrid_G;
+    out[1] = ft.ungrid_spb;
+    out[2] = ft.grid_cc;
+    out[3] = 0;
+  }
+  if (ms) {
+    ms[0] = ft.tune_ungrid_ms;
+    ms[1] = ft.tune_grid_ms;
+  }
   return MRG_OK;
 }
 
@@ -698,6 +751,51 @@ mrg_status mrg_forward_coil(mrg_plan *p, int frame, const void *X, const void *s
 }
 
 static mrg_status capture(mrg_plan *p, const std::function<mrg_status(cudaStream_t)> &body, cudaGraphExec_t *exec);
+
+// ---------------------------------------------------------------------------
+// Differentiable E: loss, d loss / d image, d loss / d trajectory
+// ---------------------------------------------------------------------------
+mrg_status mrg_grad(mrg_plan *p, int frame, const void *X, const void *y, int64_t coil_stride, double *loss,
+                    void *grad_x, float *grad_k, void *stream) {
+  MRG_TRY(check_frame(p, frame));
+  if (!X || !y || !grad_x || !grad_k) {
+    set_error("null argument");
+    return MRG_ERR_INVALID;
+  }
+  if (p->C > 1 && !p->has_smaps) {
+    set_error("coil maps not set");
+    return MRG_ERR_STATE;
+  }
+  FrameTraj &ft = p->frames[frame];
+  if (p->C > 1 && coil_stride < ft.M) {
+    set_error("coil_stride smaller than the sample count");
+    return MRG_ERR_INVALID;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  const GridConst gc = grid_const(p);
+  if (!ft.sdw) MRG_TRY(launch_sample_dweights(gc, ft, st));
+  const size_t ybytes = sizeof(float2) * (size_t)(coil_stride * (p->C - 1) + ft.M);
+  void *dX, *dy, *dgx, *dgk;
+  bool sX, sy, sgx, sgk;
+  MRG_TRY(dev_view(p, 0, X, sizeof(float2) * p->nimg, true, st, &dX, &sX));
+  MRG_TRY(dev_view(p, 1, y, ybytes, true, st, &dy, &sy));
+  MRG_TRY(dev_view(p, 2, grad_x, sizeof(float2) * p->nimg, false, st, &dgx, &sgx));
+  MRG_TRY(dev_view(p, 3, grad_k, sizeof(float) * 3 * (size_t)ft.M, false, st, &dgk, &sgk));
+  // E passes up to the oversampled grid (the ungrid step is replaced by the gradient gather)
+  MRG_TRY(launch_zero(&p->d_sc->e, sizeof(double), st));
+  MRG_TRY(launch_gather_samples(ft, p->C, (const float2 *)dy, coil_stride, p->d_y, st, false));
+  MRG_TRY(run_E_grid(p, (const float2 *)dX, plan_smap(p), st));
+  MRG_TRY(launch_ungrid_grad(gc, ft, p->d_grid, p->d_y, (const float2 *)dy, coil_stride, (float *)dgk,
+                             &p->d_sc->e, st));
+  // grad_x = E^*(2r): the adjoint without density weights or taper
+  MRG_TRY(launch_zero(dgx, sizeof(float2) * p->nimg, st));
+  MRG_TRY(run_EH(p, ft, p->d_y, plan_smap(p), (float2 *)dgx, st));
+  if (loss) MRG_CUDA(cudaMemcpyAsync(loss, &p->d_sc->e, sizeof(double), cudaMemcpyDeviceToHost, st));
+  if (sgx) MRG_CUDA(cudaMemcpyAsync(grad_x, dgx, sizeof(float2) * p->nimg, cudaMemcpyDeviceToHost, st));
+  if (sgk) MRG_CUDA(cudaMemcpyAsync(grad_k, dgk, sizeof(float) * 3 * (size_t)ft.M, cudaMemcpyDeviceToHost, st));
+  MRG_CUDA(cudaStreamSynchronize(st));
+  return MRG_OK;
+}
 
 // ---------------------------------------------------------------------------
 // SENSE-CG (src/recon_lib.cpp:1523-1759)

@@ -87,6 +87,7 @@ void build_geometry(Geometry &g, const mrg_config &cfg, int Nx, int Ny, int Nz) 
     double s = 0.0;
     for (float v : f) s += v;
     const double scale = 0.5 * g.grid_mod[d] / s;
+    g.kb_norm[d] = scale;
     for (float &v : f) v = (float)(v * scale);
   }
   // deapodisation windows with the chop sign, 1/S and the crop folded in,

@@ -117,6 +117,24 @@ __global__ void k_traj_sort(int64_t M, const int *__restrict__ key, const int *_
   }
 }
 
+// Analytic Kaiser-Bessel kernel with the table's beta and scale:
+//   K(d) = n I0(beta sqrt(1-u^2)) / I0(beta),  u = d / dwin  (d in grid units)
+//   K'(d) = -n beta^2 u (I1(z)/z) / (I0(beta) dwin),  z = beta sqrt(1-u^2)
+__device__ __forceinline__ double kb_value(const GridConst &g, int d, double dist) {
+  const double u = dist / (double)g.dwin[d];
+  if (u > 1.0) return 0.0;
+  const double b = (double)g.beta[d];
+  return g.kb_norm[d] * cyl_bessel_i0(b * sqrt(fmax(1.0 - u * u, 0.0))) / cyl_bessel_i0(b);
+}
+__device__ __forceinline__ double kb_deriv(const GridConst &g, int d, double dist) {
+  const double u = dist / (double)g.dwin[d];
+  if (u > 1.0) return 0.0;
+  const double b = (double)g.beta[d];
+  const double z = b * sqrt(fmax(1.0 - u * u, 0.0));
+  const double i1z = (z > 1e-6) ? cyl_bessel_i1(z) / z : 0.5 + z * z / 16.0;
+  return -g.kb_norm[d] * b * b * u * i1z / (cyl_bessel_i0(b) * (double)g.dwin[d]);
+}
+
 // Tap weights of every valid sample, computed once (src/gridFFT.cpp:1110-1148).
 __global__ void k_sample_weights(GridConst g, int nvalid, const float4 *__restrict__ spos, float4 *swt, int4 *sst) {
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nvalid; s += gridDim.x * blockDim.x) {
@@ -131,7 +149,19 @@ __global__ void k_sample_weights(GridConst g, int nvalid, const float4 *__restri
       st[d] = a;
       n[d] = b - a + 1;
 #pragma unroll
-      for (int k = 0; k < 8; k++) w[8 * d + k] = (k < n[d]) ? tap_w(g.lut[d], g.gmod[d], dk[d], a + k) : 0.0f;
+      for (int k = 0; k < 8; k++) {
+        float v = 0.0f;
+        if (k < n[d]) {
+          const int l = a + k;
+          if (g.eval == 1) {
+            const double kv = kb_value(g, d, fabs((double)dk[d] - (double)l));
+            v = (float)((l & 1) ? kv : -kv);
+          } else {
+            v = tap_w(g.lut[d], g.gmod[d], dk[d], l);
+          }
+        }
+        w[8 * d + k] = v;
+      }
     }
 #pragma unroll
     for (int k = 0; k < 6; k++) swt[6 * (int64_t)s + k] = make_float4(w[4 * k], w[4 * k + 1], w[4 * k + 2], w[4 * k + 3]);
@@ -203,6 +233,7 @@ void traj_free(FrameTraj &ft) {
   cudaFree(ft.items);
   cudaFree(ft.split_blocks);
   cudaFree(ft.dsorted);
+  cudaFree(ft.sdw);
   ft = FrameTraj();
 }
 
@@ -577,6 +608,159 @@ mrg_status launch_grid(const GridConst &gc, const FrameTraj &ft, const float2 *y
   if (C <= 16) return launch_grid_cc<16>(gc, ft, yw, grid, st);
   if (C <= 24) return launch_grid_cc<24>(gc, ft, yw, grid, st);
   return launch_grid_cc<32>(gc, ft, yw, grid, st);
+}
+
+
+// ---------------------------------------------------------------------------
+// differentiable E: d(tap weight)/dk and the fused value + derivative gather
+// ---------------------------------------------------------------------------
+__global__ void k_sample_dweights(GridConst g, int nvalid, const float4 *__restrict__ spos,
+                                  const int4 *__restrict__ sst, float4 *sdw) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nvalid; s += gridDim.x * blockDim.x) {
+    const float4 p = spos[s];
+    const int4 t = sst[s];
+    const float dk[3] = {p.x, p.y, p.z};
+    const int st[3] = {t.x, t.y, t.z};
+    const int n[3] = {t.w & 15, (t.w >> 4) & 15, (t.w >> 8) & 15};
+    float w[24];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+        float v = 0.0f;
+        if (k < n[d]) {
+          const int l = st[d] + k;
+          const double diff = (double)dk[d] - (double)l;
+          // d/dk [chop(l) K(|dk - l|)] = chop(l) K'(|d|) sign(d) * grid ratio
+          double dv = kb_deriv(g, d, fabs(diff)) * (diff < 0 ? -1.0 : 1.0) * (double)g.grid[d];
+          v = (float)((l & 1) ? dv : -dv);
+        }
+        w[8 * d + k] = v;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 6; k++) sdw[6 * (int64_t)s + k] = make_float4(w[4 * k], w[4 * k + 1], w[4 * k + 2], w[4 * k + 3]);
+  }
+}
+
+mrg_status launch_sample_dweights(const GridConst &gc, FrameTraj &ft, cudaStream_t st) {
+  if (!ft.sdw) MRG_CUDA(cudaMalloc(&ft.sdw, sizeof(float4) * 6 * (size_t)std::max(ft.nvalid, 1)));
+  if (ft.nvalid == 0) return MRG_OK;
+  k_sample_dweights<<<grid_blocks(ft.nvalid, 256), 256, 0, st>>>(gc, ft.nvalid, ft.spos, ft.sst, ft.sdw);
+  MRG_LAUNCHED();
+  return MRG_OK;
+}
+
+template <int G>
+__global__ void __launch_bounds__(256) k_ungrid_grad(const GridConst g, int nvalid, int64_t M,
+                                                    const float4 *__restrict__ swt, const float4 *__restrict__ sdw,
+                                                    const int4 *__restrict__ sst, const int *__restrict__ perm,
+                                                    const float2 *__restrict__ grid, float2 *__restrict__ ys,
+                                                    float *__restrict__ gk, double *loss) {
+  const int64_t gid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
+  const int lane = threadIdx.x % G;
+  const bool valid = gid < nvalid;
+  const int C = g.C;
+  const int64_t S0 = g.S[0], S1 = g.S[1];
+  float gx = 0.f, gy = 0.f, gz = 0.f;
+  double ls = 0.0;
+  if (valid) {
+    const int4 t = __ldg(sst + gid);
+    const int nx = t.w & 15, ny = (t.w >> 4) & 15, nz = (t.w >> 8) & 15;
+    const float *w = reinterpret_cast<const float *>(swt + 6 * gid);
+    const float *dw = reinterpret_cast<const float *>(sdw + 6 * gid);
+    for (int cb = 0; cb < C; cb += G) {
+      const int c = cb + lane;
+      if (c >= C) break;
+      float2 v = make_float2(0.f, 0.f), vx = v, vy = v, vz = v;
+      for (int kz = 0; kz < nz; kz++) {
+        const float wz = __ldg(w + 16 + kz), dwz = __ldg(dw + 16 + kz);
+        for (int ky = 0; ky < ny; ky++) {
+          const float wyv = __ldg(w + 8 + ky), dwy = __ldg(dw + 8 + ky);
+          const float a = wz * wyv, bz = dwz * wyv, by = wz * dwy;
+          const float2 *row = grid + (((int64_t)(t.z + kz) * S1 + (t.y + ky)) * S0 + t.x) * C + c;
+          for (int kx = 0; kx < nx; kx++) {
+            const float wxv = __ldg(w + kx), dwx = __ldg(dw + kx);
+            const float2 gv = __ldg(row + (int64_t)kx * C);
+            const float f0 = a * wxv, fx = a * dwx, fy = by * wxv, fz = bz * wxv;
+            v.x += f0 * gv.x; v.y += f0 * gv.y;
+            vx.x += fx * gv.x; vx.y += fx * gv.y;
+            vy.x += fy * gv.x; vy.y += fy * gv.y;
+            vz.x += fz * gv.x; vz.y += fz * gv.y;
+          }
+        }
+      }
+      const int64_t o = gid * C + c;
+      const float2 yv = ys[o];
+      const float2 r = make_float2(v.x - yv.x, v.y - yv.y);
+      ys[o] = make_float2(2.f * r.x, 2.f * r.y);
+      // dL/dk = sum_c 2 Re(conj(r) dv/dk)
+      gx += 2.f * (r.x * vx.x + r.y * vx.y);
+      gy += 2.f * (r.x * vy.x + r.y * vy.y);
+      gz += 2.f * (r.x * vz.x + r.y * vz.y);
+      ls += (double)r.x * r.x + (double)r.y * r.y;
+    }
+  }
+#pragma unroll
+  for (int off = G / 2; off > 0; off >>= 1) {
+    gx += __shfl_xor_sync(0xffffffffu, gx, off);
+    gy += __shfl_xor_sync(0xffffffffu, gy, off);
+    gz += __shfl_xor_sync(0xffffffffu, gz, off);
+  }
+  if (valid && lane == 0) {
+    const int64_t u = perm[gid];
+    gk[u] = gx;
+    gk[M + u] = gy;
+    gk[2 * M + u] = gz;
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) ls += __shfl_xor_sync(0xffffffffu, ls, off);
+  if ((threadIdx.x & 31) == 0 && ls != 0.0) atomicAdd(loss, ls);
+}
+
+// Samples that do not contribute: E is 0 there, so r = -y and dL/dk = 0.
+__global__ void k_grad_invalid(int64_t M, int nvalid, int C, const int *__restrict__ perm,
+                               const float2 *__restrict__ y, int64_t stride, float *gk, double *loss) {
+  double ls = 0.0;
+  for (int64_t s = nvalid + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < M; s += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t u = perm[s];
+    gk[u] = 0.f;
+    gk[M + u] = 0.f;
+    gk[2 * M + u] = 0.f;
+    for (int c = 0; c < C; c++) {
+      const float2 v = y[(int64_t)c * stride + u];
+      ls += (double)v.x * v.x + (double)v.y * v.y;
+    }
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) ls += __shfl_xor_sync(0xffffffffu, ls, off);
+  if ((threadIdx.x & 31) == 0 && ls != 0.0) atomicAdd(loss, ls);
+}
+
+mrg_status launch_ungrid_grad(const GridConst &gc, const FrameTraj &ft, const float2 *grid, float2 *ysorted,
+                              const float2 *y_user, int64_t stride, float *grad_k, double *loss, cudaStream_t st) {
+  if (ft.nvalid > 0) {
+    int G = 1;
+    while (G < gc.C && G < 32) G *= 2;
+    const int blocks = (int)(((int64_t)ft.nvalid * G + 255) / 256);
+#define GRAD_ARGS gc, ft.nvalid, ft.M, ft.swt, ft.sdw, ft.sst, ft.perm, grid, ysorted, grad_k, loss
+    switch (G) {
+      case 1: k_ungrid_grad<1><<<blocks, 256, 0, st>>>(GRAD_ARGS); break;
+      case 2: k_ungrid_grad<2><<<blocks, 256, 0, st>>>(GRAD_ARGS); break;
+      case 4: k_ungrid_grad<4><<<blocks, 256, 0, st>>>(GRAD_ARGS); break;
+      case 8: k_ungrid_grad<8><<<blocks, 256, 0, st>>>(GRAD_ARGS); break;
+      case 16: k_ungrid_grad<16><<<blocks, 256, 0, st>>>(GRAD_ARGS); break;
+      default: k_ungrid_grad<32><<<blocks, 256, 0, st>>>(GRAD_ARGS); break;
+    }
+#undef GRAD_ARGS
+    MRG_LAUNCHED();
+  }
+  if (ft.M > ft.nvalid) {
+    k_grad_invalid<<<grid_blocks(ft.M - ft.nvalid, 256), 256, 0, st>>>(ft.M, ft.nvalid, gc.C, ft.perm, y_user, stride,
+                                                                       grad_k, loss);
+    MRG_LAUNCHED();
+  }
+  return MRG_OK;
 }
 
 // ---------------------------------------------------------------------------

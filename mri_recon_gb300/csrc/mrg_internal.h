@@ -50,6 +50,7 @@ inline void count_launch(int n = 1) { g_launches.fetch_add(n, std::memory_order_
 struct Geometry {
   int N[3], S[3], og[3];
   float grid[3], dwin[3], beta[3], grid_mod[3];
+  double kb_norm[3];  // the table's normalisation factor (analytic evaluation uses the same scale)
   float k_rad;
   int kernel_type;
   int lut_len;
@@ -118,6 +119,9 @@ struct GridConst {
   int nt[3];   // sort tiles per axis
   int nb[3];   // gridding blocks per axis
   int C;       // coils
+  int eval;    // 0: table interpolation, 1: analytic Kaiser-Bessel
+  float beta[3];
+  double kb_norm[3];
 };
 
 struct FrameTraj {
@@ -135,6 +139,7 @@ struct FrameTraj {
   int *split_blocks = nullptr;
   int nsplit = 0;
   float2 *dsorted = nullptr;  // measured data [nvalid][C], unweighted
+  float4 *sdw = nullptr;      // [nvalid][6] d(tap weight)/dk per axis (allocated by mrg_grad)
   bool has_data = false;
   // launch shapes picked by autotune_frame (0: defaults)
   int ungrid_G = 0, ungrid_spb = 0, grid_cc = 0;
@@ -150,6 +155,13 @@ mrg_status launch_ungrid(const GridConst &gc, const FrameTraj &ft, const float2 
                          float2 *y, bool weigh, cudaStream_t st);
 // grid = scatter of the already weighted samples yw (gridFFT::chop_grid_forward); every point written.
 mrg_status launch_grid(const GridConst &gc, const FrameTraj &ft, const float2 *yw, float2 *grid, cudaStream_t st);
+// d(weights)/dk per sample (analytic Kaiser-Bessel derivative), for mrg_grad.
+mrg_status launch_sample_dweights(const GridConst &gc, FrameTraj &ft, cudaStream_t st);
+// Per sample: v = E x (from the grid), r = v - ysorted; writes 2r over ysorted, grad_k
+// (user order, [3][M]) and adds sum |r|^2 (and sum |y|^2 of the non-contributing samples
+// read from the user's y) into *loss.
+mrg_status launch_ungrid_grad(const GridConst &gc, const FrameTraj &ft, const float2 *grid, float2 *ysorted,
+                              const float2 *y_user, int64_t stride, float *grad_k, double *loss, cudaStream_t st);
 // Times the candidate launch shapes of the ungridding and gridding kernels for this
 // frame on the given buffers and stores the fastest in `ft`.
 mrg_status autotune_frame(const GridConst &gc, FrameTraj &ft, float2 *grid, float2 *y, cudaStream_t st);

@@ -67,7 +67,7 @@ class Plan:
     """Coil-batched gridFFT plan with ``ncoils`` coils and ``nframes`` trajectories."""
 
     def __init__(self, N, ncoils=1, nframes=1, overgrid=1.5, dwin=-1.0, kernel_type=KAISER_KERNEL, k_rad=9999.0,
-                 tile=0, max_pairs=0, time_grid=0):
+                 tile=0, max_pairs=0, time_grid=0, analytic_kernel=False):
         L = _lib.load()
         if np.isscalar(N):
             N = (N, N, N)
@@ -77,6 +77,7 @@ class Plan:
         L.mrg_config_default(ctypes.byref(cfg))
         cfg.overgrid, cfg.dwin, cfg.kernel_type, cfg.k_rad = overgrid, dwin, kernel_type, k_rad
         cfg.tile, cfg.max_pairs, cfg.time_grid = tile, max_pairs, time_grid
+        cfg.kernel_eval = 1 if analytic_kernel else 0
         h = ctypes.c_void_p()
         _lib.check(L.mrg_plan_create(ctypes.byref(cfg), self.N[0], self.N[1], self.N[2], self.ncoils, self.nframes,
                                      ctypes.byref(h)))
@@ -134,6 +135,13 @@ class Plan:
         _lib.check(_lib.load().mrg_frame_info(self._h, frame, *[ctypes.byref(x) for x in v]))
         return dict(zip(("M", "nvalid", "npairs", "nitems"), (x.value for x in v)))
 
+    def frame_tuning(self, frame):
+        out = (ctypes.c_int * 4)()
+        ms = (ctypes.c_float * 2)()
+        _lib.check(_lib.load().mrg_frame_tuning(self._h, frame, out, ms))
+        return dict(ungrid_lanes=out[0], ungrid_samples_per_cta=out[1], grid_coils_per_pass=out[2],
+                    ungrid_ms=ms[0], grid_ms=ms[1])
+
     def set_data(self, frame, data, stream=None):
         """data: (C, M) complex64."""
         a = _Args()
@@ -186,6 +194,24 @@ class Plan:
                                                 a.ptr(out), a.ptr(diff, np.complex64), _stream(stream)))
         return out
 
+    def grad(self, frame, X, y, stream=None):
+        """loss = sum_c ||E_c X - y_c||^2, grad_x = 2 E^*(E X - y), grad_k = dloss/dk [3, M].
+
+        Device tensors in, device tensors out (host arrays in, numpy out)."""
+        a = _Args()
+        M = self.M[frame]
+        if _is_tensor(X) and X.is_cuda:
+            gx = torch.empty(self.ishape, dtype=torch.complex64, device=X.device)
+            gk = torch.empty((3, M), dtype=torch.float32, device=X.device)
+        else:
+            gx = np.zeros(self.ishape, np.complex64)
+            gk = np.zeros((3, M), np.float32)
+        loss = ctypes.c_double()
+        gkp = gk.data_ptr() if _is_tensor(gk) else gk.ctypes.data
+        _lib.check(_lib.load().mrg_grad(self._h, frame, a.ptr(X, np.complex64), a.ptr(y, np.complex64), M,
+                                        ctypes.byref(loss), a.ptr(gx), ctypes.cast(gkp, _lib._fp), _stream(stream)))
+        return loss.value, gx, gk
+
     # -- solvers --------------------------------------------------------------
     def cg(self, iters, X=None, use_graph=True, stream=None):
         """SENSE-CG from x0 = 0.  Returns (X (nframes, Nz, Ny, Nx), residual history)."""
@@ -235,6 +261,28 @@ class Plan:
         _lib.check(_lib.load().mrg_fista(self._h, ctypes.byref(params), a.ptr(X), resid.ctypes.data_as(_lib._dp),
                                          ctypes.byref(step), int(bool(use_graph)), _stream(stream)))
         return X, resid[:params.max_iter], step.value
+
+
+if torch is not None:
+    class NufftLoss(torch.autograd.Function):
+        """loss = sum_c ||E_c(x, k) - y_c||^2 as a torch autograd function of the image x
+        (complex64, (Nz, Ny, Nx)) and the trajectory k (float32, (3, M)); gradients from
+        mrg_grad.  `plan` is a Plan whose frame 0 is re-pointed at k on every call with
+        unit weights (kw = 1)."""
+
+        @staticmethod
+        def forward(ctx, x, k, y, plan):
+            kw = torch.ones(k.shape[1], dtype=torch.float32, device=k.device)
+            plan.set_traj(0, k[0].contiguous(), k[1].contiguous(), k[2].contiguous(), kw)
+            loss, gx, gk = plan.grad(0, x.contiguous(), y.contiguous())
+            ctx.save_for_backward(gx, gk)
+            return torch.tensor(loss, dtype=torch.float64, device=x.device)
+
+        @staticmethod
+        def backward(ctx, g):
+            gx, gk = ctx.saved_tensors
+            gf = g.to(torch.float32)
+            return gx * gf, gk * gf, None, None
 
 
 def fista_params(**kw):

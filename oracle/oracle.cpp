@@ -994,6 +994,42 @@ void orc_ungrid(void *hv, void *data, const float *kx, const float *ky, const fl
   if (h->prec) h->pd.grid_backward((cx<double> *)data, kx, ky, kz, kw, M, (const cx<double> *)diff);
   else h->pf.grid_backward((cx<float> *)data, kx, ky, kz, kw, M, (const cx<float> *)diff);
 }
+// FP64 sample values at double-precision positions on the plan's current grid
+// (after orc_set_image + orc_fft3): the forward of chop_grid_backward without
+// the kw test, for finite-difference checks of trajectory gradients.
+void orc_values_at(void *hv, const double *kx, const double *ky, const double *kz, long n, void *out) {
+  OHandle *h = (OHandle *)hv;
+  OPlan<double> &p = h->pd;
+  const Geom &g = p.g;
+  cx<double> *o = (cx<double> *)out;
+#pragma omp parallel for
+  for (long i = 0; i < n; i++) {
+    const double kk[3] = {kx[i], ky[i], kz[i]};
+    double dk[3];
+    int s[3], e[3];
+    bool ok = true;
+    for (int d = 0; d < 3; d++) {
+      dk[d] = kk[d] * (double)g.grid[d] + (double)(g.S[d] / 2);
+      s[d] = std::max((int)std::ceil(dk[d] - (double)g.dwin[d]), 0);
+      e[d] = std::min((int)std::floor(dk[d] + (double)g.dwin[d]), g.S[d] - 1);
+      ok = ok && !(s[d] >= g.S[d] || e[d] < 0);
+    }
+    cx<double> acc(0, 0);
+    if (ok)
+      for (int lz = s[2]; lz <= e[2]; lz++) {
+        double wz = p.tap_raw(2, std::fabs((double)g.grid_mod[2] * (dk[2] - lz))) * (2 * (lz % 2) - 1);
+        for (int ly = s[1]; ly <= e[1]; ly++) {
+          double wy = wz * p.tap_raw(1, std::fabs((double)g.grid_mod[1] * (dk[1] - ly))) * (2 * (ly % 2) - 1);
+          for (int lx = s[0]; lx <= e[0]; lx++) {
+            double w = wy * p.tap_raw(0, std::fabs((double)g.grid_mod[0] * (dk[0] - lx))) * (2 * (lx % 2) - 1);
+            acc += w * p.grid[(long)lx + (long)g.S[0] * (ly + (long)g.S[1] * lz)];
+          }
+        }
+      }
+    o[i] = acc;
+  }
+}
+
 void orc_set_image(void *hv, const void *X, const void *smap) {
   OHandle *h = (OHandle *)hv;
   if (h->prec) h->pd.set_image((const cx<double> *)X, (const cx<double> *)smap);

@@ -48,6 +48,7 @@ def lib():
         L.orc_grid.argtypes = [vp, vp, fp, fp, fp, fp, ctypes.c_long]
         L.orc_ungrid.argtypes = [vp, vp, fp, fp, fp, fp, ctypes.c_long, vp]
         L.orc_set_image.argtypes = [vp, vp, vp]
+        L.orc_values_at.argtypes = [vp, dp, dp, dp, ctypes.c_long, vp]
         L.orc_accumulate.argtypes = [vp, vp, vp]
         L.orc_fft3.argtypes = [vp, ctypes.c_int]
         L.orc_fft1d.argtypes = [ctypes.c_int, vp, ctypes.c_int, ctypes.c_int]
@@ -190,6 +191,18 @@ class Plan:
         X, smap = self._c(X), self._c(smap)
         lib().orc_set_image(self.h, _ptr(X), _ptr(smap))
         return self.get_grid()
+
+    def values_at(self, X, smap, kx, ky, kz):
+        """FP64 plans: E X (one coil, no kw test) at float64 positions, for finite differences."""
+        assert self.prec == 1
+        self.set_image(X, smap)
+        lib().orc_fft3(self.h, -1)
+        k = [np.ascontiguousarray(v, dtype=np.float64) for v in (kx, ky, kz)]
+        out = np.zeros(k[0].size, np.complex128)
+        dp = ctypes.POINTER(ctypes.c_double)
+        lib().orc_values_at(self.h, k[0].ctypes.data_as(dp), k[1].ctypes.data_as(dp), k[2].ctypes.data_as(dp),
+                            k[0].size, _ptr(out))
+        return out
 
     def accumulate(self, grid, X, smap):
         self.set_grid(grid)
