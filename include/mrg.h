@@ -200,6 +200,21 @@ mrg_status mrg_soft_threshold(void *X, int64_t n, float value, void *stream);
 /* LOWRANKCOIL::update_threshold (src/clear.cpp:233-351) in time, Ne = 1: returns smax. */
 mrg_status mrg_llr_update_threshold(const void *X, int nframes, int Nx, int Ny, int Nz, const int block[3],
                                     float clear_amp, float clear_t2, int iteration, float *smax, void *stream);
+/* Variant of mrg_llr_update_threshold that allocates no device memory; it has no
+ * counterpart in the reference.  For callers that cannot call cudaMalloc (a fixed GPU
+ * memory budget reserved up front, or a pipeline that must not synchronise the device
+ * between kernels), its scratch lives in a fixed device array of the library, sized for
+ * at most MRG_NOALLOC_MAX_BLOCKS low-rank blocks (512 KiB held by every GPU that loads the
+ * library until exit); more blocks return MRG_ERR_UNSUPPORTED.  X must be device memory;
+ * smax may be host or device memory (a host smax makes the call wait for the result).
+ * The first call on a device looks up the array's device address; make that first call
+ * before any stream capture.  All calls share the one array, so calls that overlap on the
+ * GPU (other streams or threads) race; serialise them. */
+#define MRG_NOALLOC_MAX_BLOCKS 32768
+mrg_status mrg_llr_update_threshold_noalloc(const void *X, int nframes, int Nx, int Ny, int Nz, const int block[3],
+                                            float clear_amp, float clear_t2, int iteration, float *smax,
+                                            void *stream);
+
 /* LOWRANKCOIL::thresh (src/clear.cpp:356-556) in time, Ne = 1, with the block shifts
  * drawn from the rand() stream after rand_skip draws. */
 mrg_status mrg_llr_thresh(void *X, int nframes, int Nx, int Ny, int Nz, const int block[3], int block_iter,

@@ -64,6 +64,7 @@ SIGNATURES = {
     "mrg_soft_threshold": (_i, [_vp, _i64, _f, _vp]),
     "mrg_llr_update_threshold": (_i, [_vp, _i, _i, _i, _i, _ip, _f, _f, _i, _fp, _vp]),
     "mrg_llr_thresh": (_i, [_vp, _i, _i, _i, _i, _ip, _i, _f, _f, _i64, _vp]),
+    "mrg_llr_update_threshold_noalloc": (_i, [_vp, _i, _i, _i, _i, _ip, _f, _f, _i, _fp, _vp]),
     "mrg_plan_geometry": (_i, [ctypes.POINTER(MrgConfig), _i, _i, _i, _ip, _ip, _fp, _fp, _ip, _fp, _fp]),
     "mrg_rand_stream": (_i, [_i64, _i, _ip]),
     "mrg_grad": (_i, [_vp, _i, _vp, _vp, _i64, _dp, _vp, _fp, _vp]),

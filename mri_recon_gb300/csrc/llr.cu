@@ -259,21 +259,33 @@ static void llr_geom(LlrArgs &a, float2 *X, int Nt, const int N[3], const int bs
   }
 }
 
-mrg_status llr_update_ex(const float2 *X, int Nt, const int N[3], const int bs[3], float amp, float t2,
-                         const Scalars *sc, int iter_fixed, LlrWork &w, cudaStream_t st) {
+int llr_block_count(const int N[3], const int bs[3]) {
+  int nb = 1;
+  for (int d = 0; d < 3; d++) nb *= N[d] / std::min(bs[d], N[d]);
+  return nb;
+}
+
+mrg_status llr_update_into(const float2 *X, int Nt, const int N[3], const int bs[3], float amp, float t2,
+                           const Scalars *sc, int iter_fixed, double *sig, double *work, float *smax, cudaStream_t st) {
   LlrArgs a;
   memset(&a, 0, sizeof(a));
   int nblocks;
   llr_geom(a, const_cast<float2 *>(X), Nt, N, bs, nblocks);
-  MRG_TRY(llr_alloc(w, nblocks));
   a.mode = 0;
-  a.sig = w.sig;
+  a.sig = sig;
   MRG_TRY(llr_launch(a, nblocks, st));
   int np2 = 1;
   while (np2 < nblocks) np2 <<= 1;
-  k_llr_median<<<1, 1024, 0, st>>>(w.sig, nblocks, w.sig + nblocks, np2, amp, t2, sc, iter_fixed, w.smax);
+  k_llr_median<<<1, 1024, 0, st>>>(sig, nblocks, work, np2, amp, t2, sc, iter_fixed, smax);
   MRG_LAUNCHED();
   return MRG_OK;
+}
+
+mrg_status llr_update_ex(const float2 *X, int Nt, const int N[3], const int bs[3], float amp, float t2,
+                         const Scalars *sc, int iter_fixed, LlrWork &w, cudaStream_t st) {
+  const int nblocks = llr_block_count(N, bs);
+  MRG_TRY(llr_alloc(w, nblocks));
+  return llr_update_into(X, Nt, N, bs, amp, t2, sc, iter_fixed, w.sig, w.sig + nblocks, w.smax, st);
 }
 
 mrg_status llr_update(const float2 *X, int Nt, const int N[3], const int bs[3], float amp, float t2,

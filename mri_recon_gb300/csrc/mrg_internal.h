@@ -236,6 +236,10 @@ mrg_status llr_alloc(LlrWork &w, int nblocks);
 void llr_free(LlrWork &w);
 mrg_status llr_update(const float2 *X, int Nt, const int N[3], const int bs[3], float amp, float t2,
                       const int *iter_dev, LlrWork &w, cudaStream_t st);
+int llr_block_count(const int N[3], const int bs[3]);
+// sigma_1 of every block into sig[nblocks], median via work[next pow2 >= nblocks], result in *smax (device).
+mrg_status llr_update_into(const float2 *X, int Nt, const int N[3], const int bs[3], float amp, float t2,
+                           const Scalars *sc, int iter_fixed, double *sig, double *work, float *smax, cudaStream_t st);
 mrg_status llr_update_ex(const float2 *X, int Nt, const int N[3], const int bs[3], float amp, float t2,
                          const Scalars *sc, int iter_fixed, LlrWork &w, cudaStream_t st);
 mrg_status llr_apply_ex(float2 *X, int Nt, const int N[3], const int bs[3], int block_iter, float alpha,
