@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--e2e-solves", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain per-coil GPU path")
+    ap.add_argument("--no-side-configs", dest="side_configs", action="store_false",
+                    help="skip the throughput of the four smaller configurations")
     return ap.parse_args()
 
 
@@ -81,9 +83,20 @@ def bytes_model(c, nvalid, npairs):
 
 
 STAGES = ["E_zfft_setimg", "E_yfft", "E_xfft", "E_ungrid", "EH_grid", "EH_xfft", "EH_yfft", "EH_zfft_accum"]
-KERNEL_OF = {"E_zfft_setimg": "k_fft<Q,-1,SETIMG>", "E_yfft": "k_fft<Q,-1,PLAIN>", "E_xfft": "k_fft<Q,-1,PLAIN>",
-             "E_ungrid": "k_ungrid<32>", "EH_grid": "k_grid<32,true>", "EH_xfft": "k_fft<Q,+1,PLAIN>",
-             "EH_yfft": "k_fft<Q,+1,PLAIN>", "EH_zfft_accum": "k_fft<Q,+1,ACCUM>"}
+
+
+def kernel_of(stage, tuning, C):
+    """Kernel that runs a stage, with the launch shape the autotuner picked."""
+    if stage == "E_ungrid":
+        return "k_ungrid<%d,%d>" % (tuning["ungrid_lanes"], max(tuning["ungrid_coils_per_lane"], 1))
+    if stage == "EH_grid":
+        cc = tuning["grid_coils_per_pass"]
+        if cc < 0:
+            return "k_grid_mma<%d> (TF32 tensor cores, %d coils per pass)" % (-cc, -4 * cc)
+        return "k_grid<%d> (FP32 CUDA cores)" % (cc if cc > 0 else min(C, 32))
+    return {"E_zfft_setimg": "k_fft<Q,-1,SETIMG>", "E_yfft": "k_fft<Q,-1,PLAIN>", "E_xfft": "k_fft<Q,-1,PLAIN>",
+            "EH_xfft": "k_fft<Q,+1,PLAIN>", "EH_yfft": "k_fft<Q,+1,PLAIN>",
+            "EH_zfft_accum": "k_fft<Q,+1,ACCUM>"}[stage]
 
 
 def peaks():
@@ -207,6 +220,88 @@ def run_reference(a):
     print(json.dumps(line), flush=True)
 
 
+def side_configs(dev):
+    """Throughput of the four smaller configurations, device-timed with inputs resident:
+    SENSE-CG 64^3 x 8 (iter/s), FISTA-wavelet 128^3 x 16 (iter/s), FISTA-wavelet + time
+    low-rank 128^3 x 20 coils x 10 frames (iter/s), and the differentiable NUFFT at 96^3 x 8
+    (loss + image and trajectory gradients per second, batch of 4 trajectories)."""
+    import torch
+
+    import mri_recon_gb300 as m
+    from mri_recon_gb300 import synth
+
+    def timed(fn):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1000.0
+
+    def setup(c, T, projs, jitter=0.0):
+        N, C = c["N"], c["coils"]
+        p = m.Plan(N, C, T)
+        p.set_smaps(synth.coil_maps_torch(N, C, dev, seed=c["seed"] + 1))
+        img = torch.from_numpy(synth.phantom(N, c["ellipsoids"], seed=c["seed"])).to(dev)
+        start = 0
+        for t in range(T):
+            kx, ky, kz, kw = synth.radial_trajectory(N, int(projs[t]), c["nread"], start=start, jitter_grid=jitter,
+                                                     seed=c["seed"] + t)
+            start += int(projs[t])
+            p.set_traj(t, kx, ky, kz, kw)
+            y = p.forward(t, img)
+            y += c["noise"] * float(y.abs().max()) * torch.complex(torch.randn_like(y.real), torch.randn_like(y.real))
+            p.set_data(t, y)
+        return p, img
+
+    out = {}
+    c = synth.CONFIGS["cg64"]
+    p, _ = setup(c, 1, [c["nproj"]])
+    X = torch.empty((1,) + p.ishape, dtype=torch.complex64, device=dev)
+    p.cg_init(40, X)
+    p.cg_iterate(3, X)
+    dt = timed(lambda: p.cg_iterate(20, X))
+    out["cg64"] = {"metric": "SENSE-CG iter/s, 64^3 x 8 coils, 4096 x 64 radial", "value": 20 / dt, "unit": "iter/s"}
+    del p
+
+    def fista_rate(p, **kw):
+        base = dict(max_eig_iter=30, cycle_spins=4, wave_levels=(3, 3, 3), wave_type=1, thresh=0.1, use_threshold=1)
+        base.update(kw)
+        p.fista(m.fista_params(max_iter=2, **base))
+        t_lo = timed(lambda: p.fista(m.fista_params(max_iter=5, **base)))
+        t_hi = timed(lambda: p.fista(m.fista_params(max_iter=25, **base)))
+        return 20 / (t_hi - t_lo)
+
+    c = synth.CONFIGS["fista128"]
+    p, _ = setup(c, 1, [c["nproj"]])
+    out["fista128"] = {"metric": "FISTA-wavelet iter/s, 128^3 x 16 coils, 16384 x 128 radial, db4 3 levels, "
+                                 "4 cycle spins, fraction threshold 0.1", "value": fista_rate(p), "unit": "iter/s"}
+    del p
+    c = synth.CONFIGS["llr128"]
+    projs = synth.frame_projection_counts(c["frames"], c["proj_lo"], c["proj_hi"], c["seed"])
+    p, _ = setup(c, c["frames"], projs)
+    out["llr128"] = {"metric": "FISTA-wavelet + time low-rank iter/s, 128^3 x 20 coils x 10 frames "
+                               "(1500-3500 projections each), 8^3 blocks", "unit": "iter/s",
+                     "value": fista_rate(p, llr_block=(8, 8, 8), llr_block_iter=4, llr_alpha=0.001)}
+    del p
+    c = synth.CONFIGS["grad96"]
+    p, img = setup(c, c["batch"], [c["nproj"]] * c["batch"], jitter=c["jitter"])
+    ys = [torch.randn((c["coils"], p.M[t]), dtype=torch.complex64, device=dev) for t in range(c["batch"])]
+
+    def grads():
+        for t in range(c["batch"]):
+            p.grad(t, img, ys[t])
+    grads()
+    dt = timed(lambda: [grads() for _ in range(3)])
+    out["grad96"] = {"metric": "differentiable NUFFT evaluations/s (loss, image and trajectory gradients), "
+                               "96^3 x 8 coils, 6000 x 96 jittered radial", "value": 3 * c["batch"] / dt,
+                     "unit": "evals/s"}
+    del p
+    torch.cuda.synchronize()
+    return out
+
+
 def run_ours(a):
     import torch
     import torch.distributed as dist
@@ -280,7 +375,7 @@ def run_ours(a):
     peak, peak_kind = peaks()
     achieved = bm[dom] / (per_launch_ms[dom] / 1000.0) / 1e9
     iter_bytes = sum(bm.values()) + 9 * N ** 3 * 8
-    roofline = {"bound": "hbm", "kernel": KERNEL_OF[dom], "stage": dom, "achieved": achieved, "peak": peak,
+    roofline = {"bound": "hbm", "kernel": kernel_of(dom, out_tuning, C), "stage": dom, "achieved": achieved, "peak": peak,
                 "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
                 "traffic": ncu_traffic(dom), "algorithmic_bytes_per_launch": bm[dom],
                 "launch_ms": per_launch_ms[dom]}
@@ -368,6 +463,10 @@ def run_ours(a):
                       "d2h_bytes_per_step": int(N ** 3 * 8 + iters * 8),
                       "step": "one %d-iteration solve: trajectory + k-space host->device, set-up, CG, image "
                               "device->host" % iters}
+    if a.side_configs and rank == 0:
+        del plan
+        torch.cuda.empty_cache()
+        out["other_configs"] = side_configs(dev)
     if world > 1:
         dist.barrier()
         dist.destroy_process_group()

@@ -7,10 +7,13 @@
 //   forward(X, smap, data, kx, ky, kz, kw, M)            X += E^H (data * kw)
 //   backward(X, smap, data, kx, ky, kz, kw, M)           data = E X
 //   backward_residual(X, smap, data, kx, ky, kz, kw, M, diff)   data = E X - diff
+//   forward_sos(X, data, kx, ky, kz, kw, M)              X += |deapp(E^H (data * kw))|^2
 // Images are complex<float>[Nz][Ny][Nx] (x fastest), k-space complex<float>[M],
 // trajectories float[M] in the reference's units.  Pointers may be host or
 // device memory.  Errors throw std::runtime_error with the library's message
 // instead of exit(1).
+// k_rad may be changed between calls, as recon_lib does around the coil-map
+// estimate (src/recon_lib.cpp:2738, :2786); the next call applies it.
 //
 // A trajectory is uploaded and sorted on the first call that passes it and
 // reused while the same arrays (same addresses and length) are passed, which is
@@ -62,7 +65,14 @@ class gridFFT {
   void forward(cf *X, const cf *smap, const cf *data, const float *kx, const float *ky, const float *kz,
                const float *kw, int64_t M, void *stream = nullptr) {
     traj(kx, ky, kz, kw, M, stream);
+    sync_k_rad(stream);
     check(mrg_adjoint_coil(plan_, 0, smap, data, X, stream));
+  }
+  void forward_sos(cf *X, const cf *data, const float *kx, const float *ky, const float *kz, const float *kw,
+                   int64_t M, void *stream = nullptr) {
+    traj(kx, ky, kz, kw, M, stream);
+    sync_k_rad(stream);
+    check(mrg_adjoint_sos(plan_, 0, data, M, X, stream));
   }
   void backward(const cf *X, const cf *smap, cf *data, const float *kx, const float *ky, const float *kz,
                 const float *kw, int64_t M, void *stream = nullptr) {
@@ -101,6 +111,12 @@ class gridFFT {
     betaX = be[0]; betaY = be[1]; betaZ = be[2];
     dwinX = dw[0]; dwinY = dw[1]; dwinZ = dw[2];
     keyM_ = -1;
+    k_rad_set_ = k_rad;
+  }
+  void sync_k_rad(void *stream) {
+    if (k_rad == k_rad_set_) return;
+    check(mrg_set_k_rad(plan_, k_rad, stream));
+    k_rad_set_ = k_rad;
   }
   void traj(const float *kx, const float *ky, const float *kz, const float *kw, int64_t M, void *stream) {
     if (!plan_) throw std::runtime_error("mrg: precalc_gridding not called");
@@ -112,6 +128,7 @@ class gridFFT {
   mrg_plan *plan_ = nullptr;
   const void *key_[4] = {nullptr, nullptr, nullptr, nullptr};
   int64_t keyM_ = -1;
+  float k_rad_set_ = 9999.0f;
 };
 
 // All coils in one call (the reference's -parallel_coils path).  smaps and data are
@@ -127,6 +144,7 @@ class gridFFT_CoilThreaded : public gridFFT {
                const float *kw, int64_t M, void *stream = nullptr) {
     traj(kx, ky, kz, kw, M, stream);
     maps(smaps, stream);
+    sync_k_rad(stream);
     check(mrg_adjoint(plan_, 0, data, M, X, stream));
   }
   void backward(const cf *X, const cf *smaps, cf *data, const float *kx, const float *ky, const float *kz,

@@ -59,6 +59,9 @@ typedef struct mrg_config {
   int kernel_eval;   /* 0: interpolate the 600-per-unit table as the reference (src/gridFFT.cpp:1113-1116);
                         1: evaluate the Kaiser-Bessel kernel analytically (same beta and scale), the
                         form whose derivative mrg_grad uses, for finite-difference-consistent gradients */
+  int grid_mode;     /* gridding (E^H scatter) kernel: 0 the faster of the two (timed per frame),
+                        1 FP32 multiply-adds on the CUDA cores, 2 tensor cores in TF32 with the
+                        three-term hi/lo split (W V ~ Wh Vh + Wh Vl + Wl Vh, products to ~2^-21) */
 } mrg_config;
 
 /* Fills the reference defaults (src/gridFFT.cpp:28-60). */
@@ -102,8 +105,9 @@ mrg_status mrg_frame_info(const mrg_plan *plan, int frame, int64_t *M, int64_t *
                           int64_t *nitems);
 
 /* Launch shapes the autotuner chose for a frame (mrg_config.tile == 0): out = {ungrid lanes
- * per sample, ungrid samples per CTA, gridding coils per pass (0: all), 0}; ms = the timed
- * ungrid and grid kernels. */
+ * per sample, ungrid samples per CTA, gridding coils per pass (0: all; -n: the tensor-core
+ * kernel with 4n coils per pass), ungrid coils per lane}; ms = the timed ungrid and grid
+ * kernels. */
 mrg_status mrg_frame_tuning(const mrg_plan *plan, int frame, int out[4], float ms[2]);
 
 /* Measured k-space of one frame: ncoil arrays of M complex64, coil c at
@@ -131,6 +135,32 @@ mrg_status mrg_normal(mrg_plan *plan, int frame, const void *X, void *out, void 
 mrg_status mrg_adjoint_coil(mrg_plan *plan, int frame, const void *smap, const void *data, void *X, void *stream);
 mrg_status mrg_forward_coil(mrg_plan *plan, int frame, const void *X, const void *smap, void *data, const void *diff,
                             void *stream);
+
+/* The public gridFFT::k_rad field (src/gridFFT.h:102; default 9999): the radius of the
+ * Gaussian taper exp(-|k|^2 / (2 k_rad^2)) E^H applies to each sample
+ * (src/gridFFT.cpp:1096-1108).  The coil-map estimate sets it to the map resolution and
+ * back (src/recon_lib.cpp:2738, :2786).  Applies to every frame's trajectory. */
+mrg_status mrg_set_k_rad(mrg_plan *plan, float k_rad, void *stream);
+
+/* Map-free adjoints over all coils of the plan (data coil c at data + c*coil_stride):
+ *   mrg_adjoint_coils: images[c*image_stride + v] += E^H_c (kw * data_c), one image per
+ *     coil -- gridFFT::forward without a map (src/gridFFT.cpp:759-789, accumulate(X)
+ *     :943-958), as the coil-map estimate calls it per coil (src/recon_lib.cpp:2771-2782).
+ *   mrg_adjoint_sos: X[v] += sum_c |deapp(E^H_c (kw * data_c))|^2 -- gridFFT::forward_sos
+ *     (src/gridFFT.cpp:722-757, accumulate_sos :960-970) summed over coils. */
+mrg_status mrg_adjoint_coils(mrg_plan *plan, int frame, const void *data, int64_t coil_stride, void *images,
+                             int64_t image_stride, void *stream);
+mrg_status mrg_adjoint_sos(mrg_plan *plan, int frame, const void *data, int64_t coil_stride, void *X, void *stream);
+
+/* The default (LOWRES, SOS-normalised) coil-map estimate of RECON::calc_sensitivity_maps
+ * (src/recon_lib.cpp:2694-2950 with coil_combine_type LOWRES, smap_norm SOS, smap_thresh 0,
+ * one encode): per coil E^H without maps at k_rad = smap_res (flag -smap_res, default 8),
+ * a Gaussian blur of sigma blur[3] (flags -extra_blur, default 0: none; may be NULL), then
+ * every coil divided by the root sum of squares over coils.  The maps become the plan's
+ * maps (as mrg_set_smaps); smaps_out (may be NULL) receives them, coil c at
+ * smaps_out + c*out_stride.  k_rad is restored afterwards. */
+mrg_status mrg_lowres_smaps(mrg_plan *plan, int frame, const void *data, int64_t coil_stride, float smap_res,
+                            const float blur[3], void *smaps_out, int64_t out_stride, void *stream);
 
 /* SENSE conjugate gradient (src/recon_lib.cpp:1523-1759): X (nframes images) is
  * overwritten with the result of max_iter iterations from x0 = 0, FP32 vectors and
@@ -219,6 +249,15 @@ mrg_status mrg_llr_update_threshold_noalloc(const void *X, int nframes, int Nx, 
  * drawn from the rand() stream after rand_skip draws. */
 mrg_status mrg_llr_thresh(void *X, int nframes, int Nx, int Ny, int Nz, const int block[3], int block_iter,
                           float alpha, float smax, int64_t rand_skip, void *stream);
+
+/* gaussian_blur (src/ArrayTemplates.cpp:489-601) of nvol complex64 volumes in place
+ * (volume c at X + c*vol_stride), sigma per axis (x, y, z; <= 0 skips the axis).  Taps
+ * ii in [max(i - w, 0), min(i + w, n)) with w = (int)(5 sigma), as the reference's loop. */
+mrg_status mrg_gaussian_blur(void *X, int nvol, int Nx, int Ny, int Nz, int64_t vol_stride, const float sigma[3],
+                             void *stream);
+/* RECON::sos_normalize with smap_thresh == 0 (src/recon_lib.cpp:3043-3062): each coil
+ * divided by sqrt(sum_c |map_c|^2), coil c at maps + c*coil_stride, nvox voxels. */
+mrg_status mrg_sos_normalize(void *maps, int ncoil, int64_t coil_stride, int64_t nvox, void *stream);
 
 /* Host-only (no GPU needed): the geometry and tables mrg_plan_create would build,
  * i.e. gridFFT::precalc_gridding's S, og_s, grid ratio, Kaiser beta and the LUT / window

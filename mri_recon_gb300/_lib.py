@@ -27,7 +27,7 @@ _dp = ctypes.POINTER(ctypes.c_double)
 class MrgConfig(ctypes.Structure):
     _fields_ = [("overgrid", ctypes.c_float), ("dwin", ctypes.c_float), ("kernel_type", ctypes.c_int),
                 ("k_rad", ctypes.c_float), ("time_grid", ctypes.c_int), ("tile", ctypes.c_int),
-                ("max_pairs", ctypes.c_int), ("kernel_eval", ctypes.c_int)]
+                ("max_pairs", ctypes.c_int), ("kernel_eval", ctypes.c_int), ("grid_mode", ctypes.c_int)]
 
 
 class MrgFistaParams(ctypes.Structure):
@@ -56,6 +56,12 @@ SIGNATURES = {
     "mrg_normal": (_i, [_vp, _i, _vp, _vp, _vp]),
     "mrg_adjoint_coil": (_i, [_vp, _i, _vp, _vp, _vp, _vp]),
     "mrg_forward_coil": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _vp]),
+    "mrg_set_k_rad": (_i, [_vp, _f, _vp]),
+    "mrg_adjoint_coils": (_i, [_vp, _i, _vp, _i64, _vp, _i64, _vp]),
+    "mrg_adjoint_sos": (_i, [_vp, _i, _vp, _i64, _vp, _vp]),
+    "mrg_lowres_smaps": (_i, [_vp, _i, _vp, _i64, _f, _fp, _vp, _i64, _vp]),
+    "mrg_gaussian_blur": (_i, [_vp, _i, _i, _i, _i, _i64, _fp, _vp]),
+    "mrg_sos_normalize": (_i, [_vp, _i, _i64, _i64, _vp]),
     "mrg_cg": (_i, [_vp, _i, _vp, _dp, _i, _vp]),
     "mrg_fista_params_default": (None, [ctypes.POINTER(MrgFistaParams)]),
     "mrg_fista": (_i, [_vp, ctypes.POINTER(MrgFistaParams), _vp, _dp, _fp, _i, _vp]),

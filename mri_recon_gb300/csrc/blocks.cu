@@ -165,4 +165,41 @@ mrg_status mrg_llr_thresh(void *X, int nframes, int Nx, int Ny, int Nz, const in
   return MRG_OK;
 }
 
+mrg_status mrg_gaussian_blur(void *X, int nvol, int Nx, int Ny, int Nz, int64_t vol_stride, const float sigma[3],
+                             void *stream) {
+  if (!X || !sigma || nvol <= 0 || Nx <= 0 || Ny <= 0 || Nz <= 0) {
+    set_error("bad argument");
+    return MRG_ERR_INVALID;
+  }
+  const int64_t nimg = (int64_t)Nx * Ny * Nz;
+  if (nvol > 1 && vol_stride < nimg) {
+    set_error("vol_stride smaller than one volume");
+    return MRG_ERR_INVALID;
+  }
+  const int64_t vs = nvol > 1 ? vol_stride : nimg;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int N[3] = {Nx, Ny, Nz};
+  const size_t bytes = sizeof(float2) * (size_t)(vs * (nvol - 1) + nimg);
+  DevBuf tmp;
+  float2 *d;
+  MRG_TRY(view(X, bytes, tmp, st, &d));
+  MRG_TRY(gaussian_blur_ex(d, nvol, N, 1, vs, sigma, st));
+  return back(X, tmp, bytes, st);
+}
+
+mrg_status mrg_sos_normalize(void *maps, int ncoil, int64_t coil_stride, int64_t nvox, void *stream) {
+  if (!maps || ncoil <= 0 || nvox <= 0 || (ncoil > 1 && coil_stride < nvox)) {
+    set_error("bad argument");
+    return MRG_ERR_INVALID;
+  }
+  const int64_t vs = ncoil > 1 ? coil_stride : nvox;
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t bytes = sizeof(float2) * (size_t)(vs * (ncoil - 1) + nvox);
+  DevBuf tmp;
+  float2 *d;
+  MRG_TRY(view(maps, bytes, tmp, st, &d));
+  MRG_TRY(sos_normalize_ex(d, ncoil, nvox, 1, vs, st));
+  return back(maps, tmp, bytes, st);
+}
+
 }  // extern "C"

@@ -52,13 +52,16 @@ struct mrg_plan {
   size_t stage_cap[4] = {0, 0, 0, 0};
   float timings[8] = {0};
   int timing_on = 0, timing_calls = 0;
+  int fft_ib[6] = {0, 0, 0, 0, 0, 0};  // lines per CTA per FFT pass (0: default)
+  bool fft_tuned = false;
   cudaEvent_t tev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   int64_t graph_kernels = 0;  // kernels per replay of cg_exec
   // cached CG graph
   cudaGraphExec_t cg_exec = nullptr;
   void *cg_key[2] = {nullptr, nullptr};
   // autotuned launch shapes, reused while the sample count stays within 2x
-  int tuned_G = 0, tuned_spb = 0, tuned_cc = -1;
+  bool tuned = false;
+  int tuned_G = 0, tuned_spb = 0, tuned_cpl = 0, tuned_cc = 0;
   int64_t tuned_nvalid = 0;
   float tuned_ms[2] = {0.f, 0.f};
   // FISTA state
@@ -89,6 +92,7 @@ static GridConst grid_const(const mrg_plan *p) {
   g.B = p->B;
   g.C = p->C;
   g.eval = p->cfg.kernel_eval;
+  g.grid_mode = p->cfg.grid_mode;
   for (int d = 0; d < 3; d++) {
     g.beta[d] = p->geo.beta[d];
     g.kb_norm[d] = p->geo.kb_norm[d];
@@ -161,6 +165,17 @@ static int pass_ib(int64_t inner, int C) {
   return C * (32 / C);
 }
 
+// Lines per CTA of FFT pass k (0-2: E z/y/x, 3-5: E^H x/y/z): the autotuned value
+// when it is valid for this pass, else the default (a multiple of C, up to 32).
+static int plan_ib(const mrg_plan *p, int k, int64_t inner, int C, bool accum) {
+  const int def = pass_ib(inner, C);
+  const int v = p->fft_ib[k];
+  if (v <= 0 || v == def) return def;
+  if (accum && (v % C) != 0) return def;  // the coil sum must stay inside a CTA
+  if (v % 2) return def;
+  return v;
+}
+
 // Stage timing (mrg_set_timing): events between the four stages of E or E^H.
 static void tmark(mrg_plan *p, int k, cudaStream_t st) {
   if (p->timing_on) cudaEventRecord(p->tev[k], st);
@@ -209,7 +224,7 @@ static mrg_status run_E_grid(mrg_plan *p, const float2 *X, const float2 *smap, c
   // z pass with set_image (src/gridFFT.cpp:972-986 + fft3 along z)
   a.S = (int)Sz; a.sign = -1; a.mode = FFT_SETIMG;
   a.Lin = (int)Nz; a.in_off = g.og[2]; a.Lout = (int)Sz; a.out_off = 0;
-  a.inner = (int)(Nx * C); a.IB = pass_ib(a.inner, C); a.lfast = 0;
+  a.inner = (int)(Nx * C); a.IB = plan_ib(p, 0, a.inner, C, false); a.lfast = 0;
   a.nlines = Ny * Nx * C;
   a.in_ls = Nx * Ny * C; a.in_os = Nx * C; a.out_ls = Ny * Nx * C; a.out_os = Nx * C;
   a.scale = (float)(1. / std::sqrt((float)Sz));
@@ -224,7 +239,7 @@ static mrg_status run_E_grid(mrg_plan *p, const float2 *X, const float2 *smap, c
   memset(&b, 0, sizeof(b));
   b.S = (int)Sy; b.sign = -1; b.mode = FFT_PLAIN;
   b.Lin = (int)Ny; b.in_off = g.og[1]; b.Lout = (int)Sy; b.out_off = 0;
-  b.inner = (int)(Nx * C); b.IB = pass_ib(b.inner, C);
+  b.inner = (int)(Nx * C); b.IB = plan_ib(p, 1, b.inner, C, false);
   b.nlines = Sz * Nx * C;
   b.in_ls = Nx * C; b.in_os = Ny * Nx * C; b.out_ls = Nx * C; b.out_os = Sy * Nx * C;
   b.scale = (float)(1. / std::sqrt((float)Sy));
@@ -237,7 +252,7 @@ static mrg_status run_E_grid(mrg_plan *p, const float2 *X, const float2 *smap, c
   memset(&c, 0, sizeof(c));
   c.S = (int)Sx; c.sign = -1; c.mode = FFT_PLAIN;
   c.Lin = (int)Nx; c.in_off = g.og[0]; c.Lout = (int)Sx; c.out_off = 0;
-  c.inner = C; c.IB = pass_ib(C, C); c.lfast = (C == 1);
+  c.inner = C; c.IB = (C == 1) ? pass_ib(C, C) : plan_ib(p, 2, C, C, false); c.lfast = (C == 1);
   c.nlines = Sz * Sy * C;
   c.in_ls = C; c.in_os = Nx * C; c.out_ls = C; c.out_os = Sx * C;
   c.scale = (float)(1. / std::sqrt((float)Sx));
@@ -248,12 +263,12 @@ static mrg_status run_E_grid(mrg_plan *p, const float2 *X, const float2 *smap, c
 }
 
 // E^H for one frame: weighted sorted samples yw (data * kw * taper) -> X += ...
-static mrg_status run_EH(mrg_plan *p, const FrameTraj &ft, const float2 *y, const float2 *smap, float2 *X,
-                         cudaStream_t st) {
+// E^H up to the y transform: grid, x and y inverse FFT passes; the result is in d_t1
+// ([Sz][Ny][Nx][C], y and x already cropped).
+static mrg_status run_EH_xy(mrg_plan *p, const FrameTraj &ft, const float2 *y, cudaStream_t st) {
   const Geometry &g = p->geo;
   const int C = p->C;
-  const int64_t Nx = g.N[0], Ny = g.N[1], Nz = g.N[2], Sx = g.S[0], Sy = g.S[1], Sz = g.S[2];
-  const float *wx = p->d_win, *wy = p->d_win + Sx, *wz = p->d_win + Sx + Sy;
+  const int64_t Nx = g.N[0], Ny = g.N[1], Sx = g.S[0], Sy = g.S[1], Sz = g.S[2];
   const GridConst gc = grid_const(p);
   tmark(p, 0, st);
   MRG_TRY(launch_grid(gc, ft, y, p->d_grid, st));  // src/gridFFT.cpp:1009-1164
@@ -262,7 +277,7 @@ static mrg_status run_EH(mrg_plan *p, const FrameTraj &ft, const float2 *y, cons
   memset(&a, 0, sizeof(a));
   a.S = (int)Sx; a.sign = +1; a.mode = FFT_PLAIN;
   a.Lin = (int)Sx; a.in_off = 0; a.Lout = (int)Nx; a.out_off = g.og[0];
-  a.inner = C; a.IB = pass_ib(C, C); a.lfast = (C == 1);
+  a.inner = C; a.IB = (C == 1) ? pass_ib(C, C) : plan_ib(p, 3, C, C, false); a.lfast = (C == 1);
   a.nlines = Sz * Sy * C;
   a.in_ls = C; a.in_os = Sx * C; a.out_ls = C; a.out_os = Nx * C;
   a.scale = (float)(1. / std::sqrt((float)Sx));
@@ -274,7 +289,7 @@ static mrg_status run_EH(mrg_plan *p, const FrameTraj &ft, const float2 *y, cons
   memset(&b, 0, sizeof(b));
   b.S = (int)Sy; b.sign = +1; b.mode = FFT_PLAIN;
   b.Lin = (int)Sy; b.in_off = 0; b.Lout = (int)Ny; b.out_off = g.og[1];
-  b.inner = (int)(Nx * C); b.IB = pass_ib(b.inner, C);
+  b.inner = (int)(Nx * C); b.IB = plan_ib(p, 4, b.inner, C, false);
   b.nlines = Sz * Nx * C;
   b.in_ls = Nx * C; b.in_os = Sy * Nx * C; b.out_ls = Nx * C; b.out_os = Ny * Nx * C;
   b.scale = (float)(1. / std::sqrt((float)Sy));
@@ -282,18 +297,51 @@ static mrg_status run_EH(mrg_plan *p, const FrameTraj &ft, const float2 *y, cons
   fft_vectorize(b);
   MRG_TRY(launch_fft(b, st));
   tmark(p, 3, st);
+  return MRG_OK;
+}
+
+static mrg_status run_EH(mrg_plan *p, const FrameTraj &ft, const float2 *y, const float2 *smap, float2 *X,
+                         cudaStream_t st) {
+  const Geometry &g = p->geo;
+  const int C = p->C;
+  const int64_t Nx = g.N[0], Ny = g.N[1], Nz = g.N[2], Sx = g.S[0], Sy = g.S[1], Sz = g.S[2];
+  const float *wx = p->d_win, *wy = p->d_win + Sx, *wz = p->d_win + Sx + Sy;
+  MRG_TRY(run_EH_xy(p, ft, y, st));
   // z pass with accumulate (src/gridFFT.cpp:926-941)
   FftPass c;
   memset(&c, 0, sizeof(c));
   c.S = (int)Sz; c.sign = +1; c.mode = FFT_ACCUM;
   c.Lin = (int)Sz; c.in_off = 0; c.Lout = (int)Nz; c.out_off = g.og[2];
-  c.inner = (int)(Nx * C); c.IB = pass_ib(c.inner, C);
+  c.inner = (int)(Nx * C); c.IB = plan_ib(p, 5, c.inner, C, true);
   c.nlines = Ny * Nx * C;
   c.in_ls = Ny * Nx * C; c.in_os = Nx * C; c.out_ls = Nx * Ny * C; c.out_os = Nx * C;
   c.scale = (float)(1. / std::sqrt((float)Sz));
   c.in = p->d_t1; c.smap = smap; c.has_smap = smap != nullptr; c.acc = X;
   c.acc_atomic = (c.IB % C) != 0; c.acc_l = Nx * Ny; c.acc_o = Nx;
   c.wl = wz + g.og[2]; c.wo = wy + g.og[1]; c.wi = wx + g.og[0]; c.C = C;
+  fft_vectorize(c);
+  MRG_TRY(launch_fft(c, st));
+  tmark(p, 4, st);
+  tcollect(p, 4);
+  return MRG_OK;
+}
+
+// E^H without the coil sum: grid, the three inverse passes, and the z pass writes the
+// cropped volume t[Nz][Ny][Nx][C] (scaled, not deapodised) into d_t2.
+static mrg_status run_EH_crop(mrg_plan *p, const FrameTraj &ft, const float2 *y, cudaStream_t st) {
+  const Geometry &g = p->geo;
+  const int C = p->C;
+  const int64_t Nx = g.N[0], Ny = g.N[1], Nz = g.N[2], Sz = g.S[2];
+  MRG_TRY(run_EH_xy(p, ft, y, st));
+  FftPass c;
+  memset(&c, 0, sizeof(c));
+  c.S = (int)Sz; c.sign = +1; c.mode = FFT_PLAIN;
+  c.Lin = (int)Sz; c.in_off = 0; c.Lout = (int)Nz; c.out_off = g.og[2];
+  c.inner = (int)(Nx * C); c.IB = plan_ib(p, 5, c.inner, C, false);
+  c.nlines = Ny * Nx * C;
+  c.in_ls = Ny * Nx * C; c.in_os = Nx * C; c.out_ls = Ny * Nx * C; c.out_os = Nx * C;
+  c.scale = (float)(1. / std::sqrt((float)Sz));
+  c.in = p->d_t1; c.out = p->d_t2; c.C = C;
   fft_vectorize(c);
   MRG_TRY(launch_fft(c, st));
   tmark(p, 4, st);
@@ -319,6 +367,46 @@ static mrg_status check_frame(const mrg_plan *p, int frame) {
 
 static const float2 *plan_smap(const mrg_plan *p) { return p->has_smaps ? p->d_smap : nullptr; }
 
+extern "C" {
+static mrg_status ensure_solver(mrg_plan *p, bool fista);
+}
+
+// Picks 16 or 32 lines per CTA for each FFT pass by timing one E and one E^H of
+// this frame with each choice, using the per-stage event timing.  16 lines halve
+// a CTA's shared memory so more CTAs overlap their load, transform and store phases.
+static mrg_status tune_fft(mrg_plan *p, const FrameTraj &ft, cudaStream_t st) {
+  if (p->C > 32 || ft.nvalid == 0) return MRG_OK;
+  MRG_TRY(ensure_solver(p, false));
+  const float2 *sm = plan_smap(p) ? plan_smap(p) : (p->C > 1 ? p->d_grid : nullptr);
+  const int was_on = p->timing_on;
+  const int idx[6] = {0, 1, 2, 5, 6, 7};  // FFT stages among the eight timed stages
+  float best[6];
+  int pick[6];
+  for (int k = 0; k < 6; k++) {
+    best[k] = 1e30f;
+    pick[k] = 0;
+  }
+  for (int cand : {0, 16}) {
+    for (int k = 0; k < 6; k++) p->fft_ib[k] = cand;
+    MRG_TRY(mrg_set_timing(p, 1));
+    for (int rep = 0; rep < 2; rep++) {
+      MRG_TRY(run_E(p, ft, p->d_R, sm, nullptr, p->d_y, true, st));
+      MRG_TRY(run_EH(p, ft, p->d_y, sm, p->d_L, st));
+    }
+    float t[8];
+    int calls = 0;
+    MRG_TRY(mrg_last_timings(p, t, &calls));
+    for (int k = 0; k < 6; k++)
+      if (t[idx[k]] < best[k]) {
+        best[k] = t[idx[k]];
+        pick[k] = cand;
+      }
+  }
+  for (int k = 0; k < 6; k++) p->fft_ib[k] = pick[k];
+  p->fft_tuned = true;
+  return mrg_set_timing(p, was_on);
+}
+
 // ---------------------------------------------------------------------------
 // C ABI
 // ---------------------------------------------------------------------------
@@ -334,6 +422,7 @@ void mrg_config_default(mrg_config *cfg) {
   cfg->tile = 0;
   cfg->max_pairs = 0;
   cfg->kernel_eval = 0;
+  cfg->grid_mode = 0;
 }
 
 const char *mrg_last_error(void) { return g_err.c_str(); }
@@ -353,7 +442,8 @@ mrg_status mrg_plan_create(const mrg_config *cfg_in, int Nx, int Ny, int Nz, int
   mrg_config cfg;
   if (cfg_in) cfg = *cfg_in; else mrg_config_default(&cfg);
   if (!(cfg.overgrid >= 1.0f) || cfg.kernel_type < 0 || cfg.kernel_type > 3 || cfg.kernel_eval < 0 ||
-      cfg.kernel_eval > 1 || (cfg.kernel_eval == 1 && cfg.kernel_type != MRG_KERNEL_KAISER)) {
+      cfg.kernel_eval > 1 || (cfg.kernel_eval == 1 && cfg.kernel_type != MRG_KERNEL_KAISER) || cfg.grid_mode < 0 ||
+      cfg.grid_mode > 2) {
     set_error("bad config");
     return MRG_ERR_INVALID;
   }
@@ -522,17 +612,21 @@ mrg_status mrg_set_traj(mrg_plan *p, int frame, const float *kx, const float *ky
   if (p->cfg.tile == 0) {
     FrameTraj &ft = p->frames[frame];
     const int64_t nv = ft.nvalid;
-    if (p->tuned_cc >= 0 && nv <= 2 * p->tuned_nvalid && 2 * nv >= p->tuned_nvalid) {
+    if (p->tuned && nv <= 2 * p->tuned_nvalid && 2 * nv >= p->tuned_nvalid) {
       ft.ungrid_G = p->tuned_G;
       ft.ungrid_spb = p->tuned_spb;
+      ft.ungrid_cpl = p->tuned_cpl;
       ft.grid_cc = p->tuned_cc;
       ft.tune_ungrid_ms = p->tuned_ms[0];
       ft.tune_grid_ms = p->tuned_ms[1];
     } else {
       MRG_TRY(autotune_frame(gc, ft, p->d_grid, p->d_y, st));
+      if (!p->fft_tuned) MRG_TRY(tune_fft(p, ft, st));
       p->tuned_G = ft.ungrid_G;
       p->tuned_spb = ft.ungrid_spb;
+      p->tuned_cpl = ft.ungrid_cpl;
       p->tuned_cc = ft.grid_cc;
+      p->tuned = true;
       p->tuned_nvalid = nv;
       p->tuned_ms[0] = ft.tune_ungrid_ms;
       p->tuned_ms[1] = ft.tune_grid_ms;
@@ -559,7 +653,7 @@ mrg_status mrg_frame_tuning(const mrg_plan *p, int frame, int out[4], float ms[2
     out[0] = ft.ungrid_G;
     out[1] = ft.ungrid_spb;
     out[2] = ft.grid_cc;
-    out[3] = 0;
+    out[3] = ft.ungrid_cpl;
   }
   if (ms) {
     ms[0] = ft.tune_ungrid_ms;
@@ -746,6 +840,127 @@ mrg_status mrg_forward_coil(mrg_plan *p, int frame, const void *X, const void *s
   if (sd) {
     MRG_CUDA(cudaMemcpyAsync(data, dd, dbytes, cudaMemcpyDeviceToHost, st));
     MRG_CUDA(cudaStreamSynchronize(st));
+  }
+  return MRG_OK;
+}
+
+mrg_status mrg_set_k_rad(mrg_plan *p, float k_rad, void *stream) {
+  if (!p || !(k_rad > 0.0f)) {
+    set_error("bad argument");
+    return MRG_ERR_INVALID;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  p->geo.k_rad = k_rad;
+  p->cfg.k_rad = k_rad;
+  const GridConst gc = grid_const(p);
+  for (auto &ft : p->frames) MRG_TRY(launch_retaper(gc, ft, st));
+  return MRG_OK;
+}
+
+// Shared front of the map-free adjoints: weighted gather of every coil's samples and
+// E^H up to the cropped, transformed volume in d_t2.
+static mrg_status adjoint_crop(mrg_plan *p, int frame, const void *data, int64_t coil_stride, cudaStream_t st) {
+  MRG_TRY(check_frame(p, frame));
+  if (!data) {
+    set_error("null argument");
+    return MRG_ERR_INVALID;
+  }
+  const FrameTraj &ft = p->frames[frame];
+  if (p->C > 1 && coil_stride < ft.M) {
+    set_error("coil_stride smaller than the sample count");
+    return MRG_ERR_INVALID;
+  }
+  void *dd;
+  bool sd;
+  MRG_TRY(dev_view(p, 0, data, sizeof(float2) * (size_t)(coil_stride * (p->C - 1) + ft.M), true, st, &dd, &sd));
+  MRG_TRY(launch_gather_samples(ft, p->C, (const float2 *)dd, coil_stride, p->d_y, st, true));
+  return run_EH_crop(p, ft, p->d_y, st);
+}
+
+mrg_status mrg_adjoint_coils(mrg_plan *p, int frame, const void *data, int64_t coil_stride, void *images,
+                             int64_t image_stride, void *stream) {
+  if (!p || !images) {
+    set_error("null argument");
+    return MRG_ERR_INVALID;
+  }
+  if (p->C > 1 && image_stride < p->nimg) {
+    set_error("image_stride smaller than one image");
+    return MRG_ERR_INVALID;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  const int64_t vs = p->C > 1 ? image_stride : p->nimg;
+  const size_t ibytes = sizeof(float2) * (size_t)(vs * (p->C - 1) + p->nimg);
+  MRG_TRY(adjoint_crop(p, frame, data, coil_stride, st));
+  void *dI;
+  bool sI;
+  MRG_TRY(dev_view(p, 1, images, ibytes, true, st, &dI, &sI));
+  const Geometry &g = p->geo;
+  const float *wx = p->d_win + g.og[0], *wy = p->d_win + g.S[0] + g.og[1], *wz = p->d_win + g.S[0] + g.S[1] + g.og[2];
+  MRG_TRY(launch_coil_images(p->d_t2, p->C, g.N, wx, wy, wz, (float2 *)dI, 1, vs, true, st));
+  if (sI) {
+    MRG_CUDA(cudaMemcpyAsync(images, dI, ibytes, cudaMemcpyDeviceToHost, st));
+    MRG_CUDA(cudaStreamSynchronize(st));
+  }
+  return MRG_OK;
+}
+
+mrg_status mrg_adjoint_sos(mrg_plan *p, int frame, const void *data, int64_t coil_stride, void *X, void *stream) {
+  if (!p || !X) {
+    set_error("null argument");
+    return MRG_ERR_INVALID;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  MRG_TRY(adjoint_crop(p, frame, data, coil_stride, st));
+  void *dX;
+  bool sX;
+  MRG_TRY(dev_view(p, 1, X, sizeof(float2) * p->nimg, true, st, &dX, &sX));
+  const Geometry &g = p->geo;
+  const float *wx = p->d_win + g.og[0], *wy = p->d_win + g.S[0] + g.og[1], *wz = p->d_win + g.S[0] + g.S[1] + g.og[2];
+  MRG_TRY(launch_sos_images(p->d_t2, p->C, g.N, wx, wy, wz, (float2 *)dX, st));
+  if (sX) {
+    MRG_CUDA(cudaMemcpyAsync(X, dX, sizeof(float2) * p->nimg, cudaMemcpyDeviceToHost, st));
+    MRG_CUDA(cudaStreamSynchronize(st));
+  }
+  return MRG_OK;
+}
+
+mrg_status mrg_lowres_smaps(mrg_plan *p, int frame, const void *data, int64_t coil_stride, float smap_res,
+                            const float blur[3], void *smaps_out, int64_t out_stride, void *stream) {
+  if (!p || !(smap_res > 0.0f)) {
+    set_error("bad argument");
+    return MRG_ERR_INVALID;
+  }
+  if (smaps_out && p->C > 1 && out_stride < p->nimg) {
+    set_error("out_stride smaller than one image");
+    return MRG_ERR_INVALID;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  if (!p->d_smap) MRG_CUDA(cudaMalloc(&p->d_smap, sizeof(float2) * p->nimg * p->C));
+  const float k_rad = p->geo.k_rad;
+  MRG_TRY(mrg_set_k_rad(p, smap_res, stream));  // gridding.k_rad = smap_res (src/recon_lib.cpp:2738)
+  const mrg_status rs = adjoint_crop(p, frame, data, coil_stride, st);
+  MRG_TRY(mrg_set_k_rad(p, k_rad, stream));  // restored afterwards (src/recon_lib.cpp:2786)
+  MRG_TRY(rs);
+  const Geometry &g = p->geo;
+  const float *wx = p->d_win + g.og[0], *wy = p->d_win + g.S[0] + g.og[1], *wz = p->d_win + g.S[0] + g.S[1] + g.og[2];
+  // coil images straight into the plan's interleaved maps [v][C]
+  MRG_TRY(launch_coil_images(p->d_t2, p->C, g.N, wx, wy, wz, p->d_smap, p->C, 1, false, st));
+  const float nob[3] = {0.f, 0.f, 0.f};
+  MRG_TRY(gaussian_blur_ex(p->d_smap, p->C, g.N, p->C, 1, blur ? blur : nob, st));
+  MRG_TRY(sos_normalize_ex(p->d_smap, p->C, p->nimg, p->C, 1, st));
+  if (!p->has_smaps) invalidate_graphs(p);
+  p->has_smaps = true;
+  if (smaps_out) {
+    const int64_t vs = p->C > 1 ? out_stride : p->nimg;
+    const size_t obytes = sizeof(float2) * (size_t)(vs * (p->C - 1) + p->nimg);
+    void *dO;
+    bool sO;
+    MRG_TRY(dev_view(p, 1, smaps_out, obytes, false, st, &dO, &sO));
+    MRG_TRY(launch_deinterleave(p->d_smap, p->C, p->nimg, (float2 *)dO, vs, st));
+    if (sO) {
+      MRG_CUDA(cudaMemcpyAsync(smaps_out, dO, obytes, cudaMemcpyDeviceToHost, st));
+      MRG_CUDA(cudaStreamSynchronize(st));
+    }
   }
   return MRG_OK;
 }

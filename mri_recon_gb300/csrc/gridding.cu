@@ -46,7 +46,7 @@ __device__ __forceinline__ void tap_range(const GridConst &g, int d, float dk, i
 // ---------------------------------------------------------------------------
 __global__ void k_traj_prep(GridConst g, const float *__restrict__ kx, const float *__restrict__ ky,
                             const float *__restrict__ kz, const float *__restrict__ kw, int64_t M, float4 *pos,
-                            float *tap, int *key, int *cnt, int ntiles) {
+                            float *kr_out, int *key, int *cnt, int ntiles) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < M; i += (int64_t)gridDim.x * blockDim.x) {
     const float k[3] = {kx[i], ky[i], kz[i]};
     const float w = kw[i];
@@ -62,15 +62,15 @@ __global__ void k_traj_prep(GridConst g, const float *__restrict__ kx, const flo
       c = min(max(c, 0), g.S[d] - 1);
       cell[d] = c / g.B;
     }
-    // kr = kx*kx + ky*ky + kz*kz accumulated in float, taper in double (src/gridFFT.cpp:1096-1108)
+    // kr = kx*kx + ky*ky + kz*kz accumulated in float (src/gridFFT.cpp:1096-1106); the taper
+    // exp(-kr / (2 k_rad^2)) is taken in double when the samples are sorted
     float kr = 0.0f;
     kr = __fadd_rn(kr, __fmul_rn(k[0], k[0]));
     kr = __fadd_rn(kr, __fmul_rn(k[1], k[1]));
     kr = __fadd_rn(kr, __fmul_rn(k[2], k[2]));
-    const float tp = (float)exp(-(double)kr / (2.0 * (double)g.k_rad * (double)g.k_rad));
     const int kk = ok ? (cell[2] * g.nt[1] + cell[1]) * g.nt[0] + cell[0] : ntiles;
     pos[i] = make_float4(dk[0], dk[1], dk[2], w);
-    tap[i] = tp;
+    kr_out[i] = kr;
     key[i] = kk;
     atomicAdd(&cnt[kk], 1);
   }
@@ -105,16 +105,35 @@ __global__ void k_scan(const int *__restrict__ in, int *out, int n) {
   if (n == 0 && t == 0) out[0] = 0;
 }
 
-__global__ void k_traj_sort(int64_t M, const int *__restrict__ key, const int *__restrict__ off, int *cur,
-                            const float4 *__restrict__ pos, const float *__restrict__ tap, float4 *spos, float *stap,
-                            int *perm) {
+__device__ __forceinline__ float taper(float kr, float k_rad) {
+  return (float)exp(-(double)kr / (2.0 * (double)k_rad * (double)k_rad));
+}
+
+__global__ void k_traj_sort(int64_t M, float k_rad, const int *__restrict__ key, const int *__restrict__ off, int *cur,
+                            const float4 *__restrict__ pos, const float *__restrict__ kr, float4 *spos, float *stap,
+                            float *skr, int *perm) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < M; i += (int64_t)gridDim.x * blockDim.x) {
     const int k = key[i];
     const int s = off[k] + atomicAdd(&cur[k], 1);
     spos[s] = pos[i];
-    stap[s] = tap[i];
+    skr[s] = kr[i];
+    stap[s] = taper(kr[i], k_rad);
     perm[s] = (int)i;
   }
+}
+
+__global__ void k_retaper(int64_t M, float k_rad, const float *__restrict__ skr, float *stap) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < M; i += (int64_t)gridDim.x * blockDim.x)
+    stap[i] = taper(skr[i], k_rad);
+}
+
+// Taper of every sample for a new k_rad (the public gridFFT::k_rad field the
+// coil-map estimate lowers to the map resolution, recon_lib.cpp:2738, :2786).
+mrg_status launch_retaper(const GridConst &gc, FrameTraj &ft, cudaStream_t st) {
+  if (ft.M == 0) return MRG_OK;
+  k_retaper<<<grid_blocks(ft.M, 256), 256, 0, st>>>(ft.M, gc.k_rad, ft.skr, ft.stap);
+  MRG_LAUNCHED();
+  return MRG_OK;
 }
 
 // Analytic Kaiser-Bessel kernel with the table's beta and scale:
@@ -208,12 +227,6 @@ __global__ void k_item_fill(int nblocks, const int *__restrict__ pcnt, const int
   }
 }
 
-static int grid_blocks(int64_t n, int threads) {
-  int64_t b = (n + threads - 1) / threads;
-  if (b < 1) b = 1;
-  if (b > 152 * 64) b = 152 * 64;
-  return (int)b;
-}
 
 template <typename T>
 static mrg_status dalloc(T **p, int64_t n) {
@@ -226,6 +239,7 @@ static mrg_status dalloc(T **p, int64_t n) {
 void traj_free(FrameTraj &ft) {
   cudaFree(ft.spos);
   cudaFree(ft.stap);
+  cudaFree(ft.skr);
   cudaFree(ft.perm);
   cudaFree(ft.swt);
   cudaFree(ft.sst);
@@ -288,6 +302,7 @@ mrg_status traj_setup(const GridConst &gc, FrameTraj &ft, const float *kx, const
   SETUP_TRY(dalloc(&cur, ntiles + 1));
   SETUP_TRY(dalloc(&ft.spos, M));
   SETUP_TRY(dalloc(&ft.stap, M));
+  SETUP_TRY(dalloc(&ft.skr, M));
   SETUP_TRY(dalloc(&ft.perm, M));
   SETUP_TRY(launch_zero(cnt, sizeof(int) * (ntiles + 1), st));
   SETUP_TRY(launch_zero(cur, sizeof(int) * (ntiles + 1), st));
@@ -295,7 +310,8 @@ mrg_status traj_setup(const GridConst &gc, FrameTraj &ft, const float *kx, const
   SETUP_LAUNCHED();
   k_scan<<<1, 1024, 0, st>>>(cnt, off, ntiles + 1);
   SETUP_LAUNCHED();
-  k_traj_sort<<<grid_blocks(M, 256), 256, 0, st>>>(M, key, off, cur, pos, tap, ft.spos, ft.stap, ft.perm);
+  k_traj_sort<<<grid_blocks(M, 256), 256, 0, st>>>(M, gc.k_rad, key, off, cur, pos, tap, ft.spos, ft.stap, ft.skr,
+                                                    ft.perm);
   SETUP_LAUNCHED();
   int nvalid = 0;
   SETUP_TRY(read_int(off + ntiles, &nvalid, st, "trajectory sort failed"));
@@ -353,11 +369,13 @@ mrg_status traj_setup(const GridConst &gc, FrameTraj &ft, const float *kx, const
 // ---------------------------------------------------------------------------
 // ungridding: y[s][c] = sum_taps w * grid[tap][c]  (- diff[s][c]) [* kw * taper]
 // ---------------------------------------------------------------------------
-// G lanes per sample, one lane per coil of the chunk [blockIdx.y*G, +G).  A CTA
-// walks SPB consecutive (tile-sorted) samples for one coil chunk, so the grid
+// G lanes per sample, CPL coils per lane: the coil chunk [blockIdx.y*G*CPL, +G*CPL).
+// A CTA walks SPB consecutive (tile-sorted) samples for one coil chunk, so the grid
 // neighbourhood it reads is small enough for L1 to catch the reuse between
-// neighbouring samples.
-template <int G>
+// neighbouring samples.  The sum is taken separably, x taps first:
+//   y = sum_z wz sum_y wy sum_x wx g,
+// which needs one multiply-add per tap and coil instead of forming every 3D weight.
+template <int G, int CPL>
 __global__ void __launch_bounds__(256) k_ungrid(const GridConst g, int nvalid, int spb, const float4 *__restrict__ swt,
                                                const int4 *__restrict__ sst, const float4 *__restrict__ spos,
                                                const float *__restrict__ stap, const float2 *__restrict__ grid,
@@ -365,8 +383,8 @@ __global__ void __launch_bounds__(256) k_ungrid(const GridConst g, int nvalid, i
   constexpr int GPB = 256 / G;  // sample groups per CTA
   const int lane = threadIdx.x % G, grp = threadIdx.x / G;
   const int C = g.C;
-  const int c = blockIdx.y * G + lane;
-  const int64_t S0 = g.S[0], S1 = g.S[1];
+  const int c = (blockIdx.y * G + lane) * CPL;  // first coil of this lane
+  const int64_t ys = (int64_t)g.S[0] * C, zs = (int64_t)g.S[1] * ys;
   const int64_t s_begin = (int64_t)blockIdx.x * spb;
   const int64_t s_end = min((int64_t)nvalid, s_begin + spb);
   for (int64_t gid = s_begin + grp; gid < s_end; gid += GPB) {
@@ -374,43 +392,64 @@ __global__ void __launch_bounds__(256) k_ungrid(const GridConst g, int nvalid, i
     const int nx = t.w & 15, ny = (t.w >> 4) & 15, nz = (t.w >> 8) & 15;
     const float *w = reinterpret_cast<const float *>(swt + 6 * gid);
     const float4 wa = __ldg(swt + 6 * gid), wb = __ldg(swt + 6 * gid + 1);
-    const float4 wc = __ldg(swt + 6 * gid + 2), wd = __ldg(swt + 6 * gid + 3);
     const float wx[6] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y};
-    const float wy[6] = {wc.x, wc.y, wc.z, wc.w, wd.x, wd.y};
     if (c >= C) continue;
-    float2 acc = make_float2(0.f, 0.f);
+    float acc[2 * CPL];
+#pragma unroll
+    for (int k = 0; k < 2 * CPL; k++) acc[k] = 0.f;
+    const float2 *base = grid + ((int64_t)t.z * g.S[1] + t.y) * ys + (int64_t)t.x * C + c;
     for (int kz = 0; kz < nz; kz++) {
-      const float wz = __ldg(w + 16 + kz);
-      const float2 *slab = grid + (((int64_t)(t.z + kz) * S1 + t.y) * S0 + t.x) * C + c;
-      // all taps of one z slice unrolled: up to 36 independent gathers in flight
+      float az[2 * CPL];
 #pragma unroll
-      for (int ky = 0; ky < 6; ky++) {
-        if (ky < ny) {
-          const float wzy = wz * wy[ky];
-          const float2 *row = slab + (int64_t)ky * S0 * C;
+      for (int k = 0; k < 2 * CPL; k++) az[k] = 0.f;
+      for (int ky = 0; ky < ny; ky++) {
+        const float2 *row = base + kz * zs + ky * ys;
+        float ar[2 * CPL];
 #pragma unroll
-          for (int a = 0; a < 6; a++) {
-            if (a < nx) {
-              const float ww = wzy * wx[a];
+        for (int k = 0; k < 2 * CPL; k++) ar[k] = 0.f;
+#pragma unroll
+        for (int a = 0; a < 6; a++) {
+          if (a < nx) {
+            if (CPL == 2) {
+              const float4 v = __ldg(reinterpret_cast<const float4 *>(row + (int64_t)a * C));
+              ar[0] += wx[a] * v.x;
+              ar[1] += wx[a] * v.y;
+              ar[2] += wx[a] * v.z;
+              ar[3] += wx[a] * v.w;
+            } else {
               const float2 v = __ldg(row + (int64_t)a * C);
-              acc.x += ww * v.x;
-              acc.y += ww * v.y;
+              ar[0] += wx[a] * v.x;
+              ar[1] += wx[a] * v.y;
             }
           }
         }
+        const float wyv = __ldg(w + 8 + ky);
+#pragma unroll
+        for (int k = 0; k < 2 * CPL; k++) az[k] += wyv * ar[k];
       }
+      const float wzv = __ldg(w + 16 + kz);
+#pragma unroll
+      for (int k = 0; k < 2 * CPL; k++) acc[k] += wzv * az[k];
     }
-    const int64_t o = gid * C + c;
-    if (diff) {
-      const float2 d = diff[o];
-      acc.x -= d.x;
-      acc.y -= d.y;
+    float kw = 0.f, tp = 0.f;
+    if (weigh) {
+      kw = __ldg(&spos[gid].w);
+      tp = __ldg(stap + gid);
     }
-    if (weigh) {  // temp = data * kw; temp *= taper  (src/gridFFT.cpp:1039-1108)
-      const float kw = __ldg(&spos[gid].w), tp = __ldg(stap + gid);
-      acc = make_float2(__fmul_rn(__fmul_rn(acc.x, kw), tp), __fmul_rn(__fmul_rn(acc.y, kw), tp));
+#pragma unroll
+    for (int q = 0; q < CPL; q++) {
+      if (c + q >= C) break;
+      const int64_t o = gid * C + c + q;
+      float2 r = make_float2(acc[2 * q], acc[2 * q + 1]);
+      if (diff) {
+        const float2 d = diff[o];
+        r.x -= d.x;
+        r.y -= d.y;
+      }
+      if (weigh)  // temp = data * kw; temp *= taper  (src/gridFFT.cpp:1039-1108)
+        r = make_float2(__fmul_rn(__fmul_rn(r.x, kw), tp), __fmul_rn(__fmul_rn(r.y, kw), tp));
+      y[o] = r;
     }
-    y[o] = acc;
   }
 }
 
@@ -424,18 +463,31 @@ mrg_status launch_ungrid(const GridConst &gc, const FrameTraj &ft, const float2 
                          bool weigh, cudaStream_t st) {
   if (ft.nvalid == 0) return MRG_OK;
   int G = ft.ungrid_G > 0 ? ft.ungrid_G : ungrid_group_default(gc.C);
+  // two coils per lane (16-byte loads) when the coil count is even and the buffers allow it
+  int cpl = (ft.ungrid_cpl > 0) ? ft.ungrid_cpl : ((gc.C % 2 == 0) ? 2 : 1);
+  if (gc.C % 2 != 0 || ((uintptr_t)grid & 15) != 0) cpl = 1;
   const int spb = ft.ungrid_spb > 0 ? ft.ungrid_spb : 256;
-  const dim3 blocks((unsigned)((ft.nvalid + spb - 1) / spb), (unsigned)((gc.C + G - 1) / G));
+  const int chunk = G * cpl;
+  const dim3 blocks((unsigned)((ft.nvalid + spb - 1) / spb), (unsigned)((gc.C + chunk - 1) / chunk));
   const int wf = weigh ? 1 : 0;
 #define UNGRID_ARGS gc, ft.nvalid, spb, ft.swt, ft.sst, ft.spos, ft.stap, grid, diff, y, wf
+#define UNGRID_CASE(GG)                                                           \
+  case GG:                                                                        \
+    if (cpl == 2) k_ungrid<GG, 2><<<blocks, 256, 0, st>>>(UNGRID_ARGS);           \
+    else k_ungrid<GG, 1><<<blocks, 256, 0, st>>>(UNGRID_ARGS);                    \
+    break;
   switch (G) {
-    case 1: k_ungrid<1><<<blocks, 256, 0, st>>>(UNGRID_ARGS); break;
-    case 2: k_ungrid<2><<<blocks, 256, 0, st>>>(UNGRID_ARGS); break;
-    case 4: k_ungrid<4><<<blocks, 256, 0, st>>>(UNGRID_ARGS); break;
-    case 8: k_ungrid<8><<<blocks, 256, 0, st>>>(UNGRID_ARGS); break;
-    case 16: k_ungrid<16><<<blocks, 256, 0, st>>>(UNGRID_ARGS); break;
-    default: k_ungrid<32><<<blocks, 256, 0, st>>>(UNGRID_ARGS); break;
+    UNGRID_CASE(1)
+    UNGRID_CASE(2)
+    UNGRID_CASE(4)
+    UNGRID_CASE(8)
+    UNGRID_CASE(16)
+    default:
+      if (cpl == 2) k_ungrid<32, 2><<<blocks, 256, 0, st>>>(UNGRID_ARGS);
+      else k_ungrid<32, 1><<<blocks, 256, 0, st>>>(UNGRID_ARGS);
+      break;
   }
+#undef UNGRID_CASE
 #undef UNGRID_ARGS
   MRG_LAUNCHED();
   return MRG_OK;
@@ -470,8 +522,10 @@ __device__ __forceinline__ void cp8(void *dst, const void *src) {
 // Shared memory per warp: 32 staged pairs x (CC coil values, 24 weights, first taps).
 template <int CC>
 struct GridStage {
-  static constexpr int V = 32 * CC;    // float2
-  static constexpr int W = 32 * 24;    // float
+  static constexpr int VS = CC;        // float2 per staged pair
+  static constexpr int WS = 24;        // floats per staged pair
+  static constexpr int V = 32 * VS;
+  static constexpr int W = 32 * WS;
   static constexpr int T = 32;         // int4
   static constexpr size_t bytes = V * 8 + W * 4 + T * 16;
 };
@@ -508,16 +562,16 @@ __global__ void __launch_bounds__(256) k_grid(const GridConst g, int nitems, con
       const int s = __ldg(pairs + q0 + lane);
       cp16(stt + lane, sst + s);
 #pragma unroll
-      for (int k = 0; k < 6; k++) cp16(sw + lane * 24 + 4 * k, swt + 6 * (int64_t)s + k);
+      for (int k = 0; k < 6; k++) cp16(sw + lane * GridStage<CC>::WS + 4 * k, swt + 6 * (int64_t)s + k);
       const float2 *v = yw + (int64_t)s * C + c0;
       if (VEC) {
 #pragma unroll
         for (int c = 0; c < CC / 2; c++)
-          if (2 * c < nc) cp16(sv + lane * CC + 2 * c, v + 2 * c);
+          if (2 * c < nc) cp16(sv + lane * GridStage<CC>::VS + 2 * c, v + 2 * c);
       } else {
 #pragma unroll
         for (int c = 0; c < CC; c++)
-          if (c < nc) cp8(sv + lane * CC + c, v + c);
+          if (c < nc) cp8(sv + lane * GridStage<CC>::VS + c, v + c);
       }
     }
     asm volatile("cp.async.commit_group;\n" ::);
@@ -526,12 +580,12 @@ __global__ void __launch_bounds__(256) k_grid(const GridConst g, int nitems, con
     for (int k = 0; k < nq; k++) {
       const int4 t = stt[k];
       const int ax = gx - t.x, ay = gy - t.y, az = gz - t.z;
-      const float *w = sw + k * 24;
+      const float *w = sw + k * GridStage<CC>::WS;
       const float wx = (ax >= 0 && ax < 8) ? w[ax] : 0.0f;
       const float wy = (ay >= 0 && ay < 8) ? w[8 + ay] : 0.0f;
       const float wz = (az >= 0 && az < 8) ? w[16 + az] : 0.0f;
       const float ww = (wz * wy) * wx;  // src/gridFFT.cpp:1113-1140 order
-      const float2 *v = sv + k * CC;
+      const float2 *v = sv + k * GridStage<CC>::VS;
       if (VEC) {
 #pragma unroll
         for (int c = 0; c < CC / 2; c++) {
@@ -592,6 +646,285 @@ static mrg_status launch_grid_cc(const GridConst &gc, const FrameTraj &ft, const
   return MRG_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Gridding on the tensor cores.  For one 8x2x2 block the scatter is a product
+//   grid[32 points][cols] += W[32 points][pairs] * V[pairs][cols],
+// W the tap weights (wz*wy)*wx of each (point, staged sample) and V the weighted
+// sample values, complex values as two real columns (cols = 2 CC).  It runs as
+// mma.sync m16n8k8 in TF32 with each operand split x = hi + lo (hi = tf32(x),
+// lo = tf32(x - hi)) and three products Wh Vh + Wh Vl + Wl Vh, which carries the
+// products to about 2^-21 relative (FP32 has 2^-24).  Each chunk of 8 pairs is
+// summed by the tensor core from zero and added to the FP32 running sum with
+// round-to-nearest.
+//
+// Fragments (PTX ISA, mma.m16n8k8 .tf32, g = lane / 4, t = lane % 4):
+//   A 16x8: a0 = A[g][t], a1 = A[g+8][t], a2 = A[g][t+4], a3 = A[g+8][t+4]
+//   B 8x8:  b0 = B[t][g], b1 = B[t+4][g]
+//   D 16x8: d0 = D[g][2t], d1 = D[g][2t+1], d2 = D[g+8][2t], d3 = D[g+8][2t+1]
+// Rows: m-tile 0 holds points (px, py, 0) as row px + 8 py, m-tile 1 the z = 1 plane.
+// Columns: n-tile j, column n stands for value index n * NT + j of the staged
+// record, so a lane reads NT consecutive floats of a record for B and ends with
+// the 2 NT consecutive floats [2t NT, 2t NT + 2 NT) of each of its four points:
+// NT whole complex coil values, stored together.
+// Staged records are 16-byte chunks XOR-swizzled by the record index (stage_swz)
+// so the eight lanes of each 16-byte phase hit eight different bank groups.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t to_tf32(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;\n" : "=r"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ void split_tf32(float x, uint32_t &hi, uint32_t &lo) {
+  hi = to_tf32(x);
+  lo = to_tf32(x - __uint_as_float(hi));
+}
+// d = A B (accumulator input zero)
+__device__ __forceinline__ void mma_tf32_z(float d[4], const uint32_t a[4], uint32_t b0, uint32_t b1) {
+  asm("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%10,%10,%10,%10};\n"
+      : "=f"(d[0]), "=f"(d[1]), "=f"(d[2]), "=f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1), "f"(0.0f));
+}
+__device__ __forceinline__ void mma_tf32(float d[4], const uint32_t a[4], uint32_t b0, uint32_t b1) {
+  asm(
+      "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// XOR applied to the 16-byte chunk index of staged record k.  For 8 and 4 n-tiles
+// it takes 8 distinct values over any 8 consecutive records (conflict-free staging
+// writes, one record per lane) and keeps the B-fragment reads conflict-free (lanes
+// (g, t) of a phase read chunk 2g / 2g+1, resp. g, of records k0 + t or k0 + 4 + t).
+template <int NT>
+__device__ __forceinline__ int stage_swz(int k) {
+  if (NT >= 8) return (k & 1) | ((k & 2) << 1) | ((k & 4) >> 1);
+  if (NT == 4) return ((k & 3) << 1) | ((k & 4) >> 2);
+  if (NT == 2) return k & 2;
+  return 0;
+}
+
+// One chunk of 8 staged pairs: A fragments from the pairs' x weights and y/z
+// products, B fragments from the swizzled records, 3 MMAs per (m-tile, n-tile)
+// into a zero-based temporary added to the accumulators with round-to-nearest.
+// FULL: all 8 pairs valid (no masking of stale shared memory).
+template <int NT, bool FULL>
+__device__ __forceinline__ void grid_mma_chunk(int k0, int nq, int gq, int tq, int gx, const int4 *stt,
+                                               const float *sw, const float4 *syz, const float *sv,
+                                               float (&d)[2][NT][4]) {
+  constexpr int RV = 8 * NT;
+  const int kA = k0 + tq, kB = k0 + tq + 4;  // the lane's two pairs (columns t and t+4 of A)
+  const bool okA = FULL || kA < nq, okB = FULL || kB < nq;
+  uint32_t ah[2][4], al[2][4];
+  {
+    const int axA = gx - stt[kA].x, axB = gx - stt[kB].x;
+    float wxA = (axA >= 0 && axA < 8) ? sw[kA * 24 + axA] : 0.0f;
+    float wxB = (axB >= 0 && axB < 8) ? sw[kB * 24 + axB] : 0.0f;
+    float4 yA = syz[kA], yB = syz[kB];
+    if (!FULL) {
+      if (!okA) { wxA = 0.f; yA = make_float4(0.f, 0.f, 0.f, 0.f); }
+      if (!okB) { wxB = 0.f; yB = make_float4(0.f, 0.f, 0.f, 0.f); }
+    }
+    // m-tile 0: rows (py 0, pz 0) and (py 1, pz 0); m-tile 1: pz = 1
+    split_tf32(__fmul_rn(yA.x, wxA), ah[0][0], al[0][0]);
+    split_tf32(__fmul_rn(yA.y, wxA), ah[0][1], al[0][1]);
+    split_tf32(__fmul_rn(yB.x, wxB), ah[0][2], al[0][2]);
+    split_tf32(__fmul_rn(yB.y, wxB), ah[0][3], al[0][3]);
+    split_tf32(__fmul_rn(yA.z, wxA), ah[1][0], al[1][0]);
+    split_tf32(__fmul_rn(yA.w, wxA), ah[1][1], al[1][1]);
+    split_tf32(__fmul_rn(yB.z, wxB), ah[1][2], al[1][2]);
+    split_tf32(__fmul_rn(yB.w, wxB), ah[1][3], al[1][3]);
+  }
+  // B: NT consecutive floats [gq*NT, gq*NT + NT) of records kA and kB
+  float bA[NT], bB[NT];
+  {
+    const int f0 = gq * NT;
+    const float *rA = sv + kA * RV, *rB = sv + kB * RV;
+    const int zA = stage_swz<NT>(kA), zB = stage_swz<NT>(kB);
+    if (NT >= 4) {
+#pragma unroll
+      for (int j = 0; j < NT; j += 4) {
+        const int ch = (f0 + j) >> 2;
+        const float4 u = *reinterpret_cast<const float4 *>(rA + 4 * (ch ^ zA));
+        const float4 w = *reinterpret_cast<const float4 *>(rB + 4 * (ch ^ zB));
+        bA[j] = u.x; bA[j + 1] = u.y; bA[j + 2] = u.z; bA[j + 3] = u.w;
+        bB[j] = w.x; bB[j + 1] = w.y; bB[j + 2] = w.z; bB[j + 3] = w.w;
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < NT; j++) {
+        const int f = f0 + j;
+        bA[j] = rA[4 * ((f >> 2) ^ zA) + (f & 3)];
+        bB[j] = rB[4 * ((f >> 2) ^ zB) + (f & 3)];
+      }
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < NT; j++) {
+    uint32_t bh0, bl0, bh1, bl1;
+    split_tf32(okA ? bA[j] : 0.f, bh0, bl0);
+    split_tf32(okB ? bB[j] : 0.f, bh1, bl1);
+#pragma unroll
+    for (int m = 0; m < 2; m++) {
+      // the tensor core rounds its sums toward zero: take each chunk's three products
+      // from zero (small terms first) and add the chunk to the running sum rounded to
+      // nearest, so the truncation does not build up a bias along a long sum
+      float t[4];
+      mma_tf32_z(t, al[m], bh0, bh1);
+      mma_tf32(t, ah[m], bl0, bl1);
+      mma_tf32(t, ah[m], bh0, bh1);
+#pragma unroll
+      for (int e = 0; e < 4; e++) d[m][j][e] = __fadd_rn(d[m][j][e], t[e]);
+    }
+  }
+}
+
+template <int NT, bool VEC>
+__global__ void __launch_bounds__(256, 2) k_grid_mma(const GridConst g, int nitems, const int4 *__restrict__ items,
+                                                 const int *__restrict__ pairs, const float4 *__restrict__ swt,
+                                                 const int4 *__restrict__ sst, const float2 *__restrict__ yw,
+                                                 float2 *__restrict__ grid) {
+  constexpr int CC = 4 * NT;   // coils per pass
+  constexpr int RV = 2 * CC;   // floats per staged record
+  constexpr int NCH = RV / 4;  // 16-byte chunks per record
+  extern __shared__ __align__(16) unsigned char gsm_raw[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int item = blockIdx.x * 8 + warp;
+  if (item >= nitems) return;
+  unsigned char *base = gsm_raw + warp * (GridStage<CC>::bytes + 32 * 16);
+  float *sv = reinterpret_cast<float *>(base);
+  float *sw = reinterpret_cast<float *>(base + GridStage<CC>::V * 8);
+  int4 *stt = reinterpret_cast<int4 *>(base + GridStage<CC>::V * 8 + GridStage<CC>::W * 4);
+  float4 *syz = reinterpret_cast<float4 *>(base + GridStage<CC>::V * 8 + GridStage<CC>::W * 4 + GridStage<CC>::T * 16);
+  const int4 it = __ldg(items + item);
+  const int C = g.C;
+  const int c0 = blockIdx.y * CC;
+  const int nc = min(CC, C - c0);
+  const int bx = it.x % g.nb[0], by = (it.x / g.nb[0]) % g.nb[1], bz = it.x / (g.nb[0] * g.nb[1]);
+  const int gq = lane >> 2, tq = lane & 3;
+  const int gx = bx * BLK_X + gq, gy0 = by * BLK_Y, gz0 = bz * BLK_Z;
+  float d[2][NT][4];
+#pragma unroll
+  for (int m = 0; m < 2; m++)
+#pragma unroll
+    for (int j = 0; j < NT; j++)
+#pragma unroll
+      for (int e = 0; e < 4; e++) d[m][j][e] = 0.f;
+
+  for (int q0 = it.y; q0 < it.z; q0 += 32) {
+    const int nq = min(32, it.z - q0);
+    // Staging, with the lanes of a record copying neighbouring 16-byte pieces so each
+    // copy instruction touches few records (one lane per scattered record would cost a
+    // shared-memory wavefront per lane): lane k holds sample index s of pair k.
+    const int s_own = (lane < nq) ? __ldg(pairs + q0 + lane) : 0;
+    if (lane < nq) cp16(stt + lane, sst + s_own);
+    // weights: 8 lanes per record (6 copy one 16-byte piece each), 4 records per round
+#pragma unroll
+    for (int r0 = 0; r0 < 32; r0 += 4) {
+      const int rec = r0 + (lane >> 3), piece = lane & 7;
+      const int s = __shfl_sync(0xffffffffu, s_own, rec);
+      if (rec < nq && piece < 6) cp16(sw + rec * 24 + 4 * piece, swt + 6 * (int64_t)s + piece);
+    }
+    // sample values: NCH lanes per record, 32 / NCH records per round
+    constexpr int RPI = 32 / NCH;
+#pragma unroll
+    for (int r0 = 0; r0 < 32; r0 += RPI) {
+      const int rec = r0 + lane / NCH, q = lane % NCH;  // chunk q = coils 2q, 2q+1
+      const int s = __shfl_sync(0xffffffffu, s_own, rec);
+      if (rec < nq) {
+        const float2 *v = yw + (int64_t)s * C + c0;
+        float *dst = sv + rec * RV + 4 * (q ^ stage_swz<NT>(rec));
+        if (VEC) {
+          if (2 * q < nc) cp16(dst, v + 2 * q);
+          else *reinterpret_cast<float4 *>(dst) = make_float4(0.f, 0.f, 0.f, 0.f);
+        } else {
+          if (2 * q < nc) cp8(dst, v + 2 * q);
+          else *reinterpret_cast<float2 *>(dst) = make_float2(0.f, 0.f);
+          if (2 * q + 1 < nc) cp8(dst + 2, v + 2 * q + 1);
+          else *reinterpret_cast<float2 *>(dst + 2) = make_float2(0.f, 0.f);
+        }
+      }
+    }
+    asm volatile("cp.async.commit_group;\n" ::);
+    asm volatile("cp.async.wait_group 0;\n" ::);
+    __syncwarp();
+    // each pair's y/z weight products for this block's two y and two z planes,
+    // (wz*wy) first as src/gridFFT.cpp:1113-1140 multiplies them
+    if (lane < nq) {
+      const int4 tt = stt[lane];
+      const float *w = sw + lane * 24;
+      const int ay = gy0 - tt.y, az = gz0 - tt.z;
+      const float wy0 = (ay >= 0 && ay < 8) ? w[8 + ay] : 0.0f;
+      const float wy1 = (ay + 1 >= 0 && ay + 1 < 8) ? w[9 + ay] : 0.0f;
+      const float wz0 = (az >= 0 && az < 8) ? w[16 + az] : 0.0f;
+      const float wz1 = (az + 1 >= 0 && az + 1 < 8) ? w[17 + az] : 0.0f;
+      syz[lane] = make_float4(__fmul_rn(wz0, wy0), __fmul_rn(wz0, wy1), __fmul_rn(wz1, wy0), __fmul_rn(wz1, wy1));
+    }
+    __syncwarp();
+    for (int k0 = 0; k0 < nq; k0 += 8) {
+      if (k0 + 8 <= nq) grid_mma_chunk<NT, true>(k0, nq, gq, tq, gx, stt, sw, syz, sv, d);
+      else grid_mma_chunk<NT, false>(k0, nq, gq, tq, gx, stt, sw, syz, sv, d);
+    }
+    __syncwarp();
+  }
+  // the lane's points (gx, gy0 + h, gz0 + m) hold floats [2 t NT, 2 t NT + 2 NT) of the chunk
+#pragma unroll
+  for (int m = 0; m < 2; m++)
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      float o[2 * NT];
+#pragma unroll
+      for (int j = 0; j < NT; j++) {
+        o[j] = d[m][j][2 * h];
+        o[NT + j] = d[m][j][2 * h + 1];
+      }
+      const int cl = tq * NT;  // first coil of the lane within the chunk
+      const int64_t gi = (((int64_t)(gz0 + m) * g.S[1] + (gy0 + h)) * g.S[0] + gx) * C + c0 + cl;
+      if (it.w) {
+#pragma unroll
+        for (int j = 0; j < NT; j++)
+          if (cl + j < nc) {
+            atomicAdd(&grid[gi + j].x, o[2 * j]);
+            atomicAdd(&grid[gi + j].y, o[2 * j + 1]);
+          }
+      } else if (VEC && NT >= 2) {
+        float4 *o4 = reinterpret_cast<float4 *>(grid + gi);
+#pragma unroll
+        for (int j = 0; j < NT / 2; j++)
+          if (cl + 2 * j < nc) o4[j] = make_float4(o[4 * j], o[4 * j + 1], o[4 * j + 2], o[4 * j + 3]);
+      } else {
+#pragma unroll
+        for (int j = 0; j < NT; j++)
+          if (cl + j < nc) grid[gi + j] = make_float2(o[2 * j], o[2 * j + 1]);
+      }
+    }
+}
+
+template <int NT>
+static mrg_status launch_grid_mma(const GridConst &gc, const FrameTraj &ft, const float2 *yw, float2 *grid,
+                                  cudaStream_t st) {
+  constexpr int CC = 4 * NT;
+  const bool vec = (gc.C % 2 == 0) && (((uintptr_t)yw & 15) == 0) && (((uintptr_t)grid & 15) == 0);
+  const dim3 blocks((unsigned)((ft.nitems + 7) / 8), (unsigned)((gc.C + CC - 1) / CC));
+  const size_t smem = 8 * (GridStage<CC>::bytes + 32 * 16);  // + the y/z products of 32 pairs
+  static bool attr = false;
+  if (!attr) {
+    MRG_CUDA(cudaFuncSetAttribute(k_grid_mma<NT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    MRG_CUDA(cudaFuncSetAttribute(k_grid_mma<NT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = true;
+  }
+  if (vec)
+    k_grid_mma<NT, true><<<blocks, 256, smem, st>>>(gc, ft.nitems, ft.items, ft.pairs, ft.swt, ft.sst, yw, grid);
+  else
+    k_grid_mma<NT, false><<<blocks, 256, smem, st>>>(gc, ft.nitems, ft.items, ft.pairs, ft.swt, ft.sst, yw, grid);
+  MRG_LAUNCHED();
+  return MRG_OK;
+}
+
+// n-tiles (4 coils each) per pass of the tensor-core kernel when none was tuned.
+static int default_grid_nt(int C) { return C > 16 ? 8 : (C > 8 ? 4 : (C > 4 ? 2 : 1)); }
+
 mrg_status launch_grid(const GridConst &gc, const FrameTraj &ft, const float2 *yw, float2 *grid, cudaStream_t st) {
   if (ft.nsplit > 0) {
     const int64_t n = (int64_t)ft.nsplit * BLK_X * BLK_Y * BLK_Z * gc.C;
@@ -599,6 +932,14 @@ mrg_status launch_grid(const GridConst &gc, const FrameTraj &ft, const float2 *y
     MRG_LAUNCHED();
   }
   const int C = gc.C;
+  if (ft.grid_cc < 0 || (ft.grid_cc == 0 && gc.grid_mode == 2)) {
+    switch (ft.grid_cc < 0 ? -ft.grid_cc : default_grid_nt(C)) {
+      case 1: return launch_grid_mma<1>(gc, ft, yw, grid, st);
+      case 2: return launch_grid_mma<2>(gc, ft, yw, grid, st);
+      case 4: return launch_grid_mma<4>(gc, ft, yw, grid, st);
+      default: return launch_grid_mma<8>(gc, ft, yw, grid, st);
+    }
+  }
   if (ft.grid_cc == 16 && C > 16) return launch_grid_cc<16>(gc, ft, yw, grid, st);
   if (ft.grid_cc == 8 && C > 8) return launch_grid_cc<8>(gc, ft, yw, grid, st);
   if (C <= 1) return launch_grid_cc<1>(gc, ft, yw, grid, st);
@@ -793,27 +1134,38 @@ static float time_ms(cudaStream_t st, const std::function<mrg_status()> &f, int 
 mrg_status autotune_frame(const GridConst &gc, FrameTraj &ft, float2 *grid, float2 *y, cudaStream_t st) {
   if (ft.nvalid == 0) return MRG_OK;
   float best = 1e30f;
-  int bestG = ungrid_group_default(gc.C), bestS = 256;
-  for (int G : {4, 8, 16, 32}) {
-    if (G > 2 * gc.C && G > 4) continue;
-    for (int spb : {128, 512}) {
-      ft.ungrid_G = G;
-      ft.ungrid_spb = spb;
-      const float ms = time_ms(st, [&]() { return launch_ungrid(gc, ft, grid, nullptr, y, false, st); }, 2);
-      if (ms < best) {
-        best = ms;
-        bestG = G;
-        bestS = spb;
+  int bestG = ungrid_group_default(gc.C), bestS = 256, bestP = 1;
+  for (int cpl : {1, 2}) {
+    if (cpl == 2 && gc.C % 2) continue;
+    for (int G : {4, 8, 16, 32}) {
+      if (G * cpl > 2 * gc.C && G > 4) continue;
+      for (int spb : {128, 512}) {
+        ft.ungrid_G = G;
+        ft.ungrid_spb = spb;
+        ft.ungrid_cpl = cpl;
+        const float ms = time_ms(st, [&]() { return launch_ungrid(gc, ft, grid, nullptr, y, false, st); }, 2);
+        if (ms < best) {
+          best = ms;
+          bestG = G;
+          bestS = spb;
+          bestP = cpl;
+        }
       }
     }
   }
   ft.ungrid_G = bestG;
   ft.ungrid_spb = bestS;
+  ft.ungrid_cpl = bestP;
   ft.tune_ungrid_ms = best;
   best = 1e30f;
   int bestCC = 0;
-  for (int cc : {0, 16, 8}) {
-    if (cc && gc.C <= cc) continue;
+  // CUDA-core kernel: all coils, 16 or 8 per pass; tensor-core kernel (negative): 4n coils per pass
+  for (int cc : {0, 16, 8, -8, -4, -2, -1}) {
+    if (cc > 0 && gc.C <= cc) continue;
+    if (cc >= 0 && gc.grid_mode == 2) continue;
+    if (cc < 0 && gc.grid_mode == 1) continue;
+    if (cc < 0 && -cc > default_grid_nt(gc.C)) continue;  // more coils per pass than the plan has
+    if (cc < 0 && -cc < default_grid_nt(gc.C) / 2) continue;
     ft.grid_cc = cc;
     const float ms = time_ms(st, [&]() { return launch_grid(gc, ft, y, grid, st); }, 2);
     if (ms < best) {

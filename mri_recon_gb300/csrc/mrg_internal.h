@@ -120,6 +120,7 @@ struct GridConst {
   int nb[3];   // gridding blocks per axis
   int C;       // coils
   int eval;    // 0: table interpolation, 1: analytic Kaiser-Bessel
+  int grid_mode;  // 0: fastest timed, 1: CUDA-core gridding, 2: tensor-core gridding
   float beta[3];
   double kb_norm[3];
 };
@@ -129,6 +130,7 @@ struct FrameTraj {
   int nvalid = 0;
   float4 *spos = nullptr;   // [M] sorted, valid first: (dkx, dky, dkz, kw)
   float *stap = nullptr;    // [M] taper exp(-|k|^2/(2 k_rad^2))
+  float *skr = nullptr;     // [M] |k|^2 (float, as the reference sums it), for a new k_rad
   int *perm = nullptr;      // [M] sorted -> original sample index
   float4 *swt = nullptr;    // [nvalid][6] tap weights wx[8], wy[8], wz[8] (chop sign included, zero padded)
   int4 *sst = nullptr;      // [nvalid] first tap (sx, sy, sz) and tap counts nx | ny << 4 | nz << 8
@@ -142,13 +144,23 @@ struct FrameTraj {
   float4 *sdw = nullptr;      // [nvalid][6] d(tap weight)/dk per axis (allocated by mrg_grad)
   bool has_data = false;
   // launch shapes picked by autotune_frame (0: defaults)
-  int ungrid_G = 0, ungrid_spb = 0, grid_cc = 0;
+  int ungrid_G = 0, ungrid_spb = 0, ungrid_cpl = 0, grid_cc = 0;
   float tune_ungrid_ms = 0.f, tune_grid_ms = 0.f;
 };
 
 mrg_status traj_setup(const GridConst &gc, FrameTraj &ft, const float *kx, const float *ky, const float *kz,
                       const float *kw, int64_t M, int max_pairs, cudaStream_t st);
 void traj_free(FrameTraj &ft);
+mrg_status launch_retaper(const GridConst &gc, FrameTraj &ft, cudaStream_t st);
+// coil images / sum of squares from the cropped E^H transform t[v][c]; blur; SOS normalisation
+mrg_status launch_coil_images(const float2 *t, int C, const int N[3], const float *wx, const float *wy,
+                              const float *wz, float2 *out, int64_t es, int64_t vs, bool accumulate,
+                              cudaStream_t st);
+mrg_status launch_sos_images(const float2 *t, int C, const int N[3], const float *wx, const float *wy,
+                             const float *wz, float2 *X, cudaStream_t st);
+mrg_status gaussian_blur_ex(float2 *X, int nvol, const int N[3], int64_t es, int64_t vs, const float sigma[3],
+                            cudaStream_t st);
+mrg_status sos_normalize_ex(float2 *A, int C, int64_t nimg, int64_t es, int64_t vs, cudaStream_t st);
 // y[s][c] = sum over taps of grid (gridFFT::chop_grid_backward), minus diff[s][c] if given;
 // with `weigh` the result is multiplied by kw and the taper, ready for launch_grid.
 mrg_status launch_ungrid(const GridConst &gc, const FrameTraj &ft, const float2 *grid, const float2 *diff,
@@ -186,6 +198,7 @@ struct Scalars {
   int pad;
 };
 mrg_status launch_interleave(const float2 *src, int64_t stride, int C, int64_t n, float2 *dst, cudaStream_t st);
+mrg_status launch_deinterleave(const float2 *src, int C, int64_t n, float2 *dst, int64_t stride, cudaStream_t st);
 mrg_status launch_zero(void *p, size_t bytes, cudaStream_t st);
 mrg_status launch_copy(float2 *dst, const float2 *src, int64_t n, cudaStream_t st);
 mrg_status cg_dots(const float2 *R, const float2 *P, const float2 *L, int64_t n, double *part, int nblk,
@@ -194,6 +207,13 @@ mrg_status cg_update(float2 *X, float2 *R, const float2 *P, const float2 *L, int
                      Scalars *sc, double *resid, cudaStream_t st);
 mrg_status cg_pupdate(float2 *P, const float2 *R, int64_t n, const Scalars *sc, cudaStream_t st);
 int reduce_blocks(int64_t n);
+// Blocks for a grid-stride loop over n items: enough to fill the 152 SMs many times over.
+inline int grid_blocks(int64_t n, int threads) {
+  int64_t b = (n + threads - 1) / threads;
+  if (b < 1) b = 1;
+  if (b > 152 * 64) b = 152 * 64;
+  return (int)b;
+}
 
 // FISTA pieces
 mrg_status launch_fill(float2 *X, int64_t n, float2 v, cudaStream_t st);

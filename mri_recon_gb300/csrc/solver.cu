@@ -165,6 +165,23 @@ __global__ void k_interleave(const float2 *__restrict__ src, int64_t stride, int
   }
 }
 
+// dst[c * stride + v] = src[v * C + c]  (plan layout back to per-coil volumes)
+__global__ void k_deinterleave(const float2 *__restrict__ src, int C, int64_t n, float2 *__restrict__ dst,
+                               int64_t stride) {
+  const int64_t tot = n * C;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < tot; e += (int64_t)gridDim.x * blockDim.x) {
+    const int c = (int)(e / n);
+    const int64_t v = e - (int64_t)c * n;
+    dst[(int64_t)c * stride + v] = src[v * C + c];
+  }
+}
+
+mrg_status launch_deinterleave(const float2 *src, int C, int64_t n, float2 *dst, int64_t stride, cudaStream_t st) {
+  k_deinterleave<<<reduce_blocks(n * C), RT, 0, st>>>(src, C, n, dst, stride);
+  MRG_LAUNCHED();
+  return MRG_OK;
+}
+
 mrg_status launch_interleave(const float2 *src, int64_t stride, int C, int64_t n, float2 *dst, cudaStream_t st) {
   k_interleave<<<reduce_blocks(n * C), RT, 0, st>>>(src, stride, C, n, dst);
   MRG_LAUNCHED();

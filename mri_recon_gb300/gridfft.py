@@ -67,7 +67,7 @@ class Plan:
     """Coil-batched gridFFT plan with ``ncoils`` coils and ``nframes`` trajectories."""
 
     def __init__(self, N, ncoils=1, nframes=1, overgrid=1.5, dwin=-1.0, kernel_type=KAISER_KERNEL, k_rad=9999.0,
-                 tile=0, max_pairs=0, time_grid=0, analytic_kernel=False):
+                 tile=0, max_pairs=0, time_grid=0, analytic_kernel=False, grid_mode=0):
         L = _lib.load()
         if np.isscalar(N):
             N = (N, N, N)
@@ -78,6 +78,7 @@ class Plan:
         cfg.overgrid, cfg.dwin, cfg.kernel_type, cfg.k_rad = overgrid, dwin, kernel_type, k_rad
         cfg.tile, cfg.max_pairs, cfg.time_grid = tile, max_pairs, time_grid
         cfg.kernel_eval = 1 if analytic_kernel else 0
+        cfg.grid_mode = grid_mode
         h = ctypes.c_void_p()
         _lib.check(L.mrg_plan_create(ctypes.byref(cfg), self.N[0], self.N[1], self.N[2], self.ncoils, self.nframes,
                                      ctypes.byref(h)))
@@ -92,6 +93,7 @@ class Plan:
         self.S, self.og, self.grid_ratio, self.beta, self.dwin = tuple(S), tuple(og), tuple(gr), tuple(be), tuple(dw)
         self.lut_len = ll.value
         self.M = [0] * self.nframes
+        self.k_rad = float(k_rad)
 
     def close(self):
         if getattr(self, "_h", None):
@@ -140,7 +142,7 @@ class Plan:
         ms = (ctypes.c_float * 2)()
         _lib.check(_lib.load().mrg_frame_tuning(self._h, frame, out, ms))
         return dict(ungrid_lanes=out[0], ungrid_samples_per_cta=out[1], grid_coils_per_pass=out[2],
-                    ungrid_ms=ms[0], grid_ms=ms[1])
+                    ungrid_coils_per_lane=out[3], ungrid_ms=ms[0], grid_ms=ms[1])
 
     def set_data(self, frame, data, stream=None):
         """data: (C, M) complex64."""
@@ -192,6 +194,53 @@ class Plan:
         a = _Args()
         _lib.check(_lib.load().mrg_forward_coil(self._h, frame, a.ptr(X, np.complex64), a.ptr(smap, np.complex64),
                                                 a.ptr(out), a.ptr(diff, np.complex64), _stream(stream)))
+        return out
+
+    def set_k_rad(self, k_rad, stream=None):
+        """The public gridFFT::k_rad field: radius of E^H's Gaussian taper, every frame."""
+        _lib.check(_lib.load().mrg_set_k_rad(self._h, float(k_rad), _stream(stream)))
+        self.k_rad = float(k_rad)
+
+    def _new_images(self, like, n):
+        shape = ((n,) if n else ()) + self.ishape
+        if _is_tensor(like) and like.is_cuda:
+            return torch.zeros(shape, dtype=torch.complex64, device=like.device)
+        return np.zeros(shape, np.complex64)
+
+    def adjoint_coils(self, frame, data, images=None, stream=None):
+        """images[c] += E_c^H (data_c * kw) without maps, one image per coil
+        (gridFFT::forward without smap).  data is (C, M); returns (C,) + ishape."""
+        a = _Args()
+        if images is None:
+            images = self._new_images(data, self.ncoils)
+        elif not _is_tensor(images):
+            images = np.ascontiguousarray(images, dtype=np.complex64)
+        stride = _numel(data) // self.ncoils
+        _lib.check(_lib.load().mrg_adjoint_coils(self._h, frame, a.ptr(data, np.complex64), stride, a.ptr(images),
+                                                 _numel(images) // self.ncoils, _stream(stream)))
+        return images
+
+    def adjoint_sos(self, frame, data, X=None, stream=None):
+        """X += sum_c |deapp(E_c^H (data_c * kw))|^2 (gridFFT::forward_sos over coils)."""
+        a = _Args()
+        if X is None:
+            X = self._new_images(data, 0)
+        elif not _is_tensor(X):
+            X = np.ascontiguousarray(X, dtype=np.complex64)
+        stride = _numel(data) // self.ncoils
+        _lib.check(_lib.load().mrg_adjoint_sos(self._h, frame, a.ptr(data, np.complex64), stride, a.ptr(X),
+                                               _stream(stream)))
+        return X
+
+    def lowres_smaps(self, frame, data, smap_res=8.0, blur=(0.0, 0.0, 0.0), stream=None):
+        """Low-resolution, SOS-normalised coil maps from this frame's data; they become the
+        plan's maps and are returned as (C,) + ishape."""
+        a = _Args()
+        out = self._new_images(data, self.ncoils)
+        b = (ctypes.c_float * 3)(*[float(v) for v in blur])
+        stride = _numel(data) // self.ncoils
+        _lib.check(_lib.load().mrg_lowres_smaps(self._h, frame, a.ptr(data, np.complex64), stride, float(smap_res), b,
+                                                a.ptr(out), _numel(out) // self.ncoils, _stream(stream)))
         return out
 
     def grad(self, frame, X, y, stream=None):
@@ -285,6 +334,30 @@ if torch is not None:
             return gx * gf, gk * gf, None, None
 
 
+def gaussian_blur(X, sigma, stream=None):
+    """gaussian_blur of one volume (Nz, Ny, Nx) or a stack (n, Nz, Ny, Nx), in place; returns X."""
+    a = _Args()
+    if not _is_tensor(X):
+        X = np.ascontiguousarray(X, dtype=np.complex64)
+    shape = tuple(X.shape)
+    nvol = 1 if len(shape) == 3 else int(np.prod(shape[:-3]))
+    Nz, Ny, Nx = shape[-3:]
+    sig = (ctypes.c_float * 3)(*[float(v) for v in sigma])
+    _lib.check(_lib.load().mrg_gaussian_blur(a.ptr(X), nvol, Nx, Ny, Nz, Nx * Ny * Nz, sig, _stream(stream)))
+    return X
+
+
+def sos_normalize(maps, stream=None):
+    """RECON::sos_normalize on (C, Nz, Ny, Nx) maps, in place; returns maps."""
+    a = _Args()
+    if not _is_tensor(maps):
+        maps = np.ascontiguousarray(maps, dtype=np.complex64)
+    C = int(maps.shape[0])
+    n = _numel(maps) // C
+    _lib.check(_lib.load().mrg_sos_normalize(a.ptr(maps), C, n, n, _stream(stream)))
+    return maps
+
+
 def fista_params(**kw):
     p = _lib.MrgFistaParams()
     _lib.load().mrg_fista_params_default(ctypes.byref(p))
@@ -334,10 +407,21 @@ class gridFFT:
             self._traj_key = key
             self._traj_refs = (kx, ky, kz, kw)
 
+    def _sync_k_rad(self):
+        if self.k_rad != self._plan.k_rad:
+            self._plan.set_k_rad(self.k_rad)
+
     def forward(self, X, smap, data, kx, ky, kz, kw):
         """X += E^H data (gridFFT::forward, src/gridFFT.cpp:791-812).  smap may be None."""
         self._traj(kx, ky, kz, kw)
+        self._sync_k_rad()
         return self._plan.adjoint_coil(0, smap, data, X)
+
+    def forward_sos(self, X, data, kx, ky, kz, kw):
+        """X += |deapp(E^H data)|^2 (gridFFT::forward_sos, src/gridFFT.cpp:722-757)."""
+        self._traj(kx, ky, kz, kw)
+        self._sync_k_rad()
+        return self._plan.adjoint_sos(0, data, X)
 
     def backward(self, X, smap, data, kx, ky, kz, kw):
         """data = E X (gridFFT::backward, src/gridFFT.cpp:824-844)."""

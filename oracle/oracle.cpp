@@ -414,6 +414,29 @@ struct OPlan {
     }
   }
 
+  // gridFFT::forward_sos (gridFFT.cpp:722-757): grid, inverse FFT, deapp
+  // (:912-924: image *= winz*winy*winx), then X += image * conj(image)
+  // (accumulate_sos, :960-970).
+  void adjoint_sos(cx<R> *X, const cx<R> *data, const float *kx, const float *ky, const float *kz,
+                   const float *kw, long M) {
+    std::fill(grid.begin(), grid.end(), cx<R>(0, 0));
+    grid_forward(data, kx, ky, kz, kw, M);
+    do_ifft();
+    const int Nx = g.N[0], Ny = g.N[1], Nz = g.N[2];
+#pragma omp parallel for
+    for (int k = 0; k < Nz; k++) {
+      R wtz = g.win[2][k + g.og_s[2]];
+      for (int j = 0; j < Ny; j++) {
+        R wty = wtz * (R)g.win[1][j + g.og_s[1]];
+        for (int i = 0; i < Nx; i++) {
+          long ii = i + (long)Nx * (j + (long)Ny * k);
+          cx<R> im = grid[(i + g.og_s[0]) + (long)g.S[0] * ((j + g.og_s[1]) + (long)g.S[1] * (k + g.og_s[2]))];
+          im *= (R)(wty * (R)g.win[0][i + g.og_s[0]]);
+          X[ii] += cx<R>(im.real() * im.real() + im.imag() * im.imag(), (R)0);
+        }
+      }
+    }
+  }
   // gridFFT::forward (E^H, gridFFT.cpp:791-812)
   void adjoint(cx<R> *X, const cx<R> *smap, const cx<R> *data, const float *kx, const float *ky, const float *kz,
                const float *kw, long M) {
@@ -430,6 +453,60 @@ struct OPlan {
     grid_backward(data, kx, ky, kz, kw, M, diff);
   }
 };
+
+// ---------------------------------------------------------------------------
+// Coil-map helpers of the low-resolution map estimate (recon_lib.cpp:2694-2950).
+// ---------------------------------------------------------------------------
+// gaussian_blur_template (ArrayTemplates.cpp:489-601): per axis with sigma > 0,
+// kern[t] = exp(-(t - w)^2 / (2 sigma^2)), w = (int)(5 sigma), t = 0..2w,
+// normalised to sum 1; output i sums kern[ii - i + w] * in[ii] over
+// ii in [max(i - w, 0), min(i + w, n)) -- the upper end is exclusive, so the
+// last tap never contributes, as in the reference.
+template <typename R>
+static void gaussian_blur(cx<R> *X, int Nx, int Ny, int Nz, const float *sig) {
+  const int N[3] = {Nx, Ny, Nz};
+  const long st[3] = {1, Nx, (long)Nx * Ny};
+  for (int d = 0; d < 3; d++) {
+    if (!(sig[d] > 0)) continue;
+    const int w = (int)(5 * sig[d]);
+    std::vector<float> kern(2 * w + 1);
+    double tot = 0;
+    for (int t = 0; t <= 2 * w; t++) {
+      const float a = (float)t - w;
+      kern[t] = (float)std::exp(-(a * a) / (2.0 * (double)(sig[d] * sig[d])));
+    }
+    for (int t = 0; t <= 2 * w; t++) tot += kern[t];
+    for (int t = 0; t <= 2 * w; t++) kern[t] = (float)(kern[t] / tot);
+    const int n = N[d];
+    const int a1 = (d + 1) % 3, a2 = (d + 2) % 3;
+    const long nl = (long)N[a1] * N[a2];
+#pragma omp parallel for
+    for (long l = 0; l < nl; l++) {
+      const long b = (l % N[a1]) * st[a1] + (l / N[a1]) * st[a2];
+      std::vector<cx<R>> tmp(n);
+      for (int i = 0; i < n; i++) tmp[i] = X[b + i * st[d]];
+      for (int i = 0; i < n; i++) {
+        const int s0 = std::max(i - w, 0), e0 = std::min(i + w, n);
+        cx<R> acc(0, 0);
+        for (int ii = s0; ii < e0; ii++) acc += (R)kern[ii - (i - w)] * tmp[ii];
+        X[b + i * st[d]] = acc;
+      }
+    }
+  }
+}
+
+// sos_normalize with smap_thresh == 0 (recon_lib.cpp:3043-3062):
+// A_c /= sqrt(sum_c |A_c|^2), the sum taken coil by coil.
+template <typename R>
+static void sos_normalize(cx<R> **A, int C, long n) {
+#pragma omp parallel for
+  for (long v = 0; v < n; v++) {
+    R sos = 0;
+    for (int c = 0; c < C; c++) sos += A[c][v].real() * A[c][v].real() + A[c][v].imag() * A[c][v].imag();
+    sos = std::sqrt(sos);
+    for (int c = 0; c < C; c++) A[c][v] = cx<R>(A[c][v].real() / sos, A[c][v].imag() / sos);
+  }
+}
 
 // ---------------------------------------------------------------------------
 // glibc random() TYPE_3 stream for the default seed (the additive lagged
@@ -966,6 +1043,23 @@ void orc_adjoint(void *hv, void *X, const void *smap, const void *data, const fl
   OHandle *h = (OHandle *)hv;
   if (h->prec) h->pd.adjoint((cx<double> *)X, (const cx<double> *)smap, (const cx<double> *)data, kx, ky, kz, kw, M);
   else h->pf.adjoint((cx<float> *)X, (const cx<float> *)smap, (const cx<float> *)data, kx, ky, kz, kw, M);
+}
+void orc_adjoint_sos(void *hv, void *X, const void *data, const float *kx, const float *ky, const float *kz,
+                     const float *kw, long M) {
+  OHandle *h = (OHandle *)hv;
+  if (h->prec) h->pd.adjoint_sos((cx<double> *)X, (const cx<double> *)data, kx, ky, kz, kw, M);
+  else h->pf.adjoint_sos((cx<float> *)X, (const cx<float> *)data, kx, ky, kz, kw, M);
+}
+// gridFFT::k_rad is a public field the map estimate changes between calls
+// (recon_lib.cpp:2738, :2786).
+void orc_set_k_rad(void *hv, float k_rad) { ((OHandle *)hv)->g().k_rad = k_rad; }
+void orc_gaussian_blur(void *X, int Nx, int Ny, int Nz, const float *sig, int prec) {
+  if (prec) gaussian_blur<double>((cx<double> *)X, Nx, Ny, Nz, sig);
+  else gaussian_blur<float>((cx<float> *)X, Nx, Ny, Nz, sig);
+}
+void orc_sos_normalize(void **A, int C, long n, int prec) {
+  if (prec) sos_normalize<double>((cx<double> **)A, C, n);
+  else sos_normalize<float>((cx<float> **)A, C, n);
 }
 void orc_forward(void *hv, const void *X, const void *smap, void *data, const float *kx, const float *ky,
                  const float *kz, const float *kw, long M, const void *diff) {

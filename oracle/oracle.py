@@ -43,6 +43,10 @@ def lib():
         L.orc_get_tables.argtypes = [vp, fp, fp]
         L.orc_adjoint.argtypes = [vp, vp, vp, vp, fp, fp, fp, fp, ctypes.c_long]
         L.orc_forward.argtypes = [vp, vp, vp, vp, fp, fp, fp, fp, ctypes.c_long, vp]
+        L.orc_adjoint_sos.argtypes = [vp, vp, vp, fp, fp, fp, fp, ctypes.c_long]
+        L.orc_set_k_rad.argtypes = [vp, ctypes.c_float]
+        L.orc_gaussian_blur.argtypes = [vp] + [ctypes.c_int] * 3 + [fp, ctypes.c_int]
+        L.orc_sos_normalize.argtypes = [ctypes.POINTER(vp), ctypes.c_int, ctypes.c_long, ctypes.c_int]
         L.orc_get_grid.argtypes = [vp, vp]
         L.orc_set_grid.argtypes = [vp, vp]
         L.orc_grid.argtypes = [vp, vp, fp, fp, fp, fp, ctypes.c_long]
@@ -154,6 +158,19 @@ class Plan:
         kx, px = _f32(kx); ky, py = _f32(ky); kz, pz = _f32(kz); kw, pw = _f32(kw)
         lib().orc_adjoint(self.h, _ptr(X), _ptr(smap), _ptr(data), px, py, pz, pw, kx.size)
         return X
+
+    def adjoint_sos(self, X, data, kx, ky, kz, kw):
+        """gridFFT::forward_sos: X += |deapp(ifft(grid(data*kw)))|^2."""
+        X = self._c(X)
+        assert X.flags.writeable
+        data = self._c(data)
+        kx, px = _f32(kx); ky, py = _f32(ky); kz, pz = _f32(kz); kw, pw = _f32(kw)
+        lib().orc_adjoint_sos(self.h, _ptr(X), _ptr(data), px, py, pz, pw, kx.size)
+        return X
+
+    def set_k_rad(self, k_rad):
+        """The public gridFFT::k_rad field (taper radius of E^H)."""
+        lib().orc_set_k_rad(self.h, k_rad)
 
     def forward(self, X, smap, kx, ky, kz, kw, diff=None):
         """gridFFT::backward (E), or backward_residual when diff is given."""
@@ -323,6 +340,40 @@ def llr_thresh(vols, bs, block_iter, alpha, smax, rand_skip):
     arr = (ctypes.c_void_p * len(vols))(*[v.ctypes.data for v in vols])
     lib().orc_llr_thresh(arr, len(vols), _ip((Nx, Ny, Nz)), _ip(bs), block_iter, alpha, smax, rand_skip, prec)
     return vols
+
+
+def gaussian_blur(X, sigma):
+    """gaussian_blur_template on one [Nz][Ny][Nx] complex volume (copy), sigma = (x, y, z)."""
+    X = np.ascontiguousarray(X).copy()
+    prec = 1 if X.dtype == np.complex128 else 0
+    Nz, Ny, Nx = X.shape
+    sig = (ctypes.c_float * 3)(*[float(v) for v in sigma])
+    lib().orc_gaussian_blur(_ptr(X), Nx, Ny, Nz, sig, prec)
+    return X
+
+
+def sos_normalize(maps):
+    """RECON::sos_normalize (smap_thresh == 0) on a [C][Nz][Ny][Nx] array (copy)."""
+    maps = np.ascontiguousarray(maps).copy()
+    prec = 1 if maps.dtype == np.complex128 else 0
+    C = maps.shape[0]
+    arr = (ctypes.c_void_p * C)(*[maps[c].ctypes.data for c in range(C)])
+    lib().orc_sos_normalize(arr, C, maps[0].size, prec)
+    return maps
+
+
+def lowres_smaps(plan, data, kx, ky, kz, kw, smap_res=8.0, blur=(0.0, 0.0, 0.0)):
+    """The LOWRES coil-map estimate with SOS normalisation (recon_lib.cpp:2694-2950):
+    per coil, E^H without maps at k_rad = smap_res, Gaussian blur, then sos_normalize.
+    data is [C][M]; returns [C][Nz][Ny][Nx] and restores k_rad = 9999."""
+    plan.set_k_rad(smap_res)
+    imgs = np.zeros((len(data),) + plan.ishape, plan.cdt)
+    for c in range(len(data)):
+        plan.adjoint(imgs[c], None, data[c], kx, ky, kz, kw)
+        if any(b > 0 for b in blur):
+            imgs[c] = gaussian_blur(imgs[c], blur)
+    plan.set_k_rad(9999.0)
+    return sos_normalize(imgs)
 
 
 def glibc_rand(skip, n):

@@ -166,3 +166,40 @@ def test_errors_do_not_exit(mrg_lib):
         p.forward(0, c["X"])                       # no trajectory yet
     with pytest.raises(m.MrgError, match="UNSUPPORTED"):
         m.Plan(112, 1, 1)                           # S = 176 = 16*11: radix 11 not built
+
+
+@pytest.mark.parametrize("grid_mode", [1, 2])
+@pytest.mark.parametrize("N,C,nproj,max_pairs", [(32, 4, 700, 0), (48, 3, 500, 0), (32, 20, 400, 0),
+                                                  (32, 32, 300, 0), (32, 1, 600, 0), (32, 8, 700, 96)])
+def test_adjoint_each_gridding_kernel(mrg_lib, oracle_lib, grid_mode, N, C, nproj, max_pairs):
+    """Both gridding kernels (FP32 CUDA cores; TF32 tensor cores with the hi/lo
+    split), odd and partial coil chunks, and dense blocks split into work items
+    that flush with atomics (small max_pairs)."""
+    torch = _torch()
+    c = case(N=N, C=C, nproj=nproj)
+    p = mrg_lib.Plan(N, C, 1, grid_mode=grid_mode, max_pairs=max_pairs)
+    p.set_traj(0, c["kx"], c["ky"], c["kz"], c["kw"])
+    p.set_smaps(c["smaps"])
+    tun = p.frame_tuning(0)
+    X = torch.zeros(c["X"].shape, dtype=torch.complex64, device="cuda")
+    p.adjoint(0, torch.from_numpy(c["data"]).cuda(), X)
+    got = X.cpu().numpy()
+    r32, r64 = _oracle_EH(oracle_lib, c, 0), _oracle_EH(oracle_lib, c, 1)
+    assert rel(got, r32) < TOL, tun
+    assert rel(got, r64) < fp64_bound(r32, r64), tun
+
+
+def test_edge_samples_tensor_core_gridding(mrg_lib, oracle_lib):
+    torch = _torch()
+    N, C = 32, 4
+    c = case(N=N, C=C, nproj=10)
+    c["kx"], c["ky"], c["kz"], c["kw"] = edge_trajectory(N)
+    M = c["kx"].size
+    rng = np.random.default_rng(2)
+    c["data"] = (rng.standard_normal((C, M)) + 1j * rng.standard_normal((C, M))).astype(np.complex64)
+    p = mrg_lib.Plan(N, C, 1, grid_mode=2)
+    p.set_traj(0, c["kx"], c["ky"], c["kz"], c["kw"])
+    p.set_smaps(c["smaps"])
+    X = torch.zeros(c["X"].shape, dtype=torch.complex64, device="cuda")
+    p.adjoint(0, torch.from_numpy(c["data"]).cuda(), X)
+    assert rel(X.cpu().numpy(), _oracle_EH(oracle_lib, c, 1)) < TOL

@@ -168,3 +168,82 @@ def test_llr_jacobi_svd_vs_numpy(oracle_lib):
     ref = (U * np.maximum(s - 0.5 * smax, 0)) @ Vh
     got = np.stack([v[:8, :8, :8].ravel() for v in out], 1)
     assert rel(got, ref) < 1e-10
+
+
+def _blur_literal(X, sigma):
+    """gaussian_blur_template written out loop by loop in numpy (float32 taps)."""
+    X = X.astype(np.complex128).copy()
+    for d, s in enumerate(sigma):  # axes x, y, z of a [z][y][x] array
+        if s <= 0:
+            continue
+        w = int(5 * s)
+        t = np.arange(2 * w + 1, dtype=np.float32) - np.float32(w)
+        k = np.exp(-(t * t).astype(np.float64) / (2.0 * np.float64(np.float32(s) * np.float32(s)))).astype(np.float32)
+        k = (k / k.astype(np.float64).sum()).astype(np.float32)
+        ax = 2 - d
+        Y = np.moveaxis(X, ax, -1).copy()
+        out = np.zeros_like(Y)
+        n = Y.shape[-1]
+        for i in range(n):
+            for ii in range(max(i - w, 0), min(i + w, n)):
+                out[..., i] += k[ii - (i - w)] * Y[..., ii]
+        X = np.moveaxis(out, -1, ax)
+    return X
+
+
+def test_gaussian_blur_vs_literal(oracle_lib):
+    rng = np.random.default_rng(1)
+    X = (rng.standard_normal((9, 10, 11)) + 1j * rng.standard_normal((9, 10, 11))).astype(np.complex64)
+    for sigma in [(1.0, 0.0, 0.0), (0.0, 0.6, 0.0), (0.0, 0.0, 1.4), (0.8, 1.1, 0.5)]:
+        got = oracle_lib.gaussian_blur(X.astype(np.complex128), sigma)
+        assert np.max(np.abs(got - _blur_literal(X, sigma))) < 1e-12
+    # the upper tap ii = i + w is excluded, as in the reference's loop bound
+    e = np.zeros((1, 1, 9), np.complex128)
+    e[0, 0, 4] = 1.0
+    out = oracle_lib.gaussian_blur(e, (1.0, 0.0, 0.0))
+    # w = 5: output i reads ii in [i - 5, i + 5) through tap ii - i + 5, so an impulse
+    # at ii = 4 shows tap 9 - i at output i; tap 10 (ii = i + 5) never contributes
+    k = np.exp(-(np.arange(11, dtype=np.float32) - 5) ** 2 / 2.0).astype(np.float32)
+    k = (k / k.astype(np.float64).sum()).astype(np.float32)
+    for i in range(9):
+        t = 4 - (i - 5)
+        expect = k[t] if 0 <= t < 10 else 0.0
+        assert abs(out[0, 0, i] - expect) < 1e-7
+
+
+def test_sos_normalize_vs_numpy(oracle_lib):
+    rng = np.random.default_rng(2)
+    A = (rng.standard_normal((4, 6, 7, 8)) + 1j * rng.standard_normal((4, 6, 7, 8))).astype(np.complex128)
+    got = oracle_lib.sos_normalize(A)
+    ref = A / np.sqrt(np.sum(np.abs(A) ** 2, 0))
+    assert np.max(np.abs(got - ref)) < 1e-12
+
+
+def test_adjoint_sos_is_squared_map_free_adjoint(oracle_lib):
+    c = case(N=24, C=2, nproj=300)
+    p = oracle_lib.Plan(24)
+    a = (c["kx"], c["ky"], c["kz"], c["kw"])
+    X = np.zeros(p.ishape, np.complex64)
+    ref = np.zeros(p.ishape, np.float32)
+    for k in range(2):
+        X = p.adjoint_sos(X, c["data"][k], *a)
+        im = p.adjoint(np.zeros(p.ishape, np.complex64), None, c["data"][k], *a)
+        ref = ref + (im.real * im.real + im.imag * im.imag)
+    # the oracle's gridding adds with OpenMP atomics, so two runs differ in the last bits
+    assert rel(X.real, ref) < 1e-6 and np.all(X.imag == 0)
+
+
+def test_lowres_smaps_unit_sos_and_taper(oracle_lib):
+    c = case(N=24, C=3, nproj=400, nudft=True)
+    p = oracle_lib.Plan(24)
+    a = (c["kx"], c["ky"], c["kz"], c["kw"])
+    maps = oracle_lib.lowres_smaps(p, c["data"], *a, smap_res=8.0)
+    assert np.allclose(np.sqrt(np.sum(np.abs(maps.astype(np.complex128)) ** 2, 0)), 1.0, atol=1e-5)
+    # k_rad 8 is a strong low-pass: the map images are smoother than the full-resolution ones
+    full = p.adjoint(np.zeros(p.ishape, np.complex64), None, c["data"][0], *a)
+    p.set_k_rad(8.0)
+    low = p.adjoint(np.zeros(p.ishape, np.complex64), None, c["data"][0], *a)
+    p.set_k_rad(9999.0)
+    def hf(v):
+        return np.linalg.norm(np.diff(v, axis=2)) / np.linalg.norm(v)
+    assert hf(low) < 0.8 * hf(full)
