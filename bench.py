@@ -71,32 +71,33 @@ def bytes_model(c, nvalid, npairs):
     t1, t2, g = N * N * S * C * b, N * S * S * C * b, S ** 3 * C * b
     y = nvalid * C * b
     return {
-        "E_zfft_setimg": img + smap + t1,
-        "E_yfft": t1 + t2,
-        "E_xfft": t2 + g,
+        "E_xfft_setimg": img + smap + t1,
+        "E_zfft": t1 + t2,
+        "E_yfft": t2 + g,
         "E_ungrid": g + nvalid * 16 + y,
         "EH_grid": y + nvalid * 20 + npairs * 4 + g,
-        "EH_xfft": g + t2,
-        "EH_yfft": t2 + t1,
-        "EH_zfft_accum": t1 + smap + 2 * img,
+        "EH_yfft": g + t2,
+        "EH_zfft": t2 + t1,
+        "EH_xfft_accum": t1 + smap + 2 * img,
     }
 
 
-STAGES = ["E_zfft_setimg", "E_yfft", "E_xfft", "E_ungrid", "EH_grid", "EH_xfft", "EH_yfft", "EH_zfft_accum"]
+STAGES = ["E_xfft_setimg", "E_zfft", "E_yfft", "E_ungrid", "EH_grid", "EH_yfft", "EH_zfft", "EH_xfft_accum"]
 
 
 def kernel_of(stage, tuning, C):
     """Kernel that runs a stage, with the launch shape the autotuner picked."""
     if stage == "E_ungrid":
-        return "k_ungrid<%d,%d>" % (tuning["ungrid_lanes"], max(tuning["ungrid_coils_per_lane"], 1))
+        return "k_ungrid<%d,%d,%d>" % (tuning["ungrid_lanes"], max(tuning["ungrid_coils_per_lane"], 1),
+                                      max(tuning.get("ungrid_rows_per_step", 1), 1))
     if stage == "EH_grid":
         cc = tuning["grid_coils_per_pass"]
         if cc < 0:
             return "k_grid_mma<%d> (TF32 tensor cores, %d coils per pass)" % (-cc, -4 * cc)
         return "k_grid<%d> (FP32 CUDA cores)" % (cc if cc > 0 else min(C, 32))
-    return {"E_zfft_setimg": "k_fft<Q,-1,SETIMG>", "E_yfft": "k_fft<Q,-1,PLAIN>", "E_xfft": "k_fft<Q,-1,PLAIN>",
-            "EH_xfft": "k_fft<Q,+1,PLAIN>", "EH_yfft": "k_fft<Q,+1,PLAIN>",
-            "EH_zfft_accum": "k_fft<Q,+1,ACCUM>"}[stage]
+    return {"E_xfft_setimg": "k_fft<Q,-1,SETIMG>", "E_yfft": "k_fft<Q,-1,PLAIN>", "E_zfft": "k_fft<Q,-1,PLAIN>",
+            "EH_zfft": "k_fft<Q,+1,PLAIN>", "EH_yfft": "k_fft<Q,+1,PLAIN>",
+            "EH_xfft_accum": "k_fft<Q,+1,ACCUM>"}[stage]
 
 
 def peaks():

@@ -106,9 +106,9 @@ mrg_status mrg_frame_info(const mrg_plan *plan, int frame, int64_t *M, int64_t *
 
 /* Launch shapes the autotuner chose for a frame (mrg_config.tile == 0): out = {ungrid lanes
  * per sample, ungrid samples per CTA, gridding coils per pass (0: all; -n: the tensor-core
- * kernel with 4n coils per pass), ungrid coils per lane}; ms = the timed ungrid and grid
- * kernels. */
-mrg_status mrg_frame_tuning(const mrg_plan *plan, int frame, int out[4], float ms[2]);
+ * kernel with 4n coils per pass), ungrid coils per lane, ungrid tap rows loaded per step};
+ * ms = the timed ungrid and grid kernels. */
+mrg_status mrg_frame_tuning(const mrg_plan *plan, int frame, int out[5], float ms[2]);
 
 /* Measured k-space of one frame: ncoil arrays of M complex64, coil c at
  * data + c*coil_stride.  Used by mrg_cg / mrg_fista (data.kdata, src/mri_data.h). */
@@ -259,6 +259,25 @@ mrg_status mrg_gaussian_blur(void *X, int nvol, int Nx, int Ny, int Nz, int64_t 
  * divided by sqrt(sum_c |map_c|^2), coil c at maps + c*coil_stride, nvox voxels. */
 mrg_status mrg_sos_normalize(void *maps, int ncoil, int64_t coil_stride, int64_t nvox, void *stream);
 
+/* Pipe density compensation, RECON::dcf_calc (src/recon_lib.cpp:854-917) with the
+ * DCFgridFFT gridder (src/DCFgridFFT.cpp): kw (M floats, written) from the trajectory
+ * of one encode by `iters` rounds of Kw <- Kw / (G^T G Kw) with the polynomial kernel on
+ * a (int)(overgrid*N + 16)^3 real grid, then the |k|-dependent width correction and |Kw|.
+ * Nx, Ny, Nz: the reconstruction matrix (rcxres, rcyres, rczres).  params may be NULL
+ * (the reference's defaults: -dcf_iter 20, -dcf_dwin 2.1, -dcf_scale 1, -dcf_overgrid
+ * 2.1, -dcf_acc 1, POLY_KERNEL). */
+typedef struct mrg_dcf_params {
+  int iters;       /* -dcf_iter */
+  float dwin;      /* -dcf_dwin: kernel half width in grid points */
+  float scale;     /* -dcf_scale: trajectory scale during the estimate */
+  float overgrid;  /* -dcf_overgrid */
+  float acc;       /* -dcf_acc: kernel widening with |k| */
+  int kernel;      /* 0 POLY_KERNEL, 1 POLY_KERNEL2 (src/DCFgridFFT.h:22-23) */
+} mrg_dcf_params;
+void mrg_dcf_params_default(mrg_dcf_params *p);
+mrg_status mrg_dcf_pipe(const float *kx, const float *ky, const float *kz, int64_t M, int Nx, int Ny, int Nz,
+                        const mrg_dcf_params *params, float *kw, void *stream);
+
 /* Host-only (no GPU needed): the geometry and tables mrg_plan_create would build,
  * i.e. gridFFT::precalc_gridding's S, og_s, grid ratio, Kaiser beta and the LUT / window
  * tables (src/gridFFT.cpp:276-643).  lut (3*lut_len) and win (Sx+Sy+Sz) may be NULL
@@ -273,8 +292,9 @@ mrg_status mrg_rand_stream(int64_t skip, int n, int *out);
 /* Per-stage device timing, the -time_grid stages of src/gridFFT.cpp:727-778 split at
  * this build's kernels.  While enabled, operator calls run eagerly (no graph), each
  * stage is bracketed by CUDA events and its time accumulated:
- *   out[0..3] E:   set_image+z FFT, y FFT, x FFT, ungrid (chop_grid_backward)
- *   out[4..7] E^H: grid (chop_grid_forward), x FFT, y FFT, z FFT+accumulate
+ *   out[0..3] E:   set_image+x FFT, z FFT, y FFT, ungrid (chop_grid_backward)
+ *   out[4..7] E^H: grid (chop_grid_forward), y FFT, z FFT, x FFT+accumulate
+ * (single-coil plans run the FFT axes in the reference's order: z, y, x for E, x, y, z for E^H).
  * mrg_last_timings returns the accumulated ms and the number of operator calls
  * since the previous read, then resets them. */
 mrg_status mrg_set_timing(mrg_plan *plan, int enable);

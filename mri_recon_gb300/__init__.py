@@ -6,5 +6,5 @@ reference's gridFFT / RECON call surface.
 """
 from . import synth  # noqa: F401
 from ._lib import LIB_PATH, MrgError, load  # noqa: F401
-from .gridfft import (KAISER_KERNEL, POLY_KERNEL, SINC_KERNEL, TRIANGLE_KERNEL, Plan, fista_params,  # noqa: F401
-                      gaussian_blur, gridFFT, sos_normalize)
+from .gridfft import (KAISER_KERNEL, POLY_KERNEL, SINC_KERNEL, TRIANGLE_KERNEL, Plan, dcf_pipe,  # noqa: F401
+                      fista_params, gaussian_blur, gridFFT, sos_normalize)

@@ -30,6 +30,11 @@ class MrgConfig(ctypes.Structure):
                 ("max_pairs", ctypes.c_int), ("kernel_eval", ctypes.c_int), ("grid_mode", ctypes.c_int)]
 
 
+class MrgDcfParams(ctypes.Structure):
+    _fields_ = [("iters", ctypes.c_int), ("dwin", ctypes.c_float), ("scale", ctypes.c_float),
+                ("overgrid", ctypes.c_float), ("acc", ctypes.c_float), ("kernel", ctypes.c_int)]
+
+
 class MrgFistaParams(ctypes.Structure):
     _fields_ = [("max_iter", ctypes.c_int), ("max_eig_iter", ctypes.c_int), ("fista", ctypes.c_int),
                 ("cycle_spins", ctypes.c_int), ("wave_levels", ctypes.c_int * 3), ("wave_type", ctypes.c_int),
@@ -62,6 +67,8 @@ SIGNATURES = {
     "mrg_lowres_smaps": (_i, [_vp, _i, _vp, _i64, _f, _fp, _vp, _i64, _vp]),
     "mrg_gaussian_blur": (_i, [_vp, _i, _i, _i, _i, _i64, _fp, _vp]),
     "mrg_sos_normalize": (_i, [_vp, _i, _i64, _i64, _vp]),
+    "mrg_dcf_params_default": (None, [ctypes.POINTER(MrgDcfParams)]),
+    "mrg_dcf_pipe": (_i, [_vp, _vp, _vp, _i64, _i, _i, _i, ctypes.POINTER(MrgDcfParams), _vp, _vp]),
     "mrg_cg": (_i, [_vp, _i, _vp, _dp, _i, _vp]),
     "mrg_fista_params_default": (None, [ctypes.POINTER(MrgFistaParams)]),
     "mrg_fista": (_i, [_vp, ctypes.POINTER(MrgFistaParams), _vp, _dp, _fp, _i, _vp]),

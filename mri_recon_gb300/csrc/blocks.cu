@@ -202,4 +202,41 @@ mrg_status mrg_sos_normalize(void *maps, int ncoil, int64_t coil_stride, int64_t
   return back(maps, tmp, bytes, st);
 }
 
+void mrg_dcf_params_default(mrg_dcf_params *q) {
+  if (!q) return;
+  q->iters = 20;       // -dcf_iter      (src/recon_lib.cpp:126)
+  q->dwin = 2.1f;      // -dcf_dwin      (:127)
+  q->scale = 1.0f;     // -dcf_scale     (:128)
+  q->overgrid = 2.1f;  // -dcf_overgrid  (:129)
+  q->acc = 1.0f;       // -dcf_acc       (:130)
+  q->kernel = 0;       // DCFgridFFT::POLY_KERNEL (:857)
+}
+
+mrg_status mrg_dcf_pipe(const float *kx, const float *ky, const float *kz, int64_t M, int Nx, int Ny, int Nz,
+                        const mrg_dcf_params *q_in, float *kw, void *stream) {
+  if (!kx || !ky || !kz || !kw || M <= 0 || Nx <= 0 || Ny <= 0 || Nz <= 0) {
+    set_error("bad argument");
+    return MRG_ERR_INVALID;
+  }
+  mrg_dcf_params q;
+  if (q_in) q = *q_in; else mrg_dcf_params_default(&q);
+  if (q.iters < 0 || !(q.dwin > 0) || !(q.scale > 0) || !(q.overgrid > 0) || !(q.acc > 0) || q.kernel < 0 ||
+      q.kernel > 1) {
+    set_error("bad density-compensation parameters");
+    return MRG_ERR_INVALID;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t bytes = sizeof(float) * (size_t)M;
+  DevBuf tx, ty, tz, tw;
+  float2 *dx, *dy, *dz, *dw;
+  MRG_TRY(view(kx, bytes, tx, st, &dx));
+  MRG_TRY(view(ky, bytes, ty, st, &dy));
+  MRG_TRY(view(kz, bytes, tz, st, &dz));
+  MRG_TRY(view(kw, bytes, tw, st, &dw));
+  const int N[3] = {Nx, Ny, Nz};
+  MRG_TRY(dcf_pipe((const float *)dx, (const float *)dy, (const float *)dz, M, N, q.iters, q.dwin, q.scale,
+                   q.overgrid, q.acc, q.kernel, (float *)dw, st));
+  return back(kw, tw, bytes, st);
+}
+
 }  // extern "C"

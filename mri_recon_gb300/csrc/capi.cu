@@ -61,7 +61,7 @@ struct mrg_plan {
   void *cg_key[2] = {nullptr, nullptr};
   // autotuned launch shapes, reused while the sample count stays within 2x
   bool tuned = false;
-  int tuned_G = 0, tuned_spb = 0, tuned_cpl = 0, tuned_cc = 0;
+  int tuned_G = 0, tuned_spb = 0, tuned_cpl = 0, tuned_uy = 0, tuned_cc = 0;
   int64_t tuned_nvalid = 0;
   float tuned_ms[2] = {0.f, 0.f};
   // FISTA state
@@ -191,8 +191,13 @@ static void tcollect(mrg_plan *p, int base) {
   if (base == 0) p->timing_calls += 1;
   if (p->cfg.time_grid) {
     const float *t = p->timings + base;
-    if (base == 0) printf("Backward::copy+zfft:%.3f,yfft:%.3f,xfft:%.3f,igrid:%.3f ms\n", t[0], t[1], t[2], t[3]);
-    else printf("Forward::grid:%.3f,xfft:%.3f,yfft:%.3f,zfft+accumulate:%.3f ms\n", t[0], t[1], t[2], t[3]);
+    const bool one = (p->C == 1);  // single-coil plans run the reference's pass order
+    if (base == 0)
+      printf(one ? "Backward::copy+zfft:%.3f,yfft:%.3f,xfft:%.3f,igrid:%.3f ms\n"
+                 : "Backward::copy+xfft:%.3f,zfft:%.3f,yfft:%.3f,igrid:%.3f ms\n", t[0], t[1], t[2], t[3]);
+    else
+      printf(one ? "Forward::grid:%.3f,xfft:%.3f,yfft:%.3f,zfft+accumulate:%.3f ms\n"
+                 : "Forward::grid:%.3f,yfft:%.3f,zfft:%.3f,xfft+accumulate:%.3f ms\n", t[0], t[1], t[2], t[3]);
   }
 }
 
@@ -213,8 +218,13 @@ static mrg_status run_E(mrg_plan *p, const FrameTraj &ft, const float2 *X, const
   return MRG_OK;
 }
 
-// E up to the oversampled grid: set_image + z FFT, y FFT, x FFT (src/gridFFT.cpp:645-671, :972-986).
-static mrg_status run_E_grid(mrg_plan *p, const float2 *X, const float2 *smap, cudaStream_t st) {
+// E up to the oversampled grid: set_image + x FFT, z FFT, y FFT (src/gridFFT.cpp:645-671, :972-986).
+// Single-coil plans keep the reference's pass order (E: z, y, x; E^H: x, y, z): with one
+// coil the z lines of neighbouring x are adjacent in memory, so the image-side passes
+// (set_image, accumulate) on z lines are coalesced.  With coils innermost it is the x lines
+// that hold contiguous images and maps, so multi-coil plans run E as x, z, y and E^H as
+// y, z, x (run_E_grid, run_EH_yz, run_EH, run_EH_crop further down).
+static mrg_status run_E_grid_zxy(mrg_plan *p, const float2 *X, const float2 *smap, cudaStream_t st) {
   const Geometry &g = p->geo;
   const int C = p->C;
   const int64_t Nx = g.N[0], Ny = g.N[1], Nz = g.N[2], Sx = g.S[0], Sy = g.S[1], Sz = g.S[2];
@@ -300,7 +310,7 @@ static mrg_status run_EH_xy(mrg_plan *p, const FrameTraj &ft, const float2 *y, c
   return MRG_OK;
 }
 
-static mrg_status run_EH(mrg_plan *p, const FrameTraj &ft, const float2 *y, const float2 *smap, float2 *X,
+static mrg_status run_EH_xyz(mrg_plan *p, const FrameTraj &ft, const float2 *y, const float2 *smap, float2 *X,
                          cudaStream_t st) {
   const Geometry &g = p->geo;
   const int C = p->C;
@@ -328,7 +338,7 @@ static mrg_status run_EH(mrg_plan *p, const FrameTraj &ft, const float2 *y, cons
 
 // E^H without the coil sum: grid, the three inverse passes, and the z pass writes the
 // cropped volume t[Nz][Ny][Nx][C] (scaled, not deapodised) into d_t2.
-static mrg_status run_EH_crop(mrg_plan *p, const FrameTraj &ft, const float2 *y, cudaStream_t st) {
+static mrg_status run_EH_crop_xyz(mrg_plan *p, const FrameTraj &ft, const float2 *y, cudaStream_t st) {
   const Geometry &g = p->geo;
   const int C = p->C;
   const int64_t Nx = g.N[0], Ny = g.N[1], Nz = g.N[2], Sz = g.S[2];
@@ -341,6 +351,150 @@ static mrg_status run_EH_crop(mrg_plan *p, const FrameTraj &ft, const float2 *y,
   c.nlines = Ny * Nx * C;
   c.in_ls = Ny * Nx * C; c.in_os = Nx * C; c.out_ls = Ny * Nx * C; c.out_os = Nx * C;
   c.scale = (float)(1. / std::sqrt((float)Sz));
+  c.in = p->d_t1; c.out = p->d_t2; c.C = C;
+  fft_vectorize(c);
+  MRG_TRY(launch_fft(c, st));
+  tmark(p, 4, st);
+  tcollect(p, 4);
+  return MRG_OK;
+}
+
+static mrg_status run_E_grid(mrg_plan *p, const float2 *X, const float2 *smap, cudaStream_t st) {
+  if (p->C == 1) return run_E_grid_zxy(p, X, smap, st);
+  const Geometry &g = p->geo;
+  const int C = p->C;
+  const int64_t Nx = g.N[0], Ny = g.N[1], Nz = g.N[2], Sx = g.S[0], Sy = g.S[1], Sz = g.S[2];
+  const float *wx = p->d_win, *wy = p->d_win + Sx, *wz = p->d_win + Sx + Sy;
+  // The passes run x, z, y so that set_image works on lines along x, where X and the
+  // maps are contiguous: [Nz][Ny][Nx] -> t1 [Nz][Ny][Sx] -> t2 [Sz][Ny][Sx] -> grid [Sz][Sy][Sx].
+  FftPass a;
+  memset(&a, 0, sizeof(a));
+  // x pass with set_image (src/gridFFT.cpp:972-986 + fft3 along x), input pruned to the crop
+  a.S = (int)Sx; a.sign = -1; a.mode = FFT_SETIMG;
+  a.Lin = (int)Nx; a.in_off = g.og[0]; a.Lout = (int)Sx; a.out_off = 0;
+  a.inner = C; a.IB = plan_ib(p, 0, C, C, false); a.lfast = 0;
+  a.nlines = Nz * Ny * C;
+  a.in_ls = C; a.in_os = Nx * C; a.out_ls = C; a.out_os = Sx * C;
+  a.scale = (float)(1. / std::sqrt((float)Sx));
+  a.in = smap; a.smap = smap; a.has_smap = smap != nullptr; a.X = X; a.out = p->d_t1;
+  a.wmode = 1; a.wdiv = Ny; a.wl = wx + g.og[0]; a.wo = wz + g.og[2]; a.wi = wy + g.og[1]; a.C = C;
+  tmark(p, 0, st);
+  fft_vectorize(a);
+  MRG_TRY(launch_fft(a, st));
+  tmark(p, 1, st);
+  // z pass: t1 [Nz][Ny][Sx] -> t2 [Sz][Ny][Sx], input pruned to the crop
+  FftPass b;
+  memset(&b, 0, sizeof(b));
+  b.S = (int)Sz; b.sign = -1; b.mode = FFT_PLAIN;
+  b.Lin = (int)Nz; b.in_off = g.og[2]; b.Lout = (int)Sz; b.out_off = 0;
+  b.inner = (int)(Ny * Sx * C); b.IB = plan_ib(p, 1, b.inner, C, false);
+  b.nlines = Ny * Sx * C;
+  b.in_ls = Ny * Sx * C; b.in_os = 0; b.out_ls = Ny * Sx * C; b.out_os = 0;
+  b.scale = (float)(1. / std::sqrt((float)Sz));
+  b.in = p->d_t1; b.out = p->d_t2; b.C = C;
+  fft_vectorize(b);
+  MRG_TRY(launch_fft(b, st));
+  tmark(p, 2, st);
+  // y pass: t2 [Sz][Ny][Sx] -> grid [Sz][Sy][Sx]; the largest pass runs along y, whose rows
+  // lie Sx*C apart (z rows are a whole plane apart)
+  FftPass c;
+  memset(&c, 0, sizeof(c));
+  c.S = (int)Sy; c.sign = -1; c.mode = FFT_PLAIN;
+  c.Lin = (int)Ny; c.in_off = g.og[1]; c.Lout = (int)Sy; c.out_off = 0;
+  c.inner = (int)(Sx * C); c.IB = plan_ib(p, 2, c.inner, C, false);
+  c.nlines = Sz * Sx * C;
+  c.in_ls = Sx * C; c.in_os = Ny * Sx * C; c.out_ls = Sx * C; c.out_os = Sy * Sx * C;
+  c.scale = (float)(1. / std::sqrt((float)Sy));
+  c.in = p->d_t2; c.out = p->d_grid; c.C = C;
+  fft_vectorize(c);
+  MRG_TRY(launch_fft(c, st));
+  return MRG_OK;
+}
+
+// E^H up to the z transform: grid, then the y and z inverse passes (cropping y and z);
+// the result is t1 [Nz][Ny][Sx][C] in d_t1, so the last pass (x, cropped) can add into X
+// and read the maps along contiguous lines.
+static mrg_status run_EH_yz(mrg_plan *p, const FrameTraj &ft, const float2 *y, cudaStream_t st) {
+  const Geometry &g = p->geo;
+  const int C = p->C;
+  const int64_t Ny = g.N[1], Nz = g.N[2], Sx = g.S[0], Sy = g.S[1], Sz = g.S[2];
+  const GridConst gc = grid_const(p);
+  tmark(p, 0, st);
+  MRG_TRY(launch_grid(gc, ft, y, p->d_grid, st));  // src/gridFFT.cpp:1009-1164
+  tmark(p, 1, st);
+  // y pass: grid [Sz][Sy][Sx] -> t2 [Sz][Ny][Sx]
+  FftPass a;
+  memset(&a, 0, sizeof(a));
+  a.S = (int)Sy; a.sign = +1; a.mode = FFT_PLAIN;
+  a.Lin = (int)Sy; a.in_off = 0; a.Lout = (int)Ny; a.out_off = g.og[1];
+  a.inner = (int)(Sx * C); a.IB = plan_ib(p, 3, a.inner, C, false);
+  a.nlines = Sz * Sx * C;
+  a.in_ls = Sx * C; a.in_os = Sy * Sx * C; a.out_ls = Sx * C; a.out_os = Ny * Sx * C;
+  a.scale = (float)(1. / std::sqrt((float)Sy));
+  a.in = p->d_grid; a.out = p->d_t2; a.C = C;
+  fft_vectorize(a);
+  MRG_TRY(launch_fft(a, st));
+  tmark(p, 2, st);
+  // z pass: t2 [Sz][Ny][Sx] -> t1 [Nz][Ny][Sx]
+  FftPass b;
+  memset(&b, 0, sizeof(b));
+  b.S = (int)Sz; b.sign = +1; b.mode = FFT_PLAIN;
+  b.Lin = (int)Sz; b.in_off = 0; b.Lout = (int)Nz; b.out_off = g.og[2];
+  b.inner = (int)(Ny * Sx * C); b.IB = plan_ib(p, 4, b.inner, C, false);
+  b.nlines = Ny * Sx * C;
+  b.in_ls = Ny * Sx * C; b.in_os = 0; b.out_ls = Ny * Sx * C; b.out_os = 0;
+  b.scale = (float)(1. / std::sqrt((float)Sz));
+  b.in = p->d_t2; b.out = p->d_t1; b.C = C;
+  fft_vectorize(b);
+  MRG_TRY(launch_fft(b, st));
+  tmark(p, 3, st);
+  return MRG_OK;
+}
+
+static mrg_status run_EH(mrg_plan *p, const FrameTraj &ft, const float2 *y, const float2 *smap, float2 *X,
+                         cudaStream_t st) {
+  if (p->C == 1) return run_EH_xyz(p, ft, y, smap, X, st);
+  const Geometry &g = p->geo;
+  const int C = p->C;
+  const int64_t Nx = g.N[0], Ny = g.N[1], Nz = g.N[2], Sx = g.S[0], Sy = g.S[1];
+  const float *wx = p->d_win, *wy = p->d_win + Sx, *wz = p->d_win + Sx + Sy;
+  MRG_TRY(run_EH_yz(p, ft, y, st));
+  // x pass with accumulate (src/gridFFT.cpp:926-941): X[z][y][x] += sum_c ..., rows of X
+  // written along x
+  FftPass c;
+  memset(&c, 0, sizeof(c));
+  c.S = (int)Sx; c.sign = +1; c.mode = FFT_ACCUM;
+  c.Lin = (int)Sx; c.in_off = 0; c.Lout = (int)Nx; c.out_off = g.og[0];
+  c.inner = C; c.IB = plan_ib(p, 5, C, C, true);
+  c.nlines = Nz * Ny * C;
+  c.in_ls = C; c.in_os = Sx * C; c.out_ls = C; c.out_os = Nx * C;
+  c.scale = (float)(1. / std::sqrt((float)Sx));
+  c.in = p->d_t1; c.smap = smap; c.has_smap = smap != nullptr; c.acc = X;
+  c.acc_atomic = (c.IB % C) != 0; c.acc_l = 1; c.acc_o = Nx;
+  c.wmode = 1; c.wdiv = Ny; c.wl = wx + g.og[0]; c.wo = wz + g.og[2]; c.wi = wy + g.og[1]; c.C = C;
+  fft_vectorize(c);
+  MRG_TRY(launch_fft(c, st));
+  tmark(p, 4, st);
+  tcollect(p, 4);
+  return MRG_OK;
+}
+
+// E^H without the coil sum: grid, the three inverse passes, and the x pass writes the
+// cropped volume t[Nz][Ny][Nx][C] (scaled, not deapodised) into d_t2.
+static mrg_status run_EH_crop(mrg_plan *p, const FrameTraj &ft, const float2 *y, cudaStream_t st) {
+  if (p->C == 1) return run_EH_crop_xyz(p, ft, y, st);
+  const Geometry &g = p->geo;
+  const int C = p->C;
+  const int64_t Nx = g.N[0], Ny = g.N[1], Nz = g.N[2], Sx = g.S[0];
+  MRG_TRY(run_EH_yz(p, ft, y, st));
+  FftPass c;
+  memset(&c, 0, sizeof(c));
+  c.S = (int)Sx; c.sign = +1; c.mode = FFT_PLAIN;
+  c.Lin = (int)Sx; c.in_off = 0; c.Lout = (int)Nx; c.out_off = g.og[0];
+  c.inner = C; c.IB = (C == 1) ? pass_ib(C, C) : plan_ib(p, 5, C, C, false); c.lfast = (C == 1);
+  c.nlines = Nz * Ny * C;
+  c.in_ls = C; c.in_os = Sx * C; c.out_ls = C; c.out_os = Nx * C;
+  c.scale = (float)(1. / std::sqrt((float)Sx));
   c.in = p->d_t1; c.out = p->d_t2; c.C = C;
   fft_vectorize(c);
   MRG_TRY(launch_fft(c, st));
@@ -475,8 +629,10 @@ mrg_status mrg_plan_create(const mrg_config *cfg_in, int Nx, int Ny, int Nz, int
   p->frames.resize(nframes);
   mrg_status rs = fft_init_device();
   const int64_t S3 = (int64_t)p->geo.S[0] * p->geo.S[1] * p->geo.S[2];
-  const int64_t t2n = (int64_t)Nx * p->geo.S[1] * p->geo.S[2];
-  const int64_t t1n = (int64_t)Nx * Ny * p->geo.S[2];
+  // E runs x, z, y (and E^H y, z, x): t1 = [Nz][Ny][Sx][C], t2 = [Sz][Ny][Sx][C]; one coil
+  // keeps the z, y, x order: t1 = [Sz][Ny][Nx], t2 = [Sz][Sy][Nx]
+  const int64_t t2n = std::max((int64_t)p->geo.S[2] * Ny * p->geo.S[0], (int64_t)Nx * p->geo.S[1] * p->geo.S[2]);
+  const int64_t t1n = std::max((int64_t)Nz * Ny * p->geo.S[0], (int64_t)Nx * Ny * p->geo.S[2]);
   auto fail = [&](mrg_status s) {
     mrg_plan_destroy(p);
     return s;
@@ -616,6 +772,7 @@ mrg_status mrg_set_traj(mrg_plan *p, int frame, const float *kx, const float *ky
       ft.ungrid_G = p->tuned_G;
       ft.ungrid_spb = p->tuned_spb;
       ft.ungrid_cpl = p->tuned_cpl;
+      ft.ungrid_uy = p->tuned_uy;
       ft.grid_cc = p->tuned_cc;
       ft.tune_ungrid_ms = p->tuned_ms[0];
       ft.tune_grid_ms = p->tuned_ms[1];
@@ -625,6 +782,7 @@ mrg_status mrg_set_traj(mrg_plan *p, int frame, const float *kx, const float *ky
       p->tuned_G = ft.ungrid_G;
       p->tuned_spb = ft.ungrid_spb;
       p->tuned_cpl = ft.ungrid_cpl;
+      p->tuned_uy = ft.ungrid_uy;
       p->tuned_cc = ft.grid_cc;
       p->tuned = true;
       p->tuned_nvalid = nv;
@@ -646,7 +804,7 @@ mrg_status mrg_frame_info(const mrg_plan *p, int frame, int64_t *M, int64_t *nva
   return MRG_OK;
 }
 
-mrg_status mrg_frame_tuning(const mrg_plan *p, int frame, int out[4], float ms[2]) {
+mrg_status mrg_frame_tuning(const mrg_plan *p, int frame, int out[5], float ms[2]) {
   MRG_TRY(check_frame(p, frame));
   const FrameTraj &ft = p->frames[frame];
   if (out) {
@@ -654,6 +812,7 @@ mrg_status mrg_frame_tuning(const mrg_plan *p, int frame, int out[4], float ms[2
     out[1] = ft.ungrid_spb;
     out[2] = ft.grid_cc;
     out[3] = ft.ungrid_cpl;
+    out[4] = ft.ungrid_uy;
   }
   if (ms) {
     ms[0] = ft.tune_ungrid_ms;

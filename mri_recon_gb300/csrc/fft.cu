@@ -136,6 +136,18 @@ __device__ __forceinline__ void reg_fft(float2 (&v)[Q], const float2 *tw) {
   }
 }
 
+// Deapodisation weight of element l of line (o, i), the reference's (winz * winy) * winx
+// (src/gridFFT.cpp:972-986, :926-941): per-line factor `lw` from line_weight, then
+// elem_weight for the element.
+__device__ __forceinline__ float line_weight(const FftPass &p, int64_t o, int64_t i) {
+  if (p.wmode) return p.wo[o / p.wdiv] * p.wi[o % p.wdiv];  // winz * winy of the line's row
+  return 0.0f;
+}
+__device__ __forceinline__ float elem_weight(const FftPass &p, float lw, float wl_l, int64_t o, int64_t i) {
+  if (p.wmode) return lw * wl_l;                  // (winz * winy) * winx
+  return (wl_l * p.wo[o]) * p.wi[i / p.C];         // (winz * winy) * winx along z
+}
+
 template <int Q, int SIGN, int MODE>
 __global__ void __launch_bounds__(256, 2) k_fft(const FftPass p) {
   constexpr int S = 8 * Q;
@@ -188,8 +200,7 @@ __global__ void __launch_bounds__(256, 2) k_fft(const FftPass p) {
       // image = (winz*winy)*winx * X * smap  (src/gridFFT.cpp:972-986); smap already in smem
       if (lv) {
         const int64_t ib = o * p.in_os + i;
-        const float wyx_o = p.wo[o];
-        const float wxi = p.wi[i / p.C];
+        const float lw = line_weight(p, o, i);
         const int64_t xb = ib / p.C, xs = p.in_ls / p.C;  // X has no coil axis
         for (int l0 = t; l0 < p.Lin; l0 += 64) {
           float2 xv[8];
@@ -206,7 +217,7 @@ __global__ void __launch_bounds__(256, 2) k_fft(const FftPass p) {
           for (int k = 0; k < 8; k++) {
             const int li = l0 + 8 * k;
             if (li < p.Lin) {
-              const float w = (wv[k] * wyx_o) * wxi;
+              const float w = elem_weight(p, lw, wv[k], o, i);
               float2 *d = sm + (li + p.in_off) * IBp + j;
               *d = cmul(make_float2(w * xv[k].x, w * xv[k].y), *d);
             }
@@ -224,7 +235,7 @@ __global__ void __launch_bounds__(256, 2) k_fft(const FftPass p) {
         const int64_t off = ib + (int64_t)li * p.in_ls;
         if constexpr (MODE == FFT_SETIMG) {
           const int64_t vox = off / p.C;
-          const float w = (p.wl[li] * p.wo[o]) * p.wi[i / p.C];
+          const float w = elem_weight(p, line_weight(p, o, i), p.wl[li], o, i);
           const float2 x = p.X[vox];
           v = make_float2(w * x.x, w * x.y);
           if (p.has_smap) v = cmul(v, p.smap[off]);
@@ -314,6 +325,7 @@ __global__ void __launch_bounds__(256, 2) k_fft(const FftPass p) {
     const int C = p.C;
     if (lv) {
       const int64_t sb = o * p.out_os + i;
+      const float lw = line_weight(p, o, i);
       for (int r0 = t; r0 < p.Lout; r0 += 64) {
         float2 sv[8];
         float wv[8];
@@ -331,7 +343,7 @@ __global__ void __launch_bounds__(256, 2) k_fft(const FftPass p) {
           if (r >= p.Lout) continue;
           float2 v = sm[(r + p.out_off) * IBp + j];
           v = make_float2(v.x * p.scale, v.y * p.scale);
-          const float w = (wv[k] * p.wo[o]) * p.wi[i / C];
+          const float w = elem_weight(p, lw, wv[k], o, i);
           v = make_float2(w * v.x, w * v.y);
           if (p.has_smap) {
             float2 s2 = sv[k];
@@ -358,8 +370,15 @@ __global__ void __launch_bounds__(256, 2) k_fft(const FftPass p) {
         const int64_t ln = line0 + (int64_t)g * C;
         if (ln >= p.nlines) continue;
         const int64_t oo = ln / p.inner, ii = ln - oo * p.inner;
+        // rotated start (coil (c + r) mod C at step c): the rows of neighbouring threads sit
+        // IBp apart, a multiple of the 32 banks, so the same coil index would hit one bank
         float2 s = make_float2(0.f, 0.f);
-        for (int c = 0; c < C; c++) s = cadd(s, sm[(r + p.out_off) * IBp + g * C + c]);
+        const float2 *row = sm + (r + p.out_off) * IBp + g * C;
+        int cc = r % C;
+        for (int c = 0; c < C; c++) {
+          s = cadd(s, row[cc]);
+          cc = (cc + 1 == C) ? 0 : cc + 1;
+        }
         float2 *dst = p.acc + (int64_t)r * p.acc_l + oo * p.acc_o + ii / C;
         float2 cur = *dst;
         *dst = cadd(cur, s);

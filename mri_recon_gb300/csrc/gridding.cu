@@ -375,11 +375,39 @@ mrg_status traj_setup(const GridConst &gc, FrameTraj &ft, const float *kx, const
 // neighbouring samples.  The sum is taken separably, x taps first:
 //   y = sum_z wz sum_y wy sum_x wx g,
 // which needs one multiply-add per tap and coil instead of forming every 3D weight.
-template <int G, int CPL>
+template <int CPL>
+struct UngridVec;
+template <>
+struct UngridVec<1> {
+  typedef float2 T;
+  static __device__ __forceinline__ T zero() { return make_float2(0.f, 0.f); }
+  static __device__ __forceinline__ void fma(float *ar, float w, T v) {
+    ar[0] += w * v.x;
+    ar[1] += w * v.y;
+  }
+};
+template <>
+struct UngridVec<2> {
+  typedef float4 T;
+  static __device__ __forceinline__ T zero() { return make_float4(0.f, 0.f, 0.f, 0.f); }
+  static __device__ __forceinline__ void fma(float *ar, float w, T v) {
+    ar[0] += w * v.x;
+    ar[1] += w * v.y;
+    ar[2] += w * v.z;
+    ar[3] += w * v.w;
+  }
+};
+
+// UY rows of taps are loaded before any of them is summed, so up to 6 * UY gathers per
+// lane are in flight (the kernel is bound by the latency of these L1 gathers).  Taps
+// beyond a sample's counts load zero and carry zero weights (the tables are padded).
+template <int G, int CPL, int UY>
 __global__ void __launch_bounds__(256) k_ungrid(const GridConst g, int nvalid, int spb, const float4 *__restrict__ swt,
                                                const int4 *__restrict__ sst, const float4 *__restrict__ spos,
                                                const float *__restrict__ stap, const float2 *__restrict__ grid,
                                                const float2 *__restrict__ diff, float2 *__restrict__ y, int weigh) {
+  typedef UngridVec<CPL> V;
+  typedef typename V::T VT;
   constexpr int GPB = 256 / G;  // sample groups per CTA
   const int lane = threadIdx.x % G, grp = threadIdx.x / G;
   const int C = g.C;
@@ -402,30 +430,26 @@ __global__ void __launch_bounds__(256) k_ungrid(const GridConst g, int nvalid, i
       float az[2 * CPL];
 #pragma unroll
       for (int k = 0; k < 2 * CPL; k++) az[k] = 0.f;
-      for (int ky = 0; ky < ny; ky++) {
-        const float2 *row = base + kz * zs + ky * ys;
-        float ar[2 * CPL];
+      for (int ky0 = 0; ky0 < ny; ky0 += UY) {
+        VT v[UY][6];
 #pragma unroll
-        for (int k = 0; k < 2 * CPL; k++) ar[k] = 0.f;
+        for (int u = 0; u < UY; u++) {
+          const float2 *row = base + kz * zs + (ky0 + u) * ys;
 #pragma unroll
-        for (int a = 0; a < 6; a++) {
-          if (a < nx) {
-            if (CPL == 2) {
-              const float4 v = __ldg(reinterpret_cast<const float4 *>(row + (int64_t)a * C));
-              ar[0] += wx[a] * v.x;
-              ar[1] += wx[a] * v.y;
-              ar[2] += wx[a] * v.z;
-              ar[3] += wx[a] * v.w;
-            } else {
-              const float2 v = __ldg(row + (int64_t)a * C);
-              ar[0] += wx[a] * v.x;
-              ar[1] += wx[a] * v.y;
-            }
-          }
+          for (int a = 0; a < 6; a++)
+            v[u][a] = (ky0 + u < ny && a < nx) ? __ldg(reinterpret_cast<const VT *>(row + (int64_t)a * C)) : V::zero();
         }
-        const float wyv = __ldg(w + 8 + ky);
 #pragma unroll
-        for (int k = 0; k < 2 * CPL; k++) az[k] += wyv * ar[k];
+        for (int u = 0; u < UY; u++) {
+          float ar[2 * CPL];
+#pragma unroll
+          for (int k = 0; k < 2 * CPL; k++) ar[k] = 0.f;
+#pragma unroll
+          for (int a = 0; a < 6; a++) V::fma(ar, wx[a], v[u][a]);
+          const float wyv = (ky0 + u < ny) ? __ldg(w + 8 + ky0 + u) : 0.f;
+#pragma unroll
+          for (int k = 0; k < 2 * CPL; k++) az[k] += wyv * ar[k];
+        }
       }
       const float wzv = __ldg(w + 16 + kz);
 #pragma unroll
@@ -467,27 +491,41 @@ mrg_status launch_ungrid(const GridConst &gc, const FrameTraj &ft, const float2 
   int cpl = (ft.ungrid_cpl > 0) ? ft.ungrid_cpl : ((gc.C % 2 == 0) ? 2 : 1);
   if (gc.C % 2 != 0 || ((uintptr_t)grid & 15) != 0) cpl = 1;
   const int spb = ft.ungrid_spb > 0 ? ft.ungrid_spb : 256;
+  const int uy = ft.ungrid_uy > 0 ? ft.ungrid_uy : 1;
   const int chunk = G * cpl;
   const dim3 blocks((unsigned)((ft.nvalid + spb - 1) / spb), (unsigned)((gc.C + chunk - 1) / chunk));
   const int wf = weigh ? 1 : 0;
 #define UNGRID_ARGS gc, ft.nvalid, spb, ft.swt, ft.sst, ft.spos, ft.stap, grid, diff, y, wf
+#define UNGRID_UY(GG, PP)                                                         \
+  switch (uy) {                                                                   \
+    case 2: k_ungrid<GG, PP, 2><<<blocks, 256, 0, st>>>(UNGRID_ARGS); break;      \
+    case 3: k_ungrid<GG, PP, 3><<<blocks, 256, 0, st>>>(UNGRID_ARGS); break;      \
+    default: k_ungrid<GG, PP, 1><<<blocks, 256, 0, st>>>(UNGRID_ARGS); break;     \
+  }
 #define UNGRID_CASE(GG)                                                           \
   case GG:                                                                        \
-    if (cpl == 2) k_ungrid<GG, 2><<<blocks, 256, 0, st>>>(UNGRID_ARGS);           \
-    else k_ungrid<GG, 1><<<blocks, 256, 0, st>>>(UNGRID_ARGS);                    \
+    if (cpl == 2) { UNGRID_UY(GG, 2) }                                            \
+    else { UNGRID_UY(GG, 1) }                                                     \
     break;
   switch (G) {
-    UNGRID_CASE(1)
-    UNGRID_CASE(2)
+    case 1:
+      if (cpl == 2) k_ungrid<1, 2, 1><<<blocks, 256, 0, st>>>(UNGRID_ARGS);
+      else k_ungrid<1, 1, 1><<<blocks, 256, 0, st>>>(UNGRID_ARGS);
+      break;
+    case 2:
+      if (cpl == 2) k_ungrid<2, 2, 1><<<blocks, 256, 0, st>>>(UNGRID_ARGS);
+      else k_ungrid<2, 1, 1><<<blocks, 256, 0, st>>>(UNGRID_ARGS);
+      break;
     UNGRID_CASE(4)
     UNGRID_CASE(8)
     UNGRID_CASE(16)
     default:
-      if (cpl == 2) k_ungrid<32, 2><<<blocks, 256, 0, st>>>(UNGRID_ARGS);
-      else k_ungrid<32, 1><<<blocks, 256, 0, st>>>(UNGRID_ARGS);
+      if (cpl == 2) { UNGRID_UY(32, 2) }
+      else { UNGRID_UY(32, 1) }
       break;
   }
 #undef UNGRID_CASE
+#undef UNGRID_UY
 #undef UNGRID_ARGS
   MRG_LAUNCHED();
   return MRG_OK;
@@ -1143,6 +1181,7 @@ mrg_status autotune_frame(const GridConst &gc, FrameTraj &ft, float2 *grid, floa
         ft.ungrid_G = G;
         ft.ungrid_spb = spb;
         ft.ungrid_cpl = cpl;
+        ft.ungrid_uy = 1;
         const float ms = time_ms(st, [&]() { return launch_ungrid(gc, ft, grid, nullptr, y, false, st); }, 2);
         if (ms < best) {
           best = ms;
@@ -1156,6 +1195,19 @@ mrg_status autotune_frame(const GridConst &gc, FrameTraj &ft, float2 *grid, floa
   ft.ungrid_G = bestG;
   ft.ungrid_spb = bestS;
   ft.ungrid_cpl = bestP;
+  ft.ungrid_uy = 1;
+  int bestU = 1;
+  if (bestG >= 4) {
+    for (int uy : {2, 3}) {
+      ft.ungrid_uy = uy;
+      const float ms = time_ms(st, [&]() { return launch_ungrid(gc, ft, grid, nullptr, y, false, st); }, 2);
+      if (ms < best) {
+        best = ms;
+        bestU = uy;
+      }
+    }
+  }
+  ft.ungrid_uy = bestU;
   ft.tune_ungrid_ms = best;
   best = 1e30f;
   int bestCC = 0;

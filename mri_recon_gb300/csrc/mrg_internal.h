@@ -87,12 +87,17 @@ struct FftPass {
   const float2 *in;
   float2 *out;
   const float2 *tw;  // set by launch_fft: exp(-2 pi i m / S)
-  // FFT_SETIMG: v = (wl[l]*wo[o])*wi[i/C] * X[off/C] * in[off]  (in = smap or NULL)
-  // FFT_ACCUM : acc[(l*No + o)*Ni + i/C] += sum_c (wl*wo*wi)*v*conj(smap[...])
+  // FFT_SETIMG: v = w(l, o, i) * X[off/C] * in[off]  (in = smap or NULL)
+  // FFT_ACCUM : acc[l*acc_l + o*acc_o + i/C] += sum_c w(l, o, i)*v*conj(smap[...])
+  // w: wmode 0 (lines along z, o = y, i/C = x): (wl[l] * wo[o]) * wi[i/C]
+  //    wmode 1 (lines along x, o = z*wdiv + y):  (wo[o / wdiv] * wi[o % wdiv]) * wl[l]
+  // both the reference's (winz * winy) * winx
   const float2 *X;
   const float2 *smap;
   float2 *acc;
   const float *wl, *wo, *wi;
+  int wmode;
+  int64_t wdiv;
   int C, has_smap;
   int acc_atomic;
   int64_t acc_l, acc_o;  // accumulator strides for l and o (i/C has stride 1)
@@ -144,7 +149,7 @@ struct FrameTraj {
   float4 *sdw = nullptr;      // [nvalid][6] d(tap weight)/dk per axis (allocated by mrg_grad)
   bool has_data = false;
   // launch shapes picked by autotune_frame (0: defaults)
-  int ungrid_G = 0, ungrid_spb = 0, ungrid_cpl = 0, grid_cc = 0;
+  int ungrid_G = 0, ungrid_spb = 0, ungrid_cpl = 0, ungrid_uy = 0, grid_cc = 0;
   float tune_ungrid_ms = 0.f, tune_grid_ms = 0.f;
 };
 
@@ -161,6 +166,9 @@ mrg_status launch_sos_images(const float2 *t, int C, const int N[3], const float
 mrg_status gaussian_blur_ex(float2 *X, int nvol, const int N[3], int64_t es, int64_t vs, const float sigma[3],
                             cudaStream_t st);
 mrg_status sos_normalize_ex(float2 *A, int C, int64_t nimg, int64_t es, int64_t vs, cudaStream_t st);
+// Pipe density compensation on device trajectories (dcf.cu)
+mrg_status dcf_pipe(const float *kx, const float *ky, const float *kz, int64_t M, const int N[3], int iters,
+                    float dwin, float scale, float overgrid, float acc, int kernel, float *kw, cudaStream_t st);
 // y[s][c] = sum over taps of grid (gridFFT::chop_grid_backward), minus diff[s][c] if given;
 // with `weigh` the result is multiplied by kw and the taper, ready for launch_grid.
 mrg_status launch_ungrid(const GridConst &gc, const FrameTraj &ft, const float2 *grid, const float2 *diff,

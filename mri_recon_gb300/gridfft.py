@@ -138,11 +138,11 @@ class Plan:
         return dict(zip(("M", "nvalid", "npairs", "nitems"), (x.value for x in v)))
 
     def frame_tuning(self, frame):
-        out = (ctypes.c_int * 4)()
+        out = (ctypes.c_int * 5)()
         ms = (ctypes.c_float * 2)()
         _lib.check(_lib.load().mrg_frame_tuning(self._h, frame, out, ms))
         return dict(ungrid_lanes=out[0], ungrid_samples_per_cta=out[1], grid_coils_per_pass=out[2],
-                    ungrid_coils_per_lane=out[3], ungrid_ms=ms[0], grid_ms=ms[1])
+                    ungrid_coils_per_lane=out[3], ungrid_rows_per_step=out[4], ungrid_ms=ms[0], grid_ms=ms[1])
 
     def set_data(self, frame, data, stream=None):
         """data: (C, M) complex64."""
@@ -356,6 +356,28 @@ def sos_normalize(maps, stream=None):
     n = _numel(maps) // C
     _lib.check(_lib.load().mrg_sos_normalize(a.ptr(maps), C, n, n, _stream(stream)))
     return maps
+
+
+def dcf_pipe(kx, ky, kz, N, stream=None, **params):
+    """Pipe density compensation (RECON::dcf_calc) for one encode's trajectory; returns kw
+    (a device tensor for device input, numpy otherwise).  params: iters, dwin, scale,
+    overgrid, acc, kernel (the reference's -dcf_* flags)."""
+    a = _Args()
+    if np.isscalar(N):
+        N = (N, N, N)
+    q = _lib.MrgDcfParams()
+    _lib.load().mrg_dcf_params_default(ctypes.byref(q))
+    for k, v in params.items():
+        setattr(q, k, v)
+    M = _numel(kx)
+    if _is_tensor(kx) and kx.is_cuda:
+        out = torch.empty(M, dtype=torch.float32, device=kx.device)
+    else:
+        out = np.zeros(M, np.float32)
+    _lib.check(_lib.load().mrg_dcf_pipe(a.ptr(kx, np.float32), a.ptr(ky, np.float32), a.ptr(kz, np.float32), M,
+                                        int(N[0]), int(N[1]), int(N[2]), ctypes.byref(q), a.ptr(out),
+                                        _stream(stream)))
+    return out
 
 
 def fista_params(**kw):

@@ -509,6 +509,133 @@ static void sos_normalize(cx<R> **A, int C, long n) {
 }
 
 // ---------------------------------------------------------------------------
+// Pipe density compensation: RECON::dcf_calc (recon_lib.cpp:854-917) with
+// DCFgridFFT (DCFgridFFT.cpp): starting from Kw = 1, `iters` rounds of
+//   X = G Kw (real gridding, forward :174-277), Kw2 = G^T X (backward :323-437),
+//   Kw = |Kw2| < 1e-3 ? 0 : Kw / Kw2,
+// then Kw *= scale^3 (scale_kw :297-321) and Kw = |Kw|.  G uses the polynomial
+// kernel table (loadKernelTable :47-66 / loadKernelTable2 :68-84, normalised to
+// sum 0.5*600 :150-152) on a real grid of (int)(overgrid*N + 16) points per axis,
+// without the chop sign, taps ceil(dk - s*dwin) .. floor(dk + s*dwin) clipped,
+// s = |k|/128*(acc - 1) + 1.
+// ---------------------------------------------------------------------------
+struct ODcfParams {
+  int iters;
+  float dwin, scale, overgrid, acc;
+  int kernel;  // 0 POLY_KERNEL, 1 POLY_KERNEL2
+};
+
+static void dcf_table(float dwin, int kernel, std::vector<float> &t) {
+  const int len = (int)((float)dwin * 600.0f) + 100;
+  t.assign(len, 0.0f);
+  static const double c[2][6] = {{1., 0.04522831, -3.36020304, 1.12417012, 2.82448025, -1.63447764},
+                                 {1., 0.03056504, -3.01961845, 0.6679865, 2.77924058, -1.45923643}};
+  const double *k = c[kernel ? 1 : 0];
+  for (int i = 0; i < len; i++) {
+    const double x = double(i) / double(len), x2 = x * x, x4 = x2 * x2, x3 = x * x2, x5 = x * x4;
+    t[i] = (float)(k[0] + k[1] * x + k[2] * x2 + k[3] * x3 + k[4] * x4 + k[5] * x5);
+  }
+  double sum = 0;
+  for (int i = 0; i < len; i++) sum += t[i];
+  const double f = 0.5 * 600.0f / sum;
+  for (int i = 0; i < len; i++) t[i] = (float)(t[i] * f);
+}
+
+template <typename R>
+struct DcfTaps {
+  int s[3], e[3];
+  float dk[3], sc;
+  bool ok;
+};
+
+template <typename R>
+static DcfTaps<R> dcf_taps(float kx, float ky, float kz, const int *S, float og, float dwin, float acc) {
+  DcfTaps<R> t;
+  const float kr = std::sqrt(kx * kx + ky * ky + kz * kz);
+  t.sc = (float)(kr / 128.0 * (acc - 1) + 1);
+  const float k[3] = {kx, ky, kz};
+  t.ok = true;
+  for (int d = 0; d < 3; d++) {
+    const float c = (float)(S[d] / 2);
+    t.dk[d] = k[d] * og + c;
+    t.s[d] = std::max((int)std::ceil(t.dk[d] - t.sc * dwin), 0);
+    t.e[d] = std::min((int)std::floor(t.dk[d] + t.sc * dwin), S[d] - 1);
+    if (t.s[d] >= S[d] || t.e[d] < 0) t.ok = false;
+  }
+  return t;
+}
+
+// one axis weight: lut((int)del)*(1 - d) + lut((int)del + 1)*d in double (1.0 is a double)
+static inline double dcf_w(const std::vector<float> &lut, float dk, int l, float sc) {
+  const float del = std::fabs(600.0f * (dk - (float)l)) / sc;
+  const float d = del - (float)((int)del);
+  return lut[(int)del] * (1.0 - d) + lut[(int)del + 1] * d;
+}
+
+template <typename R>
+static void dcf_pipe(const float *kx0, const float *ky0, const float *kz0, long M, const int *N, const ODcfParams &q,
+                     float *kw_out) {
+  std::vector<float> lut;
+  dcf_table(q.dwin, q.kernel, lut);
+  int S[3];
+  for (int d = 0; d < 3; d++) S[d] = (int)(q.overgrid * N[d] + 16);
+  std::vector<float> kx(M), ky(M), kz(M);
+  for (long i = 0; i < M; i++) {
+    kx[i] = kx0[i] * q.scale;
+    ky[i] = ky0[i] * q.scale;
+    kz[i] = kz0[i] * q.scale;
+  }
+  std::vector<R> X((size_t)S[0] * S[1] * S[2]);
+  std::vector<R> kw(M, (R)1), kw2(M);
+  for (int it = 0; it < q.iters; it++) {
+    std::fill(X.begin(), X.end(), (R)0);
+    // forward (DCFgridFFT.cpp:174-277): X += w * Kw
+    for (long i = 0; i < M; i++) {
+      if (kw[i] == (R)0) continue;
+      const DcfTaps<R> t = dcf_taps<R>(kx[i], ky[i], kz[i], S, q.overgrid, q.dwin, q.acc);
+      if (!t.ok) continue;
+      for (int lz = t.s[2]; lz <= t.e[2]; lz++) {
+        const R wtz = (R)dcf_w(lut, t.dk[2], lz, t.sc);
+        for (int ly = t.s[1]; ly <= t.e[1]; ly++) {
+          const R wty = (R)(wtz * dcf_w(lut, t.dk[1], ly, t.sc));
+          for (int lx = t.s[0]; lx <= t.e[0]; lx++) {
+            const R wtx = (R)(wty * dcf_w(lut, t.dk[0], lx, t.sc));
+            X[(size_t)lx + (size_t)S[0] * (ly + (size_t)S[1] * lz)] += wtx * kw[i];
+          }
+        }
+      }
+    }
+    // backward (DCFgridFFT.cpp:323-437): Kw2 = sum w * X
+#pragma omp parallel for
+    for (long i = 0; i < M; i++) {
+      kw2[i] = 0;
+      const DcfTaps<R> t = dcf_taps<R>(kx[i], ky[i], kz[i], S, q.overgrid, q.dwin, q.acc);
+      if (!t.ok) continue;
+      R acc = 0;
+      for (int lz = t.s[2]; lz <= t.e[2]; lz++) {
+        const R wtz = (R)dcf_w(lut, t.dk[2], lz, t.sc);
+        for (int ly = t.s[1]; ly <= t.e[1]; ly++) {
+          const R wty = (R)(wtz * dcf_w(lut, t.dk[1], ly, t.sc));
+          for (int lx = t.s[0]; lx <= t.e[0]; lx++) {
+            const R wtx = (R)(wty * dcf_w(lut, t.dk[0], lx, t.sc));
+            acc += wtx * X[(size_t)lx + (size_t)S[0] * (ly + (size_t)S[1] * lz)];
+          }
+        }
+      }
+      kw2[i] = acc;
+    }
+    // update (recon_lib.cpp:895-905)
+    for (long i = 0; i < M; i++) kw[i] = (std::fabs(kw2[i]) < (R)1e-3) ? (R)0 : kw[i] / kw2[i];
+  }
+  // scale_kw (DCFgridFFT.cpp:297-321) and |Kw|
+  for (long i = 0; i < M; i++) {
+    const float kr = std::sqrt(kx[i] * kx[i] + ky[i] * ky[i] + kz[i] * kz[i]);
+    const float sc = (float)(kr / 128.0 * (q.acc - 1) + 1);
+    kw_out[i] = (float)std::fabs((R)(kw[i] * std::pow(sc, 3)));
+  }
+}
+
+// ---------------------------------------------------------------------------
 // glibc random() TYPE_3 stream for the default seed (the additive lagged
 // Fibonacci generator r[i] = r[i-3] + r[i-31], output r >> 1, seeded by the
 // Park-Miller LCG).  The reference draws its wavelet and block shifts from
@@ -1195,6 +1322,18 @@ void orc_llr_thresh(void **X, int Nt, const int *N, const int *bs, int block_ite
   for (long i = 0; i < rand_skip; i++) rng.step();
   if (prec) llr_thresh<double>((cx<double> **)X, Nt, N, p, smax, rng);
   else llr_thresh<float>((cx<float> **)X, Nt, N, p, smax, rng);
+}
+void orc_dcf_pipe(const float *kx, const float *ky, const float *kz, long M, int Nx, int Ny, int Nz,
+                  const ODcfParams *q, float *kw, int prec) {
+  const int N[3] = {Nx, Ny, Nz};
+  if (prec) dcf_pipe<double>(kx, ky, kz, M, N, *q, kw);
+  else dcf_pipe<float>(kx, ky, kz, M, N, *q, kw);
+}
+void orc_dcf_table(float dwin, int kernel, float *out, int *len) {
+  std::vector<float> t;
+  dcf_table(dwin, kernel, t);
+  if (out) std::memcpy(out, t.data(), 4 * t.size());
+  *len = (int)t.size();
 }
 void orc_glibc_rand(long skip, int n, int *out) {
   GRand rng(1);

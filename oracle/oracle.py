@@ -47,6 +47,9 @@ def lib():
         L.orc_set_k_rad.argtypes = [vp, ctypes.c_float]
         L.orc_gaussian_blur.argtypes = [vp] + [ctypes.c_int] * 3 + [fp, ctypes.c_int]
         L.orc_sos_normalize.argtypes = [ctypes.POINTER(vp), ctypes.c_int, ctypes.c_long, ctypes.c_int]
+        L.orc_dcf_pipe.argtypes = [fp, fp, fp, ctypes.c_long, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, fp,
+                                   ctypes.c_int]
+        L.orc_dcf_table.argtypes = [ctypes.c_float, ctypes.c_int, fp, ip]
         L.orc_get_grid.argtypes = [vp, vp]
         L.orc_set_grid.argtypes = [vp, vp]
         L.orc_grid.argtypes = [vp, vp, fp, fp, fp, fp, ctypes.c_long]
@@ -374,6 +377,31 @@ def lowres_smaps(plan, data, kx, ky, kz, kw, smap_res=8.0, blur=(0.0, 0.0, 0.0))
             imgs[c] = gaussian_blur(imgs[c], blur)
     plan.set_k_rad(9999.0)
     return sos_normalize(imgs)
+
+
+class DcfParams(ctypes.Structure):
+    _fields_ = [("iters", ctypes.c_int), ("dwin", ctypes.c_float), ("scale", ctypes.c_float),
+                ("overgrid", ctypes.c_float), ("acc", ctypes.c_float), ("kernel", ctypes.c_int)]
+
+
+def dcf_pipe(kx, ky, kz, N, iters=20, dwin=2.1, scale=1.0, overgrid=2.1, acc=1.0, kernel=0, prec=0):
+    """RECON::dcf_calc (Pipe iteration with the DCFgridFFT polynomial kernel); returns kw (float32)."""
+    if np.isscalar(N):
+        N = (N, N, N)
+    kx, px = _f32(kx); ky, py = _f32(ky); kz, pz = _f32(kz)
+    q = DcfParams(iters, dwin, scale, overgrid, acc, kernel)
+    out = np.zeros(kx.size, np.float32)
+    lib().orc_dcf_pipe(px, py, pz, kx.size, N[0], N[1], N[2], ctypes.byref(q),
+                       out.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), prec)
+    return out
+
+
+def dcf_table(dwin=2.1, kernel=0):
+    n = ctypes.c_int()
+    lib().orc_dcf_table(dwin, kernel, None, ctypes.byref(n))
+    out = np.zeros(n.value, np.float32)
+    lib().orc_dcf_table(dwin, kernel, out.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), ctypes.byref(n))
+    return out
 
 
 def glibc_rand(skip, n):

@@ -247,3 +247,18 @@ def test_lowres_smaps_unit_sos_and_taper(oracle_lib):
     def hf(v):
         return np.linalg.norm(np.diff(v, axis=2)) / np.linalg.norm(v)
     assert hf(low) < 0.8 * hf(full)
+
+
+def test_dcf_table_and_weights(oracle_lib):
+    """The polynomial kernel table (length (int)(2.1*600)+100, sum 0.5*600) and the Pipe
+    weights: FP32 restatement close to FP64, growing with |k| on a radial trajectory."""
+    from mri_recon_gb300 import synth
+    t = oracle_lib.dcf_table(2.1, 0)
+    assert t.size == 1360 and abs(float(t.astype(np.float64).sum()) - 300.0) < 1e-3
+    assert t[0] > t[600] > t[1200]
+    kx, ky, kz, _ = synth.radial_trajectory(20, 300, 20, seed=2)
+    w32 = oracle_lib.dcf_pipe(kx, ky, kz, 20, iters=8)
+    w64 = oracle_lib.dcf_pipe(kx, ky, kz, 20, iters=8, prec=1)
+    assert rel(w32, w64) < 1e-5
+    prof = w64.reshape(300, 20).mean(0)
+    assert np.all(np.diff(prof[2:15]) > 0)
