@@ -368,7 +368,7 @@ def run_ours(a):
     torch.cuda.synchronize()
     tms, calls = plan.timings()
     plan.set_timing(False)
-    fi = plan.frame_info(0)
+    fi = plan.frame_info(0, taps=True)
     bm = bytes_model(c, fi["nvalid"], fi["npairs"])
     out_tuning = plan.frame_tuning(0)
     per_launch_ms = {s: float(tms[i]) / max(calls, 1) for i, s in enumerate(STAGES)}
@@ -380,6 +380,17 @@ def run_ours(a):
                 "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
                 "traffic": ncu_traffic(dom), "algorithmic_bytes_per_launch": bm[dom],
                 "launch_ms": per_launch_ms[dom]}
+    # The ungridding gather is bound by the L1 data path, not HBM: every sample reads its
+    # nx*ny*nz taps x C coils (8 B each) through L1.  Nominal L1 load bandwidth: 128 B per
+    # clock per SM, at the SM clock sampled during the timed region.
+    sm_mhz = (clocks or {}).get("sm_mhz") or 2070.0
+    l1_peak = 152 * 128 * sm_mhz * 1e6 / 1e9
+    gather = fi["ntaps"] * C * 8
+    roofline["ungrid_l1_gather"] = {"bytes_per_launch": gather, "achieved": gather / (per_launch_ms["E_ungrid"] / 1e3) / 1e9,
+                                    "peak": l1_peak, "unit": "GB/s",
+                                    "frac": gather / (per_launch_ms["E_ungrid"] / 1e3) / 1e9 / l1_peak,
+                                    "peak_source": "nominal 128 B/clk/SM x 152 SMs at the sampled SM clock",
+                                    "taps_per_sample": fi["ntaps"] / max(fi["nvalid"], 1)}
     iteration_roofline = {"bytes_per_iter": iter_bytes, "achieved_GBs": iter_bytes * value / world / 1e9,
                           "frac": iter_bytes * value / world / 1e9 / peak, "peak_source": peak_kind,
                           "stage_ms": per_launch_ms}

@@ -54,7 +54,8 @@ typedef struct mrg_config {
   int kernel_type;   /* gridFFT::kernel_type, -kaiser/-triangle/-sinc/-poly_kernel */
   float k_rad;       /* gridFFT::k_rad, Gaussian taper radius of E^H (default 9999) */
   int time_grid;     /* gridFFT::time_grid, -time_grid: print per-stage device times */
-  int tile;          /* sample-sort tile edge in grid points (0: default 8 and autotuned launch shapes) */
+  int tile;          /* sample-sort tile edge in grid points, tiles in Morton order (0: default 2 and
+                        autotuned launch shapes; > 0: this edge and fixed launch shapes) */
   int max_pairs;     /* (sample, block) pairs per gridding work item (0: default) */
   int kernel_eval;   /* 0: interpolate the 600-per-unit table as the reference (src/gridFFT.cpp:1113-1116);
                         1: evaluate the Kaiser-Bessel kernel analytically (same beta and scale), the
@@ -99,10 +100,12 @@ mrg_status mrg_set_traj(mrg_plan *plan, int frame, const float *kx, const float 
                         const float *kw, int64_t M, void *stream);
 
 /* Sample bookkeeping of one frame after mrg_set_traj: M samples, nvalid of them
- * contribute (kw != 0 and inside the grid), npairs (sample, tile) pairs and nitems
- * gridding work items. */
+ * contribute (kw != 0 and inside the grid), npairs (sample, block) pairs, nitems
+ * gridding work items and ntaps grid points read by one ungridding (the sum of every
+ * valid sample's nx*ny*nz; computed on the device when ntaps is not NULL).  Any output
+ * may be NULL. */
 mrg_status mrg_frame_info(const mrg_plan *plan, int frame, int64_t *M, int64_t *nvalid, int64_t *npairs,
-                          int64_t *nitems);
+                          int64_t *nitems, int64_t *ntaps);
 
 /* Launch shapes the autotuner chose for a frame (mrg_config.tile == 0): out = {ungrid lanes
  * per sample, ungrid samples per CTA, gridding coils per pass (0: all; -n: the tensor-core

@@ -90,6 +90,8 @@ static GridConst grid_const(const mrg_plan *p) {
   g.nb[2] = p->geo.S[2] / BLK_Z;
   g.k_rad = p->geo.k_rad;
   g.B = p->B;
+  g.mbits = 0;
+  while ((1 << g.mbits) < std::max(g.nt[0], std::max(g.nt[1], g.nt[2]))) g.mbits++;
   g.C = p->C;
   g.eval = p->cfg.kernel_eval;
   g.grid_mode = p->cfg.grid_mode;
@@ -618,9 +620,9 @@ mrg_status mrg_plan_create(const mrg_config *cfg_in, int Nx, int Ny, int Nz, int
       return MRG_ERR_UNSUPPORTED;
     }
   }
-  p->B = cfg.tile > 0 ? cfg.tile : 8;
-  if (p->geo.S[0] % p->B || p->geo.S[1] % p->B || p->geo.S[2] % p->B || p->B < 4 || p->B > 16) {
-    set_error("tile must be 4..16 and divide the grid");
+  p->B = cfg.tile > 0 ? cfg.tile : 2;
+  if (p->geo.S[0] % p->B || p->geo.S[1] % p->B || p->geo.S[2] % p->B || p->B < 2 || p->B > 16) {
+    set_error("tile must be 2..16 and divide the grid");
     delete p;
     return MRG_ERR_INVALID;
   }
@@ -794,13 +796,14 @@ mrg_status mrg_set_traj(mrg_plan *p, int frame, const float *kx, const float *ky
 }
 
 mrg_status mrg_frame_info(const mrg_plan *p, int frame, int64_t *M, int64_t *nvalid, int64_t *npairs,
-                          int64_t *nitems) {
+                          int64_t *nitems, int64_t *ntaps) {
   MRG_TRY(check_frame(p, frame));
   const FrameTraj &ft = p->frames[frame];
   if (M) *M = ft.M;
   if (nvalid) *nvalid = ft.nvalid;
   if (npairs) *npairs = ft.npairs;
   if (nitems) *nitems = ft.nitems;
+  if (ntaps) MRG_TRY(count_taps(ft, ntaps));
   return MRG_OK;
 }
 

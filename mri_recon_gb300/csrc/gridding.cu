@@ -68,7 +68,13 @@ __global__ void k_traj_prep(GridConst g, const float *__restrict__ kx, const flo
     kr = __fadd_rn(kr, __fmul_rn(k[0], k[0]));
     kr = __fadd_rn(kr, __fmul_rn(k[1], k[1]));
     kr = __fadd_rn(kr, __fmul_rn(k[2], k[2]));
-    const int kk = ok ? (cell[2] * g.nt[1] + cell[1]) * g.nt[0] + cell[0] : ntiles;
+    // tiles in Morton (Z-curve) order, so samples that are neighbours in the sorted order
+    // are neighbours in k-space at every scale and a CTA's gathers share cache lines
+    int kk = 0;
+    for (int b = 0; b < g.mbits; b++)
+      kk |= (((cell[0] >> b) & 1) << (3 * b)) | (((cell[1] >> b) & 1) << (3 * b + 1)) |
+            (((cell[2] >> b) & 1) << (3 * b + 2));
+    if (!ok) kk = ntiles;
     pos[i] = make_float4(dk[0], dk[1], dk[2], w);
     kr_out[i] = kr;
     key[i] = kk;
@@ -120,6 +126,36 @@ __global__ void k_traj_sort(int64_t M, float k_rad, const int *__restrict__ key,
     stap[s] = taper(kr[i], k_rad);
     perm[s] = (int)i;
   }
+}
+
+__global__ void k_count_taps(int nvalid, const int4 *__restrict__ sst, unsigned long long *total) {
+  unsigned long long n = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nvalid; i += (int64_t)gridDim.x * blockDim.x) {
+    const int w = sst[i].w;
+    n += (unsigned long long)((w & 15) * ((w >> 4) & 15) * ((w >> 8) & 15));
+  }
+  for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
+  if ((threadIdx.x & 31) == 0 && n) atomicAdd(total, n);
+}
+
+// Taps over all valid samples of a frame (sum of nx*ny*nz): the gather count of one ungrid.
+mrg_status count_taps(const FrameTraj &ft, int64_t *out) {
+  *out = 0;
+  if (ft.nvalid == 0) return MRG_OK;
+  unsigned long long *d = nullptr, h = 0;
+  MRG_CUDA(cudaMalloc(&d, sizeof(h)));
+  cudaMemset(d, 0, sizeof(h));
+  k_count_taps<<<grid_blocks(ft.nvalid, 256), 256>>>(ft.nvalid, ft.sst, d);
+  const cudaError_t e1 = cudaGetLastError();
+  const cudaError_t e2 = cudaMemcpy(&h, d, sizeof(h), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e1 != cudaSuccess || e2 != cudaSuccess) {
+    set_error("tap count failed");
+    return MRG_ERR_CUDA;
+  }
+  count_launch();
+  *out = (int64_t)h;
+  return MRG_OK;
 }
 
 __global__ void k_retaper(int64_t M, float k_rad, const float *__restrict__ skr, float *stap) {
@@ -267,7 +303,7 @@ mrg_status traj_setup(const GridConst &gc, FrameTraj &ft, const float *kx, const
     set_error("trajectory length must be in [1, 2^31)");
     return MRG_ERR_INVALID;
   }
-  const int ntiles = gc.nt[0] * gc.nt[1] * gc.nt[2];
+  const int ntiles = 1 << (3 * gc.mbits);  // Morton key space of the sort tiles
   const int nblocks = gc.nb[0] * gc.nb[1] * gc.nb[2];
   ft.M = M;
   float4 *pos = nullptr;

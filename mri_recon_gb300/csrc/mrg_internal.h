@@ -122,6 +122,7 @@ struct GridConst {
   float k_rad;
   int B;       // sort tile edge (sample order)
   int nt[3];   // sort tiles per axis
+  int mbits;   // bits per axis of the tiles' Morton keys
   int nb[3];   // gridding blocks per axis
   int C;       // coils
   int eval;    // 0: table interpolation, 1: analytic Kaiser-Bessel
@@ -157,6 +158,7 @@ mrg_status traj_setup(const GridConst &gc, FrameTraj &ft, const float *kx, const
                       const float *kw, int64_t M, int max_pairs, cudaStream_t st);
 void traj_free(FrameTraj &ft);
 mrg_status launch_retaper(const GridConst &gc, FrameTraj &ft, cudaStream_t st);
+mrg_status count_taps(const FrameTraj &ft, int64_t *out);
 // coil images / sum of squares from the cropped E^H transform t[v][c]; blur; SOS normalisation
 mrg_status launch_coil_images(const float2 *t, int C, const int N[3], const float *wx, const float *wy,
                               const float *wz, float2 *out, int64_t es, int64_t vs, bool accumulate,

@@ -131,11 +131,13 @@ class Plan:
                                             a.ptr(kz, np.float32), a.ptr(kw, np.float32), M, _stream(stream)))
         self.M[frame] = M
 
-    def frame_info(self, frame):
-        """dict(M, nvalid, npairs, nitems) of a frame after set_traj."""
-        v = [ctypes.c_int64() for _ in range(4)]
-        _lib.check(_lib.load().mrg_frame_info(self._h, frame, *[ctypes.byref(x) for x in v]))
-        return dict(zip(("M", "nvalid", "npairs", "nitems"), (x.value for x in v)))
+    def frame_info(self, frame, taps=False):
+        """dict(M, nvalid, npairs, nitems[, ntaps]) of a frame after set_traj."""
+        v = [ctypes.c_int64() for _ in range(5)]
+        refs = [ctypes.byref(x) for x in v[:4]] + [ctypes.byref(v[4]) if taps else None]
+        _lib.check(_lib.load().mrg_frame_info(self._h, frame, *refs))
+        keys = ("M", "nvalid", "npairs", "nitems") + (("ntaps",) if taps else ())
+        return dict(zip(keys, (x.value for x in v)))
 
     def frame_tuning(self, frame):
         out = (ctypes.c_int * 5)()
