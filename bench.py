@@ -92,8 +92,10 @@ def kernel_of(stage, tuning, C):
                                       max(tuning.get("ungrid_rows_per_step", 1), 1))
     if stage == "EH_grid":
         cc = tuning["grid_coils_per_pass"]
+        if cc <= -100:
+            return "k_grid_umma<%d> (tcgen05 TF32, TMEM accumulators, %d coils per pass)" % (-cc - 100, -cc - 100)
         if cc < 0:
-            return "k_grid_mma<%d> (TF32 tensor cores, %d coils per pass)" % (-cc, -4 * cc)
+            return "k_grid_mma<%d> (mma.sync TF32, %d coils per pass)" % (-cc, -4 * cc)
         return "k_grid<%d> (FP32 CUDA cores)" % (cc if cc > 0 else min(C, 32))
     return {"E_xfft_setimg": "k_fft<Q,-1,SETIMG>", "E_yfft": "k_fft<Q,-1,PLAIN>", "E_zfft": "k_fft<Q,-1,PLAIN>",
             "EH_zfft": "k_fft<Q,+1,PLAIN>", "EH_yfft": "k_fft<Q,+1,PLAIN>",

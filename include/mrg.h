@@ -60,9 +60,11 @@ typedef struct mrg_config {
   int kernel_eval;   /* 0: interpolate the 600-per-unit table as the reference (src/gridFFT.cpp:1113-1116);
                         1: evaluate the Kaiser-Bessel kernel analytically (same beta and scale), the
                         form whose derivative mrg_grad uses, for finite-difference-consistent gradients */
-  int grid_mode;     /* gridding (E^H scatter) kernel: 0 the faster of the two (timed per frame),
-                        1 FP32 multiply-adds on the CUDA cores, 2 tensor cores in TF32 with the
-                        three-term hi/lo split (W V ~ Wh Vh + Wh Vl + Wl Vh, products to ~2^-21) */
+  int grid_mode;     /* gridding (E^H scatter) kernel: 0 the fastest (timed per frame), 1 FP32
+                        multiply-adds on the CUDA cores, 2 tensor cores through mma.sync, 3 tensor
+                        cores through tcgen05 with accumulators in tensor memory (>= 8 coils); 2 and 3
+                        in TF32 with the three-term hi/lo split (W V ~ Wh Vh + Wh Vl + Wl Vh,
+                        products to ~2^-21) */
 } mrg_config;
 
 /* Fills the reference defaults (src/gridFFT.cpp:28-60). */
@@ -108,8 +110,9 @@ mrg_status mrg_frame_info(const mrg_plan *plan, int frame, int64_t *M, int64_t *
                           int64_t *nitems, int64_t *ntaps);
 
 /* Launch shapes the autotuner chose for a frame (mrg_config.tile == 0): out = {ungrid lanes
- * per sample, ungrid samples per CTA, gridding coils per pass (0: all; -n: the tensor-core
- * kernel with 4n coils per pass), ungrid coils per lane, ungrid tap rows loaded per step};
+ * per sample, ungrid samples per CTA, gridding coils per pass (0: all; -n with n < 100: the
+ * mma.sync kernel with 4n coils per pass; -(100 + c): the tcgen05 kernel with c coils per
+ * pass), ungrid coils per lane, ungrid tap rows loaded per step};
  * ms = the timed ungrid and grid kernels. */
 mrg_status mrg_frame_tuning(const mrg_plan *plan, int frame, int out[5], float ms[2]);
 

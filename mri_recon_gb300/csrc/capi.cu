@@ -599,7 +599,7 @@ mrg_status mrg_plan_create(const mrg_config *cfg_in, int Nx, int Ny, int Nz, int
   if (cfg_in) cfg = *cfg_in; else mrg_config_default(&cfg);
   if (!(cfg.overgrid >= 1.0f) || cfg.kernel_type < 0 || cfg.kernel_type > 3 || cfg.kernel_eval < 0 ||
       cfg.kernel_eval > 1 || (cfg.kernel_eval == 1 && cfg.kernel_type != MRG_KERNEL_KAISER) || cfg.grid_mode < 0 ||
-      cfg.grid_mode > 2) {
+      cfg.grid_mode > 3) {
     set_error("bad config");
     return MRG_ERR_INVALID;
   }
@@ -763,8 +763,10 @@ mrg_status mrg_set_traj(mrg_plan *p, int frame, const float *kx, const float *ky
   MRG_TRY(dev_view(p, 2, kz, bytes, true, st, &dz, &s2));
   MRG_TRY(dev_view(p, 3, kw, bytes, true, st, &dw, &s3));
   const GridConst gc = grid_const(p);
+  // region pair lists only where the tensor-memory gridding kernel may run
+  const bool regions = umma_supported(p->C) && (p->cfg.grid_mode == 0 || p->cfg.grid_mode == 3);
   MRG_TRY(traj_setup(gc, p->frames[frame], (const float *)dx, (const float *)dy, (const float *)dz,
-                     (const float *)dw, M, p->max_pairs, st));
+                     (const float *)dw, M, p->max_pairs, regions, st));
   invalidate_graphs(p);
   MRG_TRY(ensure_y(p, (int64_t)p->frames[frame].nvalid * p->C));
   if (p->cfg.tile == 0) {
@@ -801,8 +803,8 @@ mrg_status mrg_frame_info(const mrg_plan *p, int frame, int64_t *M, int64_t *nva
   const FrameTraj &ft = p->frames[frame];
   if (M) *M = ft.M;
   if (nvalid) *nvalid = ft.nvalid;
-  if (npairs) *npairs = ft.npairs;
-  if (nitems) *nitems = ft.nitems;
+  if (npairs) *npairs = ft.blocks.npairs;
+  if (nitems) *nitems = ft.blocks.nitems;
   if (ntaps) MRG_TRY(count_taps(ft, ntaps));
   return MRG_OK;
 }

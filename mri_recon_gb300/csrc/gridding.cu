@@ -224,20 +224,21 @@ __global__ void k_sample_weights(GridConst g, int nvalid, const float4 *__restri
   }
 }
 
-// (sample, block) pairs: count (FILL = false) or fill the per-block lists.
+// (sample, block) pairs for blocks of bs.b[0] x b[1] x b[2] points: count (FILL = false)
+// or fill the per-block lists.
 template <bool FILL>
-__global__ void k_pairs(GridConst g, int nvalid, const int4 *__restrict__ sst, int *pcnt, const int *__restrict__ poff,
+__global__ void k_pairs(BlockShape bs, int nvalid, const int4 *__restrict__ sst, int *pcnt, const int *__restrict__ poff,
                         int *pcur, int *pairs) {
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nvalid; s += gridDim.x * blockDim.x) {
     const int4 t = sst[s];
     const int nx = t.w & 15, ny = (t.w >> 4) & 15, nz = (t.w >> 8) & 15;
-    const int x0 = t.x / BLK_X, x1 = (t.x + nx - 1) / BLK_X;
-    const int y0 = t.y / BLK_Y, y1 = (t.y + ny - 1) / BLK_Y;
-    const int z0 = t.z / BLK_Z, z1 = (t.z + nz - 1) / BLK_Z;
+    const int x0 = t.x / bs.b[0], x1 = (t.x + nx - 1) / bs.b[0];
+    const int y0 = t.y / bs.b[1], y1 = (t.y + ny - 1) / bs.b[1];
+    const int z0 = t.z / bs.b[2], z1 = (t.z + nz - 1) / bs.b[2];
     for (int bz = z0; bz <= z1; bz++)
       for (int by = y0; by <= y1; by++)
         for (int bx = x0; bx <= x1; bx++) {
-          const int blk = (bz * g.nb[1] + by) * g.nb[0] + bx;
+          const int blk = (bz * bs.nb[1] + by) * bs.nb[0] + bx;
           if (FILL) pairs[poff[blk] + atomicAdd(&pcur[blk], 1)] = s;
           else atomicAdd(&pcnt[blk], 1);
         }
@@ -279,9 +280,8 @@ void traj_free(FrameTraj &ft) {
   cudaFree(ft.perm);
   cudaFree(ft.swt);
   cudaFree(ft.sst);
-  cudaFree(ft.pairs);
-  cudaFree(ft.items);
-  cudaFree(ft.split_blocks);
+  pair_set_free(ft.blocks);
+  pair_set_free(ft.regions);
   cudaFree(ft.dsorted);
   cudaFree(ft.sdw);
   ft = FrameTraj();
@@ -296,24 +296,112 @@ static mrg_status read_int(const int *dev, int *host, cudaStream_t st, const cha
   return MRG_OK;
 }
 
+BlockShape block_shape(const GridConst &gc) {
+  BlockShape bs;
+  bs.b[0] = BLK_X; bs.b[1] = BLK_Y; bs.b[2] = BLK_Z;
+  for (int d = 0; d < 3; d++) bs.nb[d] = gc.S[d] / bs.b[d];
+  return bs;
+}
+BlockShape region_shape(const GridConst &gc) {
+  BlockShape bs;
+  bs.b[0] = RGN_X; bs.b[1] = RGN_Y; bs.b[2] = RGN_Z;
+  for (int d = 0; d < 3; d++) bs.nb[d] = gc.S[d] / bs.b[d];
+  return bs;
+}
+
+void pair_set_free(PairSet &ps) {
+  cudaFree(ps.pairs);
+  cudaFree(ps.items);
+  cudaFree(ps.split);
+  ps = PairSet();
+}
+
+// Pair lists of one block shape: every valid sample is listed under each block its
+// support touches; each block becomes ceil(pairs / max_pairs) work items (at least one,
+// so that every grid point is written), flagged when there are several (those flush
+// with atomics into a pre-zeroed block).
+static mrg_status build_pairs(const BlockShape &bs, int nvalid, const int4 *sst, int max_pairs, cudaStream_t st,
+                              PairSet &ps) {
+  pair_set_free(ps);
+  const int nblocks = bs.nb[0] * bs.nb[1] * bs.nb[2];
+  int *pcnt = nullptr, *poff = nullptr, *pcur = nullptr, *icnt = nullptr, *ioff = nullptr, *nsplit = nullptr;
+  mrg_status rs = MRG_OK;
+  auto cleanup = [&]() {
+    cudaFree(pcnt); cudaFree(poff); cudaFree(pcur); cudaFree(icnt); cudaFree(ioff); cudaFree(nsplit);
+  };
+#define PAIRS_TRY(x)         \
+  do {                       \
+    rs = (x);                \
+    if (rs != MRG_OK) {      \
+      cleanup();             \
+      pair_set_free(ps);     \
+      return rs;             \
+    }                        \
+  } while (0)
+#define PAIRS_LAUNCHED()                                                    \
+  do {                                                                      \
+    count_launch();                                                         \
+    if (cudaGetLastError() != cudaSuccess) PAIRS_TRY(MRG_ERR_CUDA);         \
+  } while (0)
+  PAIRS_TRY(dalloc(&pcnt, nblocks + 1));
+  PAIRS_TRY(dalloc(&poff, nblocks + 2));
+  PAIRS_TRY(dalloc(&pcur, nblocks + 1));
+  PAIRS_TRY(launch_zero(pcnt, sizeof(int) * (nblocks + 1), st));
+  PAIRS_TRY(launch_zero(pcur, sizeof(int) * (nblocks + 1), st));
+  if (nvalid > 0) {
+    k_pairs<false><<<grid_blocks(nvalid, 256), 256, 0, st>>>(bs, nvalid, sst, pcnt, nullptr, nullptr, nullptr);
+    PAIRS_LAUNCHED();
+  }
+  k_scan<<<1, 1024, 0, st>>>(pcnt, poff, nblocks);
+  PAIRS_LAUNCHED();
+  int npairs = 0;
+  PAIRS_TRY(read_int(poff + nblocks, &npairs, st, "pair count failed"));
+  ps.npairs = npairs;
+  PAIRS_TRY(dalloc(&ps.pairs, npairs));
+  if (nvalid > 0) {
+    k_pairs<true><<<grid_blocks(nvalid, 256), 256, 0, st>>>(bs, nvalid, sst, nullptr, poff, pcur, ps.pairs);
+    PAIRS_LAUNCHED();
+  }
+  PAIRS_TRY(dalloc(&icnt, nblocks + 1));
+  PAIRS_TRY(dalloc(&ioff, nblocks + 2));
+  PAIRS_TRY(dalloc(&nsplit, 1));
+  PAIRS_TRY(launch_zero(nsplit, sizeof(int), st));
+  k_item_count<<<grid_blocks(nblocks, 256), 256, 0, st>>>(nblocks, pcnt, max_pairs, icnt);
+  PAIRS_LAUNCHED();
+  k_scan<<<1, 1024, 0, st>>>(icnt, ioff, nblocks);
+  PAIRS_LAUNCHED();
+  int nitems = 0;
+  PAIRS_TRY(read_int(ioff + nblocks, &nitems, st, "item count failed"));
+  ps.nitems = nitems;
+  PAIRS_TRY(dalloc(&ps.items, nitems));
+  PAIRS_TRY(dalloc(&ps.split, nblocks));
+  k_item_fill<<<grid_blocks(nblocks, 256), 256, 0, st>>>(nblocks, pcnt, poff, icnt, ioff, max_pairs, ps.items,
+                                                         ps.split, nsplit);
+  PAIRS_LAUNCHED();
+  int ns = 0;
+  PAIRS_TRY(read_int(nsplit, &ns, st, "item fill failed"));
+  ps.nsplit = ns;
+  cleanup();
+#undef PAIRS_TRY
+#undef PAIRS_LAUNCHED
+  return MRG_OK;
+}
+
 mrg_status traj_setup(const GridConst &gc, FrameTraj &ft, const float *kx, const float *ky, const float *kz,
-                      const float *kw, int64_t M, int max_pairs, cudaStream_t st) {
+                      const float *kw, int64_t M, int max_pairs, bool regions, cudaStream_t st) {
   traj_free(ft);
   if (M <= 0 || M >= (int64_t)1 << 31) {
     set_error("trajectory length must be in [1, 2^31)");
     return MRG_ERR_INVALID;
   }
   const int ntiles = 1 << (3 * gc.mbits);  // Morton key space of the sort tiles
-  const int nblocks = gc.nb[0] * gc.nb[1] * gc.nb[2];
   ft.M = M;
   float4 *pos = nullptr;
   float *tap = nullptr;
   int *key = nullptr, *cnt = nullptr, *off = nullptr, *cur = nullptr;
-  int *pcnt = nullptr, *poff = nullptr, *pcur = nullptr, *icnt = nullptr, *ioff = nullptr, *nsplit = nullptr;
   mrg_status rs = MRG_OK;
   auto cleanup = [&]() {
     cudaFree(pos); cudaFree(tap); cudaFree(key); cudaFree(cnt); cudaFree(off); cudaFree(cur);
-    cudaFree(pcnt); cudaFree(poff); cudaFree(pcur); cudaFree(icnt); cudaFree(ioff); cudaFree(nsplit);
   };
 #define SETUP_TRY(x)         \
   do {                       \
@@ -359,43 +447,10 @@ mrg_status traj_setup(const GridConst &gc, FrameTraj &ft, const float *kx, const
   k_sample_weights<<<grid_blocks(nvalid, 256), 256, 0, st>>>(gc, nvalid, ft.spos, ft.swt, ft.sst);
   SETUP_LAUNCHED();
 
-  // 3. (sample, block) pair lists
-  SETUP_TRY(dalloc(&pcnt, nblocks + 1));
-  SETUP_TRY(dalloc(&poff, nblocks + 2));
-  SETUP_TRY(dalloc(&pcur, nblocks + 1));
-  SETUP_TRY(launch_zero(pcnt, sizeof(int) * (nblocks + 1), st));
-  SETUP_TRY(launch_zero(pcur, sizeof(int) * (nblocks + 1), st));
-  k_pairs<false><<<grid_blocks(nvalid, 256), 256, 0, st>>>(gc, nvalid, ft.sst, pcnt, nullptr, nullptr, nullptr);
-  SETUP_LAUNCHED();
-  k_scan<<<1, 1024, 0, st>>>(pcnt, poff, nblocks);
-  SETUP_LAUNCHED();
-  int npairs = 0;
-  SETUP_TRY(read_int(poff + nblocks, &npairs, st, "pair count failed"));
-  ft.npairs = npairs;
-  SETUP_TRY(dalloc(&ft.pairs, npairs));
-  k_pairs<true><<<grid_blocks(nvalid, 256), 256, 0, st>>>(gc, nvalid, ft.sst, nullptr, poff, pcur, ft.pairs);
-  SETUP_LAUNCHED();
-
-  // 4. work items: at most max_pairs pairs each; every block gets >= 1 item
-  SETUP_TRY(dalloc(&icnt, nblocks + 1));
-  SETUP_TRY(dalloc(&ioff, nblocks + 2));
-  SETUP_TRY(dalloc(&nsplit, 1));
-  SETUP_TRY(launch_zero(nsplit, sizeof(int), st));
-  k_item_count<<<grid_blocks(nblocks, 256), 256, 0, st>>>(nblocks, pcnt, max_pairs, icnt);
-  SETUP_LAUNCHED();
-  k_scan<<<1, 1024, 0, st>>>(icnt, ioff, nblocks);
-  SETUP_LAUNCHED();
-  int nitems = 0;
-  SETUP_TRY(read_int(ioff + nblocks, &nitems, st, "item count failed"));
-  ft.nitems = nitems;
-  SETUP_TRY(dalloc(&ft.items, nitems));
-  SETUP_TRY(dalloc(&ft.split_blocks, nblocks));
-  k_item_fill<<<grid_blocks(nblocks, 256), 256, 0, st>>>(nblocks, pcnt, poff, icnt, ioff, max_pairs, ft.items,
-                                                         ft.split_blocks, nsplit);
-  SETUP_LAUNCHED();
-  int ns = 0;
-  SETUP_TRY(read_int(nsplit, &ns, st, "item fill failed"));
-  ft.nsplit = ns;
+  // 3-4. (sample, block) pair lists and work items for the 8x2x2 blocks, and for the
+  // 8x4x4 regions of the tensor-memory gridding kernel when it may run
+  SETUP_TRY(build_pairs(block_shape(gc), nvalid, ft.sst, max_pairs, st, ft.blocks));
+  if (regions) SETUP_TRY(build_pairs(region_shape(gc), nvalid, ft.sst, max_pairs, st, ft.regions));
   cleanup();
 #undef SETUP_TRY
 #undef SETUP_LAUNCHED
@@ -570,18 +625,19 @@ mrg_status launch_ungrid(const GridConst &gc, const FrameTraj &ft, const float2 
 // ---------------------------------------------------------------------------
 // gridding: a warp owns an 8x2x2 block (lane = point), coils in registers
 // ---------------------------------------------------------------------------
-__global__ void k_zero_blocks(const GridConst g, const int *__restrict__ blocks, int n, float2 *grid) {
+__global__ void k_zero_blocks(const GridConst g, BlockShape bs, const int *__restrict__ blocks, int n, float2 *grid) {
   const int C = g.C;
-  const int per = BLK_X * BLK_Y * BLK_Z * C;
+  const int per = bs.b[0] * bs.b[1] * bs.b[2] * C;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < (int64_t)n * per;
        e += (int64_t)gridDim.x * blockDim.x) {
     const int b = blocks[e / per];
     int r = (int)(e % per);
     const int c = r % C;
     r /= C;
-    const int px = r % BLK_X, py = (r / BLK_X) % BLK_Y, pz = r / (BLK_X * BLK_Y);
-    const int bx = b % g.nb[0], by = (b / g.nb[0]) % g.nb[1], bz = b / (g.nb[0] * g.nb[1]);
-    const int64_t gi = (((int64_t)(bz * BLK_Z + pz) * g.S[1] + (by * BLK_Y + py)) * g.S[0] + (bx * BLK_X + px)) * C + c;
+    const int px = r % bs.b[0], py = (r / bs.b[0]) % bs.b[1], pz = r / (bs.b[0] * bs.b[1]);
+    const int bx = b % bs.nb[0], by = (b / bs.nb[0]) % bs.nb[1], bz = b / (bs.nb[0] * bs.nb[1]);
+    const int64_t gi =
+        (((int64_t)(bz * bs.b[2] + pz) * g.S[1] + (by * bs.b[1] + py)) * g.S[0] + (bx * bs.b[0] + px)) * C + c;
     grid[gi] = make_float2(0.f, 0.f);
   }
 }
@@ -704,7 +760,7 @@ template <int CC>
 static mrg_status launch_grid_cc(const GridConst &gc, const FrameTraj &ft, const float2 *yw, float2 *grid,
                                  cudaStream_t st) {
   const bool vec = (gc.C % 2 == 0) && (CC % 2 == 0) && (((uintptr_t)yw & 15) == 0);
-  const dim3 blocks((unsigned)((ft.nitems + 7) / 8), (unsigned)((gc.C + CC - 1) / CC));
+  const dim3 blocks((unsigned)((ft.blocks.nitems + 7) / 8), (unsigned)((gc.C + CC - 1) / CC));
   const size_t smem = 8 * GridStage<CC>::bytes;
   static bool attr = false;
   if (!attr) {
@@ -713,9 +769,9 @@ static mrg_status launch_grid_cc(const GridConst &gc, const FrameTraj &ft, const
     attr = true;
   }
   if (vec)
-    k_grid<CC, true><<<blocks, 256, smem, st>>>(gc, ft.nitems, ft.items, ft.pairs, ft.swt, ft.sst, yw, grid);
+    k_grid<CC, true><<<blocks, 256, smem, st>>>(gc, ft.blocks.nitems, ft.blocks.items, ft.blocks.pairs, ft.swt, ft.sst, yw, grid);
   else
-    k_grid<CC, false><<<blocks, 256, smem, st>>>(gc, ft.nitems, ft.items, ft.pairs, ft.swt, ft.sst, yw, grid);
+    k_grid<CC, false><<<blocks, 256, smem, st>>>(gc, ft.blocks.nitems, ft.blocks.items, ft.blocks.pairs, ft.swt, ft.sst, yw, grid);
   MRG_LAUNCHED();
   return MRG_OK;
 }
@@ -980,7 +1036,7 @@ static mrg_status launch_grid_mma(const GridConst &gc, const FrameTraj &ft, cons
                                   cudaStream_t st) {
   constexpr int CC = 4 * NT;
   const bool vec = (gc.C % 2 == 0) && (((uintptr_t)yw & 15) == 0) && (((uintptr_t)grid & 15) == 0);
-  const dim3 blocks((unsigned)((ft.nitems + 7) / 8), (unsigned)((gc.C + CC - 1) / CC));
+  const dim3 blocks((unsigned)((ft.blocks.nitems + 7) / 8), (unsigned)((gc.C + CC - 1) / CC));
   const size_t smem = 8 * (GridStage<CC>::bytes + 32 * 16);  // + the y/z products of 32 pairs
   static bool attr = false;
   if (!attr) {
@@ -989,9 +1045,9 @@ static mrg_status launch_grid_mma(const GridConst &gc, const FrameTraj &ft, cons
     attr = true;
   }
   if (vec)
-    k_grid_mma<NT, true><<<blocks, 256, smem, st>>>(gc, ft.nitems, ft.items, ft.pairs, ft.swt, ft.sst, yw, grid);
+    k_grid_mma<NT, true><<<blocks, 256, smem, st>>>(gc, ft.blocks.nitems, ft.blocks.items, ft.blocks.pairs, ft.swt, ft.sst, yw, grid);
   else
-    k_grid_mma<NT, false><<<blocks, 256, smem, st>>>(gc, ft.nitems, ft.items, ft.pairs, ft.swt, ft.sst, yw, grid);
+    k_grid_mma<NT, false><<<blocks, 256, smem, st>>>(gc, ft.blocks.nitems, ft.blocks.items, ft.blocks.pairs, ft.swt, ft.sst, yw, grid);
   MRG_LAUNCHED();
   return MRG_OK;
 }
@@ -1000,12 +1056,22 @@ static mrg_status launch_grid_mma(const GridConst &gc, const FrameTraj &ft, cons
 static int default_grid_nt(int C) { return C > 16 ? 8 : (C > 8 ? 4 : (C > 4 ? 2 : 1)); }
 
 mrg_status launch_grid(const GridConst &gc, const FrameTraj &ft, const float2 *yw, float2 *grid, cudaStream_t st) {
-  if (ft.nsplit > 0) {
-    const int64_t n = (int64_t)ft.nsplit * BLK_X * BLK_Y * BLK_Z * gc.C;
-    k_zero_blocks<<<grid_blocks(n, 256), 256, 0, st>>>(gc, ft.split_blocks, ft.nsplit, grid);
+  const int C = gc.C;
+  // tcgen05 kernel over 8x4x4 regions: grid_cc = -(100 + coils per pass)
+  if (ft.grid_cc <= -100 || (ft.grid_cc == 0 && gc.grid_mode == 3)) {
+    if (ft.regions.nsplit > 0) {
+      const BlockShape rs = region_shape(gc);
+      const int64_t n = (int64_t)ft.regions.nsplit * RGN_X * RGN_Y * RGN_Z * C;
+      k_zero_blocks<<<grid_blocks(n, 256), 256, 0, st>>>(gc, rs, ft.regions.split, ft.regions.nsplit, grid);
+      MRG_LAUNCHED();
+    }
+    return launch_grid_umma(gc, ft, ft.grid_cc <= -100 ? -ft.grid_cc - 100 : umma_default_cc(C), yw, grid, st);
+  }
+  if (ft.blocks.nsplit > 0) {
+    const int64_t n = (int64_t)ft.blocks.nsplit * BLK_X * BLK_Y * BLK_Z * C;
+    k_zero_blocks<<<grid_blocks(n, 256), 256, 0, st>>>(gc, block_shape(gc), ft.blocks.split, ft.blocks.nsplit, grid);
     MRG_LAUNCHED();
   }
-  const int C = gc.C;
   if (ft.grid_cc < 0 || (ft.grid_cc == 0 && gc.grid_mode == 2)) {
     switch (ft.grid_cc < 0 ? -ft.grid_cc : default_grid_nt(C)) {
       case 1: return launch_grid_mma<1>(gc, ft, yw, grid, st);
@@ -1248,14 +1314,22 @@ mrg_status autotune_frame(const GridConst &gc, FrameTraj &ft, float2 *grid, floa
   best = 1e30f;
   int bestCC = 0;
   // CUDA-core kernel: all coils, 16 or 8 per pass; tensor-core kernel (negative): 4n coils per pass
-  for (int cc : {0, 16, 8, -8, -4, -2, -1}) {
-    if (cc > 0 && gc.C <= cc) continue;
-    if (cc >= 0 && gc.grid_mode == 2) continue;
-    if (cc < 0 && gc.grid_mode == 1) continue;
-    if (cc < 0 && -cc > default_grid_nt(gc.C)) continue;  // more coils per pass than the plan has
-    if (cc < 0 && -cc < default_grid_nt(gc.C) / 2) continue;
+  // CUDA-core kernel: all coils, 16 or 8 per pass; mma.sync kernel (-n): 4n coils per pass;
+  // tcgen05 kernel (-(100 + c)): c coils per pass
+  for (int cc : {0, 16, 8, -8, -4, -2, -1, -132, -116, -108}) {
+    const int mode = cc >= 0 ? 1 : (cc > -100 ? 2 : 3);
+    if (gc.grid_mode != 0 && gc.grid_mode != mode) continue;
+    if (mode == 1 && cc > 0 && gc.C <= cc) continue;
+    if (mode == 2 && -cc > default_grid_nt(gc.C)) continue;  // more coils per pass than the plan has
+    if (mode == 2 && -cc < default_grid_nt(gc.C) / 2) continue;
+    if (mode == 3) {
+      const int c = -cc - 100;
+      if (!umma_supported(gc.C) || ft.regions.items == nullptr) continue;
+      if (c > umma_default_cc(gc.C) || c < umma_default_cc(gc.C) / 2) continue;
+    }
     ft.grid_cc = cc;
-    const float ms = time_ms(st, [&]() { return launch_grid(gc, ft, y, grid, st); }, 2);
+    float ms = time_ms(st, [&]() { return launch_grid(gc, ft, y, grid, st); }, 2);
+    if (mode == 3 && umma_error_flag()) ms = 1e30f;  // gave up waiting for its MMAs: never pick it
     if (ms < best) {
       best = ms;
       bestCC = cc;

@@ -126,9 +126,27 @@ struct GridConst {
   int nb[3];   // gridding blocks per axis
   int C;       // coils
   int eval;    // 0: table interpolation, 1: analytic Kaiser-Bessel
-  int grid_mode;  // 0: fastest timed, 1: CUDA-core gridding, 2: tensor-core gridding
+  int grid_mode;  // 0: fastest timed, 1: CUDA cores, 2: mma.sync tensor cores, 3: tcgen05 / TMEM
   float beta[3];
   double kb_norm[3];
+};
+
+// Gridding blocks of b[0] x b[1] x b[2] points, nb[d] = S[d] / b[d] per axis.
+struct BlockShape {
+  int b[3], nb[3];
+};
+// Tensor-memory gridding regions: 128 points, one TMEM lane each.
+constexpr int RGN_X = 8, RGN_Y = 4, RGN_Z = 4;
+static_assert(RGN_X * RGN_Y * RGN_Z == 128, "one region row per TMEM lane");
+
+// (sample, block) pairs of one block shape and the work items over them.
+struct PairSet {
+  int *pairs = nullptr;     // sample index per (sample, block) pair, grouped by block
+  int64_t npairs = 0;
+  int4 *items = nullptr;    // (block, p0, p1, split)
+  int nitems = 0;
+  int *split = nullptr;     // blocks with several work items (pre-zeroed, atomic flush)
+  int nsplit = 0;
 };
 
 struct FrameTraj {
@@ -140,12 +158,8 @@ struct FrameTraj {
   int *perm = nullptr;      // [M] sorted -> original sample index
   float4 *swt = nullptr;    // [nvalid][6] tap weights wx[8], wy[8], wz[8] (chop sign included, zero padded)
   int4 *sst = nullptr;      // [nvalid] first tap (sx, sy, sz) and tap counts nx | ny << 4 | nz << 8
-  int *pairs = nullptr;     // sample index per (sample, block) pair, grouped by block
-  int64_t npairs = 0;
-  int4 *items = nullptr;    // (block, p0, p1, split)
-  int nitems = 0;
-  int *split_blocks = nullptr;
-  int nsplit = 0;
+  PairSet blocks;           // 8x2x2 blocks (k_grid, k_grid_mma)
+  PairSet regions;          // 8x4x4 regions (k_grid_umma), built when that kernel may run
   float2 *dsorted = nullptr;  // measured data [nvalid][C], unweighted
   float4 *sdw = nullptr;      // [nvalid][6] d(tap weight)/dk per axis (allocated by mrg_grad)
   bool has_data = false;
@@ -155,7 +169,17 @@ struct FrameTraj {
 };
 
 mrg_status traj_setup(const GridConst &gc, FrameTraj &ft, const float *kx, const float *ky, const float *kz,
-                      const float *kw, int64_t M, int max_pairs, cudaStream_t st);
+                      const float *kw, int64_t M, int max_pairs, bool regions, cudaStream_t st);
+BlockShape block_shape(const GridConst &gc);
+BlockShape region_shape(const GridConst &gc);
+void pair_set_free(PairSet &ps);
+// tcgen05 gridding over 8x4x4 regions (grid_umma.cu): cc = coils per pass (8, 16 or 32)
+bool umma_supported(int C);
+int umma_default_cc(int C);
+mrg_status launch_grid_umma(const GridConst &gc, const FrameTraj &ft, int cc, const float2 *yw, float2 *grid,
+                            cudaStream_t st);
+// nonzero once a tcgen05 gridding launch gave up waiting for its tensor-core work
+int umma_error_flag();
 void traj_free(FrameTraj &ft);
 mrg_status launch_retaper(const GridConst &gc, FrameTraj &ft, cudaStream_t st);
 mrg_status count_taps(const FrameTraj &ft, int64_t *out);

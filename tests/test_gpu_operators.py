@@ -168,13 +168,16 @@ def test_errors_do_not_exit(mrg_lib):
         m.Plan(112, 1, 1)                           # S = 176 = 16*11: radix 11 not built
 
 
-@pytest.mark.parametrize("grid_mode", [1, 2])
+@pytest.mark.parametrize("grid_mode", [1, 2, 3])
 @pytest.mark.parametrize("N,C,nproj,max_pairs", [(32, 4, 700, 0), (48, 3, 500, 0), (32, 20, 400, 0),
-                                                  (32, 32, 300, 0), (32, 1, 600, 0), (32, 8, 700, 96)])
+                                                  (32, 32, 300, 0), (32, 1, 600, 0), (32, 8, 700, 96),
+                                                  (48, 9, 500, 0), (32, 16, 900, 200)])
 def test_adjoint_each_gridding_kernel(mrg_lib, oracle_lib, grid_mode, N, C, nproj, max_pairs):
-    """Both gridding kernels (FP32 CUDA cores; TF32 tensor cores with the hi/lo
-    split), odd and partial coil chunks, and dense blocks split into work items
-    that flush with atomics (small max_pairs)."""
+    """Every gridding kernel (FP32 CUDA cores; TF32 tensor cores with the hi/lo split
+    through mma.sync and through tcgen05 / tensor memory), odd and partial coil chunks,
+    and dense blocks split into work items that flush with atomics (small max_pairs)."""
+    if grid_mode == 3 and C < 8:
+        pytest.skip("the tcgen05 kernel needs >= 8 coils")
     torch = _torch()
     c = case(N=N, C=C, nproj=nproj)
     p = mrg_lib.Plan(N, C, 1, grid_mode=grid_mode, max_pairs=max_pairs)
