@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--e2e-solves", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain per-coil GPU path")
+    ap.add_argument("--grid-mode", type=int, default=0,
+                    help="gridding kernel (mrg_config.grid_mode): 0 fastest timed, 1 CUDA cores, 2 mma.sync, 3 tcgen05")
     ap.add_argument("--no-side-configs", dest="side_configs", action="store_false",
                     help="skip the throughput of the four smaller configurations")
     return ap.parse_args()
@@ -327,7 +329,7 @@ def run_ours(a):
     kx, ky, kz, kw = synth.radial_trajectory(N, c["nproj"], c["nread"])
     img = synth.phantom(N, c["ellipsoids"], seed=c["seed"])
     smaps = synth.coil_maps_torch(N, C, dev, seed=c["seed"] + 1)
-    plan = m.Plan(N, C, 1)
+    plan = m.Plan(N, C, 1, grid_mode=a.grid_mode)
     plan.set_traj(0, kx, ky, kz, kw)
     plan.set_smaps(smaps)
     x_true = torch.from_numpy(img).to(dev)
