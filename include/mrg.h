@@ -115,6 +115,12 @@ mrg_status mrg_frame_info(const mrg_plan *plan, int frame, int64_t *M, int64_t *
  * pass), ungrid coils per lane, ungrid tap rows loaded per step};
  * ms = the timed ungrid and grid kernels. */
 mrg_status mrg_frame_tuning(const mrg_plan *plan, int frame, int out[5], float ms[2]);
+/* Fixes a frame's launch shapes (same order and encoding as mrg_frame_tuning) after
+ * mrg_set_traj, in place of the autotuner's: for reproducible launches or to compare
+ * variants.  Gridding shapes the plan cannot run are rejected (MRG_ERR_INVALID); an
+ * ungridding shape a buffer cannot take falls back to fewer coils per lane (4 coils per
+ * lane needs a coil count divisible by 4 and 4 to 16 lanes; 2 needs an even count). */
+mrg_status mrg_frame_set_tuning(mrg_plan *plan, int frame, const int in[5]);
 
 /* Measured k-space of one frame: ncoil arrays of M complex64, coil c at
  * data + c*coil_stride.  Used by mrg_cg / mrg_fista (data.kdata, src/mri_data.h). */

@@ -826,6 +826,32 @@ mrg_status mrg_frame_tuning(const mrg_plan *p, int frame, int out[5], float ms[2
   return MRG_OK;
 }
 
+mrg_status mrg_frame_set_tuning(mrg_plan *p, int frame, const int in[5]) {
+  MRG_TRY(check_frame(p, frame));
+  if (!in) {
+    set_error("null argument");
+    return MRG_ERR_INVALID;
+  }
+  FrameTraj &ft = p->frames[frame];
+  const int G = in[0], spb = in[1], cc = in[2], cpl = in[3], uy = in[4];
+  const bool g_ok = (G == 1 || G == 2 || G == 4 || G == 8 || G == 16 || G == 32);
+  if (!g_ok || spb < 1 || !(cpl == 1 || cpl == 2 || cpl == 4) || uy < 1 || uy > 3) {
+    set_error("ungridding launch shape out of range");
+    return MRG_ERR_INVALID;
+  }
+  if (!grid_cc_allowed(p->C, ft, cc)) {
+    set_error("gridding launch shape not available for this plan's coil count and grid_mode");
+    return MRG_ERR_INVALID;
+  }
+  ft.ungrid_G = G;
+  ft.ungrid_spb = spb;
+  ft.grid_cc = cc;
+  ft.ungrid_cpl = cpl;
+  ft.ungrid_uy = uy;
+  invalidate_graphs(p);
+  return MRG_OK;
+}
+
 mrg_status mrg_set_data(mrg_plan *p, int frame, const void *data, int64_t coil_stride, void *stream) {
   MRG_TRY(check_frame(p, frame));
   if (!data) {

@@ -472,6 +472,7 @@ template <>
 struct UngridVec<1> {
   typedef float2 T;
   static __device__ __forceinline__ T zero() { return make_float2(0.f, 0.f); }
+  static __device__ __forceinline__ T load(const float2 *p) { return __ldg(p); }
   static __device__ __forceinline__ void fma(float *ar, float w, T v) {
     ar[0] += w * v.x;
     ar[1] += w * v.y;
@@ -481,11 +482,38 @@ template <>
 struct UngridVec<2> {
   typedef float4 T;
   static __device__ __forceinline__ T zero() { return make_float4(0.f, 0.f, 0.f, 0.f); }
+  static __device__ __forceinline__ T load(const float2 *p) { return __ldg(reinterpret_cast<const float4 *>(p)); }
   static __device__ __forceinline__ void fma(float *ar, float w, T v) {
     ar[0] += w * v.x;
     ar[1] += w * v.y;
     ar[2] += w * v.z;
     ar[3] += w * v.w;
+  }
+};
+// four coils per lane: one 32-byte load (address 32-byte aligned: C % 4 == 0)
+struct F8 {
+  float v[8];
+};
+template <>
+struct UngridVec<4> {
+  typedef F8 T;
+  static __device__ __forceinline__ T zero() {
+    F8 z;
+#pragma unroll
+    for (int i = 0; i < 8; i++) z.v[i] = 0.f;
+    return z;
+  }
+  static __device__ __forceinline__ T load(const float2 *p) {
+    F8 r;
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(r.v[0]), "=f"(r.v[1]), "=f"(r.v[2]), "=f"(r.v[3]), "=f"(r.v[4]), "=f"(r.v[5]), "=f"(r.v[6]),
+          "=f"(r.v[7])
+        : "l"(p));
+    return r;
+  }
+  static __device__ __forceinline__ void fma(float *ar, float w, const T &v) {
+#pragma unroll
+    for (int i = 0; i < 8; i++) ar[i] += w * v.v[i];
   }
 };
 
@@ -528,7 +556,7 @@ __global__ void __launch_bounds__(256) k_ungrid(const GridConst g, int nvalid, i
           const float2 *row = base + kz * zs + (ky0 + u) * ys;
 #pragma unroll
           for (int a = 0; a < 6; a++)
-            v[u][a] = (ky0 + u < ny && a < nx) ? __ldg(reinterpret_cast<const VT *>(row + (int64_t)a * C)) : V::zero();
+            v[u][a] = (ky0 + u < ny && a < nx) ? V::load(row + (int64_t)a * C) : V::zero();
         }
 #pragma unroll
         for (int u = 0; u < UY; u++) {
@@ -578,9 +606,11 @@ mrg_status launch_ungrid(const GridConst &gc, const FrameTraj &ft, const float2 
                          bool weigh, cudaStream_t st) {
   if (ft.nvalid == 0) return MRG_OK;
   int G = ft.ungrid_G > 0 ? ft.ungrid_G : ungrid_group_default(gc.C);
-  // two coils per lane (16-byte loads) when the coil count is even and the buffers allow it
+  // two coils per lane (16-byte loads) when the coil count is even and the buffers allow it,
+  // four (32-byte loads) when it is a multiple of 4
   int cpl = (ft.ungrid_cpl > 0) ? ft.ungrid_cpl : ((gc.C % 2 == 0) ? 2 : 1);
-  if (gc.C % 2 != 0 || ((uintptr_t)grid & 15) != 0) cpl = 1;
+  if (cpl == 4 && (gc.C % 4 != 0 || ((uintptr_t)grid & 31) != 0 || G < 4 || G > 16)) cpl = 2;
+  if (cpl == 2 && (gc.C % 2 != 0 || ((uintptr_t)grid & 15) != 0)) cpl = 1;
   const int spb = ft.ungrid_spb > 0 ? ft.ungrid_spb : 256;
   const int uy = ft.ungrid_uy > 0 ? ft.ungrid_uy : 1;
   const int chunk = G * cpl;
@@ -595,7 +625,8 @@ mrg_status launch_ungrid(const GridConst &gc, const FrameTraj &ft, const float2 
   }
 #define UNGRID_CASE(GG)                                                           \
   case GG:                                                                        \
-    if (cpl == 2) { UNGRID_UY(GG, 2) }                                            \
+    if (cpl == 4) k_ungrid<GG, 4, 1><<<blocks, 256, 0, st>>>(UNGRID_ARGS);        \
+    else if (cpl == 2) { UNGRID_UY(GG, 2) }                                       \
     else { UNGRID_UY(GG, 1) }                                                     \
     break;
   switch (G) {
@@ -1055,6 +1086,13 @@ static mrg_status launch_grid_mma(const GridConst &gc, const FrameTraj &ft, cons
 // n-tiles (4 coils each) per pass of the tensor-core kernel when none was tuned.
 static int default_grid_nt(int C) { return C > 16 ? 8 : (C > 8 ? 4 : (C > 4 ? 2 : 1)); }
 
+bool grid_cc_allowed(int C, const FrameTraj &ft, int cc) {
+  if (cc >= 0) return cc == 0 || cc == 8 || cc == 16;
+  if (cc > -100) return (cc == -1 || cc == -2 || cc == -4 || cc == -8) && -cc <= default_grid_nt(C);
+  const int c = -cc - 100;
+  return (c == 8 || c == 16 || c == 32) && umma_supported(C) && ft.regions.items != nullptr && c <= umma_default_cc(C);
+}
+
 mrg_status launch_grid(const GridConst &gc, const FrameTraj &ft, const float2 *yw, float2 *grid, cudaStream_t st) {
   const int C = gc.C;
   // tcgen05 kernel over 8x4x4 regions: grid_cc = -(100 + coils per pass)
@@ -1275,10 +1313,11 @@ mrg_status autotune_frame(const GridConst &gc, FrameTraj &ft, float2 *grid, floa
   if (ft.nvalid == 0) return MRG_OK;
   float best = 1e30f;
   int bestG = ungrid_group_default(gc.C), bestS = 256, bestP = 1;
-  for (int cpl : {1, 2}) {
-    if (cpl == 2 && gc.C % 2) continue;
+  for (int cpl : {1, 2, 4}) {
+    if (gc.C % cpl) continue;
     for (int G : {4, 8, 16, 32}) {
       if (G * cpl > 2 * gc.C && G > 4) continue;
+      if (cpl == 4 && G > 16) continue;
       for (int spb : {128, 512}) {
         ft.ungrid_G = G;
         ft.ungrid_spb = spb;
@@ -1299,7 +1338,7 @@ mrg_status autotune_frame(const GridConst &gc, FrameTraj &ft, float2 *grid, floa
   ft.ungrid_cpl = bestP;
   ft.ungrid_uy = 1;
   int bestU = 1;
-  if (bestG >= 4) {
+  if (bestG >= 4 && bestP < 4) {
     for (int uy : {2, 3}) {
       ft.ungrid_uy = uy;
       const float ms = time_ms(st, [&]() { return launch_ungrid(gc, ft, grid, nullptr, y, false, st); }, 2);

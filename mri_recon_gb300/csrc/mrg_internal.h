@@ -175,6 +175,8 @@ BlockShape region_shape(const GridConst &gc);
 void pair_set_free(PairSet &ps);
 // tcgen05 gridding over 8x4x4 regions (grid_umma.cu): cc = coils per pass (8, 16 or 32)
 bool umma_supported(int C);
+// a gridding launch shape (mrg_frame_tuning's encoding) that the frame's kernels can run
+bool grid_cc_allowed(int C, const FrameTraj &ft, int cc);
 int umma_default_cc(int C);
 mrg_status launch_grid_umma(const GridConst &gc, const FrameTraj &ft, int cc, const float2 *yw, float2 *grid,
                             cudaStream_t st);

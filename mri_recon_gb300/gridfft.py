@@ -146,6 +146,13 @@ class Plan:
         return dict(ungrid_lanes=out[0], ungrid_samples_per_cta=out[1], grid_coils_per_pass=out[2],
                     ungrid_coils_per_lane=out[3], ungrid_rows_per_step=out[4], ungrid_ms=ms[0], grid_ms=ms[1])
 
+    def set_frame_tuning(self, frame, ungrid_lanes, ungrid_samples_per_cta, grid_coils_per_pass,
+                         ungrid_coils_per_lane, ungrid_rows_per_step=1):
+        """Fixes a frame's launch shapes (the fields of frame_tuning) in place of the autotuner's."""
+        v = (ctypes.c_int * 5)(ungrid_lanes, ungrid_samples_per_cta, grid_coils_per_pass, ungrid_coils_per_lane,
+                               ungrid_rows_per_step)
+        _lib.check(_lib.load().mrg_frame_set_tuning(self._h, frame, v))
+
     def set_data(self, frame, data, stream=None):
         """data: (C, M) complex64."""
         a = _Args()

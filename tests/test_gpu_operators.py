@@ -206,3 +206,30 @@ def test_edge_samples_tensor_core_gridding(mrg_lib, oracle_lib):
     X = torch.zeros(c["X"].shape, dtype=torch.complex64, device="cuda")
     p.adjoint(0, torch.from_numpy(c["data"]).cuda(), X)
     assert rel(X.cpu().numpy(), _oracle_EH(oracle_lib, c, 1)) < TOL
+
+
+@pytest.mark.parametrize("C,G,cpl,uy", [(32, 8, 4, 1), (32, 4, 4, 1), (20, 16, 4, 1), (32, 16, 2, 3),
+                                        (12, 4, 1, 2), (32, 32, 1, 1), (6, 8, 4, 1)])
+def test_forward_each_ungrid_shape(mrg_lib, oracle_lib, C, G, cpl, uy):
+    """Every ungridding variant, fixed through mrg_frame_set_tuning: lanes per sample,
+    1, 2 or 4 coils per lane (8-, 16- and 32-byte gathers) and tap rows per step; with
+    6 coils the 4-per-lane request falls back to 2 per lane."""
+    torch = _torch()
+    c = case(N=32, C=C, nproj=500)
+    p = _plan(mrg_lib, c)
+    t = p.frame_tuning(0)
+    p.set_frame_tuning(0, G, 128, t["grid_coils_per_pass"], cpl, uy)
+    assert p.frame_tuning(0)["ungrid_lanes"] == G
+    y = p.forward(0, torch.from_numpy(c["X"]).cuda()).cpu().numpy()
+    assert rel(y, _oracle_E(oracle_lib, c, 0)) < TOL
+
+
+def test_set_frame_tuning_rejects_unavailable_shapes(mrg_lib):
+    c = case(N=32, C=4, nproj=300)
+    p = _plan(mrg_lib, c)
+    t = p.frame_tuning(0)
+    for bad in [(3, 128, 0, 1, 1), (8, 0, 0, 1, 1), (8, 128, 0, 3, 1), (8, 128, 0, 1, 4),
+                (8, 128, -8, 1, 1), (8, 128, -116, 1, 1), (8, 128, 12, 1, 1)]:
+        with pytest.raises(mrg_lib.MrgError):
+            p.set_frame_tuning(0, *bad)
+    assert p.frame_tuning(0) == t
