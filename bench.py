@@ -90,6 +90,9 @@ STAGES = ["E_xfft_setimg", "E_zfft", "E_yfft", "E_ungrid", "EH_grid", "EH_yfft",
 def kernel_of(stage, tuning, C):
     """Kernel that runs a stage, with the launch shape the autotuner picked."""
     if stage == "E_ungrid":
+        if tuning["ungrid_lanes"] < 0:
+            return "k_ungrid_mma<%d> (mma.sync TF32, 16 samples per warp, %d coils per pass)" % (
+                -tuning["ungrid_lanes"], -4 * tuning["ungrid_lanes"])
         return "k_ungrid<%d,%d,%d>" % (tuning["ungrid_lanes"], max(tuning["ungrid_coils_per_lane"], 1),
                                       max(tuning.get("ungrid_rows_per_step", 1), 1))
     if stage == "EH_grid":
@@ -390,11 +393,12 @@ def run_ours(a):
     sm_mhz = (clocks or {}).get("sm_mhz") or 2070.0
     l1_peak = 152 * 128 * sm_mhz * 1e6 / 1e9
     gather = fi["ntaps"] * C * 8
-    roofline["ungrid_l1_gather"] = {"bytes_per_launch": gather, "achieved": gather / (per_launch_ms["E_ungrid"] / 1e3) / 1e9,
-                                    "peak": l1_peak, "unit": "GB/s",
-                                    "frac": gather / (per_launch_ms["E_ungrid"] / 1e3) / 1e9 / l1_peak,
-                                    "peak_source": "nominal 128 B/clk/SM x 152 SMs at the sampled SM clock",
-                                    "taps_per_sample": fi["ntaps"] / max(fi["nvalid"], 1)}
+    if out_tuning["ungrid_lanes"] > 0:  # the CUDA-core kernel (the tensor-core one loads each value once per 16 samples)
+        roofline["ungrid_l1_gather"] = {"bytes_per_launch": gather, "achieved": gather / (per_launch_ms["E_ungrid"] / 1e3) / 1e9,
+                                        "peak": l1_peak, "unit": "GB/s",
+                                        "frac": gather / (per_launch_ms["E_ungrid"] / 1e3) / 1e9 / l1_peak,
+                                        "peak_source": "nominal 128 B/clk/SM x 152 SMs at the sampled SM clock",
+                                        "taps_per_sample": fi["ntaps"] / max(fi["nvalid"], 1)}
     iteration_roofline = {"bytes_per_iter": iter_bytes, "achieved_GBs": iter_bytes * value / world / 1e9,
                           "frac": iter_bytes * value / world / 1e9 / peak, "peak_source": peak_kind,
                           "stage_ms": per_launch_ms}

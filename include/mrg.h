@@ -110,7 +110,8 @@ mrg_status mrg_frame_info(const mrg_plan *plan, int frame, int64_t *M, int64_t *
                           int64_t *nitems, int64_t *ntaps);
 
 /* Launch shapes the autotuner chose for a frame (mrg_config.tile == 0): out = {ungrid lanes
- * per sample, ungrid samples per CTA, gridding coils per pass (0: all; -n with n < 100: the
+ * per sample (-n: the tensor-core kernel, 16 samples per warp, 4n coils per pass), ungrid
+ * samples per CTA, gridding coils per pass (0: all; -n with n < 100: the
  * mma.sync kernel with 4n coils per pass; -(100 + c): the tcgen05 kernel with c coils per
  * pass), ungrid coils per lane, ungrid tap rows loaded per step};
  * ms = the timed ungrid and grid kernels. */

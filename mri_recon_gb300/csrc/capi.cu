@@ -834,7 +834,8 @@ mrg_status mrg_frame_set_tuning(mrg_plan *p, int frame, const int in[5]) {
   }
   FrameTraj &ft = p->frames[frame];
   const int G = in[0], spb = in[1], cc = in[2], cpl = in[3], uy = in[4];
-  const bool g_ok = (G == 1 || G == 2 || G == 4 || G == 8 || G == 16 || G == 32);
+  const bool g_ok = (G == 1 || G == 2 || G == 4 || G == 8 || G == 16 || G == 32) ||
+                    ((G == -1 || G == -2 || G == -4 || G == -8) && p->C % (-4 * G) == 0);
   if (!g_ok || spb < 1 || !(cpl == 1 || cpl == 2 || cpl == 4) || uy < 1 || uy > 3) {
     set_error("ungridding launch shape out of range");
     return MRG_ERR_INVALID;

@@ -22,6 +22,7 @@
 // split across several work items (the dense k-space centre) add with global
 // atomics into a block zeroed beforehand.
 #include <algorithm>
+#include <climits>
 #include <functional>
 
 #include "mrg_internal.h"
@@ -602,9 +603,18 @@ static int ungrid_group_default(int C) {
   return G;
 }
 
+static mrg_status launch_ungrid_mma(int NT, const GridConst &gc, const FrameTraj &ft, const float2 *grid,
+                                    const float2 *diff, float2 *y, bool weigh, cudaStream_t st);
+
 mrg_status launch_ungrid(const GridConst &gc, const FrameTraj &ft, const float2 *grid, const float2 *diff, float2 *y,
                          bool weigh, cudaStream_t st) {
   if (ft.nvalid == 0) return MRG_OK;
+  // tensor-core kernel: ungrid_G = -(n-tiles per pass); needs its alignments, else the default shape
+  if (ft.ungrid_G < 0) {
+    const int NT = -ft.ungrid_G;
+    if (gc.C % (4 * NT) == 0 && ((uintptr_t)grid & 31) == 0 && ((uintptr_t)y & 15) == 0 && ((uintptr_t)diff & 15) == 0)
+      return launch_ungrid_mma(NT, gc, ft, grid, diff, y, weigh, st);
+  }
   int G = ft.ungrid_G > 0 ? ft.ungrid_G : ungrid_group_default(gc.C);
   // two coils per lane (16-byte loads) when the coil count is even and the buffers allow it,
   // four (32-byte loads) when it is a multiple of 4
@@ -1083,6 +1093,215 @@ static mrg_status launch_grid_mma(const GridConst &gc, const FrameTraj &ft, cons
   return MRG_OK;
 }
 
+// ---------------------------------------------------------------------------
+// ungridding on the tensor cores (mma.sync m16n8k8, TF32 in three terms)
+//
+// A warp takes 16 consecutive samples of the sorted order (neighbours in space) and
+// walks the union of their tap windows one row of 8 x-points at a time; each row is
+// one k-step
+//   D[16 samples][8 NT values] += W[16 samples][8 points] G[8 points][8 NT values],
+// W the samples' 3D tap weights wx wy wz (zero outside a sample's window) and G the
+// interleaved complex coil values of this pass's 4 NT coils at the row's 8 points.
+// Every grid value is loaded once per 16 samples instead of once per sample (the
+// CUDA-core kernel is bound by those L1 gathers).  Column n of n-tile j stands for
+// value NT n + j of a point, so a lane loads NT consecutive floats of a point for B
+// and ends with 2 NT consecutive floats (NT whole coils) of each of its two samples.
+// Products are split into TF32 high and low parts (hi = x with the low 13 mantissa
+// bits cleared, lo = x - hi, exact); lo's own low bits are dropped by the tensor core,
+// so each product carries a relative error near 2^-21.  Each row starts its D from
+// zero and is added to the FP32 accumulators with round-to-nearest adds: the tensor
+// core's accumulation rounds towards zero, which over a whole window biases the sum.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void split_tf32_trunc(float x, uint32_t &hi, uint32_t &lo) {
+  hi = __float_as_uint(x) & 0xffffe000u;
+  lo = __float_as_uint(x - __uint_as_float(hi));
+}
+
+template <int NT>
+struct UmVec {
+  float v[NT];
+};
+template <int NT>
+__device__ __forceinline__ void um_load(UmVec<NT> &r, const float *p) {
+  if constexpr (NT == 8) {
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(r.v[0]), "=f"(r.v[1]), "=f"(r.v[2]), "=f"(r.v[3]), "=f"(r.v[4]), "=f"(r.v[5]), "=f"(r.v[6]),
+          "=f"(r.v[7])
+        : "l"(p));
+  } else if constexpr (NT == 4) {
+    const float4 q = __ldg(reinterpret_cast<const float4 *>(p));
+    r.v[0] = q.x, r.v[1] = q.y, r.v[2] = q.z, r.v[3] = q.w;
+  } else if constexpr (NT == 2) {
+    const float2 q = __ldg(reinterpret_cast<const float2 *>(p));
+    r.v[0] = q.x, r.v[1] = q.y;
+  } else {
+    r.v[0] = __ldg(p);
+  }
+}
+
+// weight i of a sample's axis table (n taps; zero outside the window)
+__device__ __forceinline__ float um_w(const float *w, int i, int n) { return (i >= 0 && i < n) ? __ldg(w + i) : 0.f; }
+
+template <int NT>
+__global__ void __launch_bounds__(256, 2)
+    k_ungrid_mma(const GridConst g, int nvalid, int spb, const float4 *__restrict__ swt, const int4 *__restrict__ sst,
+                 const float4 *__restrict__ spos, const float *__restrict__ stap, const float2 *__restrict__ grid,
+                 const float2 *__restrict__ diff, float2 *__restrict__ y, int weigh) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int gq = lane >> 2, tq = lane & 3;
+  const int C = g.C;
+  const int c0 = blockIdx.y * 4 * NT;  // first coil of this pass
+  const int64_t ps = 2 * (int64_t)C;   // floats per grid point
+  const int64_t ys = (int64_t)g.S[0] * ps, zs = (int64_t)g.S[1] * ys;
+  const float *gbase = reinterpret_cast<const float *>(grid) + 2 * c0 + NT * gq;
+  const int64_t s_begin = (int64_t)blockIdx.x * spb;
+  const int64_t s_end = min((int64_t)nvalid, s_begin + spb);
+  for (int64_t s0 = s_begin + 16 * warp; s0 < s_end; s0 += 16 * 8) {
+    // lanes l and l + 16 describe sample s0 + l; samples past the end have empty windows
+    const int64_t sl = s0 + (lane & 15);
+    int4 t = make_int4(0, 0, 0, 0);
+    int nx = 0, ny = 0, nz = 0;
+    if (sl < s_end) {
+      t = __ldg(sst + sl);
+      nx = t.w & 15, ny = (t.w >> 4) & 15, nz = (t.w >> 8) & 15;
+    }
+    const bool live = sl < s_end;
+    const int x0 = __reduce_min_sync(0xffffffffu, live ? t.x : INT_MAX);
+    const int x1 = __reduce_max_sync(0xffffffffu, live ? t.x + nx : INT_MIN);
+    const int y0 = __reduce_min_sync(0xffffffffu, live ? t.y : INT_MAX);
+    const int y1 = __reduce_max_sync(0xffffffffu, live ? t.y + ny : INT_MIN);
+    const int z0 = __reduce_min_sync(0xffffffffu, live ? t.z : INT_MAX);
+    const int z1 = __reduce_max_sync(0xffffffffu, live ? t.z + nz : INT_MIN);
+    // this lane's two samples: rows gq and gq + 8 of the fragments
+    int sx[2], sy[2], sz[2], cx[2], cy[2], cz[2];
+    const float *wt[2];
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const int src = gq + 8 * h;
+      sx[h] = __shfl_sync(0xffffffffu, t.x, src);
+      sy[h] = __shfl_sync(0xffffffffu, t.y, src);
+      sz[h] = __shfl_sync(0xffffffffu, t.z, src);
+      cx[h] = __shfl_sync(0xffffffffu, nx, src);
+      cy[h] = __shfl_sync(0xffffffffu, ny, src);
+      cz[h] = __shfl_sync(0xffffffffu, nz, src);
+      wt[h] = reinterpret_cast<const float *>(swt + 6 * (s0 + src));
+    }
+    float acc[NT][4];
+#pragma unroll
+    for (int j = 0; j < NT; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+    const int nyu = y1 - y0, nrows = nyu * (z1 - z0);
+    for (int xb = x0; xb < x1; xb += 8) {
+      // a0 = W[gq][tq], a1 = W[gq+8][tq], a2 = W[gq][tq+4], a3 = W[gq+8][tq+4]
+      const float wx0 = um_w(wt[0], xb + tq - sx[0], cx[0]), wx1 = um_w(wt[1], xb + tq - sx[1], cx[1]);
+      const float wx2 = um_w(wt[0], xb + tq + 4 - sx[0], cx[0]), wx3 = um_w(wt[1], xb + tq + 4 - sx[1], cx[1]);
+      // points past the grid's edge carry zero weight: load a point that exists instead
+      const int xa = min(xb + tq, g.S[0] - 1), xc = min(xb + tq + 4, g.S[0] - 1);
+      const float *pa = gbase + xa * ps, *pc = gbase + xc * ps;
+      UmVec<NT> ba, bc, na, nc;
+      um_load<NT>(ba, pa + z0 * zs + y0 * ys);
+      um_load<NT>(bc, pc + z0 * zs + y0 * ys);
+      int yy = y0, zz = z0;
+      for (int r = 0; r < nrows; r++) {
+        // next row's values in flight while this one is multiplied
+        int yn = yy + 1, zn = zz;
+        if (yn == y1) yn = y0, zn++;
+        if (r + 1 < nrows) {
+          um_load<NT>(na, pa + zn * zs + yn * ys);
+          um_load<NT>(nc, pc + zn * zs + yn * ys);
+        }
+        const float wyz0 = um_w(wt[0] + 16, zz - sz[0], cz[0]) * um_w(wt[0] + 8, yy - sy[0], cy[0]);
+        const float wyz1 = um_w(wt[1] + 16, zz - sz[1], cz[1]) * um_w(wt[1] + 8, yy - sy[1], cy[1]);
+        uint32_t ah[4], al[4];
+        split_tf32_trunc(wx0 * wyz0, ah[0], al[0]);
+        split_tf32_trunc(wx1 * wyz1, ah[1], al[1]);
+        split_tf32_trunc(wx2 * wyz0, ah[2], al[2]);
+        split_tf32_trunc(wx3 * wyz1, ah[3], al[3]);
+#pragma unroll
+        for (int j = 0; j < NT; j++) {
+          uint32_t bh0, bl0, bh1, bl1;
+          split_tf32_trunc(ba.v[j], bh0, bl0);
+          split_tf32_trunc(bc.v[j], bh1, bl1);
+          float d[4];
+          mma_tf32_z(d, al, bh0, bh1);
+          mma_tf32(d, ah, bl0, bl1);
+          mma_tf32(d, ah, bh0, bh1);
+#pragma unroll
+          for (int i = 0; i < 4; i++) acc[j][i] = __fadd_rn(acc[j][i], d[i]);
+        }
+        ba = na;
+        bc = nc;
+        yy = yn;
+        zz = zn;
+      }
+    }
+    // lane holds values [2 NT tq, 2 NT tq + 2 NT) of rows gq and gq + 8: value m < NT is
+    // column 2 tq of n-tile m, value NT + m column 2 tq + 1 of n-tile m
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const int64_t s = s0 + gq + 8 * h;
+      if (s >= s_end) continue;
+      float kw = 0.f, tp = 0.f;
+      if (weigh) {
+        kw = __ldg(&spos[s].w);
+        tp = __ldg(stap + s);
+      }
+      float v[2 * NT];
+#pragma unroll
+      for (int m = 0; m < NT; m++) {
+        v[m] = acc[m][2 * h];
+        v[NT + m] = acc[m][2 * h + 1];
+      }
+      const int64_t o = s * C + c0 + NT * tq;
+#pragma unroll
+      for (int q = 0; q < NT; q++) {
+        float2 r = make_float2(v[2 * q], v[2 * q + 1]);
+        if (diff) {
+          const float2 dd = diff[o + q];
+          r.x -= dd.x;
+          r.y -= dd.y;
+        }
+        if (weigh)  // temp = data * kw; temp *= taper  (src/gridFFT.cpp:1039-1108)
+          r = make_float2(__fmul_rn(__fmul_rn(r.x, kw), tp), __fmul_rn(__fmul_rn(r.y, kw), tp));
+        v[2 * q] = r.x;
+        v[2 * q + 1] = r.y;
+      }
+      if constexpr (NT >= 2) {
+#pragma unroll
+        for (int q = 0; q < NT; q += 2)
+          *reinterpret_cast<float4 *>(y + o + q) = make_float4(v[2 * q], v[2 * q + 1], v[2 * q + 2], v[2 * q + 3]);
+      } else {
+        y[o] = make_float2(v[0], v[1]);
+      }
+    }
+  }
+}
+
+// n-tiles per pass of the tensor-core ungridding kernel (0: not available for C coils)
+int ungrid_mma_nt(int C) {
+  if (C % 32 == 0) return 8;
+  if (C % 16 == 0) return 4;
+  if (C % 8 == 0) return 2;
+  if (C % 4 == 0) return 1;
+  return 0;
+}
+
+static mrg_status launch_ungrid_mma(int NT, const GridConst &gc, const FrameTraj &ft, const float2 *grid,
+                                    const float2 *diff, float2 *y, bool weigh, cudaStream_t st) {
+  const int spb = ft.ungrid_spb > 0 ? ft.ungrid_spb : 512;
+  const dim3 blocks((unsigned)((ft.nvalid + spb - 1) / spb), (unsigned)(gc.C / (4 * NT)));
+  const int wf = weigh ? 1 : 0;
+#define UMMA_ARGS gc, ft.nvalid, spb, ft.swt, ft.sst, ft.spos, ft.stap, grid, diff, y, wf
+  switch (NT) {
+    case 8: k_ungrid_mma<8><<<blocks, 256, 0, st>>>(UMMA_ARGS); break;
+    case 4: k_ungrid_mma<4><<<blocks, 256, 0, st>>>(UMMA_ARGS); break;
+    case 2: k_ungrid_mma<2><<<blocks, 256, 0, st>>>(UMMA_ARGS); break;
+    default: k_ungrid_mma<1><<<blocks, 256, 0, st>>>(UMMA_ARGS); break;
+  }
+#undef UMMA_ARGS
+  MRG_LAUNCHED();
+  return MRG_OK;
+}
+
 // n-tiles (4 coils each) per pass of the tensor-core kernel when none was tuned.
 static int default_grid_nt(int C) { return C > 16 ? 8 : (C > 8 ? 4 : (C > 4 ? 2 : 1)); }
 
@@ -1349,6 +1568,29 @@ mrg_status autotune_frame(const GridConst &gc, FrameTraj &ft, float2 *grid, floa
     }
   }
   ft.ungrid_uy = bestU;
+  // tensor-core kernel: wins only where samples are dense (16 consecutive samples share most
+  // of their windows, e.g. 1.86 against 2.5 ms at 128^3 x 32 with every spoke inside |k| < 8);
+  // for a full 3D radial trajectory it is several times slower (windows spread apart)
+  if (const int nt = ungrid_mma_nt(gc.C)) {
+    const int keepG = ft.ungrid_G, keepS = ft.ungrid_spb, keepP = ft.ungrid_cpl, keepU = ft.ungrid_uy;
+    int mmaS = 0;
+    for (int spb : {256}) {
+      ft.ungrid_G = -nt;
+      ft.ungrid_spb = spb;
+      ft.ungrid_cpl = 1;
+      ft.ungrid_uy = 1;
+      const float ms = time_ms(st, [&]() { return launch_ungrid(gc, ft, grid, nullptr, y, false, st); }, 2);
+      if (ms < best) {
+        best = ms;
+        mmaS = spb;
+      }
+    }
+    if (mmaS) {
+      ft.ungrid_spb = mmaS;
+    } else {
+      ft.ungrid_G = keepG, ft.ungrid_spb = keepS, ft.ungrid_cpl = keepP, ft.ungrid_uy = keepU;
+    }
+  }
   ft.tune_ungrid_ms = best;
   best = 1e30f;
   int bestCC = 0;

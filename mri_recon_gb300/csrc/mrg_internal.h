@@ -177,6 +177,8 @@ void pair_set_free(PairSet &ps);
 bool umma_supported(int C);
 // a gridding launch shape (mrg_frame_tuning's encoding) that the frame's kernels can run
 bool grid_cc_allowed(int C, const FrameTraj &ft, int cc);
+// n-tiles (4 coils each) per pass of the tensor-core ungridding kernel; 0: needs C % 4 == 0
+int ungrid_mma_nt(int C);
 int umma_default_cc(int C);
 mrg_status launch_grid_umma(const GridConst &gc, const FrameTraj &ft, int cc, const float2 *yw, float2 *grid,
                             cudaStream_t st);

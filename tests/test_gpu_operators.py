@@ -209,26 +209,49 @@ def test_edge_samples_tensor_core_gridding(mrg_lib, oracle_lib):
 
 
 @pytest.mark.parametrize("C,G,cpl,uy", [(32, 8, 4, 1), (32, 4, 4, 1), (20, 16, 4, 1), (32, 16, 2, 3),
-                                        (12, 4, 1, 2), (32, 32, 1, 1), (6, 8, 4, 1)])
+                                        (12, 4, 1, 2), (32, 32, 1, 1), (6, 8, 4, 1),
+                                        (32, -8, 1, 1), (32, -4, 1, 1), (64, -8, 1, 1), (16, -4, 1, 1),
+                                        (8, -2, 1, 1), (20, -1, 1, 1)])
 def test_forward_each_ungrid_shape(mrg_lib, oracle_lib, C, G, cpl, uy):
     """Every ungridding variant, fixed through mrg_frame_set_tuning: lanes per sample,
     1, 2 or 4 coils per lane (8-, 16- and 32-byte gathers) and tap rows per step; with
-    6 coils the 4-per-lane request falls back to 2 per lane."""
+    6 coils the 4-per-lane request falls back to 2 per lane.  Negative lanes: the
+    tensor-core kernel with 4 |G| coils per pass (one or more passes)."""
     torch = _torch()
     c = case(N=32, C=C, nproj=500)
     p = _plan(mrg_lib, c)
     t = p.frame_tuning(0)
-    p.set_frame_tuning(0, G, 128, t["grid_coils_per_pass"], cpl, uy)
+    p.set_frame_tuning(0, G, 128 if G > 0 else 256, t["grid_coils_per_pass"], cpl, uy)
     assert p.frame_tuning(0)["ungrid_lanes"] == G
     y = p.forward(0, torch.from_numpy(c["X"]).cuda()).cpu().numpy()
-    assert rel(y, _oracle_E(oracle_lib, c, 0)) < TOL
+    r32, r64 = _oracle_E(oracle_lib, c, 0), _oracle_E(oracle_lib, c, 1)
+    assert rel(y, r32) < TOL
+    assert rel(y, r64) < fp64_bound(r32, r64)
+
+
+@pytest.mark.parametrize("spb", [16, 100, 1024])
+def test_tensor_core_ungrid_residual_and_normal(mrg_lib, oracle_lib, spb):
+    """The tensor-core ungridding kernel on the residual (E x - data) and inside the
+    normal operator (samples weighted by kw and the taper), with sample ranges per CTA
+    that end inside a 16-sample group."""
+    torch = _torch()
+    c = case(N=32, C=8, nproj=700)
+    p = _plan(mrg_lib, c)
+    t = p.frame_tuning(0)
+    p.set_frame_tuning(0, -2, spb, t["grid_coils_per_pass"], 1, 1)
+    y = p.forward(0, torch.from_numpy(c["X"]).cuda(), diff=torch.from_numpy(c["data"]).cuda()).cpu().numpy()
+    assert rel(y, _oracle_E(oracle_lib, c, 0, diff=c["data"])) < TOL
+    got = p.normal(0, torch.from_numpy(c["X"]).cuda()).cpu().numpy()
+    O = oracle_lib.Plan(32, prec=1)
+    fr = [dict(kx=c["kx"], ky=c["ky"], kz=c["kz"], kw=c["kw"], data=c["data"])]
+    assert rel(got, O.normal(fr, c["smaps"], 0, c["X"])) < TOL
 
 
 def test_set_frame_tuning_rejects_unavailable_shapes(mrg_lib):
     c = case(N=32, C=4, nproj=300)
     p = _plan(mrg_lib, c)
     t = p.frame_tuning(0)
-    for bad in [(3, 128, 0, 1, 1), (8, 0, 0, 1, 1), (8, 128, 0, 3, 1), (8, 128, 0, 1, 4),
+    for bad in [(3, 128, 0, 1, 1), (8, 0, 0, 1, 1), (8, 128, 0, 3, 1), (8, 128, 0, 1, 4), (-2, 128, 0, 1, 1),
                 (8, 128, -8, 1, 1), (8, 128, -116, 1, 1), (8, 128, 12, 1, 1)]:
         with pytest.raises(mrg_lib.MrgError):
             p.set_frame_tuning(0, *bad)
