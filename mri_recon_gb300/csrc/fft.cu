@@ -148,22 +148,38 @@ __device__ __forceinline__ float elem_weight(const FftPass &p, float lw, float w
   return (wl_l * p.wo[o]) * p.wi[i / p.C];         // (winz * winy) * winx along z
 }
 
-template <int Q, int SIGN, int MODE>
+// P: shared-memory row pitch when it is a compile-time constant (IB = P lines, no
+// padding), else 0 (pitch and IB from the pass).  With P fixed every shared-memory
+// address in the transform steps is the thread's base plus a constant.
+template <int Q, int SIGN, int MODE, int P>
 __global__ void __launch_bounds__(256, 2) k_fft(const FftPass p) {
   constexpr int S = 8 * Q;
-  extern __shared__ float2 sm[];  // [S][IB+1] data, then S twiddles
-  const int IB = p.IB, IBp = p.lfast ? p.IB + 1 : p.IB;  // pad only for column-wise (contiguous-line) access
+  extern __shared__ float2 sm[];  // [S][IBp] data, then S twiddles
+  const int IB = P ? P : p.IB;
+  const int IBp = P ? P : (p.lfast ? p.IB + 1 : p.IB);  // pad only for column-wise (contiguous-line) access
   const int tid = threadIdx.x;
-  float2 *tw = sm + S * (p.IB + 1);
+  float2 *tw = sm + S * (IB + 1);
   for (int m = tid; m < S; m += blockDim.x) tw[m] = p.tw[m];
   const int j = tid % IB, t = tid / IB;  // 8 threads per line
+  // Line (o, i) of the CTA's IB lines.  When inner % IB == 0 (nib = inner / IB) every line
+  // of the CTA shares o and one 32-bit division per thread finds it.
+  int64_t o0 = 0, i0 = 0;
+  if (p.nib) {
+    const unsigned b = blockIdx.x, ob = b / (unsigned)p.nib;
+    o0 = ob;
+    i0 = (int64_t)(b - ob * (unsigned)p.nib) * IB;
+  }
   const int64_t line = (int64_t)blockIdx.x * IB + j;
   const bool lv = line < p.nlines;
   int64_t o = 0, i = 0;
-  if (lv) {
+  if (p.nib) {
+    o = o0;
+    i = i0 + j;
+  } else if (lv) {
     o = line / p.inner;
     i = line - o * p.inner;
   }
+  float2 *col = sm + j;  // this thread's column
 
   // ---- load (zero rows outside [in_off, in_off + Lin)) ----
   if (p.vec16 && !(MODE == FFT_SETIMG && !p.has_smap)) {
@@ -173,20 +189,24 @@ __global__ void __launch_bounds__(256, 2) k_fft(const FftPass p) {
     const int64_t ln = (int64_t)blockIdx.x * IB + 2 * jp;
     const bool pv = ln < p.nlines;
     int64_t po = 0, pi = 0;
-    if (pv) {
+    if (p.nib) {
+      po = o0;
+      pi = i0 + 2 * jp;
+    } else if (pv) {
       po = ln / p.inner;
       pi = ln - po * p.inner;
     }
     const float2 *src = (MODE == FFT_SETIMG) ? p.smap : p.in;
-    const float2 *gb = src + po * p.in_os + pi;
-    for (int li = r0; li < p.Lin; li += rstep) {
-      float2 *dst = sm + (li + p.in_off) * IBp + 2 * jp;
-      if (pv) {
-        const unsigned sa = (unsigned)__cvta_generic_to_shared(dst);
-        asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gb + (int64_t)li * p.in_ls));
-      } else {
-        *reinterpret_cast<float4 *>(dst) = make_float4(0.f, 0.f, 0.f, 0.f);
-      }
+    const float2 *gs = src + po * p.in_os + pi + (int64_t)r0 * p.in_ls;
+    const int64_t gstep = (int64_t)rstep * p.in_ls;
+    unsigned sa = (unsigned)__cvta_generic_to_shared(sm + (r0 + p.in_off) * IBp + 2 * jp);
+    const unsigned sstep = (unsigned)(rstep * IBp * (int)sizeof(float2));
+    if (pv) {
+      for (int li = r0; li < p.Lin; li += rstep, gs += gstep, sa += sstep)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gs));
+    } else {
+      for (int li = r0; li < p.Lin; li += rstep)
+        *reinterpret_cast<float4 *>(sm + (li + p.in_off) * IBp + 2 * jp) = make_float4(0.f, 0.f, 0.f, 0.f);
     }
     for (int e = tid; e < (S - p.Lin) * IB; e += blockDim.x) {
       const int jj = e % IB, k = e / IB;
@@ -218,7 +238,7 @@ __global__ void __launch_bounds__(256, 2) k_fft(const FftPass p) {
             const int li = l0 + 8 * k;
             if (li < p.Lin) {
               const float w = elem_weight(p, lw, wv[k], o, i);
-              float2 *d = sm + (li + p.in_off) * IBp + j;
+              float2 *d = col + (li + p.in_off) * IBp;
               *d = cmul(make_float2(w * xv[k].x, w * xv[k].y), *d);
             }
           }
@@ -243,7 +263,7 @@ __global__ void __launch_bounds__(256, 2) k_fft(const FftPass p) {
           v = p.in[off];
         }
       }
-      sm[r * IBp + j] = v;
+      col[r * IBp] = v;
     }
     __syncthreads();
   } else {
@@ -263,25 +283,28 @@ __global__ void __launch_bounds__(256, 2) k_fft(const FftPass p) {
   // ---- step A: 8-point DFTs over n1 (rows Q*n1 + n2), twiddle W_S^(n2*k1) ----
   for (int n2 = t; n2 < Q; n2 += 8) {
     float2 a[8];
+    float2 *c2 = col + n2 * IBp;
 #pragma unroll
-    for (int n1 = 0; n1 < 8; n1++) a[n1] = sm[(Q * n1 + n2) * IBp + j];
+    for (int n1 = 0; n1 < 8; n1++) a[n1] = c2[Q * n1 * IBp];
     reg_fft<8, SIGN, S>(a, tw);
 #pragma unroll
     for (int k1 = 1; k1 < 8; k1++) a[k1] = cmul(a[k1], twid<SIGN>(tw, n2 * k1));
 #pragma unroll
-    for (int k1 = 0; k1 < 8; k1++) sm[(Q * k1 + n2) * IBp + j] = a[k1];
+    for (int k1 = 0; k1 < 8; k1++) c2[Q * k1 * IBp] = a[k1];
   }
   __syncthreads();
 
   // ---- step C: Q-point DFT of rows Q*t .. Q*t+Q-1 -> rows t + 8*k2 ----
   {
     float2 v[Q];
+    const float2 *cq = col + Q * t * IBp;
 #pragma unroll
-    for (int n2 = 0; n2 < Q; n2++) v[n2] = sm[(Q * t + n2) * IBp + j];
+    for (int n2 = 0; n2 < Q; n2++) v[n2] = cq[n2 * IBp];
     reg_fft<Q, SIGN, S>(v, tw);
     __syncthreads();
+    float2 *ct = col + t * IBp;
 #pragma unroll
-    for (int k2 = 0; k2 < Q; k2++) sm[(t + 8 * k2) * IBp + j] = v[k2];
+    for (int k2 = 0; k2 < Q; k2++) ct[8 * k2 * IBp] = v[k2];
   }
   __syncthreads();
 
@@ -292,20 +315,30 @@ __global__ void __launch_bounds__(256, 2) k_fft(const FftPass p) {
       const int jp = tid % npair, r0 = tid / npair, rstep = blockDim.x / npair;
       const int64_t ln = (int64_t)blockIdx.x * IB + 2 * jp;
       if (ln < p.nlines) {
-        const int64_t po = ln / p.inner, pi = ln - po * p.inner;
-        float4 *ob = reinterpret_cast<float4 *>(p.out + po * p.out_os + pi);
-        const int64_t ls4 = p.out_ls / 2;
+        int64_t po, pi;
+        if (p.nib) {
+          po = o0;
+          pi = i0 + 2 * jp;
+        } else {
+          po = ln / p.inner;
+          pi = ln - po * p.inner;
+        }
+        float4 *ob = reinterpret_cast<float4 *>(p.out + po * p.out_os + pi + (int64_t)r0 * p.out_ls);
+        const int64_t ostep = (int64_t)rstep * (p.out_ls / 2);
+        const float4 *sv = reinterpret_cast<const float4 *>(sm + (r0 + p.out_off) * IBp + 2 * jp);
+        const int svstep = rstep * IBp / 2;
+        const float sc = p.scale;
 #pragma unroll 4
-        for (int r = r0; r < p.Lout; r += rstep) {
-          const float4 v = *reinterpret_cast<const float4 *>(sm + (r + p.out_off) * IBp + 2 * jp);
-          ob[(int64_t)r * ls4] = make_float4(v.x * p.scale, v.y * p.scale, v.z * p.scale, v.w * p.scale);
+        for (int r = r0; r < p.Lout; r += rstep, ob += ostep, sv += svstep) {
+          const float4 v = *sv;
+          *ob = make_float4(v.x * sc, v.y * sc, v.z * sc, v.w * sc);
         }
       }
     } else if (!p.lfast) {
       if (lv) {
         const int64_t ob = o * p.out_os + i;
         for (int r = t; r < p.Lout; r += 8) {
-          float2 v = sm[(r + p.out_off) * IBp + j];
+          float2 v = col[(r + p.out_off) * IBp];
           p.out[ob + (int64_t)r * p.out_ls] = make_float2(v.x * p.scale, v.y * p.scale);
         }
       }
@@ -341,7 +374,7 @@ __global__ void __launch_bounds__(256, 2) k_fft(const FftPass p) {
         for (int k = 0; k < 8; k++) {
           const int r = r0 + 8 * k;
           if (r >= p.Lout) continue;
-          float2 v = sm[(r + p.out_off) * IBp + j];
+          float2 v = col[(r + p.out_off) * IBp];
           v = make_float2(v.x * p.scale, v.y * p.scale);
           const float w = elem_weight(p, lw, wv[k], o, i);
           v = make_float2(w * v.x, w * v.y);
@@ -355,7 +388,7 @@ __global__ void __launch_bounds__(256, 2) k_fft(const FftPass p) {
             atomicAdd(&dst->x, v.x);
             atomicAdd(&dst->y, v.y);
           } else {
-            sm[(r + p.out_off) * IBp + j] = v;
+            col[(r + p.out_off) * IBp] = v;
           }
         }
       }
@@ -369,7 +402,14 @@ __global__ void __launch_bounds__(256, 2) k_fft(const FftPass p) {
         const int g = e % G, r = e / G;
         const int64_t ln = line0 + (int64_t)g * C;
         if (ln >= p.nlines) continue;
-        const int64_t oo = ln / p.inner, ii = ln - oo * p.inner;
+        int64_t oo, ii;
+        if (p.nib) {
+          oo = o0;
+          ii = i0 + (int64_t)g * C;
+        } else {
+          oo = ln / p.inner;
+          ii = ln - oo * p.inner;
+        }
         // rotated start (coil (c + r) mod C at step c): the rows of neighbouring threads sit
         // IBp apart, a multiple of the 32 banks, so the same coil index would hit one bank
         float2 s = make_float2(0.f, 0.f);
@@ -387,6 +427,27 @@ __global__ void __launch_bounds__(256, 2) k_fft(const FftPass p) {
   }
 }
 
+// Q values that get kernels with a compile-time pitch (lines of 192..384 points)
+constexpr bool fixed_pitch_q(int Q) { return Q >= 24; }
+
+template <int Q, int P>
+static mrg_status launch_qp(const FftPass &pp, const dim3 grid, const dim3 block, size_t smem, cudaStream_t st) {
+  void (*fn)(const FftPass);
+  if (pp.mode == FFT_SETIMG) fn = k_fft<Q, -1, FFT_SETIMG, P>;
+  else if (pp.mode == FFT_ACCUM) fn = k_fft<Q, +1, FFT_ACCUM, P>;
+  else if (pp.sign < 0) fn = k_fft<Q, -1, FFT_PLAIN, P>;
+  else fn = k_fft<Q, +1, FFT_PLAIN, P>;
+  static int attr_set[4] = {0, 0, 0, 0};  // per instantiation: set the smem cap once
+  const int slot = pp.mode == FFT_PLAIN ? (pp.sign < 0 ? 0 : 1) : (pp.mode == FFT_SETIMG ? 2 : 3);
+  if (!attr_set[slot]) {
+    MRG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 8 * Q * 34 * (int)sizeof(float2)));
+    attr_set[slot] = 1;
+  }
+  fn<<<grid, block, smem, st>>>(pp);
+  MRG_LAUNCHED();
+  return MRG_OK;
+}
+
 template <int Q>
 static mrg_status launch_q(const FftPass &p, cudaStream_t st) {
   const size_t smem = (size_t)8 * Q * (p.IB + 2) * sizeof(float2);
@@ -396,22 +457,15 @@ static mrg_status launch_q(const FftPass &p, cudaStream_t st) {
     return MRG_ERR_UNSUPPORTED;
   }
   const dim3 grid((unsigned)nblk64), block(8 * p.IB);
-  void (*fn)(const FftPass);
-  if (p.mode == FFT_SETIMG) fn = k_fft<Q, -1, FFT_SETIMG>;
-  else if (p.mode == FFT_ACCUM) fn = k_fft<Q, +1, FFT_ACCUM>;
-  else if (p.sign < 0) fn = k_fft<Q, -1, FFT_PLAIN>;
-  else fn = k_fft<Q, +1, FFT_PLAIN>;
-  static int attr_set[4] = {0, 0, 0, 0};  // per instantiation: set the smem cap once
-  const int slot = p.mode == FFT_PLAIN ? (p.sign < 0 ? 0 : 1) : (p.mode == FFT_SETIMG ? 2 : 3);
-  if (!attr_set[slot]) {
-    MRG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 8 * Q * 34 * (int)sizeof(float2)));
-    attr_set[slot] = 1;
-  }
   FftPass pp = p;
   pp.tw = g_tw[8 * Q];
-  fn<<<grid, block, smem, st>>>(pp);
-  MRG_LAUNCHED();
-  return MRG_OK;
+  // CTAs that never straddle an outer row find their row with one 32-bit division
+  pp.nib = (p.inner % p.IB == 0 && p.nlines % p.inner == 0) ? (int)(p.inner / p.IB) : 0;
+  if constexpr (fixed_pitch_q(Q)) {
+    if (!p.lfast && p.IB == 32) return launch_qp<Q, 32>(pp, grid, block, smem, st);
+    if (!p.lfast && p.IB == 16) return launch_qp<Q, 16>(pp, grid, block, smem, st);
+  }
+  return launch_qp<Q, 0>(pp, grid, block, smem, st);
 }
 
 void fft_vectorize(FftPass &p) {

@@ -81,6 +81,7 @@ struct FftPass {
   int Lin, in_off, Lout, out_off;
   int inner, IB, lfast;
   int vec16, vec16o;  // 16-byte loads / stores of line pairs (set by fft_vectorize)
+  int nib;            // inner / IB when no CTA straddles an outer row, else 0 (set by launch_fft)
   int64_t nlines;
   int64_t in_ls, in_os, out_ls, out_os;
   float scale;
