@@ -60,11 +60,11 @@ typedef struct mrg_config {
   int kernel_eval;   /* 0: interpolate the 600-per-unit table as the reference (src/gridFFT.cpp:1113-1116);
                         1: evaluate the Kaiser-Bessel kernel analytically (same beta and scale), the
                         form whose derivative mrg_grad uses, for finite-difference-consistent gradients */
-  int grid_mode;     /* gridding (E^H scatter) kernel: 0 the faster of 1 and 2 (timed per frame),
+  int grid_mode;     /* gridding (E^H scatter) kernel: 0 the fastest of 1, 2 and 3 (timed per frame),
                         1 FP32 multiply-adds on the CUDA cores, 2 tensor cores through mma.sync, 3
-                        tensor cores through tcgen05 with accumulators in tensor memory (>= 8 coils;
-                        only when asked for: slower than 2 today); 2 and 3 in TF32 with the
-                        three-term hi/lo split (W V ~ Wh Vh + Wh Vl + Wl Vh, products to ~2^-21) */
+                        tensor cores through tcgen05 with W and the accumulators in tensor memory
+                        (>= 8 coils); 2 and 3 in TF32 with the three-term hi/lo split
+                        (W V ~ Wh Vh + Wh Vl + Wl Vh, products to ~2^-20) */
 } mrg_config;
 
 /* Fills the reference defaults (src/gridFFT.cpp:28-60). */

@@ -764,7 +764,7 @@ mrg_status mrg_set_traj(mrg_plan *p, int frame, const float *kx, const float *ky
   MRG_TRY(dev_view(p, 3, kw, bytes, true, st, &dw, &s3));
   const GridConst gc = grid_const(p);
   // region pair lists only where the tensor-memory gridding kernel may run
-  const bool regions = umma_supported(p->C) && p->cfg.grid_mode == 3;
+  const bool regions = umma_supported(p->C) && (p->cfg.grid_mode == 0 || p->cfg.grid_mode == 3);
   MRG_TRY(traj_setup(gc, p->frames[frame], (const float *)dx, (const float *)dy, (const float *)dz,
                      (const float *)dw, M, p->max_pairs, regions, st));
   invalidate_graphs(p);

@@ -1,23 +1,27 @@
 // Gridding (gridFFT::chop_grid_forward, src/gridFFT.cpp:1009-1164) on the fifth-generation
-// tensor cores: tcgen05.mma with the accumulator in tensor memory.
+// tensor cores: tcgen05.mma with the operand W and the accumulators in tensor memory.
 //
-// The grid is cut into regions of 8x4x4 = 128 points, one TMEM lane (one thread of the
-// 128-thread CTA) per point.  For a region, the scatter of its (sample, region) pairs is
+// The grid is cut into regions of 8x4x4 = 128 points, one TMEM lane per point.  For a region, the scatter of its (sample, region) pairs is
 // the GEMM
 //   grid[128 points][N] += W[128 points][K pairs] * V[K pairs][N],   N = 2 * coils,
 // W the tap weights (wz*wy)*wx of each point for each sample, V the weighted sample
 // values with real and imaginary parts as separate columns.  Both operands are split
-// x = hi + lo (hi = tf32(x), lo = tf32(x - hi)) and the product taken as
-// Wl*Vh + Wh*Vl + Wh*Vh in TF32, products exact to about 2^-21.
+// x = hi + lo (hi = x with the low 13 mantissa bits cleared, lo = x - hi exactly; the
+// tensor core drops lo's own low bits) and the product taken as Wl*Vh + Wh*Vl + Wh*Vh
+// in TF32, each product within about 2^-20 of the FP32 one.
 //
-// Per chunk of 32 pairs the CTA stages the pairs' tap weights and values with cp.async,
-// writes W and V (hi and lo) into shared memory in the K-major, unswizzled canonical
-// layout, and one thread issues 12 MMAs (4 k-steps x 3 terms) into one of two TMEM
-// accumulator slots, committing them to that slot's mbarrier.  While they run, the
-// threads build the next chunk in the other buffer.  Each chunk is summed by the tensor
-// core from zero and added into the thread's FP32 registers with round-to-nearest when
-// its slot is reused: the tensor core rounds its sums toward zero, which along one long
-// accumulation became a bias (measured on the mma.sync kernel: 3.4e-5 from FP64 at 256^3).
+// One persistent 512-thread CTA per SM (four warpgroups, each thread owning the TMEM lane
+// of one point) walks its work items chunk by chunk.  Per chunk of 64 pairs: the pairs'
+// records (first taps, tap weights, sample values) are copied with cp.async one chunk
+// ahead; the threads tabulate (wz*wy) and wx per pair, each warpgroup writes two k-steps
+// of W (hi and lo, its threads' own rows) into tensor memory with tcgen05.st, all threads
+// write V into shared memory (K-major canonical layout), and one thread issues up to 24
+// MMAs (8 k-steps x 3 terms, A read from tensor memory) into one of two accumulator
+// slots, committing them to the slot's mbarrier.  While they run the CTA prepares the
+// next chunk in the other slot.  The tensor core adds into its accumulator rounding
+// toward zero (measured: bit-identical to an RZ emulation), so each chunk is summed from
+// zero and added into the thread's FP32 registers with round-to-nearest when its slot is
+// reused; along a whole region the truncation would otherwise build up a bias.
 //
 // Every mbarrier wait is bounded (about two seconds of SM clock); a kernel that runs
 // out of time sets an error flag, waits once more (bounded) for its own MMAs, frees its
@@ -30,21 +34,35 @@ namespace {
 
 __device__ int g_umma_error = 0;
 
-constexpr int UK = 32;  // pairs per chunk: four k-steps of 8 TF32 values
+constexpr int TK = 64;      // pairs per chunk: eight k-steps of 8 TF32 values
+constexpr int TP = TK + 4;  // row pitch (floats) of the per-pair weight tables: conflict-free 16-byte reads
+constexpr int NBLD = 512;   // builder threads: four warpgroups; warp w reaches TMEM lanes 32 (w % 4) .. + 31
+constexpr int NTHR = NBLD + 32;  // and one warp that issues the MMAs
 
 template <int CC>
-struct UmmaLayout {
-  static constexpr int N = 2 * CC;              // accumulator columns
-  static constexpr int A = 128 * UK * 4;        // bytes of one W operand (hi or lo)
-  static constexpr int B = N * UK * 4;          // bytes of one V operand (hi or lo)
-  static constexpr int BUF = 2 * A + 2 * B;     // W hi, W lo, V hi, V lo
-  static constexpr int SV = UK * N * 4;         // staged sample values [k][N]
-  static constexpr int SW = UK * 24 * 4;        // staged tap weights [k][24]
-  static constexpr int ST = UK * 16;            // staged first taps [k]
-  static constexpr int SYZ = UK * 16 * 4;       // (wz*wy) per pair and (py, pz) [k][pz*4 + py]
-  static constexpr int SX = UK * 8 * 4;         // wx per pair and px [k][px]
-  static constexpr int TOTAL = 2 * BUF + SV + SW + ST + SYZ + SX;
-  static constexpr int TCOLS = (2 * N < 32) ? 32 : 2 * N;  // two accumulator slots
+struct TcLayout {
+  static constexpr int N = 2 * CC;               // accumulator columns
+  static constexpr int NQ = N / 4;               // accumulator columns drained by each warpgroup
+  static constexpr int BOP = N * TK * 4;         // one V operand (hi or lo), K-major canonical
+  static constexpr int SV = TK * N * 4;          // staged sample values [k][N]
+  static constexpr int SW = TK * 24 * 4;         // staged tap weights [k][24]
+  static constexpr int ST = TK * 16;             // staged first taps [k]
+  static constexpr int STAGE = SV + SW + ST;
+  static constexpr int SYZ = 16 * TP * 4;        // (wz*wy)[pz*4 + py][k]
+  static constexpr int SX = 8 * TP * 4;          // wx[px][k]
+  static constexpr int OFF_B = 0;                             // 2 slots x (V hi, V lo)
+  static constexpr int OFF_STAGE = OFF_B + 4 * BOP;           // 2 staging buffers
+  static constexpr int OFF_SYZ = OFF_STAGE + 2 * STAGE;
+  static constexpr int OFF_SX = OFF_SYZ + SYZ;
+  static constexpr int USED = OFF_SX + SX;
+  // more than half of the SM's shared memory, so one CTA per SM owns all 512 TMEM columns
+  static constexpr int TOTAL = USED > 120 * 1024 ? USED : 120 * 1024;
+  // tensor memory: accumulators at columns [0, 2N), W of slot s at A0 + 2 TK s (hi) and
+  // A0 + 2 TK s + TK (lo)
+  static constexpr int A0 = 2 * N;
+  static constexpr int TCOLS = 512;
+  static_assert(A0 + 4 * TK <= TCOLS, "tensor memory columns");
+  static_assert(NQ % 4 == 0 && NQ >= 4, "drain width");
 };
 
 __device__ __forceinline__ uint32_t s_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -58,13 +76,15 @@ __device__ __forceinline__ void ucp8(void *dst, const void *src) {
 
 // Byte offset of element (row r, k) in the K-major canonical layout without swizzle:
 // 8-row x 16-byte core matrices, K-adjacent cores 128 bytes apart (LBO), 8-row groups
-// 1024 bytes apart (SBO).
-__device__ __forceinline__ int canon(int r, int k) { return (r >> 3) * 1024 + (k >> 2) * 128 + (r & 7) * 16 + (k & 3) * 4; }
+// TK * 32 bytes apart (SBO).
+__device__ __forceinline__ int canon(int r, int k) {
+  return (r >> 3) * (TK * 32) + (k >> 2) * 128 + (r & 7) * 16 + (k & 3) * 4;
+}
 
 // Shared-memory matrix descriptor: start address, LBO and SBO in 16-byte units,
 // descriptor version 1, no swizzle.
 __device__ __forceinline__ uint64_t sdesc(uint32_t addr) {
-  return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(1024 >> 4) << 32) |
+  return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)((TK * 32) >> 4) << 32) |
          ((uint64_t)1 << 46);
 }
 
@@ -74,31 +94,26 @@ __device__ __forceinline__ uint32_t idesc() {
   return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
 }
 
-__device__ __forceinline__ uint32_t tf32_rn(float x) {
-  uint32_t r;
-  asm("cvt.rna.tf32.f32 %0, %1;\n" : "=r"(r) : "f"(x));
-  return r;
-}
-__device__ __forceinline__ void split4(const float (&v)[4], uint4 &hi, uint4 &lo) {
-  uint32_t h[4], l[4];
-#pragma unroll
-  for (int i = 0; i < 4; i++) {
-    h[i] = tf32_rn(v[i]);
-    l[i] = tf32_rn(v[i] - __uint_as_float(h[i]));
-  }
-  hi = make_uint4(h[0], h[1], h[2], h[3]);
-  lo = make_uint4(l[0], l[1], l[2], l[3]);
-}
+__device__ __forceinline__ uint32_t hi_bits(float x) { return __float_as_uint(x) & 0xffffe000u; }
 
-__device__ __forceinline__ void mma_tf32(uint32_t tmem, uint64_t a, uint64_t b, uint32_t id, uint32_t accumulate) {
+// d (+)= A B with A (128 x 8) in tensor memory, B from a shared-memory descriptor
+__device__ __forceinline__ void mma_tA(uint32_t d, uint32_t a, uint64_t b, uint32_t id, uint32_t accumulate) {
   asm volatile(
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
-      "l"(a), "l"(b), "r"(id), "r"(accumulate));
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n}\n" ::"r"(d),
+      "r"(a), "l"(b), "r"(id), "r"(accumulate));
 }
 
-// Bounded wait for phase `parity` of an mbarrier; false after ~2 s of SM clock.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+// 8 columns of this thread's tensor-memory lane
+__device__ __forceinline__ void tst8(uint32_t ta, const uint32_t (&r)[8]) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(ta), "r"(r[0]),
+               "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7])
+               : "memory");
+}
+
+// Bounded wait for phase `parity` of an mbarrier; false after ~2 s of SM clock.  Between
+// tries the thread sleeps `nap` ns, so a waiting warp takes few issue slots from the others.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, unsigned nap = 32) {
   const long long t0 = clock64();
   for (;;) {
     uint32_t done;
@@ -109,48 +124,153 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
         : "memory");
     if (done) return true;
     if (clock64() - t0 > 4000000000LL) return false;
+    __nanosleep(nap);
   }
 }
 
-// Drains accumulator slot `slot` (this thread's lane = row) into acc with
-// round-to-nearest adds.
-template <int N>
-__device__ __forceinline__ void drain(uint32_t tmem, int slot, int warp, float (&acc)[N]) {
+// Drains this warp's NQ columns of an accumulator slot (lane = row) into acc with
+// round-to-nearest adds: all loads issued, one wait (tied to the loaded registers so no
+// use can move above it).
+template <int NQ>
+__device__ __forceinline__ void drain(uint32_t ta, float (&acc)[NQ]) {
+  uint32_t v[NQ];
 #pragma unroll
-  for (int c0 = 0; c0 < N; c0 += 16) {
-    uint32_t v[16];
-    const uint32_t ta = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(slot * N + c0);
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-          "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
-        : "r"(ta));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int j = 0; j < 16; j++) acc[c0 + j] = __fadd_rn(acc[c0 + j], __uint_as_float(v[j]));
+  for (int c0 = 0; c0 < NQ; c0 += 4)
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(v[c0]), "=r"(v[c0 + 1]), "=r"(v[c0 + 2]), "=r"(v[c0 + 3])
+                 : "r"(ta + (uint32_t)c0));
+  if constexpr (NQ == 16) {
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(v[0]), "+r"(v[1]), "+r"(v[2]), "+r"(v[3]), "+r"(v[4]), "+r"(v[5]), "+r"(v[6]), "+r"(v[7]),
+                   "+r"(v[8]), "+r"(v[9]), "+r"(v[10]), "+r"(v[11]), "+r"(v[12]), "+r"(v[13]), "+r"(v[14]),
+                   "+r"(v[15])::"memory");
+  } else if constexpr (NQ == 8) {
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(v[0]), "+r"(v[1]), "+r"(v[2]), "+r"(v[3]), "+r"(v[4]), "+r"(v[5]), "+r"(v[6]),
+                   "+r"(v[7])::"memory");
+  } else {
+    static_assert(NQ == 4, "drain width");
+    asm volatile("tcgen05.wait::ld.sync.aligned;" : "+r"(v[0]), "+r"(v[1]), "+r"(v[2]), "+r"(v[3])::"memory");
   }
+#pragma unroll
+  for (int j = 0; j < NQ; j++) acc[j] = __fadd_rn(acc[j], __uint_as_float(v[j]));
 }
 
-// CC coils per pass (blockIdx.y picks the chunk of coils), persistent over work items.
+// Issues the cp.async copies of the records of one chunk (pair indices already in shared
+// memory, `idx`) into staging buffer `st`; rows k >= nq of the sample values are zeroed.
 template <int CC, bool VEC>
-__global__ void __launch_bounds__(128, 2)
-    k_grid_umma(const GridConst g, BlockShape rs, int nitems, const int4 *__restrict__ items,
-                const int *__restrict__ pairs, const float4 *__restrict__ swt, const int4 *__restrict__ sst,
-                const float2 *__restrict__ yw, float2 *__restrict__ grid) {
-  typedef UmmaLayout<CC> L;
-  constexpr int N = L::N;
-  constexpr int NCH = N / 4;        // 16-byte pieces per sample record
-  constexpr int RPI = 128 / NCH;    // records per staging round
+__device__ __forceinline__ void stage_chunk(unsigned char *st, const int *idx, int nq, int tid, int C, int c0, int nc,
+                                            const float4 *__restrict__ swt, const int4 *__restrict__ sst,
+                                            const float2 *__restrict__ yw) {
+  typedef TcLayout<CC> L;
+  constexpr int N = L::N, NCH = N / 4;
+  float *sv = reinterpret_cast<float *>(st);
+  float *sw = reinterpret_cast<float *>(st + L::SV);
+  int4 *stt = reinterpret_cast<int4 *>(st + L::SV + L::SW);
+  if (tid < nq) ucp16(stt + tid, sst + idx[tid]);
+  for (int e = tid; e < TK * 6; e += NBLD) {  // 6 pieces of 16 bytes per record
+    const int k = e / 6, piece = e - 6 * k;
+    if (k < nq) ucp16(sw + k * 24 + 4 * piece, swt + 6 * (int64_t)idx[k] + piece);
+  }
+#pragma unroll
+  for (int e0 = 0; e0 < TK * NCH; e0 += NBLD) {
+    const int e = e0 + tid;
+    const int k = e / NCH, q = e % NCH;  // piece q = floats 4q..4q+3 = coils 2q, 2q+1
+    float *dst = sv + k * N + 4 * q;
+    if (e < TK * NCH) {
+      if (k < nq) {
+        const float2 *v = yw + (int64_t)idx[k] * C + c0;
+        if (VEC) {
+          if (2 * q < nc) ucp16(dst, v + 2 * q);
+          else *reinterpret_cast<float4 *>(dst) = make_float4(0.f, 0.f, 0.f, 0.f);
+        } else {
+          if (2 * q < nc) ucp8(dst, v + 2 * q);
+          else *reinterpret_cast<float2 *>(dst) = make_float2(0.f, 0.f);
+          if (2 * q + 1 < nc) ucp8(dst + 2, v + 2 * q + 1);
+          else *reinterpret_cast<float2 *>(dst + 2) = make_float2(0.f, 0.f);
+        }
+      } else {
+        *reinterpret_cast<float4 *>(dst) = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+    }
+  }
+}
+
+// Copies the pair (sample) indices of one chunk into `idx`.
+__device__ __forceinline__ void stage_idx(int *idx, const int *__restrict__ pairs, int q0, int nq, int tid) {
+  if (tid < nq) asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s_u32(idx + tid)), "l"(pairs + q0 + tid));
+}
+
+// Work item x field as packed region origin: x0 | y0 << 11 | z0 << 22.
+__global__ void k_pack_regions(BlockShape rs, int nitems, int4 *items) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nitems; i += gridDim.x * blockDim.x) {
+    const int r = items[i].x;
+    const int rx = r % rs.nb[0], ry = (r / rs.nb[0]) % rs.nb[1], rz = r / (rs.nb[0] * rs.nb[1]);
+    items[i].x = (rx * RGN_X) | ((ry * RGN_Y) << 11) | ((rz * RGN_Z) << 22);
+  }
+}
+
+// A CTA's walk over its chunks: item (-1 past the end), its work item and first pair.
+struct ChunkPos {
+  int item, q0;
+  int4 it;
+};
+__device__ __forceinline__ ChunkPos first_chunk(int item, int nitems, const int4 *__restrict__ items) {
+  ChunkPos p;
+  p.item = item < nitems ? item : -1;
+  p.it = p.item >= 0 ? __ldg(items + item) : make_int4(0, 0, 0, 0);
+  p.q0 = p.it.y;
+  return p;
+}
+__device__ __forceinline__ ChunkPos next_chunk(const ChunkPos &p, int nitems, const int4 *__restrict__ items) {
+  if (p.item < 0) return p;
+  if (p.q0 + TK < p.it.z) {
+    ChunkPos n = p;
+    n.q0 += TK;
+    return n;
+  }
+  return first_chunk(p.item + gridDim.x, nitems, items);
+}
+
+__device__ __forceinline__ void bld_sync() { asm volatile("bar.sync 1, %0;" ::"n"(NBLD) : "memory"); }
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ bool bld_and(bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n .reg .pred p, q;\n setp.ne.u32 q, %1, 0;\n bar.red.and.pred p, 1, %2, q;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(r)
+      : "r"((uint32_t)v), "n"(NBLD)
+      : "memory");
+  return r != 0;
+}
+
+// CC coils per pass (blockIdx.y picks the chunk of coils), one persistent CTA per SM over
+// the work items; the CTA walks its items' chunks in order (an item without pairs is one
+// empty chunk).  Warps 0-15 build the operands: thread tid owns point tid % 128 (its TMEM
+// lane), warpgroup g = tid / 128 writes k-steps g and g + 4 of W and drains accumulator
+// columns [g NQ, g NQ + NQ).  Warp 16 issues the MMAs.  Per slot s: full[s] (the 16
+// builder warps arrive when the slot's operands are written) and done[s] (the MMAs'
+// commit, or a plain arrive for an empty chunk); the builders wait done[s] of chunk c - 2
+// before they reuse slot s for chunk c, so neither barrier runs two phases ahead of its
+// waiter.
+template <int CC, bool VEC>
+__global__ void __launch_bounds__(NTHR, 1)
+    k_grid_umma(const GridConst g, int nitems, const int4 *__restrict__ items, const int *__restrict__ pairs,
+                const float4 *__restrict__ swt, const int4 *__restrict__ sst, const float2 *__restrict__ yw,
+                float2 *__restrict__ grid) {
+  typedef TcLayout<CC> L;
+  constexpr int N = L::N, NQ = L::NQ;
   extern __shared__ __align__(1024) unsigned char usm[];
-  __shared__ __align__(8) uint64_t bar[2];
+  __shared__ __align__(8) uint64_t full[2], done[2];
   __shared__ uint32_t tslot;
-  float *sv = reinterpret_cast<float *>(usm + 2 * L::BUF);
-  float *sw = reinterpret_cast<float *>(usm + 2 * L::BUF + L::SV);
-  int4 *stt = reinterpret_cast<int4 *>(usm + 2 * L::BUF + L::SV + L::SW);
-  float *syz = reinterpret_cast<float *>(usm + 2 * L::BUF + L::SV + L::SW + L::ST);
-  float *sx = reinterpret_cast<float *>(usm + 2 * L::BUF + L::SV + L::SW + L::ST + L::SYZ);
+  __shared__ int slot_nks[2];
+  __shared__ __align__(16) int sidx[3][TK];
+  float *syz = reinterpret_cast<float *>(usm + L::OFF_SYZ);
+  float *sx = reinterpret_cast<float *>(usm + L::OFF_SX);
   const int tid = threadIdx.x, warp = tid >> 5;
-  const int px = tid & 7, py = (tid >> 3) & 3, pz = tid >> 5;  // this thread's point (TMEM lane = tid)
   const int C = g.C, c0 = blockIdx.y * CC, nc = min(CC, C - c0);
 
   if (warp == 0) {
@@ -159,177 +279,229 @@ __global__ void __launch_bounds__(128, 2)
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(s_u32(&bar[0])), "r"(1));
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(s_u32(&bar[1])), "r"(1));
+    for (int s = 0; s < 2; s++) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(s_u32(&full[s])), "r"(NBLD / 32));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(s_u32(&done[s])), "r"(1));
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tslot;
-  uint32_t phase[2] = {0u, 0u};
-  bool pending[2] = {false, false};
-  bool ok = true;
 
-  for (int item = blockIdx.x; item < nitems && ok; item += gridDim.x) {
-    const int4 it = __ldg(items + item);
-    const int rx = it.x % rs.nb[0], ry = (it.x / rs.nb[0]) % rs.nb[1], rz = it.x / (rs.nb[0] * rs.nb[1]);
-    const int x0 = rx * RGN_X, y0 = ry * RGN_Y, z0 = rz * RGN_Z;
-    float acc[N];
-#pragma unroll
-    for (int j = 0; j < N; j++) acc[j] = 0.f;
-    int buf = 0;
-    for (int q0 = it.y; q0 < it.z && ok; q0 += UK, buf ^= 1) {
-      const int nq = min(UK, it.z - q0);
-      // ---- stage the chunk's pairs: first taps, tap weights, sample values ----
-      const int s_own = (tid < nq) ? __ldg(pairs + q0 + tid) : 0;  // thread k: sample of pair k
-      __shared__ int ssmp[UK];
-      if (tid < UK) ssmp[tid] = s_own;
-      __syncthreads();
-      if (tid < nq) ucp16(stt + tid, sst + s_own);
-      for (int e = tid; e < UK * 6; e += 128) {  // 6 pieces of 16 bytes per record
-        const int k = e / 6, piece = e % 6;
-        if (k < nq) ucp16(sw + k * 24 + 4 * piece, swt + 6 * (int64_t)ssmp[k] + piece);
+  if (warp == NBLD / 32) {
+    // ---------------- MMA warp ----------------
+    const uint32_t id = idesc<N>();
+    for (int c = 0;; c++) {
+      const int s = c & 1;
+      if (!mbar_wait(s_u32(&full[s]), (uint32_t)((c >> 1) & 1), 256)) {
+        atomicExch(&g_umma_error, 1);
+        break;
       }
+      const int nks = slot_nks[s];
+      if (nks < 0) break;  // the builders are done
+      if ((tid & 31) == 0) {
+        if (nks > 0) {
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t d = tmem + (uint32_t)(s * N);
+          const uint32_t a_h = tmem + (uint32_t)(L::A0 + 2 * TK * s), a_l = a_h + TK;
+          const uint32_t bb = s_u32(usm + L::OFF_B + s * 2 * L::BOP);
+          const uint64_t dh = sdesc(bb), dl = sdesc(bb + L::BOP);
 #pragma unroll
-      for (int r0 = 0; r0 < UK; r0 += RPI) {
-        const int k = r0 + tid / NCH, q = tid % NCH;  // piece q = floats 4q..4q+3 = coils 2q, 2q+1
-        if (k < UK) {
-          float *dst = sv + k * N + 4 * q;
-          if (k < nq) {
-            const float2 *v = yw + (int64_t)ssmp[k] * C + c0;
-            if (VEC) {
-              if (2 * q < nc) ucp16(dst, v + 2 * q);
-              else *reinterpret_cast<float4 *>(dst) = make_float4(0.f, 0.f, 0.f, 0.f);
-            } else {
-              if (2 * q < nc) ucp8(dst, v + 2 * q);
-              else *reinterpret_cast<float2 *>(dst) = make_float2(0.f, 0.f);
-              if (2 * q + 1 < nc) ucp8(dst + 2, v + 2 * q + 1);
-              else *reinterpret_cast<float2 *>(dst + 2) = make_float2(0.f, 0.f);
+          for (int ks = 0; ks < TK / 8; ks++) {
+            if (ks < nks) {
+              const uint64_t o = (uint64_t)(ks * 16);  // 8 k = two cores = 256 bytes
+              mma_tA(d, a_l + 8 * ks, dh + o, id, ks > 0 ? 1u : 0u);  // small terms first
+              mma_tA(d, a_h + 8 * ks, dl + o, id, 1u);
+              mma_tA(d, a_h + 8 * ks, dh + o, id, 1u);
             }
-          } else {
-            *reinterpret_cast<float4 *>(dst) = make_float4(0.f, 0.f, 0.f, 0.f);
           }
+          asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                           s_u32(&done[s]))
+                       : "memory");
+        } else {
+          mbar_arrive(s_u32(&done[s]));
         }
       }
+      __syncwarp();
+    }
+  } else {
+    // ---------------- builder warps ----------------
+    const int wg = tid >> 7, pt = tid & 127;
+    const int px = pt & 7, py = (pt >> 3) & 3, pz = pt >> 5;  // this thread's point (TMEM lane = pt)
+    const uint32_t lane_base = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
+    // per slot s, bit s: a chunk written and not yet waited for / it had MMAs / the done[s]
+    // phase to wait for next (bit masks keep them in registers)
+    unsigned outstanding = 0u, mma = 0u, dphase = 0u;
+    bool ok = true;
+    float acc[NQ];
+#pragma unroll
+    for (int j = 0; j < NQ; j++) acc[j] = 0.f;
+    // Waits (bounded) for the chunk last written into slot s and sums it; the builders
+    // give up together so their barriers stay matched.
+    auto retire = [&](int s) -> bool {
+      if (!((outstanding >> s) & 1u)) return true;
+      if (!bld_and(mbar_wait(s_u32(&done[s]), (dphase >> s) & 1u))) return false;
+      dphase ^= 1u << s;
+      outstanding &= ~(1u << s);
+      if ((mma >> s) & 1u) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        drain<NQ>(lane_base + (uint32_t)(s * N + wg * NQ), acc);
+      }
+      return true;
+    };
+    ChunkPos cur = first_chunk(blockIdx.x, nitems, items);
+    ChunkPos nxt = next_chunk(cur, nitems, items);
+    // prologue: indices of the first chunk, then its records and the next chunk's indices
+    if (cur.item >= 0) stage_idx(sidx[0], pairs, cur.q0, min(TK, cur.it.z - cur.q0), tid);
+    asm volatile("cp.async.commit_group;\n" ::);
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    bld_sync();
+    if (cur.item >= 0)
+      stage_chunk<CC, VEC>(usm + L::OFF_STAGE, sidx[0], min(TK, cur.it.z - cur.q0), tid, C, c0, nc, swt, sst, yw);
+    if (nxt.item >= 0) stage_idx(sidx[1], pairs, nxt.q0, min(TK, nxt.it.z - nxt.q0), tid);
+    asm volatile("cp.async.commit_group;\n" ::);
+    int c = 0;
+    while (cur.item >= 0) {
+      const int nq = min(TK, cur.it.z - cur.q0);
+      const bool last = cur.q0 + TK >= cur.it.z;
+      const ChunkPos nxt2 = next_chunk(nxt, nitems, items);
+      // records of chunk c and indices of chunk c + 1 have landed
+      asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+      bld_sync();
+      if (nxt.item >= 0)
+        stage_chunk<CC, VEC>(usm + L::OFF_STAGE + ((c + 1) & 1) * L::STAGE, sidx[(c + 1) % 3],
+                             min(TK, nxt.it.z - nxt.q0), tid, C, c0, nc, swt, sst, yw);
+      if (nxt2.item >= 0) stage_idx(sidx[(c + 2) % 3], pairs, nxt2.q0, min(TK, nxt2.it.z - nxt2.q0), tid);
       asm volatile("cp.async.commit_group;\n" ::);
-      asm volatile("cp.async.wait_group 0;\n" ::);
-      __syncthreads();
+      const unsigned char *stg = usm + L::OFF_STAGE + (c & 1) * L::STAGE;
+      const float *sv = reinterpret_cast<const float *>(stg);
+      const float *sw = reinterpret_cast<const float *>(stg + L::SV);
+      const int4 *stt = reinterpret_cast<const int4 *>(stg + L::SV + L::SW);
+      const int x0 = cur.it.x & 2047, y0 = (cur.it.x >> 11) & 2047, z0 = cur.it.x >> 22;
       // ---- per pair: (wz*wy) for the region's 4 y and 4 z planes, wx for its 8 x ----
       {
-        const int k = tid >> 2, zz = tid & 3;  // 32 pairs x 4 z planes
-        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-        float2 xv = make_float2(0.f, 0.f);
+        const int k = tid >> 3, j = tid & 7;  // 64 pairs x 8 threads
+        const int zz = j >> 1, y2 = 2 * (j & 1);
+        float wyz0 = 0.f, wyz1 = 0.f, wx = 0.f;
         if (k < nq) {
           const int4 t = stt[k];
           const float *w = sw + k * 24;
-          const int az = z0 + zz - t.z;
+          const int az = z0 + zz - t.z, ay = y0 + y2 - t.y, ax = x0 + j - t.x;
           const float wz = (az >= 0 && az < 8) ? w[16 + az] : 0.0f;
-          float wy[4];
-#pragma unroll
-          for (int yy = 0; yy < 4; yy++) {
-            const int ay = y0 + yy - t.y;
-            wy[yy] = (ay >= 0 && ay < 8) ? w[8 + ay] : 0.0f;
-          }
           // (wz * wy) first, as src/gridFFT.cpp:1113-1140 multiplies them
-          v = make_float4(__fmul_rn(wz, wy[0]), __fmul_rn(wz, wy[1]), __fmul_rn(wz, wy[2]), __fmul_rn(wz, wy[3]));
-          const int ax0 = x0 + 2 * zz - t.x, ax1 = ax0 + 1;  // this thread also fills wx for x = 2zz, 2zz+1
-          xv = make_float2((ax0 >= 0 && ax0 < 8) ? w[ax0] : 0.0f, (ax1 >= 0 && ax1 < 8) ? w[ax1] : 0.0f);
+          wyz0 = __fmul_rn(wz, (ay >= 0 && ay < 8) ? w[8 + ay] : 0.0f);
+          wyz1 = __fmul_rn(wz, (ay + 1 >= 0 && ay + 1 < 8) ? w[9 + ay] : 0.0f);
+          wx = (ax >= 0 && ax < 8) ? w[ax] : 0.0f;
         }
-        *reinterpret_cast<float4 *>(syz + k * 16 + zz * 4) = v;
-        *reinterpret_cast<float2 *>(sx + k * 8 + 2 * zz) = xv;
+        syz[(zz * 4 + y2) * TP + k] = wyz0;
+        syz[(zz * 4 + y2 + 1) * TP + k] = wyz1;
+        sx[j * TP + k] = wx;
       }
-      __syncthreads();
-      // ---- the slot of this buffer is free once its chunk (two back) is summed ----
-      if (pending[buf]) {
-        // every thread waits (bounded); they give up together so the barriers stay matched
-        ok = __syncthreads_and(mbar_wait(s_u32(&bar[buf]), phase[buf]) ? 1 : 0) != 0;
-        if (!ok) break;
-        phase[buf] ^= 1u;
-        pending[buf] = false;
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        drain<N>(tmem, buf, warp, acc);
+      bld_sync();
+      const int slot = c & 1;
+      // ---- the slot is free once its chunk (two back) is summed ----
+      if (!retire(slot)) {
+        ok = false;
+        break;
       }
-      // ---- W (this thread's row) and V into buffer buf, hi and lo ----
-      unsigned char *base = usm + buf * L::BUF;
-      unsigned char *ah = base, *al = base + L::A, *bh = base + 2 * L::A, *bl = base + 2 * L::A + L::B;
+      const int nks = (nq + 7) >> 3;  // k-steps with pairs
+      // ---- W: this thread's row, k-steps wg and wg + 4, hi and lo, into tensor memory ----
+      {
+        const float *ryz = syz + (pz * 4 + py) * TP, *rxx = sx + px * TP;
+        const uint32_t ta = lane_base + (uint32_t)(L::A0 + 2 * TK * slot);
 #pragma unroll
-      for (int k4 = 0; k4 < UK / 4; k4++) {
-        float w4[4];
+        for (int h = 0; h < 2; h++) {
+          const int ks = wg + 4 * h;
+          if (ks < nks) {
+            const float4 a0 = *reinterpret_cast<const float4 *>(ryz + 8 * ks);
+            const float4 a1 = *reinterpret_cast<const float4 *>(ryz + 8 * ks + 4);
+            const float4 b0 = *reinterpret_cast<const float4 *>(rxx + 8 * ks);
+            const float4 b1 = *reinterpret_cast<const float4 *>(rxx + 8 * ks + 4);
+            const float w[8] = {__fmul_rn(a0.x, b0.x), __fmul_rn(a0.y, b0.y), __fmul_rn(a0.z, b0.z),
+                                __fmul_rn(a0.w, b0.w), __fmul_rn(a1.x, b1.x), __fmul_rn(a1.y, b1.y),
+                                __fmul_rn(a1.z, b1.z), __fmul_rn(a1.w, b1.w)};
+            uint32_t hh[8], ll[8];
 #pragma unroll
-        for (int i = 0; i < 4; i++) {
-          const int k = 4 * k4 + i;
-          w4[i] = __fmul_rn(syz[k * 16 + pz * 4 + py], sx[k * 8 + px]);  // (wz*wy)*wx
+            for (int i = 0; i < 8; i++) {
+              hh[i] = hi_bits(w[i]);
+              ll[i] = __float_as_uint(w[i] - __uint_as_float(hh[i]));
+            }
+            tst8(ta + 8 * ks, hh);
+            tst8(ta + TK + 8 * ks, ll);
+          }
         }
-        uint4 h, l;
-        split4(w4, h, l);
-        *reinterpret_cast<uint4 *>(ah + canon(tid, 4 * k4)) = h;
-        *reinterpret_cast<uint4 *>(al + canon(tid, 4 * k4)) = l;
       }
+      // ---- V: K-major canonical, hi and lo, into the slot's shared buffers ----
+      {
+        // (n, 4 consecutive k) units; NBLD is a multiple of N, so a thread keeps its n
+        static_assert(NBLD % N == 0, "one column per thread");
+        const int n = tid % N;
+        unsigned char *bh = usm + L::OFF_B + slot * 2 * L::BOP + canon(n, 0);
+        const float *sp = sv + n;
+        for (int k4 = tid / N; k4 < 2 * nks; k4 += NBLD / N) {
+          const float *q = sp + 4 * k4 * N;
+          const float v[4] = {q[0], q[N], q[2 * N], q[3 * N]};
+          uint32_t hh[4], ll[4];
 #pragma unroll
-      for (int u = tid; u < N * (UK / 4); u += 128) {
-        const int n = u % N, k4 = u / N;
-        float v4[4];
-#pragma unroll
-        for (int i = 0; i < 4; i++) v4[i] = sv[(4 * k4 + i) * N + n];
-        uint4 h, l;
-        split4(v4, h, l);
-        *reinterpret_cast<uint4 *>(bh + canon(n, 4 * k4)) = h;
-        *reinterpret_cast<uint4 *>(bl + canon(n, 4 * k4)) = l;
+          for (int i = 0; i < 4; i++) {
+            hh[i] = hi_bits(v[i]);
+            ll[i] = __float_as_uint(v[i] - __uint_as_float(hh[i]));
+          }
+          *reinterpret_cast<uint4 *>(bh + k4 * 128) = make_uint4(hh[0], hh[1], hh[2], hh[3]);
+          *reinterpret_cast<uint4 *>(bh + L::BOP + k4 * 128) = make_uint4(ll[0], ll[1], ll[2], ll[3]);
+        }
       }
+      if (tid == 0) slot_nks[slot] = nks;
+      asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      __syncthreads();
-      if (tid == 0) {
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t id = idesc<N>();
-        const uint32_t d = tmem + (uint32_t)(buf * N);
-        const uint32_t a_h = s_u32(ah), a_l = s_u32(al), b_h = s_u32(bh), b_l = s_u32(bl);
-#pragma unroll
-        for (int ks = 0; ks < UK / 8; ks++) {
-          const uint32_t o = (uint32_t)(ks * 256);  // 8 k = two cores along K
-          mma_tf32(d, sdesc(a_l + o), sdesc(b_h + o), id, ks > 0 ? 1u : 0u);  // small terms first
-          mma_tf32(d, sdesc(a_h + o), sdesc(b_l + o), id, 1u);
-          mma_tf32(d, sdesc(a_h + o), sdesc(b_h + o), id, 1u);
+      __syncwarp();
+      if ((tid & 31) == 0) mbar_arrive(s_u32(&full[slot]));
+      outstanding |= 1u << slot;
+      mma = nks > 0 ? (mma | (1u << slot)) : (mma & ~(1u << slot));
+      ++c;
+      if (last) {
+        // ---- sum what is still in flight (the older chunk first), then write the region ----
+        if (!retire(slot ^ 1) || !retire(slot)) {
+          ok = false;
+          break;
         }
-        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                         s_u32(&bar[buf]))
-                     : "memory");
+        // this thread's coils: [c0 + wg NQ / 2, + NQ / 2) of its point
+        const int cl = wg * (NQ / 2);
+        const int64_t gi = (((int64_t)(z0 + pz) * g.S[1] + (y0 + py)) * g.S[0] + (x0 + px)) * C + c0 + cl;
+        if (cur.it.w) {
+#pragma unroll
+          for (int j = 0; j < NQ; j++)
+            if (cl + (j >> 1) < nc) atomicAdd(reinterpret_cast<float *>(grid + gi) + j, acc[j]);
+        } else if (VEC) {
+          float4 *o4 = reinterpret_cast<float4 *>(grid + gi);
+#pragma unroll
+          for (int j = 0; j < NQ / 4; j++)
+            if (cl + 2 * j < nc) o4[j] = make_float4(acc[4 * j], acc[4 * j + 1], acc[4 * j + 2], acc[4 * j + 3]);
+        } else {
+#pragma unroll
+          for (int j = 0; j < NQ / 2; j++)
+            if (cl + j < nc) grid[gi + j] = make_float2(acc[2 * j], acc[2 * j + 1]);
+        }
+#pragma unroll
+        for (int j = 0; j < NQ; j++) acc[j] = 0.f;
       }
-      pending[buf] = true;
+      cur = nxt;
+      nxt = nxt2;
     }
-    // ---- sum what is still in flight, then write the region ----
-    for (int b = 0; b < 2 && ok; b++) {
-      if (!pending[b]) continue;
-      ok = __syncthreads_and(mbar_wait(s_u32(&bar[b]), phase[b]) ? 1 : 0) != 0;
-      if (!ok) break;
-      phase[b] ^= 1u;
-      pending[b] = false;
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      drain<N>(tmem, b, warp, acc);
-    }
-    if (!ok) break;
-    const int64_t gi = (((int64_t)(z0 + pz) * g.S[1] + (y0 + py)) * g.S[0] + (x0 + px)) * C + c0;
-    if (it.w) {
-#pragma unroll
-      for (int j = 0; j < N; j++)
-        if ((j >> 1) < nc) atomicAdd(reinterpret_cast<float *>(grid + gi) + j, acc[j]);
-    } else if (VEC) {
-      float4 *o4 = reinterpret_cast<float4 *>(grid + gi);
-#pragma unroll
-      for (int j = 0; j < N / 4; j++)
-        if (2 * j < nc) o4[j] = make_float4(acc[4 * j], acc[4 * j + 1], acc[4 * j + 2], acc[4 * j + 3]);
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+    if (ok) {
+      // both slots are retired (the last chunk ended an item): tell the MMA warp to stop
+      if (tid == 0) slot_nks[c & 1] = -1;
+      __syncwarp();
+      if ((tid & 31) == 0) mbar_arrive(s_u32(&full[c & 1]));
     } else {
-#pragma unroll
-      for (int j = 0; j < N / 2; j++)
-        if (j < nc) grid[gi + j] = make_float2(acc[2 * j], acc[2 * j + 1]);
+      atomicExch(&g_umma_error, 1);
+      for (int s = 0; s < 2; s++)  // let MMAs still in flight finish before the memory is freed
+        if ((outstanding >> s) & 1u) mbar_wait(s_u32(&done[s]), (dphase >> s) & 1u);
     }
-    __syncthreads();  // the staging area and barriers are reused by the next item
-  }
-  if (!ok) {
-    atomicExch(&g_umma_error, 1);
-    for (int b = 0; b < 2; b++)  // let MMAs still in flight finish before the memory is freed
-      if (pending[b]) mbar_wait(s_u32(&bar[b]), phase[b]);
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
@@ -339,6 +511,8 @@ __global__ void __launch_bounds__(128, 2)
 }  // namespace
 
 bool umma_supported(int C) { return C >= 8; }
+// region origins packed in 11 + 11 + 10 bits
+bool umma_grid_fits(const int S[3]) { return S[0] <= 2048 && S[1] <= 2048 && S[2] <= 1024; }
 int umma_default_cc(int C) { return C > 16 ? 32 : (C > 8 ? 16 : 8); }
 
 int umma_error_flag() {
@@ -353,28 +527,34 @@ int umma_error_flag() {
 template <int CC>
 static mrg_status launch_umma_cc(const GridConst &gc, const FrameTraj &ft, const float2 *yw, float2 *grid,
                                  cudaStream_t st) {
-  typedef UmmaLayout<CC> L;
+  typedef TcLayout<CC> L;
   const bool vec = (gc.C % 2 == 0) && (((uintptr_t)yw & 15) == 0) && (((uintptr_t)grid & 15) == 0);
-  static int ctas_per_sm = 0;
-  if (ctas_per_sm == 0) {
+  static bool attr = false;
+  if (!attr) {
     MRG_CUDA(cudaFuncSetAttribute(k_grid_umma<CC, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, L::TOTAL));
     MRG_CUDA(cudaFuncSetAttribute(k_grid_umma<CC, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, L::TOTAL));
-    int n = 0;
-    MRG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_grid_umma<CC, true>, 128, L::TOTAL));
-    // TMEM: at most 512 columns per SM are shared by the resident CTAs
-    ctas_per_sm = std::max(1, std::min(n, 512 / L::TCOLS));
+    attr = true;
   }
   int sms = 152;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
-  const int nx = std::max(1, std::min(ft.regions.nitems, sms * ctas_per_sm));
-  const dim3 blocks((unsigned)nx, (unsigned)((gc.C + CC - 1) / CC));
-  const BlockShape rs = region_shape(gc);
+  // one CTA per SM (its shared memory keeps a second one off the SM, so the 512 TMEM
+  // columns it allocates are always free); every coil pass gets its share of the SMs
+  const int npass = (gc.C + CC - 1) / CC;
+  const int nx = std::max(1, std::min(ft.regions.nitems, std::max(1, sms / npass)));
+  const dim3 blocks((unsigned)nx, (unsigned)npass);
   if (vec)
-    k_grid_umma<CC, true><<<blocks, 128, L::TOTAL, st>>>(gc, rs, ft.regions.nitems, ft.regions.items,
-                                                         ft.regions.pairs, ft.swt, ft.sst, yw, grid);
+    k_grid_umma<CC, true><<<blocks, NTHR, L::TOTAL, st>>>(gc, ft.regions.nitems, ft.regions.items, ft.regions.pairs,
+                                                          ft.swt, ft.sst, yw, grid);
   else
-    k_grid_umma<CC, false><<<blocks, 128, L::TOTAL, st>>>(gc, rs, ft.regions.nitems, ft.regions.items,
-                                                          ft.regions.pairs, ft.swt, ft.sst, yw, grid);
+    k_grid_umma<CC, false><<<blocks, NTHR, L::TOTAL, st>>>(gc, ft.regions.nitems, ft.regions.items,
+                                                           ft.regions.pairs, ft.swt, ft.sst, yw, grid);
+  MRG_LAUNCHED();
+  return MRG_OK;
+}
+
+mrg_status pack_region_items(const GridConst &gc, PairSet &ps, cudaStream_t st) {
+  if (ps.nitems == 0) return MRG_OK;
+  k_pack_regions<<<grid_blocks(ps.nitems, 256), 256, 0, st>>>(region_shape(gc), ps.nitems, ps.items);
   MRG_LAUNCHED();
   return MRG_OK;
 }

@@ -451,7 +451,10 @@ mrg_status traj_setup(const GridConst &gc, FrameTraj &ft, const float *kx, const
   // 3-4. (sample, block) pair lists and work items for the 8x2x2 blocks, and for the
   // 8x4x4 regions of the tensor-memory gridding kernel when it may run
   SETUP_TRY(build_pairs(block_shape(gc), nvalid, ft.sst, max_pairs, st, ft.blocks));
-  if (regions) SETUP_TRY(build_pairs(region_shape(gc), nvalid, ft.sst, max_pairs, st, ft.regions));
+  if (regions && umma_grid_fits(gc.S)) {
+    SETUP_TRY(build_pairs(region_shape(gc), nvalid, ft.sst, max_pairs, st, ft.regions));
+    SETUP_TRY(pack_region_items(gc, ft.regions, st));
+  }
   cleanup();
 #undef SETUP_TRY
 #undef SETUP_LAUNCHED
@@ -1594,14 +1597,11 @@ mrg_status autotune_frame(const GridConst &gc, FrameTraj &ft, float2 *grid, floa
   ft.tune_ungrid_ms = best;
   best = 1e30f;
   int bestCC = 0;
-  // CUDA-core kernel: all coils, 16 or 8 per pass; tensor-core kernel (negative): 4n coils per pass
   // CUDA-core kernel: all coils, 16 or 8 per pass; mma.sync kernel (-n): 4n coils per pass;
   // tcgen05 kernel (-(100 + c)): c coils per pass
   for (int cc : {0, 16, 8, -8, -4, -2, -1, -132, -116, -108}) {
     const int mode = cc >= 0 ? 1 : (cc > -100 ? 2 : 3);
-    // the tcgen05 kernel runs only when asked for (grid_mode 3): measured slower than the
-    // mma.sync kernel (9.4 vs 3.6 ms at 128^3 x 32), so timing it would only lengthen set-up
-    if (mode == 3 ? gc.grid_mode != 3 : (gc.grid_mode != 0 && gc.grid_mode != mode)) continue;
+    if (gc.grid_mode != 0 && gc.grid_mode != mode) continue;
     if (mode == 1 && cc > 0 && gc.C <= cc) continue;
     if (mode == 2 && -cc > default_grid_nt(gc.C)) continue;  // more coils per pass than the plan has
     if (mode == 2 && -cc < default_grid_nt(gc.C) / 2) continue;

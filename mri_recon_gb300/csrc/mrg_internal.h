@@ -176,6 +176,9 @@ BlockShape region_shape(const GridConst &gc);
 void pair_set_free(PairSet &ps);
 // tcgen05 gridding over 8x4x4 regions (grid_umma.cu): cc = coils per pass (8, 16 or 32)
 bool umma_supported(int C);
+bool umma_grid_fits(const int S[3]);
+// Packs the region origin into each work item of the tcgen05 kernel's pair set.
+mrg_status pack_region_items(const GridConst &gc, PairSet &ps, cudaStream_t st);
 // a gridding launch shape (mrg_frame_tuning's encoding) that the frame's kernels can run
 bool grid_cc_allowed(int C, const FrameTraj &ft, int cc);
 // n-tiles (4 coils each) per pass of the tensor-core ungridding kernel; 0: needs C % 4 == 0
