@@ -521,10 +521,15 @@ struct UngridVec<4> {
   }
 };
 
-// UY rows of taps are loaded before any of them is summed, so up to 6 * UY gathers per
-// lane are in flight (the kernel is bound by the latency of these L1 gathers).  Taps
-// beyond a sample's counts load zero and carry zero weights (the tables are padded).
-template <int G, int CPL, int UY>
+// A window of 5 x 5 x 5 taps (every sample but those at exact half-integer positions or
+// clipped at the grid's edge) is summed fully unrolled, with its weights in registers and
+// every gather unpredicated, so the loads of later rows can be issued early (the kernel
+// is bound by the latency of these L1 gathers).  Other windows take the general loop,
+// where UY rows of taps are loaded before any of them is summed and taps beyond a
+// sample's counts load zero and carry zero weights (the tables are padded).  CT: the coil
+// count as a compile-time constant (0: from the plan), which turns the tap offsets into
+// immediates.
+template <int G, int CPL, int UY, int CT = 0>
 __global__ void __launch_bounds__(256) k_ungrid(const GridConst g, int nvalid, int spb, const float4 *__restrict__ swt,
                                                const int4 *__restrict__ sst, const float4 *__restrict__ spos,
                                                const float *__restrict__ stap, const float2 *__restrict__ grid,
@@ -533,7 +538,7 @@ __global__ void __launch_bounds__(256) k_ungrid(const GridConst g, int nvalid, i
   typedef typename V::T VT;
   constexpr int GPB = 256 / G;  // sample groups per CTA
   const int lane = threadIdx.x % G, grp = threadIdx.x / G;
-  const int C = g.C;
+  const int C = CT ? CT : g.C;
   const int c = (blockIdx.y * G + lane) * CPL;  // first coil of this lane
   const int64_t ys = (int64_t)g.S[0] * C, zs = (int64_t)g.S[1] * ys;
   const int64_t s_begin = (int64_t)blockIdx.x * spb;
@@ -549,6 +554,33 @@ __global__ void __launch_bounds__(256) k_ungrid(const GridConst g, int nvalid, i
 #pragma unroll
     for (int k = 0; k < 2 * CPL; k++) acc[k] = 0.f;
     const float2 *base = grid + ((int64_t)t.z * g.S[1] + t.y) * ys + (int64_t)t.x * C + c;
+    if (nx == 5 && ny == 5 && nz == 5) {
+      const float4 wc = __ldg(swt + 6 * gid + 2), wd = __ldg(swt + 6 * gid + 4), we = __ldg(swt + 6 * gid + 5);
+      const float wy[5] = {wc.x, wc.y, wc.z, wc.w, __ldg(w + 12)};
+      const float wz[5] = {wd.x, wd.y, wd.z, wd.w, we.x};
+#pragma unroll
+      for (int kz = 0; kz < 5; kz++) {
+        float az[2 * CPL];
+#pragma unroll
+        for (int k = 0; k < 2 * CPL; k++) az[k] = 0.f;
+#pragma unroll
+        for (int ky = 0; ky < 5; ky++) {
+          const float2 *row = base + kz * zs + ky * ys;
+          VT v[5];
+#pragma unroll
+          for (int a = 0; a < 5; a++) v[a] = V::load(row + a * C);
+          float ar[2 * CPL];
+#pragma unroll
+          for (int k = 0; k < 2 * CPL; k++) ar[k] = 0.f;
+#pragma unroll
+          for (int a = 0; a < 5; a++) V::fma(ar, wx[a], v[a]);
+#pragma unroll
+          for (int k = 0; k < 2 * CPL; k++) az[k] += wy[ky] * ar[k];
+        }
+#pragma unroll
+        for (int k = 0; k < 2 * CPL; k++) acc[k] += wz[kz] * az[k];
+      }
+    } else {
     for (int kz = 0; kz < nz; kz++) {
       float az[2 * CPL];
 #pragma unroll
@@ -577,6 +609,7 @@ __global__ void __launch_bounds__(256) k_ungrid(const GridConst g, int nvalid, i
       const float wzv = __ldg(w + 16 + kz);
 #pragma unroll
       for (int k = 0; k < 2 * CPL; k++) acc[k] += wzv * az[k];
+    }
     }
     float kw = 0.f, tp = 0.f;
     if (weigh) {
@@ -629,6 +662,7 @@ mrg_status launch_ungrid(const GridConst &gc, const FrameTraj &ft, const float2 
   const int chunk = G * cpl;
   const dim3 blocks((unsigned)((ft.nvalid + spb - 1) / spb), (unsigned)((gc.C + chunk - 1) / chunk));
   const int wf = weigh ? 1 : 0;
+  const bool c32 = gc.C == 32 && uy == 1;  // coil count as a compile-time constant
 #define UNGRID_ARGS gc, ft.nvalid, spb, ft.swt, ft.sst, ft.spos, ft.stap, grid, diff, y, wf
 #define UNGRID_UY(GG, PP)                                                         \
   switch (uy) {                                                                   \
@@ -638,9 +672,13 @@ mrg_status launch_ungrid(const GridConst &gc, const FrameTraj &ft, const float2 
   }
 #define UNGRID_CASE(GG)                                                           \
   case GG:                                                                        \
-    if (cpl == 4) k_ungrid<GG, 4, 1><<<blocks, 256, 0, st>>>(UNGRID_ARGS);        \
-    else if (cpl == 2) { UNGRID_UY(GG, 2) }                                       \
-    else { UNGRID_UY(GG, 1) }                                                     \
+    if (cpl == 4) {                                                               \
+      if (c32) k_ungrid<GG, 4, 1, 32><<<blocks, 256, 0, st>>>(UNGRID_ARGS);       \
+      else k_ungrid<GG, 4, 1><<<blocks, 256, 0, st>>>(UNGRID_ARGS);               \
+    } else if (cpl == 2) {                                                        \
+      if (c32) k_ungrid<GG, 2, 1, 32><<<blocks, 256, 0, st>>>(UNGRID_ARGS);       \
+      else { UNGRID_UY(GG, 2) }                                                   \
+    } else { UNGRID_UY(GG, 1) }                                                   \
     break;
   switch (G) {
     case 1:
