@@ -50,6 +50,9 @@ def parse():
                     help="gridding kernel (mrg_config.grid_mode): 0 fastest timed, 1 CUDA cores, 2 mma.sync, 3 tcgen05")
     ap.add_argument("--no-side-configs", dest="side_configs", action="store_false",
                     help="skip the throughput of the four smaller configurations")
+    ap.add_argument("--profile-range", action="store_true",
+                    help="bracket the two per-stage timing iterations with cudaProfilerStart/Stop "
+                         "(for ncu --profile-from-start off: captures the launch shapes the bench runs)")
     return ap.parse_args()
 
 
@@ -371,8 +374,12 @@ def run_ours(a):
 
     # --- per-stage timing (eager, events between stages) for the roofline ---
     plan.set_timing(True)
+    if a.profile_range:
+        torch.cuda.profiler.start()
     plan.cg_iterate(2, X, use_graph=False)
     torch.cuda.synchronize()
+    if a.profile_range:
+        torch.cuda.profiler.stop()
     tms, calls = plan.timings()
     plan.set_timing(False)
     fi = plan.frame_info(0, taps=True)

@@ -678,7 +678,10 @@ mrg_status launch_ungrid(const GridConst &gc, const FrameTraj &ft, const float2 
     } else if (cpl == 2) {                                                        \
       if (c32) k_ungrid<GG, 2, 1, 32><<<blocks, 256, 0, st>>>(UNGRID_ARGS);       \
       else { UNGRID_UY(GG, 2) }                                                   \
-    } else { UNGRID_UY(GG, 1) }                                                   \
+    } else {                                                                      \
+      if (c32) k_ungrid<GG, 1, 1, 32><<<blocks, 256, 0, st>>>(UNGRID_ARGS);       \
+      else { UNGRID_UY(GG, 1) }                                                   \
+    }                                                                             \
     break;
   switch (G) {
     case 1:
@@ -693,7 +696,10 @@ mrg_status launch_ungrid(const GridConst &gc, const FrameTraj &ft, const float2 
     UNGRID_CASE(8)
     UNGRID_CASE(16)
     default:
-      if (cpl == 2) { UNGRID_UY(32, 2) }
+      if (c32) {
+        if (cpl == 2) k_ungrid<32, 2, 1, 32><<<blocks, 256, 0, st>>>(UNGRID_ARGS);
+        else k_ungrid<32, 1, 1, 32><<<blocks, 256, 0, st>>>(UNGRID_ARGS);
+      } else if (cpl == 2) { UNGRID_UY(32, 2) }
       else { UNGRID_UY(32, 1) }
       break;
   }
