@@ -11,12 +11,12 @@
 // in TF32, each product within about 2^-20 of the FP32 one.
 //
 // One persistent 512-thread CTA per SM (four warpgroups, each thread owning the TMEM lane
-// of one point) walks its work items chunk by chunk.  Per chunk of 64 pairs: the pairs'
+// of one point) walks its work items chunk by chunk.  Per chunk of 96 pairs: the pairs'
 // records (first taps, tap weights, sample values) are copied with cp.async one chunk
-// ahead; the threads tabulate (wz*wy) and wx per pair, each warpgroup writes two k-steps
+// ahead; the threads tabulate (wz*wy) and wx per pair, each warpgroup writes three k-steps
 // of W (hi and lo, its threads' own rows) into tensor memory with tcgen05.st, all threads
-// write V into shared memory (K-major canonical layout), and one thread issues up to 24
-// MMAs (8 k-steps x 3 terms, A read from tensor memory) into one of two accumulator
+// write V into shared memory (K-major canonical layout), and one thread issues up to 36
+// MMAs (12 k-steps x 3 terms, A read from tensor memory) into one of two accumulator
 // slots, committing them to the slot's mbarrier.  While they run the CTA prepares the
 // next chunk in the other slot.  The tensor core adds into its accumulator rounding
 // toward zero (measured: bit-identical to an RZ emulation), so each chunk is summed from
@@ -34,7 +34,7 @@ namespace {
 
 __device__ int g_umma_error = 0;
 
-constexpr int TK = 64;      // pairs per chunk: eight k-steps of 8 TF32 values
+constexpr int TK = 96;      // pairs per chunk: twelve k-steps of 8 TF32 values
 constexpr int TP = TK + 4;  // row pitch (floats) of the per-pair weight tables: conflict-free 16-byte reads
 constexpr int NBLD = 512;   // builder threads: four warpgroups; warp w reaches TMEM lanes 32 (w % 4) .. + 31
 constexpr int NTHR = NBLD + 32;  // and one warp that issues the MMAs
@@ -250,7 +250,7 @@ __device__ __forceinline__ bool bld_and(bool v) {
 // CC coils per pass (blockIdx.y picks the chunk of coils), one persistent CTA per SM over
 // the work items; the CTA walks its items' chunks in order (an item without pairs is one
 // empty chunk).  Warps 0-15 build the operands: thread tid owns point tid % 128 (its TMEM
-// lane), warpgroup g = tid / 128 writes k-steps g and g + 4 of W and drains accumulator
+// lane), warpgroup g = tid / 128 writes k-steps g, g + 4, g + 8 of W and drains accumulator
 // columns [g NQ, g NQ + NQ).  Warp 16 issues the MMAs.  Per slot s: full[s] (the 16
 // builder warps arrive when the slot's operands are written) and done[s] (the MMAs'
 // commit, or a plain arrive for an empty chunk); the builders wait done[s] of chunk c - 2
@@ -381,9 +381,8 @@ __global__ void __launch_bounds__(NTHR, 1)
       const int4 *stt = reinterpret_cast<const int4 *>(stg + L::SV + L::SW);
       const int x0 = cur.it.x & 2047, y0 = (cur.it.x >> 11) & 2047, z0 = cur.it.x >> 22;
       // ---- per pair: (wz*wy) for the region's 4 y and 4 z planes, wx for its 8 x ----
-      {
-        const int k = tid >> 3, j = tid & 7;  // 64 pairs x 8 threads
-        const int zz = j >> 1, y2 = 2 * (j & 1);
+      for (int k = tid >> 3; k < 8 * ((nq + 7) >> 3); k += NBLD / 8) {  // 8 threads per pair
+        const int j = tid & 7, zz = j >> 1, y2 = 2 * (j & 1);
         float wyz0 = 0.f, wyz1 = 0.f, wx = 0.f;
         if (k < nq) {
           const int4 t = stt[k];
@@ -407,12 +406,12 @@ __global__ void __launch_bounds__(NTHR, 1)
         break;
       }
       const int nks = (nq + 7) >> 3;  // k-steps with pairs
-      // ---- W: this thread's row, k-steps wg and wg + 4, hi and lo, into tensor memory ----
+      // ---- W: this thread's row, k-steps wg, wg + 4, wg + 8, hi and lo, into tensor memory ----
       {
         const float *ryz = syz + (pz * 4 + py) * TP, *rxx = sx + px * TP;
         const uint32_t ta = lane_base + (uint32_t)(L::A0 + 2 * TK * slot);
 #pragma unroll
-        for (int h = 0; h < 2; h++) {
+        for (int h = 0; h < TK / 32; h++) {
           const int ks = wg + 4 * h;
           if (ks < nks) {
             const float4 a0 = *reinterpret_cast<const float4 *>(ryz + 8 * ks);
