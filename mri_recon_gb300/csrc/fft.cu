@@ -13,6 +13,8 @@
 // of a line, a twiddle, then a Q-point DFT in registers per thread (radices 2,
 // 3, 4, 5).  Twiddles exp(-2 pi i m / S) are computed on the host in double,
 // staged in shared memory per CTA and read as broadcasts.
+#include <algorithm>
+
 #include "mrg_internal.h"
 
 namespace mrg {
@@ -427,6 +429,94 @@ __global__ void __launch_bounds__(256, 2) k_fft(const FftPass p) {
   }
 }
 
+// Plain passes, persistent: a CTA walks tiles of IB lines (IB = P, no tile straddles an
+// outer row, 16-byte line-pair copies).  Once the Q-point step has read a tile's rows into
+// registers, the next tile's copies are issued into the same shared memory, so they run
+// while this tile is transformed and stored (straight from registers, rows t + 8 k2 of
+// line j: IB lines x 8 bytes contiguous per row).
+template <int Q, int SIGN, int P>
+__global__ void __launch_bounds__(8 * P) k_fft_pp(const FftPass p, int ntiles) {
+  constexpr int S = 8 * Q, IB = P, NPAIR = IB / 2;
+  extern __shared__ float2 sm[];  // [S][IB] data, then S twiddles
+  float2 *tw = sm + S * (IB + 1);
+  const int tid = threadIdx.x;
+  for (int m = tid; m < S; m += blockDim.x) tw[m] = p.tw[m];
+  const int j = tid % IB, t = tid / IB;
+  float2 *col = sm + j;
+  const int jp = tid % NPAIR, r0 = tid / NPAIR, rstep = blockDim.x / NPAIR;
+  const unsigned nib = (unsigned)p.nib;
+  auto issue = [&](int tile) {
+    const unsigned ob = (unsigned)tile / nib;
+    const int64_t i0 = (int64_t)((unsigned)tile - ob * nib) * IB;
+    const float2 *gs = p.in + (int64_t)ob * p.in_os + i0 + 2 * jp + (int64_t)r0 * p.in_ls;
+    const int64_t gstep = (int64_t)rstep * p.in_ls;
+    unsigned sa = (unsigned)__cvta_generic_to_shared(sm + (r0 + p.in_off) * IB + 2 * jp);
+    const unsigned sstep = (unsigned)(rstep * IB * (int)sizeof(float2));
+    for (int li = r0; li < p.Lin; li += rstep, gs += gstep, sa += sstep)
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gs));
+    for (int e = tid; e < (S - p.Lin) * IB; e += blockDim.x) {
+      const int jj = e % IB, k = e / IB;
+      const int r = (k < p.in_off) ? k : k + p.Lin;
+      sm[r * IB + jj] = make_float2(0.f, 0.f);
+    }
+    asm volatile("cp.async.commit_group;\n" ::);
+  };
+  int tile = blockIdx.x;
+  if (tile < ntiles) issue(tile);
+  for (; tile < ntiles; tile += gridDim.x) {
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    __syncthreads();
+    // ---- step A: 8-point DFTs over n1 (rows Q*n1 + n2), twiddle W_S^(n2*k1) ----
+    for (int n2 = t; n2 < Q; n2 += 8) {
+      float2 a[8];
+      float2 *c2 = col + n2 * IB;
+#pragma unroll
+      for (int n1 = 0; n1 < 8; n1++) a[n1] = c2[Q * n1 * IB];
+      reg_fft<8, SIGN, S>(a, tw);
+#pragma unroll
+      for (int k1 = 1; k1 < 8; k1++) a[k1] = cmul(a[k1], twid<SIGN>(tw, n2 * k1));
+#pragma unroll
+      for (int k1 = 0; k1 < 8; k1++) c2[Q * k1 * IB] = a[k1];
+    }
+    __syncthreads();
+    // ---- step C: rows Q*t .. Q*t+Q-1 into registers; then the buffer is free ----
+    float2 v[Q];
+    const float2 *cq = col + Q * t * IB;
+#pragma unroll
+    for (int n2 = 0; n2 < Q; n2++) v[n2] = cq[n2 * IB];
+    __syncthreads();
+    if (tile + (int)gridDim.x < ntiles) issue(tile + gridDim.x);
+    reg_fft<Q, SIGN, S>(v, tw);
+    const unsigned ob = (unsigned)tile / nib;
+    const int64_t i = (int64_t)((unsigned)tile - ob * nib) * IB + j;
+    float2 *go = p.out + (int64_t)ob * p.out_os + i;
+    const float sc = p.scale;
+#pragma unroll
+    for (int k2 = 0; k2 < Q; k2++) {
+      const int r = t + 8 * k2 - p.out_off;
+      if (r >= 0 && r < p.Lout) go[(int64_t)r * p.out_ls] = make_float2(v[k2].x * sc, v[k2].y * sc);
+    }
+  }
+}
+
+template <int Q, int SIGN, int P>
+static mrg_status launch_pp(const FftPass &pp, cudaStream_t st) {
+  const size_t smem = (size_t)8 * Q * (P + 2) * sizeof(float2);
+  static int ctas = 0;
+  if (!ctas) {
+    MRG_CUDA(cudaFuncSetAttribute(k_fft_pp<Q, SIGN, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    MRG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctas, k_fft_pp<Q, SIGN, P>, 8 * P, smem));
+    if (ctas < 1) ctas = 1;
+  }
+  int sms = 152;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+  const int ntiles = (int)(pp.nlines / P);
+  const int nblk = std::max(1, std::min(ntiles, sms * ctas));
+  k_fft_pp<Q, SIGN, P><<<nblk, 8 * P, smem, st>>>(pp, ntiles);
+  MRG_LAUNCHED();
+  return MRG_OK;
+}
+
 // Q values that get kernels with a compile-time pitch (lines of 192..384 points)
 constexpr bool fixed_pitch_q(int Q) { return Q >= 24; }
 
@@ -462,6 +552,12 @@ static mrg_status launch_q(const FftPass &p, cudaStream_t st) {
   // CTAs that never straddle an outer row find their row with one 32-bit division
   pp.nib = (p.inner % p.IB == 0 && p.nlines % p.inner == 0) ? (int)(p.inner / p.IB) : 0;
   if constexpr (fixed_pitch_q(Q)) {
+    // plain passes whose tiles never straddle an outer row and copy line pairs: persistent
+    if (p.mode == FFT_PLAIN && !p.lfast && pp.nib && p.vec16 && p.nlines / p.IB <= 0x7fffffff &&
+        (p.IB == 16 || p.IB == 32)) {
+      if (p.IB == 16) return p.sign < 0 ? launch_pp<Q, -1, 16>(pp, st) : launch_pp<Q, +1, 16>(pp, st);
+      return p.sign < 0 ? launch_pp<Q, -1, 32>(pp, st) : launch_pp<Q, +1, 32>(pp, st);
+    }
     if (!p.lfast && p.IB == 32) return launch_qp<Q, 32>(pp, grid, block, smem, st);
     if (!p.lfast && p.IB == 16) return launch_qp<Q, 16>(pp, grid, block, smem, st);
   }
