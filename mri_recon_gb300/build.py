@@ -45,7 +45,8 @@ def _compile(src, obj, verbose_ptxas):
 def build(force=False, verbose_ptxas=False, jobs=None):
     os.makedirs(OUT, exist_ok=True)
     srcs = sorted(glob.glob(os.path.join(SRC, "*.cu")) + glob.glob(os.path.join(SRC, "*.cpp")))
-    headers = glob.glob(os.path.join(SRC, "*.h")) + glob.glob(os.path.join(ROOT, "include", "*.h"))
+    headers = (glob.glob(os.path.join(SRC, "*.h")) + glob.glob(os.path.join(SRC, "*.cuh")) +
+               glob.glob(os.path.join(ROOT, "include", "*.h")))
     hdr_t = max(os.path.getmtime(h) for h in headers)
     todo, objs = [], []
     for s in srcs:

@@ -1,0 +1,546 @@
+// Kernels of the batched strided FFT passes, shared by the translation units that
+// instantiate them for different line lengths (fft.cu, fft_large.cu, fft_large2.cu).
+//
+// Replaces the per-axis line FFTs of NDarray::fft3 (src/ArrayTemplates.cpp:276-427)
+// as used by gridFFT::do_fft / do_ifft (src/gridFFT.cpp:645-711): every axis is
+// transformed with FFTW's sign convention (forward = exp(-i...)) and scaled by
+// 1/sqrt(S).  The E side is pruned (only the crop of the image is non-zero) and
+// the E^H side only produces the crop it keeps, which is exact because the
+// dropped inputs are zero and the dropped outputs are never read.
+//
+// One CTA transforms IB lines (consecutive "inner" elements, coalesced rows of
+// IB complex values) of length S = 8*Q held in shared memory as [S][IB+1].
+// Each line is split S = 8 x Q (four-step): 8-point DFTs across the 8 threads
+// of a line, a twiddle, then a Q-point DFT in registers per thread (radices 2,
+// 3, 4, 5).  Twiddles exp(-2 pi i m / S) are computed on the host in double,
+// staged in shared memory per CTA and read as broadcasts.
+#pragma once
+
+#include <algorithm>
+
+#include "mrg_internal.h"
+
+namespace mrg {
+
+// per-size twiddle tables exp(-2 pi i m / S), m < S, built once per device (fft.cu)
+extern float2 *g_tw[1024];
+
+// lengths 192..288 (fft_large.cu) and 320..384 (fft_large2.cu)
+mrg_status launch_fft_192_288(const FftPass &p, cudaStream_t st);
+mrg_status launch_fft_320_384(const FftPass &p, cudaStream_t st);
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+// SIGN * i * a
+template <int SIGN>
+__device__ __forceinline__ float2 imul(float2 a) {
+  return SIGN > 0 ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
+}
+template <int SIGN>
+__device__ __forceinline__ float2 twid(const float2 *tw, int m) {
+  float2 w = tw[m];
+  if (SIGN > 0) w.y = -w.y;
+  return w;
+}
+
+// t[q] <- sum_p t[p] * exp(SIGN*2*pi*i*p*q/P)
+template <int P, int SIGN>
+__device__ __forceinline__ void bfly(float2 (&t)[P]) {
+  if constexpr (P == 2) {
+    float2 a = t[0], b = t[1];
+    t[0] = cadd(a, b);
+    t[1] = csub(a, b);
+  } else if constexpr (P == 3) {
+    const float h = 0.86602540378443864676f;
+    float2 s = cadd(t[1], t[2]), d = csub(t[1], t[2]);
+    float2 m = make_float2(t[0].x - 0.5f * s.x, t[0].y - 0.5f * s.y);
+    float2 r = imul<SIGN>(make_float2(h * d.x, h * d.y));
+    t[0] = cadd(t[0], s);
+    t[1] = cadd(m, r);
+    t[2] = csub(m, r);
+  } else if constexpr (P == 4) {
+    float2 a = cadd(t[0], t[2]), b = csub(t[0], t[2]);
+    float2 c = cadd(t[1], t[3]), d = imul<SIGN>(csub(t[1], t[3]));
+    t[0] = cadd(a, c);
+    t[2] = csub(a, c);
+    t[1] = cadd(b, d);
+    t[3] = csub(b, d);
+  } else if constexpr (P == 5) {
+    const float c1 = 0.30901699437494742410f, c2 = -0.80901699437494742410f;
+    const float s1 = 0.95105651629515357212f, s2 = 0.58778525229247312917f;
+    const float2 a1 = cadd(t[1], t[4]), a2 = cadd(t[2], t[3]);
+    const float2 b1 = csub(t[1], t[4]), b2 = csub(t[2], t[3]);
+    const float2 m1 = make_float2(t[0].x + c1 * a1.x + c2 * a2.x, t[0].y + c1 * a1.y + c2 * a2.y);
+    const float2 m2 = make_float2(t[0].x + c2 * a1.x + c1 * a2.x, t[0].y + c2 * a1.y + c1 * a2.y);
+    const float2 r1 = imul<SIGN>(make_float2(s1 * b1.x + s2 * b2.x, s1 * b1.y + s2 * b2.y));
+    const float2 r2 = imul<SIGN>(make_float2(s2 * b1.x - s1 * b2.x, s2 * b1.y - s1 * b2.y));
+    t[0] = cadd(t[0], cadd(a1, a2));
+    t[1] = cadd(m1, r1);
+    t[4] = csub(m1, r1);
+    t[2] = cadd(m2, r2);
+    t[3] = csub(m2, r2);
+  } else {
+    static_assert(P == 2 || P == 3 || P == 4 || P == 5, "radix");
+  }
+}
+
+constexpr int first_factor(int q) { return (q % 4 == 0) ? 4 : ((q % 2 == 0) ? 2 : ((q % 3 == 0) ? 3 : 5)); }
+
+// In-register DFT of length Q (decimation in time), natural order in and out;
+// tw is the length-S table, S a multiple of Q.
+template <int Q, int SIGN, int S>
+__device__ __forceinline__ void reg_fft(float2 (&v)[Q], const float2 *tw) {
+  if constexpr (Q == 1) {
+    return;
+  } else {
+    constexpr int P = first_factor(Q);
+    constexpr int Q2 = Q / P;
+    float2 sub[P][Q2];
+#pragma unroll
+    for (int p = 0; p < P; p++)
+#pragma unroll
+      for (int m = 0; m < Q2; m++) sub[p][m] = v[p + P * m];
+#pragma unroll
+    for (int p = 0; p < P; p++) reg_fft<Q2, SIGN, S>(sub[p], tw);
+#pragma unroll
+    for (int k = 0; k < Q2; k++) {
+      float2 t[P];
+#pragma unroll
+      for (int p = 0; p < P; p++) t[p] = (p * k == 0) ? sub[p][k] : cmul(sub[p][k], twid<SIGN>(tw, p * k * (S / Q)));
+      bfly<P, SIGN>(t);
+#pragma unroll
+      for (int q = 0; q < P; q++) v[k + Q2 * q] = t[q];
+    }
+  }
+}
+
+// Deapodisation weight of element l of line (o, i), the reference's (winz * winy) * winx
+// (src/gridFFT.cpp:972-986, :926-941): per-line factor `lw` from line_weight, then
+// elem_weight for the element.
+__device__ __forceinline__ float line_weight(const FftPass &p, int64_t o, int64_t i) {
+  if (p.wmode) return p.wo[o / p.wdiv] * p.wi[o % p.wdiv];  // winz * winy of the line's row
+  return 0.0f;
+}
+__device__ __forceinline__ float elem_weight(const FftPass &p, float lw, float wl_l, int64_t o, int64_t i) {
+  if (p.wmode) return lw * wl_l;                  // (winz * winy) * winx
+  return (wl_l * p.wo[o]) * p.wi[i / p.C];         // (winz * winy) * winx along z
+}
+
+// P: shared-memory row pitch when it is a compile-time constant (IB = P lines, no
+// padding), else 0 (pitch and IB from the pass).  With P fixed every shared-memory
+// address in the transform steps is the thread's base plus a constant.
+template <int Q, int SIGN, int MODE, int P>
+__global__ void __launch_bounds__(256, 2) k_fft(const FftPass p) {
+  constexpr int S = 8 * Q;
+  extern __shared__ float2 sm[];  // [S][IBp] data, then S twiddles
+  const int IB = P ? P : p.IB;
+  const int IBp = P ? P : (p.lfast ? p.IB + 1 : p.IB);  // pad only for column-wise (contiguous-line) access
+  const int tid = threadIdx.x;
+  float2 *tw = sm + S * (IB + 1);
+  for (int m = tid; m < S; m += blockDim.x) tw[m] = p.tw[m];
+  const int j = tid % IB, t = tid / IB;  // 8 threads per line
+  // Line (o, i) of the CTA's IB lines.  When inner % IB == 0 (nib = inner / IB) every line
+  // of the CTA shares o and one 32-bit division per thread finds it.
+  int64_t o0 = 0, i0 = 0;
+  if (p.nib) {
+    const unsigned b = blockIdx.x, ob = b / (unsigned)p.nib;
+    o0 = ob;
+    i0 = (int64_t)(b - ob * (unsigned)p.nib) * IB;
+  }
+  const int64_t line = (int64_t)blockIdx.x * IB + j;
+  const bool lv = line < p.nlines;
+  int64_t o = 0, i = 0;
+  if (p.nib) {
+    o = o0;
+    i = i0 + j;
+  } else if (lv) {
+    o = line / p.inner;
+    i = line - o * p.inner;
+  }
+  float2 *col = sm + j;  // this thread's column
+
+  // ---- load (zero rows outside [in_off, in_off + Lin)) ----
+  if (p.vec16 && !(MODE == FFT_SETIMG && !p.has_smap)) {
+    // 16-byte asynchronous copies (two adjacent lines per copy), many in flight
+    const int npair = IB >> 1;
+    const int jp = tid % npair, r0 = tid / npair, rstep = blockDim.x / npair;
+    const int64_t ln = (int64_t)blockIdx.x * IB + 2 * jp;
+    const bool pv = ln < p.nlines;
+    int64_t po = 0, pi = 0;
+    if (p.nib) {
+      po = o0;
+      pi = i0 + 2 * jp;
+    } else if (pv) {
+      po = ln / p.inner;
+      pi = ln - po * p.inner;
+    }
+    const float2 *src = (MODE == FFT_SETIMG) ? p.smap : p.in;
+    const float2 *gs = src + po * p.in_os + pi + (int64_t)r0 * p.in_ls;
+    const int64_t gstep = (int64_t)rstep * p.in_ls;
+    unsigned sa = (unsigned)__cvta_generic_to_shared(sm + (r0 + p.in_off) * IBp + 2 * jp);
+    const unsigned sstep = (unsigned)(rstep * IBp * (int)sizeof(float2));
+    if (pv) {
+      for (int li = r0; li < p.Lin; li += rstep, gs += gstep, sa += sstep)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gs));
+    } else {
+      for (int li = r0; li < p.Lin; li += rstep)
+        *reinterpret_cast<float4 *>(sm + (li + p.in_off) * IBp + 2 * jp) = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    for (int e = tid; e < (S - p.Lin) * IB; e += blockDim.x) {
+      const int jj = e % IB, k = e / IB;
+      const int r = (k < p.in_off) ? k : k + p.Lin;
+      sm[r * IBp + jj] = make_float2(0.f, 0.f);
+    }
+    asm volatile("cp.async.commit_group;\n" ::);
+    asm volatile("cp.async.wait_group 0;\n" ::);
+    __syncthreads();
+    if constexpr (MODE == FFT_SETIMG) {
+      // image = (winz*winy)*winx * X * smap  (src/gridFFT.cpp:972-986); smap already in smem
+      if (lv) {
+        const int64_t ib = o * p.in_os + i;
+        const float lw = line_weight(p, o, i);
+        const int64_t xb = ib / p.C, xs = p.in_ls / p.C;  // X has no coil axis
+        for (int l0 = t; l0 < p.Lin; l0 += 64) {
+          float2 xv[8];
+          float wv[8];
+#pragma unroll
+          for (int k = 0; k < 8; k++) {  // 8 independent loads in flight
+            const int li = l0 + 8 * k;
+            if (li < p.Lin) {
+              xv[k] = __ldg(p.X + xb + (int64_t)li * xs);
+              wv[k] = __ldg(p.wl + li);
+            }
+          }
+#pragma unroll
+          for (int k = 0; k < 8; k++) {
+            const int li = l0 + 8 * k;
+            if (li < p.Lin) {
+              const float w = elem_weight(p, lw, wv[k], o, i);
+              float2 *d = col + (li + p.in_off) * IBp;
+              *d = cmul(make_float2(w * xv[k].x, w * xv[k].y), *d);
+            }
+          }
+        }
+      }
+      __syncthreads();
+    }
+  } else if (!p.lfast) {
+    const int64_t ib = o * p.in_os + i;
+    for (int r = t; r < S; r += 8) {
+      float2 v = make_float2(0.f, 0.f);
+      const int li = r - p.in_off;
+      if (lv && li >= 0 && li < p.Lin) {
+        const int64_t off = ib + (int64_t)li * p.in_ls;
+        if constexpr (MODE == FFT_SETIMG) {
+          const int64_t vox = off / p.C;
+          const float w = elem_weight(p, line_weight(p, o, i), p.wl[li], o, i);
+          const float2 x = p.X[vox];
+          v = make_float2(w * x.x, w * x.y);
+          if (p.has_smap) v = cmul(v, p.smap[off]);
+        } else {
+          v = p.in[off];
+        }
+      }
+      col[r * IBp] = v;
+    }
+    __syncthreads();
+  } else {
+    // inner == 1 and in_ls == 1: each line is contiguous; sweep along lines.
+    const int64_t l0 = (int64_t)blockIdx.x * IB;
+    for (int e = tid; e < S * IB; e += blockDim.x) {
+      const int jj = e / S, r = e - jj * S;
+      float2 v = make_float2(0.f, 0.f);
+      const int li = r - p.in_off;
+      const int64_t ln = l0 + jj;
+      if (ln < p.nlines && li >= 0 && li < p.Lin) v = p.in[ln * p.in_os + li];
+      sm[r * IBp + jj] = v;
+    }
+    __syncthreads();
+  }
+
+  // ---- step A: 8-point DFTs over n1 (rows Q*n1 + n2), twiddle W_S^(n2*k1) ----
+  for (int n2 = t; n2 < Q; n2 += 8) {
+    float2 a[8];
+    float2 *c2 = col + n2 * IBp;
+#pragma unroll
+    for (int n1 = 0; n1 < 8; n1++) a[n1] = c2[Q * n1 * IBp];
+    reg_fft<8, SIGN, S>(a, tw);
+#pragma unroll
+    for (int k1 = 1; k1 < 8; k1++) a[k1] = cmul(a[k1], twid<SIGN>(tw, n2 * k1));
+#pragma unroll
+    for (int k1 = 0; k1 < 8; k1++) c2[Q * k1 * IBp] = a[k1];
+  }
+  __syncthreads();
+
+  // ---- step C: Q-point DFT of rows Q*t .. Q*t+Q-1 -> rows t + 8*k2 ----
+  {
+    float2 v[Q];
+    const float2 *cq = col + Q * t * IBp;
+#pragma unroll
+    for (int n2 = 0; n2 < Q; n2++) v[n2] = cq[n2 * IBp];
+    reg_fft<Q, SIGN, S>(v, tw);
+    __syncthreads();
+    float2 *ct = col + t * IBp;
+#pragma unroll
+    for (int k2 = 0; k2 < Q; k2++) ct[8 * k2 * IBp] = v[k2];
+  }
+  __syncthreads();
+
+  // ---- store ----
+  if constexpr (MODE != FFT_ACCUM) {
+    if (p.vec16o) {
+      const int npair = IB >> 1;
+      const int jp = tid % npair, r0 = tid / npair, rstep = blockDim.x / npair;
+      const int64_t ln = (int64_t)blockIdx.x * IB + 2 * jp;
+      if (ln < p.nlines) {
+        int64_t po, pi;
+        if (p.nib) {
+          po = o0;
+          pi = i0 + 2 * jp;
+        } else {
+          po = ln / p.inner;
+          pi = ln - po * p.inner;
+        }
+        float4 *ob = reinterpret_cast<float4 *>(p.out + po * p.out_os + pi + (int64_t)r0 * p.out_ls);
+        const int64_t ostep = (int64_t)rstep * (p.out_ls / 2);
+        const float4 *sv = reinterpret_cast<const float4 *>(sm + (r0 + p.out_off) * IBp + 2 * jp);
+        const int svstep = rstep * IBp / 2;
+        const float sc = p.scale;
+#pragma unroll 4
+        for (int r = r0; r < p.Lout; r += rstep, ob += ostep, sv += svstep) {
+          const float4 v = *sv;
+          *ob = make_float4(v.x * sc, v.y * sc, v.z * sc, v.w * sc);
+        }
+      }
+    } else if (!p.lfast) {
+      if (lv) {
+        const int64_t ob = o * p.out_os + i;
+        for (int r = t; r < p.Lout; r += 8) {
+          float2 v = col[(r + p.out_off) * IBp];
+          p.out[ob + (int64_t)r * p.out_ls] = make_float2(v.x * p.scale, v.y * p.scale);
+        }
+      }
+    } else {
+      const int64_t l0 = (int64_t)blockIdx.x * IB;
+      for (int e = tid; e < p.Lout * IB; e += blockDim.x) {
+        const int jj = e / p.Lout, r = e - jj * p.Lout;
+        const int64_t ln = l0 + jj;
+        if (ln < p.nlines) {
+          float2 v = sm[(r + p.out_off) * IBp + jj];
+          p.out[ln * p.out_os + r] = make_float2(v.x * p.scale, v.y * p.scale);
+        }
+      }
+    }
+  } else {
+    // X += sum_c (wl*wo*wi) * v * conj(smap)   (gridFFT::accumulate, src/gridFFT.cpp:926-941)
+    const int C = p.C;
+    if (lv) {
+      const int64_t sb = o * p.out_os + i;
+      const float lw = line_weight(p, o, i);
+      for (int r0 = t; r0 < p.Lout; r0 += 64) {
+        float2 sv[8];
+        float wv[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) {  // 8 independent smap loads in flight
+          const int r = r0 + 8 * k;
+          if (r < p.Lout) {
+            sv[k] = p.has_smap ? __ldg(p.smap + sb + (int64_t)r * p.out_ls) : make_float2(1.f, 0.f);
+            wv[k] = __ldg(p.wl + r);
+          }
+        }
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+          const int r = r0 + 8 * k;
+          if (r >= p.Lout) continue;
+          float2 v = col[(r + p.out_off) * IBp];
+          v = make_float2(v.x * p.scale, v.y * p.scale);
+          const float w = elem_weight(p, lw, wv[k], o, i);
+          v = make_float2(w * v.x, w * v.y);
+          if (p.has_smap) {
+            float2 s2 = sv[k];
+            s2.y = -s2.y;
+            v = cmul(v, s2);
+          }
+          if (p.acc_atomic) {
+            float2 *dst = p.acc + (int64_t)r * p.acc_l + o * p.acc_o + i / C;
+            atomicAdd(&dst->x, v.x);
+            atomicAdd(&dst->y, v.y);
+          } else {
+            col[(r + p.out_off) * IBp] = v;
+          }
+        }
+      }
+    }
+    if (!p.acc_atomic) {
+      __syncthreads();
+      // IB is a multiple of C: the C lines of one voxel are consecutive in this CTA.
+      const int G = IB / C;
+      const int64_t line0 = (int64_t)blockIdx.x * IB;
+      for (int e = tid; e < p.Lout * G; e += blockDim.x) {
+        const int g = e % G, r = e / G;
+        const int64_t ln = line0 + (int64_t)g * C;
+        if (ln >= p.nlines) continue;
+        int64_t oo, ii;
+        if (p.nib) {
+          oo = o0;
+          ii = i0 + (int64_t)g * C;
+        } else {
+          oo = ln / p.inner;
+          ii = ln - oo * p.inner;
+        }
+        // rotated start (coil (c + r) mod C at step c): the rows of neighbouring threads sit
+        // IBp apart, a multiple of the 32 banks, so the same coil index would hit one bank
+        float2 s = make_float2(0.f, 0.f);
+        const float2 *row = sm + (r + p.out_off) * IBp + g * C;
+        int cc = r % C;
+        for (int c = 0; c < C; c++) {
+          s = cadd(s, row[cc]);
+          cc = (cc + 1 == C) ? 0 : cc + 1;
+        }
+        float2 *dst = p.acc + (int64_t)r * p.acc_l + oo * p.acc_o + ii / C;
+        float2 cur = *dst;
+        *dst = cadd(cur, s);
+      }
+    }
+  }
+}
+
+// Plain passes, persistent: a CTA walks tiles of IB lines (IB = P, no tile straddles an
+// outer row, 16-byte line-pair copies).  Once the Q-point step has read a tile's rows into
+// registers, the next tile's copies are issued into the same shared memory, so they run
+// while this tile is transformed and stored (straight from registers, rows t + 8 k2 of
+// line j: IB lines x 8 bytes contiguous per row).
+template <int Q, int SIGN, int P>
+__global__ void __launch_bounds__(8 * P) k_fft_pp(const FftPass p, int ntiles) {
+  constexpr int S = 8 * Q, IB = P, NPAIR = IB / 2;
+  extern __shared__ float2 sm[];  // [S][IB] data, then S twiddles
+  float2 *tw = sm + S * (IB + 1);
+  const int tid = threadIdx.x;
+  for (int m = tid; m < S; m += blockDim.x) tw[m] = p.tw[m];
+  const int j = tid % IB, t = tid / IB;
+  float2 *col = sm + j;
+  const int jp = tid % NPAIR, r0 = tid / NPAIR, rstep = blockDim.x / NPAIR;
+  const unsigned nib = (unsigned)p.nib;
+  auto issue = [&](int tile) {
+    const unsigned ob = (unsigned)tile / nib;
+    const int64_t i0 = (int64_t)((unsigned)tile - ob * nib) * IB;
+    const float2 *gs = p.in + (int64_t)ob * p.in_os + i0 + 2 * jp + (int64_t)r0 * p.in_ls;
+    const int64_t gstep = (int64_t)rstep * p.in_ls;
+    unsigned sa = (unsigned)__cvta_generic_to_shared(sm + (r0 + p.in_off) * IB + 2 * jp);
+    const unsigned sstep = (unsigned)(rstep * IB * (int)sizeof(float2));
+    for (int li = r0; li < p.Lin; li += rstep, gs += gstep, sa += sstep)
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gs));
+    for (int e = tid; e < (S - p.Lin) * IB; e += blockDim.x) {
+      const int jj = e % IB, k = e / IB;
+      const int r = (k < p.in_off) ? k : k + p.Lin;
+      sm[r * IB + jj] = make_float2(0.f, 0.f);
+    }
+    asm volatile("cp.async.commit_group;\n" ::);
+  };
+  int tile = blockIdx.x;
+  if (tile < ntiles) issue(tile);
+  for (; tile < ntiles; tile += gridDim.x) {
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    __syncthreads();
+    // ---- step A: 8-point DFTs over n1 (rows Q*n1 + n2), twiddle W_S^(n2*k1) ----
+    for (int n2 = t; n2 < Q; n2 += 8) {
+      float2 a[8];
+      float2 *c2 = col + n2 * IB;
+#pragma unroll
+      for (int n1 = 0; n1 < 8; n1++) a[n1] = c2[Q * n1 * IB];
+      reg_fft<8, SIGN, S>(a, tw);
+#pragma unroll
+      for (int k1 = 1; k1 < 8; k1++) a[k1] = cmul(a[k1], twid<SIGN>(tw, n2 * k1));
+#pragma unroll
+      for (int k1 = 0; k1 < 8; k1++) c2[Q * k1 * IB] = a[k1];
+    }
+    __syncthreads();
+    // ---- step C: rows Q*t .. Q*t+Q-1 into registers; then the buffer is free ----
+    float2 v[Q];
+    const float2 *cq = col + Q * t * IB;
+#pragma unroll
+    for (int n2 = 0; n2 < Q; n2++) v[n2] = cq[n2 * IB];
+    __syncthreads();
+    if (tile + (int)gridDim.x < ntiles) issue(tile + gridDim.x);
+    reg_fft<Q, SIGN, S>(v, tw);
+    const unsigned ob = (unsigned)tile / nib;
+    const int64_t i = (int64_t)((unsigned)tile - ob * nib) * IB + j;
+    float2 *go = p.out + (int64_t)ob * p.out_os + i;
+    const float sc = p.scale;
+#pragma unroll
+    for (int k2 = 0; k2 < Q; k2++) {
+      const int r = t + 8 * k2 - p.out_off;
+      if (r >= 0 && r < p.Lout) go[(int64_t)r * p.out_ls] = make_float2(v[k2].x * sc, v[k2].y * sc);
+    }
+  }
+}
+
+template <int Q, int SIGN, int P>
+static mrg_status launch_pp(const FftPass &pp, cudaStream_t st) {
+  const size_t smem = (size_t)8 * Q * (P + 2) * sizeof(float2);
+  static int ctas = 0;
+  if (!ctas) {
+    MRG_CUDA(cudaFuncSetAttribute(k_fft_pp<Q, SIGN, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    MRG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctas, k_fft_pp<Q, SIGN, P>, 8 * P, smem));
+    if (ctas < 1) ctas = 1;
+  }
+  int sms = 152;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+  const int ntiles = (int)(pp.nlines / P);
+  const int nblk = std::max(1, std::min(ntiles, sms * ctas));
+  k_fft_pp<Q, SIGN, P><<<nblk, 8 * P, smem, st>>>(pp, ntiles);
+  MRG_LAUNCHED();
+  return MRG_OK;
+}
+
+// Q values that get kernels with a compile-time pitch (lines of 192..384 points)
+constexpr bool fixed_pitch_q(int Q) { return Q >= 24; }
+
+template <int Q, int P>
+static mrg_status launch_qp(const FftPass &pp, const dim3 grid, const dim3 block, size_t smem, cudaStream_t st) {
+  void (*fn)(const FftPass);
+  if (pp.mode == FFT_SETIMG) fn = k_fft<Q, -1, FFT_SETIMG, P>;
+  else if (pp.mode == FFT_ACCUM) fn = k_fft<Q, +1, FFT_ACCUM, P>;
+  else if (pp.sign < 0) fn = k_fft<Q, -1, FFT_PLAIN, P>;
+  else fn = k_fft<Q, +1, FFT_PLAIN, P>;
+  static int attr_set[4] = {0, 0, 0, 0};  // per instantiation: set the smem cap once
+  const int slot = pp.mode == FFT_PLAIN ? (pp.sign < 0 ? 0 : 1) : (pp.mode == FFT_SETIMG ? 2 : 3);
+  if (!attr_set[slot]) {
+    MRG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 8 * Q * 34 * (int)sizeof(float2)));
+    attr_set[slot] = 1;
+  }
+  fn<<<grid, block, smem, st>>>(pp);
+  MRG_LAUNCHED();
+  return MRG_OK;
+}
+
+template <int Q>
+static mrg_status launch_q(const FftPass &p, cudaStream_t st) {
+  const size_t smem = (size_t)8 * Q * (p.IB + 2) * sizeof(float2);
+  const int64_t nblk64 = (p.nlines + p.IB - 1) / p.IB;
+  if (nblk64 > 0x7fffffff) {
+    set_error("fft pass too large");
+    return MRG_ERR_UNSUPPORTED;
+  }
+  const dim3 grid((unsigned)nblk64), block(8 * p.IB);
+  FftPass pp = p;
+  pp.tw = g_tw[8 * Q];
+  // CTAs that never straddle an outer row find their row with one 32-bit division
+  pp.nib = (p.inner % p.IB == 0 && p.nlines % p.inner == 0) ? (int)(p.inner / p.IB) : 0;
+  if constexpr (fixed_pitch_q(Q)) {
+    // plain passes whose tiles never straddle an outer row and copy line pairs: persistent
+    if (p.mode == FFT_PLAIN && !p.lfast && pp.nib && p.vec16 && p.nlines / p.IB <= 0x7fffffff &&
+        (p.IB == 16 || p.IB == 32)) {
+      if (p.IB == 16) return p.sign < 0 ? launch_pp<Q, -1, 16>(pp, st) : launch_pp<Q, +1, 16>(pp, st);
+      return p.sign < 0 ? launch_pp<Q, -1, 32>(pp, st) : launch_pp<Q, +1, 32>(pp, st);
+    }
+    if (!p.lfast && p.IB == 32) return launch_qp<Q, 32>(pp, grid, block, smem, st);
+    if (!p.lfast && p.IB == 16) return launch_qp<Q, 16>(pp, grid, block, smem, st);
+  }
+  return launch_qp<Q, 0>(pp, grid, block, smem, st);
+}
+
+}  // namespace mrg

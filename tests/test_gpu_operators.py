@@ -43,7 +43,9 @@ def _oracle_EH(O, c, prec):
     return X
 
 
-@pytest.mark.parametrize("N,C,nproj", [(32, 4, 700), (64, 8, 1500), (48, 3, 500)])
+# N = 8, 16, 40, 80: oversampled lines of 16, 32, 64 and 128 points
+@pytest.mark.parametrize("N,C,nproj", [(32, 4, 700), (64, 8, 1500), (48, 3, 500), (8, 2, 60), (16, 4, 200),
+                                       (40, 3, 600), (80, 2, 1500)])
 def test_forward_E_matches_oracle(mrg_lib, oracle_lib, N, C, nproj):
     torch = _torch()
     c = case(N=N, C=C, nproj=nproj)
@@ -63,7 +65,8 @@ def test_forward_residual_matches_oracle(mrg_lib, oracle_lib):
     assert rel(y, _oracle_E(oracle_lib, c, 0, diff=c["data"])) < TOL
 
 
-@pytest.mark.parametrize("N,C,nproj", [(32, 4, 700), (64, 8, 1500), (48, 3, 500), (32, 20, 400)])
+@pytest.mark.parametrize("N,C,nproj", [(32, 4, 700), (64, 8, 1500), (48, 3, 500), (32, 20, 400), (8, 2, 60),
+                                       (16, 4, 200), (40, 3, 600), (80, 2, 1500), (168, 1, 1500)])
 def test_adjoint_EH_matches_oracle(mrg_lib, oracle_lib, N, C, nproj):
     torch = _torch()
     c = case(N=N, C=C, nproj=nproj)
