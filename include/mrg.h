@@ -230,7 +230,52 @@ void mrg_fista_params_default(mrg_fista_params *p);
 mrg_status mrg_fista(mrg_plan *plan, const mrg_fista_params *params, void *X, double *resid, float *step,
                      int use_graph, void *stream);
 
+/* CLEAR: per-coil images with a coil low-rank constraint (the CLEAR recon_type,
+ * src/recon_lib.cpp:1025-1238; LOWRANKCOIL with dim = 2, src/clear.cpp:99-232, :561-914).
+ * Each iteration: R_c = E_c^H W (E_c X_c - d_c) per coil image (E_c without coil maps),
+ * step X_c -= (sum |R|^2 / sum P conj(R)) R_c with P_c = E_c^H W E_c R_c, then the coil
+ * low-rank threshold of the X_c.  The coil images are combined at the end by the first
+ * right singular vector of each block.  Coil maps are not used; frame trajectories and
+ * data must be set.  The soft threshold of the reference's loop is off here (its
+ * default, threshold_type none).  ncoil <= 32. */
+typedef struct mrg_clear_params {
+  int max_iter;            /* -max_iter */
+  int block[3];            /* -clear_nx/ny/nz (default 4) */
+  int block_iter;          /* -clear_block_iter (default 4) */
+  float alpha_coil;        /* -clear_alpha_coil (default 0.01; 0: no threshold) */
+  float clear_amp;         /* -clear_amp (default 4) */
+  float clear_t2;          /* -clear_t2 (default 6) */
+  float early_stop_thresh; /* -early_stop_thresh (default 0: never) */
+  int early_stop_range;    /* -early_stop_range (default 5) */
+  int64_t rand_skip;       /* rand() draws consumed before the first block shift (default 0) */
+} mrg_clear_params;
+
+void mrg_clear_params_default(mrg_clear_params *p);
+
+/* X: nframes combined images (output, host or device).  coil_images (may be NULL): the
+ * final per-coil images as nframes x nvox x ncoil complex64, coil innermost (the
+ * reference writes them to ClearRaw.h5).  resid (host, may be NULL): sum |R|^2 of each
+ * iteration run.  iters (host, may be NULL): iterations run (fewer than max_iter after an
+ * early stop). */
+mrg_status mrg_clear(mrg_plan *plan, const mrg_clear_params *params, void *X, void *coil_images, double *resid,
+                     int *iters, void *stream);
+
 /* Building blocks exposed for drop-in use and parity tests. */
+/* LOWRANKCOIL::update_threshold with dim = 2 (src/clear.cpp:99-232) on nframes x nvox x
+ * ncoil complex64 (coil innermost): median of the blocks' non-zero sigma_1 times
+ * (1 + clear_amp exp(-iteration / clear_t2)) into *smax (host). */
+mrg_status mrg_clear_update_threshold(const void *X, int nframes, int ncoil, int Nx, int Ny, int Nz,
+                                      const int block[3], float clear_amp, float clear_t2, int iteration,
+                                      float *smax, void *stream);
+/* LOWRANKCOIL::thresh with dim = 2 (src/clear.cpp:561-813), in place, block shifts drawn
+ * from the rand() stream after rand_skip draws. */
+mrg_status mrg_clear_thresh(void *X, int nframes, int ncoil, int Nx, int Ny, int Nz, const int block[3],
+                            int block_iter, float alpha, float smax, int64_t rand_skip, void *stream);
+/* LOWRANKCOIL::combine (src/clear.cpp:815-914): out (nframes x nvox) = A v1 per block,
+ * v1 scaled so that its largest-magnitude component is real and positive (a singular
+ * vector is defined up to a unit phase); voxels outside whole blocks are left as they are. */
+mrg_status mrg_clear_combine(const void *X, int nframes, int ncoil, int Nx, int Ny, int Nz, const int block[3],
+                             void *out, void *stream);
 /* WAVELET3D::forward/backward (src/wavelet3D.cpp:563-624) on nvol volumes of
  * Nx*Ny*Nz complex64, in place, circular shifts shift[3] (wavelet3D.cpp:443-448). */
 mrg_status mrg_wavelet(void *X, int nvol, int Nx, int Ny, int Nz, const int levels[3], const int shift[3],

@@ -43,6 +43,12 @@ class MrgFistaParams(ctypes.Structure):
                 ("clear_t2", ctypes.c_float), ("rand_skip", ctypes.c_int64)]
 
 
+class MrgClearParams(ctypes.Structure):
+    _fields_ = [("max_iter", ctypes.c_int), ("block", ctypes.c_int * 3), ("block_iter", ctypes.c_int),
+                ("alpha_coil", ctypes.c_float), ("clear_amp", ctypes.c_float), ("clear_t2", ctypes.c_float),
+                ("early_stop_thresh", ctypes.c_float), ("early_stop_range", ctypes.c_int), ("rand_skip", ctypes.c_int64)]
+
+
 SIGNATURES = {
     "mrg_config_default": (None, [ctypes.POINTER(MrgConfig)]),
     "mrg_last_error": (ctypes.c_char_p, []),
@@ -72,6 +78,11 @@ SIGNATURES = {
     "mrg_cg": (_i, [_vp, _i, _vp, _dp, _i, _vp]),
     "mrg_fista_params_default": (None, [ctypes.POINTER(MrgFistaParams)]),
     "mrg_fista": (_i, [_vp, ctypes.POINTER(MrgFistaParams), _vp, _dp, _fp, _i, _vp]),
+    "mrg_clear_params_default": (None, [ctypes.POINTER(MrgClearParams)]),
+    "mrg_clear": (_i, [_vp, ctypes.POINTER(MrgClearParams), _vp, _vp, _dp, _ip, _vp]),
+    "mrg_clear_update_threshold": (_i, [_vp, _i, _i, _i, _i, _i, _ip, _f, _f, _i, _fp, _vp]),
+    "mrg_clear_thresh": (_i, [_vp, _i, _i, _i, _i, _i, _ip, _i, _f, _f, _i64, _vp]),
+    "mrg_clear_combine": (_i, [_vp, _i, _i, _i, _i, _i, _ip, _vp, _vp]),
     "mrg_wavelet": (_i, [_vp, _i, _i, _i, _i, _ip, _ip, _i, _i, _vp]),
     "mrg_fraction_threshold": (_i, [_vp, _i, _i64, _f, _fp, _vp]),
     "mrg_soft_threshold": (_i, [_vp, _i64, _f, _vp]),

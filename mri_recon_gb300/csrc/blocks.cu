@@ -1,5 +1,5 @@
-// Standalone C ABI for the FISTA building blocks: wavelet, fraction / soft
-// threshold and the low-rank block operations, on caller buffers.
+// Standalone C ABI for the FISTA and CLEAR building blocks: wavelet, fraction / soft
+// threshold and the low-rank block operations (time and coil), on caller buffers.
 #include <cstring>
 
 #include "mrg_internal.h"
@@ -161,6 +161,90 @@ mrg_status mrg_llr_thresh(void *X, int nframes, int Nx, int Ny, int Nz, const in
   MRG_CUDA(cudaMemcpyAsync(dsm.p, &smax, sizeof(float), cudaMemcpyHostToDevice, st));
   MRG_TRY(llr_apply(d, nframes, N, bs, block_iter, alpha, (const int *)dsh.p, (const float *)dsm.p, st));
   MRG_TRY(back(X, tmp, bytes, st));
+  MRG_CUDA(cudaStreamSynchronize(st));
+  return MRG_OK;
+}
+
+static bool clear_args_ok(const void *X, int nframes, int ncoil, int Nx, int Ny, int Nz, const int block[3]) {
+  if (!X || !block || nframes <= 0 || ncoil <= 0 || Nx <= 0 || Ny <= 0 || Nz <= 0 || block[0] < 1 || block[1] < 1 ||
+      block[2] < 1) {
+    set_error("bad argument");
+    return false;
+  }
+  return true;
+}
+
+mrg_status mrg_clear_update_threshold(const void *X, int nframes, int ncoil, int Nx, int Ny, int Nz,
+                                      const int block[3], float clear_amp, float clear_t2, int iteration,
+                                      float *smax, void *stream) {
+  if (!clear_args_ok(X, nframes, ncoil, Nx, Ny, Nz, block) || !smax) {
+    set_error("bad argument");
+    return MRG_ERR_INVALID;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  const int N[3] = {Nx, Ny, Nz};
+  const int nb = coil_llr_blocks(N, block);
+  int np2 = 1;
+  while (np2 < nb) np2 <<= 1;
+  const size_t bytes = sizeof(float2) * (size_t)nframes * Nx * Ny * Nz * ncoil;
+  DevBuf tmp, work;
+  float2 *d;
+  MRG_TRY(view(X, bytes, tmp, st, &d));
+  MRG_CUDA(cudaMalloc(&work.p, sizeof(double) * (size_t)(nb + np2) + 16));
+  double *sig = (double *)work.p;
+  float *dsm = (float *)(sig + nb + np2);
+  MRG_TRY(coil_llr_update(d, nframes, ncoil, N, block, clear_amp, clear_t2, iteration, sig, sig + nb, dsm, st));
+  MRG_CUDA(cudaMemcpyAsync(smax, dsm, sizeof(float), cudaMemcpyDeviceToHost, st));
+  MRG_CUDA(cudaStreamSynchronize(st));
+  return MRG_OK;
+}
+
+mrg_status mrg_clear_thresh(void *X, int nframes, int ncoil, int Nx, int Ny, int Nz, const int block[3],
+                            int block_iter, float alpha, float smax, int64_t rand_skip, void *stream) {
+  if (!clear_args_ok(X, nframes, ncoil, Nx, Ny, Nz, block) || block_iter <= 0 || rand_skip < 0) {
+    set_error("bad argument");
+    return MRG_ERR_INVALID;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  const int N[3] = {Nx, Ny, Nz};
+  int bs[3];
+  for (int d = 0; d < 3; d++) bs[d] = std::min(block[d], N[d]);
+  // block shifts in the reference's draw order (clear.cpp:612-615); no zero-shift rule
+  // for block_iter == 1 here, unlike the time low-rank threshold
+  GlibcRand r;
+  r.skip(rand_skip);
+  std::vector<int> sh(3 * block_iter);
+  for (int it = 0; it < block_iter; it++)
+    for (int d = 0; d < 3; d++) sh[3 * it + d] = r.next() % bs[d] - bs[d] / 2;
+  const size_t bytes = sizeof(float2) * (size_t)nframes * Nx * Ny * Nz * ncoil;
+  DevBuf tmp, dsh, dsm;
+  float2 *d;
+  MRG_TRY(view(X, bytes, tmp, st, &d));
+  MRG_CUDA(cudaMalloc(&dsh.p, sizeof(int) * sh.size()));
+  MRG_CUDA(cudaMemcpyAsync(dsh.p, sh.data(), sizeof(int) * sh.size(), cudaMemcpyHostToDevice, st));
+  MRG_CUDA(cudaMalloc(&dsm.p, sizeof(float)));
+  MRG_CUDA(cudaMemcpyAsync(dsm.p, &smax, sizeof(float), cudaMemcpyHostToDevice, st));
+  MRG_TRY(coil_llr_thresh(d, nframes, ncoil, N, bs, alpha, block_iter, (const int *)dsh.p, (const float *)dsm.p, st));
+  MRG_TRY(back(X, tmp, bytes, st));
+  MRG_CUDA(cudaStreamSynchronize(st));
+  return MRG_OK;
+}
+
+mrg_status mrg_clear_combine(const void *X, int nframes, int ncoil, int Nx, int Ny, int Nz, const int block[3],
+                             void *out, void *stream) {
+  if (!clear_args_ok(X, nframes, ncoil, Nx, Ny, Nz, block) || !out) {
+    set_error("bad argument");
+    return MRG_ERR_INVALID;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  const int N[3] = {Nx, Ny, Nz};
+  const size_t nv = (size_t)nframes * Nx * Ny * Nz;
+  DevBuf tmp, tout;
+  float2 *d, *o;
+  MRG_TRY(view(X, sizeof(float2) * nv * ncoil, tmp, st, &d));
+  MRG_TRY(view(out, sizeof(float2) * nv, tout, st, &o));  // voxels outside whole blocks keep their values
+  MRG_TRY(coil_combine(d, nframes, ncoil, N, block, o, st));
+  MRG_TRY(back(out, tout, sizeof(float2) * nv, st));
   MRG_CUDA(cudaStreamSynchronize(st));
   return MRG_OK;
 }

@@ -1587,7 +1587,146 @@ extern "C" mrg_status mrg_fista(mrg_plan *p, const mrg_fista_params *q, void *X,
   return MRG_OK;
 }
 
+// CLEAR (src/recon_lib.cpp:1025-1238).  The per-coil images XX, the gradients RR and
+// E^H W E RR (one frame at a time) are [frame][voxel][coil] stacks, the layout the
+// operators read coil maps in: E_c X_c is run as E of a unit image with "maps" X_c for
+// all coils at once, and E_c^H of every coil comes out of the cropped adjoint transform.
+extern "C" mrg_status mrg_clear(mrg_plan *p, const mrg_clear_params *q, void *X, void *coil_images, double *resid,
+                                int *iters, void *stream) {
+  if (!p || !q || !X || q->max_iter < 0 || q->block[0] < 1 || q->block[1] < 1 || q->block[2] < 1) {
+    set_error("bad argument");
+    return MRG_ERR_INVALID;
+  }
+  if (q->alpha_coil != 0.0f && (q->block_iter < 1 || q->rand_skip < 0)) {
+    set_error("bad low-rank block parameters");
+    return MRG_ERR_INVALID;
+  }
+  if (p->C > 32) {
+    set_error("CLEAR supports at most 32 coils");
+    return MRG_ERR_UNSUPPORTED;
+  }
+  for (int t = 0; t < p->T; t++) {
+    MRG_TRY(check_frame(p, t));
+    if (!p->frames[t].has_data) {
+      set_error("k-space data not set for a frame");
+      return MRG_ERR_STATE;
+    }
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  const Geometry &g = p->geo;
+  const int C = p->C, T = p->T;
+  const int64_t n = p->nimg, nc = n * C, ntc = nc * T;
+  int bs[3];
+  for (int d = 0; d < 3; d++) bs[d] = std::min(q->block[d], g.N[d]);  // clear.cpp:109-112
+  const int nb = coil_llr_blocks(g.N, bs);
+  int np2 = 1;
+  while (np2 < nb) np2 <<= 1;
+  const int nblk = reduce_blocks(nc);
+  const int iters_max = std::max(q->max_iter, 1);
+  // block shifts: 3 rand() draws per block iteration, only in iterations that threshold
+  // (LOWRANKCOIL::thresh returns before drawing when clear_alpha_coil is 0)
+  std::vector<int> sh((size_t)iters_max * 3 * std::max(q->block_iter, 1), 0);
+  if (q->alpha_coil != 0.0f) {
+    GlibcRand rng;
+    rng.skip(q->rand_skip);
+    for (size_t i = 0; i < (size_t)q->max_iter * q->block_iter; i++)
+      for (int d = 0; d < 3; d++) sh[3 * i + d] = rng.next() % bs[d] - bs[d] / 2;
+  }
+  struct Bufs {
+    void *p[4] = {nullptr, nullptr, nullptr, nullptr};
+    ~Bufs() {
+      for (void *x : p) cudaFree(x);
+    }
+  } b;
+  const size_t sbytes = sizeof(double) * (3 * (size_t)iters_max + 3 * (size_t)nblk + nb + np2) + sizeof(float) +
+                        sizeof(int) * sh.size() + 64;
+  MRG_CUDA(cudaMalloc(&b.p[0], sizeof(float2) * ntc));  // XX
+  MRG_CUDA(cudaMalloc(&b.p[1], sizeof(float2) * ntc));  // RR
+  MRG_CUDA(cudaMalloc(&b.p[2], sizeof(float2) * (nc + n)));  // PP of one frame, unit image
+  MRG_CUDA(cudaMalloc(&b.p[3], sbytes));
+  float2 *XX = (float2 *)b.p[0], *RR = (float2 *)b.p[1], *PP = (float2 *)b.p[2], *ones = PP + nc;
+  double *acc = (double *)b.p[3], *part = acc + 3 * iters_max, *sig = part + 3 * nblk, *work = sig + nb;
+  float *smax = (float *)(work + np2);
+  int *dsh = (int *)(smax + 2);
+  MRG_CUDA(cudaMemcpyAsync(dsh, sh.data(), sizeof(int) * sh.size(), cudaMemcpyHostToDevice, st));
+  MRG_CUDA(cudaMemsetAsync(acc, 0, sizeof(double) * 3 * iters_max, st));
+  MRG_TRY(launch_zero(XX, sizeof(float2) * ntc, st));  // XX = 0
+  MRG_TRY(launch_fill(ones, n, make_float2(1.0f, 0.0f), st));
+  const float *wx = p->d_win + g.og[0], *wy = p->d_win + g.S[0] + g.og[1], *wz = p->d_win + g.S[0] + g.S[1] + g.og[2];
+  std::vector<float> diffs;  // residual / residual of iteration 0, for the early stop
+  std::vector<double> hacc(3);
+  double error0 = 0.0;
+  int done = 0;
+  for (int it = 0; it < q->max_iter; it++) {
+    double *ai = acc + 3 * it;
+    for (int t = 0; t < T; t++) {
+      const FrameTraj &ft = p->frames[t];
+      float2 *Xt = XX + t * nc, *Rt = RR + t * nc;
+      // R_c = E_c^H W (E_c X_c - d_c)
+      MRG_TRY(run_E(p, ft, ones, Xt, ft.dsorted, p->d_y, true, st));
+      MRG_TRY(run_EH_crop(p, ft, p->d_y, st));
+      MRG_TRY(launch_coil_images(p->d_t2, C, g.N, wx, wy, wz, Rt, C, 1, false, st));
+      // P_c = E_c^H W E_c R_c
+      MRG_TRY(run_E(p, ft, ones, Rt, nullptr, p->d_y, true, st));
+      MRG_TRY(run_EH_crop(p, ft, p->d_y, st));
+      MRG_TRY(launch_coil_images(p->d_t2, C, g.N, wx, wy, wz, PP, C, 1, false, st));
+      MRG_TRY(clear_dots(Rt, PP, nc, part, nblk, ai, st));
+    }
+    MRG_TRY(clear_step(XX, RR, ntc, ai, st));  // XX -= (R^H R / sum P conj R) R
+    done = it + 1;
+    if (q->alpha_coil != 0.0f) {  // lrankcoil.update_threshold(XX, 2, it); lrankcoil.thresh(XX, 2)
+      MRG_TRY(coil_llr_update(XX, T, C, g.N, bs, q->clear_amp, q->clear_t2, it, sig, work, smax, st));
+      MRG_TRY(coil_llr_thresh(XX, T, C, g.N, bs, q->alpha_coil, q->block_iter, dsh + 3 * (size_t)q->block_iter * it,
+                              smax, st));
+    }
+    if (q->early_stop_range > 0 && q->early_stop_thresh > 0.0f) {  // src/recon_lib.cpp:1118-1125, :1210-1219
+      MRG_CUDA(cudaMemcpyAsync(hacc.data(), ai, sizeof(double) * 3, cudaMemcpyDeviceToHost, st));
+      MRG_CUDA(cudaStreamSynchronize(st));
+      if (it == 0) error0 = hacc[0];
+      diffs.push_back((float)(hacc[0] / error0));
+      if ((int)diffs.size() > q->early_stop_range) diffs.erase(diffs.begin());
+      if ((int)diffs.size() == q->early_stop_range) {
+        double sq = 0.0, sm = 0.0;
+        for (float v : diffs) {
+          sm += v;
+          sq += (double)v * v;
+        }
+        const float mean = (float)(sm / diffs.size());
+        const float sd = (float)std::sqrt(sq / diffs.size() - (double)mean * mean);
+        if (sd < q->early_stop_thresh) break;
+      }
+    }
+  }
+  // lrankcoil.combine(XX, X) into zeroed images
+  void *dX;
+  bool sX;
+  MRG_TRY(dev_view(p, 0, X, sizeof(float2) * n * T, false, st, &dX, &sX));
+  MRG_TRY(launch_zero(dX, sizeof(float2) * n * T, st));
+  MRG_TRY(coil_combine(XX, T, C, g.N, bs, (float2 *)dX, st));
+  if (sX) MRG_CUDA(cudaMemcpyAsync(X, dX, sizeof(float2) * n * T, cudaMemcpyDeviceToHost, st));
+  if (coil_images) MRG_CUDA(cudaMemcpyAsync(coil_images, XX, sizeof(float2) * ntc, cudaMemcpyDefault, st));
+  if (resid)
+    for (int it = 0; it < done; it++)
+      MRG_CUDA(cudaMemcpyAsync(resid + it, acc + 3 * it, sizeof(double), cudaMemcpyDeviceToHost, st));
+  if (iters) *iters = done;
+  MRG_CUDA(cudaStreamSynchronize(st));
+  return MRG_OK;
+}
+
 extern "C" {
+
+void mrg_clear_params_default(mrg_clear_params *q) {
+  if (!q) return;
+  q->max_iter = 50;
+  q->block[0] = q->block[1] = q->block[2] = 4;
+  q->block_iter = 4;
+  q->alpha_coil = 0.01f;
+  q->clear_amp = 4.0f;
+  q->clear_t2 = 6.0f;
+  q->early_stop_thresh = 0.0f;
+  q->early_stop_range = 5;
+  q->rand_skip = 0;
+}
 
 void mrg_fista_params_default(mrg_fista_params *q) {
   if (!q) return;

@@ -206,6 +206,15 @@ __global__ void k_llr_median(const double *__restrict__ sig, int n, double *work
   }
 }
 
+mrg_status llr_median(const double *sig, int n, double *work, float amp, float t2, int iter, float *smax,
+                      cudaStream_t st) {
+  int np2 = 1;
+  while (np2 < n) np2 <<= 1;
+  k_llr_median<<<1, 1024, 0, st>>>(sig, n, work, np2, amp, t2, nullptr, iter, smax);
+  MRG_LAUNCHED();
+  return MRG_OK;
+}
+
 mrg_status llr_alloc(LlrWork &w, int nblocks) {
   if (w.nb >= nblocks && w.sig) return MRG_OK;
   llr_free(w);

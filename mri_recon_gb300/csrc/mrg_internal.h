@@ -304,6 +304,22 @@ mrg_status llr_update_into(const float2 *X, int Nt, const int N[3], const int bs
                            const Scalars *sc, int iter_fixed, double *sig, double *work, float *smax, cudaStream_t st);
 mrg_status llr_update_ex(const float2 *X, int Nt, const int N[3], const int bs[3], float amp, float t2,
                          const Scalars *sc, int iter_fixed, LlrWork &w, cudaStream_t st);
+// Median of the n non-zero sigma_1 in sig (work: next power of two doubles) times
+// (1 + amp exp(-iter / t2)) into the device float smax.
+mrg_status llr_median(const double *sig, int n, double *work, float amp, float t2, int iter, float *smax,
+                      cudaStream_t st);
+// CLEAR coil low rank on [frame][voxel][coil] stacks (clear.cu)
+int coil_llr_blocks(const int N[3], const int bs[3]);
+mrg_status coil_llr_update(const float2 *X, int T, int C, const int N[3], const int bs[3], float amp, float t2,
+                           int iter, double *sig, double *work, float *smax, cudaStream_t st);
+mrg_status coil_llr_thresh(float2 *X, int T, int C, const int N[3], const int bs[3], float alpha, int block_iter,
+                           const int *shifts, const float *smax, cudaStream_t st);
+mrg_status coil_combine(const float2 *X, int T, int C, const int N[3], const int bs[3], float2 *out,
+                        cudaStream_t st);
+// CLEAR gradient step: acc[0..2] += (sum |R|^2, sum P conj(R)); X -= (acc0 / acc12) R
+mrg_status clear_dots(const float2 *R, const float2 *P, int64_t n, double *part, int nblk, double *acc,
+                      cudaStream_t st);
+mrg_status clear_step(float2 *X, const float2 *R, int64_t n, const double *acc, cudaStream_t st);
 mrg_status llr_apply_ex(float2 *X, int Nt, const int N[3], const int bs[3], int block_iter, float alpha,
                         const int *shifts, const Scalars *sc, int per_it, int off_base, const float *smax_dev,
                         cudaStream_t st);

@@ -321,6 +321,29 @@ class Plan:
         return X, resid[:params.max_iter], step.value
 
 
+    def clear(self, params, X=None, coil_images=None, stream=None):
+        """CLEAR (RECON CLEAR recon_type): returns the combined images X (nframes, Nz, Ny, Nx),
+        the residual energy per iteration run, and coil_images (nframes, Nz, Ny, Nx, ncoils)
+        when an array or True is passed for it (None: not returned)."""
+        a = _Args()
+        if X is None:
+            X = self._new_images(None, self.nframes)
+        if coil_images is True:
+            shape = (self.nframes,) + self.ishape + (self.ncoils,)
+            if _is_tensor(X) and X.is_cuda:
+                coil_images = torch.empty(shape, dtype=torch.complex64, device=X.device)
+            else:
+                coil_images = np.zeros(shape, np.complex64)
+        resid = np.zeros(max(params.max_iter, 1), np.float64)
+        iters = ctypes.c_int()
+        _lib.check(_lib.load().mrg_clear(self._h, ctypes.byref(params), a.ptr(X),
+                                         a.ptr(coil_images) if coil_images is not None else None,
+                                         resid.ctypes.data_as(_lib._dp), ctypes.byref(iters), _stream(stream)))
+        if coil_images is None:
+            return X, resid[:iters.value]
+        return X, resid[:iters.value], coil_images
+
+
 if torch is not None:
     class NufftLoss(torch.autograd.Function):
         """loss = sum_c ||E_c(x, k) - y_c||^2 as a torch autograd function of the image x
@@ -387,6 +410,59 @@ def dcf_pipe(kx, ky, kz, N, stream=None, **params):
                                         int(N[0]), int(N[1]), int(N[2]), ctypes.byref(q), a.ptr(out),
                                         _stream(stream)))
     return out
+
+
+def _coil_stack(XX):
+    """(nframes, Nz, Ny, Nx, ncoils) complex64 stack -> (array, nframes, ncoils, Nx, Ny, Nz)."""
+    if not _is_tensor(XX):
+        XX = np.ascontiguousarray(XX, dtype=np.complex64)
+    T, Nz, Ny, Nx, C = (int(v) for v in XX.shape)
+    return XX, T, C, Nx, Ny, Nz
+
+
+def clear_update_threshold(XX, block=(4, 4, 4), clear_amp=4.0, clear_t2=6.0, iteration=0, stream=None):
+    """LOWRANKCOIL::update_threshold(image, 2, iteration) on a coil stack (nframes, Nz, Ny, Nx, ncoils)."""
+    a = _Args()
+    XX, T, C, Nx, Ny, Nz = _coil_stack(XX)
+    smax = ctypes.c_float()
+    _lib.check(_lib.load().mrg_clear_update_threshold(a.ptr(XX), T, C, Nx, Ny, Nz, (ctypes.c_int * 3)(*block),
+                                                      clear_amp, clear_t2, iteration, ctypes.byref(smax),
+                                                      _stream(stream)))
+    return smax.value
+
+
+def clear_thresh(XX, smax, block=(4, 4, 4), block_iter=4, alpha=0.01, rand_skip=0, stream=None):
+    """LOWRANKCOIL::thresh(image, 2) in place on a coil stack (nframes, Nz, Ny, Nx, ncoils); returns it."""
+    a = _Args()
+    XX, T, C, Nx, Ny, Nz = _coil_stack(XX)
+    _lib.check(_lib.load().mrg_clear_thresh(a.ptr(XX), T, C, Nx, Ny, Nz, (ctypes.c_int * 3)(*block), block_iter,
+                                            alpha, smax, rand_skip, _stream(stream)))
+    return XX
+
+
+def clear_combine(XX, block=(4, 4, 4), out=None, stream=None):
+    """LOWRANKCOIL::combine of a coil stack (nframes, Nz, Ny, Nx, ncoils) into (nframes, Nz, Ny, Nx)."""
+    a = _Args()
+    XX, T, C, Nx, Ny, Nz = _coil_stack(XX)
+    if out is None:
+        if _is_tensor(XX):
+            out = torch.zeros(XX.shape[:-1], dtype=torch.complex64, device=XX.device)
+        else:
+            out = np.zeros(XX.shape[:-1], np.complex64)
+    _lib.check(_lib.load().mrg_clear_combine(a.ptr(XX), T, C, Nx, Ny, Nz, (ctypes.c_int * 3)(*block), a.ptr(out),
+                                             _stream(stream)))
+    return out
+
+
+def clear_params(**kw):
+    p = _lib.MrgClearParams()
+    _lib.load().mrg_clear_params_default(ctypes.byref(p))
+    for k, v in kw.items():
+        if k == "block":
+            p.block[:] = list(v)
+        else:
+            setattr(p, k, v)
+    return p
 
 
 def fista_params(**kw):

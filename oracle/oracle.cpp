@@ -958,6 +958,154 @@ static void llr_thresh(cx<R> **X, int Nt, const int N[3], const LLRParams &p, fl
 }
 
 // ---------------------------------------------------------------------------
+// Coil low rank for CLEAR (clear.cpp:99-232, :561-914 with dim = 2, Ne = 1) on
+// per-coil images XX[t*C + c].  A block matrix has Nt*Np rows (frame t, voxel v
+// of the block, x fastest: the reference's count) and C columns (coils).
+// ---------------------------------------------------------------------------
+struct CoilBlocks {
+  int bs[3], B[3], nb, Np;
+};
+
+static CoilBlocks coil_blocks(const int N[3], const int *bs) {
+  CoilBlocks cb;
+  for (int d = 0; d < 3; d++) {
+    cb.bs[d] = std::min(bs[d], N[d]);  // clear.cpp:109-112
+    cb.B[d] = N[d] / cb.bs[d];
+  }
+  cb.nb = cb.B[0] * cb.B[1] * cb.B[2];
+  cb.Np = cb.bs[0] * cb.bs[1] * cb.bs[2];
+  return cb;
+}
+
+// voxel offsets of block b (i = b % Bx, j = (b / Bx) % By, k = b / (Bx By)) shifted by sh,
+// wrapped periodically (clear.cpp:629-648)
+static void coil_block_idx(const int N[3], const CoilBlocks &cb, int b, const int sh[3], std::vector<long> &idx) {
+  int i0 = (b % cb.B[0]) * cb.bs[0] + sh[0];
+  int j0 = ((b / cb.B[0]) % cb.B[1]) * cb.bs[1] + sh[1];
+  int k0 = (b / (cb.B[0] * cb.B[1])) * cb.bs[2] + sh[2];
+  idx.resize(cb.Np);
+  int c = 0;
+  for (int kk = k0; kk < k0 + cb.bs[2]; kk++)
+    for (int jj = j0; jj < j0 + cb.bs[1]; jj++)
+      for (int ii = i0; ii < i0 + cb.bs[0]; ii++) {
+        int px = (ii + N[0]) % N[0], py = (jj + N[1]) % N[1], pz = (kk + N[2]) % N[2];
+        idx[c++] = px + (long)N[0] * (py + (long)N[1] * pz);
+      }
+}
+
+// update_threshold(image, 2, iter): the gather writes A(count, t) inside the coil loop
+// with count restarting per coil (clear.cpp:185-199), so A holds the last coil's block of
+// frame t in column t (Nt <= C, or the reference's column index runs out of range);
+// sigma_1 of that A per block, median of the non-zero ones times the amplitude schedule.
+template <typename R>
+static float coil_update_threshold(cx<R> **XX, int Nt, int C, const int N[3], const int *bs, float amp, float t2,
+                                   int iter) {
+  const CoilBlocks cb = coil_blocks(N, bs);
+  const int R_ = Nt * cb.Np, nt = std::min(Nt, C);
+  std::vector<double> sb(cb.nb);
+  const int zero[3] = {0, 0, 0};
+#pragma omp parallel for schedule(dynamic)
+  for (int b = 0; b < cb.nb; b++) {
+    std::vector<long> idx;
+    coil_block_idx(N, cb, b, zero, idx);
+    std::vector<cx<double>> A((size_t)R_ * C, cx<double>(0, 0)), V;
+    std::vector<double> sv;
+    for (int t = 0; t < nt; t++)
+      for (int v = 0; v < cb.Np; v++) A[(t * cb.Np + v) + (size_t)R_ * t] = cx<double>(XX[t * C + C - 1][idx[v]]);
+    jacobi_svd(A, R_, C, sv, V);
+    sb[b] = *std::max_element(sv.begin(), sv.end());
+  }
+  float ampv = 1 + amp * std::exp(-((float)iter) / t2);
+  std::vector<double> nz;
+  for (double v : sb) if (v != 0) nz.push_back(v);
+  std::sort(nz.begin(), nz.end());
+  double med = 0;
+  if (!nz.empty()) {
+    size_t h = nz.size() / 2;
+    med = (nz.size() % 2) ? nz[h] : 0.5 * (nz[h - 1] + nz[h]);
+  }
+  return (float)(med * ampv);
+}
+
+static void coil_gather(cx<double> *A, int R_, const std::vector<long> &idx, int Np, int Nt, int C, void **XXv, int prec) {
+  for (int c = 0; c < C; c++)
+    for (int t = 0; t < Nt; t++)
+      for (int v = 0; v < Np; v++) {
+        const long i = idx[v];
+        A[(t * Np + v) + (size_t)R_ * c] = prec ? ((cx<double> **)XXv)[t * C + c][i]
+                                                : cx<double>(((cx<float> **)XXv)[t * C + c][i]);
+      }
+}
+
+// thresh(image, 2) (clear.cpp:561-813): per block iteration three rand() shifts (no
+// zero-shift rule here), A = U diag(max(s - alpha smax / block_iter, 0)) V^H.
+template <typename R>
+static void coil_thresh(cx<R> **XX, int Nt, int C, const int N[3], const int *bs, int block_iter, float alpha,
+                        float smax, GRand &rng) {
+  const CoilBlocks cb = coil_blocks(N, bs);
+  const int R_ = Nt * cb.Np;
+  double clear_alpha = alpha;
+  if (clear_alpha == 0.0) return;
+  clear_alpha *= smax;
+  const int prec = sizeof(R) == 8;
+  for (int it = 0; it < block_iter; it++) {
+    int sh[3];
+    for (int d = 0; d < 3; d++) sh[d] = rng.next() % cb.bs[d] - cb.bs[d] / 2;
+#pragma omp parallel for schedule(dynamic)
+    for (int b = 0; b < cb.nb; b++) {
+      std::vector<long> idx;
+      coil_block_idx(N, cb, b, sh, idx);
+      std::vector<cx<double>> A((size_t)R_ * C), V;
+      std::vector<double> sv;
+      coil_gather(A.data(), R_, idx, cb.Np, Nt, C, (void **)XX, prec);
+      jacobi_svd(A, R_, C, sv, V);
+      std::vector<double> f(C);
+      for (int j = 0; j < C; j++) {
+        double sp = std::max(sv[j] - clear_alpha / block_iter, 0.0);
+        f[j] = (sv[j] > 0) ? sp / sv[j] : 0.0;
+      }
+      for (int r = 0; r < R_; r++) {
+        const int t = r / cb.Np, v = r % cb.Np;
+        for (int c = 0; c < C; c++) {
+          cx<double> acc(0, 0);
+          for (int j = 0; j < C; j++) acc += A[r + (size_t)R_ * j] * f[j] * std::conj(V[c + (size_t)C * j]);
+          XX[t * C + c][idx[v]] = cx<R>((R)acc.real(), (R)acc.imag());
+        }
+      }
+    }
+  }
+}
+
+// combine (clear.cpp:815-914): im = A v1, v1 the right singular vector of the largest
+// singular value, here scaled so that its largest-magnitude component is real positive.
+template <typename R>
+static void coil_combine(cx<R> **XX, int Nt, int C, const int N[3], const int *bs, cx<R> **im) {
+  const CoilBlocks cb = coil_blocks(N, bs);
+  const int R_ = Nt * cb.Np;
+  const int prec = sizeof(R) == 8;
+  const int zero[3] = {0, 0, 0};
+#pragma omp parallel for schedule(dynamic)
+  for (int b = 0; b < cb.nb; b++) {
+    std::vector<long> idx;
+    coil_block_idx(N, cb, b, zero, idx);
+    std::vector<cx<double>> A((size_t)R_ * C), V;
+    std::vector<double> sv;
+    coil_gather(A.data(), R_, idx, cb.Np, Nt, C, (void **)XX, prec);
+    jacobi_svd(A, R_, C, sv, V);  // A = U diag(s)
+    int j = (int)(std::max_element(sv.begin(), sv.end()) - sv.begin());
+    int m = 0;
+    for (int c = 1; c < C; c++)
+      if (std::norm(V[c + (size_t)C * j]) > std::norm(V[m + (size_t)C * j])) m = c;
+    const cx<double> vm = V[m + (size_t)C * j];
+    const cx<double> ph = std::abs(vm) > 0 ? std::conj(vm) / std::abs(vm) : cx<double>(1, 0);
+    for (int r = 0; r < R_; r++) {
+      const cx<double> a = A[r + (size_t)R_ * j] * ph;  // (A v1)_r = (U s)_r1
+      im[r / cb.Np][idx[r % cb.Np]] = cx<R>((R)a.real(), (R)a.imag());
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // C ABI for ctypes (tests / bench baseline leg).
 // ---------------------------------------------------------------------------
 struct OHandle {
@@ -1137,6 +1285,95 @@ static void run_fista(OHandle *h, const OFrames &F, const OFistaParams &q, void 
       if (thr_out) thr_out[it] = thr;
     }
   }
+}
+
+struct OClearParams {
+  int max_iter;
+  int bs[3];
+  int block_iter;
+  float alpha_coil;
+  float clear_amp, clear_t2;
+  float early_stop_thresh;
+  int early_stop_range;
+  long rand_skip;
+};
+
+// CLEAR (recon_lib.cpp:1025-1238): per-coil images XX[t*C + c] from zero; per iteration
+//   R_c = E_c^H W (E_c X_c - d_c), P_c = E_c^H W E_c R_c (E_c: gridFFT without maps),
+//   scale = sum |R|^2 / sum P conj(R), X_c -= scale R_c, coil low rank;
+// then the combine into im[t].  conj_sum (ArrayTemplates.cpp:462-480) sums in complex
+// float per z slice; the energy sums float norms in double (ArrayTemplates.hpp:132-150).
+template <typename R>
+static int run_clear(OHandle *h, const OFrames &F, const OClearParams &q, void **XXv, void **imv, double *resid) {
+  OPlan<R> &p = P<R>(h);
+  const long n = p.isize();
+  const int Nt = F.Nt, C = F.C, Nz = p.g.N[2];
+  const long plane = (long)p.g.N[0] * p.g.N[1];
+  cx<R> **XX = (cx<R> **)XXv;
+  std::vector<std::vector<cx<R>>> RR((size_t)Nt * C, std::vector<cx<R>>(n));
+  std::vector<cx<R>> Pm(n), tmp;
+  for (int i = 0; i < Nt * C; i++) std::fill(XX[i], XX[i] + n, cx<R>(0, 0));
+  GRand rng(1);
+  for (long i = 0; i < q.rand_skip; i++) rng.step();
+  std::vector<float> diffs;
+  double error0 = 0.0;
+  int done = 0;
+  for (int it = 0; it < q.max_iter; it++) {
+    cx<double> rhp(0, 0);
+    for (int t = 0; t < Nt; t++) {
+      const long M = F.M[t];
+      tmp.resize(M);
+      for (int c = 0; c < C; c++) {
+        cx<R> *Rc = RR[(size_t)t * C + c].data();
+        p.forward(XX[t * C + c], nullptr, tmp.data(), F.kx[t], F.ky[t], F.kz[t], F.kw[t], M,
+                  (const cx<R> *)F.data[t * C + c]);
+        std::fill(Rc, Rc + n, cx<R>(0, 0));
+        p.adjoint(Rc, nullptr, tmp.data(), F.kx[t], F.ky[t], F.kz[t], F.kw[t], M);
+        std::fill(Pm.begin(), Pm.end(), cx<R>(0, 0));
+        p.forward(Rc, nullptr, tmp.data(), F.kx[t], F.ky[t], F.kz[t], F.kw[t], M, nullptr);
+        p.adjoint(Pm.data(), nullptr, tmp.data(), F.kx[t], F.ky[t], F.kz[t], F.kw[t], M);
+        std::vector<cx<R>> st(Nz, cx<R>(0, 0));
+#pragma omp parallel for
+        for (int k = 0; k < Nz; k++)
+          for (long qq = 0; qq < plane; qq++) st[k] += Pm[k * plane + qq] * std::conj(Rc[k * plane + qq]);
+        cx<R> sum(0, 0);
+        for (int k = 0; k < Nz; k++) sum += st[k];
+        rhp += cx<double>(sum.real(), sum.imag());
+      }
+    }
+    double rhr = 0;
+    for (auto &v : RR)
+      for (long i = 0; i < n; i++) rhr += (double)(R)std::norm(v[i]);
+    if (it == 0) error0 = rhr;
+    if (resid) resid[it] = rhr;
+    const cx<double> sd = cx<double>(rhr, 0) / rhp;
+    const cx<R> scale((R)sd.real(), (R)sd.imag());
+    for (int i = 0; i < Nt * C; i++)
+      for (long j = 0; j < n; j++) {
+        RR[i][j] *= scale;
+        XX[i][j] -= RR[i][j];
+      }
+    done = it + 1;
+    if (q.alpha_coil != 0.0f) {
+      const float smax = coil_update_threshold<R>(XX, Nt, C, p.g.N, q.bs, q.clear_amp, q.clear_t2, it);
+      coil_thresh<R>(XX, Nt, C, p.g.N, q.bs, q.block_iter, q.alpha_coil, smax, rng);
+    }
+    if (q.early_stop_range > 0 && q.early_stop_thresh > 0.0f) {
+      diffs.push_back((float)(std::fabs(rhr) / error0));
+      if ((int)diffs.size() > q.early_stop_range) diffs.erase(diffs.begin());
+      if ((int)diffs.size() == q.early_stop_range) {
+        double sm = 0, sq = 0;
+        for (float v : diffs) { sm += v; sq += (double)v * v; }
+        float mean = (float)(sm / diffs.size());
+        float stdev = (float)std::sqrt(sq / diffs.size() - (double)mean * mean);
+        if (stdev < q.early_stop_thresh) break;
+      }
+    }
+  }
+  cx<R> **im = (cx<R> **)imv;
+  for (int t = 0; t < Nt; t++) std::fill(im[t], im[t] + n, cx<R>(0, 0));
+  coil_combine<R>(XX, Nt, C, p.g.N, q.bs, im);
+  return done;
 }
 
 extern "C" {
@@ -1339,6 +1576,26 @@ void orc_glibc_rand(long skip, int n, int *out) {
   GRand rng(1);
   for (long i = 0; i < skip; i++) rng.step();
   for (int i = 0; i < n; i++) out[i] = rng.next();
+}
+float orc_clear_update_threshold(void **XX, int Nt, int C, const int *N, const int *bs, float amp, float t2, int iter,
+                                 int prec) {
+  return prec ? coil_update_threshold<double>((cx<double> **)XX, Nt, C, N, bs, amp, t2, iter)
+              : coil_update_threshold<float>((cx<float> **)XX, Nt, C, N, bs, amp, t2, iter);
+}
+void orc_clear_thresh(void **XX, int Nt, int C, const int *N, const int *bs, int block_iter, float alpha, float smax,
+                      long rand_skip, int prec) {
+  GRand rng(1);
+  for (long i = 0; i < rand_skip; i++) rng.step();
+  if (prec) coil_thresh<double>((cx<double> **)XX, Nt, C, N, bs, block_iter, alpha, smax, rng);
+  else coil_thresh<float>((cx<float> **)XX, Nt, C, N, bs, block_iter, alpha, smax, rng);
+}
+void orc_clear_combine(void **XX, int Nt, int C, const int *N, const int *bs, void **im, int prec) {
+  if (prec) coil_combine<double>((cx<double> **)XX, Nt, C, N, bs, (cx<double> **)im);
+  else coil_combine<float>((cx<float> **)XX, Nt, C, N, bs, (cx<float> **)im);
+}
+int orc_clear(void *hv, const OFrames *F, const OClearParams *q, void **XX, void **im, double *resid) {
+  OHandle *h = (OHandle *)hv;
+  return h->prec ? run_clear<double>(h, *F, *q, XX, im, resid) : run_clear<float>(h, *F, *q, XX, im, resid);
 }
 int orc_num_threads(void) { return omp_get_max_threads(); }
 }

@@ -70,6 +70,15 @@ def lib():
         L.orc_llr_update_threshold.restype = ctypes.c_float
         L.orc_llr_update_threshold.argtypes = [ctypes.POINTER(vp), ctypes.c_int, ip, ip, ctypes.c_float, ctypes.c_float, ctypes.c_int, ctypes.c_int]
         L.orc_llr_thresh.argtypes = [ctypes.POINTER(vp), ctypes.c_int, ip, ip, ctypes.c_int, ctypes.c_float, ctypes.c_float, ctypes.c_long, ctypes.c_int]
+        L.orc_clear_update_threshold.restype = ctypes.c_float
+        L.orc_clear_update_threshold.argtypes = [ctypes.POINTER(vp), ctypes.c_int, ctypes.c_int, ip, ip, ctypes.c_float,
+                                                 ctypes.c_float, ctypes.c_int, ctypes.c_int]
+        L.orc_clear_thresh.argtypes = [ctypes.POINTER(vp), ctypes.c_int, ctypes.c_int, ip, ip, ctypes.c_int,
+                                       ctypes.c_float, ctypes.c_float, ctypes.c_long, ctypes.c_int]
+        L.orc_clear_combine.argtypes = [ctypes.POINTER(vp), ctypes.c_int, ctypes.c_int, ip, ip, ctypes.POINTER(vp),
+                                        ctypes.c_int]
+        L.orc_clear.restype = ctypes.c_int
+        L.orc_clear.argtypes = [vp, vp, vp, ctypes.POINTER(vp), ctypes.POINTER(vp), dp]
         L.orc_glibc_rand.argtypes = [ctypes.c_long, ctypes.c_int, ip]
         L.orc_num_threads.restype = ctypes.c_int
         _lib = L
@@ -102,6 +111,19 @@ class FistaParams(ctypes.Structure):
                 ("use_threshold", ctypes.c_int), ("llr_bs", ctypes.c_int * 3), ("llr_block_iter", ctypes.c_int),
                 ("llr_alpha", ctypes.c_float), ("clear_amp", ctypes.c_float), ("clear_t2", ctypes.c_float),
                 ("rand_skip", ctypes.c_long)]
+
+
+class ClearParams(ctypes.Structure):
+    _fields_ = [("max_iter", ctypes.c_int), ("bs", ctypes.c_int * 3), ("block_iter", ctypes.c_int),
+                ("alpha_coil", ctypes.c_float), ("clear_amp", ctypes.c_float), ("clear_t2", ctypes.c_float),
+                ("early_stop_thresh", ctypes.c_float), ("early_stop_range", ctypes.c_int), ("rand_skip", ctypes.c_long)]
+
+
+def clear_params(max_iter=50, bs=(4, 4, 4), block_iter=4, alpha_coil=0.01, clear_amp=4.0, clear_t2=6.0,
+                 early_stop_thresh=0.0, early_stop_range=5, rand_skip=0):
+    """The CLEAR loop's parameters with the reference's defaults (clear.cpp:47-61, recon_lib.cpp:83-85)."""
+    return ClearParams(max_iter, (ctypes.c_int * 3)(*bs), block_iter, alpha_coil, clear_amp, clear_t2,
+                       early_stop_thresh, early_stop_range, rand_skip)
 
 
 class Plan:
@@ -236,9 +258,10 @@ class Plan:
         return self.get_grid()
 
     # solvers ---------------------------------------------------------------
-    def _frames(self, frames, smaps):
-        """frames: list of dicts with kx, ky, kz, kw (float32, M) and data (C, M)."""
-        C = len(smaps)
+    def _frames(self, frames, smaps, ncoil=None):
+        """frames: list of dicts with kx, ky, kz, kw (float32, M) and data (C, M); smaps None
+        (no maps, ncoil coils) or a list of C maps."""
+        C = len(smaps) if smaps is not None else ncoil
         keep = []
         Nt = len(frames)
         arrs = {k: (ctypes.c_void_p * Nt)() for k in ("kx", "ky", "kz", "kw")}
@@ -255,7 +278,7 @@ class Plan:
                 keep.append(d)
                 datas[t * C + c] = d.ctypes.data
         sm = (ctypes.c_void_p * C)()
-        for c in range(C):
+        for c in range(C if smaps is not None else 0):
             s = self._c(smaps[c])
             keep.append(s)
             sm[c] = s.ctypes.data
@@ -293,6 +316,56 @@ class Plan:
         lib().orc_fista(self.h, ctypes.byref(F), ctypes.byref(params), Xp, resid.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
                         ctypes.byref(step), thr.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
         return X, resid[:params.max_iter], step.value, thr[:params.max_iter]
+
+
+    def clear(self, frames, params):
+        """CLEAR (recon_lib.cpp:1025-1238) without coil maps: returns the coil images
+        (T, C, Nz, Ny, Nx), the combined images (T, Nz, Ny, Nx), sum |R|^2 per iteration
+        and the number of iterations run."""
+        C = len(frames[0]["data"])
+        F, keep = self._frames(frames, None, C)
+        Nt = len(frames)
+        XX = np.zeros((Nt, C) + self.ishape, self.cdt)
+        im = np.zeros((Nt,) + self.ishape, self.cdt)
+        xp = (ctypes.c_void_p * (Nt * C))(*[XX[t, c].ctypes.data for t in range(Nt) for c in range(C)])
+        ip_ = (ctypes.c_void_p * Nt)(*[im[t].ctypes.data for t in range(Nt)])
+        resid = np.zeros(max(params.max_iter, 1), np.float64)
+        done = lib().orc_clear(self.h, ctypes.byref(F), ctypes.byref(params), xp, ip_,
+                               resid.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+        return XX, im, resid[:done], done
+
+
+def _coil_ptrs(XX):
+    T, C = XX.shape[:2]
+    return (ctypes.c_void_p * (T * C))(*[XX[t, c].ctypes.data for t in range(T) for c in range(C)])
+
+
+def clear_update_threshold(XX, bs, amp=4.0, t2=6.0, iteration=0):
+    """LOWRANKCOIL::update_threshold(image, 2, iteration) on coil images (T, C, Nz, Ny, Nx)."""
+    XX = np.ascontiguousarray(XX)
+    T, C, Nz, Ny, Nx = XX.shape
+    prec = 1 if XX.dtype == np.complex128 else 0
+    return lib().orc_clear_update_threshold(_coil_ptrs(XX), T, C, _ip((Nx, Ny, Nz)), _ip(bs), amp, t2, iteration, prec)
+
+
+def clear_thresh(XX, bs, block_iter, alpha, smax, rand_skip):
+    """LOWRANKCOIL::thresh(image, 2) on a copy of coil images (T, C, Nz, Ny, Nx)."""
+    XX = np.ascontiguousarray(XX).copy()
+    T, C, Nz, Ny, Nx = XX.shape
+    prec = 1 if XX.dtype == np.complex128 else 0
+    lib().orc_clear_thresh(_coil_ptrs(XX), T, C, _ip((Nx, Ny, Nz)), _ip(bs), block_iter, alpha, smax, rand_skip, prec)
+    return XX
+
+
+def clear_combine(XX, bs, out=None):
+    """LOWRANKCOIL::combine of coil images (T, C, Nz, Ny, Nx) into (T, Nz, Ny, Nx)."""
+    XX = np.ascontiguousarray(XX)
+    T, C, Nz, Ny, Nx = XX.shape
+    prec = 1 if XX.dtype == np.complex128 else 0
+    im = np.zeros((T, Nz, Ny, Nx), XX.dtype) if out is None else np.ascontiguousarray(out, XX.dtype).copy()
+    ip_ = (ctypes.c_void_p * T)(*[im[t].ctypes.data for t in range(T)])
+    lib().orc_clear_combine(_coil_ptrs(XX), T, C, _ip((Nx, Ny, Nz)), _ip(bs), ip_, prec)
+    return im
 
 
 def fft1d(x, sign, prec=1):
