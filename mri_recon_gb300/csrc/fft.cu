@@ -1,12 +1,16 @@
 // Batched strided complex FFT passes for the oversampled 3D grid (the algorithm and the
 // kernels are in fft_kernels.cuh).  This unit holds the twiddle tables, the dispatch and
-// the kernels for lines of 16..160 points; fft_large.cu and fft_large2.cu instantiate the
-// longer lines, so the three compile in parallel.
+// the kernels for lines of 16..160 points and the lengths with a prime factor >= 7;
+// fft_large.cu and fft_large2.cu instantiate the other longer lines, so the three compile
+// in parallel.
 #include "fft_kernels.cuh"
 
 namespace mrg {
 
-static const int kSupportedQ[] = {2, 3, 4, 5, 6, 8, 9, 10, 12, 15, 16, 18, 20, 24, 30, 32, 36, 40, 45, 48};
+// line lengths S = 8 Q; the default oversampled size 16 ceil(1.5 N / 16) is 8 Q with Q
+// even, so every N up to 256 has its length here
+static const int kSupportedQ[] = {2,  3,  4,  5,  6,  8,  9,  10, 12, 14, 15, 16, 18, 20, 22, 24, 26,
+                                  28, 30, 32, 34, 36, 38, 40, 42, 44, 45, 46, 48};
 
 bool fft_size_supported(int S) {
   if (S % 8) return false;
@@ -78,10 +82,19 @@ mrg_status launch_fft(const FftPass &p, cudaStream_t st) {
     case 128: return launch_q<16>(p, st);
     case 144: return launch_q<18>(p, st);
     case 160: return launch_q<20>(p, st);
+    case 112: return launch_q<14>(p, st);
+    case 176: return launch_q<22>(p, st);
+    case 208: return launch_q<26>(p, st);
+    case 224: return launch_q<28>(p, st);
+    case 272: return launch_q<34>(p, st);
+    case 304: return launch_q<38>(p, st);
     case 192:
     case 240:
     case 256:
     case 288: return launch_fft_192_288(p, st);
+    case 336: return launch_q<42>(p, st);
+    case 352: return launch_q<44>(p, st);
+    case 368: return launch_q<46>(p, st);
     case 320:
     case 360:
     case 384: return launch_fft_320_384(p, st);

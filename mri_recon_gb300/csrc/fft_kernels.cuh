@@ -12,7 +12,7 @@
 // IB complex values) of length S = 8*Q held in shared memory as [S][IB+1].
 // Each line is split S = 8 x Q (four-step): 8-point DFTs across the 8 threads
 // of a line, a twiddle, then a Q-point DFT in registers per thread (radices 2,
-// 3, 4, 5).  Twiddles exp(-2 pi i m / S) are computed on the host in double,
+// 3, 4, 5 and direct DFTs of larger primes).  Twiddles exp(-2 pi i m / S) are computed on the host in double,
 // staged in shared memory per CTA and read as broadcasts.
 #pragma once
 
@@ -87,7 +87,49 @@ __device__ __forceinline__ void bfly(float2 (&t)[P]) {
   }
 }
 
-constexpr int first_factor(int q) { return (q % 4 == 0) ? 4 : ((q % 2 == 0) ? 2 : ((q % 3 == 0) ? 3 : 5)); }
+// DFT of odd prime length P >= 7 from symmetric pairs: with a_j = t_j + t_{P-j},
+// b_j = t_j - t_{P-j}, X_k = t_0 + sum_j cos(2 pi jk/P) a_j + SIGN i sum_j sin(2 pi jk/P) b_j
+// and X_{P-k} the same with the sine term negated.  cos and sin come from the length-S
+// table (tw[m] = exp(-2 pi i m / S), S a multiple of P).
+template <int P, int SIGN, int S>
+__device__ __forceinline__ void bfly_prime(float2 (&t)[P], const float2 *tw) {
+  constexpr int H = (P - 1) / 2;
+  float2 a[H], b[H];
+#pragma unroll
+  for (int j = 1; j <= H; j++) {
+    a[j - 1] = cadd(t[j], t[P - j]);
+    b[j - 1] = csub(t[j], t[P - j]);
+  }
+  const float2 t0 = t[0];
+  float2 s = t0;
+#pragma unroll
+  for (int j = 0; j < H; j++) s = cadd(s, a[j]);
+  t[0] = s;
+#pragma unroll
+  for (int k = 1; k <= H; k++) {
+    float2 m = t0, r = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int j = 1; j <= H; j++) {
+      const float2 w = tw[((j * k) % P) * (S / P)];  // (cos, -sin)
+      m = make_float2(m.x + w.x * a[j - 1].x, m.y + w.x * a[j - 1].y);
+      r = make_float2(r.x - w.y * b[j - 1].x, r.y - w.y * b[j - 1].y);
+    }
+    const float2 ir = imul<SIGN>(r);
+    t[k] = cadd(m, ir);
+    t[P - k] = csub(m, ir);
+  }
+}
+
+// radix of the first decimation step: 4, 2, 3, 5, then the smallest prime factor
+constexpr int first_factor(int q) {
+  if (q % 4 == 0) return 4;
+  if (q % 2 == 0) return 2;
+  if (q % 3 == 0) return 3;
+  if (q % 5 == 0) return 5;
+  for (int f = 7; f < q; f += 2)
+    if (q % f == 0) return f;
+  return q;
+}
 
 // In-register DFT of length Q (decimation in time), natural order in and out;
 // tw is the length-S table, S a multiple of Q.
@@ -110,7 +152,10 @@ __device__ __forceinline__ void reg_fft(float2 (&v)[Q], const float2 *tw) {
       float2 t[P];
 #pragma unroll
       for (int p = 0; p < P; p++) t[p] = (p * k == 0) ? sub[p][k] : cmul(sub[p][k], twid<SIGN>(tw, p * k * (S / Q)));
-      bfly<P, SIGN>(t);
+      if constexpr (P <= 5)
+        bfly<P, SIGN>(t);
+      else
+        bfly_prime<P, SIGN, S>(t, tw);
 #pragma unroll
       for (int q = 0; q < P; q++) v[k + Q2 * q] = t[q];
     }
@@ -496,8 +541,11 @@ static mrg_status launch_pp(const FftPass &pp, cudaStream_t st) {
   return MRG_OK;
 }
 
-// Q values that get kernels with a compile-time pitch (lines of 192..384 points)
-constexpr bool fixed_pitch_q(int Q) { return Q >= 24; }
+// Q values that get kernels with a compile-time pitch (lines of 192..384 points whose
+// factors are 2, 3 and 5; the other lengths run the generic kernel)
+constexpr bool fixed_pitch_q(int Q) {
+  return Q == 24 || Q == 30 || Q == 32 || Q == 36 || Q == 40 || Q == 45 || Q == 48;
+}
 
 template <int Q, int P>
 static mrg_status launch_qp(const FftPass &pp, const dim3 grid, const dim3 block, size_t smem, cudaStream_t st) {

@@ -57,6 +57,30 @@ def test_forward_E_matches_oracle(mrg_lib, oracle_lib, N, C, nproj):
     assert rel(y, r64) < fp64_bound(r32, r64)
 
 
+# line lengths with a prime factor >= 7 (direct prime DFTs): 112 = 16*7, 176 = 16*11, 208 = 16*13
+# at the default overgrid; 272 = 16*17, 304 = 16*19, 336 = 48*7, 352 = 32*11, 368 = 16*23 via
+# a large overgrid on a 32^3 image
+@pytest.mark.parametrize("N,overgrid,C,nproj", [(70, 1.5, 2, 800), (112, 1.5, 1, 1200), (136, 1.5, 1, 1200),
+                                                (32, 8.4, 2, 300), (32, 9.4, 1, 300), (32, 10.4, 1, 300),
+                                                (32, 10.9, 1, 300), (32, 11.3, 2, 300)])
+def test_prime_factor_lengths_match_oracle(mrg_lib, oracle_lib, N, overgrid, C, nproj):
+    torch = _torch()
+    c = case(N=N, C=C, nproj=nproj)
+    p = _plan(mrg_lib, c, overgrid=overgrid)
+    a = (c["kx"], c["ky"], c["kz"], c["kw"])
+    o32 = oracle_lib.Plan(N, overgrid=overgrid, prec=0)
+    assert tuple(p.S) == tuple(o32.S)
+    y = p.forward(0, torch.from_numpy(c["X"]).cuda()).cpu().numpy()
+    ref = np.stack([o32.forward(c["X"], c["smaps"][k], *a) for k in range(C)])
+    assert rel(y, ref) < TOL
+    X = torch.zeros(c["X"].shape, dtype=torch.complex64, device="cuda")
+    p.adjoint(0, torch.from_numpy(c["data"]).cuda(), X)
+    refX = np.zeros(o32.ishape, o32.cdt)
+    for k in range(C):
+        refX = o32.adjoint(refX, c["smaps"][k], c["data"][k], *a)
+    assert rel(X.cpu().numpy(), refX) < TOL
+
+
 def test_forward_residual_matches_oracle(mrg_lib, oracle_lib):
     torch = _torch()
     c = case(N=32, C=4, nproj=700)
