@@ -175,6 +175,31 @@ mrg_status mrg_adjoint_sos(mrg_plan *plan, int frame, const void *data, int64_t 
 mrg_status mrg_lowres_smaps(mrg_plan *plan, int frame, const void *data, int64_t coil_stride, float smap_res,
                             const float blur[3], void *smaps_out, int64_t out_stride, void *stream);
 
+/* ESPIRiT coil maps (SPIRIT::generateEigenCoils, src/spirit.cpp:137-550; the ESPIRIT
+ * branch of calc_sensitivity_maps, src/recon_lib.cpp:2892-2899).  Fields are the -sp_*
+ * flags (-sp_kr_f / -sp_cr set all three axes). */
+typedef struct mrg_espirit_params {
+  float kernel_radius[3]; /* -sp_krx_f/-sp_kry_f/-sp_krz_f (default 3), at most 7 */
+  int calib_radius[3];    /* -sp_crx/-sp_cry/-sp_crz (default 12); must exceed ceil(kernel_radius) */
+  float svd_thresh;       /* -sp_svd_thresh (default 0.01): keep s >= s0 sqrt(svd_thresh) */
+  int square;             /* -sp_square (1) or -sp_circle (0, default) regions */
+} mrg_espirit_params;
+
+void mrg_espirit_params_default(mrg_espirit_params *p);
+
+/* Maps from caller coil images: images and maps are Nx*Ny*Nz voxels x ncoil complex64,
+ * coil innermost (host or device).  kept (may be NULL): kernel vectors kept; sv (host,
+ * may be NULL): the first sv_cap calibration singular values, descending.  ncoil <= 32. */
+mrg_status mrg_espirit(const void *images, int ncoil, int Nx, int Ny, int Nz, const mrg_espirit_params *params,
+                       void *maps, int *kept, double *sv, int sv_cap, void *stream);
+/* ESPIRiT maps of a plan: the map-free E^H of each coil of `frame` (the plan's k_rad as
+ * set: the reference leaves the taper off for ESPIRiT), the optional Gaussian blur
+ * (extra_blurX/Y/Z, NULL for none), then mrg_espirit; the maps become the plan's maps and
+ * are also written to smaps_out (may be NULL; coil c at smaps_out + c*out_stride). */
+mrg_status mrg_espirit_smaps(mrg_plan *plan, int frame, const void *data, int64_t coil_stride,
+                             const mrg_espirit_params *params, const float blur[3], void *smaps_out,
+                             int64_t out_stride, int *kept, void *stream);
+
 /* SENSE conjugate gradient (src/recon_lib.cpp:1523-1759): X (nframes images) is
  * overwritten with the result of max_iter iterations from x0 = 0, FP32 vectors and
  * FP64 scalars.  resid (host, may be NULL) receives sum|r|^2 after each iteration.

@@ -49,6 +49,11 @@ class MrgClearParams(ctypes.Structure):
                 ("early_stop_thresh", ctypes.c_float), ("early_stop_range", ctypes.c_int), ("rand_skip", ctypes.c_int64)]
 
 
+class MrgEspiritParams(ctypes.Structure):
+    _fields_ = [("kernel_radius", ctypes.c_float * 3), ("calib_radius", ctypes.c_int * 3),
+                ("svd_thresh", ctypes.c_float), ("square", ctypes.c_int)]
+
+
 SIGNATURES = {
     "mrg_config_default": (None, [ctypes.POINTER(MrgConfig)]),
     "mrg_last_error": (ctypes.c_char_p, []),
@@ -78,6 +83,9 @@ SIGNATURES = {
     "mrg_cg": (_i, [_vp, _i, _vp, _dp, _i, _vp]),
     "mrg_fista_params_default": (None, [ctypes.POINTER(MrgFistaParams)]),
     "mrg_fista": (_i, [_vp, ctypes.POINTER(MrgFistaParams), _vp, _dp, _fp, _i, _vp]),
+    "mrg_espirit_params_default": (None, [ctypes.POINTER(MrgEspiritParams)]),
+    "mrg_espirit": (_i, [_vp, _i, _i, _i, _i, ctypes.POINTER(MrgEspiritParams), _vp, _ip, _dp, _i, _vp]),
+    "mrg_espirit_smaps": (_i, [_vp, _i, _vp, _i64, ctypes.POINTER(MrgEspiritParams), _fp, _vp, _i64, _ip, _vp]),
     "mrg_clear_params_default": (None, [ctypes.POINTER(MrgClearParams)]),
     "mrg_clear": (_i, [_vp, ctypes.POINTER(MrgClearParams), _vp, _vp, _dp, _ip, _vp]),
     "mrg_clear_update_threshold": (_i, [_vp, _i, _i, _i, _i, _i, _ip, _f, _f, _i, _fp, _vp]),

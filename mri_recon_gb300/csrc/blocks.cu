@@ -249,6 +249,49 @@ mrg_status mrg_clear_combine(const void *X, int nframes, int ncoil, int Nx, int 
   return MRG_OK;
 }
 
+void mrg_espirit_params_default(mrg_espirit_params *p) {
+  if (!p) return;
+  for (int d = 0; d < 3; d++) {  // src/spirit.cpp:9-34
+    p->kernel_radius[d] = 3.0f;
+    p->calib_radius[d] = 12;
+  }
+  p->svd_thresh = 0.01f;
+  p->square = 0;
+}
+
+mrg_status mrg_espirit(const void *images, int ncoil, int Nx, int Ny, int Nz, const mrg_espirit_params *params,
+                       void *maps, int *kept, double *sv, int sv_cap, void *stream) {
+  if (!images || !maps || !params || ncoil <= 0 || Nx <= 0 || Ny <= 0 || Nz <= 0 || (sv && sv_cap < 0)) {
+    set_error("bad argument");
+    return MRG_ERR_INVALID;
+  }
+  for (int d = 0; d < 3; d++)
+    if (!(params->kernel_radius[d] >= 0.0f) || params->kernel_radius[d] > 7.0f) {
+      set_error("ESPIRiT kernel radius must be in [0, 7]");
+      return MRG_ERR_INVALID;
+    }
+  cudaStream_t st = (cudaStream_t)stream;
+  const int N[3] = {Nx, Ny, Nz};
+  const size_t bytes = sizeof(float2) * (size_t)Nx * Ny * Nz * ncoil;
+  DevBuf ti, tm;
+  float2 *di, *dm;
+  MRG_TRY(view(images, bytes, ti, st, &di));
+  MRG_TRY(view(maps, bytes, tm, st, &dm));
+  EspiritParams q;
+  for (int d = 0; d < 3; d++) {
+    q.kr_f[d] = params->kernel_radius[d];
+    q.cr[d] = params->calib_radius[d];
+  }
+  q.svd_thresh = params->svd_thresh;
+  q.square = params->square;
+  q.sv_out = sv;
+  q.sv_cap = sv ? sv_cap : 0;
+  MRG_TRY(espirit_maps(di, ncoil, N, q, dm, kept, st));
+  MRG_TRY(back(maps, tm, bytes, st));
+  MRG_CUDA(cudaStreamSynchronize(st));
+  return MRG_OK;
+}
+
 mrg_status mrg_gaussian_blur(void *X, int nvol, int Nx, int Ny, int Nz, int64_t vol_stride, const float sigma[3],
                              void *stream) {
   if (!X || !sigma || nvol <= 0 || Nx <= 0 || Ny <= 0 || Nz <= 0) {

@@ -1156,6 +1156,68 @@ mrg_status mrg_lowres_smaps(mrg_plan *p, int frame, const void *data, int64_t co
   return MRG_OK;
 }
 
+mrg_status mrg_espirit_smaps(mrg_plan *p, int frame, const void *data, int64_t coil_stride,
+                             const mrg_espirit_params *params, const float blur[3], void *smaps_out,
+                             int64_t out_stride, int *kept, void *stream) {
+  if (!p || !params) {
+    set_error("bad argument");
+    return MRG_ERR_INVALID;
+  }
+  if (smaps_out && p->C > 1 && out_stride < p->nimg) {
+    set_error("out_stride smaller than one image");
+    return MRG_ERR_INVALID;
+  }
+  for (int d = 0; d < 3; d++)
+    if (!(params->kernel_radius[d] >= 0.0f) || params->kernel_radius[d] > 7.0f) {
+      set_error("ESPIRiT kernel radius must be in [0, 7]");
+      return MRG_ERR_INVALID;
+    }
+  cudaStream_t st = (cudaStream_t)stream;
+  if (!p->d_smap) MRG_CUDA(cudaMalloc(&p->d_smap, sizeof(float2) * p->nimg * p->C));
+  const Geometry &g = p->geo;
+  if (p->C == 1) {  // one coil: the map is 1 (src/recon_lib.cpp:2703-2708)
+    MRG_TRY(launch_fill(p->d_smap, p->nimg, make_float2(1.0f, 0.0f), st));
+    if (kept) *kept = 0;
+  } else {
+    // coil images (gridding.forward per coil, k_rad unchanged: src/recon_lib.cpp:2737-2739)
+    MRG_TRY(adjoint_crop(p, frame, data, coil_stride, st));
+    const float *wx = p->d_win + g.og[0], *wy = p->d_win + g.S[0] + g.og[1], *wz = p->d_win + g.S[0] + g.S[1] + g.og[2];
+    float2 *img = nullptr;
+    MRG_CUDA(cudaMalloc(&img, sizeof(float2) * p->nimg * p->C));
+    mrg_status s = launch_coil_images(p->d_t2, p->C, g.N, wx, wy, wz, img, p->C, 1, false, st);
+    const float nob[3] = {0.f, 0.f, 0.f};
+    if (s == MRG_OK) s = gaussian_blur_ex(img, p->C, g.N, p->C, 1, blur ? blur : nob, st);
+    EspiritParams q;
+    for (int d = 0; d < 3; d++) {
+      q.kr_f[d] = params->kernel_radius[d];
+      q.cr[d] = params->calib_radius[d];
+    }
+    q.svd_thresh = params->svd_thresh;
+    q.square = params->square;
+    q.sv_out = nullptr;
+    q.sv_cap = 0;
+    if (s == MRG_OK) s = espirit_maps(img, p->C, g.N, q, p->d_smap, kept, st);
+    cudaStreamSynchronize(st);
+    cudaFree(img);
+    MRG_TRY(s);
+  }
+  if (!p->has_smaps) invalidate_graphs(p);
+  p->has_smaps = true;
+  if (smaps_out) {
+    const int64_t vs = p->C > 1 ? out_stride : p->nimg;
+    const size_t obytes = sizeof(float2) * (size_t)(vs * (p->C - 1) + p->nimg);
+    void *dO;
+    bool sO;
+    MRG_TRY(dev_view(p, 1, smaps_out, obytes, false, st, &dO, &sO));
+    MRG_TRY(launch_deinterleave(p->d_smap, p->C, p->nimg, (float2 *)dO, vs, st));
+    if (sO) {
+      MRG_CUDA(cudaMemcpyAsync(smaps_out, dO, obytes, cudaMemcpyDeviceToHost, st));
+      MRG_CUDA(cudaStreamSynchronize(st));
+    }
+  }
+  return MRG_OK;
+}
+
 static mrg_status capture(mrg_plan *p, const std::function<mrg_status(cudaStream_t)> &body, cudaGraphExec_t *exec);
 
 // ---------------------------------------------------------------------------

@@ -308,6 +308,17 @@ mrg_status llr_update_ex(const float2 *X, int Nt, const int N[3], const int bs[3
 // (1 + amp exp(-iter / t2)) into the device float smax.
 mrg_status llr_median(const double *sig, int n, double *work, float amp, float t2, int iter, float *smax,
                       cudaStream_t st);
+// ESPIRiT maps from coil images [voxel][coil] (espirit.cu)
+struct EspiritParams {
+  float kr_f[3];
+  int cr[3];
+  float svd_thresh;
+  int square;
+  double *sv_out;  // host, may be NULL: calibration singular values, descending
+  int sv_cap;
+};
+mrg_status espirit_maps(const float2 *img, int C, const int N[3], const EspiritParams &q, float2 *maps, int *nV_out,
+                        cudaStream_t st);
 // CLEAR coil low rank on [frame][voxel][coil] stacks (clear.cu)
 int coil_llr_blocks(const int N[3], const int bs[3]);
 mrg_status coil_llr_update(const float2 *X, int T, int C, const int N[3], const int bs[3], float amp, float t2,

@@ -252,6 +252,20 @@ class Plan:
                                                 a.ptr(out), _numel(out) // self.ncoils, _stream(stream)))
         return out
 
+    def espirit_smaps(self, frame, data, params=None, blur=None, stream=None):
+        """ESPIRiT maps from one frame's k-space (the ESPIRIT branch of calc_sensitivity_maps);
+        they become the plan's maps.  Returns (maps (ncoils, Nz, Ny, Nx), kernel vectors kept)."""
+        a = _Args()
+        params = params if params is not None else espirit_params()
+        d = data if _is_tensor(data) else np.ascontiguousarray(data, dtype=np.complex64)
+        M = _numel(d) // self.ncoils
+        out = self._new_images(d, self.ncoils)
+        bl = (ctypes.c_float * 3)(*blur) if blur is not None else None
+        kept = ctypes.c_int()
+        _lib.check(_lib.load().mrg_espirit_smaps(self._h, frame, a.ptr(d), M, ctypes.byref(params), bl, a.ptr(out),
+                                                 _numel(out) // self.ncoils, ctypes.byref(kept), _stream(stream)))
+        return out, kept.value
+
     def grad(self, frame, X, y, stream=None):
         """loss = sum_c ||E_c X - y_c||^2, grad_x = 2 E^*(E X - y), grad_k = dloss/dk [3, M].
 
@@ -452,6 +466,41 @@ def clear_combine(XX, block=(4, 4, 4), out=None, stream=None):
     _lib.check(_lib.load().mrg_clear_combine(a.ptr(XX), T, C, Nx, Ny, Nz, (ctypes.c_int * 3)(*block), a.ptr(out),
                                              _stream(stream)))
     return out
+
+
+def espirit_params(kernel_radius=None, calib_radius=None, svd_thresh=None, square=None):
+    """SPIRIT options (-sp_kr_f / -sp_cr as scalars set all three axes)."""
+    p = _lib.MrgEspiritParams()
+    _lib.load().mrg_espirit_params_default(ctypes.byref(p))
+    if kernel_radius is not None:
+        p.kernel_radius[:] = [float(v) for v in (kernel_radius if not np.isscalar(kernel_radius) else (kernel_radius,) * 3)]
+    if calib_radius is not None:
+        p.calib_radius[:] = [int(v) for v in (calib_radius if not np.isscalar(calib_radius) else (calib_radius,) * 3)]
+    if svd_thresh is not None:
+        p.svd_thresh = svd_thresh
+    if square is not None:
+        p.square = int(bool(square))
+    return p
+
+
+def espirit(images, params=None, sv_cap=0, stream=None):
+    """ESPIRiT maps from coil images (Nz, Ny, Nx, ncoils) complex64, coil innermost: returns
+    (maps of the same shape, kernel vectors kept, the first sv_cap calibration singular values)."""
+    a = _Args()
+    if not _is_tensor(images):
+        images = np.ascontiguousarray(images, dtype=np.complex64)
+    Nz, Ny, Nx, C = (int(v) for v in images.shape)
+    params = params if params is not None else espirit_params()
+    if _is_tensor(images):
+        maps = torch.empty_like(images)
+    else:
+        maps = np.zeros(images.shape, np.complex64)
+    kept = ctypes.c_int()
+    sv = np.zeros(max(sv_cap, 1), np.float64)
+    _lib.check(_lib.load().mrg_espirit(a.ptr(images), C, Nx, Ny, Nz, ctypes.byref(params), a.ptr(maps),
+                                       ctypes.byref(kept), sv.ctypes.data_as(_lib._dp) if sv_cap else None, sv_cap,
+                                       _stream(stream)))
+    return maps, kept.value, sv[:sv_cap]
 
 
 def clear_params(**kw):

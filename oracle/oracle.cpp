@@ -1106,6 +1106,190 @@ static void coil_combine(cx<R> **XX, int Nt, int C, const int N[3], const int *b
 }
 
 // ---------------------------------------------------------------------------
+// ESPIRiT coil maps (spirit.cpp:9-66 defaults and init, :137-550), in FP64 from
+// the float coil images that gridding.forward leaves in the maps
+// (recon_lib.cpp:2892-2899).  kr_f / cr / svd_thresh / shape are the -sp_* flags.
+// ---------------------------------------------------------------------------
+struct OEspirit {
+  float kr_f[3];     // kernel radii (krx_f, kry_f, krz_f)
+  int cr[3];         // calibration radii (crx, cry, crz)
+  float svd_thresh;  // singular values >= s0 * sqrt(svd_thresh) are kept
+  int square;        // 1: SP_SQUARE, 0: SP_CIRCLE
+};
+
+static inline double chop_sign(long i) { return (double)(2 * (i % 2) - 1); }
+
+// ifft (ArrayTemplates.cpp:35-88): fftshift (x (2((i+j+k)%2)-1)), FFTW_BACKWARD 3D,
+// fftshift, x 1/sqrt(Nz*Ny*Nx) (float)
+static void centered_ifft3(std::vector<cx<double>> &a, const int N[3]) {
+  const long nx = N[0], ny = N[1], nz = N[2];
+  for (long k = 0; k < nz; k++)
+    for (long j = 0; j < ny; j++)
+      for (long i = 0; i < nx; i++) a[i + nx * (j + ny * k)] *= chop_sign(i + j + k);
+  const long st[3] = {1, nx, nx * ny};
+  for (int ax = 0; ax < 3; ax++) {
+    const int n = N[ax];
+    FFT1<double> plan(n, +1);
+    std::vector<cx<double>> buf(n), work(n);
+    const int o1 = ax == 0 ? 1 : 0, o2 = ax == 2 ? 1 : 2;
+    for (long b = 0; b < N[o2]; b++)
+      for (long c = 0; c < N[o1]; c++) {
+        cx<double> *base = a.data() + b * st[o2] + c * st[o1];
+        for (int i = 0; i < n; i++) buf[i] = base[i * st[ax]];
+        plan.run(buf.data(), work.data());
+        for (int i = 0; i < n; i++) base[i * st[ax]] = buf[i];
+      }
+  }
+  const double scale = (double)(float)(1.0 / std::sqrt((float)nz * (float)ny * (float)nx));
+  for (long k = 0; k < nz; k++)
+    for (long j = 0; j < ny; j++)
+      for (long i = 0; i < nx; i++) a[i + nx * (j + ny * k)] *= chop_sign(i + j + k) * scale;
+}
+
+// rad <= 1 tests of calibrate_ellipsoid (spirit.cpp:199-243, :256-301)
+static bool in_acs(int ix, int iy, int iz, const int c[3], bool square) {
+  if (square) return true;
+  float rad;
+  if (c[2] == 0) rad = (float)(ix * ix) / (c[0] * c[0]) + (float)(iy * iy) / (c[1] * c[1]);
+  else rad = (float)(ix * ix) / (c[0] * c[0]) + (float)(iy * iy) / (c[1] * c[1]) + (float)(iz * iz) / (c[2] * c[2]);
+  return !(rad > 1);
+}
+static bool in_kernel(int jx, int jy, int jz, const float kf[3], bool square) {
+  if (square) return true;
+  float krad;
+  if (kf[2] == 0) krad = (float)(jx * jx) / (kf[0] * kf[0]) + (float)(jy * jy) / (kf[1] * kf[1]);
+  else krad = (float)(jx * jx) / (kf[0] * kf[0]) + (float)(jy * jy) / (kf[1] * kf[1]) + (float)(jz * jz) / (kf[2] * kf[2]);
+  return krad <= 1;
+}
+
+// Returns nV; maps[c] (N^3 each, x fastest) receive the maps, sv (may be NULL) the
+// calibration singular values in descending order (min(rows, cols) of them).
+static int espirit(const cx<float> *const *img, int C, const int N[3], const OEspirit &q, cx<double> **maps,
+                   double *sv, double *ratio) {
+  const long nx = N[0], ny = N[1], nz = N[2], n3 = nx * ny * nz;
+  // init (spirit.cpp:36-64)
+  float kf[3] = {q.kr_f[0], q.kr_f[1], q.kr_f[2]};
+  int kr[3], cr[3];
+  for (int d = 0; d < 3; d++) {
+    kr[d] = (int)std::ceil(kf[d]);
+    cr[d] = q.cr[d];
+  }
+  if (nz == 1) kr[2] = 0, cr[2] = 0;
+  // generateEigenCoils: ifft of each coil image back to k-space (spirit.cpp:146-151)
+  std::vector<std::vector<cx<double>>> K(C, std::vector<cx<double>>(n3));
+  for (int c = 0; c < C; c++) {
+    for (long i = 0; i < n3; i++) K[c][i] = cx<double>(img[c][i]);
+    centered_ifft3(K[c], N);
+  }
+  // calibrate_ellipsoid (spirit.cpp:181-400)
+  const int ce[3] = {cr[0] - kr[0], cr[1] - kr[1], cr[2] - kr[2]};
+  const long cx0 = nx / 2, cy0 = ny / 2, cz0 = nz / 2;
+  struct Off { int x, y, z; };
+  std::vector<Off> rows, kpts;
+  for (int iz = -ce[2]; iz <= ce[2]; iz++)
+    for (int iy = -ce[1]; iy <= ce[1]; iy++)
+      for (int ix = -ce[0]; ix <= ce[0]; ix++)
+        if (in_acs(ix, iy, iz, ce, q.square)) rows.push_back({ix, iy, iz});
+  for (int jz = -kr[2]; jz <= kr[2]; jz++)
+    for (int jy = -kr[1]; jy <= kr[1]; jy++)
+      for (int jx = -kr[0]; jx <= kr[0]; jx++)
+        if (in_kernel(jx, jy, jz, kf, q.square)) kpts.push_back({jx, jy, jz});
+  const int m = (int)rows.size(), nk = (int)kpts.size(), n = nk * C;
+  std::vector<cx<double>> A((size_t)m * n);  // column-major
+  for (int r = 0; r < m; r++)
+    for (int c = 0; c < C; c++)
+      for (int o = 0; o < nk; o++) {
+        const long x = kpts[o].x + rows[r].x + cx0, y = kpts[o].y + rows[r].y + cy0, z = kpts[o].z + rows[r].z + cz0;
+        A[r + (size_t)m * (c * nk + o)] = K[c][x + nx * (y + ny * z)];
+      }
+  // svd_econ(U, s, V, A, "r") by one-sided Jacobi on the columns of A (V accumulated) or,
+  // when A has more columns than rows, of A^H (its rotated columns are V diag(s))
+  std::vector<double> s;
+  std::vector<cx<double>> V;
+  const int kmin = std::min(m, n);
+  if (m < n) {
+    std::vector<cx<double>> B((size_t)n * m), W;
+    for (int r = 0; r < m; r++)
+      for (int c = 0; c < n; c++) B[c + (size_t)n * r] = std::conj(A[r + (size_t)m * c]);
+    jacobi_svd(B, n, m, s, W);
+    V.assign((size_t)n * m, cx<double>(0, 0));  // n x m: column j = B_j / s_j
+    for (int j = 0; j < m; j++)
+      if (s[j] > 0)
+        for (int c = 0; c < n; c++) V[c + (size_t)n * j] = B[c + (size_t)n * j] / s[j];
+  } else {
+    jacobi_svd(A, m, n, s, V);
+  }
+  std::vector<int> ord(s.size());
+  for (int j = 0; j < (int)s.size(); j++) ord[j] = j;
+  std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return s[a] > s[b]; });
+  const float thresh = (float)(s[ord[0]] * std::sqrt(q.svd_thresh));
+  int nV = 0;
+  for (int j = 0; j < kmin; j++)
+    if (s[ord[j]] >= thresh) nV++;
+  if (sv)
+    for (int j = 0; j < kmin; j++) sv[j] = s[ord[j]];
+  // kernel k(jx, jy, jz, coil, v) over the (2kr+1)^3 box (spirit.cpp:356-392)
+  const int bx = 2 * kr[0] + 1, by = 2 * kr[1] + 1, bz = 2 * kr[2] + 1, nb = bx * by * bz;
+  std::vector<cx<double>> kern((size_t)nb * C * nV, cx<double>(0, 0));  // [v][c][box]
+  for (int v = 0; v < nV; v++)
+    for (int c = 0; c < C; c++)
+      for (int o = 0; o < nk; o++) {
+        const int bi = (kpts[o].x + kr[0]) + bx * ((kpts[o].y + kr[1]) + by * (kpts[o].z + kr[2]));
+        kern[((size_t)v * C + c) * nb + bi] = V[(size_t)(c * nk + o) + (size_t)n * ord[v]];
+      }
+  // prep + getcoils (spirit.cpp:402-525): the kernel placed at the centre of each axis and
+  // inverse-FFT'd with the chop signs is, per axis, H(x, j) = m(x) m(N/2 + j) e^{2 pi i (N/2+j) x / N} / sqrt(N)
+  auto H = [&](int ax, long x, int j) -> cx<double> {
+    const long NN = N[ax], nn = NN / 2 + j;
+    const double sc = (double)(float)(1. / std::sqrt((float)NN));
+    const double a = 2.0 * M_PI * (double)((nn * x) % NN) / (double)NN;
+    return cx<double>(std::cos(a), std::sin(a)) * (chop_sign(x) * chop_sign(nn) * sc);
+  };
+#pragma omp parallel
+  {
+    std::vector<cx<double>> Ax((size_t)C * nV), Bh((size_t)nV * C), Vb;
+    std::vector<double> sb;
+#pragma omp for collapse(2) schedule(dynamic)
+    for (long z = 0; z < nz; z++)
+      for (long y = 0; y < ny; y++)
+        for (long x = 0; x < nx; x++) {
+          std::fill(Ax.begin(), Ax.end(), cx<double>(0, 0));
+          for (int jz = -kr[2]; jz <= kr[2]; jz++) {
+            const cx<double> hz = H(2, z, jz);
+            for (int jy = -kr[1]; jy <= kr[1]; jy++) {
+              const cx<double> hzy = hz * H(1, y, jy);
+              for (int jx = -kr[0]; jx <= kr[0]; jx++) {
+                const cx<double> h = hzy * H(0, x, jx);
+                const int bi = (jx + kr[0]) + bx * ((jy + kr[1]) + by * (jz + kr[2]));
+                for (int v = 0; v < nV; v++)
+                  for (int c = 0; c < C; c++) Ax[c + (size_t)C * v] += h * kern[((size_t)v * C + c) * nb + bi];
+              }
+            }
+          }
+          // svd_econ(U, s, V, A, "left"): U(:, 0) is the right singular vector of A^H
+          for (int v = 0; v < nV; v++)
+            for (int c = 0; c < C; c++) Bh[v + (size_t)nV * c] = std::conj(Ax[c + (size_t)C * v]);
+          jacobi_svd(Bh, nV, C, sb, Vb);
+          const int j0 = (int)(std::max_element(sb.begin(), sb.end()) - sb.begin());
+          if (ratio) {  // (s_2 / s_1)^2: the eigenvalue ratio that decides how well u is defined
+            double s2 = 0;
+            for (int j = 0; j < C; j++)
+              if (j != j0) s2 = std::max(s2, sb[j]);
+            ratio[x + nx * (y + ny * z)] = sb[j0] > 0 ? (s2 / sb[j0]) * (s2 / sb[j0]) : 1.0;
+          }
+          // LR(c) = conj(U(c, 0)); phase_correct (spirit.cpp:527-550)
+          const long vi = x + nx * (y + ny * z);
+          double mag = 0;
+          for (int c = 0; c < C; c++) mag += std::norm(Vb[c + (size_t)C * j0]);
+          const cx<double> m0 = std::conj(Vb[(size_t)C * j0]);
+          const cx<double> ci = std::polar(1.0, -std::arg(m0)) / std::sqrt(mag);
+          for (int c = 0; c < C; c++) maps[c][vi] = std::conj(Vb[c + (size_t)C * j0]) * ci;
+        }
+  }
+  return nV;
+}
+
+// ---------------------------------------------------------------------------
 // C ABI for ctypes (tests / bench baseline leg).
 // ---------------------------------------------------------------------------
 struct OHandle {
@@ -1596,6 +1780,14 @@ void orc_clear_combine(void **XX, int Nt, int C, const int *N, const int *bs, vo
 int orc_clear(void *hv, const OFrames *F, const OClearParams *q, void **XX, void **im, double *resid) {
   OHandle *h = (OHandle *)hv;
   return h->prec ? run_clear<double>(h, *F, *q, XX, im, resid) : run_clear<float>(h, *F, *q, XX, im, resid);
+}
+int orc_espirit(const void **img, int C, const int *N, const float *kr_f, const int *cr, float svd_thresh, int square,
+                void **maps, double *sv, double *ratio) {
+  OEspirit q;
+  for (int d = 0; d < 3; d++) q.kr_f[d] = kr_f[d], q.cr[d] = cr[d];
+  q.svd_thresh = svd_thresh;
+  q.square = square;
+  return espirit((const cx<float> *const *)img, C, N, q, (cx<double> **)maps, sv, ratio);
 }
 int orc_num_threads(void) { return omp_get_max_threads(); }
 }

@@ -79,6 +79,9 @@ def lib():
                                         ctypes.c_int]
         L.orc_clear.restype = ctypes.c_int
         L.orc_clear.argtypes = [vp, vp, vp, ctypes.POINTER(vp), ctypes.POINTER(vp), dp]
+        L.orc_espirit.restype = ctypes.c_int
+        L.orc_espirit.argtypes = [ctypes.POINTER(vp), ctypes.c_int, ip, fp, ip, ctypes.c_float, ctypes.c_int,
+                                  ctypes.POINTER(vp), dp, dp]
         L.orc_glibc_rand.argtypes = [ctypes.c_long, ctypes.c_int, ip]
         L.orc_num_threads.restype = ctypes.c_int
         _lib = L
@@ -366,6 +369,25 @@ def clear_combine(XX, bs, out=None):
     ip_ = (ctypes.c_void_p * T)(*[im[t].ctypes.data for t in range(T)])
     lib().orc_clear_combine(_coil_ptrs(XX), T, C, _ip((Nx, Ny, Nz)), _ip(bs), ip_, prec)
     return im
+
+
+def espirit(images, kr_f=(3.0, 3.0, 3.0), cr=(12, 12, 12), svd_thresh=0.01, square=False):
+    """ESPIRiT maps (spirit.cpp) from coil images (C, Nz, Ny, Nx) complex64: returns the maps
+    (C, Nz, Ny, Nx) complex128, the number of kernel vectors kept, the calibration
+    singular values (descending) and per voxel (s_2 / s_1)^2 of A_x (how well defined
+    the dominant vector is)."""
+    images = np.ascontiguousarray(images, dtype=np.complex64)
+    C, Nz, Ny, Nx = images.shape
+    maps = np.zeros(images.shape, np.complex128)
+    ip_ = (ctypes.c_void_p * C)(*[images[c].ctypes.data for c in range(C)])
+    mp = (ctypes.c_void_p * C)(*[maps[c].ctypes.data for c in range(C)])
+    sv = np.zeros(200000, np.float64)
+    kf = (ctypes.c_float * 3)(*kr_f)
+    ratio = np.zeros((Nz, Ny, Nx), np.float64)
+    nV = lib().orc_espirit(ip_, C, _ip((Nx, Ny, Nz)), kf, _ip(cr), svd_thresh, int(bool(square)), mp,
+                           sv.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                           ratio.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+    return maps, nV, sv[sv > 0], ratio
 
 
 def fft1d(x, sign, prec=1):
