@@ -392,7 +392,8 @@ def run_ours(a):
     iter_bytes = sum(bm.values()) + 9 * N ** 3 * 8
     roofline = {"bound": "hbm", "kernel": kernel_of(dom, out_tuning, C), "stage": dom, "achieved": achieved, "peak": peak,
                 "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-                "traffic": ncu_traffic(dom), "algorithmic_bytes_per_launch": bm[dom],
+                "traffic": ncu_traffic(dom) if a.config == "cg256" else None,  # the summary is for 256^3 x 32
+                "algorithmic_bytes_per_launch": bm[dom],
                 "launch_ms": per_launch_ms[dom]}
     # The ungridding gather is bound by the L1 data path, not HBM: every sample reads its
     # nx*ny*nz taps x C coils (8 B each) through L1.  Nominal L1 load bandwidth: 128 B per

@@ -261,8 +261,9 @@ mrg_status mrg_fista(mrg_plan *plan, const mrg_fista_params *params, void *X, do
  * step X_c -= (sum |R|^2 / sum P conj(R)) R_c with P_c = E_c^H W E_c R_c, then the coil
  * low-rank threshold of the X_c.  The coil images are combined at the end by the first
  * right singular vector of each block.  Coil maps are not used; frame trajectories and
- * data must be set.  The soft threshold of the reference's loop is off here (its
- * default, threshold_type none).  ncoil <= 32. */
+ * data must be set.  With use_threshold the loop's L1_threshold (src/recon_lib.cpp:
+ * 1152-1159, :2416-2527) runs on frame 0's coil images first: wavelet, fraction threshold,
+ * soft threshold, with cycle spinning.  ncoil <= 32. */
 typedef struct mrg_clear_params {
   int max_iter;            /* -max_iter */
   int block[3];            /* -clear_nx/ny/nz (default 4) */
@@ -272,7 +273,12 @@ typedef struct mrg_clear_params {
   float clear_t2;          /* -clear_t2 (default 6) */
   float early_stop_thresh; /* -early_stop_thresh (default 0: never) */
   int early_stop_range;    /* -early_stop_range (default 5) */
-  int64_t rand_skip;       /* rand() draws consumed before the first block shift (default 0) */
+  int64_t rand_skip;       /* rand() draws consumed before the first shift (default 0) */
+  int use_threshold;       /* -threshold_type fraction (1) or none (0, default) */
+  float thresh;            /* -thresh: fraction of coefficients set to zero */
+  int cycle_spins;         /* -cycle_spins (default 4) */
+  int wave_levels[3];      /* -wavelet_levelsX/Y/Z (default 4) */
+  int wave_type;           /* 0 DB2, 1 DB4 (default) */
 } mrg_clear_params;
 
 void mrg_clear_params_default(mrg_clear_params *p);

@@ -46,7 +46,9 @@ class MrgFistaParams(ctypes.Structure):
 class MrgClearParams(ctypes.Structure):
     _fields_ = [("max_iter", ctypes.c_int), ("block", ctypes.c_int * 3), ("block_iter", ctypes.c_int),
                 ("alpha_coil", ctypes.c_float), ("clear_amp", ctypes.c_float), ("clear_t2", ctypes.c_float),
-                ("early_stop_thresh", ctypes.c_float), ("early_stop_range", ctypes.c_int), ("rand_skip", ctypes.c_int64)]
+                ("early_stop_thresh", ctypes.c_float), ("early_stop_range", ctypes.c_int), ("rand_skip", ctypes.c_int64),
+                ("use_threshold", ctypes.c_int), ("thresh", ctypes.c_float), ("cycle_spins", ctypes.c_int),
+                ("wave_levels", ctypes.c_int * 3), ("wave_type", ctypes.c_int)]
 
 
 class MrgEspiritParams(ctypes.Structure):

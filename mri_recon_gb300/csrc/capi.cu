@@ -1663,6 +1663,10 @@ extern "C" mrg_status mrg_clear(mrg_plan *p, const mrg_clear_params *q, void *X,
     set_error("bad low-rank block parameters");
     return MRG_ERR_INVALID;
   }
+  if (q->use_threshold && (q->cycle_spins < 1 || q->wave_type < 0 || q->wave_type > 1 || q->rand_skip < 0)) {
+    set_error("bad wavelet / cycle-spin parameters");
+    return MRG_ERR_INVALID;
+  }
   if (p->C > 32) {
     set_error("CLEAR supports at most 32 coils");
     return MRG_ERR_UNSUPPORTED;
@@ -1685,32 +1689,52 @@ extern "C" mrg_status mrg_clear(mrg_plan *p, const mrg_clear_params *q, void *X,
   while (np2 < nb) np2 <<= 1;
   const int nblk = reduce_blocks(nc);
   const int iters_max = std::max(q->max_iter, 1);
-  // block shifts: 3 rand() draws per block iteration, only in iterations that threshold
-  // (LOWRANKCOIL::thresh returns before drawing when clear_alpha_coil is 0)
+  // rand() draws per iteration in the reference's order: 3 wavelet shifts per cycle spin
+  // (L1_threshold, wavelet3D.cpp:443-448), then 3 block shifts per block iteration
+  // (LOWRANKCOIL::thresh, which returns before drawing when clear_alpha_coil is 0)
   std::vector<int> sh((size_t)iters_max * 3 * std::max(q->block_iter, 1), 0);
-  if (q->alpha_coil != 0.0f) {
+  std::vector<int> wsh((size_t)iters_max * 3 * std::max(q->use_threshold ? q->cycle_spins : 1, 1), 0);
+  {
     GlibcRand rng;
     rng.skip(q->rand_skip);
-    for (size_t i = 0; i < (size_t)q->max_iter * q->block_iter; i++)
-      for (int d = 0; d < 3; d++) sh[3 * i + d] = rng.next() % bs[d] - bs[d] / 2;
+    const int wN = q->wave_type == 0 ? 2 : 4;
+    for (int it = 0; it < q->max_iter; it++) {
+      if (q->use_threshold)
+        for (int sp = 0; sp < q->cycle_spins; sp++)
+          for (int d = 0; d < 3; d++) wsh[((size_t)it * q->cycle_spins + sp) * 3 + d] = rng.next() % wN;
+      if (q->alpha_coil != 0.0f)
+        for (int b = 0; b < q->block_iter; b++)
+          for (int d = 0; d < 3; d++) sh[((size_t)it * q->block_iter + b) * 3 + d] = rng.next() % bs[d] - bs[d] / 2;
+    }
   }
+  int L[3] = {0, 0, 0}, max_level = 0;
+  if (q->use_threshold) wavelet_levels(g.N, q->wave_levels, L, &max_level);
   struct Bufs {
-    void *p[4] = {nullptr, nullptr, nullptr, nullptr};
+    void *p[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    ThrWork thr;
     ~Bufs() {
       for (void *x : p) cudaFree(x);
+      thr_free(thr);
     }
   } b;
-  const size_t sbytes = sizeof(double) * (3 * (size_t)iters_max + 3 * (size_t)nblk + nb + np2) + sizeof(float) +
-                        sizeof(int) * sh.size() + 64;
+  const size_t sbytes = sizeof(double) * (3 * (size_t)iters_max + 3 * (size_t)nblk + nb + np2) + 2 * sizeof(float) +
+                        sizeof(int) * (sh.size() + wsh.size()) + 64;
   MRG_CUDA(cudaMalloc(&b.p[0], sizeof(float2) * ntc));  // XX
   MRG_CUDA(cudaMalloc(&b.p[1], sizeof(float2) * ntc));  // RR
   MRG_CUDA(cudaMalloc(&b.p[2], sizeof(float2) * (nc + n)));  // PP of one frame, unit image
   MRG_CUDA(cudaMalloc(&b.p[3], sbytes));
   float2 *XX = (float2 *)b.p[0], *RR = (float2 *)b.p[1], *PP = (float2 *)b.p[2], *ones = PP + nc;
   double *acc = (double *)b.p[3], *part = acc + 3 * iters_max, *sig = part + 3 * nblk, *work = sig + nb;
-  float *smax = (float *)(work + np2);
-  int *dsh = (int *)(smax + 2);
+  float *smax = (float *)(work + np2), *dthr = smax + 1;
+  int *dsh = (int *)(smax + 2), *dwsh = dsh + sh.size();
   MRG_CUDA(cudaMemcpyAsync(dsh, sh.data(), sizeof(int) * sh.size(), cudaMemcpyHostToDevice, st));
+  MRG_CUDA(cudaMemcpyAsync(dwsh, wsh.data(), sizeof(int) * wsh.size(), cudaMemcpyHostToDevice, st));
+  float2 *W = nullptr;  // frame 0's coil images as C volumes for the wavelet
+  if (q->use_threshold) {
+    MRG_CUDA(cudaMalloc(&b.p[4], sizeof(float2) * nc));
+    W = (float2 *)b.p[4];
+    MRG_TRY(thr_alloc(b.thr, nc));
+  }
   MRG_CUDA(cudaMemsetAsync(acc, 0, sizeof(double) * 3 * iters_max, st));
   MRG_TRY(launch_zero(XX, sizeof(float2) * ntc, st));  // XX = 0
   MRG_TRY(launch_fill(ones, n, make_float2(1.0f, 0.0f), st));
@@ -1736,6 +1760,18 @@ extern "C" mrg_status mrg_clear(mrg_plan *p, const mrg_clear_params *q, void *X,
     }
     MRG_TRY(clear_step(XX, RR, ntc, ai, st));  // XX -= (R^H R / sum P conj R) R
     done = it + 1;
+    if (q->use_threshold) {  // L1_threshold(XX(0, all, all)) with cycle spinning (src/recon_lib.cpp:2491-2509)
+      MRG_TRY(launch_deinterleave(XX, C, n, W, n, st));
+      const float scale = (float)(1. / (float)q->cycle_spins);
+      for (int sp = 0; sp < q->cycle_spins; sp++) {
+        const int *s3 = dwsh + ((size_t)it * q->cycle_spins + sp) * 3;
+        MRG_TRY(wavelet3d(W, C, g.N, L, max_level, s3, q->wave_type, 0, st));
+        if (sp == 0) MRG_TRY(fraction_threshold(W, nc, q->thresh, scale, b.thr, dthr, st));
+        MRG_TRY(soft_threshold(W, nc, dthr, st));
+        MRG_TRY(wavelet3d(W, C, g.N, L, max_level, s3, q->wave_type, 1, st));
+      }
+      MRG_TRY(launch_interleave(W, n, C, n, XX, st));
+    }
     if (q->alpha_coil != 0.0f) {  // lrankcoil.update_threshold(XX, 2, it); lrankcoil.thresh(XX, 2)
       MRG_TRY(coil_llr_update(XX, T, C, g.N, bs, q->clear_amp, q->clear_t2, it, sig, work, smax, st));
       MRG_TRY(coil_llr_thresh(XX, T, C, g.N, bs, q->alpha_coil, q->block_iter, dsh + 3 * (size_t)q->block_iter * it,
@@ -1788,6 +1824,11 @@ void mrg_clear_params_default(mrg_clear_params *q) {
   q->early_stop_thresh = 0.0f;
   q->early_stop_range = 5;
   q->rand_skip = 0;
+  q->use_threshold = 0;
+  q->thresh = 0.0f;
+  q->cycle_spins = 4;
+  q->wave_levels[0] = q->wave_levels[1] = q->wave_levels[2] = 4;
+  q->wave_type = 1;
 }
 
 void mrg_fista_params_default(mrg_fista_params *q) {

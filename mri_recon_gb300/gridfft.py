@@ -507,8 +507,8 @@ def clear_params(**kw):
     p = _lib.MrgClearParams()
     _lib.load().mrg_clear_params_default(ctypes.byref(p))
     for k, v in kw.items():
-        if k == "block":
-            p.block[:] = list(v)
+        if k in ("block", "wave_levels"):
+            getattr(p, k)[:] = list(v)
         else:
             setattr(p, k, v)
     return p

@@ -1480,6 +1480,11 @@ struct OClearParams {
   float early_stop_thresh;
   int early_stop_range;
   long rand_skip;
+  int use_threshold;
+  float thresh;
+  int cycle_spins;
+  int wave_levels[3];
+  int wave_type;
 };
 
 // CLEAR (recon_lib.cpp:1025-1238): per-coil images XX[t*C + c] from zero; per iteration
@@ -1499,6 +1504,7 @@ static int run_clear(OHandle *h, const OFrames &F, const OClearParams &q, void *
   for (int i = 0; i < Nt * C; i++) std::fill(XX[i], XX[i] + n, cx<R>(0, 0));
   GRand rng(1);
   for (long i = 0; i < q.rand_skip; i++) rng.step();
+  Wave wave(p.g.N[0], p.g.N[1], p.g.N[2], q.wave_levels, q.wave_type);
   std::vector<float> diffs;
   double error0 = 0.0;
   int done = 0;
@@ -1538,6 +1544,16 @@ static int run_clear(OHandle *h, const OFrames &F, const OClearParams &q, void *
         XX[i][j] -= RR[i][j];
       }
     done = it + 1;
+    if (q.use_threshold) {  // L1_threshold(XX(0, all, all)): frame 0's coil images
+      float thr = 0;
+      for (int spin = 0; spin < q.cycle_spins; spin++) {
+        wave.random_shift(rng);
+        for (int c = 0; c < C; c++) wave.forward<R>(XX[c]);
+        if (spin == 0) thr = (float)(1. / (float)q.cycle_spins) * get_threshold<R>(XX, C, n, q.thresh, q.thresh);
+        for (int c = 0; c < C; c++) soft_threshold<R>(XX[c], n, thr);
+        for (int c = 0; c < C; c++) wave.backward<R>(XX[c]);
+      }
+    }
     if (q.alpha_coil != 0.0f) {
       const float smax = coil_update_threshold<R>(XX, Nt, C, p.g.N, q.bs, q.clear_amp, q.clear_t2, it);
       coil_thresh<R>(XX, Nt, C, p.g.N, q.bs, q.block_iter, q.alpha_coil, smax, rng);

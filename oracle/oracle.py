@@ -119,14 +119,18 @@ class FistaParams(ctypes.Structure):
 class ClearParams(ctypes.Structure):
     _fields_ = [("max_iter", ctypes.c_int), ("bs", ctypes.c_int * 3), ("block_iter", ctypes.c_int),
                 ("alpha_coil", ctypes.c_float), ("clear_amp", ctypes.c_float), ("clear_t2", ctypes.c_float),
-                ("early_stop_thresh", ctypes.c_float), ("early_stop_range", ctypes.c_int), ("rand_skip", ctypes.c_long)]
+                ("early_stop_thresh", ctypes.c_float), ("early_stop_range", ctypes.c_int), ("rand_skip", ctypes.c_long),
+                ("use_threshold", ctypes.c_int), ("thresh", ctypes.c_float), ("cycle_spins", ctypes.c_int),
+                ("wave_levels", ctypes.c_int * 3), ("wave_type", ctypes.c_int)]
 
 
 def clear_params(max_iter=50, bs=(4, 4, 4), block_iter=4, alpha_coil=0.01, clear_amp=4.0, clear_t2=6.0,
-                 early_stop_thresh=0.0, early_stop_range=5, rand_skip=0):
+                 early_stop_thresh=0.0, early_stop_range=5, rand_skip=0, use_threshold=0, thresh=0.0,
+                 cycle_spins=4, wave_levels=(4, 4, 4), wave_type=1):
     """The CLEAR loop's parameters with the reference's defaults (clear.cpp:47-61, recon_lib.cpp:83-85)."""
     return ClearParams(max_iter, (ctypes.c_int * 3)(*bs), block_iter, alpha_coil, clear_amp, clear_t2,
-                       early_stop_thresh, early_stop_range, rand_skip)
+                       early_stop_thresh, early_stop_range, rand_skip, use_threshold, thresh, cycle_spins,
+                       (ctypes.c_int * 3)(*wave_levels), wave_type)
 
 
 class Plan:

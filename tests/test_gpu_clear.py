@@ -93,15 +93,21 @@ def _plan(mrg_lib, N, C, T, frames, device=True):
     return p
 
 
-@pytest.mark.parametrize("N,C,T,nproj,iters,alpha", [(16, 4, 1, 300, 4, 0.01), (16, 3, 2, 200, 3, 0.01),
-                                                      (16, 1, 1, 300, 3, 0.01), (20, 6, 1, 400, 3, 0.0)])
-def test_clear_matches_oracle(mrg_lib, oracle_lib, N, C, T, nproj, iters, alpha):
+# the last two cases add the loop's L1-wavelet soft threshold (cycle spinning, DB4 and DB2)
+@pytest.mark.parametrize("N,C,T,nproj,iters,alpha,l1", [
+    (16, 4, 1, 300, 4, 0.01, None), (16, 3, 2, 200, 3, 0.01, None), (16, 1, 1, 300, 3, 0.01, None),
+    (20, 6, 1, 400, 3, 0.0, None),
+    (16, 4, 1, 300, 3, 0.01, dict(use_threshold=1, thresh=0.2, cycle_spins=3, wave_levels=(2, 2, 2), wave_type=1)),
+    (16, 3, 2, 200, 2, 0.0, dict(use_threshold=1, thresh=0.1, cycle_spins=2, wave_levels=(3, 3, 3), wave_type=0,
+                                 rand_skip=5))])
+def test_clear_matches_oracle(mrg_lib, oracle_lib, N, C, T, nproj, iters, alpha, l1):
     import torch
     frames = _inputs(oracle_lib, N, C, T, nproj, 9)
     p = _plan(mrg_lib, N, C, T, frames)
     X = torch.zeros((T, N, N, N), dtype=torch.complex64, device="cuda")
-    X, resid, XX = p.clear(mrg_lib.clear_params(max_iter=iters, alpha_coil=alpha), X=X, coil_images=True)
-    q = oracle_lib.clear_params(max_iter=iters, alpha_coil=alpha)
+    extra = l1 or {}
+    X, resid, XX = p.clear(mrg_lib.clear_params(max_iter=iters, alpha_coil=alpha, **extra), X=X, coil_images=True)
+    q = oracle_lib.clear_params(max_iter=iters, alpha_coil=alpha, **extra)
     XX64, im64, r64, d64 = oracle_lib.Plan(N, prec=1).clear(frames, q)
     XX32, im32, r32, d32 = oracle_lib.Plan(N, prec=0).clear(frames, q)
     XX = XX.cpu().numpy().transpose(0, 4, 1, 2, 3)
