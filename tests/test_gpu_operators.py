@@ -192,7 +192,7 @@ def test_errors_do_not_exit(mrg_lib):
     with pytest.raises(m.MrgError, match="STATE"):
         p.forward(0, c["X"])                       # no trajectory yet
     with pytest.raises(m.MrgError, match="UNSUPPORTED"):
-        m.Plan(112, 1, 1)                           # S = 176 = 16*11: radix 11 not built
+        m.Plan(300, 1, 1)                           # S = 464 = 8*58: lines longer than 384 not built
 
 
 @pytest.mark.parametrize("grid_mode", [1, 2, 3])
