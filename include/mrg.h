@@ -149,6 +149,13 @@ mrg_status mrg_adjoint_coil(mrg_plan *plan, int frame, const void *smap, const v
 mrg_status mrg_forward_coil(mrg_plan *plan, int frame, const void *X, const void *smap, void *data, const void *diff,
                             void *stream);
 
+/* gridFFT::do_fft / do_ifft (src/gridFFT.cpp:645-711) on a caller grid, unpruned: grid is
+ * Sz x Sy x Sx x ncoil complex64 (coil innermost, host or device), transformed in place
+ * along z, y, x (sign -1, FFTW_FORWARD) or x, y, z (sign +1, FFTW_BACKWARD), each axis
+ * scaled by 1/sqrt(S) (src/ArrayTemplates.cpp:276-427).  The operators run the same
+ * passes pruned to the image crop; this entry exposes them for cross-checks. */
+mrg_status mrg_fft3(mrg_plan *plan, void *grid, int sign, void *stream);
+
 /* The public gridFFT::k_rad field (src/gridFFT.h:102; default 9999): the radius of the
  * Gaussian taper exp(-|k|^2 / (2 k_rad^2)) E^H applies to each sample
  * (src/gridFFT.cpp:1096-1108).  The coil-map estimate sets it to the map resolution and

@@ -85,6 +85,7 @@ SIGNATURES = {
     "mrg_cg": (_i, [_vp, _i, _vp, _dp, _i, _vp]),
     "mrg_fista_params_default": (None, [ctypes.POINTER(MrgFistaParams)]),
     "mrg_fista": (_i, [_vp, ctypes.POINTER(MrgFistaParams), _vp, _dp, _fp, _i, _vp]),
+    "mrg_fft3": (_i, [_vp, _vp, _i, _vp]),
     "mrg_espirit_params_default": (None, [ctypes.POINTER(MrgEspiritParams)]),
     "mrg_espirit": (_i, [_vp, _i, _i, _i, _i, ctypes.POINTER(MrgEspiritParams), _vp, _ip, _dp, _i, _vp]),
     "mrg_espirit_smaps": (_i, [_vp, _i, _vp, _i64, ctypes.POINTER(MrgEspiritParams), _fp, _vp, _i64, _ip, _vp]),

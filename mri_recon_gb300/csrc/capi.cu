@@ -1156,6 +1156,44 @@ mrg_status mrg_lowres_smaps(mrg_plan *p, int frame, const void *data, int64_t co
   return MRG_OK;
 }
 
+mrg_status mrg_fft3(mrg_plan *p, void *grid, int sign, void *stream) {
+  if (!p || !grid || (sign != -1 && sign != 1)) {
+    set_error("bad argument");
+    return MRG_ERR_INVALID;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  const Geometry &g = p->geo;
+  const int C = p->C;
+  const int64_t Sx = g.S[0], Sy = g.S[1], Sz = g.S[2];
+  const size_t bytes = sizeof(float2) * (size_t)Sx * Sy * Sz * C;
+  void *dG;
+  bool sG;
+  MRG_TRY(dev_view(p, 0, grid, bytes, true, st, &dG, &sG));
+  float2 *G = (float2 *)dG;
+  // axis d: lines of S[d] points, element stride ls, `inner` lines per outer row of stride os
+  auto pass = [&](int d) -> mrg_status {
+    const int64_t S = g.S[d];
+    const int64_t ls = d == 0 ? C : (d == 1 ? Sx * C : Sy * Sx * C);
+    const int64_t inner = ls, outer = (Sx * Sy * Sz * C) / (S * ls);
+    FftPass a;
+    memset(&a, 0, sizeof(a));
+    a.S = (int)S; a.sign = sign; a.mode = FFT_PLAIN;
+    a.Lin = (int)S; a.in_off = 0; a.Lout = (int)S; a.out_off = 0;
+    a.inner = inner; a.IB = pass_ib(inner, C); a.lfast = 0;
+    a.nlines = outer * inner;
+    a.in_ls = ls; a.in_os = S * ls; a.out_ls = ls; a.out_os = S * ls;
+    a.scale = (float)(1. / std::sqrt((float)S));
+    a.in = G; a.out = G; a.C = C;
+    fft_vectorize(a);
+    return launch_fft(a, st);
+  };
+  const int order[3] = {2, 1, 0};  // do_fft: z, y, x; do_ifft: x, y, z
+  for (int k = 0; k < 3; k++) MRG_TRY(pass(sign < 0 ? order[k] : order[2 - k]));
+  if (sG) MRG_CUDA(cudaMemcpyAsync(grid, dG, bytes, cudaMemcpyDeviceToHost, st));
+  MRG_CUDA(cudaStreamSynchronize(st));
+  return MRG_OK;
+}
+
 mrg_status mrg_espirit_smaps(mrg_plan *p, int frame, const void *data, int64_t coil_stride,
                              const mrg_espirit_params *params, const float blur[3], void *smaps_out,
                              int64_t out_stride, int *kept, void *stream) {

@@ -252,6 +252,12 @@ class Plan:
                                                 a.ptr(out), _numel(out) // self.ncoils, _stream(stream)))
         return out
 
+    def fft3(self, grid, sign=-1, stream=None):
+        """do_fft (sign -1) / do_ifft (sign +1) of a grid (Sz, Sy, Sx, ncoils), unpruned, in place."""
+        a = _Args()
+        _lib.check(_lib.load().mrg_fft3(self._h, a.ptr(grid), int(sign), _stream(stream)))
+        return grid
+
     def espirit_smaps(self, frame, data, params=None, blur=None, stream=None):
         """ESPIRiT maps from one frame's k-space (the ESPIRIT branch of calc_sensitivity_maps);
         they become the plan's maps.  Returns (maps (ncoils, Nz, Ny, Nx), kernel vectors kept)."""

@@ -283,3 +283,22 @@ def test_set_frame_tuning_rejects_unavailable_shapes(mrg_lib):
         with pytest.raises(mrg_lib.MrgError):
             p.set_frame_tuning(0, *bad)
     assert p.frame_tuning(0) == t
+
+
+# Every line length the default geometry reaches, against cuFFT (torch.fft on the device) in
+# single and double precision: 16, 32, 48, 64, 112 (7), 176 (11), 192, 256, 304 (19), 368 (23), 384
+@pytest.mark.parametrize("N", [8, 16, 32, 40, 70, 112, 128, 168, 200, 236, 256])
+@pytest.mark.parametrize("sign", [-1, 1])
+def test_fft3_against_cufft(mrg_lib, N, sign):
+    torch = _torch()
+    C = 2
+    p = mrg_lib.Plan(N, C, 1)
+    Sx, Sy, Sz = p.S
+    g = torch.randn((Sz, Sy, Sx, C), dtype=torch.complex64, device="cuda", generator=torch.Generator("cuda").manual_seed(N))
+    f = torch.fft.fftn if sign < 0 else torch.fft.ifftn  # FFTW_FORWARD e^{-i}, FFTW_BACKWARD e^{+i}
+    ref64 = f(g.to(torch.complex128), dim=(0, 1, 2), norm="ortho")
+    ref32 = f(g, dim=(0, 1, 2), norm="ortho")
+    got = p.fft3(g.clone(), sign)
+    e64 = float(torch.linalg.norm(got - ref64) / torch.linalg.norm(ref64))
+    e32 = float(torch.linalg.norm(ref32 - ref64) / torch.linalg.norm(ref64))
+    assert e64 < max(1e-6, 2 * e32), (e64, e32)
