@@ -231,11 +231,52 @@ def run_reference(a):
     print(json.dumps(line), flush=True)
 
 
+def caller_rows(p, img, c, dev, timed):
+    """The callers either side of the operators on the 128^3 x 16-coil FISTA workload, each
+    device-timed after one untimed call: low-resolution coil maps, Pipe density compensation
+    of the trajectory, ESPIRiT maps and CLEAR iterations.  A failure is recorded, not raised."""
+    import torch
+
+    import mri_recon_gb300 as m
+    from mri_recon_gb300 import synth
+    out = {}
+    N, C = c["N"], c["coils"]
+    y = p.forward(0, img)
+    kx, ky, kz, kw = synth.radial_trajectory(N, c["nproj"], c["nread"], seed=c["seed"])
+    desc = "%d^3 x %d coils, %d x %d radial" % (N, C, c["nproj"], c["nread"])
+    rows = [
+        ("smaps_lowres128", "low-resolution coil maps (E^H per coil at k_rad 8, SOS normalisation), " + desc,
+         "maps/s", 1, lambda: p.lowres_smaps(0, y, smap_res=8.0)),
+        ("dcf128", "Pipe density compensation, 20 iterations, %d x %d radial at %d^3" % (c["nproj"], c["nread"], N),
+         "runs/s", 1, lambda: m.dcf_pipe(kx, ky, kz, N)),
+        ("espirit128", "ESPIRiT maps (kernel radius 3, calibration radius 12), " + desc, "maps/s", 1,
+         lambda: p.espirit_smaps(0, y)),
+    ]
+    for name, metric, unit, n, fn in rows:
+        try:
+            fn()
+            dt = timed(fn)
+            out[name] = {"metric": metric, "value": n / dt, "unit": unit}
+        except Exception as e:  # noqa: BLE001
+            out[name] = {"metric": metric, "error": str(e)[:200]}
+    try:
+        X = torch.zeros((1, N, N, N), dtype=torch.complex64, device=dev)
+        p.clear(m.clear_params(max_iter=1), X=X)
+        t_lo = timed(lambda: p.clear(m.clear_params(max_iter=2), X=X))
+        t_hi = timed(lambda: p.clear(m.clear_params(max_iter=6), X=X))
+        out["clear128"] = {"metric": "CLEAR iter/s (per-coil gradient step, coil low rank on 4^3 blocks, "
+                                     "4 block iterations), " + desc, "value": 4 / (t_hi - t_lo), "unit": "iter/s"}
+    except Exception as e:  # noqa: BLE001
+        out["clear128"] = {"metric": "CLEAR iter/s", "error": str(e)[:200]}
+    return out
+
+
 def side_configs(dev):
     """Throughput of the four smaller configurations, device-timed with inputs resident:
     SENSE-CG 64^3 x 8 (iter/s), FISTA-wavelet 128^3 x 16 (iter/s), FISTA-wavelet + time
     low-rank 128^3 x 20 coils x 10 frames (iter/s), and the differentiable NUFFT at 96^3 x 8
-    (loss + image and trajectory gradients per second, batch of 4 trajectories)."""
+    (loss + image and trajectory gradients per second, batch of 4 trajectories); plus the
+    callers of the operators on the 128^3 x 16 workload (caller_rows)."""
     import torch
 
     import mri_recon_gb300 as m
@@ -285,9 +326,10 @@ def side_configs(dev):
         return 20 / (t_hi - t_lo)
 
     c = synth.CONFIGS["fista128"]
-    p, _ = setup(c, 1, [c["nproj"]])
+    p, img = setup(c, 1, [c["nproj"]])
     out["fista128"] = {"metric": "FISTA-wavelet iter/s, 128^3 x 16 coils, 16384 x 128 radial, db4 3 levels, "
                                  "4 cycle spins, fraction threshold 0.1", "value": fista_rate(p), "unit": "iter/s"}
+    out.update(caller_rows(p, img, c, dev, timed))
     del p
     c = synth.CONFIGS["llr128"]
     projs = synth.frame_projection_counts(c["frames"], c["proj_lo"], c["proj_hi"], c["seed"])
