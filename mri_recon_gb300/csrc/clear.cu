@@ -46,28 +46,48 @@ __device__ __forceinline__ double2 zmul(double2 a, double2 b) {
 __device__ __forceinline__ double2 zconj(double2 a) { return make_double2(a.x, -a.y); }
 
 // Cyclic Hermitian Jacobi on G (n x n, leading dimension CL_LD), accumulating the
-// eigenvectors in V; warp-wide (lane k updates element k).  lam = the eigenvalues.
+// eigenvectors in V; warp-wide (lane k updates element k).  lam = the eigenvalues.  FP64
+// division and square root are slow on this part, so lane 0 alone computes each rotation
+// and shuffles it to the warp, and the off-diagonal norm is summed lane-strided.
 __device__ void herm_jacobi(double2 *G, double2 *V, double *lam, int n) {
   const int k = threadIdx.x & 31;
   for (int sweep = 0; sweep < 40; sweep++) {
     double off = 0.0, diag = 0.0;
-    for (int p = 0; p < n; p++) {
-      diag += G[p * CL_LD + p].x * G[p * CL_LD + p].x;
-      for (int q = p + 1; q < n; q++) off += G[p * CL_LD + q].x * G[p * CL_LD + q].x + G[p * CL_LD + q].y * G[p * CL_LD + q].y;
+    for (int e = k; e < n * n; e += 32) {
+      const int p = e / n, q = e - p * n;
+      const double2 g = G[p * CL_LD + q];
+      if (q > p) off += g.x * g.x + g.y * g.y;
+      else if (q == p) diag += g.x * g.x;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      off += __shfl_xor_sync(0xffffffffu, off, o);
+      diag += __shfl_xor_sync(0xffffffffu, diag, o);
     }
     if (off <= 1e-26 * diag || off == 0.0) break;  // |offdiag| <= 1e-13 |diag|
     for (int p = 0; p < n - 1; p++) {
       for (int q = p + 1; q < n; q++) {
-        const double2 gpq = G[p * CL_LD + q];
-        const double r = sqrt(gpq.x * gpq.x + gpq.y * gpq.y);
-        __syncwarp();
-        if (r <= 1e-300) continue;
-        const double2 e = make_double2(gpq.x / r, gpq.y / r);  // e^{i phi}
-        const double tau = (G[q * CL_LD + q].x - G[p * CL_LD + p].x) / (2.0 * r);
-        const double t = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
-        const double c = 1.0 / sqrt(1.0 + t * t), s = t * c;
-        const double2 se = make_double2(s * e.x, s * e.y), sec = make_double2(s * e.x, -s * e.y);
-        __syncwarp();
+        double c = 1.0, sx = 0.0, sy = 0.0;  // rotation: c and s e^{i phi}
+        int skip = 0;
+        if (k == 0) {
+          const double2 gpq = G[p * CL_LD + q];
+          const double r = sqrt(gpq.x * gpq.x + gpq.y * gpq.y);
+          if (r <= 1e-300) {
+            skip = 1;
+          } else {
+            const double tau = (G[q * CL_LD + q].x - G[p * CL_LD + p].x) / (2.0 * r);
+            const double t = (tau >= 0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+            c = 1.0 / sqrt(1.0 + t * t);
+            const double sr = t * c / r;  // s / r: s e^{i phi} = (s / r) g_pq
+            sx = sr * gpq.x;
+            sy = sr * gpq.y;
+          }
+        }
+        skip = __shfl_sync(0xffffffffu, skip, 0);
+        if (skip) continue;
+        c = __shfl_sync(0xffffffffu, c, 0);
+        sx = __shfl_sync(0xffffffffu, sx, 0);
+        sy = __shfl_sync(0xffffffffu, sy, 0);
+        const double2 se = make_double2(sx, sy), sec = make_double2(sx, -sy);
         if (k < n) {  // G <- G J, V <- V J
           const double2 gp = G[k * CL_LD + p], gq = G[k * CL_LD + q];
           const double2 a1 = zmul(sec, gq), a2 = zmul(se, gp);
@@ -99,10 +119,6 @@ __device__ void herm_jacobi(double2 *G, double2 *V, double *lam, int n) {
   if (k < n) lam[k] = fmax(G[k * CL_LD + k].x, 0.0);
 }
 
-// One CTA per block.  SA: the block matrix is gathered into shared memory; otherwise
-// (blocks too large for shared memory) every read goes to X, which the L1 serves.  A
-// row r (one frame's voxel) is read and rewritten by one warp only (lane = coil), so
-// the in-place update needs no staging.
 template <bool SA>
 __global__ void __launch_bounds__(256) k_llr_coil(const CoilLlrArgs a) {
   extern __shared__ __align__(16) unsigned char cl_sm[];
@@ -217,12 +233,16 @@ __global__ void __launch_bounds__(256) k_llr_coil(const CoilLlrArgs a) {
   }
   // M = V diag(f) V^H with f = max(s - tau, 0) / s  (src/clear.cpp:712-722)
   const double tau = a.alpha * (double)(*a.smax) / a.block_iter;
+  if (threadIdx.x < C) {  // f_j in place of lam_j
+    const double s = sqrt(lam[threadIdx.x]);
+    lam[threadIdx.x] = (s > 0.0) ? fmax(s - tau, 0.0) / s : 0.0;
+  }
+  __syncthreads();
   for (int e = threadIdx.x; e < C * C; e += blockDim.x) {
     const int r = e / C, cidx = e % C;
     double2 acc = make_double2(0.0, 0.0);
     for (int j = 0; j < C; j++) {
-      const double s = sqrt(lam[j]);
-      const double f = (s > 0.0) ? fmax(s - tau, 0.0) / s : 0.0;
+      const double f = lam[j];
       const double2 t = zmul(V[r * CL_LD + j], zconj(V[cidx * CL_LD + j]));
       acc.x += f * t.x;
       acc.y += f * t.y;
