@@ -178,6 +178,138 @@ __global__ void __launch_bounds__(256) k_llr_coil(const CoilLlrArgs a) {
       if (lane < C) As[r * C + lane] = a.X[row(r) + lane];
     __syncthreads();
   }
+  if (SA && C <= 16) {
+    // One-sided Jacobi on the columns of the block matrix in shared memory, in FP32 (FP64 is
+    // slow on this part): A W = U diag(s) column by column, W = V accumulated.  Round-robin
+    // rounds over the coil columns; warp w rotates pairs w, w + 8, ... of a round.  Measured
+    // against the FP64 oracle: <= 2e-6 per threshold application up to 16 coils, 1.4e-5 at
+    // 32 coils, so wider blocks take the FP64 Gram path below.
+    float2 *Vf = reinterpret_cast<float2 *>(G);  // V[c][j] at c * 33 + j
+    float *sg = reinterpret_cast<float *>(lam);  // column norms, then threshold factors
+    __shared__ unsigned s_off;
+    __shared__ float s_fl;
+    const int Ce = C + (C & 1), half = Ce / 2;
+    for (int e = threadIdx.x; e < C * 33; e += blockDim.x) Vf[e] = make_float2((e / 33) == (e % 33) ? 1.f : 0.f, 0.f);
+    if (warp == 0) {  // floor of the pair test: (1e-6 x the largest column norm)^2
+      float mx = 0.f;
+      for (int j = 0; j < C; j++) {
+        float sq = 0.f;
+        for (int r = lane; r < R; r += 32) {
+          const float2 x = As[r * C + j];
+          sq += x.x * x.x + x.y * x.y;
+        }
+        for (int o = 16; o > 0; o >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
+        mx = fmaxf(mx, sq);
+      }
+      if (lane == 0) s_fl = 1e-12f * mx;
+    }
+    __syncthreads();
+    const float fl = s_fl;
+    for (int sweep = 0; sweep < 40; sweep++) {
+      if (threadIdx.x == 0) s_off = 0u;
+      __syncthreads();
+      for (int rnd = 0; rnd < Ce - 1; rnd++) {
+        for (int pp = warp; pp < half; pp += nwarp) {
+          const int jp = pp == 0 ? 0 : 1 + (pp - 1 + rnd) % (Ce - 1);
+          const int jq = 1 + (Ce - 2 - pp + rnd) % (Ce - 1);  // position Ce - 1 - pp >= 1
+          if (jp >= C || jq >= C) continue;                    // the padding column of an odd C
+          float al = 0.f, be = 0.f, gr = 0.f, gi = 0.f;
+          for (int r = lane; r < R; r += 32) {
+            const float2 x = As[r * C + jp], y = As[r * C + jq];
+            al += x.x * x.x + x.y * x.y;
+            be += y.x * y.x + y.y * y.y;
+            gr += x.x * y.x + x.y * y.y;  // conj(x) y
+            gi += x.x * y.y - x.y * y.x;
+          }
+          for (int o = 16; o > 0; o >>= 1) {
+            al += __shfl_xor_sync(0xffffffffu, al, o);
+            be += __shfl_xor_sync(0xffffffffu, be, o);
+            gr += __shfl_xor_sync(0xffffffffu, gr, o);
+            gi += __shfl_xor_sync(0xffffffffu, gi, o);
+          }
+          const float ag = sqrtf(gr * gr + gi * gi);
+          if (!(al > 0.f && be > 0.f && ag > 0.f)) continue;
+          const float rel = ag / sqrtf(fmaxf(al, fl) * fmaxf(be, fl));
+          if (lane == 0) atomicMax(&s_off, __float_as_uint(rel));
+          if (rel < 4e-7f) continue;
+          const float zeta = (be - al) / (2.f * ag);
+          const float t = (zeta >= 0.f ? 1.f : -1.f) / (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
+          const float cs = 1.f / sqrtf(1.f + t * t), sn = cs * t;
+          const float phx = gr / ag, phy = gi / ag;
+          auto rot = [&](float2 *px, float2 *py) {  // x' = cs x - sn y', y' = (sn x + cs y') ph, y' = y conj(ph)
+            const float2 x = *px, y0 = *py;
+            const float2 y = make_float2(y0.x * phx + y0.y * phy, y0.y * phx - y0.x * phy);
+            *px = make_float2(cs * x.x - sn * y.x, cs * x.y - sn * y.y);
+            const float2 u = make_float2(sn * x.x + cs * y.x, sn * x.y + cs * y.y);
+            *py = make_float2(u.x * phx - u.y * phy, u.x * phy + u.y * phx);
+          };
+          for (int r = lane; r < R; r += 32) rot(As + r * C + jp, As + r * C + jq);
+          if (lane < C) rot(Vf + lane * 33 + jp, Vf + lane * 33 + jq);
+        }
+        __syncthreads();
+      }
+      const float off = __uint_as_float(s_off);
+      __syncthreads();
+      if (off < 4e-7f) break;
+    }
+    for (int j = warp; j < C; j += nwarp) {  // s_j = |column j of A W|
+      float sq = 0.f;
+      for (int r = lane; r < R; r += 32) {
+        const float2 x = As[r * C + j];
+        sq += x.x * x.x + x.y * x.y;
+      }
+      for (int o = 16; o > 0; o >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
+      if (lane == 0) sg[j] = sqrtf(sq);
+    }
+    __syncthreads();
+    if (a.mode == 2) {
+      // combine: A v1 = column jmax of A W, times the phase that makes v1's largest
+      // component real and positive
+      if (threadIdx.x == 0) {
+        int j = 0;
+        for (int q = 1; q < C; q++)
+          if (sg[q] > sg[j]) j = q;
+        jmax = j;
+        int m = 0;
+        float mm = -1.f;
+        for (int q = 0; q < C; q++) {
+          const float2 x = Vf[q * 33 + j];
+          const float n2 = x.x * x.x + x.y * x.y;
+          if (n2 > mm) mm = n2, m = q;
+        }
+        const float2 x = Vf[m * 33 + j];
+        const float n = sqrtf(mm);
+        ph = (n > 0.f) ? make_double2(x.x / n, -x.y / n) : make_double2(1.0, 0.0);
+      }
+      __syncthreads();
+      const float px = (float)ph.x, py = (float)ph.y;
+      for (int r = threadIdx.x; r < R; r += blockDim.x) {
+        const float2 x = As[r * C + jmax];
+        a.out[row(r) / C] = make_float2(x.x * px - x.y * py, x.x * py + x.y * px);
+      }
+      return;
+    }
+    // threshold: A' = (A W) diag(f) V^H, f = max(s - tau, 0) / s
+    const double tau = a.alpha * (double)(*a.smax) / a.block_iter;
+    __syncthreads();
+    if (threadIdx.x < C) {
+      const float sj = sg[threadIdx.x];
+      sg[threadIdx.x] = sj > 0.f ? (float)(fmax((double)sj - tau, 0.0) / (double)sj) : 0.f;
+    }
+    __syncthreads();
+    for (int r = warp; r < R; r += nwarp) {
+      float2 acc = make_float2(0.f, 0.f);
+      if (lane < C)
+        for (int j = 0; j < C; j++) {
+          const float2 x = As[r * C + j], v = Vf[lane * 33 + j];
+          const float f = sg[j];
+          acc.x += f * (x.x * v.x + x.y * v.y);  // x f conj(v)
+          acc.y += f * (x.y * v.x - x.x * v.y);
+        }
+      if (lane < C) a.X[row(r) + lane] = acc;
+    }
+    return;
+  }
   auto ld = [&](int r, int c) -> float2 { return SA ? As[r * C + c] : a.X[row(r) + c]; };
   // Gram matrix G = A^H A in FP64 (upper triangle, mirrored)
   for (int e = threadIdx.x; e < C * C; e += blockDim.x) {
