@@ -118,3 +118,24 @@ def test_clear_loop_reduces_data_error(oracle_lib):
     e0 = sum(np.linalg.norm(d * np.sqrt(cs["kw"])) ** 2 for d in cs["data"])
     assert done == 6 and err(XX6) < err(XX1) < e0
     assert np.all(np.isfinite(im)) and np.abs(im).max() > 0
+
+
+def test_clear_l1_threshold_by_hand(oracle_lib):
+    """One iteration with the loop's L1 threshold and no coil threshold: the gradient step,
+    then on frame 0's coil images the DB4 wavelet at the glibc rand() shifts after rand_skip
+    draws, the fraction threshold over all coils, the soft threshold, the inverse wavelet."""
+    cs = case(N=16, C=3, nproj=200, seed=8)
+    O = oracle_lib.Plan(16, prec=1)
+    frames = [dict(kx=cs["kx"], ky=cs["ky"], kz=cs["kz"], kw=cs["kw"], data=cs["data"])]
+    plain, _, _, _ = O.clear(frames, oracle_lib.clear_params(max_iter=1, alpha_coil=0.0))
+    q = oracle_lib.clear_params(max_iter=1, alpha_coil=0.0, use_threshold=1, thresh=0.3, cycle_spins=1,
+                                wave_levels=(2, 2, 2), wave_type=1, rand_skip=7)
+    got, _, _, _ = O.clear(frames, q)
+    r = oracle_lib.glibc_rand(7, 3)
+    shift = tuple(int(v) % 4 for v in r)
+    W = [oracle_lib.wavelet(plain[0, c], (2, 2, 2), shift, 1) for c in range(3)]
+    thr = oracle_lib.fraction_threshold(W, 0.3)
+    ref = np.stack([oracle_lib.wavelet(oracle_lib.soft_threshold(w, thr), (2, 2, 2), shift, 1, inverse=True)
+                    for w in W])
+    assert rel(got[0], ref) < 1e-12
+    assert rel(got[0], plain[0]) > 1e-3
