@@ -84,3 +84,31 @@ def test_errors_are_reported_not_fatal(mrg_lib):
     cfg = MrgConfig()
     L.mrg_config_default(ctypes.byref(cfg))
     assert abs(cfg.overgrid - 1.5) < 1e-7 and cfg.kernel_type == 1 and abs(cfg.k_rad - 9999.0) < 1e-3
+
+
+def test_loop_parameter_defaults_are_the_references(mrg_lib):
+    """FISTA (src/recon_lib.cpp:83-133), CLEAR (src/clear.cpp:47-61) and SPIRIT
+    (src/spirit.cpp:9-34) defaults, and the DCF flags (src/recon_lib.cpp), set without a GPU;
+    the Python structures match the C layout."""
+    from mri_recon_gb300 import _lib
+    L = mrg_lib.load()
+    f = _lib.MrgFistaParams()
+    L.mrg_fista_params_default(ctypes.byref(f))
+    assert f.max_iter == 50 and f.max_eig_iter == 30 and f.cycle_spins == 4 and list(f.wave_levels) == [4, 4, 4]
+    assert f.wave_type == 1 and list(f.llr_block) == [4, 4, 4] and f.llr_block_iter == 4 and f.llr_alpha == 0.0
+    c = _lib.MrgClearParams()
+    L.mrg_clear_params_default(ctypes.byref(c))
+    assert c.max_iter == 50 and list(c.block) == [4, 4, 4] and c.block_iter == 4
+    assert abs(c.alpha_coil - 0.01) < 1e-9 and c.clear_amp == 4.0 and c.clear_t2 == 6.0
+    assert c.early_stop_thresh == 0.0 and c.early_stop_range == 5 and c.rand_skip == 0
+    assert c.use_threshold == 0 and c.cycle_spins == 4 and list(c.wave_levels) == [4, 4, 4] and c.wave_type == 1
+    e = _lib.MrgEspiritParams()
+    L.mrg_espirit_params_default(ctypes.byref(e))
+    assert list(e.kernel_radius) == [3.0, 3.0, 3.0] and list(e.calib_radius) == [12, 12, 12]
+    assert abs(e.svd_thresh - 0.01) < 1e-9 and e.square == 0
+    d = _lib.MrgDcfParams()
+    L.mrg_dcf_params_default(ctypes.byref(d))
+    assert d.iters == 20 and abs(d.dwin - 2.1) < 1e-6
+    # the Python wrappers fill the same structures
+    assert list(mrg_lib.espirit_params(kernel_radius=2.5, calib_radius=9).kernel_radius) == [2.5, 2.5, 2.5]
+    assert list(mrg_lib.clear_params(block=(8, 8, 2), wave_levels=(3, 3, 3)).block) == [8, 8, 2]
