@@ -112,3 +112,27 @@ def test_loop_parameter_defaults_are_the_references(mrg_lib):
     # the Python wrappers fill the same structures
     assert list(mrg_lib.espirit_params(kernel_radius=2.5, calib_radius=9).kernel_radius) == [2.5, 2.5, 2.5]
     assert list(mrg_lib.clear_params(block=(8, 8, 2), wave_levels=(3, 3, 3)).block) == [8, 8, 2]
+
+
+def test_new_entry_points_reject_bad_arguments_without_a_gpu(mrg_lib):
+    """Argument checks of the CLEAR, ESPIRiT and FFT entry points run before any CUDA call."""
+    from mri_recon_gb300 import _lib
+    L = mrg_lib.load()
+    ip3 = (ctypes.c_int * 3)
+    buf = np.zeros(64, np.complex64)
+    ptr = ctypes.c_void_p(buf.ctypes.data)
+    cp = _lib.MrgClearParams()
+    L.mrg_clear_params_default(ctypes.byref(cp))
+    assert L.mrg_clear(None, ctypes.byref(cp), ptr, None, None, None, None) == 1
+    assert L.mrg_clear_thresh(ptr, 1, 4, 4, 4, 4, ip3(0, 4, 4), 4, 0.1, 1.0, 0, None) == 1
+    assert L.mrg_clear_thresh(ptr, 1, 4, 4, 4, 4, ip3(4, 4, 4), 0, 0.1, 1.0, 0, None) == 1
+    assert L.mrg_clear_combine(ptr, 0, 4, 4, 4, 4, ip3(4, 4, 4), ptr, None) == 1
+    assert L.mrg_clear_update_threshold(ptr, 1, 4, 4, 4, 4, ip3(4, 4, 4), 4.0, 6.0, 0, None, None) == 1
+    ep = _lib.MrgEspiritParams()
+    L.mrg_espirit_params_default(ctypes.byref(ep))
+    ep.kernel_radius[0] = 8.0
+    assert L.mrg_espirit(ptr, 4, 4, 4, 4, ctypes.byref(ep), ptr, None, None, 0, None) == 1
+    assert b"radius" in L.mrg_last_error()
+    assert L.mrg_espirit(None, 4, 4, 4, 4, ctypes.byref(ep), ptr, None, None, 0, None) == 1
+    assert L.mrg_espirit_smaps(None, 0, ptr, 0, ctypes.byref(ep), None, None, 0, None, None) == 1
+    assert L.mrg_fft3(None, ptr, -1, None) == 1
