@@ -185,6 +185,8 @@ struct FFT1 {
       tw[k] = cx<R>((R)std::cos(a), (R)std::sin(a));
     }
   }
+  // len * ts == n at every level, so the twiddle index r * k * ts stays below n, and the
+  // p-point DFT's W_p^(rq) is tw[((r q) mod p) * n / p]; radices 2 and 4 use butterflies.
   void rec(const cx<R> *in, long is, cx<R> *out, int len, int fi, long ts) const {
     if (len == 1) { out[0] = in[0]; return; }
     int p = fac[fi], m = len / p;
@@ -193,12 +195,27 @@ struct FFT1 {
     std::vector<cx<R>> tv;
     cx<R> *tp = t;
     if (p > 64) { tv.resize(p); tp = tv.data(); }
+    const long np = n / p;
+    const R sg = (R)(tw[np].imag() >= 0 ? 1 : -1);  // W_4^1 = sg * i when p == 4
     for (int k = 0; k < m; k++) {
-      for (int r = 0; r < p; r++) tp[r] = out[r * m + k] * tw[(long)r * k * ts % n];
-      for (int q = 0; q < p; q++) {
-        cx<R> acc(0, 0);
-        for (int r = 0; r < p; r++) acc += tp[r] * tw[(long)r * q * m * ts % n];
-        out[k + m * q] = acc;
+      tp[0] = out[k];
+      for (int r = 1; r < p; r++) tp[r] = out[r * m + k] * tw[(long)r * k * ts];
+      if (p == 2) {
+        out[k] = tp[0] + tp[1];
+        out[k + m] = tp[0] - tp[1];
+      } else if (p == 4) {
+        const cx<R> a = tp[0] + tp[2], b = tp[0] - tp[2], c = tp[1] + tp[3], d0 = tp[1] - tp[3];
+        const cx<R> d(-sg * d0.imag(), sg * d0.real());  // (sg i) (t1 - t3)
+        out[k] = a + c;
+        out[k + m] = b + d;
+        out[k + 2 * m] = a - c;
+        out[k + 3 * m] = b - d;
+      } else {
+        for (int q = 0; q < p; q++) {
+          cx<R> acc = tp[0];
+          for (int r = 1; r < p; r++) acc += tp[r] * tw[((long)r * q % p) * np];
+          out[k + m * q] = acc;
+        }
       }
     }
   }
