@@ -51,7 +51,7 @@ void build_geometry(Geometry &g, const mrg_config &cfg, int Nx, int Ny, int Nz) 
     g.lut_len = glen + 10;
     std::vector<float> &f = g.lut[d];
     f.assign(glen + 10, 0.0f);
-    g.beta[d] = 0.0f;
+    g.beta[d] = 12.0f;  // gridFFT's betaX/Y/Z default, kept by the kernels other than Kaiser-Bessel
     switch (cfg.kernel_type) {
       case MRG_KERNEL_TRIANGLE:
         for (int i = 0; i < glen + 1; i++) f[i] = 1.0f - (float)i / (float)glen;
@@ -59,8 +59,10 @@ void build_geometry(Geometry &g, const mrg_config &cfg, int Nx, int Ny, int Nz) 
       case MRG_KERNEL_SINC:
         for (int i = 0; i < glen + 1; i++) {
           const float pos = ((float)i * (float)dw) / ((float)glen);
-          f[i] = (pos < 0.01f) ? 1.0f : (float)(std::sin(pos * kRefPI) / (pos * kRefPI));
-          f[i] *= (float)(0.54 + 0.46 * std::cos(kRefPI * (float)i / ((float)glen)));
+          // the cut-off compares the float position with the double 0.01, and the Hamming
+          // factor multiplies in double (src/gridFFT.cpp:409-417)
+          f[i] = (pos < 0.01) ? 1.0f : (float)(std::sin(pos * kRefPI) / (pos * kRefPI));
+          f[i] = (float)(f[i] * (0.54 + 0.46 * std::cos(kRefPI * (float)i / ((float)glen))));
         }
         break;
       case MRG_KERNEL_POLY: {

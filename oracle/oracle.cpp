@@ -105,7 +105,7 @@ static void build_geom(Geom &g, int Nx, int Ny, int Nz, float overgrid, float dw
     g.lut_len = glen + 10;
     std::vector<float> &f = g.lut[d];
     f.assign(glen + 10, 0.0f);
-    g.beta[d] = 0;
+    g.beta[d] = 12;  // gridFFT() default (gridFFT.cpp:33-35), kept by non-Kaiser kernels
     if (ktype == K_TRIANGLE) {
       for (int i = 0; i < glen + 1; i++) f[i] = 1.0f - (float)i / (float)glen;
     } else if (ktype == K_KAISER) {
@@ -122,8 +122,8 @@ static void build_geom(Geom &g, int Nx, int Ny, int Nz, float overgrid, float dw
     } else if (ktype == K_SINC) {
       for (int i = 0; i < glen + 1; i++) {
         float pos = ((float)i * (float)dw) / ((float)glen);
-        f[i] = (pos < 0.01f) ? 1.0f : (float)(std::sin(pos * kPI) / (pos * kPI));
-        f[i] *= (float)(0.54 + 0.46 * std::cos(kPI * (float)i / ((float)glen)));
+        f[i] = (pos < 0.01) ? 1.0f : (float)(std::sin(pos * kPI) / (pos * kPI));  // double 0.01
+        f[i] = (float)(f[i] * (0.54 + 0.46 * std::cos(kPI * (float)i / ((float)glen))));   // gridFFT.cpp:409-417
       }
     } else {  // polynomial table (gridFFT.cpp:248-269), filled over the whole length
       int len = glen + 10;
@@ -1360,6 +1360,47 @@ static void normal_op(OHandle *h, const OFrames &F, int t, const cx<R> *X, cx<R>
   }
 }
 
+// The vector part of one CG iteration (recon_lib.cpp:1659-1722) on Nt frames of n voxels
+// (Nz planes): alpha = sum|r|^2 / sum p^H L in complex<double> per-z partial sums cast to
+// float, X += alpha P, R -= alpha L, beta = sum|r_new|^2 / sum|r|^2, P = R + beta P.
+// Returns sum|r_new|^2.
+template <typename R>
+static double cg_vectors(int Nt, long n, int Nz, cx<R> **X, cx<R> **Rr, cx<R> **Pp, cx<R> *const *L) {
+  const long plane = n / Nz;
+  std::vector<cx<double>> a_rr(Nz), a_pl(Nz), a_rn(Nz);
+  for (int t = 0; t < Nt; t++) {
+#pragma omp parallel for
+    for (int k = 0; k < Nz; k++)
+      for (long q = 0; q < plane; q++) {
+        long i = k * plane + q;
+        a_rr[k] += (double)(R)std::norm(Rr[t][i]);
+        cx<R> pl = std::conj(Pp[t][i]) * L[t][i];
+        a_pl[k] += cx<double>(pl.real(), pl.imag());
+      }
+  }
+  cx<double> rr(0, 0), pl(0, 0), rn(0, 0);
+  for (int k = 0; k < Nz; k++) { rr += a_rr[k]; pl += a_pl[k]; }
+  cx<double> ds = rr / pl;
+  cx<R> scale((R)ds.real(), (R)ds.imag());
+  for (int t = 0; t < Nt; t++) {
+#pragma omp parallel for
+    for (int k = 0; k < Nz; k++)
+      for (long q = 0; q < plane; q++) {
+        long i = k * plane + q;
+        X[t][i] += scale * Pp[t][i];
+        Rr[t][i] -= scale * L[t][i];
+        a_rn[k] += (double)(R)std::norm(Rr[t][i]);
+      }
+  }
+  for (int k = 0; k < Nz; k++) rn += a_rn[k];
+  cx<double> d2 = rn / rr;
+  cx<R> scale2((R)d2.real(), (R)d2.imag());
+  for (int t = 0; t < Nt; t++)
+#pragma omp parallel for
+    for (long i = 0; i < n; i++) Pp[t][i] = Rr[t][i] + scale2 * Pp[t][i];
+  return rn.real();
+}
+
 // SENSE-CG (recon_lib.cpp:1523-1759).  X[t] must be zero on entry.
 template <typename R>
 static void run_cg(OHandle *h, const OFrames &F, int iters, void **Xv, double *resid) {
@@ -1376,43 +1417,21 @@ static void run_cg(OHandle *h, const OFrames &F, int iters, void **Xv, double *r
                 F.kw[t], F.M[t]);
     Pp[t] = Rr[t];
   }
+  std::vector<cx<R> *> xp(Nt), rp(Nt), pp(Nt), lp(Nt);
+  for (int t = 0; t < Nt; t++) {
+    xp[t] = X[t];
+    rp[t] = Rr[t].data();
+    pp[t] = Pp[t].data();
+    lp[t] = L[t].data();
+  }
+  (void)plane;
   for (int it = 0; it < iters; it++) {
     for (int t = 0; t < Nt; t++) {
       std::fill(L[t].begin(), L[t].end(), cx<R>(0, 0));
       normal_op<R>(h, F, t, Pp[t].data(), L[t].data(), tmp, false);
     }
-    std::vector<cx<double>> a_rr(Nz), a_pl(Nz), a_rn(Nz);
-    for (int t = 0; t < Nt; t++) {
-#pragma omp parallel for
-      for (int k = 0; k < Nz; k++)
-        for (long q = 0; q < plane; q++) {
-          long i = k * plane + q;
-          a_rr[k] += (double)(R)std::norm(Rr[t][i]);
-          cx<R> pl = std::conj(Pp[t][i]) * L[t][i];
-          a_pl[k] += cx<double>(pl.real(), pl.imag());
-        }
-    }
-    cx<double> rr(0, 0), pl(0, 0), rn(0, 0);
-    for (int k = 0; k < Nz; k++) { rr += a_rr[k]; pl += a_pl[k]; }
-    cx<double> ds = rr / pl;
-    cx<R> scale((R)ds.real(), (R)ds.imag());
-    for (int t = 0; t < Nt; t++) {
-#pragma omp parallel for
-      for (int k = 0; k < Nz; k++)
-        for (long q = 0; q < plane; q++) {
-          long i = k * plane + q;
-          X[t][i] += scale * Pp[t][i];
-          Rr[t][i] -= scale * L[t][i];
-          a_rn[k] += (double)(R)std::norm(Rr[t][i]);
-        }
-    }
-    for (int k = 0; k < Nz; k++) rn += a_rn[k];
-    cx<double> d2 = rn / rr;
-    cx<R> scale2((R)d2.real(), (R)d2.imag());
-    for (int t = 0; t < Nt; t++)
-#pragma omp parallel for
-      for (long i = 0; i < n; i++) Pp[t][i] = Rr[t][i] + scale2 * Pp[t][i];
-    if (resid) resid[it] = rn.real();
+    const double rn = cg_vectors<R>(Nt, n, Nz, xp.data(), rp.data(), pp.data(), lp.data());
+    if (resid) resid[it] = rn;
   }
 }
 
@@ -1734,6 +1753,13 @@ void orc_fista(void *hv, const OFrames *F, const OFistaParams *q, void **X, doub
   if (h->prec) run_fista<double>(h, *F, *q, X, resid, step, thr); else run_fista<float>(h, *F, *q, X, resid, step, thr);
 }
 // E^H W E per frame, summed over coils, accumulated into out.
+// One CG iteration's vector updates on caller images (the CPU baseline's timing of them).
+double orc_cg_vectors(int Nt, long n, int Nz, void **X, void **R, void **P, void **L, int prec) {
+  if (prec)
+    return cg_vectors<double>(Nt, n, Nz, (cx<double> **)X, (cx<double> **)R, (cx<double> **)P, (cx<double> **)L);
+  return cg_vectors<float>(Nt, n, Nz, (cx<float> **)X, (cx<float> **)R, (cx<float> **)P, (cx<float> **)L);
+}
+
 void orc_normal(void *hv, const OFrames *F, int t, const void *X, void *out) {
   OHandle *h = (OHandle *)hv;
   if (h->prec) { std::vector<cx<double>> tmp; normal_op<double>(h, *F, t, (const cx<double> *)X, (cx<double> *)out, tmp, false); }

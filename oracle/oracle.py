@@ -83,6 +83,8 @@ def lib():
         L.orc_espirit.argtypes = [ctypes.POINTER(vp), ctypes.c_int, ip, fp, ip, ctypes.c_float, ctypes.c_int,
                                   ctypes.POINTER(vp), dp, dp]
         L.orc_glibc_rand.argtypes = [ctypes.c_long, ctypes.c_int, ip]
+        L.orc_cg_vectors.restype = ctypes.c_double
+        L.orc_cg_vectors.argtypes = [ctypes.c_int, ctypes.c_long, ctypes.c_int] + [ctypes.POINTER(vp)] * 4 + [ctypes.c_int]
         L.orc_num_threads.restype = ctypes.c_int
         _lib = L
     return _lib
@@ -507,6 +509,16 @@ def glibc_rand(skip, n):
     out = (ctypes.c_int * n)()
     lib().orc_glibc_rand(skip, n, out)
     return np.array(out[:], dtype=np.int64)
+
+
+def cg_vectors(X, R, P, L):
+    """One CG iteration's vector updates (X, R, P updated in place; L read) on lists of
+    (Nz, Ny, Nx) complex64 frames; returns sum |r|^2 after the update."""
+    Nz = X[0].shape[0]
+    n = X[0].size
+    arr = lambda vs: (ctypes.c_void_p * len(vs))(*[v.ctypes.data for v in vs])
+    prec = 1 if X[0].dtype == np.complex128 else 0
+    return lib().orc_cg_vectors(len(X), n, Nz, arr(X), arr(R), arr(P), arr(L), prec)
 
 
 def num_threads():

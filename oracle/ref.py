@@ -1,0 +1,161 @@
+"""REFERENCE CHECKER -- TEST INFRASTRUCTURE ONLY.
+
+ctypes front end for ``oracle/_ref/libref.so``: the reference's own gridFFT.cpp,
+ArrayTemplates.cpp, wavelet3D.cpp and threshold.cpp compiled unmodified (``make -C oracle
+ref``) against the stand-in Blitz++ / FFTW / Armadillo / HDF5 headers of
+``oracle/refshim`` and driven by ``oracle/ref_driver.cpp``.  The tests use it to pin the
+oracle restatement (and, through committed fixtures, the CUDA path) to the reference's
+code.  It can only be built where the reference sources are present; ``available()``
+says whether it is.
+
+Conventions as in ``oracle.py``: images C-ordered (Nz, Ny, Nx) complex64, k-space flat
+complex64 arrays of M samples, trajectories float32, grids (Sz, Sy, Sx).
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_ref", "libref.so")
+REF_SRC = os.environ.get("MRG_REFERENCE_SRC", "/root/reference/src")
+_lib = None
+
+
+def build():
+    """Compile oracle/_ref/libref.so from the reference sources (no-op when they are absent)."""
+    if not os.path.isdir(REF_SRC):
+        return False
+    subprocess.run(["make", "-s", "-C", _HERE, "ref", "REF_SRC=" + REF_SRC], check=True)
+    return os.path.exists(LIB_PATH)
+
+
+def available():
+    return os.path.exists(LIB_PATH) or build()
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not available():
+            raise RuntimeError("oracle/_ref/libref.so is not built and the reference sources are not present")
+        L = ctypes.CDLL(LIB_PATH)
+        vp, i, f, l = ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_long
+        ip, fp = ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_float)
+        geo = [i, i, i, f, f, i]
+        L.ref_tables.argtypes = geo + [ip, ip, fp, ip, fp, fp]
+        L.ref_forward.argtypes = geo + [f, vp, vp, fp, fp, fp, fp, l, vp, vp]
+        L.ref_adjoint.argtypes = geo + [f, vp, vp, vp, fp, fp, fp, fp, l]
+        L.ref_grid.argtypes = geo + [f, vp, fp, fp, fp, fp, l, vp]
+        L.ref_ungrid.argtypes = geo + [vp, fp, fp, fp, fp, l, vp, vp]
+        L.ref_fft.argtypes = [i, i, i, f, i, vp]
+        L.ref_wavelet.argtypes = [i, i, i, ip, ip, i, i, vp]
+        L.ref_fraction_threshold.restype = ctypes.c_float
+        L.ref_fraction_threshold.argtypes = [i, i, i, i, ctypes.POINTER(vp), f, i]
+        _lib = L
+    return _lib
+
+
+def _c64(a):
+    return np.ascontiguousarray(a, dtype=np.complex64)
+
+
+def _f32(a):
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    return a, a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+def _p(a):
+    return None if a is None else ctypes.c_void_p(a.ctypes.data)
+
+
+class Gridder:
+    """A reference gridFFT set up by precalc_gridding for an Nx x Ny x Nz 3D non-Cartesian
+    acquisition (a new object per call, as the driver builds one per call)."""
+
+    def __init__(self, N, overgrid=1.5, dwin=-1.0, kernel=1, k_rad=9999.0):
+        self.N = (N, N, N) if np.isscalar(N) else tuple(N)  # (Nx, Ny, Nz)
+        self.geo = (self.N[0], self.N[1], self.N[2], float(overgrid), float(dwin), int(kernel))
+        self.k_rad = float(k_rad)
+        self.S, self.og, self.beta, lut, win = self.tables()
+        self.lut, self.win = lut, win
+
+    @property
+    def ishape(self):
+        return (self.N[2], self.N[1], self.N[0])
+
+    @property
+    def gshape(self):
+        return (self.S[2], self.S[1], self.S[0])
+
+    def tables(self):
+        S, og, ll = (ctypes.c_int * 3)(), (ctypes.c_int * 3)(), ctypes.c_int()
+        be = (ctypes.c_float * 3)()
+        fp = ctypes.POINTER(ctypes.c_float)
+        assert lib().ref_tables(*self.geo, S, og, be, ctypes.byref(ll), None, None) == 0
+        lut = np.zeros(3 * ll.value, np.float32)
+        win = np.zeros(sum(S), np.float32)
+        assert lib().ref_tables(*self.geo, S, og, be, ctypes.byref(ll), lut.ctypes.data_as(fp),
+                                win.ctypes.data_as(fp)) == 0
+        s0, s1 = S[0], S[0] + S[1]
+        return tuple(S), tuple(og), tuple(be), lut.reshape(3, -1), (win[:s0], win[s0:s1], win[s1:])
+
+    def forward(self, X, smap, kx, ky, kz, kw, diff=None):
+        """gridFFT::backward (E), or backward_residual when diff is given."""
+        X, smap = _c64(X), _c64(smap)
+        diff = None if diff is None else _c64(diff)
+        (kx, px), (ky, py), (kz, pz), (kw, pw) = _f32(kx), _f32(ky), _f32(kz), _f32(kw)
+        out = np.zeros(kx.size, np.complex64)
+        assert lib().ref_forward(*self.geo, self.k_rad, _p(X), _p(smap), px, py, pz, pw, kx.size, _p(out),
+                                 _p(diff)) == 0
+        return out
+
+    def adjoint(self, X, smap, data, kx, ky, kz, kw):
+        """gridFFT::forward (E^H): X += ..."""
+        X = _c64(X).copy()
+        smap, data = _c64(smap), _c64(data)
+        (kx, px), (ky, py), (kz, pz), (kw, pw) = _f32(kx), _f32(ky), _f32(kz), _f32(kw)
+        assert lib().ref_adjoint(*self.geo, self.k_rad, _p(X), _p(smap), _p(data), px, py, pz, pw, kx.size) == 0
+        return X
+
+    def grid(self, data, kx, ky, kz, kw):
+        """chop_grid_forward into a zeroed grid."""
+        data = _c64(data)
+        (kx, px), (ky, py), (kz, pz), (kw, pw) = _f32(kx), _f32(ky), _f32(kz), _f32(kw)
+        g = np.zeros(self.gshape, np.complex64)
+        assert lib().ref_grid(*self.geo, self.k_rad, _p(data), px, py, pz, pw, kx.size, _p(g)) == 0
+        return g
+
+    def ungrid(self, grid, kx, ky, kz, kw, diff=None):
+        """chop_grid_backward from a grid."""
+        grid = _c64(grid).reshape(self.gshape)
+        diff = None if diff is None else _c64(diff)
+        (kx, px), (ky, py), (kz, pz), (kw, pw) = _f32(kx), _f32(ky), _f32(kz), _f32(kw)
+        out = np.zeros(kx.size, np.complex64)
+        assert lib().ref_ungrid(*self.geo, _p(grid), px, py, pz, pw, kx.size, _p(out), _p(diff)) == 0
+        return out
+
+    def fft(self, grid, inverse):
+        """do_fft (pruned to the crop) or do_ifft."""
+        g = _c64(grid).reshape(self.gshape).copy()
+        assert lib().ref_fft(self.N[0], self.N[1], self.N[2], self.geo[3], int(bool(inverse)), _p(g)) == 0
+        return g
+
+
+def wavelet(X, levels, shift, wtype=1, inverse=False):
+    """WAVELET3D forward / backward of one (Nz, Ny, Nx) volume with shifts (x, y, z)."""
+    X = _c64(X).copy()
+    Nz, Ny, Nx = X.shape
+    assert lib().ref_wavelet(Nx, Ny, Nz, (ctypes.c_int * 3)(*levels), (ctypes.c_int * 3)(*shift), int(wtype),
+                             int(bool(inverse)), _p(X)) == 0
+    return X
+
+
+def fraction_threshold(vols, fraction, apply=False):
+    """THRESHOLD -threshold_type fraction: (threshold, thresholded volumes or None)."""
+    vols = [_c64(v).copy() for v in vols]
+    Nz, Ny, Nx = vols[0].shape
+    arr = (ctypes.c_void_p * len(vols))(*[v.ctypes.data for v in vols])
+    t = lib().ref_fraction_threshold(Nx, Ny, Nz, len(vols), arr, float(fraction), int(bool(apply)))
+    return float(t), (vols if apply else None)

@@ -1,0 +1,202 @@
+// C entry points over the reference's own gridFFT, WAVELET3D and THRESHOLD classes
+// (src/gridFFT.cpp, src/ArrayTemplates.cpp, src/wavelet3D.cpp, src/threshold.cpp compiled
+// unmodified against the stand-in headers in refshim/), for checking the oracle
+// restatement against the reference itself.  Test infrastructure only: built into
+// oracle/_ref/libref.so by `make -C oracle ref` where the reference sources are present,
+// and loaded only by tests/test_oracle_ref.py.
+//
+// Layouts: images are C-order (Nz, Ny, Nx) complex64, i.e. x fastest, which is the
+// memory order of the reference's column-major Blitz arrays (Nx, Ny, Nz); k-space and
+// trajectories are flat arrays of M samples, an (M, 1, 1) column-major array; the
+// oversampled grid is (Sz, Sy, Sx).
+#include <complex>
+#include <cstring>
+#include <vector>
+
+#include "gridFFT.h"
+#include "threshold.h"
+#include "wavelet3D.h"
+
+using namespace NDarray;
+typedef std::complex<float> cf;
+
+// MRI_DATA's constructor lives in src/mri_data.cpp, which needs HDF5 and Armadillo; the
+// gridding set-up reads only trajectory_type and dft_needed, which the driver sets.
+MRI_DATA::MRI_DATA(void) {}
+
+namespace {
+
+template <typename T>
+Array<T, 3> col3(int n0, int n1, int n2, const void *src) {
+  Array<T, 3> a;
+  a.setStorage(ColumnMajorArray<3>());
+  a.resize(n0, n1, n2);
+  if (src) std::memcpy(a.data(), src, sizeof(T) * (size_t)n0 * n1 * n2);
+  else a = T(0);
+  return a;
+}
+
+struct Config {
+  float overgrid, dwin;
+  int kernel_type;
+  float k_rad;
+};
+
+// gridFFT set up as the reference's callers do: public fields first, then
+// precalc_gridding(Nz, Ny, Nx, data) for a 3D non-Cartesian acquisition.
+void setup(gridFFT &g, const Config &c, int Nx, int Ny, int Nz) {
+  g.overgrid = c.overgrid;
+  g.kernel_type = c.kernel_type;
+  if (c.dwin > 0.0f) g.dwinX = g.dwinY = g.dwinZ = c.dwin;
+  g.k_rad = c.k_rad;
+  MRI_DATA data;
+  for (int d = 0; d < 3; d++) {
+    data.trajectory_type(d) = MRI_DATA::NONCARTESIAN;
+    data.dft_needed(d) = true;
+  }
+  data.Num_Coils = 1;
+  g.precalc_gridding(Nz, Ny, Nx, data);
+}
+
+struct Traj {
+  Array<float, 3> kx, ky, kz, kw;
+  Traj(const float *x, const float *y, const float *z, const float *w, long M)
+      : kx(col3<float>((int)M, 1, 1, x)), ky(col3<float>((int)M, 1, 1, y)), kz(col3<float>((int)M, 1, 1, z)),
+        kw(col3<float>((int)M, 1, 1, w)) {}
+};
+
+}  // namespace
+
+extern "C" {
+
+// precalc_gridding: S, og_s, beta, the kernel tables grid_filterX/Y/Z (lut_len each, lut may
+// be NULL) and the windows winx/winy/winz (Sx + Sy + Sz floats, may be NULL).
+int ref_tables(int Nx, int Ny, int Nz, float overgrid, float dwin, int kernel_type, int *S, int *og, float *beta,
+               int *lut_len, float *lut, float *win) {
+  gridFFT g;
+  setup(g, Config{overgrid, dwin, kernel_type, 9999.0f}, Nx, Ny, Nz);
+  S[0] = g.Sx, S[1] = g.Sy, S[2] = g.Sz;
+  og[0] = g.og_sx, og[1] = g.og_sy, og[2] = g.og_sz;
+  beta[0] = g.betaX, beta[1] = g.betaY, beta[2] = g.betaZ;
+  const Array<float, 1> *f[3] = {&g.grid_filterX, &g.grid_filterY, &g.grid_filterZ};
+  *lut_len = (int)f[0]->numElements();
+  if (lut)
+    for (int d = 0; d < 3; d++) {
+      if (f[d]->numElements() != *lut_len) return 1;
+      for (int i = 0; i < *lut_len; i++) lut[d * *lut_len + i] = (*f[d])(i);
+    }
+  if (win) {
+    int o = 0;
+    for (int i = 0; i < g.Sx; i++) win[o++] = g.winx(i);
+    for (int i = 0; i < g.Sy; i++) win[o++] = g.winy(i);
+    for (int i = 0; i < g.Sz; i++) win[o++] = g.winz(i);
+  }
+  return 0;
+}
+
+// gridFFT::backward (E) or backward_residual (diff != NULL): data = E(X smap) (- diff).
+int ref_forward(int Nx, int Ny, int Nz, float overgrid, float dwin, int kernel_type, float k_rad, const void *X,
+                const void *smap, const float *kx, const float *ky, const float *kz, const float *kw, long M,
+                void *data, const void *diff) {
+  gridFFT g;
+  setup(g, Config{overgrid, dwin, kernel_type, k_rad}, Nx, Ny, Nz);
+  Array<cf, 3> x = col3<cf>(Nx, Ny, Nz, X), s = col3<cf>(Nx, Ny, Nz, smap), d = col3<cf>((int)M, 1, 1, nullptr);
+  Traj t(kx, ky, kz, kw, M);
+  if (diff) {
+    Array<cf, 3> df = col3<cf>((int)M, 1, 1, diff);
+    g.backward_residual(x, s, d, t.kx, t.ky, t.kz, t.kw, df);
+  } else {
+    g.backward(x, s, d, t.kx, t.ky, t.kz, t.kw);
+  }
+  std::memcpy(data, d.data(), sizeof(cf) * (size_t)M);
+  return 0;
+}
+
+// gridFFT::forward (E^H) with a map: X += E^H(data) conj(smap), X read and written.
+int ref_adjoint(int Nx, int Ny, int Nz, float overgrid, float dwin, int kernel_type, float k_rad, void *X,
+                const void *smap, const void *data, const float *kx, const float *ky, const float *kz, const float *kw,
+                long M) {
+  gridFFT g;
+  setup(g, Config{overgrid, dwin, kernel_type, k_rad}, Nx, Ny, Nz);
+  Array<cf, 3> x = col3<cf>(Nx, Ny, Nz, X), s = col3<cf>(Nx, Ny, Nz, smap), d = col3<cf>((int)M, 1, 1, data);
+  Traj t(kx, ky, kz, kw, M);
+  g.forward(x, s, d, t.kx, t.ky, t.kz, t.kw);
+  std::memcpy(X, x.data(), sizeof(cf) * (size_t)Nx * Ny * Nz);
+  return 0;
+}
+
+// chop_grid_forward into a zeroed grid (Sz, Sy, Sx), written to `grid`.
+int ref_grid(int Nx, int Ny, int Nz, float overgrid, float dwin, int kernel_type, float k_rad, const void *data,
+             const float *kx, const float *ky, const float *kz, const float *kw, long M, void *grid) {
+  gridFFT g;
+  setup(g, Config{overgrid, dwin, kernel_type, k_rad}, Nx, Ny, Nz);
+  Array<cf, 3> d = col3<cf>((int)M, 1, 1, data);
+  Traj t(kx, ky, kz, kw, M);
+  g.k3d_grid = cf(0.0f, 0.0f);
+  g.chop_grid_forward(d, t.kx, t.ky, t.kz, t.kw);
+  std::memcpy(grid, g.k3d_grid.data(), sizeof(cf) * (size_t)g.Sx * g.Sy * g.Sz);
+  return 0;
+}
+
+// chop_grid_backward from a caller grid (Sz, Sy, Sx): data = taps * grid (- diff).
+int ref_ungrid(int Nx, int Ny, int Nz, float overgrid, float dwin, int kernel_type, const void *grid, const float *kx,
+               const float *ky, const float *kz, const float *kw, long M, void *data, const void *diff) {
+  gridFFT g;
+  setup(g, Config{overgrid, dwin, kernel_type, 9999.0f}, Nx, Ny, Nz);
+  std::memcpy(g.k3d_grid.data(), grid, sizeof(cf) * (size_t)g.Sx * g.Sy * g.Sz);
+  Array<cf, 3> d = col3<cf>((int)M, 1, 1, nullptr);
+  Array<cf, 3> df = diff ? col3<cf>((int)M, 1, 1, diff) : Array<cf, 3>();
+  Traj t(kx, ky, kz, kw, M);
+  g.chop_grid_backward(d, t.kx, t.ky, t.kz, t.kw, df, diff != nullptr);
+  std::memcpy(data, d.data(), sizeof(cf) * (size_t)M);
+  return 0;
+}
+
+// do_fft (pruned: the input is read inside the crop only) or do_ifft on a caller grid.
+int ref_fft(int Nx, int Ny, int Nz, float overgrid, int inverse, void *grid) {
+  gridFFT g;
+  setup(g, Config{overgrid, -1.0f, KAISER_KERNEL, 9999.0f}, Nx, Ny, Nz);
+  const size_t n = (size_t)g.Sx * g.Sy * g.Sz;
+  std::memcpy(g.k3d_grid.data(), grid, sizeof(cf) * n);
+  if (inverse) g.do_ifft();
+  else g.do_fft();
+  std::memcpy(grid, g.k3d_grid.data(), sizeof(cf) * n);
+  return 0;
+}
+
+// WAVELET3D forward (inverse = 0) or backward of one volume in place, with the shifts S set
+// as random_shift would have set them.
+int ref_wavelet(int Nx, int Ny, int Nz, const int *levels, const int *shift, int wave_type, int inverse, void *X) {
+  Array<cf, 3> x = col3<cf>(Nx, Ny, Nz, X);
+  int l[3] = {levels[0], levels[1], levels[2]};
+  WAVELET3D w(x, l, wave_type);
+  for (int d = 0; d < 3; d++) w.S[d] = shift[d];
+  if (inverse) w.backward(x);
+  else w.forward(x);
+  std::memcpy(X, x.data(), sizeof(cf) * (size_t)Nx * Ny * Nz);
+  return 0;
+}
+
+// THRESHOLD with -threshold_type fraction -thresh <fraction>: update_threshold over nvol
+// volumes (frames) gives global_threshold; with apply != 0 exec_threshold then soft
+// thresholds the volumes in place.  Returns the threshold.
+float ref_fraction_threshold(int Nx, int Ny, int Nz, int nvol, void **vols, float fraction, int apply) {
+  char val[64];
+  std::snprintf(val, sizeof(val), "%.9g", fraction);
+  const char *args[] = {"-threshold_type", "fraction", "-thresh", val};
+  THRESHOLD th(4, args);
+  th.VERBOSE = false;
+  Array<Array<cf, 3>, 2> coef;
+  coef.setStorage(ColumnMajorArray<2>());
+  coef.resize(nvol, 1);
+  for (int t = 0; t < nvol; t++) coef(t, 0).reference(col3<cf>(Nx, Ny, Nz, vols[t]));
+  WAVELET3D wave;
+  th.update_threshold(coef, wave, 1.0f);
+  if (apply) {
+    th.exec_threshold(coef, wave);
+    for (int t = 0; t < nvol; t++) std::memcpy(vols[t], coef(t, 0).data(), sizeof(cf) * (size_t)Nx * Ny * Nz);
+  }
+  return th.global_threshold;
+}
+
+}  // extern "C"

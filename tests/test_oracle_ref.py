@@ -1,0 +1,162 @@
+"""The oracle restatement (and the library's host-side tables) against the reference's own
+code: src/gridFFT.cpp, src/ArrayTemplates.cpp, src/wavelet3D.cpp and src/threshold.cpp
+compiled unmodified into oracle/_ref/libref.so (``make -C oracle ref``, stand-in headers
+for Blitz++ / FFTW / Armadillo / HDF5 in oracle/refshim).
+
+Tolerances: tables bit for bit; operators and stages at relative L2 <= 1e-6 (both sides
+FP32; the reference adds its gridding with unordered OpenMP atomics and its stand-in FFT
+rounds a double-precision transform, so the last bits differ); wavelets and thresholds
+at 1e-6.  These tests need the reference sources and are skipped where they are absent
+(the GPU host).
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from tests.helpers import case, edge_trajectory, rel
+
+R = pytest.importorskip("oracle.ref")
+if not R.available():
+    pytest.skip("reference sources not present: oracle/_ref cannot be built here", allow_module_level=True)
+
+TOL = 1e-6
+
+
+@pytest.fixture(scope="module")
+def O():
+    from oracle import oracle
+    oracle.build()
+    return oracle
+
+
+@pytest.mark.parametrize("kernel", [1, 0, 2, 3])
+@pytest.mark.parametrize("N,overgrid", [(32, 1.5), (64, 1.5), (96, 1.5), ((40, 48, 24), 1.5), (64, 1.375),
+                                        (32, 2.0)])
+def test_tables_equal_reference(O, mrg_lib, kernel, N, overgrid):
+    """precalc_gridding / precalc_kernel: S, crop, beta, kernel tables and deapodisation
+    windows, bit for bit, from the oracle and from the library's host code."""
+    g = R.Gridder(N, overgrid=overgrid, kernel=kernel)
+    o = O.Plan(N, overgrid=overgrid, kernel=kernel)
+    lut, win = o.tables()
+    assert g.S == o.S and g.og == o.og
+    assert g.beta == o.beta
+    assert np.array_equal(g.lut, lut)
+    for a, b in zip(g.win, win):
+        assert np.array_equal(a, b)
+    # the library's tables (mrg_plan_geometry, no GPU needed)
+    from mri_recon_gb300._lib import MrgConfig, _fp
+    L = mrg_lib.load()
+    cfg = MrgConfig()
+    L.mrg_config_default(ctypes.byref(cfg))
+    cfg.kernel_type, cfg.overgrid = kernel, overgrid
+    Nx, Ny, Nz = (N, N, N) if np.isscalar(N) else N
+    S, og, gr, be, ll = (ctypes.c_int * 3)(), (ctypes.c_int * 3)(), (ctypes.c_float * 3)(), (ctypes.c_float * 3)(), \
+        ctypes.c_int()
+    assert L.mrg_plan_geometry(ctypes.byref(cfg), Nx, Ny, Nz, S, og, gr, be, ctypes.byref(ll), None, None) == 0
+    mlut = np.zeros(3 * ll.value, np.float32)
+    mwin = np.zeros(sum(S), np.float32)
+    assert L.mrg_plan_geometry(ctypes.byref(cfg), Nx, Ny, Nz, S, og, gr, be, ctypes.byref(ll),
+                               mlut.ctypes.data_as(_fp), mwin.ctypes.data_as(_fp)) == 0
+    assert tuple(S) == g.S and tuple(og) == g.og and tuple(be) == g.beta
+    assert np.array_equal(mlut.reshape(3, -1), g.lut)
+    assert np.array_equal(mwin, np.concatenate(g.win))
+
+
+def _traj(N, nproj, seed=3):
+    c = case(N=N, C=1, nproj=nproj, seed=seed)
+    return c, (c["kx"], c["ky"], c["kz"], c["kw"])
+
+
+def test_gridding_and_ungridding_match_reference(O):
+    """chop_grid_forward and chop_grid_backward on the 64^3 SENSE-CG geometry (4096 x 64
+    radial), and on samples at the grid edge, outside it, at kw == 0 and at half-integer
+    positions."""
+    c, a = _traj(64, 4096)
+    g, o = R.Gridder(64), O.Plan(64)
+    d = c["data"][0]
+    assert rel(o.grid(d, *a), g.grid(d, *a)) < TOL
+    rng = np.random.default_rng(4)
+    grid = (rng.standard_normal(g.gshape) + 1j * rng.standard_normal(g.gshape)).astype(np.complex64)
+    assert rel(o.ungrid(grid, *a), g.ungrid(grid, *a)) < TOL
+    assert rel(o.ungrid(grid, *a, diff=d), g.ungrid(grid, *a, diff=d)) < TOL
+    e = edge_trajectory(32)
+    g32, o32 = R.Gridder(32), O.Plan(32)
+    de = (rng.standard_normal(e[0].size) + 1j * rng.standard_normal(e[0].size)).astype(np.complex64)
+    assert rel(o32.grid(de, *e), g32.grid(de, *e)) < TOL
+    grid32 = (rng.standard_normal(g32.gshape) + 1j * rng.standard_normal(g32.gshape)).astype(np.complex64)
+    ue, ur = o32.ungrid(grid32, *e), g32.ungrid(grid32, *e)
+    assert rel(ue, ur) < TOL
+    assert np.array_equal(ue == 0, ur == 0)  # the same samples are dropped
+
+
+@pytest.mark.parametrize("N", [32, (40, 24, 56)])
+def test_fft_passes_match_reference(O, N):
+    """do_fft (pruned: only the crop is read) and do_ifft."""
+    g, o = R.Gridder(N), O.Plan(N)
+    rng = np.random.default_rng(6)
+    grid = (rng.standard_normal(g.gshape) + 1j * rng.standard_normal(g.gshape)).astype(np.complex64)
+    assert rel(o.fft3(grid, +1), g.fft(grid, inverse=True)) < TOL
+    # the forward transform of a grid holding an image in its crop, as set_image leaves it
+    img = np.zeros(g.gshape, np.complex64)
+    Nx, Ny, Nz = g.N
+    sx, sy, sz = g.og
+    img[sz:sz + Nz, sy:sy + Ny, sx:sx + Nx] = grid[sz:sz + Nz, sy:sy + Ny, sx:sx + Nx]
+    assert rel(o.fft3(img, -1), g.fft(img, inverse=False)) < TOL
+
+
+@pytest.mark.parametrize("kernel", [1, 0, 2, 3])
+def test_operators_match_reference(O, kernel):
+    """gridFFT::backward (E), backward_residual and forward (E^H) with a coil map."""
+    N = 64 if kernel == 1 else 32
+    c, a = _traj(N, 4096 if N == 64 else 800, seed=9)
+    g, o = R.Gridder(N, kernel=kernel), O.Plan(N, kernel=kernel)
+    sm = c["smaps"][0]
+    assert rel(o.forward(c["img"], sm, *a), g.forward(c["img"], sm, *a)) < TOL
+    d = c["data"][0]
+    assert rel(o.forward(c["img"], sm, *a, diff=d), g.forward(c["img"], sm, *a, diff=d)) < TOL
+    X0 = c["X"] * np.complex64(0.1)
+    assert rel(o.adjoint(X0.copy(), sm, d, *a), g.adjoint(X0, sm, d, *a)) < TOL
+
+
+def test_taper_radius_matches_reference(O):
+    """E^H with the Gaussian taper of a small k_rad (the coil-map estimate's smap_res)."""
+    c, a = _traj(32, 800, seed=10)
+    g, o = R.Gridder(32, k_rad=8.0), O.Plan(32, k_rad=8.0)
+    X0 = np.zeros(g.ishape, np.complex64)
+    assert rel(o.adjoint(X0.copy(), c["smaps"][0], c["data"][0], *a), g.adjoint(X0, c["smaps"][0], c["data"][0], *a)) < TOL
+
+
+def test_fp64_oracle_against_reference(O):
+    """The FP64 twin is as close to the FP32 reference as FP32 rounding allows."""
+    c, a = _traj(64, 4096, seed=11)
+    g, o64 = R.Gridder(64), O.Plan(64, prec=1)
+    X0 = np.zeros(g.ishape, np.complex64)
+    d = c["data"][0]
+    assert rel(o64.adjoint(X0.astype(np.complex128), c["smaps"][0], d, *a), g.adjoint(X0, c["smaps"][0], d, *a)) < 1e-5
+
+
+@pytest.mark.parametrize("wtype", [1, 0])
+@pytest.mark.parametrize("shape,levels,shift", [((32, 32, 32), (3, 3, 3), (0, 0, 0)), ((32, 32, 32), (3, 3, 3), (1, 2, 3)),
+                                                ((16, 40, 48), (4, 4, 4), (3, 0, 2)), ((24, 24, 24), (2, 3, 4), (1, 1, 0))])
+def test_wavelet_matches_reference(O, wtype, shape, levels, shift):
+    """WAVELET3D forward3D / backward3D with the shifts random_shift would set."""
+    rng = np.random.default_rng(12)
+    X = (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)).astype(np.complex64)
+    f = R.wavelet(X, levels, shift, wtype)
+    assert rel(O.wavelet(X, levels, shift, wtype), f) < TOL
+    assert rel(O.wavelet(f, levels, shift, wtype, inverse=True), R.wavelet(f, levels, shift, wtype, inverse=True)) < TOL
+
+
+@pytest.mark.parametrize("fraction", [0.1, 0.5, 0.9])
+def test_fraction_threshold_matches_reference(O, fraction):
+    """THRESHOLD::get_threshold (bisection, its thresh * max starting bound) and the
+    grouped-complex soft threshold over several frames."""
+    rng = np.random.default_rng(13)
+    vols = [(rng.standard_normal((24, 24, 24)) + 1j * rng.standard_normal((24, 24, 24))).astype(np.complex64)
+            for _ in range(3)]
+    t_ref, out_ref = R.fraction_threshold(vols, fraction, apply=True)
+    t = O.fraction_threshold(vols, fraction)
+    assert abs(t - t_ref) <= 1e-6 * t_ref
+    for v, r in zip(vols, out_ref):
+        assert rel(O.soft_threshold(v, t), r) < TOL
