@@ -17,6 +17,7 @@
 // A(count, t) inside the coil loop, count restarting per coil), so the last coil's block
 // is what remains and sigma_1 = max over frames of its block norm; that is what is
 // computed here, then the median of the non-zero sigma_1 times (1 + amp exp(-iter/t2)).
+#include "jacobi.cuh"
 #include "mrg_internal.h"
 
 namespace mrg {
@@ -184,84 +185,11 @@ __global__ void __launch_bounds__(256) k_llr_coil(const CoilLlrArgs a) {
     // rounds over the coil columns; warp w rotates pairs w, w + 8, ... of a round.  Measured
     // against the FP64 oracle: <= 2e-6 per threshold application up to 16 coils, 1.4e-5 at
     // 32 coils, so wider blocks take the FP64 Gram path below.
-    float2 *Vf = reinterpret_cast<float2 *>(G);  // V[c][j] at c * 33 + j
+    float2 *Vf = reinterpret_cast<float2 *>(G);  // V[c][j] at c * JAC_LDV + j
     float *sg = reinterpret_cast<float *>(lam);  // column norms, then threshold factors
     __shared__ unsigned s_off;
     __shared__ float s_fl;
-    const int Ce = C + (C & 1), half = Ce / 2;
-    for (int e = threadIdx.x; e < C * 33; e += blockDim.x) Vf[e] = make_float2((e / 33) == (e % 33) ? 1.f : 0.f, 0.f);
-    if (warp == 0) {  // floor of the pair test: (1e-6 x the largest column norm)^2
-      float mx = 0.f;
-      for (int j = 0; j < C; j++) {
-        float sq = 0.f;
-        for (int r = lane; r < R; r += 32) {
-          const float2 x = As[r * C + j];
-          sq += x.x * x.x + x.y * x.y;
-        }
-        for (int o = 16; o > 0; o >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
-        mx = fmaxf(mx, sq);
-      }
-      if (lane == 0) s_fl = 1e-12f * mx;
-    }
-    __syncthreads();
-    const float fl = s_fl;
-    for (int sweep = 0; sweep < 40; sweep++) {
-      if (threadIdx.x == 0) s_off = 0u;
-      __syncthreads();
-      for (int rnd = 0; rnd < Ce - 1; rnd++) {
-        for (int pp = warp; pp < half; pp += nwarp) {
-          const int jp = pp == 0 ? 0 : 1 + (pp - 1 + rnd) % (Ce - 1);
-          const int jq = 1 + (Ce - 2 - pp + rnd) % (Ce - 1);  // position Ce - 1 - pp >= 1
-          if (jp >= C || jq >= C) continue;                    // the padding column of an odd C
-          float al = 0.f, be = 0.f, gr = 0.f, gi = 0.f;
-          for (int r = lane; r < R; r += 32) {
-            const float2 x = As[r * C + jp], y = As[r * C + jq];
-            al += x.x * x.x + x.y * x.y;
-            be += y.x * y.x + y.y * y.y;
-            gr += x.x * y.x + x.y * y.y;  // conj(x) y
-            gi += x.x * y.y - x.y * y.x;
-          }
-          for (int o = 16; o > 0; o >>= 1) {
-            al += __shfl_xor_sync(0xffffffffu, al, o);
-            be += __shfl_xor_sync(0xffffffffu, be, o);
-            gr += __shfl_xor_sync(0xffffffffu, gr, o);
-            gi += __shfl_xor_sync(0xffffffffu, gi, o);
-          }
-          const float ag = sqrtf(gr * gr + gi * gi);
-          if (!(al > 0.f && be > 0.f && ag > 0.f)) continue;
-          const float rel = ag / sqrtf(fmaxf(al, fl) * fmaxf(be, fl));
-          if (lane == 0) atomicMax(&s_off, __float_as_uint(rel));
-          if (rel < 4e-7f) continue;
-          const float zeta = (be - al) / (2.f * ag);
-          const float t = (zeta >= 0.f ? 1.f : -1.f) / (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
-          const float cs = 1.f / sqrtf(1.f + t * t), sn = cs * t;
-          const float phx = gr / ag, phy = gi / ag;
-          auto rot = [&](float2 *px, float2 *py) {  // x' = cs x - sn y', y' = (sn x + cs y') ph, y' = y conj(ph)
-            const float2 x = *px, y0 = *py;
-            const float2 y = make_float2(y0.x * phx + y0.y * phy, y0.y * phx - y0.x * phy);
-            *px = make_float2(cs * x.x - sn * y.x, cs * x.y - sn * y.y);
-            const float2 u = make_float2(sn * x.x + cs * y.x, sn * x.y + cs * y.y);
-            *py = make_float2(u.x * phx - u.y * phy, u.x * phy + u.y * phx);
-          };
-          for (int r = lane; r < R; r += 32) rot(As + r * C + jp, As + r * C + jq);
-          if (lane < C) rot(Vf + lane * 33 + jp, Vf + lane * 33 + jq);
-        }
-        __syncthreads();
-      }
-      const float off = __uint_as_float(s_off);
-      __syncthreads();
-      if (off < 4e-7f) break;
-    }
-    for (int j = warp; j < C; j += nwarp) {  // s_j = |column j of A W|
-      float sq = 0.f;
-      for (int r = lane; r < R; r += 32) {
-        const float2 x = As[r * C + j];
-        sq += x.x * x.x + x.y * x.y;
-      }
-      for (int o = 16; o > 0; o >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
-      if (lane == 0) sg[j] = sqrtf(sq);
-    }
-    __syncthreads();
+    jacobi_onesided_f32(As, R, C, C, Vf, sg, &s_off, &s_fl);
     if (a.mode == 2) {
       // combine: A v1 = column jmax of A W, times the phase that makes v1's largest
       // component real and positive
@@ -273,11 +201,11 @@ __global__ void __launch_bounds__(256) k_llr_coil(const CoilLlrArgs a) {
         int m = 0;
         float mm = -1.f;
         for (int q = 0; q < C; q++) {
-          const float2 x = Vf[q * 33 + j];
+          const float2 x = Vf[q * JAC_LDV + j];
           const float n2 = x.x * x.x + x.y * x.y;
           if (n2 > mm) mm = n2, m = q;
         }
-        const float2 x = Vf[m * 33 + j];
+        const float2 x = Vf[m * JAC_LDV + j];
         const float n = sqrtf(mm);
         ph = (n > 0.f) ? make_double2(x.x / n, -x.y / n) : make_double2(1.0, 0.0);
       }
@@ -301,7 +229,7 @@ __global__ void __launch_bounds__(256) k_llr_coil(const CoilLlrArgs a) {
       float2 acc = make_float2(0.f, 0.f);
       if (lane < C)
         for (int j = 0; j < C; j++) {
-          const float2 x = As[r * C + j], v = Vf[lane * 33 + j];
+          const float2 x = As[r * C + j], v = Vf[lane * JAC_LDV + j];
           const float f = sg[j];
           acc.x += f * (x.x * v.x + x.y * v.y);  // x f conj(v)
           acc.y += f * (x.y * v.x - x.x * v.y);
@@ -414,25 +342,29 @@ mrg_status coil_llr_launch(CoilLlrArgs &a, int T, int C, const int N[3], const i
   a.T = T;
   a.C = C;
   a.nvox = (int64_t)N[0] * N[1] * N[2];
-  int nblocks = 1;
+  int64_t nblocks = 1;
   for (int d = 0; d < 3; d++) {
     a.N[d] = N[d];
     a.bs[d] = std::min(bs[d], N[d]);  // src/clear.cpp:109-112
     a.nb[d] = N[d] / a.bs[d];
     nblocks *= a.nb[d];
   }
-  static bool attr = false;
-  if (!attr) {
+  if (nblocks > INT32_MAX) {
+    set_error("too many coil low-rank blocks for one launch");
+    return MRG_ERR_UNSUPPORTED;
+  }
+  static DeviceOnce once;
+  MRG_TRY(device_once(once, []() -> mrg_status {
     MRG_CUDA(cudaFuncSetAttribute(k_llr_coil<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CL_SMEM_MAX));
     MRG_CUDA(cudaFuncSetAttribute(k_llr_coil<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CL_SMEM_MAX));
-    attr = true;
-  }
+    return MRG_OK;
+  }));
   const bool sa = coil_llr_smem(T, C, a.bs, true) <= CL_SMEM_MAX;
   const size_t smem = coil_llr_smem(T, C, a.bs, sa);
   if (sa)
-    k_llr_coil<true><<<nblocks, 256, smem, st>>>(a);
+    k_llr_coil<true><<<(unsigned)nblocks, 256, smem, st>>>(a);
   else
-    k_llr_coil<false><<<nblocks, 256, smem, st>>>(a);
+    k_llr_coil<false><<<(unsigned)nblocks, 256, smem, st>>>(a);
   MRG_LAUNCHED();
   return MRG_OK;
 }
@@ -507,8 +439,8 @@ mrg_status clear_step(float2 *X, const float2 *R, int64_t n, const double *acc, 
   return MRG_OK;
 }
 
-int coil_llr_blocks(const int N[3], const int bs[3]) {
-  int nb = 1;
+int64_t coil_llr_blocks(const int N[3], const int bs[3]) {
+  int64_t nb = 1;
   for (int d = 0; d < 3; d++) nb *= N[d] / std::min(bs[d], N[d]);
   return nb;
 }
@@ -521,7 +453,7 @@ mrg_status coil_llr_update(const float2 *X, int T, int C, const int N[3], const 
   a.mode = 0;
   a.sig = sig;
   MRG_TRY(coil_llr_launch(a, T, C, N, bs, st));
-  return llr_median(sig, coil_llr_blocks(N, bs), work, amp, t2, iter, smax, st);
+  return llr_median(sig, (int)coil_llr_blocks(N, bs), work, amp, t2, iter, smax, st);
 }
 
 mrg_status coil_llr_thresh(float2 *X, int T, int C, const int N[3], const int bs[3], float alpha, int block_iter,
