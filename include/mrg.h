@@ -39,7 +39,7 @@ typedef enum mrg_status {
   MRG_ERR_CUDA = 2,        /* CUDA runtime error (message in mrg_last_error) */
   MRG_ERR_NOMEM = 3,       /* device allocation failed */
   MRG_ERR_STATE = 4,       /* call out of order (e.g. no trajectory set) */
-  MRG_ERR_TIMEOUT = 5,     /* reserved: a bounded device-side wait ran out */
+  MRG_ERR_TIMEOUT = 5,     /* a bounded device-side wait ran out (see mrg_set_wait_limit) */
   MRG_ERR_UNSUPPORTED = 6  /* grid size or option this build does not implement */
 } mrg_status;
 
@@ -156,6 +156,19 @@ mrg_status mrg_forward_coil(mrg_plan *plan, int frame, const void *X, const void
  * passes pruned to the image crop; this entry exposes them for cross-checks. */
 mrg_status mrg_fft3(mrg_plan *plan, void *grid, int sign, void *stream);
 
+/* gridFFT::chop_grid_forward / chop_grid_backward (src/gridFFT.cpp:1009-1164, :1166-1322;
+ * src/gridFFT.h:177-186) on a caller grid, all coils of a frame, as RECON::kspace_residual
+ * calls them on the public k3d_grid (src/recon_lib.cpp:2218-2252).  The grid is
+ * Sz x Sy x Sx x ncoil complex64, coil innermost (for one coil the reference's
+ * column-major k3d_grid), host or device; the chop sign (-1)^l of every tap is part of the
+ * weights, as in the reference.
+ *   mrg_grid:   grid = scatter of data_c * kw * taper (the whole grid is written: the
+ *               reference's caller zeroes k3d_grid first, then chop_grid_forward adds);
+ *   mrg_ungrid: data_c = sum over the taps of grid_c, or that minus diff_c (diff may be NULL). */
+mrg_status mrg_grid(mrg_plan *plan, int frame, const void *data, int64_t coil_stride, void *grid, void *stream);
+mrg_status mrg_ungrid(mrg_plan *plan, int frame, const void *grid, void *data, int64_t coil_stride, const void *diff,
+                      void *stream);
+
 /* The public gridFFT::k_rad field (src/gridFFT.h:102; default 9999): the radius of the
  * Gaussian taper exp(-|k|^2 / (2 k_rad^2)) E^H applies to each sample
  * (src/gridFFT.cpp:1096-1108).  The coil-map estimate sets it to the map resolution and
@@ -214,7 +227,8 @@ mrg_status mrg_espirit_smaps(mrg_plan *plan, int frame, const void *data, int64_
 mrg_status mrg_cg(mrg_plan *plan, int max_iter, void *X, double *resid, int use_graph, void *stream);
 
 /* Differentiable E (no counterpart in the reference; its operator is gridFFT::backward,
- * src/gridFFT.cpp:824-844, with unit density weights): for one frame
+ * src/gridFFT.cpp:824-844, with unit density weights), Kaiser-Bessel plans only (other
+ * kernels return MRG_ERR_UNSUPPORTED): for one frame
  *   loss   = sum_c || E_c(x, k) - y_c ||^2                     (host double, may be NULL)
  *   grad_x = 2 sum_c E_c^* (E_c x - y_c)  complex64 image       (the exact adjoint, no kw or taper)
  *   grad_k = dloss/dk as float32 [3][M] (kx, ky, kz rows) in the reference's k units,
@@ -253,12 +267,17 @@ typedef struct mrg_fista_params {
   float clear_t2;        /* -clear_t2 (default 6) */
   int64_t rand_skip;     /* rand() draws consumed before the first shift; -1: the
                             2*N^3*nframes draws of the max-eigen seeding */
+  float early_stop_thresh; /* -early_stop_thresh (default 0: never stop early) */
+  int early_stop_range;    /* -early_stop_range (default 5) */
 } mrg_fista_params;
 
 void mrg_fista_params_default(mrg_fista_params *p);
 
 /* X (nframes images, overwritten), resid (host, may be NULL): sum|E^H W(Ex-d)|^2 per
- * iteration, step (host, may be NULL): the 1/max-eigenvalue step size. */
+ * iteration run, step (host, may be NULL): the 1/max-eigenvalue step size.  With
+ * early_stop_thresh > 0 the loop ends once the standard deviation of the last
+ * early_stop_range ratios sum|R|^2 / (iteration 0's sum|R|^2) is below it
+ * (src/recon_lib.cpp:2081-2087, :2154-2163); mrg_last_iterations gives the count run. */
 mrg_status mrg_fista(mrg_plan *plan, const mrg_fista_params *params, void *X, double *resid, float *step,
                      int use_graph, void *stream);
 
@@ -380,6 +399,29 @@ mrg_status mrg_dcf_pipe(const float *kx, const float *ky, const float *kz, int64
  * to query sizes first. */
 mrg_status mrg_plan_geometry(const mrg_config *cfg, int Nx, int Ny, int Nz, int S[3], int og[3], float grid[3],
                              float beta[3], int *lut_len, float *lut, float *win);
+/* Gating (host-only, no GPU needed).  Samples are flat in the reference's (readout,
+ * projection, slice) order, readout fastest: sample s belongs to readout r = s / nread.
+ * gate_times (nreadouts doubles) is GATING::gate_times of one encode (the frame index of
+ * each readout as a real number; computing it from ECG / respiratory / time signals is the
+ * gating subsystem's job and not done here); rweight (nreadouts floats, may be NULL) the
+ * respiratory weight GATING::weight_data multiplies in first (src/gating.cpp:1080-1094).
+ * The frame weight of readout r is Tw = rweight[r] * (floor(gate_times[r]) == frame),
+ * GATING::hist_weight (src/gating.cpp:1130-1139).
+ *   mrg_gate_weights: kw_out[s] = kw[s] * Tw(r) -- the time weight the loops apply when the
+ *     data are not pregated (src/recon_lib.cpp:1543-1557); kw_out may alias kw.
+ *   mrg_pregate: RECON::pregate_data (src/recon_lib.cpp:675-776) for one frame: the samples
+ *     with Tw > 0, in order, into kx/ky/kz/kw_out, kw scaled by 1e6 / count (in the
+ *     reference's float / double mix), or 1 with reset_dens, and the ncoil data arrays
+ *     (coil c at data + c*coil_stride into data_out + c*out_stride, complex64; both may be
+ *     NULL).  *count receives the frame's sample count; with every output NULL only the
+ *     count is computed, to size the outputs. */
+mrg_status mrg_gate_weights(const double *gate_times, const float *rweight, int64_t nreadouts, int nread, int frame,
+                            const float *kw, float *kw_out);
+mrg_status mrg_pregate(const double *gate_times, const float *rweight, int64_t nreadouts, int nread, int frame,
+                       int reset_dens, const float *kx, const float *ky, const float *kz, const float *kw,
+                       const void *data, int ncoil, int64_t coil_stride, float *kx_out, float *ky_out, float *kz_out,
+                       float *kw_out, void *data_out, int64_t out_stride, int64_t *count);
+
 /* Host-only: n values of the glibc rand() stream for the default seed after `skip`
  * draws, the source of the reference's wavelet and block shifts
  * (src/wavelet3D.cpp:443-448, src/clear.cpp:408-410). */
@@ -398,6 +440,23 @@ mrg_status mrg_last_timings(mrg_plan *plan, float out[8], int *calls);
 
 /* Number of kernels this library launched since load (process-wide counter). */
 int64_t mrg_kernel_launches(void);
+
+/* Bounded device-side waits (no counterpart in the reference, whose loops run on the
+ * host).  The tensor-core gridding kernel synchronises its warps through shared-memory
+ * barriers; every such wait gives up after `seconds` of GPU time (default 2), records
+ * the failure in the plan and returns, leaving the context usable.  A call that waits for
+ * the GPU before it returns (host buffers, mrg_cg, mrg_fista, mrg_clear, mrg_grad,
+ * mrg_cg_residuals) then returns MRG_ERR_TIMEOUT; calls that return without waiting
+ * (device buffers, mrg_cg_iterate) leave it to the next waiting call or to
+ * mrg_plan_check.  The record is cleared when it is reported.  0 makes a wait give up
+ * after its first unsuccessful try (for tests). */
+mrg_status mrg_set_wait_limit(mrg_plan *plan, double seconds);
+/* Waits for `stream` and reports (MRG_ERR_TIMEOUT) and clears a wait that ran out in this
+ * plan's kernels since the last report. */
+mrg_status mrg_plan_check(mrg_plan *plan, void *stream);
+/* Iterations the last mrg_cg / mrg_fista / mrg_clear on this plan ran (fewer than max_iter
+ * after an early stop). */
+mrg_status mrg_last_iterations(const mrg_plan *plan, int *iters);
 
 #ifdef __cplusplus
 }

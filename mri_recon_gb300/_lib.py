@@ -40,7 +40,8 @@ class MrgFistaParams(ctypes.Structure):
                 ("cycle_spins", ctypes.c_int), ("wave_levels", ctypes.c_int * 3), ("wave_type", ctypes.c_int),
                 ("thresh", ctypes.c_float), ("use_threshold", ctypes.c_int), ("llr_block", ctypes.c_int * 3),
                 ("llr_block_iter", ctypes.c_int), ("llr_alpha", ctypes.c_float), ("clear_amp", ctypes.c_float),
-                ("clear_t2", ctypes.c_float), ("rand_skip", ctypes.c_int64)]
+                ("clear_t2", ctypes.c_float), ("rand_skip", ctypes.c_int64), ("early_stop_thresh", ctypes.c_float),
+                ("early_stop_range", ctypes.c_int)]
 
 
 class MrgClearParams(ctypes.Structure):
@@ -109,6 +110,14 @@ SIGNATURES = {
     "mrg_set_timing": (_i, [_vp, _i]),
     "mrg_last_timings": (_i, [_vp, _fp, _ip]),
     "mrg_kernel_launches": (_i64, []),
+    "mrg_gate_weights": (_i, [_vp, _vp, _i64, _i, _i, _vp, _vp]),
+    "mrg_pregate": (_i, [_vp, _vp, _i64, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _i, _i64, _vp, _vp, _vp, _vp, _vp,
+                         _i64, ctypes.POINTER(_i64)]),
+    "mrg_grid": (_i, [_vp, _i, _vp, _i64, _vp, _vp]),
+    "mrg_ungrid": (_i, [_vp, _i, _vp, _vp, _i64, _vp, _vp]),
+    "mrg_set_wait_limit": (_i, [_vp, ctypes.c_double]),
+    "mrg_plan_check": (_i, [_vp, _vp]),
+    "mrg_last_iterations": (_i, [_vp, _ip]),
 }
 
 _lib = None

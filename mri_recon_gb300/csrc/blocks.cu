@@ -115,7 +115,8 @@ mrg_status mrg_soft_threshold(void *X, int64_t n, float value, void *stream) {
 
 mrg_status mrg_llr_update_threshold(const void *X, int nframes, int Nx, int Ny, int Nz, const int block[3],
                                     float clear_amp, float clear_t2, int iteration, float *smax, void *stream) {
-  if (!X || !block || !smax || nframes <= 0 || Nx <= 0 || Ny <= 0 || Nz <= 0) {
+  if (!X || !block || !smax || nframes <= 0 || Nx <= 0 || Ny <= 0 || Nz <= 0 || block[0] < 1 || block[1] < 1 ||
+      block[2] < 1) {
     set_error("bad argument");
     return MRG_ERR_INVALID;
   }
@@ -135,7 +136,8 @@ mrg_status mrg_llr_update_threshold(const void *X, int nframes, int Nx, int Ny, 
 
 mrg_status mrg_llr_thresh(void *X, int nframes, int Nx, int Ny, int Nz, const int block[3], int block_iter, float alpha,
                           float smax, int64_t rand_skip, void *stream) {
-  if (!X || !block || nframes <= 0 || Nx <= 0 || Ny <= 0 || Nz <= 0 || block_iter <= 0 || rand_skip < 0) {
+  if (!X || !block || nframes <= 0 || Nx <= 0 || Ny <= 0 || Nz <= 0 || block_iter <= 0 || rand_skip < 0 ||
+      block[0] < 1 || block[1] < 1 || block[2] < 1) {
     set_error("bad argument");
     return MRG_ERR_INVALID;
   }
@@ -183,7 +185,12 @@ mrg_status mrg_clear_update_threshold(const void *X, int nframes, int ncoil, int
   }
   cudaStream_t st = (cudaStream_t)stream;
   const int N[3] = {Nx, Ny, Nz};
-  const int nb = coil_llr_blocks(N, block);
+  const int64_t nb64 = coil_llr_blocks(N, block);
+  if (nb64 > (int64_t)(1 << 30)) {
+    set_error("too many coil low-rank blocks (" + std::to_string(nb64) + ")");
+    return MRG_ERR_UNSUPPORTED;
+  }
+  const int nb = (int)nb64;
   int np2 = 1;
   while (np2 < nb) np2 <<= 1;
   const size_t bytes = sizeof(float2) * (size_t)nframes * Nx * Ny * Nz * ncoil;

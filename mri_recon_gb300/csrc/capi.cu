@@ -23,6 +23,26 @@ namespace mrg {
 static thread_local std::string g_err;
 void set_error(const std::string &msg) { g_err = msg; }
 std::atomic<int64_t> g_launches{0};
+
+int device_sms() {
+  static std::mutex mu;
+  static int sms[64] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+    cudaGetLastError();
+    return 152;
+  }
+  std::lock_guard<std::mutex> lock(mu);
+  if (!sms[dev]) {
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1) {
+      cudaGetLastError();
+      n = 152;
+    }
+    sms[dev] = n;
+  }
+  return sms[dev];
+}
 }  // namespace mrg
 
 using namespace mrg;
@@ -69,6 +89,10 @@ struct mrg_plan {
   LlrWork llr;
   int *d_wshift = nullptr, *d_lshift = nullptr;
   float *d_thr = nullptr;
+  // bounded device-side waits: limit of one wait and the error word the kernels set
+  long long wait_ns = MRG_DEFAULT_WAIT_NS;
+  int *d_err = nullptr;
+  int last_iters = 0;  // iterations the last mrg_cg / mrg_fista / mrg_clear ran
 };
 
 // ---------------------------------------------------------------------------
@@ -99,7 +123,44 @@ static GridConst grid_const(const mrg_plan *p) {
     g.beta[d] = p->geo.beta[d];
     g.kb_norm[d] = p->geo.kb_norm[d];
   }
+  g.err = p->d_err;
+  g.wait_ns = p->wait_ns;
   return g;
+}
+
+// After the caller's stream has been synchronised: MRG_ERR_TIMEOUT (and the word cleared)
+// when a bounded device-side wait of this plan's kernels ran out since the last check.
+static mrg_status plan_check(mrg_plan *p, cudaStream_t st) {
+  if (!p->d_err) return MRG_OK;
+  int h = 0;
+  MRG_CUDA(cudaMemcpyAsync(&h, p->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  MRG_CUDA(cudaStreamSynchronize(st));
+  if (h) {
+    MRG_CUDA(cudaMemsetAsync(p->d_err, 0, sizeof(int), st));
+    MRG_CUDA(cudaStreamSynchronize(st));
+    set_error("a bounded device-side wait ran out (tensor-core gridding gave up); results of the calls since "
+              "the last check are incomplete");
+    return MRG_ERR_TIMEOUT;
+  }
+  return MRG_OK;
+}
+
+// The reference's early-stop rule (src/recon_lib.cpp:2081-2087, :2154-2163): residual
+// ratios of the last `range` iterations, their standard deviation in the reference's
+// float / double mix, below `thresh`.
+static bool early_stop_met(std::vector<float> &diffs, float ratio, int range, float thresh) {
+  diffs.push_back(ratio);
+  if ((int)diffs.size() > range) diffs.erase(diffs.begin());
+  if ((int)diffs.size() != range) return false;
+  double sum = 0.0, sq = 0.0;  // std::accumulate / std::inner_product with a double 0.0
+  for (float v : diffs) {
+    sum += v;
+    sq += (double)v * v;
+  }
+  const float mean = (float)(sum / diffs.size());
+  const float sq_sum = (float)sq;
+  const float stdev = std::sqrt(sq_sum / (float)diffs.size() - mean * mean);
+  return stdev < thresh;
 }
 
 static bool is_device_ptr(const void *ptr) {
@@ -654,6 +715,11 @@ mrg_status mrg_plan_create(const mrg_config *cfg_in, int Nx, int Ny, int Nz, int
   ALLOC(p->d_t2, sizeof(float2) * t2n * ncoil);
   ALLOC(p->d_t1, sizeof(float2) * t1n * ncoil);
   ALLOC(p->d_sc, sizeof(Scalars));
+  ALLOC(p->d_err, sizeof(int));
+  if (cudaMemset(p->d_err, 0, sizeof(int)) != cudaSuccess) {
+    set_error("error word initialisation failed");
+    return fail(MRG_ERR_CUDA);
+  }
   p->nblk = reduce_blocks(p->nimg * nframes);
   ALLOC(p->d_part, sizeof(double) * 3 * p->nblk);
 #undef ALLOC
@@ -678,7 +744,7 @@ mrg_status mrg_plan_destroy(mrg_plan *p) {
   for (auto &f : p->frames) traj_free(f);
   cudaFree(p->d_lut); cudaFree(p->d_win); cudaFree(p->d_grid); cudaFree(p->d_t2); cudaFree(p->d_t1);
   cudaFree(p->d_smap); cudaFree(p->d_y); cudaFree(p->d_R); cudaFree(p->d_P); cudaFree(p->d_L); cudaFree(p->d_Xo);
-  cudaFree(p->d_part); cudaFree(p->d_sc); cudaFree(p->d_resid);
+  cudaFree(p->d_part); cudaFree(p->d_sc); cudaFree(p->d_resid); cudaFree(p->d_err);
   for (int k = 0; k < 4; k++) cudaFree(p->d_stage[k]);
   if (p->cg_exec) cudaGraphExecDestroy(p->cg_exec);
   for (int k = 0; k < 5; k++)
@@ -902,7 +968,7 @@ mrg_status mrg_adjoint(mrg_plan *p, int frame, const void *data, int64_t coil_st
     MRG_CUDA(cudaMemcpyAsync(X, dX, sizeof(float2) * p->nimg, cudaMemcpyDeviceToHost, st));
     MRG_CUDA(cudaStreamSynchronize(st));
   }
-  return MRG_OK;
+  return sX ? plan_check(p, st) : MRG_OK;
 }
 
 mrg_status mrg_forward(mrg_plan *p, int frame, const void *X, void *data, int64_t coil_stride, const void *diff,
@@ -942,7 +1008,7 @@ mrg_status mrg_forward(mrg_plan *p, int frame, const void *X, void *data, int64_
     MRG_CUDA(cudaMemcpyAsync(data, dd, dbytes, cudaMemcpyDeviceToHost, st));
     MRG_CUDA(cudaStreamSynchronize(st));
   }
-  return MRG_OK;
+  return sd ? plan_check(p, st) : MRG_OK;
 }
 
 mrg_status mrg_normal(mrg_plan *p, int frame, const void *X, void *out, void *stream) {
@@ -968,7 +1034,7 @@ mrg_status mrg_normal(mrg_plan *p, int frame, const void *X, void *out, void *st
     MRG_CUDA(cudaMemcpyAsync(out, dO, sizeof(float2) * p->nimg, cudaMemcpyDeviceToHost, st));
     MRG_CUDA(cudaStreamSynchronize(st));
   }
-  return MRG_OK;
+  return sO ? plan_check(p, st) : MRG_OK;
 }
 
 mrg_status mrg_adjoint_coil(mrg_plan *p, int frame, const void *smap, const void *data, void *X, void *stream) {
@@ -994,7 +1060,7 @@ mrg_status mrg_adjoint_coil(mrg_plan *p, int frame, const void *smap, const void
     MRG_CUDA(cudaMemcpyAsync(X, dX, sizeof(float2) * p->nimg, cudaMemcpyDeviceToHost, st));
     MRG_CUDA(cudaStreamSynchronize(st));
   }
-  return MRG_OK;
+  return sX ? plan_check(p, st) : MRG_OK;
 }
 
 mrg_status mrg_forward_coil(mrg_plan *p, int frame, const void *X, const void *smap, void *data, const void *diff,
@@ -1032,7 +1098,7 @@ mrg_status mrg_forward_coil(mrg_plan *p, int frame, const void *X, const void *s
     MRG_CUDA(cudaMemcpyAsync(data, dd, dbytes, cudaMemcpyDeviceToHost, st));
     MRG_CUDA(cudaStreamSynchronize(st));
   }
-  return MRG_OK;
+  return sd ? plan_check(p, st) : MRG_OK;
 }
 
 mrg_status mrg_set_k_rad(mrg_plan *p, float k_rad, void *stream) {
@@ -1092,7 +1158,7 @@ mrg_status mrg_adjoint_coils(mrg_plan *p, int frame, const void *data, int64_t c
     MRG_CUDA(cudaMemcpyAsync(images, dI, ibytes, cudaMemcpyDeviceToHost, st));
     MRG_CUDA(cudaStreamSynchronize(st));
   }
-  return MRG_OK;
+  return sI ? plan_check(p, st) : MRG_OK;
 }
 
 mrg_status mrg_adjoint_sos(mrg_plan *p, int frame, const void *data, int64_t coil_stride, void *X, void *stream) {
@@ -1112,7 +1178,7 @@ mrg_status mrg_adjoint_sos(mrg_plan *p, int frame, const void *data, int64_t coi
     MRG_CUDA(cudaMemcpyAsync(X, dX, sizeof(float2) * p->nimg, cudaMemcpyDeviceToHost, st));
     MRG_CUDA(cudaStreamSynchronize(st));
   }
-  return MRG_OK;
+  return sX ? plan_check(p, st) : MRG_OK;
 }
 
 mrg_status mrg_lowres_smaps(mrg_plan *p, int frame, const void *data, int64_t coil_stride, float smap_res,
@@ -1194,6 +1260,73 @@ mrg_status mrg_fft3(mrg_plan *p, void *grid, int sign, void *stream) {
   return MRG_OK;
 }
 
+mrg_status mrg_grid(mrg_plan *p, int frame, const void *data, int64_t coil_stride, void *grid, void *stream) {
+  MRG_TRY(check_frame(p, frame));
+  if (!data || !grid) {
+    set_error("null argument");
+    return MRG_ERR_INVALID;
+  }
+  const FrameTraj &ft = p->frames[frame];
+  if (p->C > 1 && coil_stride < ft.M) {
+    set_error("coil_stride smaller than the sample count");
+    return MRG_ERR_INVALID;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  const Geometry &g = p->geo;
+  const size_t gbytes = sizeof(float2) * (size_t)g.S[0] * g.S[1] * g.S[2] * p->C;
+  void *dd, *dG;
+  bool sd, sG;
+  MRG_TRY(dev_view(p, 0, data, sizeof(float2) * (size_t)(coil_stride * (p->C - 1) + ft.M), true, st, &dd, &sd));
+  MRG_TRY(dev_view(p, 1, grid, gbytes, false, st, &dG, &sG));
+  // data * kw * taper in the sorted order, then the scatter (every grid point is written)
+  MRG_TRY(launch_gather_samples(ft, p->C, (const float2 *)dd, coil_stride, p->d_y, st, true));
+  const GridConst gc = grid_const(p);
+  MRG_TRY(launch_grid(gc, ft, p->d_y, (float2 *)dG, st));
+  if (sG) {
+    MRG_CUDA(cudaMemcpyAsync(grid, dG, gbytes, cudaMemcpyDeviceToHost, st));
+    MRG_CUDA(cudaStreamSynchronize(st));
+  }
+  return sG ? plan_check(p, st) : MRG_OK;
+}
+
+mrg_status mrg_ungrid(mrg_plan *p, int frame, const void *grid, void *data, int64_t coil_stride, const void *diff,
+                      void *stream) {
+  MRG_TRY(check_frame(p, frame));
+  if (!data || !grid) {
+    set_error("null argument");
+    return MRG_ERR_INVALID;
+  }
+  const FrameTraj &ft = p->frames[frame];
+  if (p->C > 1 && coil_stride < ft.M) {
+    set_error("coil_stride smaller than the sample count");
+    return MRG_ERR_INVALID;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  const Geometry &g = p->geo;
+  const size_t gbytes = sizeof(float2) * (size_t)g.S[0] * g.S[1] * g.S[2] * p->C;
+  const size_t dbytes = sizeof(float2) * (size_t)(coil_stride * (p->C - 1) + ft.M);
+  void *dG, *dd, *ddf = nullptr;
+  bool sG, sd, sdf = false;
+  MRG_TRY(dev_view(p, 0, grid, gbytes, true, st, &dG, &sG));
+  MRG_TRY(dev_view(p, 1, data, dbytes, false, st, &dd, &sd));
+  float2 *dsort = nullptr;
+  if (diff) {  // the sorted copy of diff lives behind the samples in the y buffer
+    MRG_TRY(dev_view(p, 2, diff, dbytes, true, st, &ddf, &sdf));
+    const int64_t ny = std::max<int64_t>(1, (int64_t)ft.nvalid * p->C);
+    MRG_TRY(ensure_y(p, 2 * ny));
+    dsort = p->d_y + ny;
+    MRG_TRY(launch_gather_samples(ft, p->C, (const float2 *)ddf, coil_stride, dsort, st));
+  }
+  const GridConst gc = grid_const(p);
+  MRG_TRY(launch_ungrid(gc, ft, (const float2 *)dG, dsort, p->d_y, false, st));
+  MRG_TRY(launch_scatter_samples(ft, p->C, p->d_y, (float2 *)dd, coil_stride, st));
+  if (sd) {
+    MRG_CUDA(cudaMemcpyAsync(data, dd, dbytes, cudaMemcpyDeviceToHost, st));
+    MRG_CUDA(cudaStreamSynchronize(st));
+  }
+  return sd ? plan_check(p, st) : MRG_OK;
+}
+
 mrg_status mrg_espirit_smaps(mrg_plan *p, int frame, const void *data, int64_t coil_stride,
                              const mrg_espirit_params *params, const float blur[3], void *smaps_out,
                              int64_t out_stride, int *kept, void *stream) {
@@ -1272,6 +1405,10 @@ mrg_status mrg_grad(mrg_plan *p, int frame, const void *X, const void *y, int64_
     set_error("coil maps not set");
     return MRG_ERR_STATE;
   }
+  if (p->cfg.kernel_type != MRG_KERNEL_KAISER) {
+    set_error("the trajectory gradient needs the Kaiser-Bessel kernel (its analytic derivative)");
+    return MRG_ERR_UNSUPPORTED;
+  }
   FrameTraj &ft = p->frames[frame];
   if (p->C > 1 && coil_stride < ft.M) {
     set_error("coil_stride smaller than the sample count");
@@ -1300,7 +1437,7 @@ mrg_status mrg_grad(mrg_plan *p, int frame, const void *X, const void *y, int64_
   if (sgx) MRG_CUDA(cudaMemcpyAsync(grad_x, dgx, sizeof(float2) * p->nimg, cudaMemcpyDeviceToHost, st));
   if (sgk) MRG_CUDA(cudaMemcpyAsync(grad_k, dgk, sizeof(float) * 3 * (size_t)ft.M, cudaMemcpyDeviceToHost, st));
   MRG_CUDA(cudaStreamSynchronize(st));
-  return MRG_OK;
+  return plan_check(p, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -1425,7 +1562,7 @@ mrg_status mrg_cg_residuals(mrg_plan *p, double *resid, int n, void *stream) {
   cudaStream_t st = (cudaStream_t)stream;
   if (n > 0) MRG_CUDA(cudaMemcpyAsync(resid, p->d_resid, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
   MRG_CUDA(cudaStreamSynchronize(st));
-  return MRG_OK;
+  return plan_check(p, st);
 }
 
 mrg_status mrg_cg(mrg_plan *p, int max_iter, void *X, double *resid, int use_graph, void *stream) {
@@ -1441,10 +1578,11 @@ mrg_status mrg_cg(mrg_plan *p, int max_iter, void *X, double *resid, int use_gra
   MRG_TRY(dev_view(p, 0, X, sizeof(float2) * nt, false, st, &dX, &sX));
   MRG_TRY(mrg_cg_init(p, max_iter, dX, stream));
   MRG_TRY(mrg_cg_iterate(p, max_iter, dX, use_graph, stream));
+  p->last_iters = max_iter;
   if (resid && max_iter > 0) MRG_TRY(mrg_cg_residuals(p, resid, max_iter, stream));
   if (sX) MRG_CUDA(cudaMemcpyAsync(X, dX, sizeof(float2) * nt, cudaMemcpyDeviceToHost, st));
   MRG_CUDA(cudaStreamSynchronize(st));
-  return MRG_OK;
+  return plan_check(p, st);
 }
 
 mrg_status mrg_set_timing(mrg_plan *p, int enable) {
@@ -1573,6 +1711,11 @@ extern "C" mrg_status mrg_fista(mrg_plan *p, const mrg_fista_params *q, void *X,
     set_error("bad low-rank block parameters");
     return MRG_ERR_INVALID;
   }
+  const bool early_stop = q->early_stop_thresh > 0.0f;
+  if (early_stop && q->early_stop_range < 1) {
+    set_error("early_stop_range must be at least 1");
+    return MRG_ERR_INVALID;
+  }
   for (int t = 0; t < p->T; t++) {
     MRG_TRY(check_frame(p, t));
     if (!p->frames[t].has_data) {
@@ -1661,30 +1804,66 @@ extern "C" mrg_status mrg_fista(mrg_plan *p, const mrg_fista_params *q, void *X,
   MRG_TRY(launch_zero(p->d_Xo, sizeof(float2) * nt, st));
   MRG_CUDA(cudaMemcpyAsync(&p->d_sc->it, &z.it, sizeof(int), cudaMemcpyHostToDevice, st));
   MRG_CUDA(cudaStreamSynchronize(st));
+  // Early stop (src/recon_lib.cpp:2081-2087, :2154-2163): after each iteration the ratio of its
+  // sum |R|^2 to iteration 0's joins the last early_stop_range ratios; the loop ends once
+  // their standard deviation is below early_stop_thresh.  Checking reads one residual back
+  // per iteration, so it runs only when a threshold is set.
+  std::vector<float> diffs;
+  double error0 = 0.0;
+  auto stop_after = [&](int it) -> int {  // 1: stop, 0: go on, < 0: -(mrg_status)
+    if (!early_stop) return 0;
+    double r = 0.0;
+    if (cudaMemcpyAsync(&r, p->d_resid + it, sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess) {
+      set_error("residual read-back failed");
+      return -(int)MRG_ERR_CUDA;
+    }
+    if (it == 0) error0 = r;
+    const float ratio = (float)(std::fabs(r) / error0);
+    return early_stop_met(diffs, ratio, q->early_stop_range, q->early_stop_thresh) ? 1 : 0;
+  };
+  int done = 0;
   if (use_graph && q->max_iter > 1) {
     MRG_TRY(fista_iteration(p, f, st));  // iteration 0 eagerly, then replay the captured iteration
     MRG_CUDA(cudaStreamSynchronize(st));
-    cudaGraphExec_t ge = nullptr;
-    MRG_TRY(capture(p, [&](cudaStream_t cs) { return fista_iteration(p, f, cs); }, &ge));
-    mrg_status rs = MRG_OK;
-    for (int it = 1; it < q->max_iter && rs == MRG_OK; it++) {
-      if (cudaGraphLaunch(ge, st) != cudaSuccess) rs = MRG_ERR_CUDA;
-      count_launch();
-    }
-    cudaGraphExecDestroy(ge);
-    if (rs != MRG_OK) {
-      set_error("graph launch failed");
-      return rs;
+    done = 1;
+    int stop = stop_after(0);
+    if (stop < 0) return (mrg_status)(-stop);
+    if (!stop) {
+      cudaGraphExec_t ge = nullptr;
+      MRG_TRY(capture(p, [&](cudaStream_t cs) { return fista_iteration(p, f, cs); }, &ge));
+      mrg_status rs = MRG_OK;
+      for (int it = 1; it < q->max_iter && rs == MRG_OK; it++) {
+        if (cudaGraphLaunch(ge, st) != cudaSuccess) {
+          rs = MRG_ERR_CUDA;
+          set_error("graph launch failed");
+          break;
+        }
+        count_launch();
+        done = it + 1;
+        stop = stop_after(it);
+        if (stop < 0) rs = (mrg_status)(-stop);
+        if (stop) break;
+      }
+      cudaGraphExecDestroy(ge);
+      if (rs != MRG_OK) return rs;
     }
   } else {
-    for (int it = 0; it < q->max_iter; it++) MRG_TRY(fista_iteration(p, f, st));
+    for (int it = 0; it < q->max_iter; it++) {
+      MRG_TRY(fista_iteration(p, f, st));
+      done = it + 1;
+      const int stop = stop_after(it);
+      if (stop < 0) return (mrg_status)(-stop);
+      if (stop) break;
+    }
   }
-  if (resid && q->max_iter > 0)
-    MRG_CUDA(cudaMemcpyAsync(resid, p->d_resid, sizeof(double) * q->max_iter, cudaMemcpyDeviceToHost, st));
+  p->last_iters = done;
+  if (resid && done > 0)
+    MRG_CUDA(cudaMemcpyAsync(resid, p->d_resid, sizeof(double) * done, cudaMemcpyDeviceToHost, st));
   if (step) MRG_CUDA(cudaMemcpyAsync(step, &p->d_sc->step, sizeof(float), cudaMemcpyDeviceToHost, st));
   if (sX) MRG_CUDA(cudaMemcpyAsync(X, dX, sizeof(float2) * nt, cudaMemcpyDeviceToHost, st));
   MRG_CUDA(cudaStreamSynchronize(st));
-  return MRG_OK;
+  return plan_check(p, st);
 }
 
 // CLEAR (src/recon_lib.cpp:1025-1238).  The per-coil images XX, the gradients RR and
@@ -1722,7 +1901,12 @@ extern "C" mrg_status mrg_clear(mrg_plan *p, const mrg_clear_params *q, void *X,
   const int64_t n = p->nimg, nc = n * C, ntc = nc * T;
   int bs[3];
   for (int d = 0; d < 3; d++) bs[d] = std::min(q->block[d], g.N[d]);  // clear.cpp:109-112
-  const int nb = coil_llr_blocks(g.N, bs);
+  const int64_t nb64 = coil_llr_blocks(g.N, bs);
+  if (nb64 > (int64_t)(1 << 30)) {
+    set_error("too many coil low-rank blocks (" + std::to_string(nb64) + ")");
+    return MRG_ERR_UNSUPPORTED;
+  }
+  const int nb = (int)nb64;
   int np2 = 1;
   while (np2 < nb) np2 <<= 1;
   const int nblk = reduce_blocks(nc);
@@ -1819,18 +2003,8 @@ extern "C" mrg_status mrg_clear(mrg_plan *p, const mrg_clear_params *q, void *X,
       MRG_CUDA(cudaMemcpyAsync(hacc.data(), ai, sizeof(double) * 3, cudaMemcpyDeviceToHost, st));
       MRG_CUDA(cudaStreamSynchronize(st));
       if (it == 0) error0 = hacc[0];
-      diffs.push_back((float)(hacc[0] / error0));
-      if ((int)diffs.size() > q->early_stop_range) diffs.erase(diffs.begin());
-      if ((int)diffs.size() == q->early_stop_range) {
-        double sq = 0.0, sm = 0.0;
-        for (float v : diffs) {
-          sm += v;
-          sq += (double)v * v;
-        }
-        const float mean = (float)(sm / diffs.size());
-        const float sd = (float)std::sqrt(sq / diffs.size() - (double)mean * mean);
-        if (sd < q->early_stop_thresh) break;
-      }
+      if (early_stop_met(diffs, (float)(std::fabs(hacc[0]) / error0), q->early_stop_range, q->early_stop_thresh))
+        break;
     }
   }
   // lrankcoil.combine(XX, X) into zeroed images
@@ -1845,8 +2019,9 @@ extern "C" mrg_status mrg_clear(mrg_plan *p, const mrg_clear_params *q, void *X,
     for (int it = 0; it < done; it++)
       MRG_CUDA(cudaMemcpyAsync(resid + it, acc + 3 * it, sizeof(double), cudaMemcpyDeviceToHost, st));
   if (iters) *iters = done;
+  p->last_iters = done;
   MRG_CUDA(cudaStreamSynchronize(st));
-  return MRG_OK;
+  return plan_check(p, st);
 }
 
 extern "C" {
@@ -1885,6 +2060,37 @@ void mrg_fista_params_default(mrg_fista_params *q) {
   q->clear_amp = 4.0f;
   q->clear_t2 = 6.0f;
   q->rand_skip = -1;
+  q->early_stop_thresh = 0.0f;
+  q->early_stop_range = 5;
+}
+
+mrg_status mrg_set_wait_limit(mrg_plan *p, double seconds) {
+  if (!p || !(seconds >= 0.0) || seconds > 3600.0) {
+    set_error("wait limit must be within [0, 3600] seconds");
+    return MRG_ERR_INVALID;
+  }
+  p->wait_ns = (long long)(seconds * 1e9);
+  invalidate_graphs(p);  // captured launches carry the old limit
+  return MRG_OK;
+}
+
+mrg_status mrg_plan_check(mrg_plan *p, void *stream) {
+  if (!p) {
+    set_error("null plan");
+    return MRG_ERR_INVALID;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  MRG_CUDA(cudaStreamSynchronize(st));
+  return plan_check(p, st);
+}
+
+mrg_status mrg_last_iterations(const mrg_plan *p, int *iters) {
+  if (!p || !iters) {
+    set_error("null argument");
+    return MRG_ERR_INVALID;
+  }
+  *iters = p->last_iters;
+  return MRG_OK;
 }
 
 }  // extern "C"

@@ -191,11 +191,11 @@ mrg_status gaussian_blur_ex(float2 *X, int nvol, const int N[3], int64_t es, int
     }
     a.nlines = sz[0] * sz[1] * sz[2];
     a.w = w;
-    static bool attr = false;
-    if (!attr) {
+    static DeviceOnce once;
+    MRG_TRY(device_once(once, []() -> mrg_status {
       MRG_CUDA(cudaFuncSetAttribute(k_blur, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
-      attr = true;
-    }
+      return MRG_OK;
+    }));
     k_blur<<<(unsigned)((a.nlines + 31) / 32), 256, smem, st>>>(a);
     MRG_LAUNCHED();
   }

@@ -19,26 +19,37 @@ bool fft_size_supported(int S) {
   return false;
 }
 
-// Per-size twiddle tables exp(-2 pi i m / S), m < S, built once per device.
-float2 *g_tw[1024];
-static int g_tw_dev = -1;
+// Per-size twiddle tables exp(-2 pi i m / S), m < S, built once on each device (a table
+// lives in the memory of the device it was built on).
+static float2 *g_tw[kTwDevices][1024];
+static DeviceOnce g_tw_once;
 
 mrg_status fft_init_device() {
   int dev = 0;
   MRG_CUDA(cudaGetDevice(&dev));
-  if (g_tw_dev == dev) return MRG_OK;
-  for (int q : kSupportedQ) {
-    const int S = 8 * q;
-    std::vector<float2> tw(S);
-    for (int m = 0; m < S; m++) {
-      const double a = -2.0 * 3.141592653589793238462643 * (double)m / (double)S;
-      tw[m] = make_float2((float)cos(a), (float)sin(a));
-    }
-    MRG_CUDA(cudaMalloc(&g_tw[S], sizeof(float2) * S));
-    MRG_CUDA(cudaMemcpy(g_tw[S], tw.data(), sizeof(float2) * S, cudaMemcpyHostToDevice));
+  if (dev < 0 || dev >= kTwDevices) {
+    set_error("device ordinal beyond the FFT twiddle tables");
+    return MRG_ERR_UNSUPPORTED;
   }
-  g_tw_dev = dev;
-  return MRG_OK;
+  return device_once(g_tw_once, [dev]() -> mrg_status {
+    for (int q : kSupportedQ) {
+      const int S = 8 * q;
+      std::vector<float2> tw(S);
+      for (int m = 0; m < S; m++) {
+        const double a = -2.0 * 3.141592653589793238462643 * (double)m / (double)S;
+        tw[m] = make_float2((float)cos(a), (float)sin(a));
+      }
+      MRG_CUDA(cudaMalloc(&g_tw[dev][S], sizeof(float2) * S));
+      MRG_CUDA(cudaMemcpy(g_tw[dev][S], tw.data(), sizeof(float2) * S, cudaMemcpyHostToDevice));
+    }
+    return MRG_OK;
+  });
+}
+
+const float2 *fft_twiddles(int S) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kTwDevices || S < 0 || S >= 1024) return nullptr;
+  return g_tw[dev][S];
 }
 
 

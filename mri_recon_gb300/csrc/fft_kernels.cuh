@@ -23,7 +23,9 @@
 namespace mrg {
 
 // per-size twiddle tables exp(-2 pi i m / S), m < S, built once per device (fft.cu)
-extern float2 *g_tw[1024];
+// Twiddle table of length-S lines on the current device (fft_init_device builds them).
+constexpr int kTwDevices = 64;
+const float2 *fft_twiddles(int S);
 
 // lengths 192..288 (fft_large.cu) and 320..384 (fft_large2.cu)
 mrg_status launch_fft_192_288(const FftPass &p, cudaStream_t st);
@@ -526,14 +528,16 @@ __global__ void __launch_bounds__(8 * P) k_fft_pp(const FftPass p, int ntiles) {
 template <int Q, int SIGN, int P>
 static mrg_status launch_pp(const FftPass &pp, cudaStream_t st) {
   const size_t smem = (size_t)8 * Q * (P + 2) * sizeof(float2);
-  static int ctas = 0;
-  if (!ctas) {
+  static DeviceOnce once;
+  static int ctas = 1;  // resident CTAs per SM (the same kernel and shape on every device of a process)
+  MRG_TRY(device_once(once, [smem]() -> mrg_status {
     MRG_CUDA(cudaFuncSetAttribute(k_fft_pp<Q, SIGN, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    MRG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctas, k_fft_pp<Q, SIGN, P>, 8 * P, smem));
-    if (ctas < 1) ctas = 1;
-  }
-  int sms = 152;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+    int c = 0;
+    MRG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_fft_pp<Q, SIGN, P>, 8 * P, smem));
+    ctas = c < 1 ? 1 : c;
+    return MRG_OK;
+  }));
+  const int sms = device_sms();
   const int ntiles = (int)(pp.nlines / P);
   const int nblk = std::max(1, std::min(ntiles, sms * ctas));
   k_fft_pp<Q, SIGN, P><<<nblk, 8 * P, smem, st>>>(pp, ntiles);
@@ -554,12 +558,12 @@ static mrg_status launch_qp(const FftPass &pp, const dim3 grid, const dim3 block
   else if (pp.mode == FFT_ACCUM) fn = k_fft<Q, +1, FFT_ACCUM, P>;
   else if (pp.sign < 0) fn = k_fft<Q, -1, FFT_PLAIN, P>;
   else fn = k_fft<Q, +1, FFT_PLAIN, P>;
-  static int attr_set[4] = {0, 0, 0, 0};  // per instantiation: set the smem cap once
+  static DeviceOnce once[4];  // per instantiation and mode: set the smem cap once on each device
   const int slot = pp.mode == FFT_PLAIN ? (pp.sign < 0 ? 0 : 1) : (pp.mode == FFT_SETIMG ? 2 : 3);
-  if (!attr_set[slot]) {
+  MRG_TRY(device_once(once[slot], [fn]() -> mrg_status {
     MRG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 8 * Q * 34 * (int)sizeof(float2)));
-    attr_set[slot] = 1;
-  }
+    return MRG_OK;
+  }));
   fn<<<grid, block, smem, st>>>(pp);
   MRG_LAUNCHED();
   return MRG_OK;
@@ -575,7 +579,11 @@ static mrg_status launch_q(const FftPass &p, cudaStream_t st) {
   }
   const dim3 grid((unsigned)nblk64), block(8 * p.IB);
   FftPass pp = p;
-  pp.tw = g_tw[8 * Q];
+  pp.tw = fft_twiddles(8 * Q);
+  if (!pp.tw) {
+    set_error("FFT twiddles not built on this device");
+    return MRG_ERR_STATE;
+  }
   // CTAs that never straddle an outer row find their row with one 32-bit division
   pp.nib = (p.inner % p.IB == 0 && p.nlines % p.inner == 0) ? (int)(p.inner / p.IB) : 0;
   if constexpr (fixed_pitch_q(Q)) {

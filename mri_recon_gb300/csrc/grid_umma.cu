@@ -23,16 +23,15 @@
 // zero and added into the thread's FP32 registers with round-to-nearest when its slot is
 // reused; along a whole region the truncation would otherwise build up a bias.
 //
-// Every mbarrier wait is bounded (about two seconds of SM clock); a kernel that runs
-// out of time sets an error flag, waits once more (bounded) for its own MMAs, frees its
-// tensor memory and returns.
+// Every mbarrier wait is bounded (GridConst::wait_ns of the GPU's global timer, two
+// seconds by default); a kernel whose wait runs out sets the plan's error word, waits
+// (bounded, at least the default limit) for the MMAs it already issued, frees its tensor
+// memory and returns, and the plan's next synchronising call reports MRG_ERR_TIMEOUT.
 #include "mrg_internal.h"
 
 namespace mrg {
 
 namespace {
-
-__device__ int g_umma_error = 0;
 
 constexpr int TK = 96;      // pairs per chunk: twelve k-steps of 8 TF32 values
 constexpr int TP = TK + 4;  // row pitch (floats) of the per-pair weight tables: conflict-free 16-byte reads
@@ -111,10 +110,28 @@ __device__ __forceinline__ void tst8(uint32_t ta, const uint32_t (&r)[8]) {
                : "memory");
 }
 
-// Bounded wait for phase `parity` of an mbarrier; false after ~2 s of SM clock.  Between
-// tries the thread sleeps `nap` ns, so a waiting warp takes few issue slots from the others.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, unsigned nap = 32) {
-  const long long t0 = clock64();
+__device__ __forceinline__ long long gtimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return (long long)t;
+}
+
+// Bounded wait for phase `parity` of an mbarrier; false once `limit_ns` of the global
+// timer have passed.  try_wait itself may suspend the thread for a while before it reports
+// failure, so a limit of 0 takes one non-blocking test_wait instead: it gives up at once
+// unless the phase has already completed.  Between tries the thread sleeps `nap` ns, so a
+// waiting warp takes few issue slots from the others.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, long long limit_ns, unsigned nap = 32) {
+  if (limit_ns <= 0) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return done != 0;
+  }
+  const long long t0 = gtimer_ns();
   for (;;) {
     uint32_t done;
     asm volatile(
@@ -123,9 +140,13 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, unsigne
         : "r"(bar), "r"(parity)
         : "memory");
     if (done) return true;
-    if (clock64() - t0 > 4000000000LL) return false;
+    if (gtimer_ns() - t0 >= limit_ns) return false;
     __nanosleep(nap);
   }
+}
+
+__device__ __forceinline__ void flag_wait_error(const GridConst &g) {
+  if (g.err) atomicExch(g.err, MRG_WAIT_EXPIRED);
 }
 
 // Drains this warp's NQ columns of an accumulator slot (lane = row) into acc with
@@ -295,8 +316,8 @@ __global__ void __launch_bounds__(NTHR, 1)
     const uint32_t id = idesc<N>();
     for (int c = 0;; c++) {
       const int s = c & 1;
-      if (!mbar_wait(s_u32(&full[s]), (uint32_t)((c >> 1) & 1), 256)) {
-        atomicExch(&g_umma_error, 1);
+      if (!mbar_wait(s_u32(&full[s]), (uint32_t)((c >> 1) & 1), g.wait_ns, 256)) {
+        flag_wait_error(g);
         break;
       }
       const int nks = slot_nks[s];
@@ -342,7 +363,7 @@ __global__ void __launch_bounds__(NTHR, 1)
     // give up together so their barriers stay matched.
     auto retire = [&](int s) -> bool {
       if (!((outstanding >> s) & 1u)) return true;
-      if (!bld_and(mbar_wait(s_u32(&done[s]), (dphase >> s) & 1u))) return false;
+      if (!bld_and(mbar_wait(s_u32(&done[s]), (dphase >> s) & 1u, g.wait_ns))) return false;
       dphase ^= 1u << s;
       outstanding &= ~(1u << s);
       if ((mma >> s) & 1u) {
@@ -497,9 +518,13 @@ __global__ void __launch_bounds__(NTHR, 1)
       __syncwarp();
       if ((tid & 31) == 0) mbar_arrive(s_u32(&full[c & 1]));
     } else {
-      atomicExch(&g_umma_error, 1);
-      for (int s = 0; s < 2; s++)  // let MMAs still in flight finish before the memory is freed
-        if ((outstanding >> s) & 1u) mbar_wait(s_u32(&done[s]), (dphase >> s) & 1u);
+      flag_wait_error(g);
+      // let MMAs still in flight finish before the tensor memory is freed: the MMA warp
+      // either issued a slot's MMAs and their commit, which arrive within microseconds, or
+      // gave up before it, so this wait has at least the default limit whatever the plan's
+      const long long lim = g.wait_ns > MRG_DEFAULT_WAIT_NS ? g.wait_ns : MRG_DEFAULT_WAIT_NS;
+      for (int s = 0; s < 2; s++)
+        if ((outstanding >> s) & 1u) mbar_wait(s_u32(&done[s]), (dphase >> s) & 1u, lim);
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -514,9 +539,10 @@ bool umma_supported(int C) { return C >= 8; }
 bool umma_grid_fits(const int S[3]) { return S[0] <= 2048 && S[1] <= 2048 && S[2] <= 1024; }
 int umma_default_cc(int C) { return C > 16 ? 32 : (C > 8 ? 16 : 8); }
 
-int umma_error_flag() {
+int read_wait_error(const GridConst &gc) {
+  if (!gc.err) return 0;
   int h = 0;
-  if (cudaMemcpyFromSymbol(&h, g_umma_error, sizeof(int)) != cudaSuccess) {
+  if (cudaMemcpy(&h, gc.err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
@@ -528,14 +554,13 @@ static mrg_status launch_umma_cc(const GridConst &gc, const FrameTraj &ft, const
                                  cudaStream_t st) {
   typedef TcLayout<CC> L;
   const bool vec = (gc.C % 2 == 0) && (((uintptr_t)yw & 15) == 0) && (((uintptr_t)grid & 15) == 0);
-  static bool attr = false;
-  if (!attr) {
+  static DeviceOnce once;
+  MRG_TRY(device_once(once, []() -> mrg_status {
     MRG_CUDA(cudaFuncSetAttribute(k_grid_umma<CC, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, L::TOTAL));
     MRG_CUDA(cudaFuncSetAttribute(k_grid_umma<CC, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, L::TOTAL));
-    attr = true;
-  }
-  int sms = 152;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+    return MRG_OK;
+  }));
+  const int sms = device_sms();
   // one CTA per SM (its shared memory keeps a second one off the SM, so the 512 TMEM
   // columns it allocates are always free); every coil pass gets its share of the SMs
   const int npass = (gc.C + CC - 1) / CC;

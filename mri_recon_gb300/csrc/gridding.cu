@@ -850,12 +850,12 @@ static mrg_status launch_grid_cc(const GridConst &gc, const FrameTraj &ft, const
   const bool vec = (gc.C % 2 == 0) && (CC % 2 == 0) && (((uintptr_t)yw & 15) == 0);
   const dim3 blocks((unsigned)((ft.blocks.nitems + 7) / 8), (unsigned)((gc.C + CC - 1) / CC));
   const size_t smem = 8 * GridStage<CC>::bytes;
-  static bool attr = false;
-  if (!attr) {
+  static DeviceOnce once;
+  MRG_TRY(device_once(once, [smem]() -> mrg_status {
     MRG_CUDA(cudaFuncSetAttribute(k_grid<CC, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     MRG_CUDA(cudaFuncSetAttribute(k_grid<CC, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr = true;
-  }
+    return MRG_OK;
+  }));
   if (vec)
     k_grid<CC, true><<<blocks, 256, smem, st>>>(gc, ft.blocks.nitems, ft.blocks.items, ft.blocks.pairs, ft.swt, ft.sst, yw, grid);
   else
@@ -1126,12 +1126,12 @@ static mrg_status launch_grid_mma(const GridConst &gc, const FrameTraj &ft, cons
   const bool vec = (gc.C % 2 == 0) && (((uintptr_t)yw & 15) == 0) && (((uintptr_t)grid & 15) == 0);
   const dim3 blocks((unsigned)((ft.blocks.nitems + 7) / 8), (unsigned)((gc.C + CC - 1) / CC));
   const size_t smem = 8 * (GridStage<CC>::bytes + 32 * 16);  // + the y/z products of 32 pairs
-  static bool attr = false;
-  if (!attr) {
+  static DeviceOnce once;
+  MRG_TRY(device_once(once, [smem]() -> mrg_status {
     MRG_CUDA(cudaFuncSetAttribute(k_grid_mma<NT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     MRG_CUDA(cudaFuncSetAttribute(k_grid_mma<NT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr = true;
-  }
+    return MRG_OK;
+  }));
   if (vec)
     k_grid_mma<NT, true><<<blocks, 256, smem, st>>>(gc, ft.blocks.nitems, ft.blocks.items, ft.blocks.pairs, ft.swt, ft.sst, yw, grid);
   else
@@ -1656,7 +1656,10 @@ mrg_status autotune_frame(const GridConst &gc, FrameTraj &ft, float2 *grid, floa
     }
     ft.grid_cc = cc;
     float ms = time_ms(st, [&]() { return launch_grid(gc, ft, y, grid, st); }, 2);
-    if (mode == 3 && umma_error_flag()) ms = 1e30f;  // gave up waiting for its MMAs: never pick it
+    if (mode == 3 && read_wait_error(gc)) {  // gave up waiting for its MMAs: never pick it
+      ms = 1e30f;
+      MRG_CUDA(cudaMemset(gc.err, 0, sizeof(int)));
+    }
     if (ms < best) {
       best = ms;
       bestCC = cc;

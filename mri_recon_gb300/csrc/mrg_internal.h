@@ -5,6 +5,7 @@
 
 #include <atomic>
 #include <cstdint>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -41,6 +42,33 @@ inline void count_launch(int n = 1) { g_launches.fetch_add(n, std::memory_order_
     mrg_status s_ = (call);        \
     if (s_ != MRG_OK) return s_;   \
   } while (0)
+
+// One-time set-up per device.  Kernel attributes (cudaFuncSetAttribute) and device
+// tables belong to the device that is current when they are set, so a process that
+// drives several GPUs has to set them once on each; `fn` runs with that device current.
+struct DeviceOnce {
+  std::mutex mu;
+  uint64_t done = 0;  // bit d: set up on device d
+};
+template <class F>
+inline mrg_status device_once(DeviceOnce &o, F &&fn) {
+  int dev = 0;
+  MRG_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fn();  // beyond the mask: set up on every call
+  std::lock_guard<std::mutex> lock(o.mu);
+  if ((o.done >> dev) & 1ull) return MRG_OK;
+  const mrg_status s = fn();
+  if (s == MRG_OK) o.done |= 1ull << dev;
+  return s;
+}
+// Streaming multiprocessors of the current device.
+int device_sms();
+
+// Error word of a plan's bounded device-side waits (GridConst::err): 0 while every wait
+// ended in time, MRG_WAIT_EXPIRED once one ran out.
+constexpr int MRG_WAIT_EXPIRED = 1;
+// Default limit of one bounded wait, in nanoseconds of the GPU's global timer.
+constexpr long long MRG_DEFAULT_WAIT_NS = 2000000000LL;
 
 // ---------------------------------------------------------------------------
 // Geometry: grid sizes, crop, kernel LUT and deapodisation windows, computed on
@@ -130,6 +158,8 @@ struct GridConst {
   int grid_mode;  // 0: fastest timed, 1: CUDA cores, 2: mma.sync tensor cores, 3: tcgen05 / TMEM
   float beta[3];
   double kb_norm[3];
+  int *err;          // device word set to MRG_WAIT_EXPIRED when a bounded wait runs out (may be NULL)
+  long long wait_ns; // limit of one bounded wait (GPU global timer, ns)
 };
 
 // Gridding blocks of b[0] x b[1] x b[2] points, nb[d] = S[d] / b[d] per axis.
@@ -186,8 +216,8 @@ int ungrid_mma_nt(int C);
 int umma_default_cc(int C);
 mrg_status launch_grid_umma(const GridConst &gc, const FrameTraj &ft, int cc, const float2 *yw, float2 *grid,
                             cudaStream_t st);
-// nonzero once a tcgen05 gridding launch gave up waiting for its tensor-core work
-int umma_error_flag();
+// the error word gc.err (0 when gc.err is NULL); reading it waits for the device
+int read_wait_error(const GridConst &gc);
 void traj_free(FrameTraj &ft);
 mrg_status launch_retaper(const GridConst &gc, FrameTraj &ft, cudaStream_t st);
 mrg_status count_taps(const FrameTraj &ft, int64_t *out);
@@ -298,7 +328,9 @@ mrg_status llr_alloc(LlrWork &w, int nblocks);
 void llr_free(LlrWork &w);
 mrg_status llr_update(const float2 *X, int Nt, const int N[3], const int bs[3], float amp, float t2,
                       const int *iter_dev, LlrWork &w, cudaStream_t st);
-int llr_block_count(const int N[3], const int bs[3]);
+// Blocks of bs[0] x bs[1] x bs[2] voxels (clipped to N) that tile N; 64-bit, so callers can
+// reject counts their buffers and launches cannot take.
+int64_t llr_block_count(const int N[3], const int bs[3]);
 // sigma_1 of every block into sig[nblocks], median via work[next pow2 >= nblocks], result in *smax (device).
 mrg_status llr_update_into(const float2 *X, int Nt, const int N[3], const int bs[3], float amp, float t2,
                            const Scalars *sc, int iter_fixed, double *sig, double *work, float *smax, cudaStream_t st);
@@ -320,7 +352,7 @@ struct EspiritParams {
 mrg_status espirit_maps(const float2 *img, int C, const int N[3], const EspiritParams &q, float2 *maps, int *nV_out,
                         cudaStream_t st);
 // CLEAR coil low rank on [frame][voxel][coil] stacks (clear.cu)
-int coil_llr_blocks(const int N[3], const int bs[3]);
+int64_t coil_llr_blocks(const int N[3], const int bs[3]);
 mrg_status coil_llr_update(const float2 *X, int T, int C, const int N[3], const int bs[3], float amp, float t2,
                            int iter, double *sig, double *work, float *smax, cudaStream_t st);
 mrg_status coil_llr_thresh(float2 *X, int T, int C, const int N[3], const int bs[3], float alpha, int block_iter,

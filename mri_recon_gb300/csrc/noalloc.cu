@@ -71,20 +71,30 @@ extern "C" mrg_status mrg_llr_update_threshold_noalloc(const void *X, int nframe
     return MRG_ERR_INVALID;
   }
   const int N[3] = {Nx, Ny, Nz};
-  const int nb = llr_block_count(N, block);
+  const int64_t nb = llr_block_count(N, block);  // 64-bit: a huge shape cannot wrap under the limit
   if (nb > MRG_NOALLOC_MAX_BLOCKS) {
     set_error("mrg_llr_update_threshold_noalloc: " + std::to_string(nb) + " low-rank blocks exceed the limit of " +
               std::to_string(MRG_NOALLOC_MAX_BLOCKS) + " of its fixed scratch array");
     return MRG_ERR_UNSUPPORTED;
   }
+  cudaStream_t st = (cudaStream_t)stream;
+  const bool smax_on_device = on_device(smax);
+  if (!smax_on_device) {
+    // a host smax is read back with a stream synchronisation, which a capturing stream forbids
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    MRG_CUDA(cudaStreamIsCapturing(st, &cs));
+    if (cs != cudaStreamCaptureStatusNone) {
+      set_error("mrg_llr_update_threshold_noalloc inside a stream capture needs smax in device memory");
+      return MRG_ERR_INVALID;
+    }
+  }
   double *scratch = nullptr;
   MRG_TRY(scratch_address(&scratch));
-  cudaStream_t st = (cudaStream_t)stream;
   float *smax_dev = reinterpret_cast<float *>(scratch + 2 * MRG_NOALLOC_MAX_BLOCKS);
   // every scratch element the kernels read is written first in this call: no clearing needed
   MRG_TRY(llr_update_into(static_cast<const float2 *>(X), nframes, N, block, clear_amp, clear_t2, nullptr, iteration,
                           scratch, scratch + MRG_NOALLOC_MAX_BLOCKS, smax_dev, st));
   MRG_CUDA(cudaMemcpyAsync(smax, smax_dev, sizeof(float), cudaMemcpyDefault, st));
-  if (!on_device(smax)) MRG_CUDA(cudaStreamSynchronize(st));
+  if (!smax_on_device) MRG_CUDA(cudaStreamSynchronize(st));
   return MRG_OK;
 }

@@ -145,12 +145,12 @@ static mrg_status wave_pass(WaveArgs a, int nvol, int inverse, cudaStream_t st) 
     return MRG_ERR_UNSUPPORTED;
   }
   const dim3 grid((unsigned)((a.nlines + 31) / 32), (unsigned)nvol);
-  static bool attr = false;
-  if (!attr) {
+  static DeviceOnce once;
+  MRG_TRY(device_once(once, []() -> mrg_status {
     MRG_CUDA(cudaFuncSetAttribute(k_wave<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
     MRG_CUDA(cudaFuncSetAttribute(k_wave<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
-    attr = true;
-  }
+    return MRG_OK;
+  }));
   if (inverse) k_wave<1><<<grid, 256, smem, st>>>(a);
   else k_wave<0><<<grid, 256, smem, st>>>(a);
   MRG_LAUNCHED();

@@ -205,6 +205,33 @@ class Plan:
                                                 a.ptr(out), a.ptr(diff, np.complex64), _stream(stream)))
         return out
 
+    def grid(self, frame, data, out=None, stream=None):
+        """chop_grid_forward of data_c * kw onto a (Sz, Sy, Sx, C) grid (every point written)."""
+        a = _Args()
+        stride = _numel(data) // self.ncoils
+        gshape = (self.S[2], self.S[1], self.S[0], self.ncoils)
+        if out is None:
+            if _is_tensor(data) and data.is_cuda:
+                out = torch.empty(gshape, dtype=torch.complex64, device=data.device)
+            else:
+                out = np.zeros(gshape, np.complex64)
+        _lib.check(_lib.load().mrg_grid(self._h, frame, a.ptr(data, np.complex64), stride, a.ptr(out),
+                                        _stream(stream)))
+        return out
+
+    def ungrid(self, frame, grid, out=None, diff=None, stream=None):
+        """chop_grid_backward from a (Sz, Sy, Sx, C) grid: (C, M) samples (minus diff)."""
+        a = _Args()
+        M = self.M[frame]
+        if out is None:
+            if _is_tensor(grid) and grid.is_cuda:
+                out = torch.empty((self.ncoils, M), dtype=torch.complex64, device=grid.device)
+            else:
+                out = np.zeros((self.ncoils, M), np.complex64)
+        _lib.check(_lib.load().mrg_ungrid(self._h, frame, a.ptr(grid, np.complex64), a.ptr(out), M,
+                                          a.ptr(diff, np.complex64), _stream(stream)))
+        return out
+
     def set_k_rad(self, k_rad, stream=None):
         """The public gridFFT::k_rad field: radius of E^H's Gaussian taper, every frame."""
         _lib.check(_lib.load().mrg_set_k_rad(self._h, float(k_rad), _stream(stream)))
@@ -338,7 +365,22 @@ class Plan:
         step = ctypes.c_float()
         _lib.check(_lib.load().mrg_fista(self._h, ctypes.byref(params), a.ptr(X), resid.ctypes.data_as(_lib._dp),
                                          ctypes.byref(step), int(bool(use_graph)), _stream(stream)))
-        return X, resid[:params.max_iter], step.value
+        return X, resid[:self.last_iterations()], step.value
+
+    def last_iterations(self):
+        """Iterations the last cg / fista / clear call ran (fewer than max_iter after an early stop)."""
+        n = ctypes.c_int()
+        _lib.check(_lib.load().mrg_last_iterations(self._h, ctypes.byref(n)))
+        return n.value
+
+    def set_wait_limit(self, seconds):
+        """Limit of each bounded device-side wait (default 2 s); 0 gives up after the first try."""
+        _lib.check(_lib.load().mrg_set_wait_limit(self._h, float(seconds)))
+
+    def check(self, stream=None):
+        """Waits for the stream; raises MrgError (MRG_ERR_TIMEOUT) if a bounded wait ran out since
+        the last report."""
+        _lib.check(_lib.load().mrg_plan_check(self._h, _stream(stream)))
 
 
     def clear(self, params, X=None, coil_images=None, stream=None):
@@ -518,6 +560,44 @@ def clear_params(**kw):
         else:
             setattr(p, k, v)
     return p
+
+
+def gate_weights(gate_times, kw, nread, frame, rweight=None):
+    """kw times the frame weight rweight * (floor(gate_time) == frame) of each sample's readout
+    (GATING::hist_weight); gate_times / rweight: one value per readout of nread samples."""
+    gt = np.ascontiguousarray(gate_times, np.float64)
+    rw = None if rweight is None else np.ascontiguousarray(rweight, np.float32)
+    kw = np.ascontiguousarray(kw, np.float32)
+    out = np.empty_like(kw)
+    _lib.check(_lib.load().mrg_gate_weights(gt.ctypes.data, None if rw is None else rw.ctypes.data, gt.size, int(nread),
+                                            int(frame), kw.ctypes.data, out.ctypes.data))
+    return out
+
+
+def pregate(gate_times, nread, frame, kx, ky, kz, kw, data=None, rweight=None, reset_dens=False):
+    """RECON::pregate_data for one frame: (kx, ky, kz, kw, data) of the frame's samples, kw scaled
+    by 1e6 / count (or 1 with reset_dens); data (C, M) complex64 or None."""
+    L = _lib.load()
+    gt = np.ascontiguousarray(gate_times, np.float64)
+    rw = None if rweight is None else np.ascontiguousarray(rweight, np.float32)
+    rwp = None if rw is None else rw.ctypes.data
+    ks = [np.ascontiguousarray(v, np.float32) for v in (kx, ky, kz, kw)]
+    n = ctypes.c_int64()
+    _lib.check(L.mrg_pregate(gt.ctypes.data, rwp, gt.size, int(nread), int(frame), int(bool(reset_dens)), None, None,
+                             None, None, None, 0, 0, None, None, None, None, None, 0, ctypes.byref(n)))
+    outs = [np.empty(n.value, np.float32) for _ in range(4)]
+    if data is not None:
+        d = np.ascontiguousarray(data, np.complex64).reshape(-1, ks[0].size)
+        od = np.empty((d.shape[0], n.value), np.complex64)
+        dp, odp, C = d.ctypes.data, od.ctypes.data, d.shape[0]
+    else:
+        d = od = None
+        dp = odp = None
+        C = 0
+    _lib.check(L.mrg_pregate(gt.ctypes.data, rwp, gt.size, int(nread), int(frame), int(bool(reset_dens)),
+                             *[k.ctypes.data for k in ks], dp, C, ks[0].size, *[o.ctypes.data for o in outs], odp,
+                             n.value, ctypes.byref(n)))
+    return tuple(outs) + (od,)
 
 
 def fista_params(**kw):

@@ -190,6 +190,27 @@ def nudft(img, kx, ky, kz, chunk=8192):
     return out
 
 
+def nudft_torch(imgs, kx, ky, kz, device, chunk=16384):
+    """nudft() of several images at once, evaluated in FP64 with torch on `device` (the same
+    separable contraction as nudft; used to synthesise test data quickly).  imgs: (C, Nz, Ny,
+    Nx).  Returns (C, M) complex128 numpy."""
+    import torch
+    im = torch.as_tensor(np.asarray(imgs), device=device).to(torch.complex128)
+    C, Nz, Ny, Nx = im.shape
+    M = kx.size
+    out = torch.zeros((C, M), dtype=torch.complex128, device=device)
+    r = [(torch.arange(n, dtype=torch.float64, device=device) - n / 2) / n for n in (Nx, Ny, Nz)]
+    imz = im.permute(1, 0, 2, 3).reshape(Nz, C * Ny * Nx)
+    k = [torch.as_tensor(np.asarray(v, dtype=np.float64), device=device) for v in (kx, ky, kz)]
+    for s in range(0, M, chunk):
+        e = min(M, s + chunk)
+        ph = [torch.exp(-2j * np.pi * torch.outer(k[d][s:e], r[d])) for d in range(3)]  # (m, N_d)
+        a = (ph[2] @ imz).reshape(e - s, C, Ny, Nx)           # sum over z
+        b = torch.einsum("mcyx,my->mcx", a, ph[1])             # sum over y
+        out[:, s:e] = torch.einsum("mcx,mx->cm", b, ph[0])     # sum over x
+    return out.cpu().numpy()
+
+
 def add_noise(y, level, seed):
     """Complex Gaussian noise with standard deviation level*max|y| per component."""
     g = _rng(seed)

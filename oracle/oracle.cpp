@@ -1753,6 +1753,41 @@ void orc_fista(void *hv, const OFrames *F, const OFistaParams *q, void **X, doub
   if (h->prec) run_fista<double>(h, *F, *q, X, resid, step, thr); else run_fista<float>(h, *F, *q, X, resid, step, thr);
 }
 // E^H W E per frame, summed over coils, accumulated into out.
+// GATING::hist_weight (gating.cpp:1130-1139) after the respiratory factor of
+// GATING::weight_data (gating.cpp:1080-1094), and RECON::pregate_data (recon_lib.cpp:675-776)
+// for one encode and frame: Kweight(i,j,k) = 1 * rweight(j,k) * (floor(gate_times(j,k)) == t),
+// the points with Kweight > 0 in (k, j, i) loop order, kw times Kw_Scale = 1e6/(float)count.
+// Returns the count; outputs may be NULL (count only).
+long orc_pregate(const double *gate_times, const float *rweight, long nreadouts, int nread, int t, int reset_dens,
+                 const float *kx, const float *ky, const float *kz, const float *kw, const void *data, int ncoil,
+                 long stride, float *kxo, float *kyo, float *kzo, float *kwo, void *datao, long ostride) {
+  std::vector<float> Kweight((size_t)nreadouts * nread, 1.0f);
+  for (long r = 0; r < nreadouts; r++)
+    for (int i = 0; i < nread; i++) {
+      float &w = Kweight[(size_t)r * nread + i];
+      if (rweight) w *= rweight[r];
+      w *= (std::floor(gate_times[r]) == t) ? (1.0) : (0.0);
+    }
+  int number_of_points = 0;
+  for (float w : Kweight)
+    if (w > 0) number_of_points++;
+  const float Kw_Scale = (1e6 / ((float)number_of_points));
+  if (!kxo) return number_of_points;
+  const cx<float> *d = (const cx<float> *)data;
+  cx<float> *o = (cx<float> *)datao;
+  long p = 0;
+  for (long s = 0; s < nreadouts * (long)nread; s++) {
+    if (!(Kweight[s] > 0)) continue;
+    kxo[p] = kx[s];
+    kyo[p] = ky[s];
+    kzo[p] = kz[s];
+    kwo[p] = reset_dens ? 1.0f : Kw_Scale * kw[s];
+    for (int c = 0; o && c < ncoil; c++) o[c * ostride + p] = d[c * stride + s];
+    p++;
+  }
+  return number_of_points;
+}
+
 // One CG iteration's vector updates on caller images (the CPU baseline's timing of them).
 double orc_cg_vectors(int Nt, long n, int Nz, void **X, void **R, void **P, void **L, int prec) {
   if (prec)

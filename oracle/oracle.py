@@ -83,6 +83,9 @@ def lib():
         L.orc_espirit.argtypes = [ctypes.POINTER(vp), ctypes.c_int, ip, fp, ip, ctypes.c_float, ctypes.c_int,
                                   ctypes.POINTER(vp), dp, dp]
         L.orc_glibc_rand.argtypes = [ctypes.c_long, ctypes.c_int, ip]
+        L.orc_pregate.restype = ctypes.c_long
+        L.orc_pregate.argtypes = [vp, vp, ctypes.c_long, ctypes.c_int, ctypes.c_int, ctypes.c_int] + [vp] * 5 + \
+            [ctypes.c_int, ctypes.c_long] + [vp] * 5 + [ctypes.c_long]
         L.orc_cg_vectors.restype = ctypes.c_double
         L.orc_cg_vectors.argtypes = [ctypes.c_int, ctypes.c_long, ctypes.c_int] + [ctypes.POINTER(vp)] * 4 + [ctypes.c_int]
         L.orc_num_threads.restype = ctypes.c_int
@@ -509,6 +512,23 @@ def glibc_rand(skip, n):
     out = (ctypes.c_int * n)()
     lib().orc_glibc_rand(skip, n, out)
     return np.array(out[:], dtype=np.int64)
+
+
+def pregate(gate_times, nread, t, kx, ky, kz, kw, data, rweight=None, reset_dens=False):
+    """RECON::pregate_data for one frame (see orc_pregate): (kx, ky, kz, kw, data)."""
+    gt = np.ascontiguousarray(gate_times, np.float64)
+    rw = None if rweight is None else np.ascontiguousarray(rweight, np.float32)
+    ks = [np.ascontiguousarray(v, np.float32) for v in (kx, ky, kz, kw)]
+    d = np.ascontiguousarray(data, np.complex64).reshape(-1, ks[0].size)
+    P = ctypes.c_void_p
+    rwp = None if rw is None else P(rw.ctypes.data)
+    n = lib().orc_pregate(P(gt.ctypes.data), rwp, gt.size, nread, t, int(reset_dens), *[P(k.ctypes.data) for k in ks],
+                          P(d.ctypes.data), d.shape[0], ks[0].size, None, None, None, None, None, 0)
+    outs = [np.empty(n, np.float32) for _ in range(4)]
+    od = np.empty((d.shape[0], n), np.complex64)
+    lib().orc_pregate(P(gt.ctypes.data), rwp, gt.size, nread, t, int(reset_dens), *[P(k.ctypes.data) for k in ks],
+                      P(d.ctypes.data), d.shape[0], ks[0].size, *[P(o.ctypes.data) for o in outs], P(od.ctypes.data), n)
+    return tuple(outs) + (od,)
 
 
 def cg_vectors(X, R, P, L):

@@ -11,14 +11,24 @@ def rel(a, b):
 
 
 def case(N=32, C=4, nproj=600, nread=None, seed=7, jitter=0.0, noise=0.01, ellipsoids=6, nudft=False):
-    """Phantom, coil maps, radial trajectory and k-space for one frame."""
+    """Phantom, coil maps, radial trajectory and k-space for one frame.  With nudft the
+    k-space is the FP64 direct NUDFT of the phantom times each map plus noise (evaluated
+    with torch on the GPU when there is one, else with numpy)."""
     nread = nread or N
     kx, ky, kz, kw = synth.radial_trajectory(N, nproj, nread, jitter_grid=jitter, seed=seed)
     img = synth.phantom(N, ellipsoids, seed=seed)
     smaps = synth.coil_maps(N, C, seed=seed + 1)
     rng = np.random.default_rng(seed)
     if nudft:
-        data = np.stack([synth.nudft(img * smaps[c], kx, ky, kz) for c in range(C)]).astype(np.complex64)
+        try:
+            import torch
+            gpu = torch.cuda.is_available()
+        except ImportError:
+            gpu = False
+        if gpu:
+            data = synth.nudft_torch(img[None] * smaps, kx, ky, kz, "cuda").astype(np.complex64)
+        else:
+            data = np.stack([synth.nudft(img * smaps[c], kx, ky, kz) for c in range(C)]).astype(np.complex64)
         data = synth.add_noise(data, noise, seed + 2)
     else:
         data = (rng.standard_normal((C, kx.size)) + 1j * rng.standard_normal((C, kx.size))).astype(np.complex64)

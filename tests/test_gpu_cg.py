@@ -15,14 +15,17 @@ def _cg_case(N, C, nproj, nread, seed):
     return c
 
 
-def _run(mrg_lib, oracle_lib, N, C, nproj, nread, iters, seed=5, use_graph=True):
+def _run(mrg_lib, oracle_lib, N, C, nproj, nread, iters, seed=5, use_graph=True, nudft=False):
     import torch
     from mri_recon_gb300 import synth
-    c = case(N=N, C=C, nproj=nproj, nread=nread, seed=seed)
+    c = case(N=N, C=C, nproj=nproj, nread=nread, seed=seed, nudft=nudft, ellipsoids=10 if nudft else 6)
     O64 = oracle_lib.Plan(N, prec=1)
     a = (c["kx"], c["ky"], c["kz"], c["kw"])
-    y = np.stack([O64.forward(c["img"], c["smaps"][k], *a) for k in range(C)]).astype(np.complex64)
-    y = synth.add_noise(y, 0.01, seed)
+    if nudft:  # FP64 direct NUDFT of the phantom times each map, 1% noise (helpers.case)
+        y = c["data"]
+    else:
+        y = np.stack([O64.forward(c["img"], c["smaps"][k], *a) for k in range(C)]).astype(np.complex64)
+        y = synth.add_noise(y, 0.01, seed)
     p = mrg_lib.Plan(N, C, 1)
     p.set_traj(0, *a)
     p.set_smaps(torch.from_numpy(c["smaps"]).cuda())
@@ -43,8 +46,10 @@ def test_cg_small_matches_oracle(mrg_lib, oracle_lib, use_graph):
 
 
 def test_cg_64cube_8coils_20iters(mrg_lib, oracle_lib):
-    """The SENSE-CG configuration at 64^3 x 8 coils, 4096 x 64 radial, 20 iterations."""
-    X, r, X32, r32, X64, r64 = _run(mrg_lib, oracle_lib, 64, 8, 4096, 64, 20)
+    """The SENSE-CG configuration at its stated size and iteration count: 64^3 x 8 coils,
+    4096 x 64 radial, 20 iterations, k-space from an FP64 direct NUDFT of a 10-ellipsoid
+    phantom times Gaussian coil maps plus 1% noise."""
+    X, r, X32, r32, X64, r64 = _run(mrg_lib, oracle_lib, 64, 8, 4096, 64, 20, nudft=True)
     e64, e32 = rel(X, X64), rel(X, X32)
     print("cg64 rel-L2 vs FP64 oracle %.3g, vs FP32 oracle %.3g, FP32 oracle vs FP64 %.3g" % (e64, e32, rel(X32, X64)))
     assert e64 < TOL_ITER

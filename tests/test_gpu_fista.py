@@ -73,21 +73,26 @@ def test_llr_blocks_match_oracle(mrg_lib, oracle_lib):
     assert rel(Y, np.stack(refY)) < 1e-5
 
 
-def _fista_inputs(N, C, T, nproj, seed):
+def _fista_inputs(N, C, T, nproj, seed, ellipsoids=6):
+    """Per-frame trajectories (projection counts `nproj`, one per frame or one for all, frames
+    interleaved by golden-means rotation) and ellipsoid phantoms modulated per frame."""
     from mri_recon_gb300 import synth
     frames = []
     smaps = synth.coil_maps(N, C, seed=seed)
+    counts = list(nproj) if np.ndim(nproj) else [nproj] * T
+    start = 0
     for t in range(T):
-        kx, ky, kz, kw = synth.radial_trajectory(N, nproj, N, start=t * nproj)
-        img = synth.phantom(N, 6, seed=seed, frame=t, nframes=max(T, 1))
+        kx, ky, kz, kw = synth.radial_trajectory(N, int(counts[t]), N, start=start)
+        start += int(counts[t])
+        img = synth.phantom(N, ellipsoids, seed=seed, frame=t, nframes=max(T, 1))
         frames.append(dict(kx=kx, ky=ky, kz=kz, kw=kw, img=img))
     return frames, smaps
 
 
-def _run_fista(mrg_lib, oracle_lib, N, C, T, nproj, iters, llr_alpha=0.0, use_graph=True, seed=21):
+def _run_fista(mrg_lib, oracle_lib, N, C, T, nproj, iters, llr_alpha=0.0, use_graph=True, seed=21, ellipsoids=6):
     import torch
     from mri_recon_gb300 import synth
-    frames, smaps = _fista_inputs(N, C, T, nproj, seed)
+    frames, smaps = _fista_inputs(N, C, T, nproj, seed, ellipsoids)
     O64 = oracle_lib.Plan(N, prec=1)
     for fr in frames:
         a = (fr["kx"], fr["ky"], fr["kz"], fr["kw"])
@@ -127,3 +132,123 @@ def test_fista_with_llr_matches_oracle(mrg_lib, oracle_lib):
     print("fista+llr rel-L2 vs FP64 %.3g vs FP32 %.3g" % (rel(X, X64), rel(X, X32)))
     assert rel(X, X64) < 1e-4
     assert rel(X, X32) < 1e-4
+
+
+def test_fista_100_iterations_db4(mrg_lib, oracle_lib):
+    """The FISTA L1-wavelet configuration at its stated iteration count and transform: 100
+    iterations, Daubechies-4 with 3 levels, 4 cycle spins, fraction threshold 0.1, 8 coils
+    (at 48^3 with 1800 x 48 radial, 4x below Nyquist like the 128^3 x 16384 x 128 case)."""
+    X, r, s, X32, r32, s32, X64, r64, s64 = _run_fista(mrg_lib, oracle_lib, 48, 8, 1, 1800, 100, ellipsoids=10)
+    e64, e32 = rel(X, X64), rel(X, X32)
+    print("fista 48^3 x 8, 100 it: rel-L2 vs FP64 %.3g, vs FP32 %.3g, FP32 vs FP64 %.3g" % (e64, e32, rel(X32, X64)))
+    assert abs(s - s64) / s64 < 1e-5
+    assert e64 < 1e-4
+    assert e32 < 1e-4
+
+
+def test_fista_llr_uneven_frames(mrg_lib, oracle_lib):
+    """The gated low-rank configuration's structure: 10 frames with uneven projection counts
+    (the 1500-3500 per frame of 128^3 scaled by (32/128)^2), 8^3 blocks, clear_alpha_time
+    0.001, 4 block iterations, frame intensities modulated by a sinusoid."""
+    from mri_recon_gb300 import synth
+    counts = synth.frame_projection_counts(10, 94, 219, seed=1237)
+    assert counts.min() != counts.max()
+    X, r, s, X32, r32, s32, X64, r64, s64 = _run_fista(mrg_lib, oracle_lib, 32, 4, 10, counts, 10, llr_alpha=0.001)
+    e64, e32 = rel(X, X64), rel(X, X32)
+    print("fista+llr 10 uneven frames: rel-L2 vs FP64 %.3g, vs FP32 %.3g" % (e64, e32))
+    assert e64 < 1e-4
+    assert e32 < 1e-4
+
+
+def _early_stop_index(resid, rng_, thresh):
+    """Iteration count at which the reference's early-stop rule ends the loop
+    (src/recon_lib.cpp:2081-2087, :2154-2163), restated on the host."""
+    diffs = []
+    for it, r in enumerate(resid):
+        diffs.append(np.float32(abs(r) / resid[0]))
+        if len(diffs) > rng_:
+            diffs.pop(0)
+        if len(diffs) == rng_:
+            mean = np.float32(sum(float(v) for v in diffs) / len(diffs))
+            sq = np.float32(sum(float(v) * float(v) for v in diffs))
+            sd = np.sqrt(np.float32(sq / np.float32(len(diffs)) - mean * mean))
+            if sd < thresh:
+                return it + 1
+    return len(resid)
+
+
+@pytest.mark.parametrize("use_graph", [True, False])
+def test_fista_early_stop(mrg_lib, use_graph):
+    import torch
+    c = case(N=32, C=4, nproj=900, seed=31)
+    p = mrg_lib.Plan(32, 4, 1)
+    p.set_traj(0, c["kx"], c["ky"], c["kz"], c["kw"])
+    p.set_smaps(torch.from_numpy(c["smaps"]).cuda())
+    p.set_data(0, torch.from_numpy(c["data"]).cuda())
+    base = dict(max_iter=12, max_eig_iter=10, cycle_spins=2, wave_levels=(2, 2, 2), wave_type=1, thresh=0.1,
+                use_threshold=1)
+    X_full, r_full, _ = p.fista(mrg_lib.fista_params(**base), use_graph=use_graph)
+    X_full = X_full.cpu().numpy()
+    assert p.last_iterations() == 12 and len(r_full) == 12
+    # a threshold that fires as soon as the window is full
+    X3, r3, _ = p.fista(mrg_lib.fista_params(early_stop_thresh=10.0, early_stop_range=3, **base),
+                        use_graph=use_graph)
+    assert p.last_iterations() == 3 and len(r3) == 3
+    np.testing.assert_allclose(r3, r_full[:3], rtol=1e-12)
+    X_three, _, _ = p.fista(mrg_lib.fista_params(**dict(base, max_iter=3)), use_graph=use_graph)
+    assert rel(X3.cpu().numpy(), X_three.cpu().numpy()) < 1e-6
+    # a threshold between two of the window's standard deviations stops where the host rule says
+    sds = []
+    for it in range(4, 12):
+        w = (np.abs(r_full[it - 4:it + 1]) / r_full[0]).astype(np.float32).astype(np.float64)
+        sds.append(float(np.std(w)))
+    sds = sorted(set(sds))
+    thr = float(np.float32(0.5 * (sds[len(sds) // 2 - 1] + sds[len(sds) // 2])))  # between two window values
+    want = _early_stop_index(r_full, 5, np.float32(thr))
+    _, rs, _ = p.fista(mrg_lib.fista_params(early_stop_thresh=thr, early_stop_range=5, **base), use_graph=use_graph)
+    assert p.last_iterations() == want == len(rs)
+    assert 5 <= want <= 12
+    # a range below 1 is rejected
+    from mri_recon_gb300 import _lib
+    with pytest.raises(_lib.MrgError):
+        p.fista(mrg_lib.fista_params(early_stop_thresh=0.1, early_stop_range=0, **base))
+
+
+def test_pregated_frames_fista_llr(mrg_lib, oracle_lib):
+    """Frames cut from one acquisition by the library's pregate (time gating of each readout,
+    uneven frame sizes, kw scaled by 1e6 / count), then FISTA + low rank in time on the GPU
+    against the oracle on the same frames."""
+    import torch
+    from mri_recon_gb300 import synth
+    N, C, T, nproj = 24, 3, 4, 1600
+    kx, ky, kz, kw = synth.radial_trajectory(N, nproj, N)
+    rng = np.random.default_rng(5)
+    gate = np.sort(rng.uniform(0, T, nproj)) ** 1.3 / T ** 0.3   # readout times, frames of uneven size
+    smaps = synth.coil_maps(N, C, seed=8)
+    img = synth.phantom(N, 6, seed=8)
+    O64 = oracle_lib.Plan(N, prec=1)
+    y = np.stack([O64.forward(img, smaps[c], kx, ky, kz, kw) for c in range(C)]).astype(np.complex64)
+    frames, counts = [], []
+    for t in range(T):
+        fx, fy, fz, fw, fd = mrg_lib.pregate(gate, N, t, kx, ky, kz, kw, y)
+        frames.append(dict(kx=fx, ky=fy, kz=fz, kw=fw, data=fd))
+        counts.append(fx.size)
+    assert len(set(counts)) == T and sum(counts) == kx.size
+    p = mrg_lib.Plan(N, C, T)
+    for t, fr in enumerate(frames):
+        p.set_traj(t, fr["kx"], fr["ky"], fr["kz"], fr["kw"])
+        p.set_data(t, torch.from_numpy(fr["data"]).cuda())
+    p.set_smaps(torch.from_numpy(smaps).cuda())
+    kwp = dict(max_iter=4, max_eig_iter=20, cycle_spins=2, wave_levels=(2, 2, 2), wave_type=1, thresh=0.1,
+               use_threshold=1, llr_block=(8, 8, 8), llr_block_iter=2, llr_alpha=0.05)
+    X, _, step = p.fista(mrg_lib.fista_params(**kwp))
+    q = oracle_lib.FistaParams()
+    q.max_iter, q.max_eig_iter, q.cycle_spins = 4, 20, 2
+    q.wave_levels[:] = [2, 2, 2]
+    q.wave_type, q.thresh, q.use_threshold = 1, 0.1, 1
+    q.llr_bs[:] = [8, 8, 8]
+    q.llr_block_iter, q.llr_alpha, q.clear_amp, q.clear_t2 = 2, 0.05, 4.0, 6.0
+    q.rand_skip = 2 * N ** 3 * T
+    X64, _, s64, _ = O64.fista(frames, smaps, q)
+    assert abs(step - s64) / s64 < 1e-5
+    assert rel(X.cpu().numpy(), np.stack(X64)) < 1e-4

@@ -302,3 +302,40 @@ def test_fft3_against_cufft(mrg_lib, N, sign):
     e64 = float(torch.linalg.norm(got - ref64) / torch.linalg.norm(ref64))
     e32 = float(torch.linalg.norm(ref32 - ref64) / torch.linalg.norm(ref64))
     assert e64 < max(1e-6, 2 * e32), (e64, e32)
+
+
+@pytest.mark.parametrize("kernel,overgrid,dwin,N,C", [(1, 1.5, -1.0, 32, 4), (0, 1.0, 1.0, 32, 2), (1, 1.5, -1.0, 24, 8)])
+def test_grid_and_ungrid_on_a_caller_grid(mrg_lib, oracle_lib, kernel, overgrid, dwin, N, C):
+    """chop_grid_forward / chop_grid_backward on a caller grid (mrg_grid / mrg_ungrid), per
+    coil against the oracle; the triangle kernel at overgrid 1.0 and half width 1 is the
+    setting of RECON::kspace_residual (src/recon_lib.cpp:2218-2252)."""
+    import torch
+    c = case(N=N, C=C, nproj=500, seed=41)
+    a = (c["kx"], c["ky"], c["kz"], c["kw"])
+    p = mrg_lib.Plan(N, C, 2, kernel_type=kernel, overgrid=overgrid, dwin=dwin)
+    e = edge_trajectory(N)
+    p.set_traj(0, *a)
+    p.set_traj(1, *e)
+    o = oracle_lib.Plan(N, kernel=kernel, overgrid=overgrid, dwin=dwin)
+    G = p.grid(0, torch.from_numpy(c["data"]).cuda()).cpu().numpy()
+    for k in range(C):
+        assert rel(G[..., k], o.grid(c["data"][k], *a)) < 1e-5
+    Gh = p.grid(0, c["data"])  # host buffers
+    assert rel(Gh, G) < 1e-6
+    rng = np.random.default_rng(42)
+    grid = (rng.standard_normal(G.shape) + 1j * rng.standard_normal(G.shape)).astype(np.complex64)
+    y = p.ungrid(0, torch.from_numpy(grid).cuda()).cpu().numpy()
+    yd = p.ungrid(0, grid, diff=c["data"])
+    for k in range(C):
+        ref = o.ungrid(np.ascontiguousarray(grid[..., k]), *a)
+        assert rel(y[k], ref) < 1e-5
+        assert rel(yd[k], o.ungrid(np.ascontiguousarray(grid[..., k]), *a, diff=c["data"][k])) < 1e-5
+    # edge samples: outside the grid, kw == 0, half-integer positions
+    de = (rng.standard_normal((C, e[0].size)) + 1j * rng.standard_normal((C, e[0].size))).astype(np.complex64)
+    Ge = p.grid(1, de)
+    ye = p.ungrid(1, grid)
+    for k in range(C):
+        assert rel(Ge[..., k], o.grid(de[k], *e)) < 1e-5
+        r = o.ungrid(np.ascontiguousarray(grid[..., k]), *e)
+        assert rel(ye[k], r) < 1e-5
+        assert np.array_equal(ye[k] == 0, r == 0)

@@ -136,3 +136,61 @@ def test_new_entry_points_reject_bad_arguments_without_a_gpu(mrg_lib):
     assert L.mrg_espirit(None, 4, 4, 4, 4, ctypes.byref(ep), ptr, None, None, 0, None) == 1
     assert L.mrg_espirit_smaps(None, 0, ptr, 0, ctypes.byref(ep), None, None, 0, None, None) == 1
     assert L.mrg_fft3(None, ptr, -1, None) == 1
+
+
+def test_low_rank_entry_points_reject_empty_blocks_without_a_gpu(mrg_lib):
+    """A block edge below 1 is an argument error (status 1), not an integer division by
+    zero in the block count or the shift draw (src/clear.cpp:408-410 takes rand() % block)."""
+    L = mrg_lib.load()
+    ip3 = (ctypes.c_int * 3)
+    buf = np.zeros(2 * 8 ** 3, np.complex64)
+    ptr = ctypes.c_void_p(buf.ctypes.data)
+    v = ctypes.c_float()
+    for block in [(0, 8, 8), (8, 0, 8), (8, 8, -1)]:
+        assert L.mrg_llr_update_threshold(ptr, 2, 8, 8, 8, ip3(*block), 4.0, 6.0, 0, ctypes.byref(v), None) == 1
+        assert L.mrg_llr_thresh(ptr, 2, 8, 8, 8, ip3(*block), 4, 0.1, 1.0, 0, None) == 1
+        assert L.mrg_llr_update_threshold_noalloc(ptr, 2, 8, 8, 8, ip3(*block), 4.0, 6.0, 0, ctypes.byref(v),
+                                                  None) == 1
+
+
+def test_plan_calls_reject_a_null_plan_without_a_gpu(mrg_lib):
+    L = mrg_lib.load()
+    n = ctypes.c_int()
+    assert L.mrg_set_wait_limit(None, 1.0) == 1
+    assert L.mrg_plan_check(None, None) == 1
+    assert L.mrg_last_iterations(None, ctypes.byref(n)) == 1
+    from mri_recon_gb300 import _lib
+    f = _lib.MrgFistaParams()
+    L.mrg_fista_params_default(ctypes.byref(f))
+    assert f.early_stop_thresh == 0.0 and f.early_stop_range == 5  # src/recon_lib.cpp:84-85
+
+
+def test_gating_weights_and_pregate_match_oracle(mrg_lib, oracle_lib):
+    """GATING::hist_weight with the respiratory factor, and RECON::pregate_data for each
+    frame, from the library's host code against the oracle's restatement: bit for bit."""
+    from mri_recon_gb300 import synth
+    rng = np.random.default_rng(21)
+    nproj, nread, T = 700, 16, 10
+    kx, ky, kz, kw = synth.radial_trajectory(32, nproj, nread)
+    gate = rng.uniform(0, T, nproj)
+    gate[:7] = [0.0, 1.0, 2.999999, 9.0, 9.999, -0.5, 10.0]   # integers, edges, outside [0, T)
+    rweight = rng.uniform(0, 1, nproj).astype(np.float32)
+    rweight[::9] = 0.0
+    data = (rng.standard_normal((3, kx.size)) + 1j * rng.standard_normal((3, kx.size))).astype(np.complex64)
+    total = 0
+    for rw in (None, rweight):
+        for reset in (False, True):
+            for t in list(range(T)) + [T, -1]:
+                got = mrg_lib.pregate(gate, nread, t, kx, ky, kz, kw, data, rweight=rw, reset_dens=reset)
+                want = oracle_lib.pregate(gate, nread, t, kx, ky, kz, kw, data, rweight=rw, reset_dens=reset)
+                for g_, w_ in zip(got, want):
+                    assert g_.shape == w_.shape and np.array_equal(g_, w_)
+                if rw is None and not reset and 0 <= t < T:
+                    total += got[0].size
+    # without respiratory weights every readout in [0, T) lands in exactly one frame
+    assert total == nread * int(np.sum((np.floor(gate) >= 0) & (np.floor(gate) < T)))
+    # the time weight of the non-pregated loops
+    for t in (0, 3):
+        w = mrg_lib.gate_weights(gate, kw, nread, t, rweight=rweight)
+        mask = np.repeat(rweight * (np.floor(gate) == t), nread).astype(np.float32)
+        assert np.array_equal(w, kw * mask)

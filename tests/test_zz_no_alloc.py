@@ -58,3 +58,26 @@ def test_noalloc_rejects_what_it_cannot_hold(mrg_lib):
     assert L.mrg_llr_update_threshold_noalloc(ctypes.c_void_p(Xd.data_ptr()), 1, 512, 256, 512, _ip((1, 1, 1)), 4.0,
                                               6.0, 0, ctypes.byref(v), None) == 6
     assert b"exceed the limit" in L.mrg_last_error()
+    # one block past the limit: 33 x 993 x 1 blocks of one voxel = 32769
+    assert L.mrg_llr_update_threshold_noalloc(ctypes.c_void_p(Xd.data_ptr()), 1, 33, 993, 1, _ip((1, 1, 1)), 4.0,
+                                              6.0, 0, ctypes.byref(v), None) == 6
+    # 2^16 x 2^16 x 2^16 blocks: 2^48, which a 32-bit count would have wrapped to 0
+    assert L.mrg_llr_update_threshold_noalloc(ctypes.c_void_p(Xd.data_ptr()), 1, 65536, 65536, 65536,
+                                              _ip((1, 1, 1)), 4.0, 6.0, 0, ctypes.byref(v), None) == 6
+    # a block edge below 1
+    assert L.mrg_llr_update_threshold_noalloc(ctypes.c_void_p(Xd.data_ptr()), 1, 8, 8, 8, _ip((0, 8, 8)), 4.0,
+                                              6.0, 0, ctypes.byref(v), None) == 1
+
+
+def test_noalloc_at_the_limit_then_smaller(mrg_lib):
+    """Exactly MRG_NOALLOC_MAX_BLOCKS blocks (64^3 in 2^3 blocks, 2 frames) fill the sort
+    buffer to its end; a smaller call right after must not see the larger call's leftovers."""
+    import torch
+    L = mrg_lib.load()
+    rng = np.random.default_rng(77)
+    for nframes, N, block, it in [(2, 64, (2, 2, 2), 1), (6, 32, (8, 8, 8), 0), (2, 64, (2, 2, 2), 5)]:
+        X = rng.standard_normal((nframes, N, N, N)) + 1j * rng.standard_normal((nframes, N, N, N))
+        Xd = torch.from_numpy(X.astype(np.complex64)).cuda()
+        ref, got = _both(L, Xd, nframes, N, block, it)
+        assert ref > 0
+        assert abs(got - ref) <= 1e-6 * ref, (nframes, N, block, got, ref)
