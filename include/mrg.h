@@ -258,8 +258,9 @@ typedef struct mrg_fista_params {
   int cycle_spins;       /* -cycle_spins (default 4) */
   int wave_levels[3];    /* -wavelet_levelsX/Y/Z (default 4) */
   int wave_type;         /* 0 DB2, 1 DB4 (-wavelet_type, default DB4) */
-  float thresh;          /* -thresh: fraction of coefficients set to zero */
-  int use_threshold;     /* -threshold_type fraction (1) or none (0) */
+  float thresh;          /* -thresh: fraction of coefficients set to zero (fraction), or the
+                            threshold value (fixed) */
+  int use_threshold;     /* -threshold_type: none (0), fraction (1) or fixed (2) */
   int llr_block[3];      /* -clear_nx/ny/nz (default 4) */
   int llr_block_iter;    /* -clear_block_iter (default 4) */
   float llr_alpha;       /* -clear_alpha_time (0: off) */
@@ -421,6 +422,29 @@ mrg_status mrg_pregate(const double *gate_times, const float *rweight, int64_t n
                        int reset_dens, const float *kx, const float *ky, const float *kz, const float *kw,
                        const void *data, int ncoil, int64_t coil_stride, float *kx_out, float *ky_out, float *kz_out,
                        float *kw_out, void *data_out, int64_t out_stride, int64_t *count);
+
+/* Reader of the reference's k-space files (MRI_DATA::read_external_data,
+ * src/mri_data.cpp:769-906) without the HDF5 library: the subset of the HDF5 format they use
+ * (superblocks 0-3, symbol-table and compact link groups, object headers 1 and 2,
+ * contiguous and compact datasets of little-endian integers, IEEE floats and (real, imag)
+ * float compounds, scalar attributes).  Chunked / compressed datasets and dense groups
+ * return MRG_ERR_UNSUPPORTED.  Host-only except mrg_h5_load_encode.
+ *   mrg_h5_attr_int: an integer attribute of a group ("Kdata", "Num_Coils");
+ *   mrg_h5_dataset_info: rank and dimensions (HDF5 order: the slowest first) of a dataset;
+ *   mrg_h5_read: a whole dataset converted to float32 (complex_out = 0) or complex64, n
+ *     elements, into a host buffer;
+ *   mrg_h5_mri_info: Num_Encodings, Num_Coils and the samples per encode (size of KX_E<e>,
+ *     up to max_encodings of them);
+ *   mrg_h5_load_encode: KX/KY/KZ/KW_E<e> and KData_E<e>_C<c> of one encode read into pinned
+ *     host memory and set as a plan frame's trajectory and data (mrg_set_traj, mrg_set_data). */
+typedef struct mrg_h5 mrg_h5;
+mrg_status mrg_h5_open(const char *path, mrg_h5 **out);
+mrg_status mrg_h5_close(mrg_h5 *h);
+mrg_status mrg_h5_attr_int(mrg_h5 *h, const char *group, const char *name, int *value);
+mrg_status mrg_h5_dataset_info(mrg_h5 *h, const char *path, int *rank, int64_t dims[8], int *is_complex);
+mrg_status mrg_h5_read(mrg_h5 *h, const char *path, int complex_out, void *dst, int64_t n);
+mrg_status mrg_h5_mri_info(mrg_h5 *h, int *num_encodings, int *num_coils, int64_t *samples, int max_encodings);
+mrg_status mrg_h5_load_encode(mrg_h5 *h, int encode, mrg_plan *plan, int frame, void *stream);
 
 /* Host-only: n values of the glibc rand() stream for the default seed after `skip`
  * draws, the source of the reference's wavelet and block shifts

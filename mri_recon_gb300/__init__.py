@@ -8,4 +8,4 @@ from . import synth  # noqa: F401
 from ._lib import LIB_PATH, MrgError, load  # noqa: F401
 from .gridfft import (KAISER_KERNEL, POLY_KERNEL, SINC_KERNEL, TRIANGLE_KERNEL, Plan, clear_combine,  # noqa: F401
                       clear_params, clear_thresh, clear_update_threshold, dcf_pipe, espirit, espirit_params,
-                      fista_params, gate_weights, gaussian_blur, gridFFT, pregate, sos_normalize)
+                      fista_params, gate_weights, gaussian_blur, gridFFT, H5File, pregate, sos_normalize)

@@ -113,6 +113,13 @@ SIGNATURES = {
     "mrg_gate_weights": (_i, [_vp, _vp, _i64, _i, _i, _vp, _vp]),
     "mrg_pregate": (_i, [_vp, _vp, _i64, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _i, _i64, _vp, _vp, _vp, _vp, _vp,
                          _i64, ctypes.POINTER(_i64)]),
+    "mrg_h5_open": (_i, [ctypes.c_char_p, ctypes.POINTER(_vp)]),
+    "mrg_h5_close": (_i, [_vp]),
+    "mrg_h5_attr_int": (_i, [_vp, ctypes.c_char_p, ctypes.c_char_p, _ip]),
+    "mrg_h5_dataset_info": (_i, [_vp, ctypes.c_char_p, _ip, ctypes.POINTER(_i64), _ip]),
+    "mrg_h5_read": (_i, [_vp, ctypes.c_char_p, _i, _vp, _i64]),
+    "mrg_h5_mri_info": (_i, [_vp, _ip, _ip, ctypes.POINTER(_i64), _i]),
+    "mrg_h5_load_encode": (_i, [_vp, _i, _vp, _i, _vp]),
     "mrg_grid": (_i, [_vp, _i, _vp, _i64, _vp, _vp]),
     "mrg_ungrid": (_i, [_vp, _i, _vp, _vp, _i64, _vp, _vp]),
     "mrg_set_wait_limit": (_i, [_vp, ctypes.c_double]),

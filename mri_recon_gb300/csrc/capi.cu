@@ -223,17 +223,20 @@ static mrg_status ensure_y(mrg_plan *p, int64_t n) {
   return MRG_OK;
 }
 
-static int pass_ib(int64_t inner, int C) {
-  if (C > 32) return 32;
-  return C * (32 / C);
+// Default lines per CTA of a pass of length S: a multiple of C up to the kernel's limit
+// (32, or 16 for lines above 384 points).
+static int pass_ib(int64_t inner, int C, int S) {
+  const int m = fft_max_lines_per_cta(S);
+  if (C > m) return m;
+  return C * (m / C);
 }
 
 // Lines per CTA of FFT pass k (0-2: E z/y/x, 3-5: E^H x/y/z): the autotuned value
 // when it is valid for this pass, else the default (a multiple of C, up to 32).
-static int plan_ib(const mrg_plan *p, int k, int64_t inner, int C, bool accum) {
-  const int def = pass_ib(inner, C);
+static int plan_ib(const mrg_plan *p, int k, int64_t inner, int C, bool accum, int S) {
+  const int def = pass_ib(inner, C, S);
   const int v = p->fft_ib[k];
-  if (v <= 0 || v == def) return def;
+  if (v <= 0 || v == def || v > fft_max_lines_per_cta(S)) return def;
   if (accum && (v % C) != 0) return def;  // the coil sum must stay inside a CTA
   if (v % 2) return def;
   return v;
@@ -297,7 +300,7 @@ static mrg_status run_E_grid_zxy(mrg_plan *p, const float2 *X, const float2 *sma
   // z pass with set_image (src/gridFFT.cpp:972-986 + fft3 along z)
   a.S = (int)Sz; a.sign = -1; a.mode = FFT_SETIMG;
   a.Lin = (int)Nz; a.in_off = g.og[2]; a.Lout = (int)Sz; a.out_off = 0;
-  a.inner = (int)(Nx * C); a.IB = plan_ib(p, 0, a.inner, C, false); a.lfast = 0;
+  a.inner = (int)(Nx * C); a.IB = plan_ib(p, 0, a.inner, C, false, a.S); a.lfast = 0;
   a.nlines = Ny * Nx * C;
   a.in_ls = Nx * Ny * C; a.in_os = Nx * C; a.out_ls = Ny * Nx * C; a.out_os = Nx * C;
   a.scale = (float)(1. / std::sqrt((float)Sz));
@@ -312,7 +315,7 @@ static mrg_status run_E_grid_zxy(mrg_plan *p, const float2 *X, const float2 *sma
   memset(&b, 0, sizeof(b));
   b.S = (int)Sy; b.sign = -1; b.mode = FFT_PLAIN;
   b.Lin = (int)Ny; b.in_off = g.og[1]; b.Lout = (int)Sy; b.out_off = 0;
-  b.inner = (int)(Nx * C); b.IB = plan_ib(p, 1, b.inner, C, false);
+  b.inner = (int)(Nx * C); b.IB = plan_ib(p, 1, b.inner, C, false, b.S);
   b.nlines = Sz * Nx * C;
   b.in_ls = Nx * C; b.in_os = Ny * Nx * C; b.out_ls = Nx * C; b.out_os = Sy * Nx * C;
   b.scale = (float)(1. / std::sqrt((float)Sy));
@@ -325,7 +328,7 @@ static mrg_status run_E_grid_zxy(mrg_plan *p, const float2 *X, const float2 *sma
   memset(&c, 0, sizeof(c));
   c.S = (int)Sx; c.sign = -1; c.mode = FFT_PLAIN;
   c.Lin = (int)Nx; c.in_off = g.og[0]; c.Lout = (int)Sx; c.out_off = 0;
-  c.inner = C; c.IB = (C == 1) ? pass_ib(C, C) : plan_ib(p, 2, C, C, false); c.lfast = (C == 1);
+  c.inner = C; c.IB = (C == 1) ? pass_ib(C, C, c.S) : plan_ib(p, 2, C, C, false, c.S); c.lfast = (C == 1);
   c.nlines = Sz * Sy * C;
   c.in_ls = C; c.in_os = Nx * C; c.out_ls = C; c.out_os = Sx * C;
   c.scale = (float)(1. / std::sqrt((float)Sx));
@@ -350,7 +353,7 @@ static mrg_status run_EH_xy(mrg_plan *p, const FrameTraj &ft, const float2 *y, c
   memset(&a, 0, sizeof(a));
   a.S = (int)Sx; a.sign = +1; a.mode = FFT_PLAIN;
   a.Lin = (int)Sx; a.in_off = 0; a.Lout = (int)Nx; a.out_off = g.og[0];
-  a.inner = C; a.IB = (C == 1) ? pass_ib(C, C) : plan_ib(p, 3, C, C, false); a.lfast = (C == 1);
+  a.inner = C; a.IB = (C == 1) ? pass_ib(C, C, a.S) : plan_ib(p, 3, C, C, false, a.S); a.lfast = (C == 1);
   a.nlines = Sz * Sy * C;
   a.in_ls = C; a.in_os = Sx * C; a.out_ls = C; a.out_os = Nx * C;
   a.scale = (float)(1. / std::sqrt((float)Sx));
@@ -362,7 +365,7 @@ static mrg_status run_EH_xy(mrg_plan *p, const FrameTraj &ft, const float2 *y, c
   memset(&b, 0, sizeof(b));
   b.S = (int)Sy; b.sign = +1; b.mode = FFT_PLAIN;
   b.Lin = (int)Sy; b.in_off = 0; b.Lout = (int)Ny; b.out_off = g.og[1];
-  b.inner = (int)(Nx * C); b.IB = plan_ib(p, 4, b.inner, C, false);
+  b.inner = (int)(Nx * C); b.IB = plan_ib(p, 4, b.inner, C, false, b.S);
   b.nlines = Sz * Nx * C;
   b.in_ls = Nx * C; b.in_os = Sy * Nx * C; b.out_ls = Nx * C; b.out_os = Ny * Nx * C;
   b.scale = (float)(1. / std::sqrt((float)Sy));
@@ -385,7 +388,7 @@ static mrg_status run_EH_xyz(mrg_plan *p, const FrameTraj &ft, const float2 *y, 
   memset(&c, 0, sizeof(c));
   c.S = (int)Sz; c.sign = +1; c.mode = FFT_ACCUM;
   c.Lin = (int)Sz; c.in_off = 0; c.Lout = (int)Nz; c.out_off = g.og[2];
-  c.inner = (int)(Nx * C); c.IB = plan_ib(p, 5, c.inner, C, true);
+  c.inner = (int)(Nx * C); c.IB = plan_ib(p, 5, c.inner, C, true, c.S);
   c.nlines = Ny * Nx * C;
   c.in_ls = Ny * Nx * C; c.in_os = Nx * C; c.out_ls = Nx * Ny * C; c.out_os = Nx * C;
   c.scale = (float)(1. / std::sqrt((float)Sz));
@@ -410,7 +413,7 @@ static mrg_status run_EH_crop_xyz(mrg_plan *p, const FrameTraj &ft, const float2
   memset(&c, 0, sizeof(c));
   c.S = (int)Sz; c.sign = +1; c.mode = FFT_PLAIN;
   c.Lin = (int)Sz; c.in_off = 0; c.Lout = (int)Nz; c.out_off = g.og[2];
-  c.inner = (int)(Nx * C); c.IB = plan_ib(p, 5, c.inner, C, false);
+  c.inner = (int)(Nx * C); c.IB = plan_ib(p, 5, c.inner, C, false, c.S);
   c.nlines = Ny * Nx * C;
   c.in_ls = Ny * Nx * C; c.in_os = Nx * C; c.out_ls = Ny * Nx * C; c.out_os = Nx * C;
   c.scale = (float)(1. / std::sqrt((float)Sz));
@@ -435,7 +438,7 @@ static mrg_status run_E_grid(mrg_plan *p, const float2 *X, const float2 *smap, c
   // x pass with set_image (src/gridFFT.cpp:972-986 + fft3 along x), input pruned to the crop
   a.S = (int)Sx; a.sign = -1; a.mode = FFT_SETIMG;
   a.Lin = (int)Nx; a.in_off = g.og[0]; a.Lout = (int)Sx; a.out_off = 0;
-  a.inner = C; a.IB = plan_ib(p, 0, C, C, false); a.lfast = 0;
+  a.inner = C; a.IB = plan_ib(p, 0, C, C, false, a.S); a.lfast = 0;
   a.nlines = Nz * Ny * C;
   a.in_ls = C; a.in_os = Nx * C; a.out_ls = C; a.out_os = Sx * C;
   a.scale = (float)(1. / std::sqrt((float)Sx));
@@ -450,7 +453,7 @@ static mrg_status run_E_grid(mrg_plan *p, const float2 *X, const float2 *smap, c
   memset(&b, 0, sizeof(b));
   b.S = (int)Sz; b.sign = -1; b.mode = FFT_PLAIN;
   b.Lin = (int)Nz; b.in_off = g.og[2]; b.Lout = (int)Sz; b.out_off = 0;
-  b.inner = (int)(Ny * Sx * C); b.IB = plan_ib(p, 1, b.inner, C, false);
+  b.inner = (int)(Ny * Sx * C); b.IB = plan_ib(p, 1, b.inner, C, false, b.S);
   b.nlines = Ny * Sx * C;
   b.in_ls = Ny * Sx * C; b.in_os = 0; b.out_ls = Ny * Sx * C; b.out_os = 0;
   b.scale = (float)(1. / std::sqrt((float)Sz));
@@ -464,7 +467,7 @@ static mrg_status run_E_grid(mrg_plan *p, const float2 *X, const float2 *smap, c
   memset(&c, 0, sizeof(c));
   c.S = (int)Sy; c.sign = -1; c.mode = FFT_PLAIN;
   c.Lin = (int)Ny; c.in_off = g.og[1]; c.Lout = (int)Sy; c.out_off = 0;
-  c.inner = (int)(Sx * C); c.IB = plan_ib(p, 2, c.inner, C, false);
+  c.inner = (int)(Sx * C); c.IB = plan_ib(p, 2, c.inner, C, false, c.S);
   c.nlines = Sz * Sx * C;
   c.in_ls = Sx * C; c.in_os = Ny * Sx * C; c.out_ls = Sx * C; c.out_os = Sy * Sx * C;
   c.scale = (float)(1. / std::sqrt((float)Sy));
@@ -490,7 +493,7 @@ static mrg_status run_EH_yz(mrg_plan *p, const FrameTraj &ft, const float2 *y, c
   memset(&a, 0, sizeof(a));
   a.S = (int)Sy; a.sign = +1; a.mode = FFT_PLAIN;
   a.Lin = (int)Sy; a.in_off = 0; a.Lout = (int)Ny; a.out_off = g.og[1];
-  a.inner = (int)(Sx * C); a.IB = plan_ib(p, 3, a.inner, C, false);
+  a.inner = (int)(Sx * C); a.IB = plan_ib(p, 3, a.inner, C, false, a.S);
   a.nlines = Sz * Sx * C;
   a.in_ls = Sx * C; a.in_os = Sy * Sx * C; a.out_ls = Sx * C; a.out_os = Ny * Sx * C;
   a.scale = (float)(1. / std::sqrt((float)Sy));
@@ -503,7 +506,7 @@ static mrg_status run_EH_yz(mrg_plan *p, const FrameTraj &ft, const float2 *y, c
   memset(&b, 0, sizeof(b));
   b.S = (int)Sz; b.sign = +1; b.mode = FFT_PLAIN;
   b.Lin = (int)Sz; b.in_off = 0; b.Lout = (int)Nz; b.out_off = g.og[2];
-  b.inner = (int)(Ny * Sx * C); b.IB = plan_ib(p, 4, b.inner, C, false);
+  b.inner = (int)(Ny * Sx * C); b.IB = plan_ib(p, 4, b.inner, C, false, b.S);
   b.nlines = Ny * Sx * C;
   b.in_ls = Ny * Sx * C; b.in_os = 0; b.out_ls = Ny * Sx * C; b.out_os = 0;
   b.scale = (float)(1. / std::sqrt((float)Sz));
@@ -528,7 +531,7 @@ static mrg_status run_EH(mrg_plan *p, const FrameTraj &ft, const float2 *y, cons
   memset(&c, 0, sizeof(c));
   c.S = (int)Sx; c.sign = +1; c.mode = FFT_ACCUM;
   c.Lin = (int)Sx; c.in_off = 0; c.Lout = (int)Nx; c.out_off = g.og[0];
-  c.inner = C; c.IB = plan_ib(p, 5, C, C, true);
+  c.inner = C; c.IB = plan_ib(p, 5, C, C, true, c.S);
   c.nlines = Nz * Ny * C;
   c.in_ls = C; c.in_os = Sx * C; c.out_ls = C; c.out_os = Nx * C;
   c.scale = (float)(1. / std::sqrt((float)Sx));
@@ -554,7 +557,7 @@ static mrg_status run_EH_crop(mrg_plan *p, const FrameTraj &ft, const float2 *y,
   memset(&c, 0, sizeof(c));
   c.S = (int)Sx; c.sign = +1; c.mode = FFT_PLAIN;
   c.Lin = (int)Sx; c.in_off = 0; c.Lout = (int)Nx; c.out_off = g.og[0];
-  c.inner = C; c.IB = (C == 1) ? pass_ib(C, C) : plan_ib(p, 5, C, C, false); c.lfast = (C == 1);
+  c.inner = C; c.IB = (C == 1) ? pass_ib(C, C, c.S) : plan_ib(p, 5, C, C, false, c.S); c.lfast = (C == 1);
   c.nlines = Nz * Ny * C;
   c.in_ls = C; c.in_os = Sx * C; c.out_ls = C; c.out_os = Nx * C;
   c.scale = (float)(1. / std::sqrt((float)Sx));
@@ -1245,7 +1248,7 @@ mrg_status mrg_fft3(mrg_plan *p, void *grid, int sign, void *stream) {
     memset(&a, 0, sizeof(a));
     a.S = (int)S; a.sign = sign; a.mode = FFT_PLAIN;
     a.Lin = (int)S; a.in_off = 0; a.Lout = (int)S; a.out_off = 0;
-    a.inner = inner; a.IB = pass_ib(inner, C); a.lfast = 0;
+    a.inner = inner; a.IB = pass_ib(inner, C, a.S); a.lfast = 0;
     a.nlines = outer * inner;
     a.in_ls = ls; a.in_os = S * ls; a.out_ls = ls; a.out_os = S * ls;
     a.scale = (float)(1. / std::sqrt((float)S));
@@ -1687,7 +1690,8 @@ static mrg_status fista_iteration(mrg_plan *p, const FistaCtx &f, cudaStream_t s
     for (int spin = 0; spin < q.cycle_spins; spin++) {
       MRG_TRY(wavelet3d_ex(X, p->T, f.N, f.L, f.max_level, p->d_wshift, p->d_sc, 3 * q.cycle_spins, 3 * spin,
                            q.wave_type, 0, st));
-      if (spin == 0) MRG_TRY(fraction_threshold(X, nt, q.thresh, scale, p->thr, p->d_thr, st));
+      // a fixed threshold (use_threshold 2) was written to d_thr once, before the loop
+      if (spin == 0 && q.use_threshold == 1) MRG_TRY(fraction_threshold(X, nt, q.thresh, scale, p->thr, p->d_thr, st));
       MRG_TRY(soft_threshold(X, nt, p->d_thr, st));
       MRG_TRY(wavelet3d_ex(X, p->T, f.N, f.L, f.max_level, p->d_wshift, p->d_sc, 3 * q.cycle_spins, 3 * spin,
                            q.wave_type, 1, st));
@@ -1705,6 +1709,10 @@ extern "C" mrg_status mrg_fista(mrg_plan *p, const mrg_fista_params *q, void *X,
   }
   if (q->use_threshold && (q->cycle_spins < 1 || q->wave_type < 0 || q->wave_type > 1)) {
     set_error("bad wavelet / cycle-spin parameters");
+    return MRG_ERR_INVALID;
+  }
+  if (q->use_threshold < 0 || q->use_threshold > 2) {
+    set_error("use_threshold must be 0 (none), 1 (fraction) or 2 (fixed)");
     return MRG_ERR_INVALID;
   }
   if (q->llr_alpha > 0.0f && (q->llr_block_iter < 1 || q->llr_block[0] < 1 || q->llr_block[1] < 1 || q->llr_block[2] < 1)) {
@@ -1767,7 +1775,14 @@ extern "C" mrg_status mrg_fista(mrg_plan *p, const mrg_fista_params *q, void *X,
   MRG_CUDA(cudaMemcpyAsync(p->d_wshift, wsh.data(), sizeof(int) * wsh.size(), cudaMemcpyHostToDevice, st));
   MRG_CUDA(cudaMemcpyAsync(p->d_lshift, lsh.data(), sizeof(int) * lsh.size(), cudaMemcpyHostToDevice, st));
   if (!p->d_thr) MRG_CUDA(cudaMalloc(&p->d_thr, sizeof(float)));
-  if (q->use_threshold) MRG_TRY(thr_alloc(p->thr, nt));
+  if (q->use_threshold == 1) MRG_TRY(thr_alloc(p->thr, nt));
+  if (q->use_threshold == 2) {
+    // THRESHOLD::update_threshold, TH_FIXED: global_threshold = thresh * scale with the cycle-spin
+    // scale 1/cycle_spins passed as float (src/threshold.cpp:196-198, src/recon_lib.cpp:2499-2501)
+    const float scale = (float)(1.0 / (float)q->cycle_spins);
+    const float fixed = (float)((double)q->thresh * (double)scale);
+    MRG_CUDA(cudaMemcpy(p->d_thr, &fixed, sizeof(float), cudaMemcpyHostToDevice));
+  }
   void *dX;
   bool sX;
   MRG_TRY(dev_view(p, 0, X, sizeof(float2) * nt, false, st, &dX, &sX));

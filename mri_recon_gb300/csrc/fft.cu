@@ -11,13 +11,19 @@ namespace mrg {
 // even, so every N up to 256 has its length here
 static const int kSupportedQ[] = {2,  3,  4,  5,  6,  8,  9,  10, 12, 14, 15, 16, 18, 20, 22, 24, 26,
                                   28, 30, 32, 34, 36, 38, 40, 42, 44, 45, 46, 48};
+// lines of 400..768 points: S = 16 Q (fft_long.cu)
+static const int kLongQ[] = {25, 26, 27, 28, 30, 32, 33, 34, 35, 36, 38, 39, 40, 42, 44, 45, 46, 48};
 
 bool fft_size_supported(int S) {
   if (S % 8) return false;
   for (int q : kSupportedQ)
     if (q * 8 == S) return true;
+  for (int q : kLongQ)
+    if (q * 16 == S) return true;
   return false;
 }
+
+int fft_max_lines_per_cta(int S) { return S > 384 ? 16 : 32; }
 
 // Per-size twiddle tables exp(-2 pi i m / S), m < S, built once on each device (a table
 // lives in the memory of the device it was built on).
@@ -32,8 +38,10 @@ mrg_status fft_init_device() {
     return MRG_ERR_UNSUPPORTED;
   }
   return device_once(g_tw_once, [dev]() -> mrg_status {
-    for (int q : kSupportedQ) {
-      const int S = 8 * q;
+    std::vector<int> sizes;
+    for (int q : kSupportedQ) sizes.push_back(8 * q);
+    for (int q : kLongQ) sizes.push_back(16 * q);
+    for (int S : sizes) {
       std::vector<float2> tw(S);
       for (int m = 0; m < S; m++) {
         const double a = -2.0 * 3.141592653589793238462643 * (double)m / (double)S;
@@ -110,6 +118,7 @@ mrg_status launch_fft(const FftPass &p, cudaStream_t st) {
     case 360:
     case 384: return launch_fft_320_384(p, st);
     default:
+      if (p.S > 384) return launch_fft_long(p, st);
       set_error("unsupported FFT length " + std::to_string(p.S));
       return MRG_ERR_UNSUPPORTED;
   }

@@ -9,10 +9,11 @@
 // dropped inputs are zero and the dropped outputs are never read.
 //
 // One CTA transforms IB lines (consecutive "inner" elements, coalesced rows of
-// IB complex values) of length S = 8*Q held in shared memory as [S][IB+1].
-// Each line is split S = 8 x Q (four-step): 8-point DFTs across the 8 threads
+// IB complex values) of length S = R*Q held in shared memory as [S][IB+1].
+// Each line is split S = R x Q (four-step): R-point DFTs across the R threads
 // of a line, a twiddle, then a Q-point DFT in registers per thread (radices 2,
-// 3, 4, 5 and direct DFTs of larger primes).  Twiddles exp(-2 pi i m / S) are computed on the host in double,
+// 3, 4, 5 and direct DFTs of larger primes).  R = 8 up to 384 points; longer lines
+// (N > 256 at the default 1.5x) take R = 16, so Q stays within the registers.  Twiddles exp(-2 pi i m / S) are computed on the host in double,
 // staged in shared memory per CTA and read as broadcasts.
 #pragma once
 
@@ -27,9 +28,10 @@ namespace mrg {
 constexpr int kTwDevices = 64;
 const float2 *fft_twiddles(int S);
 
-// lengths 192..288 (fft_large.cu) and 320..384 (fft_large2.cu)
+// lengths 192..288 (fft_large.cu), 320..384 (fft_large2.cu) and 400..768 (fft_long.cu)
 mrg_status launch_fft_192_288(const FftPass &p, cudaStream_t st);
 mrg_status launch_fft_320_384(const FftPass &p, cudaStream_t st);
+mrg_status launch_fft_long(const FftPass &p, cudaStream_t st);
 
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
@@ -179,16 +181,16 @@ __device__ __forceinline__ float elem_weight(const FftPass &p, float lw, float w
 // P: shared-memory row pitch when it is a compile-time constant (IB = P lines, no
 // padding), else 0 (pitch and IB from the pass).  With P fixed every shared-memory
 // address in the transform steps is the thread's base plus a constant.
-template <int Q, int SIGN, int MODE, int P>
+template <int Q, int SIGN, int MODE, int P, int R = 8>
 __global__ void __launch_bounds__(256, 2) k_fft(const FftPass p) {
-  constexpr int S = 8 * Q;
+  constexpr int S = R * Q;
   extern __shared__ float2 sm[];  // [S][IBp] data, then S twiddles
   const int IB = P ? P : p.IB;
   const int IBp = P ? P : (p.lfast ? p.IB + 1 : p.IB);  // pad only for column-wise (contiguous-line) access
   const int tid = threadIdx.x;
   float2 *tw = sm + S * (IB + 1);
   for (int m = tid; m < S; m += blockDim.x) tw[m] = p.tw[m];
-  const int j = tid % IB, t = tid / IB;  // 8 threads per line
+  const int j = tid % IB, t = tid / IB;  // R threads per line
   // Line (o, i) of the CTA's IB lines.  When inner % IB == 0 (nib = inner / IB) every line
   // of the CTA shares o and one 32-bit division per thread finds it.
   int64_t o0 = 0, i0 = 0;
@@ -250,12 +252,12 @@ __global__ void __launch_bounds__(256, 2) k_fft(const FftPass p) {
         const int64_t ib = o * p.in_os + i;
         const float lw = line_weight(p, o, i);
         const int64_t xb = ib / p.C, xs = p.in_ls / p.C;  // X has no coil axis
-        for (int l0 = t; l0 < p.Lin; l0 += 64) {
+        for (int l0 = t; l0 < p.Lin; l0 += 8 * R) {
           float2 xv[8];
           float wv[8];
 #pragma unroll
           for (int k = 0; k < 8; k++) {  // 8 independent loads in flight
-            const int li = l0 + 8 * k;
+            const int li = l0 + R * k;
             if (li < p.Lin) {
               xv[k] = __ldg(p.X + xb + (int64_t)li * xs);
               wv[k] = __ldg(p.wl + li);
@@ -263,7 +265,7 @@ __global__ void __launch_bounds__(256, 2) k_fft(const FftPass p) {
           }
 #pragma unroll
           for (int k = 0; k < 8; k++) {
-            const int li = l0 + 8 * k;
+            const int li = l0 + R * k;
             if (li < p.Lin) {
               const float w = elem_weight(p, lw, wv[k], o, i);
               float2 *d = col + (li + p.in_off) * IBp;
@@ -276,7 +278,7 @@ __global__ void __launch_bounds__(256, 2) k_fft(const FftPass p) {
     }
   } else if (!p.lfast) {
     const int64_t ib = o * p.in_os + i;
-    for (int r = t; r < S; r += 8) {
+    for (int r = t; r < S; r += R) {
       float2 v = make_float2(0.f, 0.f);
       const int li = r - p.in_off;
       if (lv && li >= 0 && li < p.Lin) {
@@ -308,21 +310,21 @@ __global__ void __launch_bounds__(256, 2) k_fft(const FftPass p) {
     __syncthreads();
   }
 
-  // ---- step A: 8-point DFTs over n1 (rows Q*n1 + n2), twiddle W_S^(n2*k1) ----
-  for (int n2 = t; n2 < Q; n2 += 8) {
-    float2 a[8];
+  // ---- step A: R-point DFTs over n1 (rows Q*n1 + n2), twiddle W_S^(n2*k1) ----
+  for (int n2 = t; n2 < Q; n2 += R) {
+    float2 a[R];
     float2 *c2 = col + n2 * IBp;
 #pragma unroll
-    for (int n1 = 0; n1 < 8; n1++) a[n1] = c2[Q * n1 * IBp];
-    reg_fft<8, SIGN, S>(a, tw);
+    for (int n1 = 0; n1 < R; n1++) a[n1] = c2[Q * n1 * IBp];
+    reg_fft<R, SIGN, S>(a, tw);
 #pragma unroll
-    for (int k1 = 1; k1 < 8; k1++) a[k1] = cmul(a[k1], twid<SIGN>(tw, n2 * k1));
+    for (int k1 = 1; k1 < R; k1++) a[k1] = cmul(a[k1], twid<SIGN>(tw, n2 * k1));
 #pragma unroll
-    for (int k1 = 0; k1 < 8; k1++) c2[Q * k1 * IBp] = a[k1];
+    for (int k1 = 0; k1 < R; k1++) c2[Q * k1 * IBp] = a[k1];
   }
   __syncthreads();
 
-  // ---- step C: Q-point DFT of rows Q*t .. Q*t+Q-1 -> rows t + 8*k2 ----
+  // ---- step C: Q-point DFT of rows Q*t .. Q*t+Q-1 -> rows t + R*k2 ----
   {
     float2 v[Q];
     const float2 *cq = col + Q * t * IBp;
@@ -332,7 +334,7 @@ __global__ void __launch_bounds__(256, 2) k_fft(const FftPass p) {
     __syncthreads();
     float2 *ct = col + t * IBp;
 #pragma unroll
-    for (int k2 = 0; k2 < Q; k2++) ct[8 * k2 * IBp] = v[k2];
+    for (int k2 = 0; k2 < Q; k2++) ct[R * k2 * IBp] = v[k2];
   }
   __syncthreads();
 
@@ -365,7 +367,7 @@ __global__ void __launch_bounds__(256, 2) k_fft(const FftPass p) {
     } else if (!p.lfast) {
       if (lv) {
         const int64_t ob = o * p.out_os + i;
-        for (int r = t; r < p.Lout; r += 8) {
+        for (int r = t; r < p.Lout; r += R) {
           float2 v = col[(r + p.out_off) * IBp];
           p.out[ob + (int64_t)r * p.out_ls] = make_float2(v.x * p.scale, v.y * p.scale);
         }
@@ -387,12 +389,12 @@ __global__ void __launch_bounds__(256, 2) k_fft(const FftPass p) {
     if (lv) {
       const int64_t sb = o * p.out_os + i;
       const float lw = line_weight(p, o, i);
-      for (int r0 = t; r0 < p.Lout; r0 += 64) {
+      for (int r0 = t; r0 < p.Lout; r0 += 8 * R) {
         float2 sv[8];
         float wv[8];
 #pragma unroll
         for (int k = 0; k < 8; k++) {  // 8 independent smap loads in flight
-          const int r = r0 + 8 * k;
+          const int r = r0 + R * k;
           if (r < p.Lout) {
             sv[k] = p.has_smap ? __ldg(p.smap + sb + (int64_t)r * p.out_ls) : make_float2(1.f, 0.f);
             wv[k] = __ldg(p.wl + r);
@@ -400,7 +402,7 @@ __global__ void __launch_bounds__(256, 2) k_fft(const FftPass p) {
         }
 #pragma unroll
         for (int k = 0; k < 8; k++) {
-          const int r = r0 + 8 * k;
+          const int r = r0 + R * k;
           if (r >= p.Lout) continue;
           float2 v = col[(r + p.out_off) * IBp];
           v = make_float2(v.x * p.scale, v.y * p.scale);
@@ -551,17 +553,18 @@ constexpr bool fixed_pitch_q(int Q) {
   return Q == 24 || Q == 30 || Q == 32 || Q == 36 || Q == 40 || Q == 45 || Q == 48;
 }
 
-template <int Q, int P>
+template <int Q, int P, int R = 8>
 static mrg_status launch_qp(const FftPass &pp, const dim3 grid, const dim3 block, size_t smem, cudaStream_t st) {
   void (*fn)(const FftPass);
-  if (pp.mode == FFT_SETIMG) fn = k_fft<Q, -1, FFT_SETIMG, P>;
-  else if (pp.mode == FFT_ACCUM) fn = k_fft<Q, +1, FFT_ACCUM, P>;
-  else if (pp.sign < 0) fn = k_fft<Q, -1, FFT_PLAIN, P>;
-  else fn = k_fft<Q, +1, FFT_PLAIN, P>;
+  if (pp.mode == FFT_SETIMG) fn = k_fft<Q, -1, FFT_SETIMG, P, R>;
+  else if (pp.mode == FFT_ACCUM) fn = k_fft<Q, +1, FFT_ACCUM, P, R>;
+  else if (pp.sign < 0) fn = k_fft<Q, -1, FFT_PLAIN, P, R>;
+  else fn = k_fft<Q, +1, FFT_PLAIN, P, R>;
   static DeviceOnce once[4];  // per instantiation and mode: set the smem cap once on each device
   const int slot = pp.mode == FFT_PLAIN ? (pp.sign < 0 ? 0 : 1) : (pp.mode == FFT_SETIMG ? 2 : 3);
   MRG_TRY(device_once(once[slot], [fn]() -> mrg_status {
-    MRG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 8 * Q * 34 * (int)sizeof(float2)));
+    MRG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  R * Q * (256 / R + 2) * (int)sizeof(float2)));
     return MRG_OK;
   }));
   fn<<<grid, block, smem, st>>>(pp);
@@ -569,24 +572,28 @@ static mrg_status launch_qp(const FftPass &pp, const dim3 grid, const dim3 block
   return MRG_OK;
 }
 
-template <int Q>
+template <int Q, int R = 8>
 static mrg_status launch_q(const FftPass &p, cudaStream_t st) {
-  const size_t smem = (size_t)8 * Q * (p.IB + 2) * sizeof(float2);
+  if (p.IB * R > 256) {
+    set_error("fft pass: " + std::to_string(p.IB) + " lines per CTA exceed 256 threads for this length");
+    return MRG_ERR_INVALID;
+  }
+  const size_t smem = (size_t)R * Q * (p.IB + 2) * sizeof(float2);
   const int64_t nblk64 = (p.nlines + p.IB - 1) / p.IB;
   if (nblk64 > 0x7fffffff) {
     set_error("fft pass too large");
     return MRG_ERR_UNSUPPORTED;
   }
-  const dim3 grid((unsigned)nblk64), block(8 * p.IB);
+  const dim3 grid((unsigned)nblk64), block(R * p.IB);
   FftPass pp = p;
-  pp.tw = fft_twiddles(8 * Q);
+  pp.tw = fft_twiddles(R * Q);
   if (!pp.tw) {
     set_error("FFT twiddles not built on this device");
     return MRG_ERR_STATE;
   }
   // CTAs that never straddle an outer row find their row with one 32-bit division
   pp.nib = (p.inner % p.IB == 0 && p.nlines % p.inner == 0) ? (int)(p.inner / p.IB) : 0;
-  if constexpr (fixed_pitch_q(Q)) {
+  if constexpr (R == 8 && fixed_pitch_q(Q)) {
     // plain passes whose tiles never straddle an outer row and copy line pairs: persistent
     if (p.mode == FFT_PLAIN && !p.lfast && pp.nib && p.vec16 && p.nlines / p.IB <= 0x7fffffff &&
         (p.IB == 16 || p.IB == 32)) {
@@ -596,7 +603,7 @@ static mrg_status launch_q(const FftPass &p, cudaStream_t st) {
     if (!p.lfast && p.IB == 32) return launch_qp<Q, 32>(pp, grid, block, smem, st);
     if (!p.lfast && p.IB == 16) return launch_qp<Q, 16>(pp, grid, block, smem, st);
   }
-  return launch_qp<Q, 0>(pp, grid, block, smem, st);
+  return launch_qp<Q, 0, R>(pp, grid, block, smem, st);
 }
 
 }  // namespace mrg

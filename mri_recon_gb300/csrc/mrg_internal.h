@@ -132,6 +132,8 @@ struct FftPass {
   int64_t acc_l, acc_o;  // accumulator strides for l and o (i/C has stride 1)
 };
 bool fft_size_supported(int S);
+// Lines per CTA a pass of length S can take (16 threads per line above 384 points).
+int fft_max_lines_per_cta(int S);
 // Enables 16-byte line-pair copies when every stride, the line count and the pointers allow it.
 void fft_vectorize(FftPass &p);
 mrg_status fft_init_device();

@@ -600,6 +600,57 @@ def pregate(gate_times, nread, frame, kx, ky, kz, kw, data=None, rweight=None, r
     return tuple(outs) + (od,)
 
 
+class H5File:
+    """The reference's k-space file (MRI_DATA::read_external_data layout) through the library's
+    own HDF5 reader: attributes, datasets, and whole encodes loaded into a plan frame."""
+
+    def __init__(self, path):
+        h = ctypes.c_void_p()
+        _lib.check(_lib.load().mrg_h5_open(str(path).encode(), ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.load().mrg_h5_close(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def attr_int(self, group, name):
+        v = ctypes.c_int()
+        _lib.check(_lib.load().mrg_h5_attr_int(self._h, group.encode(), name.encode(), ctypes.byref(v)))
+        return v.value
+
+    def info(self, path):
+        """(dims in HDF5 order, is_complex)."""
+        r, cx = ctypes.c_int(), ctypes.c_int()
+        dims = (ctypes.c_int64 * 8)()
+        _lib.check(_lib.load().mrg_h5_dataset_info(self._h, path.encode(), ctypes.byref(r), dims, ctypes.byref(cx)))
+        return tuple(dims[:r.value]), bool(cx.value)
+
+    def read(self, path):
+        dims, cx = self.info(path)
+        out = np.empty(dims, np.complex64 if cx else np.float32)
+        _lib.check(_lib.load().mrg_h5_read(self._h, path.encode(), int(cx), out.ctypes.data, out.size))
+        return out
+
+    def mri_info(self):
+        ne, nc = ctypes.c_int(), ctypes.c_int()
+        _lib.check(_lib.load().mrg_h5_mri_info(self._h, ctypes.byref(ne), ctypes.byref(nc), None, 0))
+        m = (ctypes.c_int64 * max(ne.value, 1))()
+        _lib.check(_lib.load().mrg_h5_mri_info(self._h, None, None, m, ne.value))
+        return ne.value, nc.value, list(m[:ne.value])
+
+    def load_encode(self, encode, plan, frame, stream=None):
+        """KX/KY/KZ/KW_E<encode> and KData_E<encode>_C* into plan frame `frame` through pinned memory."""
+        _lib.check(_lib.load().mrg_h5_load_encode(self._h, int(encode), plan._h, int(frame), _stream(stream)))
+        plan.M[frame] = self.mri_info()[2][encode]
+
+
 def fista_params(**kw):
     p = _lib.MrgFistaParams()
     _lib.load().mrg_fista_params_default(ctypes.byref(p))

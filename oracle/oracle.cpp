@@ -1338,7 +1338,7 @@ struct OFistaParams {
   int wave_levels[3];
   int wave_type;       // 0 DB2, 1 DB4
   float thresh;        // fraction (-thresh)
-  int use_threshold;   // fraction thresholding on/off
+  int use_threshold;   // 0 none, 1 fraction, 2 fixed
   int llr_bs[3];
   int llr_block_iter;
   float llr_alpha;     // clear_alpha_time (0 = off)
@@ -1498,7 +1498,11 @@ static void run_fista(OHandle *h, const OFrames &F, const OFistaParams &q, void 
       for (int spin = 0; spin < q.cycle_spins; spin++) {
         wave.random_shift(rng);
         for (int t = 0; t < Nt; t++) wave.forward<R>(X[t]);
-        if (spin == 0) thr = (float)(1. / (float)q.cycle_spins) * get_threshold<R>(X, Nt, n, q.thresh, q.thresh);
+        if (spin == 0) {
+          const float scale = (float)(1. / (float)q.cycle_spins);
+          thr = (q.use_threshold == 2) ? (float)((double)q.thresh * (double)scale)  // TH_FIXED (threshold.cpp:196-198)
+                                       : scale * get_threshold<R>(X, Nt, n, q.thresh, q.thresh);
+        }
         for (int t = 0; t < Nt; t++) soft_threshold<R>(X[t], n, thr);
         for (int t = 0; t < Nt; t++) wave.backward<R>(X[t]);
       }

@@ -192,7 +192,9 @@ def test_errors_do_not_exit(mrg_lib):
     with pytest.raises(m.MrgError, match="STATE"):
         p.forward(0, c["X"])                       # no trajectory yet
     with pytest.raises(m.MrgError, match="UNSUPPORTED"):
-        m.Plan(300, 1, 1)                           # S = 464 = 8*58: lines longer than 384 not built
+        m.Plan(300, 1, 1)                           # S = 464 = 16*29: a prime factor above 23, not built
+    with pytest.raises(m.MrgError, match="UNSUPPORTED"):
+        m.Plan(520, 1, 1)                           # S = 784: lines above 768 points not built
 
 
 @pytest.mark.parametrize("grid_mode", [1, 2, 3])
@@ -339,3 +341,53 @@ def test_grid_and_ungrid_on_a_caller_grid(mrg_lib, oracle_lib, kernel, overgrid,
         r = o.ungrid(np.ascontiguousarray(grid[..., k]), *e)
         assert rel(ye[k], r) < 1e-5
         assert np.array_equal(ye[k] == 0, r == 0)
+
+
+@pytest.mark.parametrize("n", [257, 264, 320, 340, 384, 448, 512])
+@pytest.mark.parametrize("axis", [0, 1, 2])
+def test_long_lines_against_cufft(mrg_lib, n, axis):
+    """Lines above 384 points (N > 256 at the default 1.5x: 16 threads per line) along each
+    axis of the grid, forward and inverse, against cuFFT in double precision."""
+    torch = _torch()
+    N = [16, 24, 20]
+    N[axis] = n
+    C = 2
+    p = mrg_lib.Plan(tuple(N), C, 1)
+    assert p.S[axis] > 384
+    Sx, Sy, Sz = p.S
+    g = torch.randn((Sz, Sy, Sx, C), dtype=torch.complex64, device="cuda", generator=torch.Generator("cuda").manual_seed(n))
+    for sign in (-1, 1):
+        f = torch.fft.fftn if sign < 0 else torch.fft.ifftn
+        ref64 = f(g.to(torch.complex128), dim=(0, 1, 2), norm="ortho")
+        ref32 = f(g, dim=(0, 1, 2), norm="ortho")
+        got = p.fft3(g.clone(), sign)
+        e64 = float(torch.linalg.norm(got - ref64) / torch.linalg.norm(ref64))
+        e32 = float(torch.linalg.norm(ref32 - ref64) / torch.linalg.norm(ref64))
+        assert e64 < max(1e-6, 2 * e32), (n, axis, sign, e64, e32)
+
+
+@pytest.mark.parametrize("N,C", [((320, 24, 16), 3), ((16, 272, 24), 2), ((20, 16, 384), 9), ((400, 32, 32), 1)])
+def test_long_lines_operators_match_oracle(mrg_lib, oracle_lib, N, C):
+    """E and E^H with a grid axis above 384 points against the oracle (one coil: the
+    single-coil pass order; nine coils: the tensor-core gridding)."""
+    import torch
+    from mri_recon_gb300 import synth
+    rng = np.random.default_rng(3)
+    M = 30000
+    kx, ky, kz = [rng.uniform(-n / 2, n / 2, M).astype(np.float32) for n in N]
+    kw = (kx.astype(np.float64) ** 2 + ky ** 2 + kz ** 2).astype(np.float32)
+    ishape = (N[2], N[1], N[0])
+    X = (rng.standard_normal(ishape) + 1j * rng.standard_normal(ishape)).astype(np.complex64)
+    smaps = (rng.standard_normal((C,) + ishape) + 1j * rng.standard_normal((C,) + ishape)).astype(np.complex64)
+    d = (rng.standard_normal((C, M)) + 1j * rng.standard_normal((C, M))).astype(np.complex64)
+    p = mrg_lib.Plan(N, C, 1)
+    p.set_traj(0, kx, ky, kz, kw)
+    p.set_smaps(torch.from_numpy(smaps).cuda())
+    o = oracle_lib.Plan(N)
+    y = p.forward(0, torch.from_numpy(X).cuda()).cpu().numpy()
+    Xh = p.adjoint(0, d, np.zeros(ishape, np.complex64))
+    ref_h = np.zeros(ishape, np.complex64)
+    for k in range(C):
+        assert rel(y[k], o.forward(X, smaps[k], kx, ky, kz, kw)) < 1e-5
+        ref_h = o.adjoint(ref_h, smaps[k], d[k], kx, ky, kz, kw)
+    assert rel(Xh, ref_h) < 1e-5
