@@ -332,6 +332,36 @@ def caller_rows(p, img, c, dev, timed):
     return out
 
 
+def iteration_bytes(N, C, Ms, fista=None):
+    """Algorithmic HBM bytes of one iteration: per coil and frame of M samples one E^H W E
+    costs 24 N^3 + 56 S^3 + 16 M bytes (maps read twice and the crop once, the oversampled
+    grid written, transformed and read each way, samples written and read), plus per frame
+    the trajectory read once per direction and 9 image passes of the vector updates.  FISTA
+    adds per cycle spin a forward and an inverse wavelet (each level reads and writes its
+    sub-box along x, y and z) and a soft threshold, and per iteration one magnitude pass and
+    the bisection's counting passes (about 16) over 4-byte magnitudes.  fista: (spins,
+    levels) or None."""
+    S = 16 * int(np.ceil(1.5 * N / 16))
+    n3 = N ** 3
+    b = 0
+    for M in Ms:
+        b += C * (24 * n3 + 56 * S ** 3 + 16 * M) + 2 * 16 * M + 9 * 8 * n3
+    if fista:
+        spins, levels = fista
+        T = len(Ms)
+        wave = sum(3 * 2 * 8 * n3 / 8 ** l for l in range(levels))  # one direction, all levels
+        b += T * (spins * (2 * wave + 2 * 8 * n3) + 8 * n3 + 16 * 4 * n3)
+    return float(b)
+
+
+def with_roofline(row, bytes_per, per_second):
+    pk, kind = peaks()
+    row["roofline"] = {"bound": "hbm", "algorithmic_bytes_per_unit": bytes_per,
+                       "achieved_GBs": bytes_per * per_second / 1e9,
+                       "frac": bytes_per * per_second / 1e9 / pk, "peak": pk, "peak_source": kind}
+    return row
+
+
 def side_configs(dev, only=None, profile=False):
     """Throughput of the four smaller configurations, device-timed with inputs resident:
     SENSE-CG 64^3 x 8 (iter/s), FISTA-wavelet 128^3 x 16 (iter/s), FISTA-wavelet + time
@@ -383,8 +413,8 @@ def side_configs(dev, only=None, profile=False):
         p.cg_init(40, X)
         p.cg_iterate(3, X)
         dt = timed(lambda: p.cg_iterate(20, X))
-        out["cg64"] = {"metric": "SENSE-CG iter/s, 64^3 x 8 coils, 4096 x 64 radial", "value": 20 / dt,
-                       "unit": "iter/s"}
+        out["cg64"] = with_roofline({"metric": "SENSE-CG iter/s, 64^3 x 8 coils, 4096 x 64 radial", "value": 20 / dt,
+                                     "unit": "iter/s"}, iteration_bytes(64, 8, [4096 * 64]), 20 / dt)
         del p
 
     def fista_rate(p, **kw):
@@ -401,8 +431,11 @@ def side_configs(dev, only=None, profile=False):
     if want("fista128"):
         c = synth.CONFIGS["fista128"]
         p, img = setup(c, 1, [c["nproj"]])
-        out["fista128"] = {"metric": "FISTA-wavelet iter/s, 128^3 x 16 coils, 16384 x 128 radial, db4 3 levels, "
-                                     "4 cycle spins, fraction threshold 0.1", "value": fista_rate(p), "unit": "iter/s"}
+        rate = fista_rate(p)
+        out["fista128"] = with_roofline({"metric": "FISTA-wavelet iter/s, 128^3 x 16 coils, 16384 x 128 radial, db4 3 "
+                                                   "levels, 4 cycle spins, fraction threshold 0.1", "value": rate,
+                                         "unit": "iter/s"},
+                                        iteration_bytes(128, 16, [16384 * 128], fista=(4, 3)), rate)
         if only is None:
             out.update(caller_rows(p, img, c, dev, timed))
         del p
@@ -410,9 +443,12 @@ def side_configs(dev, only=None, profile=False):
         c = synth.CONFIGS["llr128"]
         projs = synth.frame_projection_counts(c["frames"], c["proj_lo"], c["proj_hi"], c["seed"])
         p, _ = setup(c, c["frames"], projs)
-        out["llr128"] = {"metric": "FISTA-wavelet + time low-rank iter/s, 128^3 x 20 coils x 10 frames "
-                                   "(1500-3500 projections each), 8^3 blocks", "unit": "iter/s",
-                         "value": fista_rate(p, llr_block=(8, 8, 8), llr_block_iter=4, llr_alpha=0.001)}
+        rate = fista_rate(p, llr_block=(8, 8, 8), llr_block_iter=4, llr_alpha=0.001)
+        # the low-rank step adds one read and write of the 10 frames per block pass (5 passes)
+        llr_b = iteration_bytes(128, 20, [int(n) * 128 for n in projs], fista=(4, 3)) + 5 * 2 * 8 * 128 ** 3 * 10
+        out["llr128"] = with_roofline({"metric": "FISTA-wavelet + time low-rank iter/s, 128^3 x 20 coils x 10 "
+                                                 "frames (1500-3500 projections each), 8^3 blocks", "unit": "iter/s",
+                                       "value": rate}, llr_b, rate)
         del p
     if want("grad96"):
         c = synth.CONFIGS["grad96"]
@@ -424,9 +460,12 @@ def side_configs(dev, only=None, profile=False):
                 p.grad(t, img, ys[t])
         grads()
         dt = timed(lambda: [grads() for _ in range(3)])
-        out["grad96"] = {"metric": "differentiable NUFFT evaluations/s (loss, image and trajectory gradients), "
-                                   "96^3 x 8 coils, 6000 x 96 jittered radial", "value": 3 * c["batch"] / dt,
-                         "unit": "evals/s"}
+        # one evaluation: E and E^H of one 96^3 x 8-coil frame (the operator bytes of one iteration
+        # without the CG vector passes) plus the gradient's extra trajectory and sample traffic
+        gb = iteration_bytes(96, 8, [6000 * 96]) - 9 * 8 * 96 ** 3 + 8 * 16 * 6000 * 96
+        out["grad96"] = with_roofline({"metric": "differentiable NUFFT evaluations/s (loss, image and trajectory "
+                                                 "gradients), 96^3 x 8 coils, 6000 x 96 jittered radial",
+                                       "value": 3 * c["batch"] / dt, "unit": "evals/s"}, gb, 3 * c["batch"] / dt)
         del p
     torch.cuda.synchronize()
     return out

@@ -286,3 +286,21 @@ def test_pregated_frames_fista_llr(mrg_lib, oracle_lib):
     X64, _, s64, _ = O64.fista(frames, smaps, q)
     assert abs(step - s64) / s64 < 1e-5
     assert rel(X.cpu().numpy(), np.stack(X64)) < 1e-4
+
+
+def test_llr_update_on_a_second_device(mrg_lib, oracle_lib):
+    """Kernel attributes (the low-rank kernel's shared-memory size) are set on every device a
+    process uses, not only the first: the update on device 1 after one on device 0."""
+    import torch
+    if torch.cuda.device_count() < 2:
+        pytest.skip("needs two visible GPUs")
+    X = _vols(13, 32, 14)  # 13 frames in 8^3 blocks: above 48 KiB of shared memory per block
+    L = _lib()
+    ref = oracle_lib.llr_update_threshold([X[t] for t in range(13)], (8, 8, 8), 4.0, 6.0, 1)
+    for dev in (0, 1):
+        with torch.cuda.device(dev):
+            Xd = torch.from_numpy(X).to("cuda:%d" % dev)
+            sm = ctypes.c_float()
+            assert L.mrg_llr_update_threshold(ctypes.c_void_p(Xd.data_ptr()), 13, 32, 32, 32, _ip((8, 8, 8)), 4.0, 6.0,
+                                              1, ctypes.byref(sm), None) == 0, L.mrg_last_error()
+            assert abs(sm.value - ref) / ref < 1e-5
