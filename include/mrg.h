@@ -122,6 +122,15 @@ mrg_status mrg_frame_tuning(const mrg_plan *plan, int frame, int out[5], float m
  * ungridding shape a buffer cannot take falls back to fewer coils per lane (4 coils per
  * lane needs a coil count divisible by 4 and 4 to 16 lanes; 2 needs an even count). */
 mrg_status mrg_frame_set_tuning(mrg_plan *plan, int frame, const int in[5]);
+/* FFT launch shapes of the plan (no counterpart in the reference, whose FFTW plans are
+ * opaque): per pass k (0-2: E's x/set_image, z, y; 3-5: E^H's y, z, x/accumulate) the
+ * lines per CTA ib[k] (0: the default, a multiple of the coil count up to 32) and xp[k] (1:
+ * the persistent set_image / accumulate kernel of the x passes of multi-coil plans, used
+ * where the pass's strides allow it).  The first mrg_set_traj of a plan tunes them by
+ * timing; mrg_set_fft_tuning fixes them afterwards (values a pass cannot take fall back
+ * to its default).  Either array may be NULL. */
+mrg_status mrg_fft_tuning(const mrg_plan *plan, int ib[6], int xp[6]);
+mrg_status mrg_set_fft_tuning(mrg_plan *plan, const int ib[6], const int xp[6]);
 
 /* Measured k-space of one frame: ncoil arrays of M complex64, coil c at
  * data + c*coil_stride.  Used by mrg_cg / mrg_fista (data.kdata, src/mri_data.h). */

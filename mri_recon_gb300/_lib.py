@@ -69,6 +69,8 @@ SIGNATURES = {
     "mrg_set_data": (_i, [_vp, _i, _vp, _i64, _vp]),
     "mrg_frame_tuning": (_i, [_vp, _i, _ip, _fp]),
     "mrg_frame_set_tuning": (_i, [_vp, _i, _ip]),
+    "mrg_fft_tuning": (_i, [_vp, _ip, _ip]),
+    "mrg_set_fft_tuning": (_i, [_vp, _ip, _ip]),
     "mrg_frame_info": (_i, [_vp, _i] + [ctypes.POINTER(_i64)] * 5),
     "mrg_adjoint": (_i, [_vp, _i, _vp, _i64, _vp, _vp]),
     "mrg_forward": (_i, [_vp, _i, _vp, _vp, _i64, _vp, _vp]),

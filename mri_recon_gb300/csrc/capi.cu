@@ -73,6 +73,7 @@ struct mrg_plan {
   float timings[8] = {0};
   int timing_on = 0, timing_calls = 0;
   int fft_ib[6] = {0, 0, 0, 0, 0, 0};  // lines per CTA per FFT pass (0: default)
+  int fft_xp[6] = {0, 0, 0, 0, 0, 0};  // persistent set_image / accumulate kernel per pass
   bool fft_tuned = false;
   cudaEvent_t tev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   int64_t graph_kernels = 0;  // kernels per replay of cg_exec
@@ -138,6 +139,11 @@ static mrg_status plan_check(mrg_plan *p, cudaStream_t st) {
   if (h) {
     MRG_CUDA(cudaMemsetAsync(p->d_err, 0, sizeof(int), st));
     MRG_CUDA(cudaStreamSynchronize(st));
+    if (h == MRG_REGION_RANGE) {
+      set_error("tensor-core gridding met a work item outside the grid and skipped it; results of the calls "
+                "since the last check are incomplete");
+      return MRG_ERR_CUDA;
+    }
     set_error("a bounded device-side wait ran out (tensor-core gridding gave up); results of the calls since "
               "the last check are incomplete");
     return MRG_ERR_TIMEOUT;
@@ -444,6 +450,7 @@ static mrg_status run_E_grid(mrg_plan *p, const float2 *X, const float2 *smap, c
   a.scale = (float)(1. / std::sqrt((float)Sx));
   a.in = smap; a.smap = smap; a.has_smap = smap != nullptr; a.X = X; a.out = p->d_t1;
   a.wmode = 1; a.wdiv = Ny; a.wl = wx + g.og[0]; a.wo = wz + g.og[2]; a.wi = wy + g.og[1]; a.C = C;
+  a.xp = p->fft_xp[0];
   tmark(p, 0, st);
   fft_vectorize(a);
   MRG_TRY(launch_fft(a, st));
@@ -538,6 +545,7 @@ static mrg_status run_EH(mrg_plan *p, const FrameTraj &ft, const float2 *y, cons
   c.in = p->d_t1; c.smap = smap; c.has_smap = smap != nullptr; c.acc = X;
   c.acc_atomic = (c.IB % C) != 0; c.acc_l = 1; c.acc_o = Nx;
   c.wmode = 1; c.wdiv = Ny; c.wl = wx + g.og[0]; c.wo = wz + g.og[2]; c.wi = wy + g.og[1]; c.C = C;
+  c.xp = p->fft_xp[5];
   fft_vectorize(c);
   MRG_TRY(launch_fft(c, st));
   tmark(p, 4, st);
@@ -591,9 +599,11 @@ extern "C" {
 static mrg_status ensure_solver(mrg_plan *p, bool fista);
 }
 
-// Picks 16 or 32 lines per CTA for each FFT pass by timing one E and one E^H of
-// this frame with each choice, using the per-stage event timing.  16 lines halve
-// a CTA's shared memory so more CTAs overlap their load, transform and store phases.
+// Picks 16 or 32 lines per CTA for each FFT pass, and for the x passes of multi-coil
+// plans the persistent set_image / accumulate kernels or the one-tile ones, by timing one
+// E and one E^H of this frame with each choice, using the per-stage event timing.  16
+// lines halve a CTA's shared memory so more CTAs overlap their load, transform and store
+// phases.
 static mrg_status tune_fft(mrg_plan *p, const FrameTraj &ft, cudaStream_t st) {
   if (p->C > 32 || ft.nvalid == 0) return MRG_OK;
   MRG_TRY(ensure_solver(p, false));
@@ -606,8 +616,13 @@ static mrg_status tune_fft(mrg_plan *p, const FrameTraj &ft, cudaStream_t st) {
     best[k] = 1e30f;
     pick[k] = 0;
   }
-  for (int cand : {0, 16}) {
-    for (int k = 0; k < 6; k++) p->fft_ib[k] = cand;
+  int pick_xp[6] = {0, 0, 0, 0, 0, 0};
+  for (int cand = 0; cand < 4; cand++) {
+    const int ib = (cand & 1) ? 16 : 0, xp = cand >> 1;
+    for (int k = 0; k < 6; k++) {
+      p->fft_ib[k] = ib;
+      p->fft_xp[k] = xp;
+    }
     MRG_TRY(mrg_set_timing(p, 1));
     for (int rep = 0; rep < 2; rep++) {
       MRG_TRY(run_E(p, ft, p->d_R, sm, nullptr, p->d_y, true, st));
@@ -619,10 +634,14 @@ static mrg_status tune_fft(mrg_plan *p, const FrameTraj &ft, cudaStream_t st) {
     for (int k = 0; k < 6; k++)
       if (t[idx[k]] < best[k]) {
         best[k] = t[idx[k]];
-        pick[k] = cand;
+        pick[k] = ib;
+        pick_xp[k] = xp;
       }
   }
-  for (int k = 0; k < 6; k++) p->fft_ib[k] = pick[k];
+  for (int k = 0; k < 6; k++) {
+    p->fft_ib[k] = pick[k];
+    p->fft_xp[k] = pick_xp[k];
+  }
   p->fft_tuned = true;
   return mrg_set_timing(p, was_on);
 }
@@ -892,6 +911,42 @@ mrg_status mrg_frame_tuning(const mrg_plan *p, int frame, int out[5], float ms[2
     ms[0] = ft.tune_ungrid_ms;
     ms[1] = ft.tune_grid_ms;
   }
+  return MRG_OK;
+}
+
+mrg_status mrg_fft_tuning(const mrg_plan *p, int ib[6], int xp[6]) {
+  if (!p) {
+    set_error("null plan");
+    return MRG_ERR_INVALID;
+  }
+  for (int k = 0; k < 6; k++) {
+    if (ib) ib[k] = p->fft_ib[k];
+    if (xp) xp[k] = p->fft_xp[k];
+  }
+  return MRG_OK;
+}
+
+mrg_status mrg_set_fft_tuning(mrg_plan *p, const int ib[6], const int xp[6]) {
+  if (!p) {
+    set_error("null plan");
+    return MRG_ERR_INVALID;
+  }
+  for (int k = 0; k < 6; k++) {
+    if (ib && (ib[k] < 0 || ib[k] > 32)) {
+      set_error("lines per CTA out of range (0..32)");
+      return MRG_ERR_INVALID;
+    }
+    if (xp && (xp[k] < 0 || xp[k] > 1)) {
+      set_error("xp must be 0 or 1");
+      return MRG_ERR_INVALID;
+    }
+  }
+  for (int k = 0; k < 6; k++) {
+    if (ib) p->fft_ib[k] = ib[k];
+    if (xp) p->fft_xp[k] = xp[k];
+  }
+  p->fft_tuned = true;
+  invalidate_graphs(p);
   return MRG_OK;
 }
 

@@ -527,6 +527,244 @@ __global__ void __launch_bounds__(8 * P) k_fft_pp(const FftPass p, int ntiles) {
   }
 }
 
+// Set-image x passes, persistent: the first pass of a multi-coil E, lines along x with the
+// coils innermost (inner == C == in_ls), so the IB lines of a tile are IB coils of one
+// image row o.  Tiles are walked as in k_fft_pp; beside a tile's maps the copies bring the
+// image row X[o][0..Lin), which becomes (w X)[l] in place once it has landed, w = (winz *
+// winy) * winx.  The 8-point step multiplies each map value by it as it reads the row
+// (src/gridFFT.cpp:972-986: image = (w X) smap).
+template <int Q, int P>
+__global__ void __launch_bounds__(8 * P) k_fft_ps(const FftPass p, int ntiles) {
+  constexpr int S = 8 * Q, IB = P, NPAIR = IB / 2;
+  extern __shared__ float2 sm[];  // [S][IB] data, S twiddles, S image row
+  float2 *tw = sm + S * (IB + 1);
+  float2 *xr = tw + S;
+  const int tid = threadIdx.x;
+  for (int m = tid; m < S; m += blockDim.x) tw[m] = p.tw[m];
+  const int j = tid % IB, t = tid / IB;
+  float2 *col = sm + j;
+  const int jp = tid % NPAIR, r0 = tid / NPAIR, rstep = blockDim.x / NPAIR;
+  const unsigned nib = (unsigned)p.nib;
+  const int64_t xos = p.in_os / p.C;  // image row pitch (X has no coil axis)
+  auto issue = [&](int tile) {
+    const unsigned ob = (unsigned)tile / nib;
+    const int64_t i0 = (int64_t)((unsigned)tile - ob * nib) * IB;
+    const float2 *gs = p.smap + (int64_t)ob * p.in_os + i0 + 2 * jp + (int64_t)r0 * p.in_ls;
+    const int64_t gstep = (int64_t)rstep * p.in_ls;
+    unsigned sa = (unsigned)__cvta_generic_to_shared(sm + (r0 + p.in_off) * IB + 2 * jp);
+    const unsigned sstep = (unsigned)(rstep * IB * (int)sizeof(float2));
+    for (int li = r0; li < p.Lin; li += rstep, gs += gstep, sa += sstep)
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gs));
+    const float2 *gx = p.X + (int64_t)ob * xos;
+    for (int li = tid; li < p.Lin; li += blockDim.x)
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"((unsigned)__cvta_generic_to_shared(xr + li)),
+                   "l"(gx + li));
+    for (int e = tid; e < (S - p.Lin) * IB; e += blockDim.x) {
+      const int jj = e % IB, k = e / IB;
+      const int r = (k < p.in_off) ? k : k + p.Lin;
+      sm[r * IB + jj] = make_float2(0.f, 0.f);
+    }
+    asm volatile("cp.async.commit_group;\n" ::);
+  };
+  int tile = blockIdx.x;
+  if (tile < ntiles) issue(tile);
+  for (; tile < ntiles; tile += gridDim.x) {
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    __syncthreads();
+    const unsigned ob = (unsigned)tile / nib;
+    {
+      const float lw = p.wo[(int64_t)ob / p.wdiv] * p.wi[(int64_t)ob % p.wdiv];  // winz * winy of the row
+      for (int li = tid; li < p.Lin; li += blockDim.x) {
+        const float w = lw * __ldg(p.wl + li);
+        const float2 x = xr[li];
+        xr[li] = make_float2(w * x.x, w * x.y);
+      }
+    }
+    __syncthreads();
+    // ---- step A with set_image: 8-point DFTs over n1 (rows Q*n1 + n2) ----
+    for (int n2 = t; n2 < Q; n2 += 8) {
+      float2 a[8];
+      float2 *c2 = col + n2 * IB;
+#pragma unroll
+      for (int n1 = 0; n1 < 8; n1++) {
+        a[n1] = c2[Q * n1 * IB];
+        const int li = Q * n1 + n2 - p.in_off;
+        if ((unsigned)li < (unsigned)p.Lin) a[n1] = cmul(xr[li], a[n1]);
+      }
+      reg_fft<8, -1, S>(a, tw);
+#pragma unroll
+      for (int k1 = 1; k1 < 8; k1++) a[k1] = cmul(a[k1], twid<-1>(tw, n2 * k1));
+#pragma unroll
+      for (int k1 = 0; k1 < 8; k1++) c2[Q * k1 * IB] = a[k1];
+    }
+    __syncthreads();
+    // ---- step C: rows into registers, then the next tile's copies ----
+    float2 v[Q];
+    const float2 *cq = col + Q * t * IB;
+#pragma unroll
+    for (int n2 = 0; n2 < Q; n2++) v[n2] = cq[n2 * IB];
+    __syncthreads();
+    if (tile + (int)gridDim.x < ntiles) issue(tile + gridDim.x);
+    reg_fft<Q, -1, S>(v, tw);
+    const int64_t i = (int64_t)((unsigned)tile - ob * nib) * IB + j;
+    float2 *go = p.out + (int64_t)ob * p.out_os + i;
+    const float sc = p.scale;
+#pragma unroll
+    for (int k2 = 0; k2 < Q; k2++) {
+      const int r = t + 8 * k2 - p.out_off;
+      if (r >= 0 && r < p.Lout) go[(int64_t)r * p.out_ls] = make_float2(v[k2].x * sc, v[k2].y * sc);
+    }
+  }
+}
+
+// Accumulate x passes, persistent: the last pass of a multi-coil E^H, lines along x with
+// one tile = the C coils of one outer row o (IB == C == inner == in_ls).  The input tile is
+// copied one tile ahead as in k_fft_pp; the maps of the row's Lout output points and the
+// row of X are copied (a second group) while the tile is transformed.  Each thread puts
+// w v conj(smap) of its coil in place of the map value, then thread r sums row r over the
+// coils into X[o][r] (src/gridFFT.cpp:926-941), so the sum needs no atomics.
+template <int Q, int P>
+__global__ void __launch_bounds__(8 * P) k_fft_pa(const FftPass p, int ntiles) {
+  constexpr int S = 8 * Q, IB = P, NPAIR = IB / 2;
+  extern __shared__ float2 sm[];  // [S][IB] data, S twiddles, [Lout][IB] maps, Lout values of X
+  float2 *tw = sm + S * (IB + 1);
+  float2 *mp = tw + S;
+  float2 *xa = mp + p.Lout * IB;
+  const int tid = threadIdx.x;
+  for (int m = tid; m < S; m += blockDim.x) tw[m] = p.tw[m];
+  const int j = tid % IB, t = tid / IB;
+  float2 *col = sm + j;
+  const int jp = tid % NPAIR, r0 = tid / NPAIR, rstep = blockDim.x / NPAIR;
+  auto issue_in = [&](int tile) {
+    const float2 *gs = p.in + (int64_t)tile * p.in_os + 2 * jp + (int64_t)r0 * p.in_ls;
+    const int64_t gstep = (int64_t)rstep * p.in_ls;
+    unsigned sa = (unsigned)__cvta_generic_to_shared(sm + (r0 + p.in_off) * IB + 2 * jp);
+    const unsigned sstep = (unsigned)(rstep * IB * (int)sizeof(float2));
+    for (int li = r0; li < p.Lin; li += rstep, gs += gstep, sa += sstep)
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gs));
+    for (int e = tid; e < (S - p.Lin) * IB; e += blockDim.x) {
+      const int jj = e % IB, k = e / IB;
+      const int r = (k < p.in_off) ? k : k + p.Lin;
+      sm[r * IB + jj] = make_float2(0.f, 0.f);
+    }
+  };
+  auto issue_maps = [&](int tile) {
+    const float2 *gm = p.smap + (int64_t)tile * p.out_os + 2 * jp + (int64_t)r0 * p.out_ls;
+    const int64_t gstep = (int64_t)rstep * p.out_ls;
+    unsigned sa = (unsigned)__cvta_generic_to_shared(mp + r0 * IB + 2 * jp);
+    const unsigned sstep = (unsigned)(rstep * IB * (int)sizeof(float2));
+    for (int r = r0; r < p.Lout; r += rstep, gm += gstep, sa += sstep)
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gm));
+    const float2 *gx = p.acc + (int64_t)tile * p.acc_o;
+    for (int r = tid; r < p.Lout; r += blockDim.x)
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"((unsigned)__cvta_generic_to_shared(xa + r)),
+                   "l"(gx + (int64_t)r * p.acc_l));
+  };
+  // Two commit groups per tile, always committed (empty past the last tile), so that
+  // "wait_group 1" always leaves exactly the newest group in flight.
+  int tile = blockIdx.x;
+  if (tile < ntiles) issue_in(tile);
+  asm volatile("cp.async.commit_group;\n" ::);
+  if (tile < ntiles) issue_maps(tile);
+  asm volatile("cp.async.commit_group;\n" ::);
+  for (; tile < ntiles; tile += gridDim.x) {
+    asm volatile("cp.async.wait_group 1;\n" ::: "memory");  // this tile's input
+    __syncthreads();
+    for (int n2 = t; n2 < Q; n2 += 8) {
+      float2 a[8];
+      float2 *c2 = col + n2 * IB;
+#pragma unroll
+      for (int n1 = 0; n1 < 8; n1++) a[n1] = c2[Q * n1 * IB];
+      reg_fft<8, +1, S>(a, tw);
+#pragma unroll
+      for (int k1 = 1; k1 < 8; k1++) a[k1] = cmul(a[k1], twid<+1>(tw, n2 * k1));
+#pragma unroll
+      for (int k1 = 0; k1 < 8; k1++) c2[Q * k1 * IB] = a[k1];
+    }
+    __syncthreads();
+    float2 v[Q];
+    const float2 *cq = col + Q * t * IB;
+#pragma unroll
+    for (int n2 = 0; n2 < Q; n2++) v[n2] = cq[n2 * IB];
+    __syncthreads();
+    const int nxt = tile + (int)gridDim.x;
+    if (nxt < ntiles) issue_in(nxt);
+    asm volatile("cp.async.commit_group;\n" ::);
+    reg_fft<Q, +1, S>(v, tw);
+    asm volatile("cp.async.wait_group 1;\n" ::: "memory");  // this tile's maps and X row
+    __syncthreads();
+    // X += sum_c (winz * winy * winx) v conj(smap)   (gridFFT::accumulate)
+    const float lw = p.wo[(int64_t)tile / p.wdiv] * p.wi[(int64_t)tile % p.wdiv];
+    const float sc = p.scale;
+#pragma unroll
+    for (int k2 = 0; k2 < Q; k2++) {
+      const int r = t + 8 * k2 - p.out_off;
+      if (r >= 0 && r < p.Lout) {
+        float2 val = make_float2(v[k2].x * sc, v[k2].y * sc);
+        const float w = lw * __ldg(p.wl + r);
+        val = make_float2(w * val.x, w * val.y);
+        float2 s2 = mp[r * IB + j];
+        s2.y = -s2.y;
+        mp[r * IB + j] = cmul(val, s2);
+      }
+    }
+    __syncthreads();
+    // rotated start (coil (c + r) mod C at step c) spreads a warp's reads over the banks
+    for (int r = tid; r < p.Lout; r += blockDim.x) {
+      float2 s = make_float2(0.f, 0.f);
+      const float2 *row = mp + r * IB;
+      int cc = r % IB;
+      for (int c = 0; c < IB; c++) {
+        s = cadd(s, row[cc]);
+        cc = (cc + 1 == IB) ? 0 : cc + 1;
+      }
+      p.acc[(int64_t)tile * p.acc_o + (int64_t)r * p.acc_l] = cadd(xa[r], s);
+    }
+    __syncthreads();
+    if (nxt < ntiles) issue_maps(nxt);
+    asm volatile("cp.async.commit_group;\n" ::);
+  }
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
+// Persistent launch over ntiles tiles.  The shared-memory cap and the resident CTAs per SM
+// (occupancy at the cap, a lower bound for smaller launches of the same kernel) are set up
+// once per device; the CTA count is the same on every device of a process.
+template <typename K>
+static mrg_status launch_persistent(K kern, int threads, size_t smem, size_t smem_cap, DeviceOnce &once, int &ctas,
+                                    int ntiles, const FftPass &pp, cudaStream_t st) {
+  MRG_TRY(device_once(once, [kern, threads, smem_cap, &ctas]() -> mrg_status {
+    MRG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cap));
+    int c = 0;
+    MRG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, kern, threads, smem_cap));
+    ctas = c < 1 ? 1 : c;
+    return MRG_OK;
+  }));
+  const int nblk = std::max(1, std::min(ntiles, device_sms() * ctas));
+  kern<<<nblk, threads, smem, st>>>(pp, ntiles);
+  MRG_LAUNCHED();
+  return MRG_OK;
+}
+
+template <int Q, int P>
+static mrg_status launch_ps(const FftPass &pp, cudaStream_t st) {
+  constexpr int S = 8 * Q;
+  const size_t smem = (size_t)S * (P + 3) * sizeof(float2);
+  static DeviceOnce once;
+  static int ctas = 1;
+  return launch_persistent(k_fft_ps<Q, P>, 8 * P, smem, smem, once, ctas, (int)(pp.nlines / P), pp, st);
+}
+
+template <int Q, int P>
+static mrg_status launch_pa(const FftPass &pp, cudaStream_t st) {
+  constexpr int S = 8 * Q;
+  const size_t smem = ((size_t)S * (P + 2) + (size_t)pp.Lout * (P + 1)) * sizeof(float2);
+  const size_t cap = ((size_t)S * (P + 2) + (size_t)S * (P + 1)) * sizeof(float2);
+  static DeviceOnce once;
+  static int ctas = 1;
+  return launch_persistent(k_fft_pa<Q, P>, 8 * P, smem, cap, once, ctas, (int)(pp.nlines / P), pp, st);
+}
+
 template <int Q, int SIGN, int P>
 static mrg_status launch_pp(const FftPass &pp, cudaStream_t st) {
   const size_t smem = (size_t)8 * Q * (P + 2) * sizeof(float2);
@@ -599,6 +837,16 @@ static mrg_status launch_q(const FftPass &p, cudaStream_t st) {
         (p.IB == 16 || p.IB == 32)) {
       if (p.IB == 16) return p.sign < 0 ? launch_pp<Q, -1, 16>(pp, st) : launch_pp<Q, +1, 16>(pp, st);
       return p.sign < 0 ? launch_pp<Q, -1, 32>(pp, st) : launch_pp<Q, +1, 32>(pp, st);
+    }
+    // set_image / accumulate x passes of multi-coil plans (lines along x, coils innermost),
+    // persistent when the plan's tuning chose it
+    if (p.xp && p.wmode == 1 && p.has_smap && pp.nib && p.vec16 && !p.lfast && p.inner == p.C && p.in_ls == p.C &&
+        (p.IB == 16 || p.IB == 32) && p.nlines / p.IB <= 0x7fffffff) {
+      if (p.mode == FFT_SETIMG && p.in_os % p.C == 0 && p.Lin <= R * Q)
+        return p.IB == 16 ? launch_ps<Q, 16>(pp, st) : launch_ps<Q, 32>(pp, st);
+      if (p.mode == FFT_ACCUM && p.IB == p.C && !p.acc_atomic && p.Lout <= R * Q && p.out_os % 2 == 0 &&
+          p.out_ls % 2 == 0 && ((uintptr_t)p.smap & 15) == 0)
+        return p.IB == 16 ? launch_pa<Q, 16>(pp, st) : launch_pa<Q, 32>(pp, st);
     }
     if (!p.lfast && p.IB == 32) return launch_qp<Q, 32>(pp, grid, block, smem, st);
     if (!p.lfast && p.IB == 16) return launch_qp<Q, 16>(pp, grid, block, smem, st);

@@ -34,7 +34,8 @@ namespace mrg {
 namespace {
 
 constexpr int TK = 96;      // pairs per chunk: twelve k-steps of 8 TF32 values
-constexpr int TP = TK + 4;  // row pitch (floats) of the per-pair weight tables: conflict-free 16-byte reads
+constexpr int TP = TK + 4;  // row pitch (floats) of the per-chunk weight tables: conflict-free 16-byte reads
+constexpr int TROWS = 24;   // table rows: (wz*wy) of the region's 16 (z, y) rows, then wx of its 8 x
 constexpr int NBLD = 512;   // builder threads: four warpgroups; warp w reaches TMEM lanes 32 (w % 4) .. + 31
 constexpr int NTHR = NBLD + 32;  // and one warp that issues the MMAs
 
@@ -44,16 +45,13 @@ struct TcLayout {
   static constexpr int NQ = N / 4;               // accumulator columns drained by each warpgroup
   static constexpr int BOP = N * TK * 4;         // one V operand (hi or lo), K-major canonical
   static constexpr int SV = TK * N * 4;          // staged sample values [k][N]
-  static constexpr int SW = TK * 24 * 4;         // staged tap weights [k][24]
-  static constexpr int ST = TK * 16;             // staged first taps [k]
-  static constexpr int STAGE = SV + SW + ST;
-  static constexpr int SYZ = 16 * TP * 4;        // (wz*wy)[pz*4 + py][k]
-  static constexpr int SX = 8 * TP * 4;          // wx[px][k]
+  static constexpr int STAB = TROWS * TP * 4;    // staged chunk table [row][k]
+  static constexpr int STAGE = SV + STAB;
   static constexpr int OFF_B = 0;                             // 2 slots x (V hi, V lo)
   static constexpr int OFF_STAGE = OFF_B + 4 * BOP;           // 2 staging buffers
-  static constexpr int OFF_SYZ = OFF_STAGE + 2 * STAGE;
-  static constexpr int OFF_SX = OFF_SYZ + SYZ;
-  static constexpr int USED = OFF_SX + SX;
+  static constexpr int RP = N + 4;                            // row pitch (floats) of the region buffer
+  static constexpr int OFF_R = OFF_STAGE + 2 * STAGE;         // a finished region [128 points][RP]
+  static constexpr int USED = OFF_R + 128 * RP * 4;
   // more than half of the SM's shared memory, so one CTA per SM owns all 512 TMEM columns
   static constexpr int TOTAL = USED > 120 * 1024 ? USED : 120 * 1024;
   // tensor memory: accumulators at columns [0, 2N), W of slot s at A0 + 2 TK s (hi) and
@@ -177,21 +175,20 @@ __device__ __forceinline__ void drain(uint32_t ta, float (&acc)[NQ]) {
   for (int j = 0; j < NQ; j++) acc[j] = __fadd_rn(acc[j], __uint_as_float(v[j]));
 }
 
-// Issues the cp.async copies of the records of one chunk (pair indices already in shared
-// memory, `idx`) into staging buffer `st`; rows k >= nq of the sample values are zeroed.
+// Issues the cp.async copies of one chunk into staging buffer `st`: its table (the first
+// 8 ceil(nq / 8) columns of each row, from `tab`) and its sample values (pair indices
+// already in shared memory, `idx`); rows k >= nq of the sample values are zeroed.
 template <int CC, bool VEC>
 __device__ __forceinline__ void stage_chunk(unsigned char *st, const int *idx, int nq, int tid, int C, int c0, int nc,
-                                            const float4 *__restrict__ swt, const int4 *__restrict__ sst,
-                                            const float2 *__restrict__ yw) {
+                                            const float *__restrict__ tab, const float2 *__restrict__ yw) {
   typedef TcLayout<CC> L;
   constexpr int N = L::N, NCH = N / 4;
   float *sv = reinterpret_cast<float *>(st);
-  float *sw = reinterpret_cast<float *>(st + L::SV);
-  int4 *stt = reinterpret_cast<int4 *>(st + L::SV + L::SW);
-  if (tid < nq) ucp16(stt + tid, sst + idx[tid]);
-  for (int e = tid; e < TK * 6; e += NBLD) {  // 6 pieces of 16 bytes per record
-    const int k = e / 6, piece = e - 6 * k;
-    if (k < nq) ucp16(sw + k * 24 + 4 * piece, swt + 6 * (int64_t)idx[k] + piece);
+  float *stb = reinterpret_cast<float *>(st + L::SV);
+  const int pr = 2 * ((nq + 7) >> 3);  // 16-byte pieces per row
+  for (int e = tid; e < TROWS * pr; e += NBLD) {
+    const int row = e / pr, o = TP * row + 4 * (e - row * pr);
+    ucp16(stb + o, tab + o);
   }
 #pragma unroll
   for (int e0 = 0; e0 < TK * NCH; e0 += NBLD) {
@@ -222,35 +219,106 @@ __device__ __forceinline__ void stage_idx(int *idx, const int *__restrict__ pair
   if (tid < nq) asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s_u32(idx + tid)), "l"(pairs + q0 + tid));
 }
 
-// Work item x field as packed region origin: x0 | y0 << 11 | z0 << 22.
+// Region origin packed into a work item's x field, unsigned: x0 | y0 << 11 | z0 << 22
+// (11, 11 and 10 bits; a z origin of 512 or more sets bit 31, so the fields are unpacked
+// with unsigned shifts).
+__device__ __forceinline__ int pack_origin(int x0, int y0, int z0) {
+  return (int)((unsigned)x0 | ((unsigned)y0 << 11) | ((unsigned)z0 << 22));
+}
+__device__ __forceinline__ void unpack_origin(int packed, int &x0, int &y0, int &z0) {
+  const unsigned u = (unsigned)packed;
+  x0 = (int)(u & 2047u);
+  y0 = (int)((u >> 11) & 2047u);
+  z0 = (int)(u >> 22);
+}
+
+// Chunks of each region work item (none for an item without pairs).
+__global__ void k_item_chunks(int nitems, const int4 *__restrict__ items, int *cnt) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nitems; i += gridDim.x * blockDim.x) {
+    const int4 it = items[i];
+    cnt[i] = (it.z - it.y + TK - 1) / TK;
+  }
+}
+
+// The per-chunk tables of the region work items (one CTA per item, one thread per pair):
+// the products the gridding kernel multiplies into W, (wz * wy) for the region's 4 z and 4
+// y planes (wz times wy first, as src/gridFFT.cpp:1113-1140) and wx for its 8 x columns,
+// zero where a plane lies outside the sample's taps.  They depend on the trajectory only.
+__global__ void k_region_tables(int nitems, const int4 *__restrict__ items, const int *__restrict__ pairs,
+                                const int *__restrict__ rchunk, const float4 *__restrict__ swt,
+                                const int4 *__restrict__ sst, float *__restrict__ rtab) {
+  for (int i = blockIdx.x; i < nitems; i += gridDim.x) {
+    const int4 it = items[i];
+    int x0, y0, z0;
+    unpack_origin(it.x, x0, y0, z0);
+    const int ch0 = rchunk[i];
+    for (int q = it.y + threadIdx.x; q < it.z; q += blockDim.x) {
+      const int s = pairs[q];
+      const int4 t = sst[s];
+      float w[24];
+#pragma unroll
+      for (int k = 0; k < 6; k++) {
+        const float4 v = swt[6 * (int64_t)s + k];
+        w[4 * k] = v.x;
+        w[4 * k + 1] = v.y;
+        w[4 * k + 2] = v.z;
+        w[4 * k + 3] = v.w;
+      }
+      const int r = q - it.y;
+      float *o = rtab + (int64_t)(ch0 + r / TK) * (TROWS * TP) + r % TK;
+#pragma unroll
+      for (int zz = 0; zz < 4; zz++) {
+        const int az = z0 + zz - t.z;
+        const float wz = (az >= 0 && az < 8) ? w[16 + az] : 0.0f;
+#pragma unroll
+        for (int yy = 0; yy < 4; yy++) {
+          const int ay = y0 + yy - t.y;
+          o[(zz * 4 + yy) * TP] = __fmul_rn(wz, (ay >= 0 && ay < 8) ? w[8 + ay] : 0.0f);
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        const int ax = x0 + j - t.x;
+        o[(16 + j) * TP] = (ax >= 0 && ax < 8) ? w[ax] : 0.0f;
+      }
+    }
+  }
+}
+
+// Work item x field as the packed region origin.
 __global__ void k_pack_regions(BlockShape rs, int nitems, int4 *items) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nitems; i += gridDim.x * blockDim.x) {
     const int r = items[i].x;
     const int rx = r % rs.nb[0], ry = (r / rs.nb[0]) % rs.nb[1], rz = r / (rs.nb[0] * rs.nb[1]);
-    items[i].x = (rx * RGN_X) | ((ry * RGN_Y) << 11) | ((rz * RGN_Z) << 22);
+    items[i].x = pack_origin(rx * RGN_X, ry * RGN_Y, rz * RGN_Z);
   }
 }
 
-// A CTA's walk over its chunks: item (-1 past the end), its work item and first pair.
+// A CTA's walk over its chunks: item (-1 past the end), its work item, first pair and
+// table chunk.
 struct ChunkPos {
-  int item, q0;
+  int item, q0, ch;
   int4 it;
 };
-__device__ __forceinline__ ChunkPos first_chunk(int item, int nitems, const int4 *__restrict__ items) {
+__device__ __forceinline__ ChunkPos first_chunk(int item, int nitems, const int4 *__restrict__ items,
+                                                const int *__restrict__ rchunk) {
   ChunkPos p;
   p.item = item < nitems ? item : -1;
   p.it = p.item >= 0 ? __ldg(items + item) : make_int4(0, 0, 0, 0);
+  p.ch = p.item >= 0 ? __ldg(rchunk + item) : 0;
   p.q0 = p.it.y;
   return p;
 }
-__device__ __forceinline__ ChunkPos next_chunk(const ChunkPos &p, int nitems, const int4 *__restrict__ items) {
+__device__ __forceinline__ ChunkPos next_chunk(const ChunkPos &p, int nitems, const int4 *__restrict__ items,
+                                               const int *__restrict__ rchunk) {
   if (p.item < 0) return p;
   if (p.q0 + TK < p.it.z) {
     ChunkPos n = p;
     n.q0 += TK;
+    n.ch += 1;
     return n;
   }
-  return first_chunk(p.item + gridDim.x, nitems, items);
+  return first_chunk(p.item + gridDim.x, nitems, items, rchunk);
 }
 
 __device__ __forceinline__ void bld_sync() { asm volatile("bar.sync 1, %0;" ::"n"(NBLD) : "memory"); }
@@ -280,7 +348,7 @@ __device__ __forceinline__ bool bld_and(bool v) {
 template <int CC, bool VEC>
 __global__ void __launch_bounds__(NTHR, 1)
     k_grid_umma(const GridConst g, int nitems, const int4 *__restrict__ items, const int *__restrict__ pairs,
-                const float4 *__restrict__ swt, const int4 *__restrict__ sst, const float2 *__restrict__ yw,
+                const int *__restrict__ rchunk, const float *__restrict__ rtab, const float2 *__restrict__ yw,
                 float2 *__restrict__ grid) {
   typedef TcLayout<CC> L;
   constexpr int N = L::N, NQ = L::NQ;
@@ -289,8 +357,6 @@ __global__ void __launch_bounds__(NTHR, 1)
   __shared__ uint32_t tslot;
   __shared__ int slot_nks[2];
   __shared__ __align__(16) int sidx[3][TK];
-  float *syz = reinterpret_cast<float *>(usm + L::OFF_SYZ);
-  float *sx = reinterpret_cast<float *>(usm + L::OFF_SX);
   const int tid = threadIdx.x, warp = tid >> 5;
   const int C = g.C, c0 = blockIdx.y * CC, nc = min(CC, C - c0);
 
@@ -352,171 +418,201 @@ __global__ void __launch_bounds__(NTHR, 1)
     const int wg = tid >> 7, pt = tid & 127;
     const int px = pt & 7, py = (pt >> 3) & 3, pz = pt >> 5;  // this thread's point (TMEM lane = pt)
     const uint32_t lane_base = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
-    // per slot s, bit s: a chunk written and not yet waited for / it had MMAs / the done[s]
-    // phase to wait for next (bit masks keep them in registers)
-    unsigned outstanding = 0u, mma = 0u, dphase = 0u;
+    // per slot s, bit s: a chunk handed to the MMA warp and not yet summed / that chunk ends
+    // its work item / the item is a split region / the done[s] phase to wait for next (bit
+    // masks keep them in registers); org0, org1: the packed region origin of slot 0's and
+    // slot 1's chunk
+    unsigned outstanding = 0u, slast = 0u, ssplit = 0u, dphase = 0u;
+    int org0 = 0, org1 = 0;
     bool ok = true;
     float acc[NQ];
 #pragma unroll
     for (int j = 0; j < NQ; j++) acc[j] = 0.f;
-    // Waits (bounded) for the chunk last written into slot s and sums it; the builders
-    // give up together so their barriers stay matched.
+    // A finished region goes out through shared memory so that each warp stores (or, into a
+    // pre-zeroed split region, adds) contiguous bytes: the threads put their accumulators in
+    // the region buffer, then thread u writes 16 bytes of point u / (N / 4).  An item without
+    // pairs writes zeros (nothing for a split region).  All builder threads call it together.
+    float *rbuf = reinterpret_cast<float *>(usm + L::OFF_R);
+    auto write_region = [&](int packed, bool split, bool zero) {
+      if (zero && split) return;
+      int rx0, ry0, rz0;
+      unpack_origin(packed, rx0, ry0, rz0);
+      // a region outside the grid would mean a corrupt work item: report it, write nothing
+      // (the condition is the same for every builder thread, so their barriers stay matched)
+      if (rx0 + RGN_X > g.S[0] || ry0 + RGN_Y > g.S[1] || rz0 + RGN_Z > g.S[2]) {
+        if (tid == 0 && g.err) atomicExch(g.err, MRG_REGION_RANGE);
+        return;
+      }
+      if (!zero) {
+        bld_sync();  // the previous region's readers are done with the buffer
+        float4 *d = reinterpret_cast<float4 *>(rbuf + pt * L::RP + wg * NQ);
+#pragma unroll
+        for (int j = 0; j < NQ / 4; j++) d[j] = make_float4(acc[4 * j], acc[4 * j + 1], acc[4 * j + 2], acc[4 * j + 3]);
+        bld_sync();
+      }
+      auto point_base = [&](int p) -> int64_t {  // grid index (float2) of coil c0 at point p
+        return (((int64_t)(rz0 + (p >> 5)) * g.S[1] + (ry0 + ((p >> 3) & 3))) * g.S[0] + (rx0 + (p & 7))) * C + c0;
+      };
+      if (VEC) {
+        constexpr int NCH = N / 4;  // 16-byte pieces per point: coils 2q, 2q + 1 in piece q
+        for (int u = tid; u < 128 * NCH; u += NBLD) {
+          const int p = u / NCH, q = u - p * NCH;
+          if (2 * q >= nc) continue;
+          float4 *o = reinterpret_cast<float4 *>(grid + point_base(p)) + q;
+          const float4 v = zero ? make_float4(0.f, 0.f, 0.f, 0.f) : *reinterpret_cast<const float4 *>(rbuf + p * L::RP + 4 * q);
+          if (split) atomicAdd(o, v);
+          else *o = v;
+        }
+      } else {
+        for (int u = tid; u < 128 * CC; u += NBLD) {
+          const int p = u / CC, q = u - p * CC;  // coil c0 + q
+          if (q >= nc) continue;
+          float2 *o = grid + point_base(p) + q;
+          const float2 v = zero ? make_float2(0.f, 0.f) : *reinterpret_cast<const float2 *>(rbuf + p * L::RP + 2 * q);
+          if (split) {
+            atomicAdd(&o->x, v.x);
+            atomicAdd(&o->y, v.y);
+          } else {
+            *o = v;
+          }
+        }
+      }
+    };
+    // Waits (bounded) for the chunk last handed over in slot s and sums it; when that chunk
+    // ends its item, the sum is the item's and goes out to the grid.  Chunks are summed in
+    // the order they were handed over and an item is written as soon as its last chunk is
+    // summed, so acc only ever holds one item.  The builders give up together so their
+    // barriers stay matched.
     auto retire = [&](int s) -> bool {
       if (!((outstanding >> s) & 1u)) return true;
       if (!bld_and(mbar_wait(s_u32(&done[s]), (dphase >> s) & 1u, g.wait_ns))) return false;
       dphase ^= 1u << s;
       outstanding &= ~(1u << s);
-      if ((mma >> s) & 1u) {
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        drain<NQ>(lane_base + (uint32_t)(s * N + wg * NQ), acc);
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      drain<NQ>(lane_base + (uint32_t)(s * N + wg * NQ), acc);
+      if ((slast >> s) & 1u) {
+        write_region(s ? org1 : org0, (ssplit >> s) & 1u, false);
+#pragma unroll
+        for (int j = 0; j < NQ; j++) acc[j] = 0.f;
       }
       return true;
     };
-    ChunkPos cur = first_chunk(blockIdx.x, nitems, items);
-    ChunkPos nxt = next_chunk(cur, nitems, items);
+    // Chunks c, c + 1 and c + 2 are known at the top of iteration c; c + 3 is looked up there,
+    // so a new work item's descriptor (a global load) has a whole iteration to arrive before
+    // its pair indices are staged.
+    ChunkPos cur = first_chunk(blockIdx.x, nitems, items, rchunk);
+    ChunkPos nxt = next_chunk(cur, nitems, items, rchunk);
+    ChunkPos nxt2 = next_chunk(nxt, nitems, items, rchunk);
+    auto ctab = [&](const ChunkPos &q) { return rtab + (int64_t)q.ch * (TROWS * TP); };
     // prologue: indices of the first chunk, then its records and the next chunk's indices
     if (cur.item >= 0) stage_idx(sidx[0], pairs, cur.q0, min(TK, cur.it.z - cur.q0), tid);
     asm volatile("cp.async.commit_group;\n" ::);
     asm volatile("cp.async.wait_group 0;\n" ::: "memory");
     bld_sync();
     if (cur.item >= 0)
-      stage_chunk<CC, VEC>(usm + L::OFF_STAGE, sidx[0], min(TK, cur.it.z - cur.q0), tid, C, c0, nc, swt, sst, yw);
+      stage_chunk<CC, VEC>(usm + L::OFF_STAGE, sidx[0], min(TK, cur.it.z - cur.q0), tid, C, c0, nc, ctab(cur), yw);
     if (nxt.item >= 0) stage_idx(sidx[1], pairs, nxt.q0, min(TK, nxt.it.z - nxt.q0), tid);
     asm volatile("cp.async.commit_group;\n" ::);
-    int c = 0;
+    int c = 0;  // chunks walked (staging buffers alternate per chunk)
+    int m = 0;  // chunks handed to the MMA warp (accumulator slots alternate per handed chunk)
     while (cur.item >= 0) {
       const int nq = min(TK, cur.it.z - cur.q0);
       const bool last = cur.q0 + TK >= cur.it.z;
-      const ChunkPos nxt2 = next_chunk(nxt, nitems, items);
+      const ChunkPos nxt3 = next_chunk(nxt2, nitems, items, rchunk);
       // records of chunk c and indices of chunk c + 1 have landed
       asm volatile("cp.async.wait_group 0;\n" ::: "memory");
       bld_sync();
       if (nxt.item >= 0)
         stage_chunk<CC, VEC>(usm + L::OFF_STAGE + ((c + 1) & 1) * L::STAGE, sidx[(c + 1) % 3],
-                             min(TK, nxt.it.z - nxt.q0), tid, C, c0, nc, swt, sst, yw);
+                             min(TK, nxt.it.z - nxt.q0), tid, C, c0, nc, ctab(nxt), yw);
       if (nxt2.item >= 0) stage_idx(sidx[(c + 2) % 3], pairs, nxt2.q0, min(TK, nxt2.it.z - nxt2.q0), tid);
       asm volatile("cp.async.commit_group;\n" ::);
-      const unsigned char *stg = usm + L::OFF_STAGE + (c & 1) * L::STAGE;
-      const float *sv = reinterpret_cast<const float *>(stg);
-      const float *sw = reinterpret_cast<const float *>(stg + L::SV);
-      const int4 *stt = reinterpret_cast<const int4 *>(stg + L::SV + L::SW);
-      const int x0 = cur.it.x & 2047, y0 = (cur.it.x >> 11) & 2047, z0 = cur.it.x >> 22;
-      // ---- per pair: (wz*wy) for the region's 4 y and 4 z planes, wx for its 8 x ----
-      for (int k = tid >> 3; k < 8 * ((nq + 7) >> 3); k += NBLD / 8) {  // 8 threads per pair
-        const int j = tid & 7, zz = j >> 1, y2 = 2 * (j & 1);
-        float wyz0 = 0.f, wyz1 = 0.f, wx = 0.f;
-        if (k < nq) {
-          const int4 t = stt[k];
-          const float *w = sw + k * 24;
-          const int az = z0 + zz - t.z, ay = y0 + y2 - t.y, ax = x0 + j - t.x;
-          const float wz = (az >= 0 && az < 8) ? w[16 + az] : 0.0f;
-          // (wz * wy) first, as src/gridFFT.cpp:1113-1140 multiplies them
-          wyz0 = __fmul_rn(wz, (ay >= 0 && ay < 8) ? w[8 + ay] : 0.0f);
-          wyz1 = __fmul_rn(wz, (ay + 1 >= 0 && ay + 1 < 8) ? w[9 + ay] : 0.0f);
-          wx = (ax >= 0 && ax < 8) ? w[ax] : 0.0f;
-        }
-        syz[(zz * 4 + y2) * TP + k] = wyz0;
-        syz[(zz * 4 + y2 + 1) * TP + k] = wyz1;
-        sx[j * TP + k] = wx;
-      }
-      bld_sync();
-      const int slot = c & 1;
-      // ---- the slot is free once its chunk (two back) is summed ----
-      if (!retire(slot)) {
-        ok = false;
-        break;
-      }
-      const int nks = (nq + 7) >> 3;  // k-steps with pairs
-      // ---- W: this thread's row, k-steps wg, wg + 4, wg + 8, hi and lo, into tensor memory ----
-      {
-        const float *ryz = syz + (pz * 4 + py) * TP, *rxx = sx + px * TP;
-        const uint32_t ta = lane_base + (uint32_t)(L::A0 + 2 * TK * slot);
-#pragma unroll
-        for (int h = 0; h < TK / 32; h++) {
-          const int ks = wg + 4 * h;
-          if (ks < nks) {
-            const float4 a0 = *reinterpret_cast<const float4 *>(ryz + 8 * ks);
-            const float4 a1 = *reinterpret_cast<const float4 *>(ryz + 8 * ks + 4);
-            const float4 b0 = *reinterpret_cast<const float4 *>(rxx + 8 * ks);
-            const float4 b1 = *reinterpret_cast<const float4 *>(rxx + 8 * ks + 4);
-            const float w[8] = {__fmul_rn(a0.x, b0.x), __fmul_rn(a0.y, b0.y), __fmul_rn(a0.z, b0.z),
-                                __fmul_rn(a0.w, b0.w), __fmul_rn(a1.x, b1.x), __fmul_rn(a1.y, b1.y),
-                                __fmul_rn(a1.z, b1.z), __fmul_rn(a1.w, b1.w)};
-            uint32_t hh[8], ll[8];
-#pragma unroll
-            for (int i = 0; i < 8; i++) {
-              hh[i] = hi_bits(w[i]);
-              ll[i] = __float_as_uint(w[i] - __uint_as_float(hh[i]));
-            }
-            tst8(ta + 8 * ks, hh);
-            tst8(ta + TK + 8 * ks, ll);
-          }
-        }
-      }
-      // ---- V: K-major canonical, hi and lo, into the slot's shared buffers ----
-      {
-        // (n, 4 consecutive k) units; NBLD is a multiple of N, so a thread keeps its n
-        static_assert(NBLD % N == 0, "one column per thread");
-        const int n = tid % N;
-        unsigned char *bh = usm + L::OFF_B + slot * 2 * L::BOP + canon(n, 0);
-        const float *sp = sv + n;
-        for (int k4 = tid / N; k4 < 2 * nks; k4 += NBLD / N) {
-          const float *q = sp + 4 * k4 * N;
-          const float v[4] = {q[0], q[N], q[2 * N], q[3 * N]};
-          uint32_t hh[4], ll[4];
-#pragma unroll
-          for (int i = 0; i < 4; i++) {
-            hh[i] = hi_bits(v[i]);
-            ll[i] = __float_as_uint(v[i] - __uint_as_float(hh[i]));
-          }
-          *reinterpret_cast<uint4 *>(bh + k4 * 128) = make_uint4(hh[0], hh[1], hh[2], hh[3]);
-          *reinterpret_cast<uint4 *>(bh + L::BOP + k4 * 128) = make_uint4(ll[0], ll[1], ll[2], ll[3]);
-        }
-      }
-      if (tid == 0) slot_nks[slot] = nks;
-      asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      __syncwarp();
-      if ((tid & 31) == 0) mbar_arrive(s_u32(&full[slot]));
-      outstanding |= 1u << slot;
-      mma = nks > 0 ? (mma | (1u << slot)) : (mma & ~(1u << slot));
       ++c;
-      if (last) {
-        // ---- sum what is still in flight (the older chunk first), then write the region ----
-        if (!retire(slot ^ 1) || !retire(slot)) {
+      if (nq == 0) {
+        // an item without pairs: its region is zero (a split region was zeroed beforehand)
+        if (!cur.it.w) write_region(cur.it.x, false, true);
+      } else {
+        const unsigned char *stg = usm + L::OFF_STAGE + ((c - 1) & 1) * L::STAGE;
+        const float *sv = reinterpret_cast<const float *>(stg);
+        const float *tb = reinterpret_cast<const float *>(stg + L::SV);
+        const int slot = m & 1;
+        // ---- the slot is free once its chunk (two back) is summed ----
+        if (!retire(slot)) {
           ok = false;
           break;
         }
-        // this thread's coils: [c0 + wg NQ / 2, + NQ / 2) of its point
-        const int cl = wg * (NQ / 2);
-        const int64_t gi = (((int64_t)(z0 + pz) * g.S[1] + (y0 + py)) * g.S[0] + (x0 + px)) * C + c0 + cl;
-        if (cur.it.w) {
+        const int nks = (nq + 7) >> 3;  // k-steps with pairs
+        // ---- W: this thread's row, k-steps wg, wg + 4, wg + 8, hi and lo, into tensor memory ----
+        {
+          const float *ryz = tb + (pz * 4 + py) * TP, *rxx = tb + (16 + px) * TP;
+          const uint32_t ta = lane_base + (uint32_t)(L::A0 + 2 * TK * slot);
 #pragma unroll
-          for (int j = 0; j < NQ; j++)
-            if (cl + (j >> 1) < nc) atomicAdd(reinterpret_cast<float *>(grid + gi) + j, acc[j]);
-        } else if (VEC) {
-          float4 *o4 = reinterpret_cast<float4 *>(grid + gi);
+          for (int h = 0; h < TK / 32; h++) {
+            const int ks = wg + 4 * h;
+            if (ks < nks) {
+              const float4 a0 = *reinterpret_cast<const float4 *>(ryz + 8 * ks);
+              const float4 a1 = *reinterpret_cast<const float4 *>(ryz + 8 * ks + 4);
+              const float4 b0 = *reinterpret_cast<const float4 *>(rxx + 8 * ks);
+              const float4 b1 = *reinterpret_cast<const float4 *>(rxx + 8 * ks + 4);
+              const float w[8] = {__fmul_rn(a0.x, b0.x), __fmul_rn(a0.y, b0.y), __fmul_rn(a0.z, b0.z),
+                                  __fmul_rn(a0.w, b0.w), __fmul_rn(a1.x, b1.x), __fmul_rn(a1.y, b1.y),
+                                  __fmul_rn(a1.z, b1.z), __fmul_rn(a1.w, b1.w)};
+              uint32_t hh[8], ll[8];
 #pragma unroll
-          for (int j = 0; j < NQ / 4; j++)
-            if (cl + 2 * j < nc) o4[j] = make_float4(acc[4 * j], acc[4 * j + 1], acc[4 * j + 2], acc[4 * j + 3]);
-        } else {
-#pragma unroll
-          for (int j = 0; j < NQ / 2; j++)
-            if (cl + j < nc) grid[gi + j] = make_float2(acc[2 * j], acc[2 * j + 1]);
+              for (int i = 0; i < 8; i++) {
+                hh[i] = hi_bits(w[i]);
+                ll[i] = __float_as_uint(w[i] - __uint_as_float(hh[i]));
+              }
+              tst8(ta + 8 * ks, hh);
+              tst8(ta + TK + 8 * ks, ll);
+            }
+          }
         }
+        // ---- V: K-major canonical, hi and lo, into the slot's shared buffers ----
+        {
+          // (n, 4 consecutive k) units; NBLD is a multiple of N, so a thread keeps its n
+          static_assert(NBLD % N == 0, "one column per thread");
+          const int n = tid % N;
+          unsigned char *bh = usm + L::OFF_B + slot * 2 * L::BOP + canon(n, 0);
+          const float *sp = sv + n;
+          for (int k4 = tid / N; k4 < 2 * nks; k4 += NBLD / N) {
+            const float *q = sp + 4 * k4 * N;
+            const float v[4] = {q[0], q[N], q[2 * N], q[3 * N]};
+            uint32_t hh[4], ll[4];
 #pragma unroll
-        for (int j = 0; j < NQ; j++) acc[j] = 0.f;
+            for (int i = 0; i < 4; i++) {
+              hh[i] = hi_bits(v[i]);
+              ll[i] = __float_as_uint(v[i] - __uint_as_float(hh[i]));
+            }
+            *reinterpret_cast<uint4 *>(bh + k4 * 128) = make_uint4(hh[0], hh[1], hh[2], hh[3]);
+            *reinterpret_cast<uint4 *>(bh + L::BOP + k4 * 128) = make_uint4(ll[0], ll[1], ll[2], ll[3]);
+          }
+        }
+        if (tid == 0) slot_nks[slot] = nks;
+        asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncwarp();
+        if ((tid & 31) == 0) mbar_arrive(s_u32(&full[slot]));
+        const unsigned b = 1u << slot;
+        outstanding |= b;
+        slast = last ? (slast | b) : (slast & ~b);
+        ssplit = cur.it.w ? (ssplit | b) : (ssplit & ~b);
+        if (slot) org1 = cur.it.x; else org0 = cur.it.x;
+        ++m;
       }
       cur = nxt;
       nxt = nxt2;
+      nxt2 = nxt3;
     }
     asm volatile("cp.async.wait_all;\n" ::: "memory");
+    // sum and write what is still in flight (the older chunk first)
+    if (ok && (!retire(m & 1) || !retire((m & 1) ^ 1))) ok = false;
     if (ok) {
-      // both slots are retired (the last chunk ended an item): tell the MMA warp to stop
-      if (tid == 0) slot_nks[c & 1] = -1;
+      // both slots are retired: tell the MMA warp to stop
+      if (tid == 0) slot_nks[m & 1] = -1;
       __syncwarp();
-      if ((tid & 31) == 0) mbar_arrive(s_u32(&full[c & 1]));
+      if ((tid & 31) == 0) mbar_arrive(s_u32(&full[m & 1]));
     } else {
       flag_wait_error(g);
       // let MMAs still in flight finish before the tensor memory is freed: the MMA warp
@@ -538,6 +634,24 @@ bool umma_supported(int C) { return C >= 8; }
 // region origins packed in 11 + 11 + 10 bits
 bool umma_grid_fits(const int S[3]) { return S[0] <= 2048 && S[1] <= 2048 && S[2] <= 1024; }
 int umma_default_cc(int C) { return C > 16 ? 32 : (C > 8 ? 16 : 8); }
+
+int64_t umma_table_floats() { return (int64_t)TROWS * TP; }
+
+mrg_status launch_item_chunks(const FrameTraj &ft, int *cnt, cudaStream_t st) {
+  if (ft.regions.nitems == 0) return MRG_OK;
+  k_item_chunks<<<grid_blocks(ft.regions.nitems, 256), 256, 0, st>>>(ft.regions.nitems, ft.regions.items, cnt);
+  MRG_LAUNCHED();
+  return MRG_OK;
+}
+
+mrg_status launch_region_tables(const FrameTraj &ft, cudaStream_t st) {
+  const int n = ft.regions.nitems;
+  if (n == 0) return MRG_OK;
+  k_region_tables<<<std::min(n, 64 * device_sms()), 128, 0, st>>>(n, ft.regions.items, ft.regions.pairs, ft.rchunk,
+                                                                   ft.swt, ft.sst, ft.rtab);
+  MRG_LAUNCHED();
+  return MRG_OK;
+}
 
 int read_wait_error(const GridConst &gc) {
   if (!gc.err) return 0;
@@ -568,10 +682,10 @@ static mrg_status launch_umma_cc(const GridConst &gc, const FrameTraj &ft, const
   const dim3 blocks((unsigned)nx, (unsigned)npass);
   if (vec)
     k_grid_umma<CC, true><<<blocks, NTHR, L::TOTAL, st>>>(gc, ft.regions.nitems, ft.regions.items, ft.regions.pairs,
-                                                          ft.swt, ft.sst, yw, grid);
+                                                          ft.rchunk, ft.rtab, yw, grid);
   else
     k_grid_umma<CC, false><<<blocks, NTHR, L::TOTAL, st>>>(gc, ft.regions.nitems, ft.regions.items,
-                                                           ft.regions.pairs, ft.swt, ft.sst, yw, grid);
+                                                           ft.regions.pairs, ft.rchunk, ft.rtab, yw, grid);
   MRG_LAUNCHED();
   return MRG_OK;
 }
@@ -586,7 +700,7 @@ mrg_status pack_region_items(const GridConst &gc, PairSet &ps, cudaStream_t st) 
 // The caller zeroes the split regions (ft.regions.split) first.
 mrg_status launch_grid_umma(const GridConst &gc, const FrameTraj &ft, int cc, const float2 *yw, float2 *grid,
                             cudaStream_t st) {
-  if (!umma_supported(gc.C) || ft.regions.items == nullptr) {
+  if (!umma_supported(gc.C) || ft.regions.items == nullptr || (ft.regions.nitems > 0 && ft.rtab == nullptr)) {
     set_error("tensor-memory gridding needs >= 8 coils and region pair lists");
     return MRG_ERR_UNSUPPORTED;
   }

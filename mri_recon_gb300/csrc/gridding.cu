@@ -283,6 +283,8 @@ void traj_free(FrameTraj &ft) {
   cudaFree(ft.sst);
   pair_set_free(ft.blocks);
   pair_set_free(ft.regions);
+  cudaFree(ft.rtab);
+  cudaFree(ft.rchunk);
   cudaFree(ft.dsorted);
   cudaFree(ft.sdw);
   ft = FrameTraj();
@@ -295,6 +297,35 @@ static mrg_status read_int(const int *dev, int *host, cudaStream_t st, const cha
     return MRG_ERR_CUDA;
   }
   return MRG_OK;
+}
+
+mrg_status build_region_tables(FrameTraj &ft, cudaStream_t st) {
+  cudaFree(ft.rtab);
+  cudaFree(ft.rchunk);
+  ft.rtab = nullptr;
+  ft.rchunk = nullptr;
+  ft.nrchunks = 0;
+  const int n = ft.regions.nitems;
+  if (n == 0) return MRG_OK;
+  int *cnt = nullptr;
+  mrg_status rs = dalloc(&cnt, n + 1);
+  if (rs == MRG_OK) rs = dalloc(&ft.rchunk, n + 2);
+  if (rs == MRG_OK) rs = launch_item_chunks(ft, cnt, st);
+  if (rs == MRG_OK) {
+    k_scan<<<1, 1024, 0, st>>>(cnt, ft.rchunk, n);
+    count_launch();
+    if (cudaGetLastError() != cudaSuccess) rs = MRG_ERR_CUDA;
+  }
+  int total = 0;
+  if (rs == MRG_OK) rs = read_int(ft.rchunk + n, &total, st, "region chunk count failed");
+  cudaFree(cnt);
+  if (rs != MRG_OK) return rs;
+  ft.nrchunks = total;
+  const int64_t nf = (int64_t)total * umma_table_floats();
+  MRG_TRY(dalloc(&ft.rtab, nf));
+  // zero: the pad entries of a last, partial k-step must be finite (their samples are zero)
+  MRG_TRY(launch_zero(ft.rtab, sizeof(float) * (size_t)std::max<int64_t>(nf, 1), st));
+  return launch_region_tables(ft, st);
 }
 
 BlockShape block_shape(const GridConst &gc) {
@@ -454,6 +485,7 @@ mrg_status traj_setup(const GridConst &gc, FrameTraj &ft, const float *kx, const
   if (regions && umma_grid_fits(gc.S)) {
     SETUP_TRY(build_pairs(region_shape(gc), nvalid, ft.sst, max_pairs, st, ft.regions));
     SETUP_TRY(pack_region_items(gc, ft.regions, st));
+    SETUP_TRY(build_region_tables(ft, st));
   }
   cleanup();
 #undef SETUP_TRY

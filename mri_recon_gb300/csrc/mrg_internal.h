@@ -67,6 +67,8 @@ int device_sms();
 // Error word of a plan's bounded device-side waits (GridConst::err): 0 while every wait
 // ended in time, MRG_WAIT_EXPIRED once one ran out.
 constexpr int MRG_WAIT_EXPIRED = 1;
+// ... or MRG_REGION_RANGE when a gridding work item named a region outside the grid
+constexpr int MRG_REGION_RANGE = 2;
 // Default limit of one bounded wait, in nanoseconds of the GPU's global timer.
 constexpr long long MRG_DEFAULT_WAIT_NS = 2000000000LL;
 
@@ -130,6 +132,7 @@ struct FftPass {
   int C, has_smap;
   int acc_atomic;
   int64_t acc_l, acc_o;  // accumulator strides for l and o (i/C has stride 1)
+  int xp;                // persistent set_image / accumulate kernels allowed (x passes)
 };
 bool fft_size_supported(int S);
 // Lines per CTA a pass of length S can take (16 threads per line above 384 points).
@@ -193,6 +196,12 @@ struct FrameTraj {
   int4 *sst = nullptr;      // [nvalid] first tap (sx, sy, sz) and tap counts nx | ny << 4 | nz << 8
   PairSet blocks;           // 8x2x2 blocks (k_grid, k_grid_mma)
   PairSet regions;          // 8x4x4 regions (k_grid_umma), built when that kernel may run
+  // per 96-pair chunk of the region work items: (wz*wy) for the region's 16 (z, y) rows and
+  // wx for its 8 x, 24 rows x 100 floats (k_grid_umma's shared-memory layout); rchunk[item]
+  // = the item's first chunk (items without pairs have none)
+  float *rtab = nullptr;
+  int *rchunk = nullptr;
+  int64_t nrchunks = 0;
   float2 *dsorted = nullptr;  // measured data [nvalid][C], unweighted
   float4 *sdw = nullptr;      // [nvalid][6] d(tap weight)/dk per axis (allocated by mrg_grad)
   bool has_data = false;
@@ -211,6 +220,12 @@ bool umma_supported(int C);
 bool umma_grid_fits(const int S[3]);
 // Packs the region origin into each work item of the tcgen05 kernel's pair set.
 mrg_status pack_region_items(const GridConst &gc, PairSet &ps, cudaStream_t st);
+// The region tables of ft.regions (ft.rtab, ft.rchunk), after pack_region_items.
+mrg_status build_region_tables(FrameTraj &ft, cudaStream_t st);
+// its pieces (grid_umma.cu): chunks per work item into cnt[], and the tables themselves
+int64_t umma_table_floats();  // floats per chunk
+mrg_status launch_item_chunks(const FrameTraj &ft, int *cnt, cudaStream_t st);
+mrg_status launch_region_tables(const FrameTraj &ft, cudaStream_t st);
 // a gridding launch shape (mrg_frame_tuning's encoding) that the frame's kernels can run
 bool grid_cc_allowed(int C, const FrameTraj &ft, int cc);
 // n-tiles (4 coils each) per pass of the tensor-core ungridding kernel; 0: needs C % 4 == 0

@@ -153,6 +153,18 @@ class Plan:
                                ungrid_rows_per_step)
         _lib.check(_lib.load().mrg_frame_set_tuning(self._h, frame, v))
 
+    def fft_tuning(self):
+        """Per FFT pass (E x, z, y; E^H y, z, x): lines per CTA and the persistent x-pass flag."""
+        ib, xp = (ctypes.c_int * 6)(), (ctypes.c_int * 6)()
+        _lib.check(_lib.load().mrg_fft_tuning(self._h, ib, xp))
+        return dict(ib=list(ib), xp=list(xp))
+
+    def set_fft_tuning(self, ib=None, xp=None):
+        """Fixes the FFT launch shapes (see fft_tuning); None leaves that field as it is."""
+        a = None if ib is None else (ctypes.c_int * 6)(*ib)
+        b = None if xp is None else (ctypes.c_int * 6)(*xp)
+        _lib.check(_lib.load().mrg_set_fft_tuning(self._h, a, b))
+
     def set_data(self, frame, data, stream=None):
         """data: (C, M) complex64."""
         a = _Args()

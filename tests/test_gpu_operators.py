@@ -391,3 +391,73 @@ def test_long_lines_operators_match_oracle(mrg_lib, oracle_lib, N, C):
         assert rel(y[k], o.forward(X, smaps[k], kx, ky, kz, kw)) < 1e-5
         ref_h = o.adjoint(ref_h, smaps[k], d[k], kx, ky, kz, kw)
     assert rel(Xh, ref_h) < 1e-5
+
+
+@pytest.mark.parametrize("N,C", [((128, 16, 24), 32), ((128, 24, 16), 16), ((256, 16, 8), 32), ((160, 8, 16), 16),
+                                 ((128, 16, 16), 8), ((240, 8, 8), 20)])
+@pytest.mark.parametrize("ib", [0, 16])
+def test_persistent_x_passes_match_oracle(mrg_lib, oracle_lib, N, C, ib):
+    """The set_image and accumulate x passes run by the persistent kernels (xp = 1; x lines
+    of 192..384 points, 16 or 32 coils per CTA) and by the one-tile kernels (xp = 0) give
+    the oracle's E and E^H; 8 and 20 coils check the fall-back to the one-tile kernels."""
+    import torch
+    rng = np.random.default_rng(5)
+    M = 20000
+    kx, ky, kz = [rng.uniform(-n / 2, n / 2, M).astype(np.float32) for n in N]
+    kw = (kx.astype(np.float64) ** 2 + ky ** 2 + kz ** 2).astype(np.float32)
+    ishape = (N[2], N[1], N[0])
+    X = (rng.standard_normal(ishape) + 1j * rng.standard_normal(ishape)).astype(np.complex64)
+    smaps = (rng.standard_normal((C,) + ishape) + 1j * rng.standard_normal((C,) + ishape)).astype(np.complex64)
+    d = (rng.standard_normal((C, M)) + 1j * rng.standard_normal((C, M))).astype(np.complex64)
+    p = mrg_lib.Plan(N, C, 1)
+    p.set_traj(0, kx, ky, kz, kw)
+    p.set_smaps(torch.from_numpy(smaps).cuda())
+    o = oracle_lib.Plan(N)
+    ref_e = np.stack([o.forward(X, smaps[k], kx, ky, kz, kw) for k in range(C)])
+    ref_h = np.zeros(ishape, np.complex64)
+    for k in range(C):
+        ref_h = o.adjoint(ref_h, smaps[k], d[k], kx, ky, kz, kw)
+    X0 = (rng.standard_normal(ishape) + 1j * rng.standard_normal(ishape)).astype(np.complex64)
+    out = {}
+    for xp in (0, 1):
+        p.set_fft_tuning(ib=[ib] * 6, xp=[xp] * 6)
+        assert p.fft_tuning() == dict(ib=[ib] * 6, xp=[xp] * 6)
+        y = p.forward(0, torch.from_numpy(X).cuda()).cpu().numpy()
+        Xh = p.adjoint(0, d, X0.copy())  # accumulates into X
+        assert rel(y, ref_e) < 1e-5
+        assert rel(Xh - X0, ref_h) < 1e-5
+        out[xp] = (y, Xh)
+    assert rel(out[1][0], out[0][0]) < 1e-6
+    assert rel(out[1][1], out[0][1]) < 1e-6
+
+
+def test_set_fft_tuning_rejects_bad_values(mrg_lib):
+    p = mrg_lib.Plan(16, 2, 1)
+    with pytest.raises(mrg_lib.MrgError):
+        p.set_fft_tuning(ib=[33] * 6)
+    with pytest.raises(mrg_lib.MrgError):
+        p.set_fft_tuning(xp=[2] * 6)
+
+
+@pytest.mark.parametrize("N,C", [((20, 16, 384), 9), ((16, 24, 400), 16)])
+def test_tensor_core_gridding_on_long_z_axes(mrg_lib, oracle_lib, N, C):
+    """The tcgen05 gridding (grid_mode 3) on z axes of 576 and 608 points: region origins
+    at z >= 512 set the top bit of the packed work-item field, which must unpack unsigned."""
+    import torch
+    rng = np.random.default_rng(11)
+    M = 30000
+    kx, ky, kz = [rng.uniform(-n / 2, n / 2, M).astype(np.float32) for n in N]
+    kw = (kx.astype(np.float64) ** 2 + ky ** 2 + kz ** 2).astype(np.float32)
+    ishape = (N[2], N[1], N[0])
+    smaps = (rng.standard_normal((C,) + ishape) + 1j * rng.standard_normal((C,) + ishape)).astype(np.complex64)
+    d = (rng.standard_normal((C, M)) + 1j * rng.standard_normal((C, M))).astype(np.complex64)
+    p = mrg_lib.Plan(N, C, 1, grid_mode=3)
+    p.set_traj(0, kx, ky, kz, kw)
+    assert p.frame_tuning(0)["grid_coils_per_pass"] <= -100  # the tcgen05 kernel
+    p.set_smaps(torch.from_numpy(smaps).cuda())
+    Xh = p.adjoint(0, d, np.zeros(ishape, np.complex64))
+    o = oracle_lib.Plan(N)
+    ref = np.zeros(ishape, np.complex64)
+    for k in range(C):
+        ref = o.adjoint(ref, smaps[k], d[k], kx, ky, kz, kw)
+    assert rel(Xh, ref) < 1e-5
