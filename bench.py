@@ -60,6 +60,10 @@ def parse():
                          "and fixed threshold) against the FP32 oracle; prints one JSON object")
     ap.add_argument("--parity-legs", default="cg4,cg32,fista_fraction,fista_fixed",
                     help="comma-separated subset of the --parity-full legs")
+    ap.add_argument("--kernel-case", default=None, choices=["wavelet_llr"],
+                    help="only a small case for one-kernel ncu captures: wavelet_llr runs three rounds of "
+                         "mrg_wavelet (DB4, 3 levels) forward + inverse and the time low-rank threshold update "
+                         "and pass (8^3 blocks) on a 10 x 128^3 stack through the C ABI")
     ap.add_argument("--side-only", default=None, choices=["cg64", "fista128", "llr128", "grad96"],
                     help="run only this smaller configuration's throughput row (with --profile-range: its "
                          "timed iterations bracketed by cudaProfilerStart/Stop)")
@@ -633,9 +637,39 @@ def parity_fista128(O, m, dev, use_threshold, thresh):
     return out
 
 
+def kernel_case_wavelet_llr():
+    """10 frames of 128^3 (168 MB): the regulariser kernels of the gated FISTA configuration."""
+    import ctypes
+
+    import torch
+
+    import mri_recon_gb300 as m
+    L = m.load()
+    ip = lambda v: (ctypes.c_int * 3)(*v)  # noqa: E731
+    g = torch.Generator(device="cuda").manual_seed(1)
+    X = torch.randn((10, 128, 128, 128), dtype=torch.complex64, device="cuda", generator=g)
+    p = ctypes.c_void_p(X.data_ptr())
+    smax = ctypes.c_float()
+    for rep in range(3):
+        for inv in (0, 1):
+            if L.mrg_wavelet(p, 10, 128, 128, 128, ip((3, 3, 3)), ip((1, 2, 3)), 1, inv, None) != 0:
+                raise RuntimeError(L.mrg_last_error().decode())
+        if L.mrg_llr_update_threshold(p, 10, 128, 128, 128, ip((8, 8, 8)), 4.0, 6.0, 2, ctypes.byref(smax), None) != 0:
+            raise RuntimeError(L.mrg_last_error().decode())
+        if L.mrg_llr_thresh(p, 10, 128, 128, 128, ip((8, 8, 8)), 4, 0.0, smax, 1000 * rep, None) != 0:
+            raise RuntimeError(L.mrg_last_error().decode())
+    torch.cuda.synchronize()
+    print(json.dumps({"kernel_case": "wavelet_llr", "smax": smax.value}), flush=True)
+
+
 def run_ours(a):
     import torch
     import torch.distributed as dist
+
+    if a.kernel_case:
+        torch.cuda.set_device(0)
+        kernel_case_wavelet_llr()
+        return
 
     if a.parity_full:
         torch.cuda.set_device(0)
