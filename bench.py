@@ -110,8 +110,8 @@ def bytes_model(c, nvalid):
 # `ncu --profile-from-start off --metrics dram__bytes_read.sum,dram__bytes_write.sum`), times 8,
 # the growth of both the sample and the grid-point count.  Summary: profiles/ncu_traffic_cg256.md.
 NCU_TRAFFIC_CG256 = {
-    "E_xfft_setimg": 1.039e10, "E_zfft": 1.566e10, "E_yfft": 2.37e10, "E_ungrid": 2.389e10,
-    "EH_grid": 3.288e10, "EH_yfft": 2.383e10, "EH_zfft": 1.577e10, "EH_xfft_accum": 1.1e10,
+    "E_xfft_setimg": 1.042e10, "E_zfft": 1.565e10, "E_yfft": 2.371e10, "E_ungrid": 2.385e10,
+    "EH_grid": 3.875e10, "EH_yfft": 2.383e10, "EH_zfft": 1.577e10, "EH_xfft_accum": 1.099e10,
 }
 
 
@@ -855,23 +855,29 @@ def run_ours(a):
         traj_host = [torch.from_numpy(v).pin_memory() for v in (kx, ky, kz, kw)]
         X_host = torch.empty((1, N, N, N), dtype=torch.complex64).pin_memory()
         del y
-        times = []
+        times, phases = [], []
         for s in range(1 + a.e2e_solves):
             torch.cuda.synchronize()
             if world > 1:
                 dist.barrier()
             t0 = time.perf_counter()
             plan.set_traj(0, *traj_host)
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
             plan.set_data(0, y_host)
+            torch.cuda.synchronize()
+            t2 = time.perf_counter()
             plan.cg(iters, X=X_host, use_graph=True)
             torch.cuda.synchronize()
             if s > 0:
-                times.append(time.perf_counter() - t0)
+                t3 = time.perf_counter()
+                times.append(t3 - t0)
+                phases.append({"set_traj_s": t1 - t0, "set_data_s": t2 - t1, "cg_s": t3 - t2})
         e2e_val, _ = replicas.job_throughput(iters, max(times), dev)
         out["e2e"] = {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(C * M * 8 + 4 * M * 4),
                       "d2h_bytes_per_step": int(N ** 3 * 8 + iters * 8),
                       "step": "one %d-iteration solve: trajectory + k-space host->device, set-up, CG, image "
-                              "device->host" % iters}
+                              "device->host" % iters, "phases": phases[-1] if phases else None}
     if a.side_configs and rank == 0:
         del plan
         torch.cuda.empty_cache()

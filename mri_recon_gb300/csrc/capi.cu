@@ -617,7 +617,7 @@ static mrg_status tune_fft(mrg_plan *p, const FrameTraj &ft, cudaStream_t st) {
     pick[k] = 0;
   }
   int pick_xp[6] = {0, 0, 0, 0, 0, 0};
-  for (int cand = 0; cand < 4; cand++) {
+  for (int cand = 0; cand < 6; cand++) {
     const int ib = (cand & 1) ? 16 : 0, xp = cand >> 1;
     for (int k = 0; k < 6; k++) {
       p->fft_ib[k] = ib;
@@ -936,8 +936,8 @@ mrg_status mrg_set_fft_tuning(mrg_plan *p, const int ib[6], const int xp[6]) {
       set_error("lines per CTA out of range (0..32)");
       return MRG_ERR_INVALID;
     }
-    if (xp && (xp[k] < 0 || xp[k] > 1)) {
-      set_error("xp must be 0 or 1");
+    if (xp && (xp[k] < 0 || xp[k] > 2)) {
+      set_error("xp must be 0, 1 or 2");
       return MRG_ERR_INVALID;
     }
   }

@@ -533,9 +533,9 @@ __global__ void __launch_bounds__(8 * P) k_fft_pp(const FftPass p, int ntiles) {
 // image row X[o][0..Lin), which becomes (w X)[l] in place once it has landed, w = (winz *
 // winy) * winx.  The 8-point step multiplies each map value by it as it reads the row
 // (src/gridFFT.cpp:972-986: image = (w X) smap).
-template <int Q, int P>
-__global__ void __launch_bounds__(8 * P) k_fft_ps(const FftPass p, int ntiles) {
-  constexpr int S = 8 * Q, IB = P, NPAIR = IB / 2;
+template <int Q, int P, int R = 8>
+__global__ void __launch_bounds__(R * P) k_fft_ps(const FftPass p, int ntiles) {
+  constexpr int S = R * Q, IB = P, NPAIR = IB / 2;
   extern __shared__ float2 sm[];  // [S][IB] data, S twiddles, S image row
   float2 *tw = sm + S * (IB + 1);
   float2 *xr = tw + S;
@@ -581,21 +581,21 @@ __global__ void __launch_bounds__(8 * P) k_fft_ps(const FftPass p, int ntiles) {
       }
     }
     __syncthreads();
-    // ---- step A with set_image: 8-point DFTs over n1 (rows Q*n1 + n2) ----
-    for (int n2 = t; n2 < Q; n2 += 8) {
-      float2 a[8];
+    // ---- step A with set_image: R-point DFTs over n1 (rows Q*n1 + n2) ----
+    for (int n2 = t; n2 < Q; n2 += R) {
+      float2 a[R];
       float2 *c2 = col + n2 * IB;
 #pragma unroll
-      for (int n1 = 0; n1 < 8; n1++) {
+      for (int n1 = 0; n1 < R; n1++) {
         a[n1] = c2[Q * n1 * IB];
         const int li = Q * n1 + n2 - p.in_off;
         if ((unsigned)li < (unsigned)p.Lin) a[n1] = cmul(xr[li], a[n1]);
       }
-      reg_fft<8, -1, S>(a, tw);
+      reg_fft<R, -1, S>(a, tw);
 #pragma unroll
-      for (int k1 = 1; k1 < 8; k1++) a[k1] = cmul(a[k1], twid<-1>(tw, n2 * k1));
+      for (int k1 = 1; k1 < R; k1++) a[k1] = cmul(a[k1], twid<-1>(tw, n2 * k1));
 #pragma unroll
-      for (int k1 = 0; k1 < 8; k1++) c2[Q * k1 * IB] = a[k1];
+      for (int k1 = 0; k1 < R; k1++) c2[Q * k1 * IB] = a[k1];
     }
     __syncthreads();
     // ---- step C: rows into registers, then the next tile's copies ----
@@ -611,7 +611,7 @@ __global__ void __launch_bounds__(8 * P) k_fft_ps(const FftPass p, int ntiles) {
     const float sc = p.scale;
 #pragma unroll
     for (int k2 = 0; k2 < Q; k2++) {
-      const int r = t + 8 * k2 - p.out_off;
+      const int r = t + R * k2 - p.out_off;
       if (r >= 0 && r < p.Lout) go[(int64_t)r * p.out_ls] = make_float2(v[k2].x * sc, v[k2].y * sc);
     }
   }
@@ -623,9 +623,9 @@ __global__ void __launch_bounds__(8 * P) k_fft_ps(const FftPass p, int ntiles) {
 // row of X are copied (a second group) while the tile is transformed.  Each thread puts
 // w v conj(smap) of its coil in place of the map value, then thread r sums row r over the
 // coils into X[o][r] (src/gridFFT.cpp:926-941), so the sum needs no atomics.
-template <int Q, int P>
-__global__ void __launch_bounds__(8 * P) k_fft_pa(const FftPass p, int ntiles) {
-  constexpr int S = 8 * Q, IB = P, NPAIR = IB / 2;
+template <int Q, int P, int R = 8>
+__global__ void __launch_bounds__(R * P) k_fft_pa(const FftPass p, int ntiles) {
+  constexpr int S = R * Q, IB = P, NPAIR = IB / 2;
   extern __shared__ float2 sm[];  // [S][IB] data, S twiddles, [Lout][IB] maps, Lout values of X
   float2 *tw = sm + S * (IB + 1);
   float2 *mp = tw + S;
@@ -670,16 +670,16 @@ __global__ void __launch_bounds__(8 * P) k_fft_pa(const FftPass p, int ntiles) {
   for (; tile < ntiles; tile += gridDim.x) {
     asm volatile("cp.async.wait_group 1;\n" ::: "memory");  // this tile's input
     __syncthreads();
-    for (int n2 = t; n2 < Q; n2 += 8) {
-      float2 a[8];
+    for (int n2 = t; n2 < Q; n2 += R) {
+      float2 a[R];
       float2 *c2 = col + n2 * IB;
 #pragma unroll
-      for (int n1 = 0; n1 < 8; n1++) a[n1] = c2[Q * n1 * IB];
-      reg_fft<8, +1, S>(a, tw);
+      for (int n1 = 0; n1 < R; n1++) a[n1] = c2[Q * n1 * IB];
+      reg_fft<R, +1, S>(a, tw);
 #pragma unroll
-      for (int k1 = 1; k1 < 8; k1++) a[k1] = cmul(a[k1], twid<+1>(tw, n2 * k1));
+      for (int k1 = 1; k1 < R; k1++) a[k1] = cmul(a[k1], twid<+1>(tw, n2 * k1));
 #pragma unroll
-      for (int k1 = 0; k1 < 8; k1++) c2[Q * k1 * IB] = a[k1];
+      for (int k1 = 0; k1 < R; k1++) c2[Q * k1 * IB] = a[k1];
     }
     __syncthreads();
     float2 v[Q];
@@ -698,7 +698,7 @@ __global__ void __launch_bounds__(8 * P) k_fft_pa(const FftPass p, int ntiles) {
     const float sc = p.scale;
 #pragma unroll
     for (int k2 = 0; k2 < Q; k2++) {
-      const int r = t + 8 * k2 - p.out_off;
+      const int r = t + R * k2 - p.out_off;
       if (r >= 0 && r < p.Lout) {
         float2 val = make_float2(v[k2].x * sc, v[k2].y * sc);
         const float w = lw * __ldg(p.wl + r);
@@ -746,23 +746,25 @@ static mrg_status launch_persistent(K kern, int threads, size_t smem, size_t sme
   return MRG_OK;
 }
 
-template <int Q, int P>
+// R = 8 or 16 threads per line (16: twice the warps per CTA at the same shared memory, for
+// the long lines whose tiles leave room for one or two CTAs per SM)
+template <int Q, int P, int R = 8>
 static mrg_status launch_ps(const FftPass &pp, cudaStream_t st) {
-  constexpr int S = 8 * Q;
+  constexpr int S = R * Q;
   const size_t smem = (size_t)S * (P + 3) * sizeof(float2);
   static DeviceOnce once;
   static int ctas = 1;
-  return launch_persistent(k_fft_ps<Q, P>, 8 * P, smem, smem, once, ctas, (int)(pp.nlines / P), pp, st);
+  return launch_persistent(k_fft_ps<Q, P, R>, R * P, smem, smem, once, ctas, (int)(pp.nlines / P), pp, st);
 }
 
-template <int Q, int P>
+template <int Q, int P, int R = 8>
 static mrg_status launch_pa(const FftPass &pp, cudaStream_t st) {
-  constexpr int S = 8 * Q;
+  constexpr int S = R * Q;
   const size_t smem = ((size_t)S * (P + 2) + (size_t)pp.Lout * (P + 1)) * sizeof(float2);
   const size_t cap = ((size_t)S * (P + 2) + (size_t)S * (P + 1)) * sizeof(float2);
   static DeviceOnce once;
   static int ctas = 1;
-  return launch_persistent(k_fft_pa<Q, P>, 8 * P, smem, cap, once, ctas, (int)(pp.nlines / P), pp, st);
+  return launch_persistent(k_fft_pa<Q, P, R>, R * P, smem, cap, once, ctas, (int)(pp.nlines / P), pp, st);
 }
 
 template <int Q, int SIGN, int P>
@@ -842,11 +844,19 @@ static mrg_status launch_q(const FftPass &p, cudaStream_t st) {
     // persistent when the plan's tuning chose it
     if (p.xp && p.wmode == 1 && p.has_smap && pp.nib && p.vec16 && !p.lfast && p.inner == p.C && p.in_ls == p.C &&
         (p.IB == 16 || p.IB == 32) && p.nlines / p.IB <= 0x7fffffff) {
-      if (p.mode == FFT_SETIMG && p.in_os % p.C == 0 && p.Lin <= R * Q)
+      // xp == 2: 16 threads per line, for the lines of 288, 320 and 384 points
+      constexpr bool r16 = (Q == 36 || Q == 40 || Q == 48);
+      if (p.mode == FFT_SETIMG && p.in_os % p.C == 0 && p.Lin <= R * Q) {
+        if constexpr (r16)
+          if (p.xp == 2) return p.IB == 16 ? launch_ps<Q / 2, 16, 16>(pp, st) : launch_ps<Q / 2, 32, 16>(pp, st);
         return p.IB == 16 ? launch_ps<Q, 16>(pp, st) : launch_ps<Q, 32>(pp, st);
+      }
       if (p.mode == FFT_ACCUM && p.IB == p.C && !p.acc_atomic && p.Lout <= R * Q && p.out_os % 2 == 0 &&
-          p.out_ls % 2 == 0 && ((uintptr_t)p.smap & 15) == 0)
+          p.out_ls % 2 == 0 && ((uintptr_t)p.smap & 15) == 0) {
+        if constexpr (r16)
+          if (p.xp == 2) return p.IB == 16 ? launch_pa<Q / 2, 16, 16>(pp, st) : launch_pa<Q / 2, 32, 16>(pp, st);
         return p.IB == 16 ? launch_pa<Q, 16>(pp, st) : launch_pa<Q, 32>(pp, st);
+      }
     }
     if (!p.lfast && p.IB == 32) return launch_qp<Q, 32>(pp, grid, block, smem, st);
     if (!p.lfast && p.IB == 16) return launch_qp<Q, 16>(pp, grid, block, smem, st);
