@@ -102,8 +102,10 @@ mrg_status mrg_set_traj(mrg_plan *plan, int frame, const float *kx, const float 
                         const float *kw, int64_t M, void *stream);
 
 /* Sample bookkeeping of one frame after mrg_set_traj: M samples, nvalid of them
- * contribute (kw != 0 and inside the grid), npairs (sample, block) pairs, nitems
- * gridding work items and ntaps grid points read by one ungridding (the sum of every
+ * contribute (kw != 0 and inside the grid), npairs (sample, block) pairs and nitems
+ * gridding work items of the 8x2x2 block lists (of the 8x4x4 region lists of the tcgen05
+ * kernel when the block lists are not built: a plan tuned to that kernel skips them on
+ * later trajectories), and ntaps grid points read by one ungridding (the sum of every
  * valid sample's nx*ny*nz; computed on the device when ntaps is not NULL).  Any output
  * may be NULL. */
 mrg_status mrg_frame_info(const mrg_plan *plan, int frame, int64_t *M, int64_t *nvalid, int64_t *npairs,

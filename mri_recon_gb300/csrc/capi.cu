@@ -857,10 +857,16 @@ mrg_status mrg_set_traj(mrg_plan *p, int frame, const float *kx, const float *ky
                      (const float *)dw, M, p->max_pairs, regions, st));
   invalidate_graphs(p);
   MRG_TRY(ensure_y(p, (int64_t)p->frames[frame].nvalid * p->C));
+  FrameTraj &ft = p->frames[frame];
+  const bool reuse = p->cfg.tile == 0 && p->tuned && ft.nvalid <= 2 * p->tuned_nvalid &&
+                     2 * ft.nvalid >= p->tuned_nvalid;
+  // the block pair lists only where a block-based gridding kernel may run: the autotuner
+  // times them, and a reused choice may be one of them
+  if (!regions || !reuse || p->tuned_cc > -100 || p->cfg.tile != 0)
+    MRG_TRY(build_block_pairs(gc, ft, p->max_pairs, st));
   if (p->cfg.tile == 0) {
-    FrameTraj &ft = p->frames[frame];
     const int64_t nv = ft.nvalid;
-    if (p->tuned && nv <= 2 * p->tuned_nvalid && 2 * nv >= p->tuned_nvalid) {
+    if (reuse) {
       ft.ungrid_G = p->tuned_G;
       ft.ungrid_spb = p->tuned_spb;
       ft.ungrid_cpl = p->tuned_cpl;
@@ -891,8 +897,9 @@ mrg_status mrg_frame_info(const mrg_plan *p, int frame, int64_t *M, int64_t *nva
   const FrameTraj &ft = p->frames[frame];
   if (M) *M = ft.M;
   if (nvalid) *nvalid = ft.nvalid;
-  if (npairs) *npairs = ft.blocks.npairs;
-  if (nitems) *nitems = ft.blocks.nitems;
+  const PairSet &ps = ft.blocks.built ? ft.blocks : ft.regions;
+  if (npairs) *npairs = ps.npairs;
+  if (nitems) *nitems = ps.nitems;
   if (ntaps) MRG_TRY(count_taps(ft, ntaps));
   return MRG_OK;
 }
@@ -968,6 +975,7 @@ mrg_status mrg_frame_set_tuning(mrg_plan *p, int frame, const int in[5]) {
     set_error("gridding launch shape not available for this plan's coil count and grid_mode");
     return MRG_ERR_INVALID;
   }
+  if (cc > -100) MRG_TRY(build_block_pairs(grid_const(p), ft, p->max_pairs, (cudaStream_t)0));
   ft.ungrid_G = G;
   ft.ungrid_spb = spb;
   ft.grid_cc = cc;
@@ -989,7 +997,7 @@ mrg_status mrg_set_data(mrg_plan *p, int frame, const void *data, int64_t coil_s
     return MRG_ERR_INVALID;
   }
   cudaStream_t st = (cudaStream_t)stream;
-  if (!ft.dsorted) MRG_CUDA(cudaMalloc(&ft.dsorted, sizeof(float2) * std::max<int64_t>(1, (int64_t)ft.nvalid * p->C)));
+  MRG_TRY(grow(ft.dsorted, ft.cap_dsorted, (int64_t)ft.nvalid * p->C));
   void *src;
   bool staged;
   const size_t bytes = sizeof(float2) * (size_t)(coil_stride * (p->C - 1) + ft.M);
@@ -1474,7 +1482,7 @@ mrg_status mrg_grad(mrg_plan *p, int frame, const void *X, const void *y, int64_
   }
   cudaStream_t st = (cudaStream_t)stream;
   const GridConst gc = grid_const(p);
-  if (!ft.sdw) MRG_TRY(launch_sample_dweights(gc, ft, st));
+  if (!ft.sdw_valid) MRG_TRY(launch_sample_dweights(gc, ft, st));
   const size_t ybytes = sizeof(float2) * (size_t)(coil_stride * (p->C - 1) + ft.M);
   void *dX, *dy, *dgx, *dgk;
   bool sX, sy, sgx, sgk;

@@ -700,7 +700,7 @@ mrg_status pack_region_items(const GridConst &gc, PairSet &ps, cudaStream_t st) 
 // The caller zeroes the split regions (ft.regions.split) first.
 mrg_status launch_grid_umma(const GridConst &gc, const FrameTraj &ft, int cc, const float2 *yw, float2 *grid,
                             cudaStream_t st) {
-  if (!umma_supported(gc.C) || ft.regions.items == nullptr || (ft.regions.nitems > 0 && ft.rtab == nullptr)) {
+  if (!umma_supported(gc.C) || !ft.regions.built || (ft.regions.nitems > 0 && ft.rtab == nullptr)) {
     set_error("tensor-memory gridding needs >= 8 coils and region pair lists");
     return MRG_ERR_UNSUPPORTED;
   }

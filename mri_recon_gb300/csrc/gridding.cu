@@ -112,6 +112,87 @@ __global__ void k_scan(const int *__restrict__ in, int *out, int n) {
   if (n == 0 && t == 0) out[0] = 0;
 }
 
+// Exclusive prefix sums of large count arrays in three passes: per chunk of SCAN_CHUNK
+// counts a CTA sum, the (few) chunk sums scanned by k_scan, then each chunk scanned in
+// shared memory and offset.  out[n] = the total.  Counts are non-negative and their total
+// fits in an int (pair and sample counts of one frame).
+constexpr int SCAN_CHUNK = 8192;  // 1024 threads x 8 counts
+
+__global__ void __launch_bounds__(1024) k_scan_sums(const int *__restrict__ in, int n, int *__restrict__ sums) {
+  __shared__ int ws[32];
+  const int base = blockIdx.x * SCAN_CHUNK;
+  int s = 0;
+  for (int k = threadIdx.x; k < SCAN_CHUNK; k += 1024)
+    if (base + k < n) s += in[base + k];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    int v = ws[threadIdx.x];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (threadIdx.x == 0) sums[blockIdx.x] = v;
+  }
+}
+
+__global__ void __launch_bounds__(1024) k_scan_chunks(const int *__restrict__ in, int n,
+                                                      const int *__restrict__ offs, int *__restrict__ out) {
+  __shared__ int ws[32];
+  const int base = blockIdx.x * SCAN_CHUNK, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // thread t takes counts base + 8t .. base + 8t + 7
+  int v[8], s = 0;
+#pragma unroll
+  for (int i = 0; i < 8; i++) {
+    const int k = base + 8 * threadIdx.x + i;
+    v[i] = k < n ? in[k] : 0;
+    s += v[i];
+  }
+  int inc = s;  // inclusive scan of the thread sums within the warp
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += t;
+  }
+  if (lane == 31) ws[warp] = inc;
+  __syncthreads();
+  if (warp == 0) {
+    int w = ws[lane], wi = w;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, wi, o);
+      if (lane >= o) wi += t;
+    }
+    ws[lane] = wi - w;  // exclusive over warps
+  }
+  __syncthreads();
+  int run = offs[blockIdx.x] + ws[warp] + inc - s;
+#pragma unroll
+  for (int i = 0; i < 8; i++) {
+    const int k = base + 8 * threadIdx.x + i;
+    if (k < n) out[k] = run;
+    run += v[i];
+  }
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 1023) out[n] = run;
+}
+
+// out[0..n] = exclusive prefix sums of in[0..n) and the total (out has n + 1 entries; one
+// more, out[n + 1], may be written as scratch by the single-CTA path for small n).
+static mrg_status launch_scan(const int *in, int *out, int n, cudaStream_t st) {
+  if (n <= 4 * SCAN_CHUNK) {
+    k_scan<<<1, 1024, 0, st>>>(in, out, n);
+    count_launch();
+    return cudaGetLastError() == cudaSuccess ? MRG_OK : MRG_ERR_CUDA;
+  }
+  const int nch = (n + SCAN_CHUNK - 1) / SCAN_CHUNK;
+  int *sums = nullptr;
+  MRG_CUDA(cudaMallocAsync(&sums, sizeof(int) * (size_t)(2 * nch + 2), st));
+  int *offs = sums + nch + 1;
+  k_scan_sums<<<nch, 1024, 0, st>>>(in, n, sums);
+  k_scan<<<1, 1024, 0, st>>>(sums, offs, nch);
+  k_scan_chunks<<<nch, 1024, 0, st>>>(in, n, offs, out);
+  count_launch(3);
+  const bool ok = cudaGetLastError() == cudaSuccess;
+  cudaFreeAsync(sums, st);
+  return ok ? MRG_OK : MRG_ERR_CUDA;
+}
+
 __device__ __forceinline__ float taper(float kr, float k_rad) {
   return (float)exp(-(double)kr / (2.0 * (double)k_rad * (double)k_rad));
 }
@@ -266,15 +347,11 @@ __global__ void k_item_fill(int nblocks, const int *__restrict__ pcnt, const int
 }
 
 
-template <typename T>
-static mrg_status dalloc(T **p, int64_t n) {
-  *p = nullptr;
-  if (n <= 0) n = 1;
-  MRG_CUDA(cudaMalloc((void **)p, sizeof(T) * (size_t)n));
-  return MRG_OK;
-}
-
 void traj_free(FrameTraj &ft) {
+  SetupScratch &x = ft.scr;
+  for (void *q : {(void *)x.pos, (void *)x.tap, (void *)x.key, (void *)x.cnt, (void *)x.off, (void *)x.cur,
+                  (void *)x.pcnt, (void *)x.poff, (void *)x.pcur, (void *)x.icnt, (void *)x.ioff, (void *)x.nsplit})
+    cudaFree(q);
   cudaFree(ft.spos);
   cudaFree(ft.stap);
   cudaFree(ft.skr);
@@ -290,6 +367,23 @@ void traj_free(FrameTraj &ft) {
   ft = FrameTraj();
 }
 
+// Clears a frame for a new trajectory, keeping its device arrays for reuse.
+static void traj_reset(FrameTraj &ft) {
+  ft.M = 0;
+  ft.nvalid = 0;
+  ft.has_data = false;
+  ft.sdw_valid = false;
+  for (PairSet *ps : {&ft.blocks, &ft.regions}) {
+    ps->npairs = 0;
+    ps->nitems = 0;
+    ps->nsplit = 0;
+    ps->built = false;
+  }
+  ft.nrchunks = 0;
+  ft.ungrid_G = ft.ungrid_spb = ft.ungrid_cpl = ft.ungrid_uy = ft.grid_cc = 0;
+  ft.tune_ungrid_ms = ft.tune_grid_ms = 0.f;
+}
+
 static mrg_status read_int(const int *dev, int *host, cudaStream_t st, const char *what) {
   if (cudaMemcpyAsync(host, dev, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
       cudaStreamSynchronize(st) != cudaSuccess) {
@@ -300,29 +394,20 @@ static mrg_status read_int(const int *dev, int *host, cudaStream_t st, const cha
 }
 
 mrg_status build_region_tables(FrameTraj &ft, cudaStream_t st) {
-  cudaFree(ft.rtab);
-  cudaFree(ft.rchunk);
-  ft.rtab = nullptr;
-  ft.rchunk = nullptr;
   ft.nrchunks = 0;
   const int n = ft.regions.nitems;
   if (n == 0) return MRG_OK;
   int *cnt = nullptr;
-  mrg_status rs = dalloc(&cnt, n + 1);
-  if (rs == MRG_OK) rs = dalloc(&ft.rchunk, n + 2);
-  if (rs == MRG_OK) rs = launch_item_chunks(ft, cnt, st);
-  if (rs == MRG_OK) {
-    k_scan<<<1, 1024, 0, st>>>(cnt, ft.rchunk, n);
-    count_launch();
-    if (cudaGetLastError() != cudaSuccess) rs = MRG_ERR_CUDA;
-  }
+  MRG_TRY(grow(ft.scr.icnt, ft.scr.cap_icnt, n + 1));  // the item scratch is free again here
+  cnt = ft.scr.icnt;
+  MRG_TRY(grow(ft.rchunk, ft.cap_rchunk, n + 2));
+  MRG_TRY(launch_item_chunks(ft, cnt, st));
+  MRG_TRY(launch_scan(cnt, ft.rchunk, n, st));
   int total = 0;
-  if (rs == MRG_OK) rs = read_int(ft.rchunk + n, &total, st, "region chunk count failed");
-  cudaFree(cnt);
-  if (rs != MRG_OK) return rs;
+  MRG_TRY(read_int(ft.rchunk + n, &total, st, "region chunk count failed"));
   ft.nrchunks = total;
   const int64_t nf = (int64_t)total * umma_table_floats();
-  MRG_TRY(dalloc(&ft.rtab, nf));
+  MRG_TRY(grow(ft.rtab, ft.cap_rtab, nf));
   // zero: the pad entries of a last, partial k-step must be finite (their samples are zero)
   MRG_TRY(launch_zero(ft.rtab, sizeof(float) * (size_t)std::max<int64_t>(nf, 1), st));
   return launch_region_tables(ft, st);
@@ -353,19 +438,17 @@ void pair_set_free(PairSet &ps) {
 // so that every grid point is written), flagged when there are several (those flush
 // with atomics into a pre-zeroed block).
 static mrg_status build_pairs(const BlockShape &bs, int nvalid, const int4 *sst, int max_pairs, cudaStream_t st,
-                              PairSet &ps) {
-  pair_set_free(ps);
+                              PairSet &ps, SetupScratch &x) {
+  ps.npairs = 0;
+  ps.nitems = 0;
+  ps.nsplit = 0;
+  ps.built = false;
   const int nblocks = bs.nb[0] * bs.nb[1] * bs.nb[2];
-  int *pcnt = nullptr, *poff = nullptr, *pcur = nullptr, *icnt = nullptr, *ioff = nullptr, *nsplit = nullptr;
   mrg_status rs = MRG_OK;
-  auto cleanup = [&]() {
-    cudaFree(pcnt); cudaFree(poff); cudaFree(pcur); cudaFree(icnt); cudaFree(ioff); cudaFree(nsplit);
-  };
 #define PAIRS_TRY(x)         \
   do {                       \
     rs = (x);                \
     if (rs != MRG_OK) {      \
-      cleanup();             \
       pair_set_free(ps);     \
       return rs;             \
     }                        \
@@ -375,71 +458,70 @@ static mrg_status build_pairs(const BlockShape &bs, int nvalid, const int4 *sst,
     count_launch();                                                         \
     if (cudaGetLastError() != cudaSuccess) PAIRS_TRY(MRG_ERR_CUDA);         \
   } while (0)
-  PAIRS_TRY(dalloc(&pcnt, nblocks + 1));
-  PAIRS_TRY(dalloc(&poff, nblocks + 2));
-  PAIRS_TRY(dalloc(&pcur, nblocks + 1));
+  PAIRS_TRY(grow(x.pcnt, x.cap_pcnt, nblocks + 1));
+  PAIRS_TRY(grow(x.poff, x.cap_poff, nblocks + 2));
+  PAIRS_TRY(grow(x.pcur, x.cap_pcur, nblocks + 1));
+  int *pcnt = x.pcnt, *poff = x.poff, *pcur = x.pcur;
   PAIRS_TRY(launch_zero(pcnt, sizeof(int) * (nblocks + 1), st));
   PAIRS_TRY(launch_zero(pcur, sizeof(int) * (nblocks + 1), st));
   if (nvalid > 0) {
     k_pairs<false><<<grid_blocks(nvalid, 256), 256, 0, st>>>(bs, nvalid, sst, pcnt, nullptr, nullptr, nullptr);
     PAIRS_LAUNCHED();
   }
-  k_scan<<<1, 1024, 0, st>>>(pcnt, poff, nblocks);
-  PAIRS_LAUNCHED();
+  PAIRS_TRY(launch_scan(pcnt, poff, nblocks, st));
   int npairs = 0;
   PAIRS_TRY(read_int(poff + nblocks, &npairs, st, "pair count failed"));
   ps.npairs = npairs;
-  PAIRS_TRY(dalloc(&ps.pairs, npairs));
+  PAIRS_TRY(grow(ps.pairs, ps.cap_pairs, npairs));
   if (nvalid > 0) {
     k_pairs<true><<<grid_blocks(nvalid, 256), 256, 0, st>>>(bs, nvalid, sst, nullptr, poff, pcur, ps.pairs);
     PAIRS_LAUNCHED();
   }
-  PAIRS_TRY(dalloc(&icnt, nblocks + 1));
-  PAIRS_TRY(dalloc(&ioff, nblocks + 2));
-  PAIRS_TRY(dalloc(&nsplit, 1));
+  PAIRS_TRY(grow(x.icnt, x.cap_icnt, nblocks + 1));
+  PAIRS_TRY(grow(x.ioff, x.cap_ioff, nblocks + 2));
+  PAIRS_TRY(grow(x.nsplit, x.cap_nsplit, 1));
+  int *icnt = x.icnt, *ioff = x.ioff, *nsplit = x.nsplit;
   PAIRS_TRY(launch_zero(nsplit, sizeof(int), st));
   k_item_count<<<grid_blocks(nblocks, 256), 256, 0, st>>>(nblocks, pcnt, max_pairs, icnt);
   PAIRS_LAUNCHED();
-  k_scan<<<1, 1024, 0, st>>>(icnt, ioff, nblocks);
-  PAIRS_LAUNCHED();
+  PAIRS_TRY(launch_scan(icnt, ioff, nblocks, st));
   int nitems = 0;
   PAIRS_TRY(read_int(ioff + nblocks, &nitems, st, "item count failed"));
   ps.nitems = nitems;
-  PAIRS_TRY(dalloc(&ps.items, nitems));
-  PAIRS_TRY(dalloc(&ps.split, nblocks));
+  PAIRS_TRY(grow(ps.items, ps.cap_items, nitems));
+  PAIRS_TRY(grow(ps.split, ps.cap_split, nblocks));
   k_item_fill<<<grid_blocks(nblocks, 256), 256, 0, st>>>(nblocks, pcnt, poff, icnt, ioff, max_pairs, ps.items,
                                                          ps.split, nsplit);
   PAIRS_LAUNCHED();
   int ns = 0;
   PAIRS_TRY(read_int(nsplit, &ns, st, "item fill failed"));
   ps.nsplit = ns;
-  cleanup();
+  ps.built = true;
 #undef PAIRS_TRY
 #undef PAIRS_LAUNCHED
   return MRG_OK;
 }
 
+mrg_status build_block_pairs(const GridConst &gc, FrameTraj &ft, int max_pairs, cudaStream_t st) {
+  if (ft.blocks.built) return MRG_OK;
+  return build_pairs(block_shape(gc), ft.nvalid, ft.sst, max_pairs, st, ft.blocks, ft.scr);
+}
+
 mrg_status traj_setup(const GridConst &gc, FrameTraj &ft, const float *kx, const float *ky, const float *kz,
                       const float *kw, int64_t M, int max_pairs, bool regions, cudaStream_t st) {
-  traj_free(ft);
+  traj_reset(ft);
   if (M <= 0 || M >= (int64_t)1 << 31) {
     set_error("trajectory length must be in [1, 2^31)");
     return MRG_ERR_INVALID;
   }
   const int ntiles = 1 << (3 * gc.mbits);  // Morton key space of the sort tiles
   ft.M = M;
-  float4 *pos = nullptr;
-  float *tap = nullptr;
-  int *key = nullptr, *cnt = nullptr, *off = nullptr, *cur = nullptr;
+  SetupScratch &x = ft.scr;
   mrg_status rs = MRG_OK;
-  auto cleanup = [&]() {
-    cudaFree(pos); cudaFree(tap); cudaFree(key); cudaFree(cnt); cudaFree(off); cudaFree(cur);
-  };
 #define SETUP_TRY(x)         \
   do {                       \
     rs = (x);                \
     if (rs != MRG_OK) {      \
-      cleanup();             \
       traj_free(ft);         \
       return rs;             \
     }                        \
@@ -450,22 +532,24 @@ mrg_status traj_setup(const GridConst &gc, FrameTraj &ft, const float *kx, const
     if (cudaGetLastError() != cudaSuccess) SETUP_TRY(MRG_ERR_CUDA);                       \
   } while (0)
   // 1. positions, validity, sort key (tile of the sample centre); counting sort by tile
-  SETUP_TRY(dalloc(&pos, M));
-  SETUP_TRY(dalloc(&tap, M));
-  SETUP_TRY(dalloc(&key, M));
-  SETUP_TRY(dalloc(&cnt, ntiles + 1));
-  SETUP_TRY(dalloc(&off, ntiles + 2));
-  SETUP_TRY(dalloc(&cur, ntiles + 1));
-  SETUP_TRY(dalloc(&ft.spos, M));
-  SETUP_TRY(dalloc(&ft.stap, M));
-  SETUP_TRY(dalloc(&ft.skr, M));
-  SETUP_TRY(dalloc(&ft.perm, M));
+  SETUP_TRY(grow(x.pos, x.cap_pos, M));
+  SETUP_TRY(grow(x.tap, x.cap_tap, M));
+  SETUP_TRY(grow(x.key, x.cap_key, M));
+  SETUP_TRY(grow(x.cnt, x.cap_cnt, ntiles + 1));
+  SETUP_TRY(grow(x.off, x.cap_off, ntiles + 2));
+  SETUP_TRY(grow(x.cur, x.cap_cur, ntiles + 1));
+  SETUP_TRY(grow(ft.spos, ft.cap_spos, M));
+  SETUP_TRY(grow(ft.stap, ft.cap_stap, M));
+  SETUP_TRY(grow(ft.skr, ft.cap_skr, M));
+  SETUP_TRY(grow(ft.perm, ft.cap_perm, M));
+  float4 *pos = x.pos;
+  float *tap = x.tap;
+  int *key = x.key, *cnt = x.cnt, *off = x.off, *cur = x.cur;
   SETUP_TRY(launch_zero(cnt, sizeof(int) * (ntiles + 1), st));
   SETUP_TRY(launch_zero(cur, sizeof(int) * (ntiles + 1), st));
   k_traj_prep<<<grid_blocks(M, 256), 256, 0, st>>>(gc, kx, ky, kz, kw, M, pos, tap, key, cnt, ntiles);
   SETUP_LAUNCHED();
-  k_scan<<<1, 1024, 0, st>>>(cnt, off, ntiles + 1);
-  SETUP_LAUNCHED();
+  SETUP_TRY(launch_scan(cnt, off, ntiles + 1, st));
   k_traj_sort<<<grid_blocks(M, 256), 256, 0, st>>>(M, gc.k_rad, key, off, cur, pos, tap, ft.spos, ft.stap, ft.skr,
                                                     ft.perm);
   SETUP_LAUNCHED();
@@ -474,20 +558,19 @@ mrg_status traj_setup(const GridConst &gc, FrameTraj &ft, const float *kx, const
   ft.nvalid = nvalid;
 
   // 2. tap weights once per trajectory
-  SETUP_TRY(dalloc(&ft.swt, 6 * (int64_t)nvalid));
-  SETUP_TRY(dalloc(&ft.sst, nvalid));
+  SETUP_TRY(grow(ft.swt, ft.cap_swt, 6 * (int64_t)nvalid));
+  SETUP_TRY(grow(ft.sst, ft.cap_sst, nvalid));
   k_sample_weights<<<grid_blocks(nvalid, 256), 256, 0, st>>>(gc, nvalid, ft.spos, ft.swt, ft.sst);
   SETUP_LAUNCHED();
 
-  // 3-4. (sample, block) pair lists and work items for the 8x2x2 blocks, and for the
-  // 8x4x4 regions of the tensor-memory gridding kernel when it may run
-  SETUP_TRY(build_pairs(block_shape(gc), nvalid, ft.sst, max_pairs, st, ft.blocks));
+  // 3-4. (sample, region) pair lists, work items and chunk tables for the 8x4x4 regions of
+  // the tensor-memory gridding kernel when it may run; the 8x2x2 block lists of the other
+  // gridding kernels are built by build_block_pairs when one of those may run
   if (regions && umma_grid_fits(gc.S)) {
-    SETUP_TRY(build_pairs(region_shape(gc), nvalid, ft.sst, max_pairs, st, ft.regions));
+    SETUP_TRY(build_pairs(region_shape(gc), nvalid, ft.sst, max_pairs, st, ft.regions, x));
     SETUP_TRY(pack_region_items(gc, ft.regions, st));
     SETUP_TRY(build_region_tables(ft, st));
   }
-  cleanup();
 #undef SETUP_TRY
 #undef SETUP_LAUNCHED
   return MRG_OK;
@@ -1388,7 +1471,7 @@ bool grid_cc_allowed(int C, const FrameTraj &ft, int cc) {
   if (cc >= 0) return cc == 0 || cc == 8 || cc == 16;
   if (cc > -100) return (cc == -1 || cc == -2 || cc == -4 || cc == -8) && -cc <= default_grid_nt(C);
   const int c = -cc - 100;
-  return (c == 8 || c == 16 || c == 32) && umma_supported(C) && ft.regions.items != nullptr && c <= umma_default_cc(C);
+  return (c == 8 || c == 16 || c == 32) && umma_supported(C) && ft.regions.built && c <= umma_default_cc(C);
 }
 
 mrg_status launch_grid(const GridConst &gc, const FrameTraj &ft, const float2 *yw, float2 *grid, cudaStream_t st) {
@@ -1402,6 +1485,10 @@ mrg_status launch_grid(const GridConst &gc, const FrameTraj &ft, const float2 *y
       MRG_LAUNCHED();
     }
     return launch_grid_umma(gc, ft, ft.grid_cc <= -100 ? -ft.grid_cc - 100 : umma_default_cc(C), yw, grid, st);
+  }
+  if (!ft.blocks.built) {
+    set_error("block pair lists not built for this frame's gridding kernel");
+    return MRG_ERR_STATE;
   }
   if (ft.blocks.nsplit > 0) {
     const int64_t n = (int64_t)ft.blocks.nsplit * BLK_X * BLK_Y * BLK_Z * C;
@@ -1461,10 +1548,12 @@ __global__ void k_sample_dweights(GridConst g, int nvalid, const float4 *__restr
 }
 
 mrg_status launch_sample_dweights(const GridConst &gc, FrameTraj &ft, cudaStream_t st) {
-  if (!ft.sdw) MRG_CUDA(cudaMalloc(&ft.sdw, sizeof(float4) * 6 * (size_t)std::max(ft.nvalid, 1)));
-  if (ft.nvalid == 0) return MRG_OK;
-  k_sample_dweights<<<grid_blocks(ft.nvalid, 256), 256, 0, st>>>(gc, ft.nvalid, ft.spos, ft.sst, ft.sdw);
-  MRG_LAUNCHED();
+  MRG_TRY(grow(ft.sdw, ft.cap_sdw, 6 * (int64_t)ft.nvalid));
+  if (ft.nvalid > 0) {
+    k_sample_dweights<<<grid_blocks(ft.nvalid, 256), 256, 0, st>>>(gc, ft.nvalid, ft.spos, ft.sst, ft.sdw);
+    MRG_LAUNCHED();
+  }
+  ft.sdw_valid = true;
   return MRG_OK;
 }
 
@@ -1678,12 +1767,13 @@ mrg_status autotune_frame(const GridConst &gc, FrameTraj &ft, float2 *grid, floa
   for (int cc : {0, 16, 8, -8, -4, -2, -1, -132, -116, -108}) {
     const int mode = cc >= 0 ? 1 : (cc > -100 ? 2 : 3);
     if (gc.grid_mode != 0 && gc.grid_mode != mode) continue;
+    if (mode != 3 && !ft.blocks.built) continue;
     if (mode == 1 && cc > 0 && gc.C <= cc) continue;
     if (mode == 2 && -cc > default_grid_nt(gc.C)) continue;  // more coils per pass than the plan has
     if (mode == 2 && -cc < default_grid_nt(gc.C) / 2) continue;
     if (mode == 3) {
       const int c = -cc - 100;
-      if (!umma_supported(gc.C) || ft.regions.items == nullptr) continue;
+      if (!umma_supported(gc.C) || !ft.regions.built) continue;
       if (c > umma_default_cc(gc.C) || c < umma_default_cc(gc.C) / 2) continue;
     }
     ft.grid_cc = cc;

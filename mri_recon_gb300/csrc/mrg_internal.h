@@ -175,6 +175,21 @@ struct BlockShape {
 constexpr int RGN_X = 8, RGN_Y = 4, RGN_Z = 4;
 static_assert(RGN_X * RGN_Y * RGN_Z == 128, "one region row per TMEM lane");
 
+// A device array that trajectory set-ups reuse: it is reallocated only when a set-up
+// needs more bytes than it holds (cap), so repeated set-ups of similar trajectories
+// allocate and free nothing (cudaFree waits for the whole device).
+template <typename T>
+inline mrg_status grow(T *&p, size_t &cap, int64_t n) {
+  const size_t want = sizeof(T) * (size_t)(n > 1 ? n : 1);
+  if (p && cap >= want) return MRG_OK;
+  cudaFree(p);
+  p = nullptr;
+  cap = 0;
+  MRG_CUDA(cudaMalloc((void **)&p, want));
+  cap = want;
+  return MRG_OK;
+}
+
 // (sample, block) pairs of one block shape and the work items over them.
 struct PairSet {
   int *pairs = nullptr;     // sample index per (sample, block) pair, grouped by block
@@ -183,6 +198,18 @@ struct PairSet {
   int nitems = 0;
   int *split = nullptr;     // blocks with several work items (pre-zeroed, atomic flush)
   int nsplit = 0;
+  bool built = false;       // built for the frame's current trajectory
+  size_t cap_pairs = 0, cap_items = 0, cap_split = 0;
+};
+
+// Temporaries of a trajectory set-up, kept with the frame for the next one.
+struct SetupScratch {
+  float4 *pos = nullptr;
+  float *tap = nullptr;
+  int *key = nullptr, *cnt = nullptr, *off = nullptr, *cur = nullptr;
+  int *pcnt = nullptr, *poff = nullptr, *pcur = nullptr, *icnt = nullptr, *ioff = nullptr, *nsplit = nullptr;
+  size_t cap_pos = 0, cap_tap = 0, cap_key = 0, cap_cnt = 0, cap_off = 0, cap_cur = 0;
+  size_t cap_pcnt = 0, cap_poff = 0, cap_pcur = 0, cap_icnt = 0, cap_ioff = 0, cap_nsplit = 0;
 };
 
 struct FrameTraj {
@@ -205,11 +232,18 @@ struct FrameTraj {
   float2 *dsorted = nullptr;  // measured data [nvalid][C], unweighted
   float4 *sdw = nullptr;      // [nvalid][6] d(tap weight)/dk per axis (allocated by mrg_grad)
   bool has_data = false;
+  bool sdw_valid = false;     // sdw computed for the current trajectory
+  // bytes held by each array above (reused by the next set-up of this frame)
+  size_t cap_spos = 0, cap_stap = 0, cap_skr = 0, cap_perm = 0, cap_swt = 0, cap_sst = 0, cap_rtab = 0,
+         cap_rchunk = 0, cap_dsorted = 0, cap_sdw = 0;
+  SetupScratch scr;
   // launch shapes picked by autotune_frame (0: defaults)
   int ungrid_G = 0, ungrid_spb = 0, ungrid_cpl = 0, ungrid_uy = 0, grid_cc = 0;
   float tune_ungrid_ms = 0.f, tune_grid_ms = 0.f;
 };
 
+// The 8x2x2 block pair lists of the CUDA-core and mma.sync gridding kernels (once per trajectory).
+mrg_status build_block_pairs(const GridConst &gc, FrameTraj &ft, int max_pairs, cudaStream_t st);
 mrg_status traj_setup(const GridConst &gc, FrameTraj &ft, const float *kx, const float *ky, const float *kz,
                       const float *kw, int64_t M, int max_pairs, bool regions, cudaStream_t st);
 BlockShape block_shape(const GridConst &gc);
