@@ -205,7 +205,19 @@ static mrg_status dev_view(mrg_plan *p, int slot, const void *ptr, size_t bytes,
     return MRG_OK;
   }
   MRG_TRY(stage_buf(p, slot, bytes, dev));
-  if (copy_in) MRG_CUDA(cudaMemcpyAsync(*dev, ptr, bytes, cudaMemcpyHostToDevice, st));
+  if (copy_in) {
+    // large pinned inputs are read by the SMs through the buffer's device-side alias
+    // (both ends of the range pinned and mapped contiguously, so every read stays inside it)
+    cudaPointerAttributes a, z;
+    const char *last = static_cast<const char *>(ptr) + bytes - 1;
+    const bool pinned = bytes >= ((size_t)64 << 20) && cudaPointerGetAttributes(&a, ptr) == cudaSuccess &&
+                        a.type == cudaMemoryTypeHost && a.devicePointer && ((uintptr_t)a.devicePointer & 15) == 0 &&
+                        cudaPointerGetAttributes(&z, last) == cudaSuccess && z.type == cudaMemoryTypeHost &&
+                        static_cast<const char *>(z.devicePointer) == static_cast<const char *>(a.devicePointer) + (bytes - 1);
+    if (!pinned) cudaGetLastError();
+    if (pinned) MRG_TRY(launch_copy_from_host(*dev, a.devicePointer, bytes, st));
+    else MRG_CUDA(cudaMemcpyAsync(*dev, ptr, bytes, cudaMemcpyHostToDevice, st));
+  }
   *staged = true;
   return MRG_OK;
 }

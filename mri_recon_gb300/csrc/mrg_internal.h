@@ -323,6 +323,8 @@ struct Scalars {
 mrg_status launch_interleave(const float2 *src, int64_t stride, int C, int64_t n, float2 *dst, cudaStream_t st);
 mrg_status launch_deinterleave(const float2 *src, int C, int64_t n, float2 *dst, int64_t stride, cudaStream_t st);
 mrg_status launch_zero(void *p, size_t bytes, cudaStream_t st);
+// dst (device) <- bytes of pinned host memory addressed through its device-side alias src
+mrg_status launch_copy_from_host(void *dst, const void *src, size_t bytes, cudaStream_t st);
 mrg_status launch_copy(float2 *dst, const float2 *src, int64_t n, cudaStream_t st);
 mrg_status cg_dots(const float2 *R, const float2 *P, const float2 *L, int64_t n, double *part, int nblk,
                    Scalars *sc, cudaStream_t st);

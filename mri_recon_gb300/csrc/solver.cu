@@ -194,6 +194,26 @@ __global__ void k_zero(uint4 *p, int64_t n16, uint8_t *tail, int ntail) {
   if (blockIdx.x == 0 && (int)threadIdx.x < ntail) tail[threadIdx.x] = 0;
 }
 
+__global__ void k_copy16(uint4 *__restrict__ dst, const uint4 *__restrict__ src, int64_t n16, uint8_t *dtail,
+                         const uint8_t *stail, int ntail) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n16; i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = src[i];
+  if (blockIdx.x == 0 && (int)threadIdx.x < ntail) dtail[threadIdx.x] = stail[threadIdx.x];
+}
+
+// Copy from pinned host memory (src: its device-side address) by the SMs: many loads in
+// flight over the CPU-GPU link instead of one copy-engine transfer.  Both ends 16-byte aligned.
+mrg_status launch_copy_from_host(void *dst, const void *src, size_t bytes, cudaStream_t st) {
+  if (bytes == 0) return MRG_OK;
+  const int64_t n16 = (int64_t)(bytes / 16);
+  const int ntail = (int)(bytes - n16 * 16);
+  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((n16 + 511) / 512, 8 * (int64_t)device_sms()));
+  k_copy16<<<blocks, 512, 0, st>>>((uint4 *)dst, (const uint4 *)src, n16, (uint8_t *)dst + n16 * 16,
+                                   (const uint8_t *)src + n16 * 16, ntail);
+  MRG_LAUNCHED();
+  return MRG_OK;
+}
+
 mrg_status launch_zero(void *p, size_t bytes, cudaStream_t st) {
   if (bytes == 0) return MRG_OK;
   if (((uintptr_t)p & 15) != 0) {
