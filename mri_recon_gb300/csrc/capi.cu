@@ -476,7 +476,7 @@ static mrg_status run_E_grid(mrg_plan *p, const float2 *X, const float2 *smap, c
   b.nlines = Ny * Sx * C;
   b.in_ls = Ny * Sx * C; b.in_os = 0; b.out_ls = Ny * Sx * C; b.out_os = 0;
   b.scale = (float)(1. / std::sqrt((float)Sz));
-  b.in = p->d_t1; b.out = p->d_t2; b.C = C;
+  b.in = p->d_t1; b.out = p->d_t2; b.C = C; b.xp = p->fft_xp[1];
   fft_vectorize(b);
   MRG_TRY(launch_fft(b, st));
   tmark(p, 2, st);
@@ -490,7 +490,7 @@ static mrg_status run_E_grid(mrg_plan *p, const float2 *X, const float2 *smap, c
   c.nlines = Sz * Sx * C;
   c.in_ls = Sx * C; c.in_os = Ny * Sx * C; c.out_ls = Sx * C; c.out_os = Sy * Sx * C;
   c.scale = (float)(1. / std::sqrt((float)Sy));
-  c.in = p->d_t2; c.out = p->d_grid; c.C = C;
+  c.in = p->d_t2; c.out = p->d_grid; c.C = C; c.xp = p->fft_xp[2];
   fft_vectorize(c);
   MRG_TRY(launch_fft(c, st));
   return MRG_OK;
@@ -516,7 +516,7 @@ static mrg_status run_EH_yz(mrg_plan *p, const FrameTraj &ft, const float2 *y, c
   a.nlines = Sz * Sx * C;
   a.in_ls = Sx * C; a.in_os = Sy * Sx * C; a.out_ls = Sx * C; a.out_os = Ny * Sx * C;
   a.scale = (float)(1. / std::sqrt((float)Sy));
-  a.in = p->d_grid; a.out = p->d_t2; a.C = C;
+  a.in = p->d_grid; a.out = p->d_t2; a.C = C; a.xp = p->fft_xp[3];
   fft_vectorize(a);
   MRG_TRY(launch_fft(a, st));
   tmark(p, 2, st);
@@ -529,7 +529,7 @@ static mrg_status run_EH_yz(mrg_plan *p, const FrameTraj &ft, const float2 *y, c
   b.nlines = Ny * Sx * C;
   b.in_ls = Ny * Sx * C; b.in_os = 0; b.out_ls = Ny * Sx * C; b.out_os = 0;
   b.scale = (float)(1. / std::sqrt((float)Sz));
-  b.in = p->d_t2; b.out = p->d_t1; b.C = C;
+  b.in = p->d_t2; b.out = p->d_t1; b.C = C; b.xp = p->fft_xp[4];
   fft_vectorize(b);
   MRG_TRY(launch_fft(b, st));
   tmark(p, 3, st);

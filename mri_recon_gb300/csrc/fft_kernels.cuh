@@ -462,9 +462,9 @@ __global__ void __launch_bounds__(256, 2) k_fft(const FftPass p) {
 // registers, the next tile's copies are issued into the same shared memory, so they run
 // while this tile is transformed and stored (straight from registers, rows t + 8 k2 of
 // line j: IB lines x 8 bytes contiguous per row).
-template <int Q, int SIGN, int P>
-__global__ void __launch_bounds__(8 * P) k_fft_pp(const FftPass p, int ntiles) {
-  constexpr int S = 8 * Q, IB = P, NPAIR = IB / 2;
+template <int Q, int SIGN, int P, int R = 8>
+__global__ void __launch_bounds__(R * P) k_fft_pp(const FftPass p, int ntiles) {
+  constexpr int S = R * Q, IB = P, NPAIR = IB / 2;
   extern __shared__ float2 sm[];  // [S][IB] data, then S twiddles
   float2 *tw = sm + S * (IB + 1);
   const int tid = threadIdx.x;
@@ -494,17 +494,17 @@ __global__ void __launch_bounds__(8 * P) k_fft_pp(const FftPass p, int ntiles) {
   for (; tile < ntiles; tile += gridDim.x) {
     asm volatile("cp.async.wait_group 0;\n" ::: "memory");
     __syncthreads();
-    // ---- step A: 8-point DFTs over n1 (rows Q*n1 + n2), twiddle W_S^(n2*k1) ----
-    for (int n2 = t; n2 < Q; n2 += 8) {
-      float2 a[8];
+    // ---- step A: R-point DFTs over n1 (rows Q*n1 + n2), twiddle W_S^(n2*k1) ----
+    for (int n2 = t; n2 < Q; n2 += R) {
+      float2 a[R];
       float2 *c2 = col + n2 * IB;
 #pragma unroll
-      for (int n1 = 0; n1 < 8; n1++) a[n1] = c2[Q * n1 * IB];
-      reg_fft<8, SIGN, S>(a, tw);
+      for (int n1 = 0; n1 < R; n1++) a[n1] = c2[Q * n1 * IB];
+      reg_fft<R, SIGN, S>(a, tw);
 #pragma unroll
-      for (int k1 = 1; k1 < 8; k1++) a[k1] = cmul(a[k1], twid<SIGN>(tw, n2 * k1));
+      for (int k1 = 1; k1 < R; k1++) a[k1] = cmul(a[k1], twid<SIGN>(tw, n2 * k1));
 #pragma unroll
-      for (int k1 = 0; k1 < 8; k1++) c2[Q * k1 * IB] = a[k1];
+      for (int k1 = 0; k1 < R; k1++) c2[Q * k1 * IB] = a[k1];
     }
     __syncthreads();
     // ---- step C: rows Q*t .. Q*t+Q-1 into registers; then the buffer is free ----
@@ -521,7 +521,7 @@ __global__ void __launch_bounds__(8 * P) k_fft_pp(const FftPass p, int ntiles) {
     const float sc = p.scale;
 #pragma unroll
     for (int k2 = 0; k2 < Q; k2++) {
-      const int r = t + 8 * k2 - p.out_off;
+      const int r = t + R * k2 - p.out_off;
       if (r >= 0 && r < p.Lout) go[(int64_t)r * p.out_ls] = make_float2(v[k2].x * sc, v[k2].y * sc);
     }
   }
@@ -767,22 +767,22 @@ static mrg_status launch_pa(const FftPass &pp, cudaStream_t st) {
   return launch_persistent(k_fft_pa<Q, P, R>, R * P, smem, cap, once, ctas, (int)(pp.nlines / P), pp, st);
 }
 
-template <int Q, int SIGN, int P>
+template <int Q, int SIGN, int P, int R = 8>
 static mrg_status launch_pp(const FftPass &pp, cudaStream_t st) {
-  const size_t smem = (size_t)8 * Q * (P + 2) * sizeof(float2);
+  const size_t smem = (size_t)R * Q * (P + 2) * sizeof(float2);
   static DeviceOnce once;
   static int ctas = 1;  // resident CTAs per SM (the same kernel and shape on every device of a process)
   MRG_TRY(device_once(once, [smem]() -> mrg_status {
-    MRG_CUDA(cudaFuncSetAttribute(k_fft_pp<Q, SIGN, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    MRG_CUDA(cudaFuncSetAttribute(k_fft_pp<Q, SIGN, P, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int c = 0;
-    MRG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_fft_pp<Q, SIGN, P>, 8 * P, smem));
+    MRG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_fft_pp<Q, SIGN, P, R>, R * P, smem));
     ctas = c < 1 ? 1 : c;
     return MRG_OK;
   }));
   const int sms = device_sms();
   const int ntiles = (int)(pp.nlines / P);
   const int nblk = std::max(1, std::min(ntiles, sms * ctas));
-  k_fft_pp<Q, SIGN, P><<<nblk, 8 * P, smem, st>>>(pp, ntiles);
+  k_fft_pp<Q, SIGN, P, R><<<nblk, R * P, smem, st>>>(pp, ntiles);
   MRG_LAUNCHED();
   return MRG_OK;
 }
@@ -837,6 +837,13 @@ static mrg_status launch_q(const FftPass &p, cudaStream_t st) {
     // plain passes whose tiles never straddle an outer row and copy line pairs: persistent
     if (p.mode == FFT_PLAIN && !p.lfast && pp.nib && p.vec16 && p.nlines / p.IB <= 0x7fffffff &&
         (p.IB == 16 || p.IB == 32)) {
+      // xp == 2: 16 threads per line for the lines of 288, 320 and 384 points
+      if constexpr (Q == 36 || Q == 40 || Q == 48) {
+        if (p.xp == 2) {
+          if (p.IB == 16) return p.sign < 0 ? launch_pp<Q / 2, -1, 16, 16>(pp, st) : launch_pp<Q / 2, +1, 16, 16>(pp, st);
+          return p.sign < 0 ? launch_pp<Q / 2, -1, 32, 16>(pp, st) : launch_pp<Q / 2, +1, 32, 16>(pp, st);
+        }
+      }
       if (p.IB == 16) return p.sign < 0 ? launch_pp<Q, -1, 16>(pp, st) : launch_pp<Q, +1, 16>(pp, st);
       return p.sign < 0 ? launch_pp<Q, -1, 32>(pp, st) : launch_pp<Q, +1, 32>(pp, st);
     }

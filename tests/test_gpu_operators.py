@@ -394,13 +394,15 @@ def test_long_lines_operators_match_oracle(mrg_lib, oracle_lib, N, C):
 
 
 @pytest.mark.parametrize("N,C", [((128, 16, 24), 32), ((128, 24, 16), 16), ((256, 16, 8), 32), ((160, 8, 16), 16),
-                                 ((192, 8, 8), 16), ((208, 8, 8), 32), ((128, 16, 16), 8), ((240, 8, 8), 20)])
+                                 ((192, 8, 8), 16), ((208, 8, 8), 32), ((128, 16, 16), 8), ((240, 8, 8), 20),
+                                 ((16, 256, 16), 16), ((8, 16, 208), 32)])
 @pytest.mark.parametrize("ib", [0, 16])
 def test_persistent_x_passes_match_oracle(mrg_lib, oracle_lib, N, C, ib):
     """The set_image and accumulate x passes run by the persistent kernels (xp = 1; x lines
     of 192..384 points, 16 or 32 coils per CTA; xp = 2: 16 threads per line for 288, 320
-    and 384 points) and by the one-tile kernels (xp = 0) give the oracle's E and E^H; 8 and
-    20 coils check the fall-back to the one-tile kernels."""
+    and 384 points, also in the plain y and z passes: the last two shapes) and by the
+    one-tile kernels (xp = 0) give the oracle's E and E^H; 8 and 20 coils check the
+    fall-back to the one-tile kernels."""
     import torch
     rng = np.random.default_rng(5)
     M = 20000
