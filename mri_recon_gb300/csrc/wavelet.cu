@@ -71,44 +71,51 @@ __device__ __forceinline__ int64_t wave_base(const WaveArgs &a, int64_t id, int6
 template <int INV>
 __global__ void __launch_bounds__(256) k_wave(const WaveArgs a) {
   extern __shared__ float2 sm[];  // [L][33]
+  __shared__ int64_t lbase[32];   // first element of each of the CTA's lines
   float2 *X = a.X + (int64_t)blockIdx.y * a.vstride;
   const int L = a.L, h = L / 2, wN = a.f.wN;
-  const int S = a.shifts[(a.sc ? a.sc->it : 0) * a.per_it + a.off + a.axis];
+  // the shift taken modulo L once, so every index below wraps with one add or subtract
+  int S = a.shifts[(a.sc ? a.sc->it : 0) * a.per_it + a.off + a.axis] % L;
+  if (S < 0) S += L;
   const int64_t line0 = (int64_t)blockIdx.x * 32;
+  const int nl = (int)min((int64_t)32, a.nlines - line0);  // lines of this CTA
   const bool lfast = (a.axis == 0);
+  int64_t st = 1;
+  wave_base(a, 0, st);  // the axis stride
+  if (threadIdx.x < nl) {
+    int64_t s2;
+    lbase[threadIdx.x] = wave_base(a, line0 + threadIdx.x, s2);
+  }
+  __syncthreads();
   // load
   for (int e = threadIdx.x; e < 32 * L; e += blockDim.x) {
-    const int jj = lfast ? e / L : e % 32;
-    const int l = lfast ? e % L : e / 32;
-    const int64_t id = line0 + jj;
-    if (id < a.nlines) {
-      int64_t st;
-      const int64_t b = wave_base(a, id, st);
-      sm[l * 33 + jj] = X[b + l * st];
-    }
+    const int jj = lfast ? e / L : (e & 31);
+    const int l = lfast ? e - jj * L : (e >> 5);
+    if (jj < nl) sm[l * 33 + jj] = X[lbase[jj] + l * st];
   }
   __syncthreads();
   // compute + store in place
   for (int e = threadIdx.x; e < 32 * L; e += blockDim.x) {
-    const int jj = lfast ? e / L : e % 32;
-    const int o = lfast ? e % L : e / 32;
-    const int64_t id = line0 + jj;
-    if (id >= a.nlines) continue;
+    const int jj = lfast ? e / L : (e & 31);
+    const int o = lfast ? e - jj * L : (e >> 5);
+    if (jj >= nl) continue;
     float2 acc = make_float2(0.f, 0.f);
     if (!INV) {
       const int p = (o < h) ? o : o - h;
       const float *flt = (o < h) ? a.f.lpf : a.f.hpf;
       for (int f = 0; f < wN; f++) {
-        int c = (2 * p - f + S) % L;
-        if (c < 0) c += L;
+        int c = 2 * p - f + S;  // in [-3, 2L - 1): (2p - f + S) mod L, a few steps at most
+        while (c < 0) c += L;
+        while (c >= L) c -= L;
         const float2 v = sm[c * 33 + jj];
         acc.x += flt[f] * v.x;
         acc.y += flt[f] * v.y;
       }
     } else {
       for (int f = 0; f < wN; f++) {
-        int r = (o - f + wN - 1 - S) % L;
-        if (r < 0) r += L;
+        int r = o - f + wN - 1 - S;  // in (-L, L + 3): (o - f + wN - 1 - S) mod L, a few steps at most
+        while (r < 0) r += L;
+        while (r >= L) r -= L;
         if (r & 1) continue;
         const int p = r >> 1;
         const float2 lo = sm[p * 33 + jj], hi = sm[(p + h) * 33 + jj];
@@ -118,9 +125,7 @@ __global__ void __launch_bounds__(256) k_wave(const WaveArgs a) {
         acc.y += hi.y * a.f.shpf[f];
       }
     }
-    int64_t st;
-    const int64_t b = wave_base(a, id, st);
-    X[b + o * st] = acc;
+    X[lbase[jj] + o * st] = acc;
   }
 }
 
@@ -139,16 +144,19 @@ static mrg_status wave_pass(WaveArgs a, int nvol, int inverse, cudaStream_t st) 
   a.L = a.axis == 0 ? a.Lx : (a.axis == 1 ? a.Ly : a.Lz);
   a.nlines = a.axis == 0 ? (int64_t)a.Ly * a.Lz : (a.axis == 1 ? (int64_t)a.Lx * a.Lz : (int64_t)a.Lx * a.Ly);
   if (a.L < 2 || a.nlines == 0) return MRG_OK;
+  // dynamic shared memory: the staged lines; the kernel's own static 256 bytes (line bases)
+  // come out of the same 227 KB per block
+  constexpr int kDynMax = 227 * 1024 - 256;
   const size_t smem = (size_t)a.L * 33 * sizeof(float2);
-  if (smem > 227 * 1024) {
+  if (smem > (size_t)kDynMax) {
     set_error("wavelet line too long");
     return MRG_ERR_UNSUPPORTED;
   }
   const dim3 grid((unsigned)((a.nlines + 31) / 32), (unsigned)nvol);
   static DeviceOnce once;
   MRG_TRY(device_once(once, []() -> mrg_status {
-    MRG_CUDA(cudaFuncSetAttribute(k_wave<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
-    MRG_CUDA(cudaFuncSetAttribute(k_wave<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+    MRG_CUDA(cudaFuncSetAttribute(k_wave<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, kDynMax));
+    MRG_CUDA(cudaFuncSetAttribute(k_wave<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kDynMax));
     return MRG_OK;
   }));
   if (inverse) k_wave<1><<<grid, 256, smem, st>>>(a);
