@@ -1,8 +1,8 @@
 // Gridding (gridFFT::chop_grid_forward, src/gridFFT.cpp:1009-1164) on the fifth-generation
 // tensor cores: tcgen05.mma with the operand W and the accumulators in tensor memory.
 //
-// The grid is cut into regions of 8x4x4 = 128 points, one TMEM lane per point.  For a region, the scatter of its (sample, region) pairs is
-// the GEMM
+// The grid is cut into regions of 8x4x4 = 128 points, one TMEM lane per point.  For a
+// region, the scatter of its (sample, region) pairs is the GEMM
 //   grid[128 points][N] += W[128 points][K pairs] * V[K pairs][N],   N = 2 * coils,
 // W the tap weights (wz*wy)*wx of each point for each sample, V the weighted sample
 // values with real and imaginary parts as separate columns.  Both operands are split
@@ -10,18 +10,21 @@
 // tensor core drops lo's own low bits) and the product taken as Wl*Vh + Wh*Vl + Wh*Vh
 // in TF32, each product within about 2^-20 of the FP32 one.
 //
-// One persistent 512-thread CTA per SM (four warpgroups, each thread owning the TMEM lane
-// of one point) walks its work items chunk by chunk.  Per chunk of 96 pairs: the pairs'
-// records (first taps, tap weights, sample values) are copied with cp.async one chunk
-// ahead; the threads tabulate (wz*wy) and wx per pair, each warpgroup writes three k-steps
-// of W (hi and lo, its threads' own rows) into tensor memory with tcgen05.st, all threads
-// write V into shared memory (K-major canonical layout), and one thread issues up to 36
-// MMAs (12 k-steps x 3 terms, A read from tensor memory) into one of two accumulator
-// slots, committing them to the slot's mbarrier.  While they run the CTA prepares the
-// next chunk in the other slot.  The tensor core adds into its accumulator rounding
-// toward zero (measured: bit-identical to an RZ emulation), so each chunk is summed from
-// zero and added into the thread's FP32 registers with round-to-nearest when its slot is
-// reused; along a whole region the truncation would otherwise build up a bias.
+// One persistent CTA per SM (512 builder threads in four warpgroups, each thread owning the
+// TMEM lane of one point, and one MMA warp) walks its work items chunk by chunk.  The
+// trajectory set-up tabulates, per 96-pair chunk, (wz*wy) of the region's 16 (z, y) rows
+// and wx of its 8 x columns for every pair (k_region_tables).  Per chunk: the chunk's table
+// and its pairs' sample values are copied with cp.async one chunk ahead; each warpgroup
+// writes three k-steps of W (hi and lo, its threads' own rows) into tensor memory with
+// tcgen05.st, all threads write V into shared memory (K-major canonical layout), and the
+// MMA warp issues up to 36 MMAs (12 k-steps x 3 terms, A read from tensor memory) into one
+// of two accumulator slots, committing them to the slot's mbarrier.  While they run the CTA
+// prepares the next chunk in the other slot.  The tensor core adds into its accumulator
+// rounding toward zero (measured: bit-identical to an RZ emulation), so each chunk is
+// summed from zero and added into the thread's FP32 registers with round-to-nearest when
+// its slot is retired (two chunks later); along a whole region the truncation would
+// otherwise build up a bias.  A work item is written when its last chunk is retired,
+// through a shared-memory buffer so that each warp stores contiguous bytes.
 //
 // Every mbarrier wait is bounded (GridConst::wait_ns of the GPU's global timer, two
 // seconds by default); a kernel whose wait runs out sets the plan's error word, waits
