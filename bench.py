@@ -785,7 +785,7 @@ def run_ours(a):
            "data": "synthetic",
            "config": bench_config(c, world), "graph": "one CG iteration per CUDA graph replay",
            "gpu_launches": int(launches), "roofline": roofline, "iteration_roofline": iteration_roofline,
-           "autotune": out_tuning,
+           "autotune": out_tuning, "fft_tuning": plan.fft_tuning(),
            "cg_residual_first_last": [float(resid[0]), float(resid[-1])]}
     if clocks:
         out["clocks"] = clocks

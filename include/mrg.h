@@ -129,7 +129,8 @@ mrg_status mrg_frame_set_tuning(mrg_plan *plan, int frame, const int in[5]);
  * lines per CTA ib[k] (0: the default, a multiple of the coil count up to 32) and xp[k] (1:
  * the persistent set_image / accumulate kernel of the x passes of multi-coil plans, used
  * where the pass's strides allow it; 2: the same with 16 threads per line, for lines of
- * 288, 320 and 384 points, which also applies to the persistent plain y and z passes).  The first mrg_set_traj of a plan tunes them by
+ * 288, 320 and 384 points, which also applies to the persistent plain y and z passes;
+ * | 4: the plain persistent passes' tiles copied by tensor maps, TMA).  The first mrg_set_traj of a plan tunes them by
  * timing; mrg_set_fft_tuning fixes them afterwards (values a pass cannot take fall back
  * to its default).  Either array may be NULL. */
 mrg_status mrg_fft_tuning(const mrg_plan *plan, int ib[6], int xp[6]);

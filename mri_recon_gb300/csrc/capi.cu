@@ -476,7 +476,7 @@ static mrg_status run_E_grid(mrg_plan *p, const float2 *X, const float2 *smap, c
   b.nlines = Ny * Sx * C;
   b.in_ls = Ny * Sx * C; b.in_os = 0; b.out_ls = Ny * Sx * C; b.out_os = 0;
   b.scale = (float)(1. / std::sqrt((float)Sz));
-  b.in = p->d_t1; b.out = p->d_t2; b.C = C; b.xp = p->fft_xp[1];
+  b.in = p->d_t1; b.out = p->d_t2; b.C = C; b.xp = p->fft_xp[1]; b.err = p->d_err;
   fft_vectorize(b);
   MRG_TRY(launch_fft(b, st));
   tmark(p, 2, st);
@@ -490,7 +490,7 @@ static mrg_status run_E_grid(mrg_plan *p, const float2 *X, const float2 *smap, c
   c.nlines = Sz * Sx * C;
   c.in_ls = Sx * C; c.in_os = Ny * Sx * C; c.out_ls = Sx * C; c.out_os = Sy * Sx * C;
   c.scale = (float)(1. / std::sqrt((float)Sy));
-  c.in = p->d_t2; c.out = p->d_grid; c.C = C; c.xp = p->fft_xp[2];
+  c.in = p->d_t2; c.out = p->d_grid; c.C = C; c.xp = p->fft_xp[2]; c.err = p->d_err;
   fft_vectorize(c);
   MRG_TRY(launch_fft(c, st));
   return MRG_OK;
@@ -516,7 +516,7 @@ static mrg_status run_EH_yz(mrg_plan *p, const FrameTraj &ft, const float2 *y, c
   a.nlines = Sz * Sx * C;
   a.in_ls = Sx * C; a.in_os = Sy * Sx * C; a.out_ls = Sx * C; a.out_os = Ny * Sx * C;
   a.scale = (float)(1. / std::sqrt((float)Sy));
-  a.in = p->d_grid; a.out = p->d_t2; a.C = C; a.xp = p->fft_xp[3];
+  a.in = p->d_grid; a.out = p->d_t2; a.C = C; a.xp = p->fft_xp[3]; a.err = p->d_err;
   fft_vectorize(a);
   MRG_TRY(launch_fft(a, st));
   tmark(p, 2, st);
@@ -529,7 +529,7 @@ static mrg_status run_EH_yz(mrg_plan *p, const FrameTraj &ft, const float2 *y, c
   b.nlines = Ny * Sx * C;
   b.in_ls = Ny * Sx * C; b.in_os = 0; b.out_ls = Ny * Sx * C; b.out_os = 0;
   b.scale = (float)(1. / std::sqrt((float)Sz));
-  b.in = p->d_t2; b.out = p->d_t1; b.C = C; b.xp = p->fft_xp[4];
+  b.in = p->d_t2; b.out = p->d_t1; b.C = C; b.xp = p->fft_xp[4]; b.err = p->d_err;
   fft_vectorize(b);
   MRG_TRY(launch_fft(b, st));
   tmark(p, 3, st);
@@ -653,6 +653,25 @@ static mrg_status tune_fft(mrg_plan *p, const FrameTraj &ft, cudaStream_t st) {
   for (int k = 0; k < 6; k++) {
     p->fft_ib[k] = pick[k];
     p->fft_xp[k] = pick_xp[k];
+  }
+  // then, with those shapes, the plain persistent passes' tiles copied by tensor maps
+  for (int k = 0; k < 6; k++) p->fft_xp[k] = pick_xp[k] | 4;
+  MRG_TRY(mrg_set_timing(p, 1));
+  for (int rep = 0; rep < 2; rep++) {
+    MRG_TRY(run_E(p, ft, p->d_R, sm, nullptr, p->d_y, true, st));
+    MRG_TRY(run_EH(p, ft, p->d_y, sm, p->d_L, st));
+  }
+  {
+    float t[8];
+    int calls = 0;
+    MRG_TRY(mrg_last_timings(p, t, &calls));
+    for (int k = 0; k < 6; k++) p->fft_xp[k] = t[idx[k]] < best[k] ? (pick_xp[k] | 4) : pick_xp[k];
+  }
+  const mrg_status chk = plan_check(p, st);
+  if (chk == MRG_ERR_TIMEOUT) {  // a tensor-map copy's wait ran out: keep the 16-byte copies
+    for (int k = 0; k < 6; k++) p->fft_xp[k] = pick_xp[k];
+  } else {
+    MRG_TRY(chk);
   }
   p->fft_tuned = true;
   return mrg_set_timing(p, was_on);
@@ -955,8 +974,8 @@ mrg_status mrg_set_fft_tuning(mrg_plan *p, const int ib[6], const int xp[6]) {
       set_error("lines per CTA out of range (0..32)");
       return MRG_ERR_INVALID;
     }
-    if (xp && (xp[k] < 0 || xp[k] > 2)) {
-      set_error("xp must be 0, 1 or 2");
+    if (xp && (xp[k] < 0 || xp[k] > 6 || (xp[k] & 3) == 3)) {
+      set_error("xp must be 0, 1 or 2, optionally | 4");
       return MRG_ERR_INVALID;
     }
   }

@@ -19,6 +19,9 @@
 
 #include <algorithm>
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "mrg_internal.h"
 
 namespace mrg {
@@ -527,6 +530,115 @@ __global__ void __launch_bounds__(R * P) k_fft_pp(const FftPass p, int ntiles) {
   }
 }
 
+// The persistent plain pass with each tile's rows brought in by the tensor-memory
+// accelerator: nbox cp.async.bulk.tensor copies of brows rows each (a 3D tensor map over
+// (2 inner floats, Lin rows, outer rows), box (2 IB floats, brows, 1): the tile's IB
+// lines), their completion counted on one mbarrier instead of every thread issuing 16-byte
+// copies.  The mbarrier wait is bounded; a CTA whose wait runs out records it in the
+// plan's error word, waits once more for the copies in flight and returns.
+__device__ __forceinline__ bool fft_mbar_wait(uint32_t bar, uint32_t parity, long long limit_ns) {
+  long long t0;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+  for (;;) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred q;\n mbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2;\n selp.u32 %0, 1, 0, q;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+    long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    if (t - t0 >= limit_ns) return false;
+    __nanosleep(64);
+  }
+}
+
+template <int Q, int SIGN, int P, int R>
+__global__ void __launch_bounds__(R * P) k_fft_pt(const __grid_constant__ CUtensorMap tmap, const FftPass p, int ntiles,
+                                                  int nbox, int brows) {
+  constexpr int S = R * Q, IB = P;
+  extern __shared__ __align__(128) float2 sm[];  // [S][IB] data, S twiddles, the mbarrier
+  float2 *tw = sm + S * (IB + 1);
+  const uint32_t bar = (uint32_t)__cvta_generic_to_shared(tw + S);
+  const int tid = threadIdx.x;
+  for (int m = tid; m < S; m += blockDim.x) tw[m] = p.tw[m];
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  const int j = tid % IB, t = tid / IB;
+  float2 *col = sm + j;
+  const unsigned nib = (unsigned)p.nib;
+  const uint32_t bytes = (uint32_t)(nbox * brows * IB * (int)sizeof(float2));
+  auto issue = [&](int tile) {
+    if (tid == 0) {
+      const unsigned ob = (unsigned)tile / nib;
+      const int x = 2 * (int)((unsigned)tile - ob * nib) * IB;  // floats: a multiple of 32
+      // the buffer's earlier generic reads (ordered by the barrier before this call) come
+      // before the asynchronous writes
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+      for (int b = 0; b < nbox; b++) {
+        const uint32_t dst = (uint32_t)__cvta_generic_to_shared(sm + (p.in_off + b * brows) * IB);
+        asm volatile(
+            "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
+            "%4}], [%5];" ::"r"(dst),
+            "l"(reinterpret_cast<uint64_t>(&tmap)), "r"(x), "r"(b * brows), "r"((int)ob), "r"(bar)
+            : "memory");
+      }
+    }
+    for (int e = tid; e < (S - p.Lin) * IB; e += blockDim.x) {  // rows outside the copied ones
+      const int jj = e % IB, k = e / IB;
+      const int r = (k < p.in_off) ? k : k + p.Lin;
+      sm[r * IB + jj] = make_float2(0.f, 0.f);
+    }
+  };
+  uint32_t phase = 0;
+  int tile = blockIdx.x;
+  if (tile < ntiles) issue(tile);
+  for (; tile < ntiles; tile += gridDim.x) {
+    const bool ok = fft_mbar_wait(bar, phase, MRG_DEFAULT_WAIT_NS);
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0 && p.err) atomicExch(p.err, MRG_WAIT_EXPIRED);
+      fft_mbar_wait(bar, phase, MRG_DEFAULT_WAIT_NS);  // the copies in flight land before the CTA leaves
+      return;
+    }
+    phase ^= 1u;
+    // ---- step A: R-point DFTs over n1 (rows Q*n1 + n2), twiddle W_S^(n2*k1) ----
+    for (int n2 = t; n2 < Q; n2 += R) {
+      float2 a[R];
+      float2 *c2 = col + n2 * IB;
+#pragma unroll
+      for (int n1 = 0; n1 < R; n1++) a[n1] = c2[Q * n1 * IB];
+      reg_fft<R, SIGN, S>(a, tw);
+#pragma unroll
+      for (int k1 = 1; k1 < R; k1++) a[k1] = cmul(a[k1], twid<SIGN>(tw, n2 * k1));
+#pragma unroll
+      for (int k1 = 0; k1 < R; k1++) c2[Q * k1 * IB] = a[k1];
+    }
+    __syncthreads();
+    // ---- step C: rows Q*t .. Q*t+Q-1 into registers; then the buffer is free ----
+    float2 v[Q];
+    const float2 *cq = col + Q * t * IB;
+#pragma unroll
+    for (int n2 = 0; n2 < Q; n2++) v[n2] = cq[n2 * IB];
+    __syncthreads();
+    if (tile + (int)gridDim.x < ntiles) issue(tile + gridDim.x);
+    reg_fft<Q, SIGN, S>(v, tw);
+    const unsigned ob = (unsigned)tile / nib;
+    const int64_t i = (int64_t)((unsigned)tile - ob * nib) * IB + j;
+    float2 *go = p.out + (int64_t)ob * p.out_os + i;
+    const float sc = p.scale;
+#pragma unroll
+    for (int k2 = 0; k2 < Q; k2++) {
+      const int r = t + R * k2 - p.out_off;
+      if (r >= 0 && r < p.Lout) go[(int64_t)r * p.out_ls] = make_float2(v[k2].x * sc, v[k2].y * sc);
+    }
+  }
+}
+
 // Set-image x passes, persistent: the first pass of a multi-coil E, lines along x with the
 // coils innermost (inner == C == in_ls), so the IB lines of a tile are IB coils of one
 // image row o.  Tiles are walked as in k_fft_pp; beside a tile's maps the copies bring the
@@ -767,6 +879,55 @@ static mrg_status launch_pa(const FftPass &pp, cudaStream_t st) {
   return launch_persistent(k_fft_pa<Q, P, R>, R * P, smem, cap, once, ctas, (int)(pp.nlines / P), pp, st);
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link to the driver
+// library); NULL where the driver does not provide it.
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder();
+
+// The tile copies of a plain persistent pass as tensor-map copies: tiles of IB lines, Lin
+// rows in nbox boxes of brows rows (nbox * brows == Lin, brows <= 256).  false where the
+// pass's layout does not fit (the caller keeps the 16-byte copies).
+inline bool fft_tensor_map(const FftPass &p, int IB, CUtensorMap *map, int *nbox, int *brows) {
+  const PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc || p.Lin < 1 || p.inner % IB || (p.nlines % p.inner) || ((uintptr_t)p.in & 15) || (p.in_ls & 1) ||
+      (p.in_os & 1))
+    return false;
+  const int nb = (p.Lin + 255) / 256;
+  if (p.Lin % nb) return false;
+  const int64_t nouter = p.nlines / p.inner;
+  const cuuint64_t dims[3] = {(cuuint64_t)(2 * p.inner), (cuuint64_t)p.Lin, (cuuint64_t)nouter};
+  const cuuint64_t strides[2] = {(cuuint64_t)(8 * p.in_ls),
+                                 (cuuint64_t)(8 * (nouter > 1 ? p.in_os : p.in_ls * (int64_t)p.Lin))};
+  const cuuint32_t box[3] = {(cuuint32_t)(2 * IB), (cuuint32_t)(p.Lin / nb), 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  if (strides[0] % 16 || strides[1] % 16 || strides[0] == 0 || strides[1] == 0) return false;
+  if (enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float2 *>(p.in), dims, strides, box, estr,
+          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return false;
+  *nbox = nb;
+  *brows = p.Lin / nb;
+  return true;
+}
+
+template <int Q, int SIGN, int P, int R>
+static mrg_status launch_pt(const FftPass &pp, const CUtensorMap &map, int nbox, int brows, cudaStream_t st) {
+  const size_t smem = (size_t)R * Q * (P + 2) * sizeof(float2) + 16;  // + the mbarrier
+  static DeviceOnce once;
+  static int ctas = 1;
+  MRG_TRY(device_once(once, [smem]() -> mrg_status {
+    MRG_CUDA(cudaFuncSetAttribute(k_fft_pt<Q, SIGN, P, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int c = 0;
+    MRG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_fft_pt<Q, SIGN, P, R>, R * P, smem));
+    ctas = c < 1 ? 1 : c;
+    return MRG_OK;
+  }));
+  const int ntiles = (int)(pp.nlines / P);
+  const int nblk = std::max(1, std::min(ntiles, device_sms() * ctas));
+  k_fft_pt<Q, SIGN, P, R><<<nblk, R * P, smem, st>>>(map, pp, ntiles, nbox, brows);
+  MRG_LAUNCHED();
+  return MRG_OK;
+}
+
 template <int Q, int SIGN, int P, int R = 8>
 static mrg_status launch_pp(const FftPass &pp, cudaStream_t st) {
   const size_t smem = (size_t)R * Q * (P + 2) * sizeof(float2);
@@ -785,6 +946,20 @@ static mrg_status launch_pp(const FftPass &pp, cudaStream_t st) {
   k_fft_pp<Q, SIGN, P, R><<<nblk, R * P, smem, st>>>(pp, ntiles);
   MRG_LAUNCHED();
   return MRG_OK;
+}
+
+// A plain persistent pass with IB = P lines per tile and R threads per line: tensor-map
+// copies when the pass asks for them (xp bit 4) and its layout allows, else 16-byte copies.
+template <int Q, int P, int R>
+static mrg_status launch_plain(const FftPass &pp, cudaStream_t st) {
+  if (pp.xp & 4) {
+    CUtensorMap map;
+    int nbox = 0, brows = 0;
+    if (fft_tensor_map(pp, P, &map, &nbox, &brows))
+      return pp.sign < 0 ? launch_pt<Q, -1, P, R>(pp, map, nbox, brows, st)
+                         : launch_pt<Q, +1, P, R>(pp, map, nbox, brows, st);
+  }
+  return pp.sign < 0 ? launch_pp<Q, -1, P, R>(pp, st) : launch_pp<Q, +1, P, R>(pp, st);
 }
 
 // Q values that get kernels with a compile-time pitch (lines of 192..384 points whose
@@ -837,31 +1012,27 @@ static mrg_status launch_q(const FftPass &p, cudaStream_t st) {
     // plain passes whose tiles never straddle an outer row and copy line pairs: persistent
     if (p.mode == FFT_PLAIN && !p.lfast && pp.nib && p.vec16 && p.nlines / p.IB <= 0x7fffffff &&
         (p.IB == 16 || p.IB == 32)) {
-      // xp == 2: 16 threads per line for the lines of 288, 320 and 384 points
+      // xp & 3 == 2: 16 threads per line for the lines of 288, 320 and 384 points
       if constexpr (Q == 36 || Q == 40 || Q == 48) {
-        if (p.xp == 2) {
-          if (p.IB == 16) return p.sign < 0 ? launch_pp<Q / 2, -1, 16, 16>(pp, st) : launch_pp<Q / 2, +1, 16, 16>(pp, st);
-          return p.sign < 0 ? launch_pp<Q / 2, -1, 32, 16>(pp, st) : launch_pp<Q / 2, +1, 32, 16>(pp, st);
-        }
+        if ((p.xp & 3) == 2) return p.IB == 16 ? launch_plain<Q / 2, 16, 16>(pp, st) : launch_plain<Q / 2, 32, 16>(pp, st);
       }
-      if (p.IB == 16) return p.sign < 0 ? launch_pp<Q, -1, 16>(pp, st) : launch_pp<Q, +1, 16>(pp, st);
-      return p.sign < 0 ? launch_pp<Q, -1, 32>(pp, st) : launch_pp<Q, +1, 32>(pp, st);
+      return p.IB == 16 ? launch_plain<Q, 16, 8>(pp, st) : launch_plain<Q, 32, 8>(pp, st);
     }
     // set_image / accumulate x passes of multi-coil plans (lines along x, coils innermost),
     // persistent when the plan's tuning chose it
-    if (p.xp && p.wmode == 1 && p.has_smap && pp.nib && p.vec16 && !p.lfast && p.inner == p.C && p.in_ls == p.C &&
+    if ((p.xp & 3) && p.wmode == 1 && p.has_smap && pp.nib && p.vec16 && !p.lfast && p.inner == p.C && p.in_ls == p.C &&
         (p.IB == 16 || p.IB == 32) && p.nlines / p.IB <= 0x7fffffff) {
       // xp == 2: 16 threads per line, for the lines of 288, 320 and 384 points
       constexpr bool r16 = (Q == 36 || Q == 40 || Q == 48);
       if (p.mode == FFT_SETIMG && p.in_os % p.C == 0 && p.Lin <= R * Q) {
         if constexpr (r16)
-          if (p.xp == 2) return p.IB == 16 ? launch_ps<Q / 2, 16, 16>(pp, st) : launch_ps<Q / 2, 32, 16>(pp, st);
+          if ((p.xp & 3) == 2) return p.IB == 16 ? launch_ps<Q / 2, 16, 16>(pp, st) : launch_ps<Q / 2, 32, 16>(pp, st);
         return p.IB == 16 ? launch_ps<Q, 16>(pp, st) : launch_ps<Q, 32>(pp, st);
       }
       if (p.mode == FFT_ACCUM && p.IB == p.C && !p.acc_atomic && p.Lout <= R * Q && p.out_os % 2 == 0 &&
           p.out_ls % 2 == 0 && ((uintptr_t)p.smap & 15) == 0) {
         if constexpr (r16)
-          if (p.xp == 2) return p.IB == 16 ? launch_pa<Q / 2, 16, 16>(pp, st) : launch_pa<Q / 2, 32, 16>(pp, st);
+          if ((p.xp & 3) == 2) return p.IB == 16 ? launch_pa<Q / 2, 16, 16>(pp, st) : launch_pa<Q / 2, 32, 16>(pp, st);
         return p.IB == 16 ? launch_pa<Q, 16>(pp, st) : launch_pa<Q, 32>(pp, st);
       }
     }

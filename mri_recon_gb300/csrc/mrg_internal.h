@@ -132,7 +132,9 @@ struct FftPass {
   int C, has_smap;
   int acc_atomic;
   int64_t acc_l, acc_o;  // accumulator strides for l and o (i/C has stride 1)
-  int xp;                // 1: persistent set_image / accumulate x passes; 2: those and the plain passes with 16 threads per line
+  int xp;                // 1: persistent set_image / accumulate x passes; 2: those and the plain passes with 16 threads
+                         // per line; | 4: the plain persistent passes' tiles copied by tensor maps
+  int *err;              // device error word (bounded waits of the tensor-map copies; may be NULL)
 };
 bool fft_size_supported(int S);
 // Lines per CTA a pass of length S can take (16 threads per line above 384 points).

@@ -400,9 +400,10 @@ def test_long_lines_operators_match_oracle(mrg_lib, oracle_lib, N, C):
 def test_persistent_x_passes_match_oracle(mrg_lib, oracle_lib, N, C, ib):
     """The set_image and accumulate x passes run by the persistent kernels (xp = 1; x lines
     of 192..384 points, 16 or 32 coils per CTA; xp = 2: 16 threads per line for 288, 320
-    and 384 points, also in the plain y and z passes: the last two shapes) and by the
-    one-tile kernels (xp = 0) give the oracle's E and E^H; 8 and 20 coils check the
-    fall-back to the one-tile kernels."""
+    and 384 points, also in the plain y and z passes: the last two shapes; xp | 4: the
+    plain persistent passes' tiles copied by tensor maps) and by the one-tile kernels (xp =
+    0) give the oracle's E and E^H; 8 and 20 coils check the fall-back to the one-tile
+    kernels."""
     import torch
     rng = np.random.default_rng(5)
     M = 20000
@@ -422,7 +423,7 @@ def test_persistent_x_passes_match_oracle(mrg_lib, oracle_lib, N, C, ib):
         ref_h = o.adjoint(ref_h, smaps[k], d[k], kx, ky, kz, kw)
     X0 = (rng.standard_normal(ishape) + 1j * rng.standard_normal(ishape)).astype(np.complex64)
     out = {}
-    for xp in (0, 1, 2):
+    for xp in (0, 1, 2, 4, 5, 6):
         p.set_fft_tuning(ib=[ib] * 6, xp=[xp] * 6)
         assert p.fft_tuning() == dict(ib=[ib] * 6, xp=[xp] * 6)
         y = p.forward(0, torch.from_numpy(X).cuda()).cpu().numpy()
@@ -430,7 +431,7 @@ def test_persistent_x_passes_match_oracle(mrg_lib, oracle_lib, N, C, ib):
         assert rel(y, ref_e) < 1e-5
         assert rel(Xh - X0, ref_h) < 1e-5
         out[xp] = (y, Xh)
-    for xp in (1, 2):
+    for xp in (1, 2, 4, 5, 6):
         assert rel(out[xp][0], out[0][0]) < 1e-6
         assert rel(out[xp][1], out[0][1]) < 1e-6
 
@@ -441,6 +442,8 @@ def test_set_fft_tuning_rejects_bad_values(mrg_lib):
         p.set_fft_tuning(ib=[33] * 6)
     with pytest.raises(mrg_lib.MrgError):
         p.set_fft_tuning(xp=[3] * 6)
+    with pytest.raises(mrg_lib.MrgError):
+        p.set_fft_tuning(xp=[7] * 6)
 
 
 @pytest.mark.parametrize("N,C", [((20, 16, 384), 9), ((16, 24, 400), 16)])
