@@ -839,6 +839,127 @@ __global__ void __launch_bounds__(R * P) k_fft_pa(const FftPass p, int ntiles) {
   asm volatile("cp.async.wait_all;\n" ::: "memory");
 }
 
+// The accumulate x pass with its copies made by the bulk-copy engine: a tile's input rows
+// (S x IB values, contiguous because IB == C == in_ls), the row's maps (Lout x IB) and its
+// X row (Lout) are contiguous in memory, so each is one cp.async.bulk copy counted on an
+// mbarrier (the input on one, the maps and X row on the other) instead of thousands of
+// 16-byte copies.  Otherwise as k_fft_pa.  Waits are bounded; a CTA whose wait runs out
+// records it in the plan's error word, waits for what it has in flight and returns.
+template <int Q, int P, int R>
+__global__ void __launch_bounds__(R * P) k_fft_pb(const FftPass p, int ntiles) {
+  constexpr int S = R * Q, IB = P;
+  extern __shared__ __align__(128) float2 sm[];  // [S][IB] data, S twiddles, maps, X row, 2 mbarriers
+  float2 *tw = sm + S * (IB + 1);
+  float2 *mp = tw + S;
+  float2 *xa = mp + p.Lout * IB;
+  const uint32_t bin = (uint32_t)__cvta_generic_to_shared(xa + p.Lout), bmp = bin + 8;
+  const int tid = threadIdx.x;
+  for (int m = tid; m < S; m += blockDim.x) tw[m] = p.tw[m];
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bin));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bmp));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  const int j = tid % IB, t = tid / IB;
+  float2 *col = sm + j;
+  const uint32_t in_bytes = (uint32_t)(S * IB * (int)sizeof(float2));
+  const uint32_t mp_bytes = (uint32_t)(p.Lout * IB * (int)sizeof(float2)), xa_bytes = (uint32_t)(p.Lout * 8);
+  auto bulk = [](uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+  };
+  auto issue_in = [&](int tile) {
+    if (tid == 0) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bin), "r"(in_bytes) : "memory");
+      bulk((uint32_t)__cvta_generic_to_shared(sm), p.in + (int64_t)tile * p.in_os, in_bytes, bin);
+    }
+  };
+  auto issue_maps = [&](int tile) {
+    if (tid == 0) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bmp), "r"(mp_bytes + xa_bytes)
+                   : "memory");
+      bulk((uint32_t)__cvta_generic_to_shared(mp), p.smap + (int64_t)tile * p.out_os, mp_bytes, bmp);
+      bulk((uint32_t)__cvta_generic_to_shared(xa), p.acc + (int64_t)tile * p.acc_o, xa_bytes, bmp);
+    }
+  };
+  uint32_t ph_in = 0, ph_mp = 0;
+  // a wait that ran out: report it, let whatever is in flight land, leave
+  auto bail = [&]() {
+    if (tid == 0 && p.err) atomicExch(p.err, MRG_WAIT_EXPIRED);
+    fft_mbar_wait(bin, ph_in, MRG_DEFAULT_WAIT_NS);
+    fft_mbar_wait(bmp, ph_mp, MRG_DEFAULT_WAIT_NS);
+  };
+  int tile = blockIdx.x;
+  if (tile < ntiles) {
+    issue_in(tile);
+    issue_maps(tile);
+  }
+  for (; tile < ntiles; tile += gridDim.x) {
+    if (__syncthreads_or(!fft_mbar_wait(bin, ph_in, MRG_DEFAULT_WAIT_NS))) {  // this tile's input
+      bail();
+      return;
+    }
+    ph_in ^= 1u;
+    for (int n2 = t; n2 < Q; n2 += R) {
+      float2 a[R];
+      float2 *c2 = col + n2 * IB;
+#pragma unroll
+      for (int n1 = 0; n1 < R; n1++) a[n1] = c2[Q * n1 * IB];
+      reg_fft<R, +1, S>(a, tw);
+#pragma unroll
+      for (int k1 = 1; k1 < R; k1++) a[k1] = cmul(a[k1], twid<+1>(tw, n2 * k1));
+#pragma unroll
+      for (int k1 = 0; k1 < R; k1++) c2[Q * k1 * IB] = a[k1];
+    }
+    __syncthreads();
+    float2 v[Q];
+    const float2 *cq = col + Q * t * IB;
+#pragma unroll
+    for (int n2 = 0; n2 < Q; n2++) v[n2] = cq[n2 * IB];
+    __syncthreads();
+    const int nxt = tile + (int)gridDim.x;
+    if (nxt < ntiles) issue_in(nxt);
+    reg_fft<Q, +1, S>(v, tw);
+    if (__syncthreads_or(!fft_mbar_wait(bmp, ph_mp, MRG_DEFAULT_WAIT_NS))) {  // this tile's maps and X row
+      bail();
+      return;
+    }
+    ph_mp ^= 1u;
+    // X += sum_c (winz * winy * winx) v conj(smap)   (gridFFT::accumulate)
+    const float lw = p.wo[(int64_t)tile / p.wdiv] * p.wi[(int64_t)tile % p.wdiv];
+    const float sc = p.scale;
+#pragma unroll
+    for (int k2 = 0; k2 < Q; k2++) {
+      const int r = t + R * k2 - p.out_off;
+      if (r >= 0 && r < p.Lout) {
+        float2 val = make_float2(v[k2].x * sc, v[k2].y * sc);
+        const float w = lw * __ldg(p.wl + r);
+        val = make_float2(w * val.x, w * val.y);
+        float2 s2 = mp[r * IB + j];
+        s2.y = -s2.y;
+        mp[r * IB + j] = cmul(val, s2);
+      }
+    }
+    __syncthreads();
+    for (int r = tid; r < p.Lout; r += blockDim.x) {
+      float2 s = make_float2(0.f, 0.f);
+      const float2 *row = mp + r * IB;
+      int cc = r % IB;
+      for (int c = 0; c < IB; c++) {
+        s = cadd(s, row[cc]);
+        cc = (cc + 1 == IB) ? 0 : cc + 1;
+      }
+      p.acc[(int64_t)tile * p.acc_o + (int64_t)r * p.acc_l] = cadd(xa[r], s);
+    }
+    __syncthreads();
+    if (nxt < ntiles) issue_maps(nxt);
+  }
+}
+
 // Persistent launch over ntiles tiles.  The shared-memory cap and the resident CTAs per SM
 // (occupancy at the cap, a lower bound for smaller launches of the same kernel) are set up
 // once per device; the CTA count is the same on every device of a process.
@@ -877,6 +998,16 @@ static mrg_status launch_pa(const FftPass &pp, cudaStream_t st) {
   static DeviceOnce once;
   static int ctas = 1;
   return launch_persistent(k_fft_pa<Q, P, R>, R * P, smem, cap, once, ctas, (int)(pp.nlines / P), pp, st);
+}
+
+template <int Q, int P, int R = 8>
+static mrg_status launch_pb(const FftPass &pp, cudaStream_t st) {
+  constexpr int S = R * Q;
+  const size_t smem = ((size_t)S * (P + 2) + (size_t)pp.Lout * (P + 1)) * sizeof(float2) + 16;
+  const size_t cap = ((size_t)S * (P + 2) + (size_t)S * (P + 1)) * sizeof(float2) + 16;
+  static DeviceOnce once;
+  static int ctas = 1;
+  return launch_persistent(k_fft_pb<Q, P, R>, R * P, smem, cap, once, ctas, (int)(pp.nlines / P), pp, st);
 }
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no link to the driver
@@ -1031,6 +1162,15 @@ static mrg_status launch_q(const FftPass &p, cudaStream_t st) {
       }
       if (p.mode == FFT_ACCUM && p.IB == p.C && !p.acc_atomic && p.Lout <= R * Q && p.out_os % 2 == 0 &&
           p.out_ls % 2 == 0 && ((uintptr_t)p.smap & 15) == 0) {
+        // xp | 4: the bulk-copy variant, where the tile, the maps and the X row are each contiguous
+        const bool bulk = (p.xp & 4) && p.in_off == 0 && p.Lin == R * Q && p.in_ls == p.C && p.out_ls == p.C &&
+                          p.acc_l == 1 && p.Lout % 2 == 0 && p.acc_o % 2 == 0 && p.in_os % 2 == 0 &&
+                          ((uintptr_t)p.in & 15) == 0 && ((uintptr_t)p.acc & 15) == 0;
+        if (bulk) {
+          if constexpr (r16)
+            if ((p.xp & 3) == 2) return p.IB == 16 ? launch_pb<Q / 2, 16, 16>(pp, st) : launch_pb<Q / 2, 32, 16>(pp, st);
+          return p.IB == 16 ? launch_pb<Q, 16>(pp, st) : launch_pb<Q, 32>(pp, st);
+        }
         if constexpr (r16)
           if ((p.xp & 3) == 2) return p.IB == 16 ? launch_pa<Q / 2, 16, 16>(pp, st) : launch_pa<Q / 2, 32, 16>(pp, st);
         return p.IB == 16 ? launch_pa<Q, 16>(pp, st) : launch_pa<Q, 32>(pp, st);
