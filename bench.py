@@ -60,10 +60,12 @@ def parse():
                          "and fixed threshold) against the FP32 oracle; prints one JSON object")
     ap.add_argument("--parity-legs", default="cg4,cg32,fista_fraction,fista_fixed",
                     help="comma-separated subset of the --parity-full legs")
-    ap.add_argument("--kernel-case", default=None, choices=["wavelet_llr"],
+    ap.add_argument("--kernel-case", default=None, choices=["wavelet_llr", "fft_tma"],
                     help="only a small case for one-kernel ncu captures: wavelet_llr runs three rounds of "
                          "mrg_wavelet (DB4, 3 levels) forward + inverse and the time low-rank threshold update "
-                         "and pass (8^3 blocks) on a 10 x 128^3 stack through the C ABI")
+                         "and pass (8^3 blocks) on a 10 x 128^3 stack through the C ABI; fft_tma runs three E "
+                         "and E^H at 256 x 256 x 16 x 16 coils (384-point x and y lines) with the FFT passes "
+                         "fixed to the persistent 16-thread kernels with tensor-map and bulk copies")
     ap.add_argument("--side-only", default=None, choices=["cg64", "fista128", "llr128", "grad96"],
                     help="run only this smaller configuration's throughput row (with --profile-range: its "
                          "timed iterations bracketed by cudaProfilerStart/Stop)")
@@ -662,13 +664,42 @@ def kernel_case_wavelet_llr():
     print(json.dumps({"kernel_case": "wavelet_llr", "smax": smax.value}), flush=True)
 
 
+def kernel_case_fft_tma():
+    """E and E^H on a 384 x 384 x 32 grid of 16 coils (0.6 GB): the x passes (set_image,
+    accumulate) and y passes run the persistent kernels with 16 threads per line and their
+    tiles copied by tensor maps / bulk copies (FFT tuning fixed to xp = 2 | 4, 16 lines per CTA)."""
+    import torch
+
+    import mri_recon_gb300 as m
+    from mri_recon_gb300 import synth
+    N, C = (256, 256, 16), 16
+    rng = np.random.default_rng(5)
+    M = 400000
+    kx, ky, kz = [rng.uniform(-n / 2, n / 2, M).astype(np.float32) for n in N]
+    kw = (kx.astype(np.float64) ** 2 + ky ** 2 + kz ** 2).astype(np.float32)
+    p = m.Plan(N, C, 1)
+    p.set_fft_tuning(ib=[16] * 6, xp=[6] * 6)  # before the first trajectory: no FFT tuning
+    p.set_traj(0, kx, ky, kz, kw)
+    ishape = (N[2], N[1], N[0])
+    g = torch.Generator(device="cuda").manual_seed(2)
+    maps = torch.randn((C,) + ishape, dtype=torch.complex64, device="cuda", generator=g)
+    p.set_smaps(maps)
+    X = torch.randn(ishape, dtype=torch.complex64, device="cuda", generator=g)
+    for _ in range(3):
+        y = p.forward(0, X)
+        Xh = p.adjoint(0, y, torch.zeros(ishape, dtype=torch.complex64, device="cuda"))
+    torch.cuda.synchronize()
+    print(json.dumps({"kernel_case": "fft_tma", "fft_tuning": p.fft_tuning(), "norm": float(Xh.abs().sum())}),
+          flush=True)
+
+
 def run_ours(a):
     import torch
     import torch.distributed as dist
 
     if a.kernel_case:
         torch.cuda.set_device(0)
-        kernel_case_wavelet_llr()
+        {"wavelet_llr": kernel_case_wavelet_llr, "fft_tma": kernel_case_fft_tma}[a.kernel_case]()
         return
 
     if a.parity_full:
