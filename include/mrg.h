@@ -365,8 +365,9 @@ mrg_status mrg_llr_update_threshold(const void *X, int nframes, int Nx, int Ny, 
  * between kernels), its scratch lives in a fixed device array of the library, sized for
  * at most MRG_NOALLOC_MAX_BLOCKS low-rank blocks (512 KiB held by every GPU that loads the
  * library until exit); more blocks return MRG_ERR_UNSUPPORTED.  X must be device memory;
- * smax may be host or device memory (a host smax makes the call wait for the result).
- * The first call on a device looks up the array's device address; make that first call
+ * smax may be host or device memory (a host smax makes the call wait for the result, so
+ * inside a stream capture smax must be device memory; a host smax there returns
+ * MRG_ERR_INVALID).  The first call on a device looks up the array's device address; make that first call
  * before any stream capture.  All calls share the one array, so calls that overlap on the
  * GPU (other streams or threads) race; serialise them. */
 #define MRG_NOALLOC_MAX_BLOCKS 32768
