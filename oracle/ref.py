@@ -1,8 +1,8 @@
 """REFERENCE CHECKER -- TEST INFRASTRUCTURE ONLY.
 
 ctypes front end for ``oracle/_ref/libref.so``: the reference's own gridFFT.cpp,
-ArrayTemplates.cpp, wavelet3D.cpp and threshold.cpp compiled unmodified (``make -C oracle
-ref``) against the stand-in Blitz++ / FFTW / Armadillo / HDF5 headers of
+ArrayTemplates.cpp, wavelet3D.cpp, threshold.cpp and clear.cpp compiled unmodified (``make
+-C oracle ref``) against the stand-in Blitz++ / FFTW / Armadillo / HDF5 headers of
 ``oracle/refshim`` and driven by ``oracle/ref_driver.cpp``.  The tests use it to pin the
 oracle restatement (and, through committed fixtures, the CUDA path) to the reference's
 code.  It can only be built where the reference sources are present; ``available()``
@@ -53,6 +53,14 @@ def lib():
         L.ref_wavelet.argtypes = [i, i, i, ip, ip, i, i, vp]
         L.ref_fraction_threshold.restype = ctypes.c_float
         L.ref_fraction_threshold.argtypes = [i, i, i, i, ctypes.POINTER(vp), f, i]
+        pv = ctypes.POINTER(vp)
+        L.ref_llr_update_threshold.restype = ctypes.c_float
+        L.ref_llr_update_threshold.argtypes = [pv, i, i, i, i, ip, f, f, i]
+        L.ref_llr_thresh.argtypes = [pv, i, i, i, i, ip, i, f, f, l]
+        L.ref_clear_update_threshold.restype = ctypes.c_float
+        L.ref_clear_update_threshold.argtypes = [pv, i, i, i, i, i, ip, f, f, i]
+        L.ref_clear_thresh.argtypes = [pv, i, i, i, i, i, ip, i, f, f, l]
+        L.ref_clear_combine.argtypes = [pv, i, i, i, i, i, ip, pv]
         _lib = L
     return _lib
 
@@ -159,3 +167,59 @@ def fraction_threshold(vols, fraction, apply=False):
     arr = (ctypes.c_void_p * len(vols))(*[v.ctypes.data for v in vols])
     t = lib().ref_fraction_threshold(Nx, Ny, Nz, len(vols), arr, float(fraction), int(bool(apply)))
     return float(t), (vols if apply else None)
+
+
+def _vols(arrs):
+    return (ctypes.c_void_p * len(arrs))(*[a.ctypes.data for a in arrs])
+
+
+def llr_update_threshold(vols, bs, amp=4.0, t2=6.0, iteration=0):
+    """LOWRANKCOIL::update_threshold(image, 0, iteration) over frames (Nz, Ny, Nx): smax."""
+    vols = [_c64(v) for v in vols]
+    Nz, Ny, Nx = vols[0].shape
+    return float(lib().ref_llr_update_threshold(_vols(vols), len(vols), Nx, Ny, Nz, (ctypes.c_int * 3)(*bs),
+                                                float(amp), float(t2), int(iteration)))
+
+
+def llr_thresh(vols, bs, block_iter, alpha, smax, rand_skip):
+    """LOWRANKCOIL::thresh(image, 0) on copies of the frames, clear_alpha_time = alpha, rand()
+    seeded with srand(1) and advanced rand_skip draws."""
+    vols = [_c64(v).copy() for v in vols]
+    Nz, Ny, Nx = vols[0].shape
+    assert lib().ref_llr_thresh(_vols(vols), len(vols), Nx, Ny, Nz, (ctypes.c_int * 3)(*bs), int(block_iter),
+                                float(alpha), float(smax), int(rand_skip)) == 0
+    return vols
+
+
+def _coil_vols(XX):
+    T, C = XX.shape[:2]
+    return [XX[t, c] for t in range(T) for c in range(C)]
+
+
+def clear_update_threshold(XX, bs, amp=4.0, t2=6.0, iteration=0):
+    """LOWRANKCOIL::update_threshold(image, 2, iteration) on coil images (T, C, Nz, Ny, Nx)."""
+    XX = _c64(XX)
+    T, C, Nz, Ny, Nx = XX.shape
+    return float(lib().ref_clear_update_threshold(_vols(_coil_vols(XX)), T, C, Nx, Ny, Nz, (ctypes.c_int * 3)(*bs),
+                                                  float(amp), float(t2), int(iteration)))
+
+
+def clear_thresh(XX, bs, block_iter, alpha, smax, rand_skip):
+    """LOWRANKCOIL::thresh(image, 2) on a copy of coil images (T, C, Nz, Ny, Nx)."""
+    XX = _c64(XX).copy()
+    T, C, Nz, Ny, Nx = XX.shape
+    assert lib().ref_clear_thresh(_vols(_coil_vols(XX)), T, C, Nx, Ny, Nz, (ctypes.c_int * 3)(*bs), int(block_iter),
+                                  float(alpha), float(smax), int(rand_skip)) == 0
+    return XX
+
+
+def clear_combine(XX, bs):
+    """LOWRANKCOIL::combine of coil images (T, C, Nz, Ny, Nx) into (T, Nz, Ny, Nx) (zero where
+    no block covers a voxel).  Each block's result carries the unit phase of its first right
+    singular vector, which the SVD leaves free."""
+    XX = _c64(XX)
+    T, C, Nz, Ny, Nx = XX.shape
+    im = np.zeros((T, Nz, Ny, Nx), np.complex64)
+    assert lib().ref_clear_combine(_vols(_coil_vols(XX)), T, C, Nx, Ny, Nz, (ctypes.c_int * 3)(*bs),
+                                   _vols([im[t] for t in range(T)])) == 0
+    return im

@@ -1,6 +1,6 @@
-// C entry points over the reference's own gridFFT, WAVELET3D and THRESHOLD classes
-// (src/gridFFT.cpp, src/ArrayTemplates.cpp, src/wavelet3D.cpp, src/threshold.cpp compiled
-// unmodified against the stand-in headers in refshim/), for checking the oracle
+// C entry points over the reference's own gridFFT, WAVELET3D, THRESHOLD and LOWRANKCOIL
+// classes (src/gridFFT.cpp, src/ArrayTemplates.cpp, src/wavelet3D.cpp, src/threshold.cpp,
+// src/clear.cpp compiled unmodified against the stand-in headers in refshim/), for checking the oracle
 // restatement against the reference itself.  Test infrastructure only: built into
 // oracle/_ref/libref.so by `make -C oracle ref` where the reference sources are present,
 // and loaded only by tests/test_oracle_ref.py.
@@ -10,9 +10,11 @@
 // trajectories are flat arrays of M samples, an (M, 1, 1) column-major array; the
 // oversampled grid is (Sz, Sy, Sx).
 #include <complex>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
+#include "clear.h"
 #include "gridFFT.h"
 #include "threshold.h"
 #include "wavelet3D.h"
@@ -56,6 +58,44 @@ void setup(gridFFT &g, const Config &c, int Nx, int Ny, int Nz) {
   }
   data.Num_Coils = 1;
   g.precalc_gridding(Nz, Ny, Nx, data);
+}
+
+// LOWRANKCOIL as recon_lib's loops use it, with the block edges update_threshold leaves
+// in its members (clamped to the image) and the rand() stream of a process that seeded it
+// with srand(1) and has drawn `skip` numbers since.
+LOWRANKCOIL lowrank(const int *bs, int Nx, int Ny, int Nz, int block_iter, float amp, float t2) {
+  LOWRANKCOIL lr;
+  lr.block_size_x = std::min(bs[0], Nx);
+  lr.block_size_y = std::min(bs[1], Ny);
+  lr.block_size_z = std::min(bs[2], Nz);
+  lr.block_iter = block_iter;
+  lr.clear_amp = amp;
+  lr.clear_t2 = t2;
+  return lr;
+}
+
+void seed_rand(long skip) {
+  std::srand(1);
+  for (long i = 0; i < skip; i++) std::rand();
+}
+
+// Nt frames (Ne = 1) of one image each, vols[t] -> image(t, 0)
+Array<Array<cf, 3>, 2> frames(void **vols, int Nt, int Nx, int Ny, int Nz) {
+  Array<Array<cf, 3>, 2> im;
+  im.setStorage(ColumnMajorArray<2>());
+  im.resize(Nt, 1);
+  for (int t = 0; t < Nt; t++) im(t, 0).reference(col3<cf>(Nx, Ny, Nz, vols[t]));
+  return im;
+}
+
+// Nt frames (Ne = 1) of C coil images, vols[t * C + c] -> image(t, 0, c)
+Array<Array<cf, 3>, 3> coil_frames(void **vols, int Nt, int C, int Nx, int Ny, int Nz) {
+  Array<Array<cf, 3>, 3> im;
+  im.setStorage(ColumnMajorArray<3>());
+  im.resize(Nt, 1, C);
+  for (int t = 0; t < Nt; t++)
+    for (int c = 0; c < C; c++) im(t, 0, c).reference(col3<cf>(Nx, Ny, Nz, vols[t * C + c]));
+  return im;
 }
 
 struct Traj {
@@ -197,6 +237,62 @@ float ref_fraction_threshold(int Nx, int Ny, int Nz, int nvol, void **vols, floa
     for (int t = 0; t < nvol; t++) std::memcpy(vols[t], coef(t, 0).data(), sizeof(cf) * (size_t)Nx * Ny * Nz);
   }
   return th.global_threshold;
+}
+
+// LOWRANKCOIL::update_threshold(image, 0, iter) over Nt frames: the time low-rank smax.
+float ref_llr_update_threshold(void **vols, int Nt, int Nx, int Ny, int Nz, const int *bs, float amp, float t2,
+                               int iter) {
+  LOWRANKCOIL lr = lowrank(bs, Nx, Ny, Nz, 1, amp, t2);
+  Array<Array<cf, 3>, 2> im = frames(vols, Nt, Nx, Ny, Nz);
+  lr.update_threshold(im, 0, iter);
+  return lr.smax;
+}
+
+// LOWRANKCOIL::thresh(image, 0) in place, with clear_alpha_time = alpha and the given smax.
+int ref_llr_thresh(void **vols, int Nt, int Nx, int Ny, int Nz, const int *bs, int block_iter, float alpha,
+                   float smax, long rand_skip) {
+  LOWRANKCOIL lr = lowrank(bs, Nx, Ny, Nz, block_iter, 4.0f, 6.0f);
+  lr.clear_alpha_time = alpha;
+  lr.smax = smax;
+  Array<Array<cf, 3>, 2> im = frames(vols, Nt, Nx, Ny, Nz);
+  seed_rand(rand_skip);
+  lr.thresh(im, 0);
+  for (int t = 0; t < Nt; t++) std::memcpy(vols[t], im(t, 0).data(), sizeof(cf) * (size_t)Nx * Ny * Nz);
+  return 0;
+}
+
+// LOWRANKCOIL::update_threshold(image, 2, iter) over Nt frames of C coil images.
+float ref_clear_update_threshold(void **vols, int Nt, int C, int Nx, int Ny, int Nz, const int *bs, float amp,
+                                 float t2, int iter) {
+  LOWRANKCOIL lr = lowrank(bs, Nx, Ny, Nz, 1, amp, t2);
+  Array<Array<cf, 3>, 3> im = coil_frames(vols, Nt, C, Nx, Ny, Nz);
+  lr.update_threshold(im, 2, iter);
+  return lr.smax;
+}
+
+// LOWRANKCOIL::thresh(image, 2) in place, with clear_alpha_coil = alpha and the given smax.
+int ref_clear_thresh(void **vols, int Nt, int C, int Nx, int Ny, int Nz, const int *bs, int block_iter, float alpha,
+                     float smax, long rand_skip) {
+  LOWRANKCOIL lr = lowrank(bs, Nx, Ny, Nz, block_iter, 4.0f, 6.0f);
+  lr.clear_alpha_coil = alpha;
+  lr.smax = smax;
+  Array<Array<cf, 3>, 3> im = coil_frames(vols, Nt, C, Nx, Ny, Nz);
+  seed_rand(rand_skip);
+  lr.thresh(im, 2);
+  for (int t = 0; t < Nt; t++)
+    for (int c = 0; c < C; c++)
+      std::memcpy(vols[t * C + c], im(t, 0, c).data(), sizeof(cf) * (size_t)Nx * Ny * Nz);
+  return 0;
+}
+
+// LOWRANKCOIL::combine(image, out): out[t] (Nt images, updated where blocks cover them).
+int ref_clear_combine(void **vols, int Nt, int C, int Nx, int Ny, int Nz, const int *bs, void **out) {
+  LOWRANKCOIL lr = lowrank(bs, Nx, Ny, Nz, 1, 4.0f, 6.0f);
+  Array<Array<cf, 3>, 3> im = coil_frames(vols, Nt, C, Nx, Ny, Nz);
+  Array<Array<cf, 3>, 2> o = frames(out, Nt, Nx, Ny, Nz);
+  lr.combine(im, o);
+  for (int t = 0; t < Nt; t++) std::memcpy(out[t], o(t, 0).data(), sizeof(cf) * (size_t)Nx * Ny * Nz);
+  return 0;
 }
 
 }  // extern "C"

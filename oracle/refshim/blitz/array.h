@@ -224,6 +224,15 @@ class Array {
     const long idx[N] = {static_cast<long>(i)...};
     return data_[offset(idx)];
   }
+  // fewer int indices than the rank: Blitz computes the offset from the indices given, so
+  // the others count as 0 (src/clear.cpp:566-568 reads the shape of image(0, 0) of a
+  // rank-3 array of images this way)
+  template <typename... I>
+  typename std::enable_if<(sizeof...(I) >= 2) && (sizeof...(I) < N) && all_index_args<I...>::value, T &>::type
+  operator()(I... i) {
+    long idx[N] = {static_cast<long>(i)...};
+    return data_[offset(idx)];
+  }
   T &operator()(const TinyVector<int, N> &i) {
     long idx[N];
     for (int d = 0; d < N; d++) idx[d] = i(d);

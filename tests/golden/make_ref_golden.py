@@ -1,9 +1,14 @@
-"""Writes tests/golden/ref_ops.npz: inputs and outputs of the reference's own gridFFT,
-WAVELET3D and THRESHOLD code (oracle/_ref/libref.so, built from the reference sources by
-`make -C oracle ref`) on small seeded cases, so that the GPU tests can check the CUDA path
-against the reference directly on a machine without the reference sources.
+"""Writes inputs and outputs of the reference's own code (oracle/_ref/libref.so, built from
+the reference sources by `make -C oracle ref`) on small seeded cases, so that the GPU tests
+can check the CUDA path against the reference directly on a machine without the reference
+sources:
 
-Run from the repository root: python tests/golden/make_ref_golden.py
+  tests/golden/ref_ops.npz      gridFFT (E, residual E, E^H, edge samples), WAVELET3D, THRESHOLD
+  tests/golden/ref_lowrank.npz  LOWRANKCOIL in time (update_threshold, thresh) and in the coil
+                                dimension (update_threshold, thresh, combine)
+
+Run from the repository root: python tests/golden/make_ref_golden.py [ops] [lowrank]
+(both when no argument is given).
 """
 import os
 import sys
@@ -14,11 +19,31 @@ ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)
 sys.path.insert(0, ROOT)
 
 from oracle import ref as R  # noqa: E402
-from tests.helpers import case, edge_trajectory  # noqa: E402
+from tests.helpers import case, edge_trajectory, low_rank_frames  # noqa: E402
 
 
-def main():
-    assert R.available(), "oracle/_ref needs the reference sources"
+def lowrank():
+    out = {}
+    rng = np.random.default_rng(211)
+    # time low rank: 6 frames of 12^3, 4^3 blocks (27 per shift), iteration 2 of the schedule
+    X = low_rank_frames(rng, 6, (12, 12, 12))
+    vols = [X[t] for t in range(6)]
+    smax = R.llr_update_threshold(vols, (4, 4, 4), 4.0, 6.0, 2)
+    out.update(llr_in=X, llr_smax=np.float32(smax))
+    out["llr_out"] = np.stack(R.llr_thresh(vols, (4, 4, 4), 4, 0.1, smax, 11))
+    out["llr_out_iter1"] = np.stack(R.llr_thresh(vols, (4, 4, 4), 1, 0.1, smax, 0))  # no shift
+    # coil low rank: 2 frames x 6 coils of 8^3 (the reference's layout (T, C, Nz, Ny, Nx))
+    XX = np.stack([low_rank_frames(rng, 6, (8, 8, 8)) for _ in range(2)])
+    smax_c = R.clear_update_threshold(XX, (4, 4, 4), 4.0, 6.0, 1)
+    out.update(coil_in=XX, coil_smax=np.float32(smax_c))
+    out["coil_out"] = R.clear_thresh(XX, (4, 4, 4), 4, 0.05, smax_c, 5)
+    out["coil_combine"] = R.clear_combine(XX, (4, 4, 4))
+    path = os.path.join(ROOT, "tests", "golden", "ref_lowrank.npz")
+    np.savez_compressed(path, **out)
+    print(path, os.path.getsize(path), "bytes")
+
+
+def ops():
     out = {}
     # two coils, 24^3 image, 400 x 24 radial: E, E residual, E^H per coil
     N, C = 24, 2
@@ -51,5 +76,11 @@ def main():
     print(path, os.path.getsize(path), "bytes")
 
 
+def main(which):
+    assert R.available(), "oracle/_ref needs the reference sources"
+    for name in which or ("ops", "lowrank"):
+        {"ops": ops, "lowrank": lowrank}[name]()
+
+
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

@@ -57,3 +57,32 @@ def edge_trajectory(N, seed=3):
     kw[5] = 0.0
     kw[20] = 0.0
     return k[:, 0].copy(), k[:, 1].copy(), k[:, 2].copy(), kw
+
+
+def low_rank_frames(rng, T, shape_zyx, rank=2, noise=0.3):
+    """T frames (T, Nz, Ny, Nx) complex64 that share `rank` spatial components with smooth
+    temporal weights, plus noise: blocks whose leading singular values stand out, as in a
+    gated series, so a low-rank threshold keeps some and removes others."""
+    comps = rng.standard_normal((rank,) + tuple(shape_zyx)) + 1j * rng.standard_normal((rank,) + tuple(shape_zyx))
+    t = np.arange(T)[:, None]
+    w = np.cos(np.pi * (np.arange(rank)[None, :] + 1) * (t + 0.5) / T) + 1.0
+    X = np.tensordot(w, comps, axes=1)
+    X += noise * (rng.standard_normal(X.shape) + 1j * rng.standard_normal(X.shape))
+    return X.astype(np.complex64)
+
+
+def align_block_phases(got, ref, bs):
+    """ref (T, Nz, Ny, Nx) with each whole unshifted block of bs = (bx, by, bz) voxels turned
+    by the unit phase that brings it closest to got: LOWRANKCOIL::combine's output per
+    block carries the phase of a singular vector, which an SVD leaves free."""
+    out = np.array(ref, copy=True)
+    Nz, Ny, Nx = ref.shape[1:]
+    bx, by, bz = bs
+    for k in range(0, Nz - bz + 1, bz):
+        for j in range(0, Ny - by + 1, by):
+            for i in range(0, Nx - bx + 1, bx):
+                sl = (slice(None), slice(k, k + bz), slice(j, j + by), slice(i, i + bx))
+                z = np.vdot(ref[sl], got[sl])
+                if abs(z) > 0:
+                    out[sl] = ref[sl] * (z / abs(z))
+    return out

@@ -1,10 +1,12 @@
 """The CUDA path against outputs of the reference's own code.
 
 tests/golden/ref_ops.npz holds seeded inputs and the outputs of the reference's gridFFT
-(E, the residual E, E^H per coil), WAVELET3D and THRESHOLD, computed by the reference
-sources compiled unmodified (oracle/_ref; tests/golden/make_ref_golden.py).  The GPU runs
-the same inputs through the C ABI.  Bound: relative L2 <= 1e-5 per operator application
-(FP32 on both sides; summation orders differ), 1e-6 for the wavelet and threshold.
+(E, the residual E, E^H per coil), WAVELET3D and THRESHOLD, and tests/golden/ref_lowrank.npz
+those of LOWRANKCOIL in time and in the coil dimension, computed by the reference sources
+compiled unmodified (oracle/_ref; tests/golden/make_ref_golden.py).  The GPU runs the same
+inputs through the C ABI.  Bound: relative L2 <= 1e-5 per operator application (FP32 on
+both sides; summation orders differ), 1e-6 for the wavelet and threshold, 1e-5 for the
+low-rank blocks (the GPU's Jacobi SVDs run in FP32 up to 16 coils).
 """
 import ctypes
 import os
@@ -12,14 +14,20 @@ import os
 import numpy as np
 import pytest
 
-from tests.helpers import rel
+from tests.helpers import align_block_phases, rel
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_ops.npz")
+LOWRANK = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_lowrank.npz")
 
 
 @pytest.fixture(scope="module")
 def gold():
     return dict(np.load(GOLD))
+
+
+@pytest.fixture(scope="module")
+def lowrank():
+    return dict(np.load(LOWRANK))
 
 
 def test_oracle_reproduces_the_reference_fixture(oracle_lib, gold):
@@ -86,3 +94,50 @@ def test_wavelet_and_threshold_match_reference_outputs(mrg_lib, gold):
     assert L.mrg_soft_threshold(ctypes.c_void_p(W.ctypes.data), W.size, ctypes.c_float(float(g["thr_value"])),
                                 None) == 0
     assert rel(W, g["thr_out"]) < 1e-6
+
+
+def test_oracle_reproduces_the_low_rank_fixture(oracle_lib, lowrank):
+    """CPU: the oracle gives the low-rank fixture's reference outputs (6 frames of 12^3 in
+    4^3 blocks; 2 frames x 6 coils of 8^3)."""
+    g = lowrank
+    X = g["llr_in"]
+    vols = [X[t] for t in range(X.shape[0])]
+    smax = float(g["llr_smax"])
+    assert abs(oracle_lib.llr_update_threshold(vols, (4, 4, 4), 4.0, 6.0, 2) - smax) <= 1e-6 * smax
+    assert rel(np.stack(oracle_lib.llr_thresh(vols, (4, 4, 4), 4, 0.1, smax, 11)), g["llr_out"]) < 1e-6
+    assert rel(np.stack(oracle_lib.llr_thresh(vols, (4, 4, 4), 1, 0.1, smax, 0)), g["llr_out_iter1"]) < 1e-6
+    XX, sc = g["coil_in"], float(g["coil_smax"])
+    assert abs(oracle_lib.clear_update_threshold(XX, (4, 4, 4), 4.0, 6.0, 1) - sc) <= 1e-6 * sc
+    assert rel(oracle_lib.clear_thresh(XX, (4, 4, 4), 4, 0.05, sc, 5), g["coil_out"]) < 1e-6
+    im = oracle_lib.clear_combine(XX, (4, 4, 4))
+    assert rel(im, align_block_phases(im, g["coil_combine"], (4, 4, 4))) < 1e-6
+
+
+@pytest.mark.gpu
+def test_low_rank_blocks_match_reference_outputs(mrg_lib, lowrank):
+    """mrg_llr_update_threshold / mrg_llr_thresh (time) and mrg_clear_update_threshold /
+    mrg_clear_thresh / mrg_clear_combine (coils) on the fixture's inputs against the
+    reference's outputs; combine after turning each reference block to the library's phase
+    of v1 (its largest-magnitude component real and positive)."""
+    g = lowrank
+    L = mrg_lib.load()
+    ip = lambda v: (ctypes.c_int * 3)(*v)  # noqa: E731
+    X = np.ascontiguousarray(g["llr_in"])
+    T, Nz, Ny, Nx = X.shape
+    sm = ctypes.c_float()
+    assert L.mrg_llr_update_threshold(ctypes.c_void_p(X.ctypes.data), T, Nx, Ny, Nz, ip((4, 4, 4)), 4.0, 6.0, 2,
+                                      ctypes.byref(sm), None) == 0
+    smax = float(g["llr_smax"])
+    assert abs(sm.value - smax) <= 1e-5 * smax
+    for block_iter, skip, key in [(4, 11, "llr_out"), (1, 0, "llr_out_iter1")]:
+        Y = X.copy()
+        assert L.mrg_llr_thresh(ctypes.c_void_p(Y.ctypes.data), T, Nx, Ny, Nz, ip((4, 4, 4)), block_iter, 0.1, smax,
+                                skip, None) == 0
+        assert rel(Y, g[key]) < 1e-5
+    XX = np.ascontiguousarray(g["coil_in"].transpose(0, 2, 3, 4, 1))  # the library's (T, Nz, Ny, Nx, C)
+    sc = float(g["coil_smax"])
+    assert abs(mrg_lib.clear_update_threshold(XX, (4, 4, 4), 4.0, 6.0, 1) - sc) <= 1e-5 * sc
+    Y = mrg_lib.clear_thresh(XX.copy(), sc, (4, 4, 4), 4, 0.05, 5)
+    assert rel(Y, g["coil_out"].transpose(0, 2, 3, 4, 1)) < 1e-5
+    im = mrg_lib.clear_combine(XX, (4, 4, 4))
+    assert rel(im, align_block_phases(im, g["coil_combine"], (4, 4, 4))) < 1e-5

@@ -1,12 +1,13 @@
 """The oracle restatement (and the library's host-side tables) against the reference's own
-code: src/gridFFT.cpp, src/ArrayTemplates.cpp, src/wavelet3D.cpp and src/threshold.cpp
-compiled unmodified into oracle/_ref/libref.so (``make -C oracle ref``, stand-in headers
-for Blitz++ / FFTW / Armadillo / HDF5 in oracle/refshim).
+code: src/gridFFT.cpp, src/ArrayTemplates.cpp, src/wavelet3D.cpp, src/threshold.cpp and
+src/clear.cpp compiled unmodified into oracle/_ref/libref.so (``make -C oracle ref``,
+stand-in headers for Blitz++ / FFTW / Armadillo / HDF5 in oracle/refshim).
 
 Tolerances: tables bit for bit; operators and stages at relative L2 <= 1e-6 (both sides
 FP32; the reference adds its gridding with unordered OpenMP atomics and its stand-in FFT
 rounds a double-precision transform, so the last bits differ); wavelets and thresholds
-at 1e-6.  These tests need the reference sources and are skipped where they are absent
+at 1e-6; the low-rank block operations of LOWRANKCOIL (SVDs in double on both sides, a
+one-sided Jacobi here and in the Armadillo stand-in) at 1e-6.  These tests need the reference sources and are skipped where they are absent
 (the GPU host).
 """
 import ctypes
@@ -14,7 +15,7 @@ import ctypes
 import numpy as np
 import pytest
 
-from tests.helpers import case, edge_trajectory, rel
+from tests.helpers import align_block_phases, case, edge_trajectory, low_rank_frames, rel
 
 R = pytest.importorskip("oracle.ref")
 if not R.available():
@@ -160,3 +161,67 @@ def test_fraction_threshold_matches_reference(O, fraction):
     assert abs(t - t_ref) <= 1e-6 * t_ref
     for v, r in zip(vols, out_ref):
         assert rel(O.soft_threshold(v, t), r) < TOL
+
+
+# (frames, (Nx, Ny, Nz), block, iteration): cubic and anisotropic blocks, blocks that do not
+# divide the image, a block larger than the image (update_threshold clamps it)
+LLR_CASES = [(6, (16, 12, 8), (4, 4, 4), 2), (10, (16, 16, 16), (8, 8, 8), 0), (4, (12, 8, 8), (8, 4, 2), 7),
+             (5, (8, 8, 4), (16, 16, 16), 1)]
+
+
+@pytest.mark.parametrize("T,N,bs,it", LLR_CASES)
+def test_time_low_rank_threshold_matches_reference(O, T, N, bs, it):
+    """LOWRANKCOIL::update_threshold(image, 0, iteration) (src/clear.cpp:233-351): the median
+    of the blocks' sigma_1 times the amplitude schedule."""
+    X = low_rank_frames(np.random.default_rng(21 + T), T, N[::-1])
+    vols = [X[t] for t in range(T)]
+    r = R.llr_update_threshold(vols, bs, 4.0, 6.0, it)
+    assert abs(O.llr_update_threshold(vols, bs, 4.0, 6.0, it) - r) <= TOL * r
+    assert abs(O.llr_update_threshold([v.astype(np.complex128) for v in vols], bs, 4.0, 6.0, it) - r) <= TOL * r
+
+
+@pytest.mark.parametrize("T,N,bs,it", LLR_CASES)
+@pytest.mark.parametrize("block_iter,rand_skip", [(4, 0), (4, 1000), (1, 5)])
+def test_time_low_rank_thresh_matches_reference(O, T, N, bs, it, block_iter, rand_skip):
+    """LOWRANKCOIL::thresh(image, 0) (src/clear.cpp:356-556): rand() block shifts (none when
+    block_iter is 1), per block A <- U max(s - alpha smax / block_iter, 0) V^H, in place."""
+    X = low_rank_frames(np.random.default_rng(31 + T), T, N[::-1])
+    vols = [X[t] for t in range(T)]
+    bsc = tuple(min(b, n) for b, n in zip(bs, N))
+    smax = R.llr_update_threshold(vols, bsc, 4.0, 6.0, it)
+    r = np.stack(R.llr_thresh(vols, bsc, block_iter, 0.1, smax, rand_skip))
+    assert rel(r, X) > 1e-2  # the threshold changed the frames
+    assert rel(np.stack(O.llr_thresh(vols, bs, block_iter, 0.1, smax, rand_skip)), r) < TOL
+    assert rel(np.stack(O.llr_thresh([v.astype(np.complex128) for v in vols], bs, block_iter, 0.1, smax,
+                                     rand_skip)), r) < TOL
+
+
+# (frames, coils, (Nx, Ny, Nz), block): frames <= coils, as the reference's update_threshold
+# with dim = 2 requires
+COIL_CASES = [(2, 6, (8, 8, 8), (4, 4, 4)), (1, 8, (12, 8, 8), (4, 4, 2)), (3, 5, (10, 12, 8), (4, 3, 4)),
+              (1, 16, (8, 8, 8), (8, 8, 8))]
+
+
+def _coil_stack(T, C, N, seed):
+    rng = np.random.default_rng(seed)
+    return np.stack([low_rank_frames(rng, C, N[::-1]) for _ in range(T)])  # (T, C, Nz, Ny, Nx)
+
+
+@pytest.mark.parametrize("T,C,N,bs", COIL_CASES)
+def test_coil_low_rank_matches_reference(O, T, C, N, bs):
+    """LOWRANKCOIL in the coil dimension: update_threshold(image, 2) (src/clear.cpp:99-232,
+    the column index t quirk included), thresh(image, 2) (:561-813, full SVDs) and combine
+    (:815-914) against the reference.  combine is compared after giving each block the
+    unit phase of the oracle's (its first right singular vector's phase is free)."""
+    XX = _coil_stack(T, C, N, 41 + C)
+    r = R.clear_update_threshold(XX, bs, 4.0, 6.0, 1)
+    assert abs(O.clear_update_threshold(XX, bs, 4.0, 6.0, 1) - r) <= TOL * r
+    for block_iter, skip in [(4, 5), (1, 0)]:
+        Y = R.clear_thresh(XX, bs, block_iter, 0.05, r, skip)
+        assert rel(Y, XX) > 1e-3
+        assert rel(O.clear_thresh(XX, bs, block_iter, 0.05, r, skip), Y) < TOL
+        assert rel(O.clear_thresh(XX.astype(np.complex128), bs, block_iter, 0.05, r, skip), Y) < TOL
+    im_ref = R.clear_combine(XX, bs)
+    im = O.clear_combine(XX, bs)
+    assert rel(np.abs(im), np.abs(im_ref)) < TOL
+    assert rel(im, align_block_phases(im, im_ref, bs)) < TOL
