@@ -97,6 +97,7 @@ class gridFFT {
     cfg.kernel_type = kernel_type;
     cfg.k_rad = k_rad;
     cfg.time_grid = time_grid;
+    cfg.fft_norm = fft_norm_;
     if (plan_) mrg_plan_destroy(plan_);
     plan_ = nullptr;
     check(mrg_plan_create(&cfg, NxT, NyT, NzT, ncoil, 1, &plan_));
@@ -126,15 +127,23 @@ class gridFFT {
     keyM_ = M;
   }
   mrg_plan *plan_ = nullptr;
+  int fft_norm_ = 0;  // mrg_config.fft_norm: 1 for the coil-threaded class's unnormalised FFTs
   const void *key_[4] = {nullptr, nullptr, nullptr, nullptr};
   int64_t keyM_ = -1;
   float k_rad_set_ = 9999.0f;
 };
 
 // All coils in one call (the reference's -parallel_coils path).  smaps and data are
-// coil-major: coil c at smaps + c*Nx*Ny*Nz and data + c*M.
+// coil-major: coil c at smaps + c*Nx*Ny*Nz and data + c*M.  As the reference's class, it
+// defaults to overgrid 1.375 (src/gridFFT_CoilThreaded.cpp:31) and transforms without the
+// 1/sqrt(S) per axis of gridFFT (its FFTW calls are unnormalised,
+// src/gridFFT_CoilThreaded.cpp:570-893), so its E and E^H are sqrt(Sx Sy Sz) times gridFFT's.
 class gridFFT_CoilThreaded : public gridFFT {
  public:
+  gridFFT_CoilThreaded() {
+    overgrid = 1.375f;
+    fft_norm_ = 1;
+  }
   void precalc_gridding(int NzT, int NyT, int NxT, int ncoils) {
     setup(NzT, NyT, NxT, ncoils);
     ncoils_ = ncoils;

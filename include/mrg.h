@@ -65,6 +65,10 @@ typedef struct mrg_config {
                         tensor cores through tcgen05 with W and the accumulators in tensor memory
                         (>= 8 coils); 2 and 3 in TF32 with the three-term hi/lo split
                         (W V ~ Wh Vh + Wh Vl + Wl Vh, products to ~2^-20) */
+  int fft_norm;      /* 0: every FFT pass scaled by 1/sqrt(S), as gridFFT's fft3 (src/ArrayTemplates.cpp:311,
+                        :338-342); 1: unnormalised passes, as gridFFT_CoilThreaded's do_fft / do_ifft
+                        (src/gridFFT_CoilThreaded.cpp:570-893), so E and E^H (and mrg_fft3) are
+                        sqrt(Sx Sy Sz) times those of 0 */
 } mrg_config;
 
 /* Fills the reference defaults (src/gridFFT.cpp:28-60). */

@@ -27,7 +27,8 @@ _dp = ctypes.POINTER(ctypes.c_double)
 class MrgConfig(ctypes.Structure):
     _fields_ = [("overgrid", ctypes.c_float), ("dwin", ctypes.c_float), ("kernel_type", ctypes.c_int),
                 ("k_rad", ctypes.c_float), ("time_grid", ctypes.c_int), ("tile", ctypes.c_int),
-                ("max_pairs", ctypes.c_int), ("kernel_eval", ctypes.c_int), ("grid_mode", ctypes.c_int)]
+                ("max_pairs", ctypes.c_int), ("kernel_eval", ctypes.c_int), ("grid_mode", ctypes.c_int),
+                ("fft_norm", ctypes.c_int)]
 
 
 class MrgDcfParams(ctypes.Structure):

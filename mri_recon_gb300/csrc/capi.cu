@@ -260,6 +260,14 @@ static int plan_ib(const mrg_plan *p, int k, int64_t inner, int C, bool accum, i
   return v;
 }
 
+// Scale of one FFT pass over S points: 1/sqrt(S), as gridFFT's fft3 scales each axis
+// (src/ArrayTemplates.cpp:311, :338-342), or 1 for a plan with fft_norm = 1, whose
+// transforms are unnormalised as gridFFT_CoilThreaded's FFTW calls are
+// (src/gridFFT_CoilThreaded.cpp:570-893): its E and E^H are then sqrt(Sx Sy Sz) larger.
+static float pass_scale(const mrg_plan *p, int64_t S) {
+  return p->cfg.fft_norm ? 1.0f : (float)(1. / std::sqrt((float)S));
+}
+
 // Stage timing (mrg_set_timing): events between the four stages of E or E^H.
 static void tmark(mrg_plan *p, int k, cudaStream_t st) {
   if (p->timing_on) cudaEventRecord(p->tev[k], st);
@@ -321,7 +329,7 @@ static mrg_status run_E_grid_zxy(mrg_plan *p, const float2 *X, const float2 *sma
   a.inner = (int)(Nx * C); a.IB = plan_ib(p, 0, a.inner, C, false, a.S); a.lfast = 0;
   a.nlines = Ny * Nx * C;
   a.in_ls = Nx * Ny * C; a.in_os = Nx * C; a.out_ls = Ny * Nx * C; a.out_os = Nx * C;
-  a.scale = (float)(1. / std::sqrt((float)Sz));
+  a.scale = pass_scale(p, Sz);
   a.in = smap; a.smap = smap; a.has_smap = smap != nullptr; a.X = X; a.out = p->d_t1;
   a.wl = wz + g.og[2]; a.wo = wy + g.og[1]; a.wi = wx + g.og[0]; a.C = C;
   tmark(p, 0, st);
@@ -336,7 +344,7 @@ static mrg_status run_E_grid_zxy(mrg_plan *p, const float2 *X, const float2 *sma
   b.inner = (int)(Nx * C); b.IB = plan_ib(p, 1, b.inner, C, false, b.S);
   b.nlines = Sz * Nx * C;
   b.in_ls = Nx * C; b.in_os = Ny * Nx * C; b.out_ls = Nx * C; b.out_os = Sy * Nx * C;
-  b.scale = (float)(1. / std::sqrt((float)Sy));
+  b.scale = pass_scale(p, Sy);
   b.in = p->d_t1; b.out = p->d_t2; b.C = C;
   fft_vectorize(b);
   MRG_TRY(launch_fft(b, st));
@@ -349,7 +357,7 @@ static mrg_status run_E_grid_zxy(mrg_plan *p, const float2 *X, const float2 *sma
   c.inner = C; c.IB = (C == 1) ? pass_ib(C, C, c.S) : plan_ib(p, 2, C, C, false, c.S); c.lfast = (C == 1);
   c.nlines = Sz * Sy * C;
   c.in_ls = C; c.in_os = Nx * C; c.out_ls = C; c.out_os = Sx * C;
-  c.scale = (float)(1. / std::sqrt((float)Sx));
+  c.scale = pass_scale(p, Sx);
   c.in = p->d_t2; c.out = p->d_grid; c.C = C;
   fft_vectorize(c);
   MRG_TRY(launch_fft(c, st));
@@ -374,7 +382,7 @@ static mrg_status run_EH_xy(mrg_plan *p, const FrameTraj &ft, const float2 *y, c
   a.inner = C; a.IB = (C == 1) ? pass_ib(C, C, a.S) : plan_ib(p, 3, C, C, false, a.S); a.lfast = (C == 1);
   a.nlines = Sz * Sy * C;
   a.in_ls = C; a.in_os = Sx * C; a.out_ls = C; a.out_os = Nx * C;
-  a.scale = (float)(1. / std::sqrt((float)Sx));
+  a.scale = pass_scale(p, Sx);
   a.in = p->d_grid; a.out = p->d_t2; a.C = C;
   fft_vectorize(a);
   MRG_TRY(launch_fft(a, st));
@@ -386,7 +394,7 @@ static mrg_status run_EH_xy(mrg_plan *p, const FrameTraj &ft, const float2 *y, c
   b.inner = (int)(Nx * C); b.IB = plan_ib(p, 4, b.inner, C, false, b.S);
   b.nlines = Sz * Nx * C;
   b.in_ls = Nx * C; b.in_os = Sy * Nx * C; b.out_ls = Nx * C; b.out_os = Ny * Nx * C;
-  b.scale = (float)(1. / std::sqrt((float)Sy));
+  b.scale = pass_scale(p, Sy);
   b.in = p->d_t2; b.out = p->d_t1; b.C = C;
   fft_vectorize(b);
   MRG_TRY(launch_fft(b, st));
@@ -409,7 +417,7 @@ static mrg_status run_EH_xyz(mrg_plan *p, const FrameTraj &ft, const float2 *y, 
   c.inner = (int)(Nx * C); c.IB = plan_ib(p, 5, c.inner, C, true, c.S);
   c.nlines = Ny * Nx * C;
   c.in_ls = Ny * Nx * C; c.in_os = Nx * C; c.out_ls = Nx * Ny * C; c.out_os = Nx * C;
-  c.scale = (float)(1. / std::sqrt((float)Sz));
+  c.scale = pass_scale(p, Sz);
   c.in = p->d_t1; c.smap = smap; c.has_smap = smap != nullptr; c.acc = X;
   c.acc_atomic = (c.IB % C) != 0; c.acc_l = Nx * Ny; c.acc_o = Nx;
   c.wl = wz + g.og[2]; c.wo = wy + g.og[1]; c.wi = wx + g.og[0]; c.C = C;
@@ -434,7 +442,7 @@ static mrg_status run_EH_crop_xyz(mrg_plan *p, const FrameTraj &ft, const float2
   c.inner = (int)(Nx * C); c.IB = plan_ib(p, 5, c.inner, C, false, c.S);
   c.nlines = Ny * Nx * C;
   c.in_ls = Ny * Nx * C; c.in_os = Nx * C; c.out_ls = Ny * Nx * C; c.out_os = Nx * C;
-  c.scale = (float)(1. / std::sqrt((float)Sz));
+  c.scale = pass_scale(p, Sz);
   c.in = p->d_t1; c.out = p->d_t2; c.C = C;
   fft_vectorize(c);
   MRG_TRY(launch_fft(c, st));
@@ -459,7 +467,7 @@ static mrg_status run_E_grid(mrg_plan *p, const float2 *X, const float2 *smap, c
   a.inner = C; a.IB = plan_ib(p, 0, C, C, false, a.S); a.lfast = 0;
   a.nlines = Nz * Ny * C;
   a.in_ls = C; a.in_os = Nx * C; a.out_ls = C; a.out_os = Sx * C;
-  a.scale = (float)(1. / std::sqrt((float)Sx));
+  a.scale = pass_scale(p, Sx);
   a.in = smap; a.smap = smap; a.has_smap = smap != nullptr; a.X = X; a.out = p->d_t1;
   a.wmode = 1; a.wdiv = Ny; a.wl = wx + g.og[0]; a.wo = wz + g.og[2]; a.wi = wy + g.og[1]; a.C = C;
   a.xp = p->fft_xp[0];
@@ -475,7 +483,7 @@ static mrg_status run_E_grid(mrg_plan *p, const float2 *X, const float2 *smap, c
   b.inner = (int)(Ny * Sx * C); b.IB = plan_ib(p, 1, b.inner, C, false, b.S);
   b.nlines = Ny * Sx * C;
   b.in_ls = Ny * Sx * C; b.in_os = 0; b.out_ls = Ny * Sx * C; b.out_os = 0;
-  b.scale = (float)(1. / std::sqrt((float)Sz));
+  b.scale = pass_scale(p, Sz);
   b.in = p->d_t1; b.out = p->d_t2; b.C = C; b.xp = p->fft_xp[1]; b.err = p->d_err;
   fft_vectorize(b);
   MRG_TRY(launch_fft(b, st));
@@ -489,7 +497,7 @@ static mrg_status run_E_grid(mrg_plan *p, const float2 *X, const float2 *smap, c
   c.inner = (int)(Sx * C); c.IB = plan_ib(p, 2, c.inner, C, false, c.S);
   c.nlines = Sz * Sx * C;
   c.in_ls = Sx * C; c.in_os = Ny * Sx * C; c.out_ls = Sx * C; c.out_os = Sy * Sx * C;
-  c.scale = (float)(1. / std::sqrt((float)Sy));
+  c.scale = pass_scale(p, Sy);
   c.in = p->d_t2; c.out = p->d_grid; c.C = C; c.xp = p->fft_xp[2]; c.err = p->d_err;
   fft_vectorize(c);
   MRG_TRY(launch_fft(c, st));
@@ -515,7 +523,7 @@ static mrg_status run_EH_yz(mrg_plan *p, const FrameTraj &ft, const float2 *y, c
   a.inner = (int)(Sx * C); a.IB = plan_ib(p, 3, a.inner, C, false, a.S);
   a.nlines = Sz * Sx * C;
   a.in_ls = Sx * C; a.in_os = Sy * Sx * C; a.out_ls = Sx * C; a.out_os = Ny * Sx * C;
-  a.scale = (float)(1. / std::sqrt((float)Sy));
+  a.scale = pass_scale(p, Sy);
   a.in = p->d_grid; a.out = p->d_t2; a.C = C; a.xp = p->fft_xp[3]; a.err = p->d_err;
   fft_vectorize(a);
   MRG_TRY(launch_fft(a, st));
@@ -528,7 +536,7 @@ static mrg_status run_EH_yz(mrg_plan *p, const FrameTraj &ft, const float2 *y, c
   b.inner = (int)(Ny * Sx * C); b.IB = plan_ib(p, 4, b.inner, C, false, b.S);
   b.nlines = Ny * Sx * C;
   b.in_ls = Ny * Sx * C; b.in_os = 0; b.out_ls = Ny * Sx * C; b.out_os = 0;
-  b.scale = (float)(1. / std::sqrt((float)Sz));
+  b.scale = pass_scale(p, Sz);
   b.in = p->d_t2; b.out = p->d_t1; b.C = C; b.xp = p->fft_xp[4]; b.err = p->d_err;
   fft_vectorize(b);
   MRG_TRY(launch_fft(b, st));
@@ -553,7 +561,7 @@ static mrg_status run_EH(mrg_plan *p, const FrameTraj &ft, const float2 *y, cons
   c.inner = C; c.IB = plan_ib(p, 5, C, C, true, c.S);
   c.nlines = Nz * Ny * C;
   c.in_ls = C; c.in_os = Sx * C; c.out_ls = C; c.out_os = Nx * C;
-  c.scale = (float)(1. / std::sqrt((float)Sx));
+  c.scale = pass_scale(p, Sx);
   c.in = p->d_t1; c.smap = smap; c.has_smap = smap != nullptr; c.acc = X;
   c.acc_atomic = (c.IB % C) != 0; c.acc_l = 1; c.acc_o = Nx;
   c.wmode = 1; c.wdiv = Ny; c.wl = wx + g.og[0]; c.wo = wz + g.og[2]; c.wi = wy + g.og[1]; c.C = C;
@@ -580,7 +588,7 @@ static mrg_status run_EH_crop(mrg_plan *p, const FrameTraj &ft, const float2 *y,
   c.inner = C; c.IB = (C == 1) ? pass_ib(C, C, c.S) : plan_ib(p, 5, C, C, false, c.S); c.lfast = (C == 1);
   c.nlines = Nz * Ny * C;
   c.in_ls = C; c.in_os = Sx * C; c.out_ls = C; c.out_os = Nx * C;
-  c.scale = (float)(1. / std::sqrt((float)Sx));
+  c.scale = pass_scale(p, Sx);
   c.in = p->d_t1; c.out = p->d_t2; c.C = C;
   fft_vectorize(c);
   MRG_TRY(launch_fft(c, st));
@@ -693,6 +701,7 @@ void mrg_config_default(mrg_config *cfg) {
   cfg->max_pairs = 0;
   cfg->kernel_eval = 0;
   cfg->grid_mode = 0;
+  cfg->fft_norm = 0;
 }
 
 const char *mrg_last_error(void) { return g_err.c_str(); }
@@ -713,7 +722,7 @@ mrg_status mrg_plan_create(const mrg_config *cfg_in, int Nx, int Ny, int Nz, int
   if (cfg_in) cfg = *cfg_in; else mrg_config_default(&cfg);
   if (!(cfg.overgrid >= 1.0f) || cfg.kernel_type < 0 || cfg.kernel_type > 3 || cfg.kernel_eval < 0 ||
       cfg.kernel_eval > 1 || (cfg.kernel_eval == 1 && cfg.kernel_type != MRG_KERNEL_KAISER) || cfg.grid_mode < 0 ||
-      cfg.grid_mode > 3) {
+      cfg.grid_mode > 3 || cfg.fft_norm < 0 || cfg.fft_norm > 1) {
     set_error("bad config");
     return MRG_ERR_INVALID;
   }
@@ -1345,7 +1354,7 @@ mrg_status mrg_fft3(mrg_plan *p, void *grid, int sign, void *stream) {
     a.inner = inner; a.IB = pass_ib(inner, C, a.S); a.lfast = 0;
     a.nlines = outer * inner;
     a.in_ls = ls; a.in_os = S * ls; a.out_ls = ls; a.out_os = S * ls;
-    a.scale = (float)(1. / std::sqrt((float)S));
+    a.scale = pass_scale(p, S);
     a.in = G; a.out = G; a.C = C;
     fft_vectorize(a);
     return launch_fft(a, st);

@@ -67,7 +67,7 @@ class Plan:
     """Coil-batched gridFFT plan with ``ncoils`` coils and ``nframes`` trajectories."""
 
     def __init__(self, N, ncoils=1, nframes=1, overgrid=1.5, dwin=-1.0, kernel_type=KAISER_KERNEL, k_rad=9999.0,
-                 tile=0, max_pairs=0, time_grid=0, analytic_kernel=False, grid_mode=0):
+                 tile=0, max_pairs=0, time_grid=0, analytic_kernel=False, grid_mode=0, fft_norm=0):
         L = _lib.load()
         if np.isscalar(N):
             N = (N, N, N)
@@ -79,6 +79,7 @@ class Plan:
         cfg.tile, cfg.max_pairs, cfg.time_grid = tile, max_pairs, time_grid
         cfg.kernel_eval = 1 if analytic_kernel else 0
         cfg.grid_mode = grid_mode
+        cfg.fft_norm = fft_norm
         h = ctypes.c_void_p()
         _lib.check(L.mrg_plan_create(ctypes.byref(cfg), self.N[0], self.N[1], self.N[2], self.ncoils, self.nframes,
                                      ctypes.byref(h)))

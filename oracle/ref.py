@@ -1,8 +1,8 @@
 """REFERENCE CHECKER -- TEST INFRASTRUCTURE ONLY.
 
 ctypes front end for ``oracle/_ref/libref.so``: the reference's own gridFFT.cpp,
-ArrayTemplates.cpp, wavelet3D.cpp, threshold.cpp and clear.cpp compiled unmodified (``make
--C oracle ref``) against the stand-in Blitz++ / FFTW / Armadillo / HDF5 headers of
+gridFFT_CoilThreaded.cpp, ArrayTemplates.cpp, wavelet3D.cpp, threshold.cpp and clear.cpp
+compiled unmodified (``make -C oracle ref``) against the stand-in Blitz++ / FFTW / Armadillo / HDF5 headers of
 ``oracle/refshim`` and driven by ``oracle/ref_driver.cpp``.  The tests use it to pin the
 oracle restatement (and, through committed fixtures, the CUDA path) to the reference's
 code.  It can only be built where the reference sources are present; ``available()``
@@ -54,6 +54,8 @@ def lib():
         L.ref_fraction_threshold.restype = ctypes.c_float
         L.ref_fraction_threshold.argtypes = [i, i, i, i, ctypes.POINTER(vp), f, i]
         pv = ctypes.POINTER(vp)
+        L.ref_coils_forward.argtypes = geo + [f, i, vp, pv, fp, fp, fp, fp, l, pv, pv]
+        L.ref_coils_adjoint.argtypes = geo + [f, i, vp, pv, pv, fp, fp, fp, fp, l]
         L.ref_llr_update_threshold.restype = ctypes.c_float
         L.ref_llr_update_threshold.argtypes = [pv, i, i, i, i, ip, f, f, i]
         L.ref_llr_thresh.argtypes = [pv, i, i, i, i, ip, i, f, f, l]
@@ -76,6 +78,10 @@ def _f32(a):
 
 def _p(a):
     return None if a is None else ctypes.c_void_p(a.ctypes.data)
+
+
+def _ptrs(arrs):
+    return (ctypes.c_void_p * len(arrs))(*[a.ctypes.data for a in arrs])
 
 
 class Gridder:
@@ -143,6 +149,28 @@ class Gridder:
         out = np.zeros(kx.size, np.complex64)
         assert lib().ref_ungrid(*self.geo, _p(grid), px, py, pz, pw, kx.size, _p(out), _p(diff)) == 0
         return out
+
+    def coils_forward(self, X, smaps, kx, ky, kz, kw, diff=None):
+        """gridFFT_CoilThreaded::backward (E of every coil of smaps (C, Nz, Ny, Nx)), or
+        backward_residual when diff (C, M) is given: (C, M)."""
+        X = _c64(X)
+        smaps = [_c64(m) for m in smaps]
+        C = len(smaps)
+        (kx, px), (ky, py), (kz, pz), (kw, pw) = _f32(kx), _f32(ky), _f32(kz), _f32(kw)
+        out = np.zeros((C, kx.size), np.complex64)
+        dif = None if diff is None else [_c64(d) for d in diff]
+        assert lib().ref_coils_forward(*self.geo, self.k_rad, C, _p(X), _ptrs(smaps), px, py, pz, pw, kx.size,
+                                       _ptrs([out[c] for c in range(C)]), None if dif is None else _ptrs(dif)) == 0
+        return out
+
+    def coils_adjoint(self, X, smaps, data, kx, ky, kz, kw):
+        """gridFFT_CoilThreaded::forward (E^H with maps, summed over the coils): X += ..."""
+        X = _c64(X).copy()
+        smaps, data = [_c64(m) for m in smaps], [_c64(d) for d in data]
+        (kx, px), (ky, py), (kz, pz), (kw, pw) = _f32(kx), _f32(ky), _f32(kz), _f32(kw)
+        assert lib().ref_coils_adjoint(*self.geo, self.k_rad, len(smaps), _p(X), _ptrs(smaps), _ptrs(data), px, py,
+                                       pz, pw, kx.size) == 0
+        return X
 
     def fft(self, grid, inverse):
         """do_fft (pruned to the crop) or do_ifft."""

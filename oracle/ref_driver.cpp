@@ -1,6 +1,7 @@
-// C entry points over the reference's own gridFFT, WAVELET3D, THRESHOLD and LOWRANKCOIL
-// classes (src/gridFFT.cpp, src/ArrayTemplates.cpp, src/wavelet3D.cpp, src/threshold.cpp,
-// src/clear.cpp compiled unmodified against the stand-in headers in refshim/), for checking the oracle
+// C entry points over the reference's own gridFFT, gridFFT_CoilThreaded, WAVELET3D,
+// THRESHOLD and LOWRANKCOIL classes (src/gridFFT.cpp, src/gridFFT_CoilThreaded.cpp,
+// src/ArrayTemplates.cpp, src/wavelet3D.cpp, src/threshold.cpp, src/clear.cpp compiled
+// unmodified against the stand-in headers in refshim/), for checking the oracle
 // restatement against the reference itself.  Test infrastructure only: built into
 // oracle/_ref/libref.so by `make -C oracle ref` where the reference sources are present,
 // and loaded only by tests/test_oracle_ref.py.
@@ -16,6 +17,7 @@
 
 #include "clear.h"
 #include "gridFFT.h"
+#include "gridFFT_CoilThreaded.h"
 #include "threshold.h"
 #include "wavelet3D.h"
 
@@ -96,6 +98,29 @@ Array<Array<cf, 3>, 3> coil_frames(void **vols, int Nt, int C, int Nx, int Ny, i
   for (int t = 0; t < Nt; t++)
     for (int c = 0; c < C; c++) im(t, 0, c).reference(col3<cf>(Nx, Ny, Nz, vols[t * C + c]));
   return im;
+}
+
+// gridFFT_CoilThreaded set up the same way, with the coil count in MRI_DATA
+// (precalc_gridding allocates one grid per coil from it)
+void setup_coils(gridFFT_CoilThreaded &g, const Config &c, int Nx, int Ny, int Nz, int C) {
+  g.overgrid = c.overgrid;
+  g.kernel_type = c.kernel_type;
+  if (c.dwin > 0.0f) g.dwinX = g.dwinY = g.dwinZ = c.dwin;
+  g.k_rad = c.k_rad;
+  MRI_DATA data;
+  for (int d = 0; d < 3; d++) {
+    data.trajectory_type(d) = MRI_DATA::NONCARTESIAN;
+    data.dft_needed(d) = true;
+  }
+  data.Num_Coils = C;
+  g.precalc_gridding(Nz, Ny, Nx, data);
+}
+
+// C arrays of n0 x n1 x n2 (column-major) over the caller's buffers, copied in
+Complex4D coil_arrays(void *const *bufs, int C, int n0, int n1, int n2) {
+  Complex4D a(C);
+  for (int c = 0; c < C; c++) a(c).reference(col3<cf>(n0, n1, n2, bufs ? bufs[c] : nullptr));
+  return a;
 }
 
 struct Traj {
@@ -201,6 +226,40 @@ int ref_fft(int Nx, int Ny, int Nz, float overgrid, int inverse, void *grid) {
   if (inverse) g.do_ifft();
   else g.do_fft();
   std::memcpy(grid, g.k3d_grid.data(), sizeof(cf) * n);
+  return 0;
+}
+
+// gridFFT_CoilThreaded::backward (E of C coils) or backward_residual (diff != NULL):
+// data[c] = E(X smap[c]) (- diff[c]), M samples each.
+int ref_coils_forward(int Nx, int Ny, int Nz, float overgrid, float dwin, int kernel_type, float k_rad, int C,
+                      const void *X, void *const *smaps, const float *kx, const float *ky, const float *kz,
+                      const float *kw, long M, void *const *data, void *const *diff) {
+  gridFFT_CoilThreaded g;
+  setup_coils(g, Config{overgrid, dwin, kernel_type, k_rad}, Nx, Ny, Nz, C);
+  Array<cf, 3> x = col3<cf>(Nx, Ny, Nz, X);
+  Complex4D s = coil_arrays(smaps, C, Nx, Ny, Nz), d = coil_arrays(nullptr, C, (int)M, 1, 1);
+  Traj t(kx, ky, kz, kw, M);
+  if (diff) {
+    Complex4D df = coil_arrays(diff, C, (int)M, 1, 1);
+    g.backward_residual(x, s, d, t.kx, t.ky, t.kz, t.kw, df);
+  } else {
+    g.backward(x, s, d, t.kx, t.ky, t.kz, t.kw);
+  }
+  for (int c = 0; c < C; c++) std::memcpy(data[c], d(c).data(), sizeof(cf) * (size_t)M);
+  return 0;
+}
+
+// gridFFT_CoilThreaded::forward (E^H of C coils with maps): X += sum_c E^H(data[c]) conj(smap[c]).
+int ref_coils_adjoint(int Nx, int Ny, int Nz, float overgrid, float dwin, int kernel_type, float k_rad, int C,
+                      void *X, void *const *smaps, void *const *data, const float *kx, const float *ky,
+                      const float *kz, const float *kw, long M) {
+  gridFFT_CoilThreaded g;
+  setup_coils(g, Config{overgrid, dwin, kernel_type, k_rad}, Nx, Ny, Nz, C);
+  Array<cf, 3> x = col3<cf>(Nx, Ny, Nz, X);
+  Complex4D s = coil_arrays(smaps, C, Nx, Ny, Nz), d = coil_arrays(data, C, (int)M, 1, 1);
+  Traj t(kx, ky, kz, kw, M);
+  g.forward(x, s, d, t.kx, t.ky, t.kz, t.kw);
+  std::memcpy(X, x.data(), sizeof(cf) * (size_t)Nx * Ny * Nz);
   return 0;
 }
 

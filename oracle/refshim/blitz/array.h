@@ -1,7 +1,8 @@
 // Stand-in for the parts of Blitz++ (blitz/array.h) that the reference's gridFFT.cpp,
-// ArrayTemplates.cpp, wavelet3D.cpp and threshold.cpp use, so that those files compile
-// unmodified into oracle/_ref (test infrastructure: the reference's own code, run as a
-// checker of the oracle restatement; Blitz++ itself is not installed here).
+// gridFFT_CoilThreaded.cpp, ArrayTemplates.cpp, wavelet3D.cpp, threshold.cpp and clear.cpp
+// use, so that those files compile unmodified into oracle/_ref (test infrastructure: the
+// reference's own code, run as a checker of the oracle restatement; Blitz++ itself is not
+// installed here).
 //
 // Written from Blitz's documented behaviour, not its source:
 //   * Array<T,N> is a strided view of a reference-counted block; the copy constructor
@@ -165,6 +166,17 @@ class Array {
   Array(const TinyVector<int, N> &s, ColumnMajorArray<N>) : Array() {
     colmajor_ = true;
     resize(s);
+  }
+  // extents followed by the column-major storage order
+  template <int M = N, typename = typename std::enable_if<M == 2>::type>
+  Array(int n0, int n1, ColumnMajorArray<2>) : Array() {
+    colmajor_ = true;
+    resize(n0, n1);
+  }
+  template <int M = N, typename = typename std::enable_if<M == 3>::type>
+  Array(int n0, int n1, int n2, ColumnMajorArray<3>) : Array() {
+    colmajor_ = true;
+    resize(n0, n1, n2);
   }
   // the copy constructor shares the data, as Blitz's does
   Array(const Array &o) = default;

@@ -5,6 +5,7 @@
 // several threads on different arrays (the reference calls fftwf_execute_dft that way).
 #include <cmath>
 #include <complex>
+#include <cstdlib>
 #include <vector>
 
 #include "fftw3.h"
@@ -116,6 +117,8 @@ fftwf_plan fftwf_plan_dft(int rank, const int *n, fftwf_complex *in, fftwf_compl
 void fftwf_execute(const fftwf_plan p) { transform(p, p->in, p->out); }
 void fftwf_execute_dft(const fftwf_plan p, fftwf_complex *in, fftwf_complex *out) { transform(p, in, out); }
 void fftwf_destroy_plan(fftwf_plan p) { delete p; }
+void *fftwf_malloc(size_t n) { return std::aligned_alloc(16, (n + 15) / 16 * 16); }
+void fftwf_free(void *p) { std::free(p); }
 int fftwf_import_wisdom_from_file(FILE *) { return 0; }
 void fftwf_export_wisdom_to_file(FILE *) {}
 int fftwf_init_threads(void) { return 1; }

@@ -54,9 +54,11 @@ int main(int argc, char **argv) {
       g.forward(lhs.data(), smaps.data() + c * n3, tmp.data(), kx.data(), ky.data(), kz.data(), kw.data(), M);
     }
     save(d + "/lhs_percoil.bin", lhs);
-    // coil-batched operator
+    // coil-batched operator with the reference class's defaults (overgrid 1.375,
+    // unnormalised FFTs: E and E^H sqrt(Sx Sy Sz) times gridFFT's)
     mrg_cxx::gridFFT_CoilThreaded gb;
     gb.precalc_gridding(N, N, N, C);
+    printf("coil-threaded: overgrid=%.3f S=%d %d %d\n", gb.overgrid, gb.Sx, gb.Sy, gb.Sz);
     std::vector<cf> y((size_t)C * M), lhs2(n3, cf(0, 0));
     gb.backward(X.data(), smaps.data(), y.data(), kx.data(), ky.data(), kz.data(), kw.data(), M);
     gb.forward(lhs2.data(), smaps.data(), y.data(), kx.data(), ky.data(), kz.data(), kw.data(), M);

@@ -86,3 +86,19 @@ def align_block_phases(got, ref, bs):
                 if abs(z) > 0:
                     out[sl] = ref[sl] * (z / abs(z))
     return out
+
+
+def aniso_case(N, C, nproj, seed):
+    """A multi-coil case on an anisotropic image N = (Nx, Ny, Nz): the radial trajectory of
+    the largest edge scaled to each axis's extent, random complex image, maps and k-space."""
+    Nx, Ny, Nz = N
+    m = max(N)
+    c = case(N=m, C=1, nproj=nproj, seed=seed)
+    rng = np.random.default_rng(seed)
+
+    def cz(*s):
+        return (rng.standard_normal(s) + 1j * rng.standard_normal(s)).astype(np.complex64)
+
+    return dict(kx=(c["kx"] * (Nx / m)).astype(np.float32), ky=(c["ky"] * (Ny / m)).astype(np.float32),
+                kz=(c["kz"] * (Nz / m)).astype(np.float32), kw=c["kw"].astype(np.float32), img=cz(Nz, Ny, Nx),
+                smaps=cz(C, Nz, Ny, Nx), data=cz(C, c["kx"].size))

@@ -30,11 +30,15 @@ def test_cxx_gridfft_dropin(mrg_lib, oracle_lib, tmp_path):
     assert "caught: mrg:" in r.stdout
     O = oracle_lib.Plan(N, prec=1)
     fr = [dict(kx=c["kx"], ky=c["ky"], kz=c["kz"], kw=c["kw"], data=c["data"])]
-    ref = O.normal(fr, c["smaps"], 0, c["X"])
     lhs1 = np.fromfile(tmp_path / "lhs_percoil.bin", np.complex64).reshape(N, N, N)
+    assert rel(lhs1, O.normal(fr, c["smaps"], 0, c["X"])) < 1e-5
+    # gridFFT_CoilThreaded: overgrid 1.375 by default (S = 48 at N = 32) and FFTs without the
+    # 1/sqrt(S) per axis, so E is sqrt(Sx Sy Sz) and E^H E Sx Sy Sz times gridFFT's
+    assert "coil-threaded: overgrid=1.375 S=48 48 48" in r.stdout
+    O2 = oracle_lib.Plan(N, overgrid=1.375, prec=1)
+    f = np.sqrt(float(np.prod(O2.gshape)))
     lhs2 = np.fromfile(tmp_path / "lhs_batched.bin", np.complex64).reshape(N, N, N)
-    assert rel(lhs1, ref) < 1e-5
-    assert rel(lhs2, ref) < 1e-5
+    assert rel(lhs2, f * f * O2.normal(fr, c["smaps"], 0, c["X"])) < 1e-5
     y = np.fromfile(tmp_path / "y_batched.bin", np.complex64).reshape(C, M)
-    refy = np.stack([O.forward(c["X"], c["smaps"][k], c["kx"], c["ky"], c["kz"], c["kw"]) for k in range(C)])
-    assert rel(y, refy) < 1e-5
+    refy = np.stack([O2.forward(c["X"], c["smaps"][k], c["kx"], c["ky"], c["kz"], c["kw"]) for k in range(C)])
+    assert rel(y, f * refy) < 1e-5

@@ -1,8 +1,9 @@
 """The CUDA path against outputs of the reference's own code.
 
 tests/golden/ref_ops.npz holds seeded inputs and the outputs of the reference's gridFFT
-(E, the residual E, E^H per coil), WAVELET3D and THRESHOLD, and tests/golden/ref_lowrank.npz
-those of LOWRANKCOIL in time and in the coil dimension, computed by the reference sources
+(E, the residual E, E^H per coil), WAVELET3D and THRESHOLD, tests/golden/ref_lowrank.npz
+those of LOWRANKCOIL in time and in the coil dimension, and tests/golden/ref_coils.npz those
+of gridFFT_CoilThreaded (its default overgrid 1.375, unnormalised FFTs), computed by the reference sources
 compiled unmodified (oracle/_ref; tests/golden/make_ref_golden.py).  The GPU runs the same
 inputs through the C ABI.  Bound: relative L2 <= 1e-5 per operator application (FP32 on
 both sides; summation orders differ), 1e-6 for the wavelet and threshold, 1e-5 for the
@@ -18,6 +19,7 @@ from tests.helpers import align_block_phases, rel
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_ops.npz")
 LOWRANK = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_lowrank.npz")
+COILS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_coils.npz")
 
 
 @pytest.fixture(scope="module")
@@ -28,6 +30,11 @@ def gold():
 @pytest.fixture(scope="module")
 def lowrank():
     return dict(np.load(LOWRANK))
+
+
+@pytest.fixture(scope="module")
+def coils():
+    return dict(np.load(COILS))
 
 
 def test_oracle_reproduces_the_reference_fixture(oracle_lib, gold):
@@ -141,3 +148,32 @@ def test_low_rank_blocks_match_reference_outputs(mrg_lib, lowrank):
     assert rel(Y, g["coil_out"].transpose(0, 2, 3, 4, 1)) < 1e-5
     im = mrg_lib.clear_combine(XX, (4, 4, 4))
     assert rel(im, align_block_phases(im, g["coil_combine"], (4, 4, 4))) < 1e-5
+
+
+def test_oracle_reproduces_the_coil_threaded_fixture(oracle_lib, coils):
+    """CPU: gridFFT_CoilThreaded's outputs (overgrid 1.375, 3 coils of 20 x 24 x 16) are the
+    oracle's gridFFT operators times sqrt(Sx Sy Sz), its transforms being unnormalised."""
+    g = coils
+    a = (g["kx"], g["ky"], g["kz"], g["kw"])
+    o = oracle_lib.Plan((20, 24, 16), overgrid=1.375)
+    f = np.sqrt(float(np.prod(o.gshape)))
+    E = np.stack([o.forward(g["img"], g["smaps"][k], *a) for k in range(3)])
+    assert rel(f * E, g["E"]) < 1e-6
+    EH = sum(o.adjoint(np.zeros(o.ishape, np.complex64), g["smaps"][k], g["data"][k], *a) for k in range(3))
+    assert rel(f * EH, g["EH"]) < 1e-6
+
+
+@pytest.mark.gpu
+def test_coil_threaded_plan_matches_reference_outputs(mrg_lib, coils):
+    """A plan with fft_norm = 1 at overgrid 1.375 (the gridFFT_CoilThreaded drop-in's
+    settings) against the reference class's E, residual E and E^H."""
+    import torch
+    g = coils
+    p = mrg_lib.Plan((20, 24, 16), 3, 1, overgrid=1.375, fft_norm=1)
+    p.set_traj(0, g["kx"], g["ky"], g["kz"], g["kw"])
+    p.set_smaps(torch.from_numpy(g["smaps"]).cuda())
+    img = torch.from_numpy(g["img"]).cuda()
+    assert rel(p.forward(0, img).cpu().numpy(), g["E"]) < 1e-5
+    assert rel(p.forward(0, img, diff=torch.from_numpy(g["data"]).cuda()).cpu().numpy(), g["E_resid"]) < 1e-5
+    X = p.adjoint(0, g["data"], np.zeros(p.ishape, np.complex64))
+    assert rel(X, g["EH"]) < 1e-5

@@ -15,7 +15,7 @@ import ctypes
 import numpy as np
 import pytest
 
-from tests.helpers import align_block_phases, case, edge_trajectory, low_rank_frames, rel
+from tests.helpers import align_block_phases, aniso_case, case, edge_trajectory, low_rank_frames, rel
 
 R = pytest.importorskip("oracle.ref")
 if not R.available():
@@ -225,3 +225,26 @@ def test_coil_low_rank_matches_reference(O, T, C, N, bs):
     im = O.clear_combine(XX, bs)
     assert rel(np.abs(im), np.abs(im_ref)) < TOL
     assert rel(im, align_block_phases(im, im_ref, bs)) < TOL
+
+
+@pytest.mark.parametrize("N,C,overgrid,kernel", [((20, 24, 16), 3, 1.375, 1), ((24, 24, 24), 2, 1.5, 1),
+                                                 ((16, 16, 24), 4, 1.5, 0), ((16, 16, 16), 2, 1.5, 3)])
+def test_coil_threaded_matches_oracle(O, N, C, overgrid, kernel):
+    """gridFFT_CoilThreaded::backward (E of every coil), backward_residual and forward (E^H
+    summed over the coils) (src/gridFFT_CoilThreaded.cpp:965-1120, its default overgrid
+    1.375 in the first case) equal the oracle's per-coil gridFFT operators times
+    sqrt(Sx Sy Sz): the class's FFTW transforms are unnormalised (:570-893) where gridFFT's
+    fft3 scales each axis by 1/sqrt(S)."""
+    c = aniso_case(N, C, 150, seed=50 + C)
+    a = (c["kx"], c["ky"], c["kz"], c["kw"])
+    g, o = R.Gridder(N, overgrid=overgrid, kernel=kernel), O.Plan(N, overgrid=overgrid, kernel=kernel)
+    f = np.sqrt(float(np.prod(g.S)))
+    E = np.stack([o.forward(c["img"], c["smaps"][k], *a) for k in range(C)])
+    assert rel(g.coils_forward(c["img"], c["smaps"], *a), f * E) < TOL
+    d = c["data"]
+    # residual: f E - d, and 0 at the samples with kw == 0 (src/gridFFT_CoilThreaded.cpp chop_grid_backward)
+    Er = np.stack([o.forward(c["img"], c["smaps"][k], *a, diff=(d[k] / np.float32(f)).astype(np.complex64))
+                   for k in range(C)])
+    assert rel(g.coils_forward(c["img"], c["smaps"], *a, diff=d), f * Er) < TOL
+    EH = sum(o.adjoint(np.zeros(o.ishape, np.complex64), c["smaps"][k], d[k], *a) for k in range(C))
+    assert rel(g.coils_adjoint(np.zeros(g.ishape, np.complex64), c["smaps"], d, *a), f * EH) < TOL
