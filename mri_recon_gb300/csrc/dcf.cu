@@ -4,7 +4,8 @@
 //   Kw2 = G^T X         (backward, :323-437)
 //   Kw  = |Kw2| < 1e-3 ? 0 : Kw / Kw2                              (:895-905)
 // for `iters` rounds, then Kw *= s^3 (scale_kw, :297-321) and Kw = |Kw|.
-// The grid has (int)(overgrid * N + 16) points per axis, centre S/2, no chop sign;
+// The grid has (int)(overgrid * N + 16) points per axis (x's extent from Nz and z's from
+// Nx, as recon_lib allocates it), centre S/2, no chop sign;
 // a sample's taps are ceil(dk - s*dwin) .. floor(dk + s*dwin) clipped to the grid,
 // s = |k|/128*(acc - 1) + 1 widening the kernel with |k|.
 //
@@ -163,7 +164,11 @@ void dcf_table(float dwin, int kernel, std::vector<float> &t) {
 mrg_status dcf_pipe(const float *kx, const float *ky, const float *kz, int64_t M, const int N[3], int iters,
                     float dwin, float scale, float overgrid, float acc, int kernel, float *kw, cudaStream_t st) {
   DcfGeo g;
-  for (int d = 0; d < 3; d++) g.S[d] = (int)(overgrid * N[d] + 16);
+  // RECON::dcf_calc allocates its image as (overgrid Nz + 16, overgrid Ny + 16, overgrid Nx
+  // + 16) in column-major order (src/recon_lib.cpp:873-875) and DCFgridFFT takes the first
+  // extent as Sx (src/DCFgridFFT.cpp:174-176, :325-327): x and z extents are swapped, which
+  // matters for anisotropic matrices only
+  for (int d = 0; d < 3; d++) g.S[d] = (int)(overgrid * N[2 - d] + 16);
   g.og = overgrid;
   g.dwin = dwin;
   g.acc = acc;

@@ -532,7 +532,8 @@ static void sos_normalize(cx<R> **A, int C, long n) {
 //   Kw = |Kw2| < 1e-3 ? 0 : Kw / Kw2,
 // then Kw *= scale^3 (scale_kw :297-321) and Kw = |Kw|.  G uses the polynomial
 // kernel table (loadKernelTable :47-66 / loadKernelTable2 :68-84, normalised to
-// sum 0.5*600 :150-152) on a real grid of (int)(overgrid*N + 16) points per axis,
+// sum 0.5*600 :150-152) on a real grid of (int)(overgrid*N + 16) points per axis (x's
+// extent from Nz and z's from Nx, as recon_lib allocates it),
 // without the chop sign, taps ceil(dk - s*dwin) .. floor(dk + s*dwin) clipped,
 // s = |k|/128*(acc - 1) + 1.
 // ---------------------------------------------------------------------------
@@ -594,8 +595,11 @@ static void dcf_pipe(const float *kx0, const float *ky0, const float *kz0, long 
                      float *kw_out) {
   std::vector<float> lut;
   dcf_table(q.dwin, q.kernel, lut);
+  // the image of RECON::dcf_calc is (overgrid Nz + 16, overgrid Ny + 16, overgrid Nx + 16)
+  // column-major (src/recon_lib.cpp:873-875), read by DCFgridFFT with its first extent as
+  // Sx (src/DCFgridFFT.cpp:174-176): the x and z extents are swapped
   int S[3];
-  for (int d = 0; d < 3; d++) S[d] = (int)(q.overgrid * N[d] + 16);
+  for (int d = 0; d < 3; d++) S[d] = (int)(q.overgrid * N[2 - d] + 16);
   std::vector<float> kx(M), ky(M), kz(M);
   for (long i = 0; i < M; i++) {
     kx[i] = kx0[i] * q.scale;

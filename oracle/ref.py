@@ -1,8 +1,8 @@
 """REFERENCE CHECKER -- TEST INFRASTRUCTURE ONLY.
 
 ctypes front end for ``oracle/_ref/libref.so``: the reference's own gridFFT.cpp,
-gridFFT_CoilThreaded.cpp, ArrayTemplates.cpp, wavelet3D.cpp, threshold.cpp and clear.cpp
-compiled unmodified (``make -C oracle ref``) against the stand-in Blitz++ / FFTW / Armadillo / HDF5 headers of
+gridFFT_CoilThreaded.cpp, DCFgridFFT.cpp, ArrayTemplates.cpp, wavelet3D.cpp, threshold.cpp
+and clear.cpp compiled unmodified (``make -C oracle ref``) against the stand-in Blitz++ / FFTW / Armadillo / HDF5 headers of
 ``oracle/refshim`` and driven by ``oracle/ref_driver.cpp``.  The tests use it to pin the
 oracle restatement (and, through committed fixtures, the CUDA path) to the reference's
 code.  It can only be built where the reference sources are present; ``available()``
@@ -56,6 +56,7 @@ def lib():
         pv = ctypes.POINTER(vp)
         L.ref_coils_forward.argtypes = geo + [f, i, vp, pv, fp, fp, fp, fp, l, pv, pv]
         L.ref_coils_adjoint.argtypes = geo + [f, i, vp, pv, pv, fp, fp, fp, fp, l]
+        L.ref_dcf_pipe.argtypes = [fp, fp, fp, l, i, i, i, i, f, f, f, f, i, fp]
         L.ref_llr_update_threshold.restype = ctypes.c_float
         L.ref_llr_update_threshold.argtypes = [pv, i, i, i, i, ip, f, f, i]
         L.ref_llr_thresh.argtypes = [pv, i, i, i, i, ip, i, f, f, l]
@@ -251,3 +252,15 @@ def clear_combine(XX, bs):
     assert lib().ref_clear_combine(_vols(_coil_vols(XX)), T, C, Nx, Ny, Nz, (ctypes.c_int * 3)(*bs),
                                    _vols([im[t] for t in range(T)])) == 0
     return im
+
+
+def dcf_pipe(kx, ky, kz, N, iters=20, dwin=2.1, scale=1.0, overgrid=2.1, acc=1.0, kernel=0):
+    """RECON::dcf_calc's Pipe iteration around the reference's DCFgridFFT; returns kw (float32)."""
+    if np.isscalar(N):
+        N = (N, N, N)
+    (kx, px), (ky, py), (kz, pz) = _f32(kx), _f32(ky), _f32(kz)
+    out = np.zeros(kx.size, np.float32)
+    assert lib().ref_dcf_pipe(px, py, pz, kx.size, N[0], N[1], N[2], int(iters), float(dwin), float(scale),
+                              float(overgrid), float(acc), int(kernel),
+                              out.ctypes.data_as(ctypes.POINTER(ctypes.c_float))) == 0
+    return out

@@ -1,7 +1,8 @@
-// C entry points over the reference's own gridFFT, gridFFT_CoilThreaded, WAVELET3D,
-// THRESHOLD and LOWRANKCOIL classes (src/gridFFT.cpp, src/gridFFT_CoilThreaded.cpp,
-// src/ArrayTemplates.cpp, src/wavelet3D.cpp, src/threshold.cpp, src/clear.cpp compiled
-// unmodified against the stand-in headers in refshim/), for checking the oracle
+// C entry points over the reference's own gridFFT, gridFFT_CoilThreaded, DCFgridFFT,
+// WAVELET3D, THRESHOLD and LOWRANKCOIL classes (src/gridFFT.cpp, src/gridFFT_CoilThreaded.cpp,
+// src/DCFgridFFT.cpp, src/ArrayTemplates.cpp, src/wavelet3D.cpp, src/threshold.cpp,
+// src/clear.cpp compiled unmodified against the stand-in headers in refshim/), for
+// checking the oracle
 // restatement against the reference itself.  Test infrastructure only: built into
 // oracle/_ref/libref.so by `make -C oracle ref` where the reference sources are present,
 // and loaded only by tests/test_oracle_ref.py.
@@ -15,6 +16,7 @@
 #include <cstring>
 #include <vector>
 
+#include "DCFgridFFT.h"
 #include "clear.h"
 #include "gridFFT.h"
 #include "gridFFT_CoilThreaded.h"
@@ -260,6 +262,47 @@ int ref_coils_adjoint(int Nx, int Ny, int Nz, float overgrid, float dwin, int ke
   Traj t(kx, ky, kz, kw, M);
   g.forward(x, s, d, t.kx, t.ky, t.kz, t.kw);
   std::memcpy(X, x.data(), sizeof(cf) * (size_t)Nx * Ny * Nz);
+  return 0;
+}
+
+// RECON::dcf_calc (src/recon_lib.cpp:855-912, which src/recon_lib.cpp cannot be compiled
+// here to provide) for one encode, around the reference's own DCFgridFFT: the gridder set
+// up as there, the trajectory scaled by `scale`, `iters` Pipe iterations from kw = 1
+// (kw <- kw / (grid then degrid of kw), 0 where that is below 1e-3), then scale_kw and the
+// magnitude.  kernel 0 is DCFgridFFT::POLY_KERNEL (recon_lib's choice), 1 POLY_KERNEL2.
+int ref_dcf_pipe(const float *kx, const float *ky, const float *kz, long M, int Nx, int Ny, int Nz, int iters,
+                 float dwin, float scale, float overgrid, float acc, int kernel, float *kw_out) {
+  DCFgridFFT dcf;
+  dcf.kernel_type = kernel;
+  dcf.dwinX = dcf.dwinY = dcf.dwinZ = dwin;
+  dcf.grid_x = dcf.grid_y = dcf.grid_z = overgrid;
+  dcf.grid_in_x = dcf.grid_in_y = dcf.grid_in_z = 1;
+  dcf.precalc_kernel();
+  dcf.acc = acc;
+  // the image's extents as the float expressions overgrid * N + 16 converted to int
+  Array<float, 3> X((int)(overgrid * Nz + 16), (int)(overgrid * Ny + 16), (int)(overgrid * Nx + 16),
+                    ColumnMajorArray<3>());
+  Array<float, 3> tx = col3<float>((int)M, 1, 1, kx), ty = col3<float>((int)M, 1, 1, ky),
+                  tz = col3<float>((int)M, 1, 1, kz);
+  tx *= scale;
+  ty *= scale;
+  tz *= scale;
+  Array<float, 3> w = col3<float>((int)M, 1, 1, nullptr), w2 = col3<float>((int)M, 1, 1, nullptr);
+  w = 1;
+  for (int it = 0; it < iters; it++) {
+    X = 0;
+    w2 = 0.0;
+    dcf.forward(X, w, tx, ty, tz);
+    dcf.backward(X, w2, tx, ty, tz);
+    for (long i = 0; i < M; i++) {
+      float &a = w(i, 0, 0);
+      const float b = w2(i, 0, 0);
+      if (std::abs(b) < 1e-3) a = 0.0f;
+      else a = a / b;
+    }
+  }
+  dcf.scale_kw(w, tx, ty, tz);
+  for (long i = 0; i < M; i++) kw_out[i] = std::abs(w(i, 0, 0));
   return 0;
 }
 

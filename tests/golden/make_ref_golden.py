@@ -8,8 +8,10 @@ sources:
                                 dimension (update_threshold, thresh, combine)
   tests/golden/ref_coils.npz    gridFFT_CoilThreaded at its default overgrid 1.375 (E, residual
                                 E, E^H over 3 coils of a 20 x 24 x 16 image)
+  tests/golden/ref_dcf.npz      the Pipe density compensation around DCFgridFFT (10 iterations,
+                                an isotropic 24^3 and an anisotropic 32 x 24 x 16 matrix)
 
-Run from the repository root: python tests/golden/make_ref_golden.py [ops] [lowrank] [coils]
+Run from the repository root: python tests/golden/make_ref_golden.py [ops] [lowrank] [coils] [dcf]
 (both when no argument is given).
 """
 import os
@@ -59,6 +61,19 @@ def coils():
     print(path, os.path.getsize(path), "bytes")
 
 
+def dcf():
+    out = {}
+    for key, N in (("iso", (24, 24, 24)), ("aniso", (32, 24, 16))):
+        m = max(N)
+        c = case(N=m, C=1, nproj=300, seed=401)
+        kx, ky, kz = (c[k] * np.float32(N[d] / m) for d, k in enumerate(("kx", "ky", "kz")))
+        out.update({key + "_kx": kx, key + "_ky": ky, key + "_kz": kz, key + "_N": np.array(N, np.int32)})
+        out[key + "_kw"] = R.dcf_pipe(kx, ky, kz, N, iters=10)
+    path = os.path.join(ROOT, "tests", "golden", "ref_dcf.npz")
+    np.savez_compressed(path, **out)
+    print(path, os.path.getsize(path), "bytes")
+
+
 def ops():
     out = {}
     # two coils, 24^3 image, 400 x 24 radial: E, E residual, E^H per coil
@@ -94,8 +109,8 @@ def ops():
 
 def main(which):
     assert R.available(), "oracle/_ref needs the reference sources"
-    for name in which or ("ops", "lowrank", "coils"):
-        {"ops": ops, "lowrank": lowrank, "coils": coils}[name]()
+    for name in which or ("ops", "lowrank", "coils", "dcf"):
+        {"ops": ops, "lowrank": lowrank, "coils": coils, "dcf": dcf}[name]()
 
 
 if __name__ == "__main__":

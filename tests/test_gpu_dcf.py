@@ -26,6 +26,20 @@ def test_dcf_matches_oracle(mrg_lib, oracle_lib, N, nproj, params):
     assert rel(got, ref64) < max(TOL, 1.25 * rel(ref32, ref64))
 
 
+def test_dcf_anisotropic_matrix(mrg_lib, oracle_lib):
+    """An anisotropic matrix: the grid's x extent comes from Nz and its z extent from Nx, as
+    recon_lib allocates the DCF image (src/recon_lib.cpp:873-875, read by DCFgridFFT as x
+    first); many samples then fall outside the grid and get weight 0."""
+    import torch
+    N = (40, 32, 24)
+    kx, ky, kz, _ = synth.radial_trajectory(40, 600, 40, seed=6)
+    kx, ky, kz = kx, (ky * 0.8).astype(np.float32), (kz * 0.6).astype(np.float32)
+    got = mrg_lib.dcf_pipe(*[torch.from_numpy(v).cuda() for v in (kx, ky, kz)], N, iters=10).cpu().numpy()
+    ref = oracle_lib.dcf_pipe(kx, ky, kz, N, iters=10)
+    assert rel(got, ref) < TOL
+    assert np.array_equal(got == 0, ref == 0) and (ref == 0).sum() > 0
+
+
 def test_dcf_host_arrays_and_edges(mrg_lib, oracle_lib):
     """numpy input, samples outside the grid (their weight goes to 0), default parameters."""
     N = 24

@@ -2,8 +2,9 @@
 
 tests/golden/ref_ops.npz holds seeded inputs and the outputs of the reference's gridFFT
 (E, the residual E, E^H per coil), WAVELET3D and THRESHOLD, tests/golden/ref_lowrank.npz
-those of LOWRANKCOIL in time and in the coil dimension, and tests/golden/ref_coils.npz those
-of gridFFT_CoilThreaded (its default overgrid 1.375, unnormalised FFTs), computed by the reference sources
+those of LOWRANKCOIL in time and in the coil dimension, tests/golden/ref_coils.npz those
+of gridFFT_CoilThreaded (its default overgrid 1.375, unnormalised FFTs), and
+tests/golden/ref_dcf.npz the Pipe density compensation around DCFgridFFT, computed by the reference sources
 compiled unmodified (oracle/_ref; tests/golden/make_ref_golden.py).  The GPU runs the same
 inputs through the C ABI.  Bound: relative L2 <= 1e-5 per operator application (FP32 on
 both sides; summation orders differ), 1e-6 for the wavelet and threshold, 1e-5 for the
@@ -20,6 +21,7 @@ from tests.helpers import align_block_phases, rel
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_ops.npz")
 LOWRANK = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_lowrank.npz")
 COILS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_coils.npz")
+DCF = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_dcf.npz")
 
 
 @pytest.fixture(scope="module")
@@ -35,6 +37,11 @@ def lowrank():
 @pytest.fixture(scope="module")
 def coils():
     return dict(np.load(COILS))
+
+
+@pytest.fixture(scope="module")
+def dcf():
+    return dict(np.load(DCF))
 
 
 def test_oracle_reproduces_the_reference_fixture(oracle_lib, gold):
@@ -177,3 +184,23 @@ def test_coil_threaded_plan_matches_reference_outputs(mrg_lib, coils):
     assert rel(p.forward(0, img, diff=torch.from_numpy(g["data"]).cuda()).cpu().numpy(), g["E_resid"]) < 1e-5
     X = p.adjoint(0, g["data"], np.zeros(p.ishape, np.complex64))
     assert rel(X, g["EH"]) < 1e-5
+
+
+def test_oracle_reproduces_the_dcf_fixture(oracle_lib, dcf):
+    """CPU: the oracle's Pipe density compensation gives the reference's weights (24^3 and the
+    anisotropic 32 x 24 x 16, whose DCF grid has x and z extents swapped as recon_lib's)."""
+    for key in ("iso", "aniso"):
+        N = tuple(int(v) for v in dcf[key + "_N"])
+        kw = oracle_lib.dcf_pipe(dcf[key + "_kx"], dcf[key + "_ky"], dcf[key + "_kz"], N, iters=10)
+        assert rel(kw, dcf[key + "_kw"]) < 1e-6
+
+
+@pytest.mark.gpu
+def test_dcf_matches_reference_outputs(mrg_lib, dcf):
+    """mrg_dcf_pipe on the fixture's trajectories against the reference's weights (the
+    gridding adds with atomics on both sides, so the sums' order differs)."""
+    for key in ("iso", "aniso"):
+        N = tuple(int(v) for v in dcf[key + "_N"])
+        kw = mrg_lib.dcf_pipe(dcf[key + "_kx"], dcf[key + "_ky"], dcf[key + "_kz"], N, iters=10)
+        assert rel(kw, dcf[key + "_kw"]) < 1e-5
+        assert np.array_equal(kw == 0, dcf[key + "_kw"] == 0)
