@@ -1,8 +1,8 @@
 """REFERENCE CHECKER -- TEST INFRASTRUCTURE ONLY.
 
 ctypes front end for ``oracle/_ref/libref.so``: the reference's own gridFFT.cpp,
-gridFFT_CoilThreaded.cpp, DCFgridFFT.cpp, ArrayTemplates.cpp, wavelet3D.cpp, threshold.cpp
-and clear.cpp compiled unmodified (``make -C oracle ref``) against the stand-in Blitz++ / FFTW / Armadillo / HDF5 headers of
+gridFFT_CoilThreaded.cpp, DCFgridFFT.cpp, ArrayTemplates.cpp, wavelet3D.cpp, threshold.cpp,
+clear.cpp and spirit.cpp compiled unmodified (``make -C oracle ref``) against the stand-in Blitz++ / FFTW / Armadillo / HDF5 headers of
 ``oracle/refshim`` and driven by ``oracle/ref_driver.cpp``.  The tests use it to pin the
 oracle restatement (and, through committed fixtures, the CUDA path) to the reference's
 code.  It can only be built where the reference sources are present; ``available()``
@@ -57,6 +57,7 @@ def lib():
         L.ref_coils_forward.argtypes = geo + [f, i, vp, pv, fp, fp, fp, fp, l, pv, pv]
         L.ref_coils_adjoint.argtypes = geo + [f, i, vp, pv, pv, fp, fp, fp, fp, l]
         L.ref_dcf_pipe.argtypes = [fp, fp, fp, l, i, i, i, i, f, f, f, f, i, fp]
+        L.ref_espirit.argtypes = [pv, i, i, i, i, fp, ip, f, i, pv]
         L.ref_llr_update_threshold.restype = ctypes.c_float
         L.ref_llr_update_threshold.argtypes = [pv, i, i, i, i, ip, f, f, i]
         L.ref_llr_thresh.argtypes = [pv, i, i, i, i, ip, i, f, f, l]
@@ -264,3 +265,15 @@ def dcf_pipe(kx, ky, kz, N, iters=20, dwin=2.1, scale=1.0, overgrid=2.1, acc=1.0
                               float(overgrid), float(acc), int(kernel),
                               out.ctypes.data_as(ctypes.POINTER(ctypes.c_float))) == 0
     return out
+
+
+def espirit(images, kr_f=(3.0, 3.0, 3.0), cr=(12, 12, 12), svd_thresh=0.01, square=False):
+    """SPIRIT::generateEigenCoils on coil images (C, Nz, Ny, Nx): the maps (C, Nz, Ny, Nx)
+    complex64."""
+    imgs = [_c64(x).copy() for x in images]
+    C = len(imgs)
+    Nz, Ny, Nx = imgs[0].shape
+    maps = np.zeros((C, Nz, Ny, Nx), np.complex64)
+    assert lib().ref_espirit(_ptrs(imgs), C, Nx, Ny, Nz, (ctypes.c_float * 3)(*kr_f), (ctypes.c_int * 3)(*cr),
+                             float(svd_thresh), int(bool(square)), _ptrs([maps[c] for c in range(C)])) == 0
+    return maps

@@ -1,8 +1,8 @@
 // C entry points over the reference's own gridFFT, gridFFT_CoilThreaded, DCFgridFFT,
-// WAVELET3D, THRESHOLD and LOWRANKCOIL classes (src/gridFFT.cpp, src/gridFFT_CoilThreaded.cpp,
-// src/DCFgridFFT.cpp, src/ArrayTemplates.cpp, src/wavelet3D.cpp, src/threshold.cpp,
-// src/clear.cpp compiled unmodified against the stand-in headers in refshim/), for
-// checking the oracle
+// WAVELET3D, THRESHOLD, LOWRANKCOIL and SPIRIT classes (src/gridFFT.cpp,
+// src/gridFFT_CoilThreaded.cpp, src/DCFgridFFT.cpp, src/ArrayTemplates.cpp,
+// src/wavelet3D.cpp, src/threshold.cpp, src/clear.cpp, src/spirit.cpp compiled unmodified
+// against the stand-in headers in refshim/), for checking the oracle
 // restatement against the reference itself.  Test infrastructure only: built into
 // oracle/_ref/libref.so by `make -C oracle ref` where the reference sources are present,
 // and loaded only by tests/test_oracle_ref.py.
@@ -20,6 +20,7 @@
 #include "clear.h"
 #include "gridFFT.h"
 #include "gridFFT_CoilThreaded.h"
+#include "spirit.h"
 #include "threshold.h"
 #include "wavelet3D.h"
 
@@ -303,6 +304,33 @@ int ref_dcf_pipe(const float *kx, const float *ky, const float *kz, long M, int 
   }
   dcf.scale_kw(w, tx, ty, tz);
   for (long i = 0; i < M; i++) kw_out[i] = std::abs(w(i, 0, 0));
+  return 0;
+}
+
+// SPIRIT::generateEigenCoils (src/spirit.cpp:137-172) as recon_lib calls it
+// (src/recon_lib.cpp:2895-2898): the kernel radii, calibration radii, singular-value
+// threshold and calibration shape set as read_commandline sets them from -sp_krx_f ..
+// -sp_square, init with the image size and coil count, then C coil images of one encode
+// (transformed in place) -> C maps.
+int ref_espirit(void *const *imgs, int C, int Nx, int Ny, int Nz, const float *kr_f, const int *cr,
+                float svd_thresh, int square, void *const *maps) {
+  SPIRIT sp;
+  sp.krx_f = kr_f[0];
+  sp.kry_f = kr_f[1];
+  sp.krz_f = kr_f[2];
+  sp.crx = cr[0];
+  sp.cry = cr[1];
+  sp.crz = cr[2];
+  sp.svd_thresh = svd_thresh;
+  sp.shape = square ? SP_SQUARE : SP_CIRCLE;
+  sp.init(Nx, Ny, Nz, C);
+  Array<Array<cf, 3>, 2> image;
+  image.setStorage(ColumnMajorArray<2>());
+  image.resize(1, C);
+  for (int c = 0; c < C; c++) image(0, c).reference(col3<cf>(Nx, Ny, Nz, imgs[c]));
+  Complex4D sm = coil_arrays(nullptr, C, Nx, Ny, Nz);
+  sp.generateEigenCoils(sm, image);
+  for (int c = 0; c < C; c++) std::memcpy(maps[c], sm(c).data(), sizeof(cf) * (size_t)Nx * Ny * Nz);
   return 0;
 }
 

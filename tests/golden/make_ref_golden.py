@@ -10,8 +10,11 @@ sources:
                                 E, E^H over 3 coils of a 20 x 24 x 16 image)
   tests/golden/ref_dcf.npz      the Pipe density compensation around DCFgridFFT (10 iterations,
                                 an isotropic 24^3 and an anisotropic 32 x 24 x 16 matrix)
+  tests/golden/ref_espirit.npz  SPIRIT::generateEigenCoils on 4 coil images of 16 x 12 x 10
+                                (anisotropic kernel and calibration radii)
 
-Run from the repository root: python tests/golden/make_ref_golden.py [ops] [lowrank] [coils] [dcf]
+Run from the repository root:
+  python tests/golden/make_ref_golden.py [ops] [lowrank] [coils] [dcf] [espirit]
 (both when no argument is given).
 """
 import os
@@ -74,6 +77,21 @@ def dcf():
     print(path, os.path.getsize(path), "bytes")
 
 
+def espirit():
+    from mri_recon_gb300 import synth
+    N, C = (16, 12, 10), 4
+    Nx, Ny, Nz = N
+    img = synth.phantom(16, 6, seed=7)[:Nz, :Ny, :Nx]
+    sm = synth.coil_maps(16, C, seed=8)[:, :Nz, :Ny, :Nx]
+    imgs = (img[None] * sm).astype(np.complex64)
+    kr, cr = (2.0, 1.5, 1.5), (6, 5, 4)
+    out = dict(imgs=imgs, kr=np.array(kr, np.float32), cr=np.array(cr, np.int32))
+    out["maps"] = R.espirit(imgs, kr, cr)
+    path = os.path.join(ROOT, "tests", "golden", "ref_espirit.npz")
+    np.savez_compressed(path, **out)
+    print(path, os.path.getsize(path), "bytes")
+
+
 def ops():
     out = {}
     # two coils, 24^3 image, 400 x 24 radial: E, E residual, E^H per coil
@@ -109,8 +127,8 @@ def ops():
 
 def main(which):
     assert R.available(), "oracle/_ref needs the reference sources"
-    for name in which or ("ops", "lowrank", "coils", "dcf"):
-        {"ops": ops, "lowrank": lowrank, "coils": coils, "dcf": dcf}[name]()
+    for name in which or ("ops", "lowrank", "coils", "dcf", "espirit"):
+        {"ops": ops, "lowrank": lowrank, "coils": coils, "dcf": dcf, "espirit": espirit}[name]()
 
 
 if __name__ == "__main__":

@@ -4,7 +4,8 @@ tests/golden/ref_ops.npz holds seeded inputs and the outputs of the reference's 
 (E, the residual E, E^H per coil), WAVELET3D and THRESHOLD, tests/golden/ref_lowrank.npz
 those of LOWRANKCOIL in time and in the coil dimension, tests/golden/ref_coils.npz those
 of gridFFT_CoilThreaded (its default overgrid 1.375, unnormalised FFTs), and
-tests/golden/ref_dcf.npz the Pipe density compensation around DCFgridFFT, computed by the reference sources
+tests/golden/ref_dcf.npz the Pipe density compensation around DCFgridFFT, and
+tests/golden/ref_espirit.npz SPIRIT's ESPIRiT maps, computed by the reference sources
 compiled unmodified (oracle/_ref; tests/golden/make_ref_golden.py).  The GPU runs the same
 inputs through the C ABI.  Bound: relative L2 <= 1e-5 per operator application (FP32 on
 both sides; summation orders differ), 1e-6 for the wavelet and threshold, 1e-5 for the
@@ -22,6 +23,7 @@ GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_o
 LOWRANK = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_lowrank.npz")
 COILS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_coils.npz")
 DCF = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_dcf.npz")
+ESPIRIT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_espirit.npz")
 
 
 @pytest.fixture(scope="module")
@@ -42,6 +44,11 @@ def coils():
 @pytest.fixture(scope="module")
 def dcf():
     return dict(np.load(DCF))
+
+
+@pytest.fixture(scope="module")
+def espirit():
+    return dict(np.load(ESPIRIT))
 
 
 def test_oracle_reproduces_the_reference_fixture(oracle_lib, gold):
@@ -204,3 +211,33 @@ def test_dcf_matches_reference_outputs(mrg_lib, dcf):
         kw = mrg_lib.dcf_pipe(dcf[key + "_kx"], dcf[key + "_ky"], dcf[key + "_kz"], N, iters=10)
         assert rel(kw, dcf[key + "_kw"]) < 1e-5
         assert np.array_equal(kw == 0, dcf[key + "_kw"] == 0)
+
+
+def _espirit_defined(oracle_lib, g):
+    """Voxels whose dominant vector is well defined ((s2/s1)^2 < 0.9 by the oracle)."""
+    _, _, _, ratio = oracle_lib.espirit(g["imgs"], kr_f=tuple(float(v) for v in g["kr"]),
+                                        cr=tuple(int(v) for v in g["cr"]))
+    return ratio < 0.9
+
+
+def test_oracle_reproduces_the_espirit_fixture(oracle_lib, espirit):
+    """CPU: the oracle's ESPIRiT maps against SPIRIT::generateEigenCoils's (16 x 12 x 10, 4 coils)."""
+    g = espirit
+    m = _espirit_defined(oracle_lib, g)
+    maps, _, _, _ = oracle_lib.espirit(g["imgs"], kr_f=tuple(float(v) for v in g["kr"]),
+                                       cr=tuple(int(v) for v in g["cr"]))
+    assert m.mean() > 0.5
+    assert rel(maps[:, m], g["maps"][:, m]) < 1e-6
+
+
+@pytest.mark.gpu
+def test_espirit_matches_reference_outputs(mrg_lib, oracle_lib, espirit):
+    """mrg_espirit on the fixture's coil images against SPIRIT's maps where the dominant
+    vector is well defined (1e-4, the bound of the GPU tests against the FP64 oracle)."""
+    g = espirit
+    m = _espirit_defined(oracle_lib, g)
+    p = mrg_lib.espirit_params(kernel_radius=tuple(float(v) for v in g["kr"]), calib_radius=tuple(int(v) for v in g["cr"]),
+                               square=0)
+    maps, kept, _ = mrg_lib.espirit(np.ascontiguousarray(np.moveaxis(g["imgs"], 0, -1)), p)
+    got = np.moveaxis(np.asarray(maps), -1, 0)
+    assert rel(got[:, m], g["maps"][:, m]) < 1e-4
