@@ -306,6 +306,20 @@ def test_fft3_against_cufft(mrg_lib, N, sign):
     assert e64 < max(1e-6, 2 * e32), (e64, e32)
 
 
+@pytest.mark.parametrize("sign", [-1, 1])
+def test_fft3_unnormalised_plan(mrg_lib, sign):
+    """mrg_fft3 on a plan with fft_norm = 1 (gridFFT_CoilThreaded's FFTW transforms) is
+    sqrt(Sx Sy Sz) times the normalised transform of fft_norm = 0."""
+    torch = _torch()
+    N, C = (40, 32, 24), 2
+    p0, p1 = mrg_lib.Plan(N, C, 1), mrg_lib.Plan(N, C, 1, fft_norm=1)
+    Sx, Sy, Sz = p0.S
+    g = torch.randn((Sz, Sy, Sx, C), dtype=torch.complex64, device="cuda", generator=torch.Generator("cuda").manual_seed(5))
+    want = p0.fft3(g.clone(), sign) * float(np.sqrt(float(Sx * Sy * Sz)))
+    got = p1.fft3(g.clone(), sign)
+    assert float(torch.linalg.norm(got - want) / torch.linalg.norm(want)) < 1e-6
+
+
 @pytest.mark.parametrize("kernel,overgrid,dwin,N,C", [(1, 1.5, -1.0, 32, 4), (0, 1.0, 1.0, 32, 2), (1, 1.5, -1.0, 24, 8)])
 def test_grid_and_ungrid_on_a_caller_grid(mrg_lib, oracle_lib, kernel, overgrid, dwin, N, C):
     """chop_grid_forward / chop_grid_backward on a caller grid (mrg_grid / mrg_ungrid), per
