@@ -54,6 +54,7 @@ def lib():
         L.ref_fraction_threshold.restype = ctypes.c_float
         L.ref_fraction_threshold.argtypes = [i, i, i, i, ctypes.POINTER(vp), f, i]
         pv = ctypes.POINTER(vp)
+        L.ref_adjoint_sos.argtypes = geo + [f, vp, vp, fp, fp, fp, fp, l]
         L.ref_coils_forward.argtypes = geo + [f, i, vp, pv, fp, fp, fp, fp, l, pv, pv]
         L.ref_coils_adjoint.argtypes = geo + [f, i, vp, pv, pv, fp, fp, fp, fp, l]
         L.ref_dcf_pipe.argtypes = [fp, fp, fp, l, i, i, i, i, f, f, f, f, i, fp]
@@ -151,6 +152,13 @@ class Gridder:
         out = np.zeros(kx.size, np.complex64)
         assert lib().ref_ungrid(*self.geo, _p(grid), px, py, pz, pw, kx.size, _p(out), _p(diff)) == 0
         return out
+
+    def adjoint_sos(self, X, data, kx, ky, kz, kw):
+        """gridFFT::forward_sos: X += |deapodised E^H data|^2 (the map-free coil image)."""
+        X, data = _c64(X).copy(), _c64(data)
+        (kx, px), (ky, py), (kz, pz), (kw, pw) = _f32(kx), _f32(ky), _f32(kz), _f32(kw)
+        assert lib().ref_adjoint_sos(*self.geo, self.k_rad, _p(X), _p(data), px, py, pz, pw, kx.size) == 0
+        return X
 
     def coils_forward(self, X, smaps, kx, ky, kz, kw, diff=None):
         """gridFFT_CoilThreaded::backward (E of every coil of smaps (C, Nz, Ny, Nx)), or

@@ -232,6 +232,18 @@ int ref_fft(int Nx, int Ny, int Nz, float overgrid, int inverse, void *grid) {
   return 0;
 }
 
+// gridFFT::forward_sos (src/gridFFT.cpp:722-748): X += |E^H data, deapodised|^2, X read and written.
+int ref_adjoint_sos(int Nx, int Ny, int Nz, float overgrid, float dwin, int kernel_type, float k_rad, void *X,
+                    const void *data, const float *kx, const float *ky, const float *kz, const float *kw, long M) {
+  gridFFT g;
+  setup(g, Config{overgrid, dwin, kernel_type, k_rad}, Nx, Ny, Nz);
+  Array<cf, 3> x = col3<cf>(Nx, Ny, Nz, X), d = col3<cf>((int)M, 1, 1, data);
+  Traj t(kx, ky, kz, kw, M);
+  g.forward_sos(x, d, t.kx, t.ky, t.kz, t.kw);
+  std::memcpy(X, x.data(), sizeof(cf) * (size_t)Nx * Ny * Nz);
+  return 0;
+}
+
 // gridFFT_CoilThreaded::backward (E of C coils) or backward_residual (diff != NULL):
 // data[c] = E(X smap[c]) (- diff[c]), M samples each.
 int ref_coils_forward(int Nx, int Ny, int Nz, float overgrid, float dwin, int kernel_type, float k_rad, int C,

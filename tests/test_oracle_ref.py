@@ -138,6 +138,20 @@ def test_anisotropic_operators_match_reference(O, N, overgrid, kernel, dwin):
         assert rel(o.adjoint(X0.copy(), sm, d, *a), g.adjoint(X0, sm, d, *a)) < TOL
 
 
+def test_sum_of_squares_adjoint_matches_reference(O):
+    """gridFFT::forward_sos (the map-free E^H whose squared magnitude is summed over coils,
+    src/gridFFT.cpp:722-748, :960-970), three coils accumulated into one image, with a taper."""
+    c = aniso_case((32, 24, 20), 3, 400, seed=61)
+    a = (c["kx"], c["ky"], c["kz"], c["kw"])
+    g, o = R.Gridder((32, 24, 20), k_rad=10.0), O.Plan((32, 24, 20), k_rad=10.0)
+    Xr = np.zeros(g.ishape, np.complex64)
+    Xo = np.zeros(o.ishape, np.complex64)
+    for k in range(3):
+        Xr = g.adjoint_sos(Xr, c["data"][k], *a)
+        Xo = o.adjoint_sos(Xo, c["data"][k], *a)
+    assert rel(Xo, Xr) < TOL
+
+
 def test_taper_radius_matches_reference(O):
     """E^H with the Gaussian taper of a small k_rad (the coil-map estimate's smap_res)."""
     c, a = _traj(32, 800, seed=10)
