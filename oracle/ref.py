@@ -55,6 +55,7 @@ def lib():
         L.ref_fraction_threshold.argtypes = [i, i, i, i, ctypes.POINTER(vp), f, i]
         pv = ctypes.POINTER(vp)
         L.ref_adjoint_sos.argtypes = geo + [f, vp, vp, fp, fp, fp, fp, l]
+        L.ref_gaussian_blur.argtypes = [vp, i, i, i, fp]
         L.ref_coils_forward.argtypes = geo + [f, i, vp, pv, fp, fp, fp, fp, l, pv, pv]
         L.ref_coils_adjoint.argtypes = geo + [f, i, vp, pv, pv, fp, fp, fp, fp, l]
         L.ref_dcf_pipe.argtypes = [fp, fp, fp, l, i, i, i, i, f, f, f, f, i, fp]
@@ -285,3 +286,11 @@ def espirit(images, kr_f=(3.0, 3.0, 3.0), cr=(12, 12, 12), svd_thresh=0.01, squa
     assert lib().ref_espirit(_ptrs(imgs), C, Nx, Ny, Nz, (ctypes.c_float * 3)(*kr_f), (ctypes.c_int * 3)(*cr),
                              float(svd_thresh), int(bool(square)), _ptrs([maps[c] for c in range(C)])) == 0
     return maps
+
+
+def gaussian_blur(X, sigma):
+    """NDarray::gaussian_blur of one (Nz, Ny, Nx) complex volume (a copy), sigma = (x, y, z)."""
+    X = _c64(X).copy()
+    Nz, Ny, Nx = X.shape
+    assert lib().ref_gaussian_blur(_p(X), Nx, Ny, Nz, (ctypes.c_float * 3)(*[float(v) for v in sigma])) == 0
+    return X

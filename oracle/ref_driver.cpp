@@ -346,6 +346,15 @@ int ref_espirit(void *const *imgs, int C, int Nx, int Ny, int Nz, const float *k
   return 0;
 }
 
+// NDarray::gaussian_blur (src/ArrayTemplates.cpp:489-608) of one complex volume in place,
+// sigma per axis (x, y, z).
+int ref_gaussian_blur(void *X, int Nx, int Ny, int Nz, const float *sigma) {
+  Array<cf, 3> x = col3<cf>(Nx, Ny, Nz, X);
+  gaussian_blur(x, sigma[0], sigma[1], sigma[2]);
+  std::memcpy(X, x.data(), sizeof(cf) * (size_t)Nx * Ny * Nz);
+  return 0;
+}
+
 // WAVELET3D forward (inverse = 0) or backward of one volume in place, with the shifts S set
 // as random_shift would have set them.
 int ref_wavelet(int Nx, int Ny, int Nz, const int *levels, const int *shift, int wave_type, int inverse, void *X) {

@@ -319,3 +319,14 @@ def test_espirit_matches_reference(O, N, C, kr, cr, square):
     m = ratio < 0.9
     assert m.mean() > 0.5
     assert rel(o[:, m], r[:, m]) < TOL
+
+
+@pytest.mark.parametrize("shape,sigma", [((16, 20, 24), (1.0, 1.0, 1.0)), ((12, 16, 20), (0.5, 2.0, 0.0)),
+                                         ((20, 12, 16), (3.0, 0.7, 1.3))])
+def test_gaussian_blur_matches_reference(O, shape, sigma):
+    """NDarray::gaussian_blur (src/ArrayTemplates.cpp:489-608: taps [max(i - w, 0),
+    min(i + w, n)) with w = (int)(5 sigma), normalised by their sum, an axis with sigma 0
+    skipped), the blur of the low-resolution coil-map estimate."""
+    rng = np.random.default_rng(62)
+    X = (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)).astype(np.complex64)
+    assert rel(O.gaussian_blur(X, sigma), R.gaussian_blur(X, sigma)) < TOL
