@@ -84,6 +84,13 @@ def test_errors_are_reported_not_fatal(mrg_lib):
     cfg = MrgConfig()
     L.mrg_config_default(ctypes.byref(cfg))
     assert abs(cfg.overgrid - 1.5) < 1e-7 and cfg.kernel_type == 1 and abs(cfg.k_rad - 9999.0) < 1e-3
+    assert cfg.fft_norm == 0  # gridFFT's normalised transforms unless asked
+    for field, bad in (("fft_norm", 2), ("fft_norm", -1), ("grid_mode", 4), ("kernel_type", 5)):
+        c2 = MrgConfig()
+        L.mrg_config_default(ctypes.byref(c2))
+        setattr(c2, field, bad)
+        assert L.mrg_plan_create(ctypes.byref(c2), 32, 32, 32, 1, 1, ctypes.byref(h)) == 1, field
+        assert b"bad config" in L.mrg_last_error()
 
 
 def test_loop_parameter_defaults_are_the_references(mrg_lib):
