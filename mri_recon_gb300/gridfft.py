@@ -1,7 +1,9 @@
 """Python mirror of the reference's gridFFT / RECON call surface over libmrg.
 
 ``Plan`` is the coil-batched operator (the reference's gridFFT_CoilThreaded plus
-the CG / FISTA loops of RECON::full_recon).  ``gridFFT`` keeps the per-coil
+the CG / FISTA loops of RECON::full_recon); by default its transforms are normalised as
+gridFFT's, and ``fft_norm=1`` with ``overgrid=1.375`` gives gridFFT_CoilThreaded's own
+unnormalised transforms and default grid.  ``gridFFT`` keeps the per-coil
 member functions and public fields of the reference class
 (src/gridFFT.h:28-194) so code written against it ports line for line:
 
@@ -64,7 +66,9 @@ def _numel(a):
 
 
 class Plan:
-    """Coil-batched gridFFT plan with ``ncoils`` coils and ``nframes`` trajectories."""
+    """Coil-batched gridFFT plan with ``ncoils`` coils and ``nframes`` trajectories.
+    fft_norm=1: unnormalised FFT passes (gridFFT_CoilThreaded), E and E^H sqrt(Sx Sy Sz)
+    times those of the default."""
 
     def __init__(self, N, ncoils=1, nframes=1, overgrid=1.5, dwin=-1.0, kernel_type=KAISER_KERNEL, k_rad=9999.0,
                  tile=0, max_pairs=0, time_grid=0, analytic_kernel=False, grid_mode=0, fft_norm=0):
