@@ -56,6 +56,7 @@ def lib():
         pv = ctypes.POINTER(vp)
         L.ref_adjoint_sos.argtypes = geo + [f, vp, vp, fp, fp, fp, fp, l]
         L.ref_gaussian_blur.argtypes = [vp, i, i, i, fp]
+        L.ref_wavelet_shifts.argtypes = [i, i, i, ip, i, l, i, ip]
         L.ref_coils_forward.argtypes = geo + [f, i, vp, pv, fp, fp, fp, fp, l, pv, pv]
         L.ref_coils_adjoint.argtypes = geo + [f, i, vp, pv, pv, fp, fp, fp, fp, l]
         L.ref_dcf_pipe.argtypes = [fp, fp, fp, l, i, i, i, i, f, f, f, f, i, fp]
@@ -294,3 +295,11 @@ def gaussian_blur(X, sigma):
     Nz, Ny, Nx = X.shape
     assert lib().ref_gaussian_blur(_p(X), Nx, Ny, Nz, (ctypes.c_float * 3)(*[float(v) for v in sigma])) == 0
     return X
+
+
+def wavelet_shifts(shape_xyz, levels, wtype, skip, n):
+    """WAVELET3D::random_shift called n times after srand(1) and `skip` draws: (n, 3) shifts."""
+    out = (ctypes.c_int * (3 * n))()
+    assert lib().ref_wavelet_shifts(*[int(v) for v in shape_xyz], (ctypes.c_int * 3)(*levels), int(wtype), int(skip),
+                                    int(n), out) == 0
+    return np.array(out[:], dtype=np.int64).reshape(n, 3)

@@ -368,6 +368,21 @@ int ref_wavelet(int Nx, int Ny, int Nz, const int *levels, const int *shift, int
   return 0;
 }
 
+// WAVELET3D::random_shift (src/wavelet3D.cpp:443-448) called n times on a transform of
+// the given type and shape, rand() seeded with srand(1) and advanced `skip` draws: the
+// shifts (x, y, z) of each call into S (3n ints), as L1_threshold's cycle spins draw them.
+int ref_wavelet_shifts(int Nx, int Ny, int Nz, const int *levels, int wave_type, long skip, int n, int *S) {
+  Array<cf, 3> x = col3<cf>(Nx, Ny, Nz, nullptr);
+  int l[3] = {levels[0], levels[1], levels[2]};
+  WAVELET3D w(x, l, wave_type);
+  seed_rand(skip);
+  for (int i = 0; i < n; i++) {
+    w.random_shift();
+    for (int d = 0; d < 3; d++) S[3 * i + d] = w.S[d];
+  }
+  return 0;
+}
+
 // THRESHOLD with -threshold_type fraction -thresh <fraction>: update_threshold over nvol
 // volumes (frames) gives global_threshold; with apply != 0 exec_threshold then soft
 // thresholds the volumes in place.  Returns the threshold.

@@ -330,3 +330,17 @@ def test_gaussian_blur_matches_reference(O, shape, sigma):
     rng = np.random.default_rng(62)
     X = (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)).astype(np.complex64)
     assert rel(O.gaussian_blur(X, sigma), R.gaussian_blur(X, sigma)) < TOL
+
+
+@pytest.mark.parametrize("wtype", [0, 1])
+@pytest.mark.parametrize("skip", [0, 7, 1000])
+def test_cycle_spin_shifts_match_reference(mrg_lib, wtype, skip):
+    """The wavelet shifts of L1_threshold's cycle spins: WAVELET3D::random_shift's rand() % wN
+    (src/wavelet3D.cpp:443-448, wN 2 for DB2 and 4 for DB4 from its constructor) against the
+    library's host stream (mrg_rand_stream) taken modulo the same wN."""
+    n = 40
+    ref = R.wavelet_shifts((32, 24, 16), (3, 3, 3), wtype, skip, n)
+    out = (ctypes.c_int * (3 * n))()
+    assert mrg_lib.load().mrg_rand_stream(skip, 3 * n, out) == 0
+    wN = 2 if wtype == 0 else 4
+    assert np.array_equal(np.array(out[:]).reshape(n, 3) % wN, ref)
