@@ -57,6 +57,7 @@ def lib():
         L.ref_adjoint_sos.argtypes = geo + [f, vp, vp, fp, fp, fp, fp, l]
         L.ref_gaussian_blur.argtypes = [vp, i, i, i, fp]
         L.ref_wavelet_shifts.argtypes = [i, i, i, ip, i, l, i, ip]
+        L.ref_dcf_table.argtypes = [f, i, fp, ip]
         L.ref_coils_forward.argtypes = geo + [f, i, vp, pv, fp, fp, fp, fp, l, pv, pv]
         L.ref_coils_adjoint.argtypes = geo + [f, i, vp, pv, pv, fp, fp, fp, fp, l]
         L.ref_dcf_pipe.argtypes = [fp, fp, fp, l, i, i, i, i, f, f, f, f, i, fp]
@@ -303,3 +304,13 @@ def wavelet_shifts(shape_xyz, levels, wtype, skip, n):
     assert lib().ref_wavelet_shifts(*[int(v) for v in shape_xyz], (ctypes.c_int * 3)(*levels), int(wtype), int(skip),
                                     int(n), out) == 0
     return np.array(out[:], dtype=np.int64).reshape(n, 3)
+
+
+def dcf_table(dwin=2.1, kernel=0):
+    """DCFgridFFT::precalc_kernel's normalised polynomial table (float32)."""
+    n = ctypes.c_int()
+    assert lib().ref_dcf_table(float(dwin), int(kernel), None, ctypes.byref(n)) == 0
+    out = np.zeros(n.value, np.float32)
+    assert lib().ref_dcf_table(float(dwin), int(kernel), out.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                               ctypes.byref(n)) == 0
+    return out

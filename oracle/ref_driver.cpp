@@ -278,6 +278,20 @@ int ref_coils_adjoint(int Nx, int Ny, int Nz, float overgrid, float dwin, int ke
   return 0;
 }
 
+// DCFgridFFT::precalc_kernel's table (src/DCFgridFFT.cpp:54-164) for the half width
+// dwin and the kernel (0 POLY_KERNEL, 1 POLY_KERNEL2): *len entries into out (NULL: the
+// length only).
+int ref_dcf_table(float dwin, int kernel, float *out, int *len) {
+  DCFgridFFT dcf;
+  dcf.kernel_type = kernel;
+  dcf.dwinX = dcf.dwinY = dcf.dwinZ = dwin;
+  dcf.precalc_kernel();
+  *len = (int)dcf.grid_filterX.numElements();
+  if (out)
+    for (int i = 0; i < *len; i++) out[i] = dcf.grid_filterX(i);
+  return 0;
+}
+
 // RECON::dcf_calc (src/recon_lib.cpp:855-912, which src/recon_lib.cpp cannot be compiled
 // here to provide) for one encode, around the reference's own DCFgridFFT: the gridder set
 // up as there, the trajectory scaled by `scale`, `iters` Pipe iterations from kw = 1

@@ -282,6 +282,14 @@ def test_coil_threaded_matches_oracle(O, N, C, overgrid, kernel):
     assert rel(g.coils_adjoint(np.zeros(g.ishape, np.complex64), c["smaps"], d, *a), f * EH) < TOL
 
 
+@pytest.mark.parametrize("kernel", [0, 1])
+@pytest.mark.parametrize("dwin", [2.1, 1.8, 2.5, 3.0])
+def test_dcf_table_equals_reference(O, kernel, dwin):
+    """DCFgridFFT::precalc_kernel's polynomial table (POLY_KERNEL, POLY_KERNEL2), its length
+    (int)(dwin * 600) + 100 and its normalisation to sum 300, bit for bit."""
+    assert np.array_equal(O.dcf_table(dwin, kernel), R.dcf_table(dwin, kernel))
+
+
 @pytest.mark.parametrize("N,params", [(32, dict()), (48, dict(iters=5, dwin=2.5, overgrid=2.0)),
                                       (40, dict(kernel=1, acc=1.5, scale=0.9)),
                                       ((40, 32, 24), dict(iters=10)), ((24, 32, 40), dict(kernel=1, acc=1.5))])
