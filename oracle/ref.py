@@ -45,6 +45,7 @@ def lib():
         ip, fp = ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_float)
         geo = [i, i, i, f, f, i]
         L.ref_tables.argtypes = geo + [ip, ip, fp, ip, fp, fp]
+        L.ref_coils_tables.argtypes = geo + [i, ip, ip, fp, ip, fp, fp]
         L.ref_forward.argtypes = geo + [f, vp, vp, fp, fp, fp, fp, l, vp, vp]
         L.ref_adjoint.argtypes = geo + [f, vp, vp, vp, fp, fp, fp, fp, l]
         L.ref_grid.argtypes = geo + [f, vp, fp, fp, fp, fp, l, vp]
@@ -162,6 +163,18 @@ class Gridder:
         (kx, px), (ky, py), (kz, pz), (kw, pw) = _f32(kx), _f32(ky), _f32(kz), _f32(kw)
         assert lib().ref_adjoint_sos(*self.geo, self.k_rad, _p(X), _p(data), px, py, pz, pw, kx.size) == 0
         return X
+
+    def coils_tables(self, C=2):
+        """S, og, beta, kernel tables and windows from gridFFT_CoilThreaded::precalc_gridding."""
+        S, og, ll = (ctypes.c_int * 3)(), (ctypes.c_int * 3)(), ctypes.c_int()
+        be = (ctypes.c_float * 3)()
+        fp = ctypes.POINTER(ctypes.c_float)
+        assert lib().ref_coils_tables(*self.geo, C, S, og, be, ctypes.byref(ll), None, None) == 0
+        lut = np.zeros(3 * ll.value, np.float32)
+        win = np.zeros(sum(S), np.float32)
+        assert lib().ref_coils_tables(*self.geo, C, S, og, be, ctypes.byref(ll), lut.ctypes.data_as(fp),
+                                      win.ctypes.data_as(fp)) == 0
+        return tuple(S), tuple(og), tuple(be), lut.reshape(3, -1), win
 
     def coils_forward(self, X, smaps, kx, ky, kz, kw, diff=None):
         """gridFFT_CoilThreaded::backward (E of every coil of smaps (C, Nz, Ny, Nx)), or

@@ -133,16 +133,9 @@ struct Traj {
         kw(col3<float>((int)M, 1, 1, w)) {}
 };
 
-}  // namespace
-
-extern "C" {
-
-// precalc_gridding: S, og_s, beta, the kernel tables grid_filterX/Y/Z (lut_len each, lut may
-// be NULL) and the windows winx/winy/winz (Sx + Sy + Sz floats, may be NULL).
-int ref_tables(int Nx, int Ny, int Nz, float overgrid, float dwin, int kernel_type, int *S, int *og, float *beta,
-               int *lut_len, float *lut, float *win) {
-  gridFFT g;
-  setup(g, Config{overgrid, dwin, kernel_type, 9999.0f}, Nx, Ny, Nz);
+// S, og_s, beta, kernel tables and windows of a gridder after precalc_gridding
+template <class G>
+int copy_tables(const G &g, int *S, int *og, float *beta, int *lut_len, float *lut, float *win) {
   S[0] = g.Sx, S[1] = g.Sy, S[2] = g.Sz;
   og[0] = g.og_sx, og[1] = g.og_sy, og[2] = g.og_sz;
   beta[0] = g.betaX, beta[1] = g.betaY, beta[2] = g.betaZ;
@@ -160,6 +153,28 @@ int ref_tables(int Nx, int Ny, int Nz, float overgrid, float dwin, int kernel_ty
     for (int i = 0; i < g.Sz; i++) win[o++] = g.winz(i);
   }
   return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+// precalc_gridding: S, og_s, beta, the kernel tables grid_filterX/Y/Z (lut_len each, lut may
+// be NULL) and the windows winx/winy/winz (Sx + Sy + Sz floats, may be NULL).
+int ref_tables(int Nx, int Ny, int Nz, float overgrid, float dwin, int kernel_type, int *S, int *og, float *beta,
+               int *lut_len, float *lut, float *win) {
+  gridFFT g;
+  setup(g, Config{overgrid, dwin, kernel_type, 9999.0f}, Nx, Ny, Nz);
+  return copy_tables(g, S, og, beta, lut_len, lut, win);
+}
+
+// The same from gridFFT_CoilThreaded::precalc_gridding (src/gridFFT_CoilThreaded.cpp:403-568)
+// for C coils.
+int ref_coils_tables(int Nx, int Ny, int Nz, float overgrid, float dwin, int kernel_type, int C, int *S, int *og,
+                     float *beta, int *lut_len, float *lut, float *win) {
+  gridFFT_CoilThreaded g;
+  setup_coils(g, Config{overgrid, dwin, kernel_type, 9999.0f}, Nx, Ny, Nz, C);
+  return copy_tables(g, S, og, beta, lut_len, lut, win);
 }
 
 // gridFFT::backward (E) or backward_residual (diff != NULL): data = E(X smap) (- diff).

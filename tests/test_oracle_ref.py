@@ -64,6 +64,18 @@ def test_tables_equal_reference(O, mrg_lib, kernel, N, overgrid):
     assert np.array_equal(mwin, np.concatenate(g.win))
 
 
+@pytest.mark.parametrize("kernel", [1, 0, 2, 3])
+@pytest.mark.parametrize("N,overgrid", [(32, 1.375), (64, 1.5), ((40, 48, 24), 1.375), (32, 2.0)])
+def test_coil_threaded_tables_equal_gridfft(kernel, N, overgrid):
+    """gridFFT_CoilThreaded::precalc_gridding builds the same S, crop, beta, kernel tables and
+    windows as gridFFT::precalc_gridding, bit for bit (so a plan's tables serve both)."""
+    g = R.Gridder(N, overgrid=overgrid, kernel=kernel)
+    S, og, be, lut, win = g.coils_tables(C=3)
+    assert S == g.S and og == g.og and be == g.beta
+    assert np.array_equal(lut, g.lut)
+    assert np.array_equal(win, np.concatenate(g.win))
+
+
 def _traj(N, nproj, seed=3):
     c = case(N=N, C=1, nproj=nproj, seed=seed)
     return c, (c["kx"], c["ky"], c["kz"], c["kw"])
