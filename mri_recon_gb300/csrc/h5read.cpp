@@ -11,13 +11,16 @@
 //   * scalar integer and float attributes (the "Kdata" group's Num_Encodings, Num_Coils,
 //     trajectory_type*, dft_needed*).
 // Chunked or filtered datasets, dense (fractal-heap) groups and big-endian data are
-// rejected with MRG_ERR_UNSUPPORTED.  The file's data are read into the caller's host
+// rejected with MRG_ERR_UNSUPPORTED.  A damaged file gives MRG_ERR_INVALID: every read is
+// bounded by its message or by the file's size, every allocation by the file's size, and
+// continuation chains and B-tree walks are capped.  The file's data are read into the caller's host
 // buffers, which may be pinned: mrg_h5_load_encode stages an encode through pinned memory
 // into a plan (mrg_set_traj, mrg_set_data).
 #include <cstdio>
 #include <cstring>
 #include <map>
 #include <memory>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -65,6 +68,10 @@ class H5File {
   mrg_status open(const char *path) {
     f_ = std::fopen(path, "rb");
     if (!f_) return fail(MRG_ERR_INVALID, std::string("cannot open ") + path);
+    if (std::fseek(f_, 0, SEEK_END) != 0) return fail(MRG_ERR_INVALID, std::string("cannot seek in ") + path);
+    const long end = std::ftell(f_);
+    if (end < 0) return fail(MRG_ERR_INVALID, std::string("cannot size ") + path);
+    fsize_ = (uint64_t)end;
     static const uint8_t sig[8] = {0x89, 'H', 'D', 'F', '\r', '\n', 0x1a, '\n'};
     for (uint64_t at = 0;; at = at ? 2 * at : 512) {  // the superblock sits at 0, 512, 1024, ...
       uint8_t b[8];
@@ -82,6 +89,7 @@ class H5File {
       if (!read_at(sb_ + 8, h, 16)) return fail(MRG_ERR_INVALID, "truncated superblock");
       so_ = h[5];
       sl_ = h[6];
+      if (so_ != 8 || sl_ != 8) return fail(MRG_ERR_UNSUPPORTED, "HDF5 offsets/lengths other than 8 bytes");
       uint64_t p = sb_ + 8 + 16 + (v == 1 ? 4 : 0);
       base_ = rd_off(p);  // base address, then free-space, end of file and driver addresses
       p += 4 * so_;
@@ -98,13 +106,13 @@ class H5File {
       if (!read_at(sb_ + 9, h, 3)) return fail(MRG_ERR_INVALID, "truncated superblock");
       so_ = h[0];
       sl_ = h[1];
+      if (so_ != 8 || sl_ != 8) return fail(MRG_ERR_UNSUPPORTED, "HDF5 offsets/lengths other than 8 bytes");
       const uint64_t p = sb_ + 12;  // base, superblock extension, end of file, root object header
       base_ = rd_off(p);
       root_ = rd_off(p + 3 * so_);
     } else {
       return fail(MRG_ERR_UNSUPPORTED, "HDF5 superblock version " + std::to_string(v));
     }
-    if (so_ != 8 || sl_ != 8) return fail(MRG_ERR_UNSUPPORTED, "HDF5 offsets/lengths other than 8 bytes");
     return MRG_OK;
   }
 
@@ -149,7 +157,25 @@ class H5File {
       return MRG_OK;
     }
     if (o.data_size < nbytes) return fail(MRG_ERR_INVALID, "contiguous dataset smaller than its dataspace");
-    if (!read_at(base_ + o.data_addr, dst, nbytes)) return fail(MRG_ERR_INVALID, "truncated dataset");
+    if (!fits(base_ + o.data_addr, nbytes) || !read_at(base_ + o.data_addr, dst, nbytes))
+      return fail(MRG_ERR_INVALID, "truncated dataset");
+    return MRG_OK;
+  }
+
+  // Elements and bytes of a dataset's dataspace, checked against where its data can be: the
+  // compact bytes, the contiguous extent inside the file, or (never written) 64 GiB.
+  mrg_status extent(const H5Object &o, uint64_t &count, uint64_t &bytes) const {
+    count = 1;
+    for (uint64_t d : o.dims) {
+      if (d != 0 && count > (1ull << 48) / d) return fail(MRG_ERR_INVALID, "HDF5 dataspace too large");
+      count *= d;
+    }
+    if (o.type.size == 0 || count > (1ull << 48) / o.type.size) return fail(MRG_ERR_INVALID, "HDF5 dataset too large");
+    bytes = count * o.type.size;
+    const uint64_t room = o.layout == 0 ? o.compact.size()
+                          : o.data_addr == kUndef ? (1ull << 36)
+                          : (o.data_size < fsize_ ? o.data_size : fsize_);
+    if (bytes > room) return fail(MRG_ERR_INVALID, "HDF5 dataset larger than its storage");
     return MRG_OK;
   }
 
@@ -160,16 +186,20 @@ class H5File {
 
  private:
   FILE *f_ = nullptr;
-  uint64_t sb_ = 0, base_ = 0, root_ = kUndef, root_btree_ = kUndef, root_heap_ = kUndef;
+  uint64_t fsize_ = 0, sb_ = 0, base_ = 0, root_ = kUndef, root_btree_ = kUndef, root_heap_ = kUndef;
   int so_ = 8, sl_ = 8;
+  int visits_ = 0;  // B-tree nodes visited by the current lookup
 
+  // [at, at + n) lies inside the file
+  bool fits(uint64_t at, uint64_t n) const { return at <= fsize_ && n <= fsize_ - at; }
   bool read_at(uint64_t at, void *dst, size_t n) {
+    if (!fits(at, n) || at > (uint64_t)0x7fffffffffffffffull) return false;
     if (std::fseek(f_, (long)at, SEEK_SET) != 0) return false;
     return std::fread(dst, 1, n, f_) == n;
   }
   uint64_t rd_le(uint64_t at, int n) {
     uint8_t b[8] = {0};
-    if (!read_at(at, b, (size_t)n)) return kUndef;
+    if (n < 1 || n > 8 || !read_at(at, b, (size_t)n)) return kUndef;
     uint64_t v = 0;
     for (int k = n - 1; k >= 0; k--) v = (v << 8) | b[k];
     return v;
@@ -191,6 +221,7 @@ class H5File {
     if (g.btree == kUndef) return MRG_OK;
     std::vector<char> heap;
     MRG_TRY(load_heap(g.heap, heap));
+    visits_ = 0;
     return search_btree(g.btree, heap, name, addr, 0);
   }
 
@@ -199,6 +230,7 @@ class H5File {
     if (!read_at(base_ + at, h, 8) || std::memcmp(h, "HEAP", 4)) return fail(MRG_ERR_INVALID, "bad HDF5 local heap");
     const uint64_t size = rd_le(base_ + at + 8, sl_);
     const uint64_t data = rd_off(base_ + at + 8 + 2 * sl_);
+    if (size > fsize_) return fail(MRG_ERR_INVALID, "bad HDF5 local heap size");
     out.assign(size + 1, 0);
     if (size && !read_at(base_ + data, out.data(), size)) return fail(MRG_ERR_INVALID, "truncated HDF5 local heap");
     return MRG_OK;
@@ -207,6 +239,7 @@ class H5File {
   mrg_status search_btree(uint64_t at, const std::vector<char> &heap, const std::string &name, uint64_t *addr,
                           int depth) {
     if (depth > 32) return fail(MRG_ERR_INVALID, "HDF5 B-tree too deep");
+    if (++visits_ > (1 << 16)) return fail(MRG_ERR_INVALID, "HDF5 B-tree too large");
     uint8_t h[8];
     if (!read_at(base_ + at, h, 8) || std::memcmp(h, "TREE", 4) || h[4] != 0)
       return fail(MRG_ERR_INVALID, "bad HDF5 group B-tree node");
@@ -249,6 +282,8 @@ class H5File {
     t.size = (uint32_t)le(p + 4, 4);
     if (cls == 0) {
       if (p[1] & 1) return fail(MRG_ERR_UNSUPPORTED, "big-endian HDF5 data");
+      if (t.size != 1 && t.size != 2 && t.size != 4 && t.size != 8)
+        return fail(MRG_ERR_UNSUPPORTED, "HDF5 integer of size " + std::to_string(t.size));
       t.is_signed = (p[1] & 8) != 0;
     } else if (cls == 1) {
       if (p[1] & 1) return fail(MRG_ERR_UNSUPPORTED, "big-endian HDF5 data");
@@ -263,6 +298,7 @@ class H5File {
         size_t name_len = l + 1;
         if (ver < 3) name_len = (name_len + 7) & ~size_t(7);
         q += name_len;
+        if (q + 4 > n) return fail(MRG_ERR_INVALID, "short HDF5 compound member");
         uint32_t off;
         if (ver < 3) {
           off = (uint32_t)le(p + q, 4);
@@ -277,6 +313,8 @@ class H5File {
         H5Type mt;
         MRG_TRY(parse_type(p + q, n - q, mt));
         if (mt.cls != 1) return fail(MRG_ERR_UNSUPPORTED, "HDF5 compound of non-float members");
+        if ((uint64_t)off + mt.size > t.size) return fail(MRG_ERR_INVALID, "HDF5 compound member outside its element");
+        if (m == 1 && mt.size != t.comp_size) return fail(MRG_ERR_UNSUPPORTED, "HDF5 compound of unequal members");
         t.comp_off[m] = off;
         t.comp_size = mt.size;
         q += 8 + 12;  // member header and floating-point properties
@@ -300,6 +338,7 @@ class H5File {
 
   mrg_status message(H5Object &o, int type, const uint8_t *p, size_t n, std::vector<std::pair<uint64_t, uint64_t>> &cont,
                      int ohver) {
+    const auto shrt = [&]() { return fail(MRG_ERR_INVALID, "short HDF5 message " + std::to_string(type)); };
     switch (type) {
       case 0x0001:
         MRG_TRY(parse_space(p, n, o.dims));
@@ -309,13 +348,17 @@ class H5File {
         MRG_TRY(parse_type(p, n, o.type));
         break;
       case 0x0008: {  // data layout
+        if (n < 3) return shrt();
         const int ver = p[0];
         if (ver >= 3) {
           o.layout = p[1];
           if (o.layout == 0) {
+            if (n < 4) return shrt();
             const size_t sz = (size_t)le(p + 2, 2);
+            if (4 + sz > n) return shrt();
             o.compact.assign(p + 4, p + 4 + sz);
           } else if (o.layout == 1) {
+            if (2 + (size_t)so_ + (size_t)sl_ > n) return shrt();
             o.data_addr = le(p + 2, so_);
             o.data_size = le(p + 2 + so_, sl_);
           }
@@ -323,13 +366,19 @@ class H5File {
           const int rank = p[1];
           o.layout = p[2];
           if (o.layout == 1) {
+            if (8 + (size_t)so_ + 4 * (size_t)rank > n) return shrt();
             o.data_addr = le(p + 8, so_);
             uint64_t sz = 1;  // bytes: the last of the sizes is the element size
-            for (int d = 0; d < rank; d++) sz *= le(p + 8 + so_ + 4 * d, 4);
+            for (int d = 0; d < rank; d++) {
+              const uint64_t e = le(p + 8 + so_ + 4 * d, 4);
+              sz = (e != 0 && sz > (1ull << 48) / e) ? (1ull << 48) : sz * e;
+            }
             o.data_size = sz;
           } else if (o.layout == 0) {
             const size_t q = 8 + 4 * (size_t)rank;
+            if (q + 4 > n) return shrt();
             const size_t sz = (size_t)le(p + q, 4);
+            if (q + 4 + sz > n) return shrt();
             o.compact.assign(p + q + 4, p + q + 4 + sz);
           }
         }
@@ -340,15 +389,19 @@ class H5File {
         o.filtered = true;
         break;
       case 0x000C: {  // attribute
+        if (n < 9) return shrt();
         const int ver = p[0];
         const size_t nl = (size_t)le(p + 2, 2), tl = (size_t)le(p + 4, 2), sl = (size_t)le(p + 6, 2);
         size_t q = (ver == 3) ? 9 : 8;
         auto pad = [&](size_t x) { return ver == 1 ? ((x + 7) & ~size_t(7)) : x; };
+        if (q + pad(nl) > n) return shrt();
         std::string name(reinterpret_cast<const char *>(p + q), nl ? nl - 1 : 0);
         q += pad(nl);
         H5Object::Attr a;
+        if (q + pad(tl) > n) return shrt();
         MRG_TRY(parse_type(p + q, tl, a.type));
         q += pad(tl);
+        if (q + pad(sl) > n) return shrt();
         MRG_TRY(parse_space(p + q, sl, a.dims));
         q += pad(sl);
         if (q <= n) a.data.assign(p + q, p + n);
@@ -356,30 +409,43 @@ class H5File {
         break;
       }
       case 0x0006: {  // link message (compact new-style group)
+        if (n < 2) return shrt();
         const int flags = p[1];
         size_t q = 2;
         int ltype = 0;
-        if (flags & 8) ltype = p[q++];
+        if (flags & 8) {
+          if (q + 1 > n) return shrt();
+          ltype = p[q++];
+        }
         if (flags & 4) q += 8;  // creation order
         if (flags & 16) q += 1;  // character set
         const int lb = 1 << (flags & 3);
+        if (q + lb > n) return shrt();
         const size_t nl = (size_t)le(p + q, lb);
         q += lb;
+        if (nl > n || q + nl > n) return shrt();
         std::string name(reinterpret_cast<const char *>(p + q), nl);
         q += nl;
-        if (ltype == 0) o.links[name] = le(p + q, so_);  // hard link
+        if (ltype == 0) {  // hard link
+          if (q + (size_t)so_ > n) return shrt();
+          o.links[name] = le(p + q, so_);
+        }
         break;
       }
       case 0x0002:  // link info: dense storage when the fractal heap address is defined
-        if (n >= 2 + so_) {
+        if (n >= 2 + (size_t)so_) {
           size_t q = 2 + ((p[1] & 1) ? 8 : 0);
+          if (q + (size_t)so_ > n) return shrt();
           if (le(p + q, so_) != (kUndef >> (64 - 8 * so_))) o.dense_links = true;
         }
         break;
       case 0x0010:  // continuation
+        if ((size_t)so_ + (size_t)sl_ > n) return shrt();
+        if (cont.size() >= 4096) return fail(MRG_ERR_INVALID, "too many HDF5 header continuations");
         cont.emplace_back(le(p, so_), le(p + so_, sl_));
         break;
       case 0x0011:  // symbol table
+        if (2 * (size_t)so_ > n) return shrt();
         o.btree = le(p, so_);
         o.heap = le(p + so_, so_);
         break;
@@ -406,7 +472,8 @@ class H5File {
       for (size_t k = 0; k < cont.size(); k++) {
         uint8_t s[4];
         const uint64_t ca = base_ + cont[k].first;
-        if (!read_at(ca, s, 4) || std::memcmp(s, "OCHK", 4)) return fail(MRG_ERR_INVALID, "bad HDF5 continuation");
+        if (!read_at(ca, s, 4) || std::memcmp(s, "OCHK", 4) || cont[k].second < 8)
+          return fail(MRG_ERR_INVALID, "bad HDF5 continuation");
         MRG_TRY(walk_v2(o, ca + 4, cont[k].second - 8, flags, cont));
       }
       return MRG_OK;
@@ -423,6 +490,7 @@ class H5File {
 
   mrg_status walk_v1(H5Object &o, uint64_t p, uint64_t size, int nmsg, int &seen,
                      std::vector<std::pair<uint64_t, uint64_t>> &cont) {
+    if (!fits(p, size)) return fail(MRG_ERR_INVALID, "truncated HDF5 object header");
     std::vector<uint8_t> blk(size);
     if (size && !read_at(p, blk.data(), size)) return fail(MRG_ERR_INVALID, "truncated HDF5 object header");
     size_t q = 0;
@@ -439,6 +507,7 @@ class H5File {
 
   mrg_status walk_v2(H5Object &o, uint64_t p, uint64_t size, int flags,
                      std::vector<std::pair<uint64_t, uint64_t>> &cont) {
+    if (!fits(p, size)) return fail(MRG_ERR_INVALID, "truncated HDF5 object header");
     std::vector<uint8_t> blk(size);
     if (size && !read_at(p, blk.data(), size)) return fail(MRG_ERR_INVALID, "truncated HDF5 object header");
     const size_t hdr = (flags & 4) ? 6 : 4;
@@ -500,6 +569,21 @@ mrg_status convert(const H5Type &t, const uint8_t *src, uint64_t n, float *dst, 
   return MRG_OK;
 }
 
+// Runs f; an allocation failure or other exception becomes a status, since nothing may
+// throw across the C ABI.
+template <class F>
+mrg_status guarded(F &&f) {
+  try {
+    return f();
+  } catch (const std::bad_alloc &) {
+    set_error("out of host memory reading an HDF5 file");
+    return MRG_ERR_NOMEM;
+  } catch (const std::exception &e) {
+    set_error(std::string("HDF5 reader: ") + e.what());
+    return MRG_ERR_INVALID;
+  }
+}
+
 }  // namespace
 
 struct mrg_h5 {
@@ -519,10 +603,12 @@ mrg_status mrg_h5_open(const char *path, mrg_h5 **out) {
     return MRG_ERR_INVALID;
   }
   *out = nullptr;
-  std::unique_ptr<mrg_h5> h(new mrg_h5());
-  MRG_TRY(h->file.open(path));
-  *out = h.release();
-  return MRG_OK;
+  return guarded([&]() -> mrg_status {
+    std::unique_ptr<mrg_h5> h(new mrg_h5());
+    MRG_TRY(h->file.open(path));
+    *out = h.release();
+    return MRG_OK;
+  });
 }
 
 mrg_status mrg_h5_close(mrg_h5 *h) {
@@ -535,21 +621,23 @@ mrg_status mrg_h5_attr_int(mrg_h5 *h, const char *group, const char *name, int *
     set_error("null argument");
     return MRG_ERR_INVALID;
   }
-  H5Object g;
-  MRG_TRY(h->file.find(group, g));
-  auto it = g.attrs.find(name);
-  if (it == g.attrs.end()) return H5File::fail(MRG_ERR_INVALID, std::string("attribute not found: ") + name);
-  const H5Object::Attr &a = it->second;
-  if (a.type.cls != 0 || a.type.size > 8 || a.data.size() < a.type.size || count_of(a.dims) != 1)
-    return H5File::fail(MRG_ERR_INVALID, std::string("attribute is not a scalar integer: ") + name);
-  float v;
-  MRG_TRY(convert(a.type, a.data.data(), 1, &v, false));
-  int64_t u = 0;
-  for (int k = (int)a.type.size - 1; k >= 0; k--) u = (u << 8) | a.data[k];
-  if (a.type.is_signed && a.type.size < 8 && ((uint64_t)u >> (8 * a.type.size - 1)) & 1)
-    u = (int64_t)((uint64_t)u | (~0ull << (8 * a.type.size)));
-  *value = (int)u;
-  return MRG_OK;
+  return guarded([&]() -> mrg_status {
+    H5Object g;
+    MRG_TRY(h->file.find(group, g));
+    auto it = g.attrs.find(name);
+    if (it == g.attrs.end()) return H5File::fail(MRG_ERR_INVALID, std::string("attribute not found: ") + name);
+    const H5Object::Attr &a = it->second;
+    if (a.type.cls != 0 || a.type.size > 8 || a.data.size() < a.type.size || count_of(a.dims) != 1)
+      return H5File::fail(MRG_ERR_INVALID, std::string("attribute is not a scalar integer: ") + name);
+    float v;
+    MRG_TRY(convert(a.type, a.data.data(), 1, &v, false));
+    int64_t u = 0;
+    for (int k = (int)a.type.size - 1; k >= 0; k--) u = (u << 8) | a.data[k];
+    if (a.type.is_signed && a.type.size < 8 && ((uint64_t)u >> (8 * a.type.size - 1)) & 1)
+      u = (int64_t)((uint64_t)u | (~0ull << (8 * a.type.size)));
+    *value = (int)u;
+    return MRG_OK;
+  });
 }
 
 mrg_status mrg_h5_dataset_info(mrg_h5 *h, const char *path, int *rank, int64_t dims[8], int *is_complex) {
@@ -557,15 +645,19 @@ mrg_status mrg_h5_dataset_info(mrg_h5 *h, const char *path, int *rank, int64_t d
     set_error("null argument");
     return MRG_ERR_INVALID;
   }
-  H5Object o;
-  MRG_TRY(h->file.find(path, o));
-  if (!o.has_space || o.type.cls < 0) return H5File::fail(MRG_ERR_INVALID, std::string("not a dataset: ") + path);
-  if (o.dims.size() > 8) return H5File::fail(MRG_ERR_UNSUPPORTED, "dataset rank above 8");
-  if (rank) *rank = (int)o.dims.size();
-  if (dims)
-    for (size_t d = 0; d < o.dims.size(); d++) dims[d] = (int64_t)o.dims[d];
-  if (is_complex) *is_complex = o.type.cls == 6;
-  return MRG_OK;
+  return guarded([&]() -> mrg_status {
+    H5Object o;
+    MRG_TRY(h->file.find(path, o));
+    if (!o.has_space || o.type.cls < 0) return H5File::fail(MRG_ERR_INVALID, std::string("not a dataset: ") + path);
+    if (o.dims.size() > 8) return H5File::fail(MRG_ERR_UNSUPPORTED, "dataset rank above 8");
+    uint64_t cnt = 0, bytes = 0;
+    MRG_TRY(h->file.extent(o, cnt, bytes));  // dims that no storage in the file could hold are rejected
+    if (rank) *rank = (int)o.dims.size();
+    if (dims)
+      for (size_t d = 0; d < o.dims.size(); d++) dims[d] = (int64_t)o.dims[d];
+    if (is_complex) *is_complex = o.type.cls == 6;
+    return MRG_OK;
+  });
 }
 
 // Reads a whole dataset as float32 (real) or complex64 (complex = 1) into dst (n elements).
@@ -574,16 +666,19 @@ mrg_status mrg_h5_read(mrg_h5 *h, const char *path, int complex_out, void *dst, 
     set_error("bad argument");
     return MRG_ERR_INVALID;
   }
-  H5Object o;
-  MRG_TRY(h->file.find(path, o));
-  if (!o.has_space || o.type.cls < 0) return H5File::fail(MRG_ERR_INVALID, std::string("not a dataset: ") + path);
-  const uint64_t cnt = count_of(o.dims);
-  if ((int64_t)cnt != n)
-    return H5File::fail(MRG_ERR_INVALID, std::string("dataset ") + path + " holds " + std::to_string(cnt) +
-                                             " elements, not " + std::to_string(n));
-  std::vector<uint8_t> raw((size_t)(cnt * o.type.size));
-  MRG_TRY(h->file.read_raw(o, raw.data(), raw.size()));
-  return convert(o.type, raw.data(), cnt, static_cast<float *>(dst), complex_out != 0);
+  return guarded([&]() -> mrg_status {
+    H5Object o;
+    MRG_TRY(h->file.find(path, o));
+    if (!o.has_space || o.type.cls < 0) return H5File::fail(MRG_ERR_INVALID, std::string("not a dataset: ") + path);
+    uint64_t cnt = 0, bytes = 0;
+    MRG_TRY(h->file.extent(o, cnt, bytes));
+    if ((int64_t)cnt != n)
+      return H5File::fail(MRG_ERR_INVALID, std::string("dataset ") + path + " holds " + std::to_string(cnt) +
+                                               " elements, not " + std::to_string(n));
+    std::vector<uint8_t> raw((size_t)bytes);
+    MRG_TRY(h->file.read_raw(o, raw.data(), raw.size()));
+    return convert(o.type, raw.data(), cnt, static_cast<float *>(dst), complex_out != 0);
+  });
 }
 
 mrg_status mrg_h5_mri_info(mrg_h5 *h, int *num_encodings, int *num_coils, int64_t *samples, int max_encodings) {
@@ -616,6 +711,7 @@ mrg_status mrg_h5_load_encode(mrg_h5 *h, int encode, mrg_plan *plan, int frame, 
   MRG_TRY(mrg_h5_attr_int(h, "Kdata", "Num_Encodings", &ne));
   MRG_TRY(mrg_h5_attr_int(h, "Kdata", "Num_Coils", &nc));
   if (encode >= ne) return H5File::fail(MRG_ERR_INVALID, "encode beyond Num_Encodings");
+  if (nc < 1 || nc > 4096) return H5File::fail(MRG_ERR_INVALID, "Num_Coils out of range: " + std::to_string(nc));
   int64_t M = 0;
   {
     int64_t dims[8];
@@ -624,7 +720,9 @@ mrg_status mrg_h5_load_encode(mrg_h5 *h, int encode, mrg_plan *plan, int frame, 
     M = 1;
     for (int d = 0; d < rank; d++) M *= dims[d];
   }
-  // pinned staging: kx, ky, kz, kw, then nc coils of complex samples
+  // pinned staging: kx, ky, kz, kw, then nc coils of complex samples (M is bounded by the
+  // file's size through mrg_h5_dataset_info)
+  if (M < 1 || (uint64_t)M > (1ull << 40)) return H5File::fail(MRG_ERR_INVALID, "bad sample count");
   const size_t need = sizeof(float) * (size_t)M * (4 + 2 * (size_t)nc);
   if (h->pinned_bytes < need) {
     if (h->pinned) cudaFreeHost(h->pinned);

@@ -57,6 +57,41 @@ def test_reader_errors(mrg_lib, tmp_path):
         mrg_lib.H5File(tmp_path / "missing.h5")
 
 
+def test_reader_survives_damaged_files(mrg_lib, tmp_path):
+    """Truncated files and files with corrupted bytes (header blocks, messages, sizes,
+    addresses) either read or fail with MrgError: no crash, no read outside a message or
+    the file, no allocation sized by a corrupted field."""
+    import random
+    from mri_recon_gb300 import _lib
+    base = tmp_path / "base.h5"
+    write_mri_file(base, _encodes(2, 2), 2)
+    data = base.read_bytes()
+    rng = random.Random(1234)
+    path = tmp_path / "damaged.h5"
+    outcomes = {"ok": 0, "error": 0}
+    for i in range(400):
+        b = bytearray(data)
+        if i < 80:
+            b = b[:rng.randrange(0, len(b))]
+        else:
+            for _ in range(rng.randint(1, 8)):
+                pos = rng.randrange(0, 4096 if rng.random() < 0.7 else len(b))
+                b[pos] = rng.randrange(256)
+        path.write_bytes(bytes(b))
+        try:
+            f = mrg_lib.H5File(path)
+            ne, nc, _ = f.mri_info()
+            for e in range(min(ne, 4)):
+                for name in ("KX_E%d", "KY_E%d", "KZ_E%d", "KW_E%d"):
+                    f.read("Kdata/" + name % e)
+                for c in range(min(nc, 4)):
+                    f.read("Kdata/KData_E%d_C%d" % (e, c))
+            outcomes["ok"] += 1
+        except _lib.MrgError:
+            outcomes["error"] += 1
+    assert outcomes["error"] > 0 and outcomes["ok"] > 0, outcomes
+
+
 @pytest.mark.gpu
 def test_load_encode_into_a_plan(mrg_lib, tmp_path):
     """An encode loaded from the file through pinned memory into a plan frame gives the same
