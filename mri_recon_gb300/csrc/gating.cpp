@@ -5,6 +5,7 @@
 // slice) column-major order, readout fastest, so sample s belongs to readout r = s / nread,
 // the (projection, slice) element of the per-readout gate times and weights.
 #include <cmath>
+#include <cstdint>
 #include <cstring>
 
 #include "mrg_internal.h"
@@ -14,7 +15,7 @@ using namespace mrg;
 namespace {
 
 bool gate_args_ok(const double *gate_times, int64_t nreadouts, int nread) {
-  if (!gate_times || nreadouts < 0 || nread < 1) {
+  if (!gate_times || nreadouts < 0 || nread < 1 || nreadouts > INT64_MAX / nread) {
     set_error("bad gating arguments");
     return false;
   }

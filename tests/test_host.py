@@ -201,3 +201,9 @@ def test_gating_weights_and_pregate_match_oracle(mrg_lib, oracle_lib):
         w = mrg_lib.gate_weights(gate, kw, nread, t, rweight=rweight)
         mask = np.repeat(rweight * (np.floor(gate) == t), nread).astype(np.float32)
         assert np.array_equal(w, kw * mask)
+    # sizes whose product would overflow are rejected before anything is read
+    L = mrg_lib.load()
+    n = ctypes.c_int64()
+    g1 = np.zeros(1, np.float64)
+    assert L.mrg_pregate(g1.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), None, 2 ** 62, 4, 0, 0, None, None, None,
+                         None, None, 0, 0, None, None, None, None, None, 0, ctypes.byref(n)) == 1
