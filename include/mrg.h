@@ -446,7 +446,9 @@ mrg_status mrg_pregate(const double *gate_times, const float *rweight, int64_t n
  * (superblocks 0-3, symbol-table and compact link groups, object headers 1 and 2,
  * contiguous and compact datasets of little-endian integers, IEEE floats and (real, imag)
  * float compounds, scalar attributes).  Chunked / compressed datasets and dense groups
- * return MRG_ERR_UNSUPPORTED.  Host-only except mrg_h5_load_encode.
+ * return MRG_ERR_UNSUPPORTED; a damaged file (truncated, corrupted sizes or addresses)
+ * returns MRG_ERR_INVALID, and no read or allocation goes beyond what the file can hold.
+ * Host-only except mrg_h5_load_encode.
  *   mrg_h5_attr_int: an integer attribute of a group ("Kdata", "Num_Coils");
  *   mrg_h5_dataset_info: rank and dimensions (HDF5 order: the slowest first) of a dataset;
  *   mrg_h5_read: a whole dataset converted to float32 (complex_out = 0) or complex64, n
