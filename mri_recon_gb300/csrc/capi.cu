@@ -714,18 +714,13 @@ mrg_status mrg_plan_create(const mrg_config *cfg_in, int Nx, int Ny, int Nz, int
     return MRG_ERR_INVALID;
   }
   *out = nullptr;
-  if (Nx <= 0 || Ny <= 0 || Nz <= 0 || ncoil <= 0 || nframes <= 0) {
+  if (ncoil <= 0 || nframes <= 0) {
     set_error("sizes must be positive");
     return MRG_ERR_INVALID;
   }
   mrg_config cfg;
   if (cfg_in) cfg = *cfg_in; else mrg_config_default(&cfg);
-  if (!(cfg.overgrid >= 1.0f) || cfg.kernel_type < 0 || cfg.kernel_type > 3 || cfg.kernel_eval < 0 ||
-      cfg.kernel_eval > 1 || (cfg.kernel_eval == 1 && cfg.kernel_type != MRG_KERNEL_KAISER) || cfg.grid_mode < 0 ||
-      cfg.grid_mode > 3 || cfg.fft_norm < 0 || cfg.fft_norm > 1) {
-    set_error("bad config");
-    return MRG_ERR_INVALID;
-  }
+  if (!config_ok(cfg, Nx, Ny, Nz)) return MRG_ERR_INVALID;
   mrg_plan *p = new mrg_plan();
   p->cfg = cfg;
   p->C = ncoil;

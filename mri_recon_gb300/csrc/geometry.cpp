@@ -145,18 +145,34 @@ int GlibcRand::next() {
   return (int)(v >> 1);
 }
 
+bool config_ok(const mrg_config &cfg, int Nx, int Ny, int Nz) {
+  if (Nx <= 0 || Ny <= 0 || Nz <= 0) {
+    set_error("sizes must be positive");
+    return false;
+  }
+  if (Nx > 65536 || Ny > 65536 || Nz > 65536) {
+    set_error("sizes above 65536");
+    return false;
+  }
+  if (!(cfg.overgrid >= 1.0f && cfg.overgrid <= 8.0f) || !(cfg.dwin == -1.0f || (cfg.dwin > 0.0f && cfg.dwin <= 16.0f)) ||
+      cfg.kernel_type < 0 || cfg.kernel_type > 3 || cfg.kernel_eval < 0 || cfg.kernel_eval > 1 ||
+      (cfg.kernel_eval == 1 && cfg.kernel_type != MRG_KERNEL_KAISER) || cfg.grid_mode < 0 || cfg.grid_mode > 3 ||
+      cfg.fft_norm < 0 || cfg.fft_norm > 1) {
+    set_error("bad config");
+    return false;
+  }
+  return true;
+}
+
 }  // namespace mrg
 
 extern "C" {
 
 mrg_status mrg_plan_geometry(const mrg_config *cfg_in, int Nx, int Ny, int Nz, int S[3], int og[3], float grid[3],
                              float beta[3], int *lut_len, float *lut, float *win) {
-  if (Nx <= 0 || Ny <= 0 || Nz <= 0) {
-    mrg::set_error("sizes must be positive");
-    return MRG_ERR_INVALID;
-  }
   mrg_config cfg;
   if (cfg_in) cfg = *cfg_in; else mrg_config_default(&cfg);
+  if (!mrg::config_ok(cfg, Nx, Ny, Nz)) return MRG_ERR_INVALID;
   mrg::Geometry g;
   mrg::build_geometry(g, cfg, Nx, Ny, Nz);
   size_t o = 0;

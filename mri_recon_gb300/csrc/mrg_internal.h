@@ -88,6 +88,10 @@ struct Geometry {
   std::vector<float> win[3];
 };
 void build_geometry(Geometry &g, const mrg_config &cfg, int Nx, int Ny, int Nz);
+// The checks of mrg_plan_create and mrg_plan_geometry: sizes in 1..65536 and options in
+// range (overgrid 1..8, dwin -1 or in (0, 16], the enumerations), so that grids and tables
+// stay well within int and memory; sets the error text when it returns false.
+bool config_ok(const mrg_config &cfg, int Nx, int Ny, int Nz);
 
 // glibc random() stream for the default seed (srand never called by the reference).
 struct GlibcRand {

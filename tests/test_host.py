@@ -85,12 +85,25 @@ def test_errors_are_reported_not_fatal(mrg_lib):
     L.mrg_config_default(ctypes.byref(cfg))
     assert abs(cfg.overgrid - 1.5) < 1e-7 and cfg.kernel_type == 1 and abs(cfg.k_rad - 9999.0) < 1e-3
     assert cfg.fft_norm == 0  # gridFFT's normalised transforms unless asked
-    for field, bad in (("fft_norm", 2), ("fft_norm", -1), ("grid_mode", 4), ("kernel_type", 5)):
+    S, og, ll = (ctypes.c_int * 3)(), (ctypes.c_int * 3)(), ctypes.c_int()
+    gr, be = (ctypes.c_float * 3)(), (ctypes.c_float * 3)()
+    for field, bad in (("fft_norm", 2), ("fft_norm", -1), ("grid_mode", 4), ("kernel_type", 5), ("dwin", 1e9),
+                       ("dwin", -2.0), ("dwin", 0.0), ("dwin", float("nan")), ("overgrid", float("nan")),
+                       ("overgrid", 100.0), ("overgrid", 0.5)):
         c2 = MrgConfig()
         L.mrg_config_default(ctypes.byref(c2))
         setattr(c2, field, bad)
+        # rejected with a status before any table is sized from it (no exception, no exit)
         assert L.mrg_plan_create(ctypes.byref(c2), 32, 32, 32, 1, 1, ctypes.byref(h)) == 1, field
         assert b"bad config" in L.mrg_last_error()
+        assert L.mrg_plan_geometry(ctypes.byref(c2), 32, 32, 32, S, og, gr, be, ctypes.byref(ll), None, None) == 1
+        assert b"bad config" in L.mrg_last_error()
+    assert L.mrg_plan_geometry(None, 70000, 32, 32, S, og, gr, be, ctypes.byref(ll), None, None) == 1
+    assert b"65536" in L.mrg_last_error()
+    c3 = MrgConfig()
+    L.mrg_config_default(ctypes.byref(c3))
+    c3.dwin, c3.overgrid = 16.0, 8.0  # the edges of the accepted ranges
+    assert L.mrg_plan_geometry(ctypes.byref(c3), 16, 16, 16, S, og, gr, be, ctypes.byref(ll), None, None) == 0
 
 
 def test_loop_parameter_defaults_are_the_references(mrg_lib):
