@@ -348,14 +348,15 @@ void mrg_dcf_params_default(mrg_dcf_params *q) {
 
 mrg_status mrg_dcf_pipe(const float *kx, const float *ky, const float *kz, int64_t M, int Nx, int Ny, int Nz,
                         const mrg_dcf_params *q_in, float *kw, void *stream) {
-  if (!kx || !ky || !kz || !kw || M <= 0 || Nx <= 0 || Ny <= 0 || Nz <= 0) {
+  if (!kx || !ky || !kz || !kw || M <= 0 || Nx <= 0 || Ny <= 0 || Nz <= 0 || Nx > 65536 || Ny > 65536 || Nz > 65536) {
     set_error("bad argument");
     return MRG_ERR_INVALID;
   }
   mrg_dcf_params q;
   if (q_in) q = *q_in; else mrg_dcf_params_default(&q);
-  if (q.iters < 0 || !(q.dwin > 0) || !(q.scale > 0) || !(q.overgrid > 0) || !(q.acc > 0) || q.kernel < 0 ||
-      q.kernel > 1) {
+  // bounded so that the grid, (int)(overgrid N + 16) per axis, and the kernel table stay small
+  if (q.iters < 0 || !(q.dwin > 0 && q.dwin <= 16) || !(q.scale > 0) || !(q.overgrid > 0 && q.overgrid <= 8) ||
+      !(q.acc > 0) || q.kernel < 0 || q.kernel > 1) {
     set_error("bad density-compensation parameters");
     return MRG_ERR_INVALID;
   }

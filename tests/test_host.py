@@ -100,6 +100,15 @@ def test_errors_are_reported_not_fatal(mrg_lib):
         assert b"bad config" in L.mrg_last_error()
     assert L.mrg_plan_geometry(None, 70000, 32, 32, S, og, gr, be, ctypes.byref(ll), None, None) == 1
     assert b"65536" in L.mrg_last_error()
+    # density-compensation parameters are checked before any device work
+    from mri_recon_gb300._lib import MrgDcfParams
+    k = np.zeros(8, np.float32)
+    kp = k.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+    for field, bad in (("overgrid", 1e6), ("dwin", 1e9), ("dwin", 0.0), ("iters", -1), ("kernel", 2)):
+        q = MrgDcfParams()
+        L.mrg_dcf_params_default(ctypes.byref(q))
+        setattr(q, field, bad)
+        assert L.mrg_dcf_pipe(kp, kp, kp, 8, 16, 16, 16, ctypes.byref(q), kp, None) == 1, field
     c3 = MrgConfig()
     L.mrg_config_default(ctypes.byref(c3))
     c3.dwin, c3.overgrid = 16.0, 8.0  # the edges of the accepted ranges
