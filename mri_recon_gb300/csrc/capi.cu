@@ -1805,7 +1805,12 @@ extern "C" mrg_status mrg_fista(mrg_plan *p, const mrg_fista_params *q, void *X,
     set_error("bad argument");
     return MRG_ERR_INVALID;
   }
-  if (q->use_threshold && (q->cycle_spins < 1 || q->wave_type < 0 || q->wave_type > 1)) {
+  // the per-iteration shift tables are sized max_iter x (cycle spins, block iterations) x 3
+  if (q->max_iter > 100000 || q->max_eig_iter > 100000) {
+    set_error("max_iter / max_eig_iter above 100000");
+    return MRG_ERR_INVALID;
+  }
+  if (q->use_threshold && (q->cycle_spins < 1 || q->cycle_spins > 64 || q->wave_type < 0 || q->wave_type > 1)) {
     set_error("bad wavelet / cycle-spin parameters");
     return MRG_ERR_INVALID;
   }
@@ -1813,7 +1818,8 @@ extern "C" mrg_status mrg_fista(mrg_plan *p, const mrg_fista_params *q, void *X,
     set_error("use_threshold must be 0 (none), 1 (fraction) or 2 (fixed)");
     return MRG_ERR_INVALID;
   }
-  if (q->llr_alpha > 0.0f && (q->llr_block_iter < 1 || q->llr_block[0] < 1 || q->llr_block[1] < 1 || q->llr_block[2] < 1)) {
+  if (q->llr_alpha > 0.0f && (q->llr_block_iter < 1 || q->llr_block_iter > 64 || q->llr_block[0] < 1 ||
+                              q->llr_block[1] < 1 || q->llr_block[2] < 1)) {
     set_error("bad low-rank block parameters");
     return MRG_ERR_INVALID;
   }
@@ -1989,11 +1995,16 @@ extern "C" mrg_status mrg_clear(mrg_plan *p, const mrg_clear_params *q, void *X,
     set_error("bad argument");
     return MRG_ERR_INVALID;
   }
-  if (q->alpha_coil != 0.0f && (q->block_iter < 1 || q->rand_skip < 0)) {
+  if (q->max_iter > 100000) {  // the shift tables are sized per iteration
+    set_error("max_iter above 100000");
+    return MRG_ERR_INVALID;
+  }
+  if (q->alpha_coil != 0.0f && (q->block_iter < 1 || q->block_iter > 64 || q->rand_skip < 0)) {
     set_error("bad low-rank block parameters");
     return MRG_ERR_INVALID;
   }
-  if (q->use_threshold && (q->cycle_spins < 1 || q->wave_type < 0 || q->wave_type > 1 || q->rand_skip < 0)) {
+  if (q->use_threshold &&
+      (q->cycle_spins < 1 || q->cycle_spins > 64 || q->wave_type < 0 || q->wave_type > 1 || q->rand_skip < 0)) {
     set_error("bad wavelet / cycle-spin parameters");
     return MRG_ERR_INVALID;
   }

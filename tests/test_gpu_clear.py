@@ -137,6 +137,8 @@ def test_clear_needs_data_and_few_coils(mrg_lib):
     p = mrg_lib.Plan(8, 2, 1)
     kx, ky, kz, kw = synth.radial_trajectory(8, 40, 8)
     p.set_traj(0, kx, ky, kz, kw)
+    with pytest.raises(mrg_lib.MrgError, match="low-rank"):
+        p.clear(mrg_lib.clear_params(max_iter=1, alpha_coil=0.01, block_iter=65))  # checked before the data
     with pytest.raises(mrg_lib.MrgError):
         p.clear(mrg_lib.clear_params(max_iter=1))  # no k-space data
     p33 = mrg_lib.Plan(8, 33, 1)

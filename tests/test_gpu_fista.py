@@ -246,6 +246,11 @@ def test_fista_early_stop(mrg_lib, use_graph):
     from mri_recon_gb300 import _lib
     with pytest.raises(_lib.MrgError):
         p.fista(mrg_lib.fista_params(early_stop_thresh=0.1, early_stop_range=0, **base))
+    # iteration and cycle-spin counts that would size the shift tables beyond reason
+    with pytest.raises(_lib.MrgError, match="cycle-spin"):
+        p.fista(mrg_lib.fista_params(**dict(base, cycle_spins=65)))
+    with pytest.raises(_lib.MrgError, match="100000"):
+        p.fista(mrg_lib.fista_params(**dict(base, max_iter=100001)))
 
 
 def test_pregated_frames_fista_llr(mrg_lib, oracle_lib):
