@@ -131,11 +131,75 @@ GlibcRand::GlibcRand() {
   skip(310);
 }
 
-void GlibcRand::skip(int64_t n) {
-  for (int64_t k = 0; k < n; k++) {
-    r[pos % 34] = r[(pos - 31) % 34] + r[(pos - 3) % 34];
-    pos++;
+namespace {
+
+// Polynomials over Z/2^32 modulo x^31 - x^28 - 1, the characteristic polynomial of the
+// stream's recurrence s_i = s_{i-31} + s_{i-3}: coefficient k of x^k in c[k].
+struct Poly31 {
+  uint32_t c[31];
+};
+
+Poly31 poly_mulmod(const Poly31 &a, const Poly31 &b) {
+  uint32_t t[61] = {0};
+  for (int i = 0; i < 31; i++) {
+    if (!a.c[i]) continue;
+    for (int j = 0; j < 31; j++) t[i + j] += a.c[i] * b.c[j];
   }
+  for (int d = 60; d >= 31; d--) {  // x^d = x^(d-31) x^31 = x^(d-3) + x^(d-31)
+    t[d - 3] += t[d];
+    t[d - 31] += t[d];
+  }
+  Poly31 out;
+  std::copy(t, t + 31, out.c);
+  return out;
+}
+
+Poly31 poly_times_x(const Poly31 &a) {
+  Poly31 out;
+  const uint32_t top = a.c[30];
+  for (int k = 30; k >= 1; k--) out.c[k] = a.c[k - 1];
+  out.c[0] = top;  // x^31 = x^28 + 1
+  out.c[28] += top;
+  return out;
+}
+
+Poly31 poly_xpow(uint64_t e) {
+  Poly31 res{}, base{};
+  res.c[0] = 1;
+  base.c[1] = 1;
+  for (; e; e >>= 1) {
+    if (e & 1) res = poly_mulmod(res, base);
+    base = poly_mulmod(base, base);
+  }
+  return res;
+}
+
+}  // namespace
+
+// Advances the stream by n draws.  Long skips jump: every later value is a fixed linear
+// combination of the last 31, s_{j+e} = sum_k c_k s_{j+k} with x^e = sum_k c_k x^k modulo
+// the characteristic polynomial, so the new 34-value window costs O(log n) polynomial
+// products instead of n steps.
+void GlibcRand::skip(int64_t n) {
+  if (n < 64) {
+    for (int64_t k = 0; k < n; k++) {
+      r[pos % 34] = r[(pos - 31) % 34] + r[(pos - 3) % 34];
+      pos++;
+    }
+    return;
+  }
+  const int64_t j = pos - 31;  // s_j .. s_{j+30} are the last 31 values
+  uint32_t base[31];
+  for (int k = 0; k < 31; k++) base[k] = r[(j + k) % 34];
+  const int64_t np = pos + n;  // the new window is s_{np-34} .. s_{np-1}
+  Poly31 p = poly_xpow((uint64_t)(np - 34 - j));
+  for (int t = 0; t < 34; t++) {
+    uint32_t v = 0;
+    for (int k = 0; k < 31; k++) v += p.c[k] * base[k];
+    r[(np - 34 + t) % 34] = v;
+    p = poly_times_x(p);
+  }
+  pos = np;
 }
 
 int GlibcRand::next() {

@@ -68,10 +68,21 @@ def test_geometry_other_kernels(mrg_lib, oracle_lib):
 
 
 def test_rand_stream_matches_oracle(mrg_lib, oracle_lib):
+    """The library's glibc random() stream against the oracle's draw-by-draw one at short and
+    long skips (long skips jump ahead through the recurrence's characteristic polynomial), and
+    a skip of 10^15 draws that only a jump can make, checked against a nearby skip."""
     L = mrg_lib.load()
-    out = (ctypes.c_int * 25)()
-    assert L.mrg_rand_stream(1000, 25, out) == 0
-    assert np.array_equal(np.array(out[:]), oracle_lib.glibc_rand(1000, 25))
+
+    def stream(skip, n):
+        out = (ctypes.c_int * n)()
+        assert L.mrg_rand_stream(skip, n, out) == 0
+        return np.array(out[:])
+
+    rng = np.random.default_rng(0)
+    for skip in list(range(0, 130)) + [int(v) for v in rng.integers(130, 200000, 20)]:
+        assert np.array_equal(stream(skip, 25), oracle_lib.glibc_rand(skip, 25)), skip
+    far = stream(10 ** 15, 20)
+    assert np.array_equal(far, stream(10 ** 15 - 7, 27)[7:])
 
 
 def test_errors_are_reported_not_fatal(mrg_lib):
