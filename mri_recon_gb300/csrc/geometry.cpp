@@ -181,25 +181,29 @@ Poly31 poly_xpow(uint64_t e) {
 // the characteristic polynomial, so the new 34-value window costs O(log n) polynomial
 // products instead of n steps.
 void GlibcRand::skip(int64_t n) {
+  if (n <= 0) return;
   if (n < 64) {
     for (int64_t k = 0; k < n; k++) {
       r[pos % 34] = r[(pos - 31) % 34] + r[(pos - 3) % 34];
       pos++;
     }
+    pos = 34 + pos % 34;  // only the position modulo 34 matters; keep it far from overflow
     return;
   }
   const int64_t j = pos - 31;  // s_j .. s_{j+30} are the last 31 values
   uint32_t base[31];
   for (int k = 0; k < 31; k++) base[k] = r[(j + k) % 34];
-  const int64_t np = pos + n;  // the new window is s_{np-34} .. s_{np-1}
-  Poly31 p = poly_xpow((uint64_t)(np - 34 - j));
+  // the new window is s_{pos+n-34} .. s_{pos+n-1}: x^(n-3) .. x^(n+30) relative to s_j, in
+  // ring slots (pos + n + t) mod 34, found without forming pos + n
+  const int b = (int)((pos % 34 + n % 34) % 34);
+  Poly31 p = poly_xpow((uint64_t)n - 3);
   for (int t = 0; t < 34; t++) {
     uint32_t v = 0;
     for (int k = 0; k < 31; k++) v += p.c[k] * base[k];
-    r[(np - 34 + t) % 34] = v;
+    r[(b + t) % 34] = v;
     p = poly_times_x(p);
   }
-  pos = np;
+  pos = 34 + b;
 }
 
 int GlibcRand::next() {

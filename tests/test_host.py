@@ -83,6 +83,8 @@ def test_rand_stream_matches_oracle(mrg_lib, oracle_lib):
         assert np.array_equal(stream(skip, 25), oracle_lib.glibc_rand(skip, 25)), skip
     far = stream(10 ** 15, 20)
     assert np.array_equal(far, stream(10 ** 15 - 7, 27)[7:])
+    edge = stream(2 ** 63 - 40, 30)  # the largest skips do not overflow the stream position
+    assert np.array_equal(edge[10:], stream(2 ** 63 - 30, 20))
 
 
 def test_errors_are_reported_not_fatal(mrg_lib):
